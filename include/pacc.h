@@ -1,0 +1,234 @@
+/*
+ * pacc.h — C ABI of phyloacc-gb300: PhyloAcc-ST's per-element Bayesian MCMC
+ * (three models per element, marginal likelihoods and posteriors of the
+ * latent conservation states) on one NVIDIA GB300 GPU.
+ *
+ * The ABI replaces the per-element seam of PhyloAcc-ST
+ *   BPP_C(c, prof, bpp, gapchar, missing_thres, filter&, verbose, consToMis,
+ *         prune, revgap, min_length)                (src/PhyloAcc-ST/bpp_c.hpp:143)
+ *   -> initMCMC -> Gibbs -> Eval2 -> Output_init    (src/PhyloAcc-ST/main.cpp:459-494)
+ * driven by the OpenMP loop over element ids       (src/PhyloAcc-ST/main.cpp:452)
+ * and the shared read-only model object BPP         (src/PhyloAcc-ST/bpp.hpp:173-404).
+ *
+ * Conventions
+ *   - Plain C types, caller-owned buffers, no exceptions, no exit().
+ *   - Node numbering is PhyloAcc's: leaves 0..S-1 and internal nodes S..N-1
+ *     in postorder of the Newick tree, root N-1, N = 2S-1
+ *     (src/PhyloAcc-ST/newick.cpp:382-400).  children[2*i+k] lists the
+ *     children of node i in increasing id order (src/PhyloAcc-ST/bpp.cpp:105-117),
+ *     -1 for leaves.
+ *   - Model index m in results: 0 = M0 (null, resZ 0), 1 = M1 (acceleration
+ *     off the conserved lineages, resZ 2), 2 = M2 (full, resZ 1)
+ *     (src/PhyloAcc-ST/main.cpp:362-364, bpp.cpp:581,590-598).
+ *   - Every function returning int returns a pacc_status code.
+ *   - A context is driven by one host thread at a time; distinct contexts are
+ *     independent and may be used from different threads.
+ */
+#ifndef PACC_H
+#define PACC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PACC_ABI_VERSION 1
+#define PACC_MAX_SPECIES 512
+
+typedef enum pacc_status {
+    PACC_OK = 0,
+    PACC_FILTERED = 1,          /* element dropped by MIN_LEN / CONSERVE_PROP / trimming (bpp_c.hpp:158-162,288-292,369-373) */
+    PACC_NAN_LIKELIHOOD = 2,    /* a marginal likelihood was NaN ("failure", bpp_c2.cpp:339-348) */
+    PACC_SAMPLER_ERROR = 3,     /* no category could be drawn ("Sample Tg error", bpp_c.cpp:686-696,727-730) */
+    PACC_OOM = 4,               /* device or host allocation failed / budget too small */
+    PACC_TIMEOUT = 5,           /* a bounded device wait expired */
+    PACC_EINVAL = 6,            /* invalid argument */
+    PACC_ECUDA = 7,             /* CUDA runtime error */
+    PACC_EBUSY = 8,             /* nothing to poll yet / queue full */
+    PACC_EUNSUPPORTED = 9       /* option outside the supported model (e.g. INDEL > 0) */
+} pacc_status;
+
+typedef enum pacc_precision {
+    PACC_FP64 = 0,              /* plain path: FP64 partials */
+    PACC_FP32 = 1               /* FP32 partials with power-of-two rescaling, FP64 sums */
+} pacc_precision;
+
+/* Tree, rate matrix and species sets: the content of the .mod file plus the
+ * OUTGROUP / CONSERVE keys (bpp.hpp:173-404). */
+typedef struct pacc_model {
+    int32_t n_species;            /* S */
+    const int32_t* children;      /* [2*N] */
+    const double* distances;      /* [N] branch length above node i (parsed as float, newick.cpp:185,300,325) */
+    const double* pi;             /* [4] BACKGROUND */
+    const double* rate_matrix;    /* [16] RATE_MAT, row-major */
+    const int32_t* outgroup;      /* species ids; a name not found in the tree maps to S (bpp.hpp:303-308) */
+    int32_t n_outgroup;
+    const int32_t* conserve;      /* species ids (bpp.hpp:237-242) */
+    int32_t n_conserve;
+} pacc_model;
+
+/* Run options.  pacc_default_opts() gives PhyloAcc-ST's defaults
+ * (src/PhyloAcc-ST/main.cpp:36-90). */
+typedef struct pacc_opts {
+    int32_t burnin;               /* BURNIN   (200) */
+    int32_t mcmc;                 /* MCMC     (800) */
+    int32_t adapt_freq;           /* ADAPT_FREQ (500) */
+    uint32_t seed;                /* SEED (5): every element's stream starts from it */
+    double init_conserve_rate;    /* INIT_CONSERVE_RATE (0.5) */
+    double init_acce_rate;        /* INIT_ACCE_RATE (1) */
+    double conserve_prior_a;      /* CONSERVE_PRIOR_A (5) */
+    double conserve_prior_b;      /* CONSERVE_PRIOR_B (0.04) */
+    double acce_prior_a;          /* ACCE_PRIOR_A (10) */
+    double acce_prior_b;          /* ACCE_PRIOR_B (0.2) */
+    int32_t ropt;                 /* ROPT (1) */
+    double cub;                   /* CUB (1) */
+    double nlb;                   /* NLB (0.6) */
+    double init_lrate;            /* INIT_LRATE (0.3) */
+    double init_lrate2;           /* INIT_LRATE2 (0.1); forced to 0 when HYPER_LRATE2_A == 0 (main.cpp:286) */
+    double init_grate;            /* INIT_GRATE (0.5) */
+    double hyper_lrate_a, hyper_lrate_b;     /* (1, 9) */
+    double hyper_grate_a, hyper_grate_b;     /* (3, 1) */
+    double hyper_lrate2_a, hyper_lrate2_b;   /* (1, 9); a == 0 selects the Dollo model */
+    double conserve_prop;         /* CONSERVE_PROP (0.8) */
+    double gap_prop;              /* GAP_PROP (0.8) */
+    double cons_to_mis;           /* CONSTOMIS (0.01) */
+    int32_t gapchar;              /* GAPCHAR ('-') */
+    int32_t prune_tree;           /* PRUNE_TREE (0) */
+    double trim_gap_percent;      /* TRIM_GAP_PERCENT (1 = off) */
+    int32_t min_len;              /* MIN_LEN (50) */
+    double indel;                 /* INDEL (0); only 0 is supported */
+    /* --- GPU keys (no counterpart in PhyloAcc-ST) --- */
+    int32_t precision;            /* pacc_precision (PACC_FP64) */
+    int32_t device;               /* CUDA device ordinal (0) */
+    int64_t memory_budget_bytes;  /* device bytes the context may hold for chain state (0 = 25% of free) */
+    int32_t max_resident;         /* max chains resident at once (0 = derived from the budget) */
+    int32_t sweeps_per_launch;    /* MCMC iterations per kernel launch (0 = run chains to completion) */
+    int32_t trace_iters;          /* record the first trace_iters iterations of every model (0 = off) */
+    int32_t block_threads;        /* threads per chain CTA (0 = autotuned) */
+    int32_t use_graphs;           /* capture the sweep launches in a CUDA graph (1) */
+} pacc_opts;
+
+/* A batch of elements.  Element e's alignment block is n_species rows of
+ * lengths[e] bytes, rows in tree leaf order (the order MatchProfAndTree
+ * produces, bpp.cpp:133-184), lower-case as LoadPhyloProfiles stores it
+ * (profile.cpp:48,60).  The bytes are copied before pacc_submit returns. */
+typedef struct pacc_element_batch {
+    int32_t n_elements;
+    const int64_t* element_no;    /* [n] value written in the "No." column */
+    const int32_t* lengths;       /* [n] alignment columns of each element */
+    const int64_t* offsets;       /* [n] byte offset of each block in `bases` */
+    const uint8_t* bases;
+} pacc_element_batch;
+
+/* Per-model summary (one row of _rate_postZ_M*.txt plus _elem_lik.txt fields). */
+typedef struct pacc_model_result {
+    double loglik;                /* marginal log-likelihood from Eval2 (bpp_c2.cpp:14-353) */
+    double max_loglik;            /* max of the traced full log-likelihood after burn-in (bpp_c.cpp:809-814) */
+    double n_rate, c_rate, g_rate, l_rate, l2_rate;  /* posterior medians (bpp_c2.cpp:742-755) */
+    int32_t failure;              /* NaN marginal likelihood */
+    int32_t n_configs;            /* Z configurations found by Eval2 */
+} pacc_model_result;
+
+/* Optional per-iteration trace (first trace_iters iterations of each model). */
+typedef struct pacc_trace {
+    double* loglik;               /* [3][T]  trace_loglik */
+    double* n_rate;               /* [3][T] */
+    double* c_rate;               /* [3][T] */
+    double* g_rate;               /* [3][T] */
+    double* l_rate;               /* [3][T] */
+    double* l2_rate;              /* [3][T] */
+    int8_t* z;                    /* [3][T][N] */
+} pacc_trace;
+
+typedef struct pacc_result {
+    int64_t element_no;
+    int32_t status;               /* PACC_OK, PACC_FILTERED, PACC_NAN_LIKELIHOOD, PACC_SAMPLER_ERROR */
+    int32_t n_nodes;              /* N */
+    pacc_model_result model[3];   /* M0, M1, M2 */
+    int32_t* max_z;               /* caller buffer [3*N] or NULL: Max_Z per model (bpp.cpp:607-614) */
+    double* post_z;               /* caller buffer [3*N*4] or NULL: countZ/MCMC per model (bpp_c2.cpp:757-781) */
+    pacc_trace trace;             /* caller buffers or NULL pointers */
+    double latency_ms;            /* submit -> result available (serving) */
+    double device_ms;             /* time the element's chain spent on the device */
+} pacc_result;
+
+typedef struct pacc_ctx pacc_ctx;
+
+/* Defaults of PhyloAcc-ST's driver plus the GPU keys. */
+void pacc_default_opts(pacc_opts* opts);
+
+/* Build a context: validates the tree, decomposes RATE_MAT in FP64
+ * (replaces eig_gen/inv at bpp.hpp:357-362), builds the null-rate
+ * transition cache (bpp.hpp:366-397) and the upper/upper_conserve sets
+ * (bpp.hpp:303-310), and reserves device memory against the budget. */
+pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* status);
+
+/* Queue a batch (replaces the element loop of main.cpp:452-500).  Columns
+ * are encoded, trimmed and the tree pruned per element on the host
+ * (bpp_c.hpp:204-428); elements are admitted to the device as chain slots
+ * and memory free up.  Returns PACC_OK or an error; per-element outcomes
+ * are reported by pacc_poll. */
+int pacc_submit(pacc_ctx* ctx, const pacc_element_batch* batch);
+
+/* Advance the device and collect up to max finished elements into out.
+ * Returns the number written (>= 0) or a negative pacc_status. */
+int pacc_poll(pacc_ctx* ctx, pacc_result* out, int max);
+
+/* Block until every submitted element has finished. */
+int pacc_sync(pacc_ctx* ctx);
+
+/* Number of submitted elements whose results have not been polled yet. */
+int pacc_pending(pacc_ctx* ctx);
+
+/* Convenience: submit + sync + poll for one batch; out[i] matches batch order. */
+int pacc_run(pacc_ctx* ctx, const pacc_element_batch* batch, pacc_result* out);
+
+void pacc_destroy(pacc_ctx* ctx);
+
+/* Last error text of the context (or of the last failed pacc_create when ctx is NULL). */
+const char* pacc_last_error(pacc_ctx* ctx);
+
+/* Device counters of the last pacc_sync/pacc_run: work units actually performed. */
+typedef struct pacc_counters {
+    double edge_updates_internal;  /* parent *= P * child-partial (internal child): 36 flop each */
+    double edge_updates_leaf;      /* parent *= column of P (leaf child): 4 (8 ambiguous) flop each */
+    double column_loglik;          /* per-column root sums + logs */
+    double tg_draws;               /* internal-base categorical draws */
+    double z_draws;                /* latent-state draws */
+    double pmatrix_builds;         /* branch transition matrices built on device */
+    double iterations;             /* MCMC iterations run (all models) */
+    double kernel_ms;              /* summed duration of the chain kernels (CUDA events) */
+    double flop;                   /* algorithmic FP work of the prunes, counted from the above */
+} pacc_counters;
+int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);
+
+/* --- Kernel-level entry points used by parity tests (same kernels as the chain) --- */
+
+/* (a) P^T = eigeninv * diag(exp(lambda*d*r)) * eigenvec for n branch lengths
+ * d[i] and rates r[i], FP64 on the device.  out: [n][16] row-major (child, parent). */
+int pacc_debug_pmatrix(pacc_ctx* ctx, int n, const double* d, const double* r, double* out);
+
+/* (b) Per-column log-likelihood of one element for a given Z (int32 [N]) and
+ * conserved/accelerated rates, using the chosen precision's pruning kernel.
+ * out: [columns after trimming]; returns the column count via *n_cols. */
+int pacc_debug_loglik(pacc_ctx* ctx, const uint8_t* bases, int32_t length, const int32_t* z,
+                      double c_rate, double n_rate, double* out, int32_t* n_cols);
+
+/* Per-element column encoding (bpp_c.hpp:204-264): Tg codes after trimming,
+ * [n_cols][N] int8 (-1 ambiguous, 0..3 base, 4 gap, 5 other; internal nodes
+ * set to 4 where both children are >= 4), plus the missing flags [N] and the
+ * pruned-tree root.  For bit-exact checks of the host preprocessing. */
+int pacc_debug_encode(pacc_ctx* ctx, const uint8_t* bases, int32_t length, int8_t* tg_out,
+                      int32_t* n_cols, uint8_t* missing_out, int32_t* root_out, int32_t* filtered);
+
+/* Philox stream words w0 .. w0+n-1 generated on the device. */
+int pacc_debug_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out);
+
+/* Measured FMA throughput of this GPU, FLOP/s: fp64 and fp32 (FMA = 2 flop). */
+int pacc_measure_fma_peak(int device, double* fp64_flops, double* fp32_flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PACC_H */

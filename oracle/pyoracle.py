@@ -1,0 +1,140 @@
+"""TEST INFRASTRUCTURE: ctypes access to oracle/_build/liboracle.so.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline call this."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from phyloacc_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            from oracle.build_oracle import build_oracle
+            build_oracle()
+        L = C.CDLL(path)
+        L.oracle_run.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts),
+                                 C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccResult), C.c_int]
+        L.oracle_run.restype = C.c_int
+        L.oracle_encode.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.POINTER(C.c_uint8),
+                                    C.c_int32, C.POINTER(C.c_int8), C.POINTER(C.c_int32), C.POINTER(C.c_uint8),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.oracle_encode.restype = C.c_int
+        L.oracle_loglik.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.POINTER(C.c_uint8),
+                                    C.c_int32, C.POINTER(C.c_int32), C.c_double, C.c_double,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.oracle_loglik.restype = C.c_int
+        L.oracle_pmatrix.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.c_int,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_pmatrix.restype = C.c_int
+        L.oracle_stream.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint32)]
+        L.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.oracle_sample_gamma.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double)]
+        L.oracle_sample_beta.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double)]
+        L.oracle_sample_categorical.argtypes = [C.c_uint32, C.c_int, C.POINTER(C.c_double), C.c_int,
+                                                C.POINTER(C.c_int32)]
+        L.oracle_eigen.argtypes = [C.POINTER(C.c_double)] * 4
+        L.oracle_eigen.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def run(ds, opts: abi.PaccOpts, threads: int = 0, element_no=None) -> abi.Results:
+    m = abi.ModelArgs(ds)
+    b = abi.BatchArgs(ds, element_no)
+    res = abi.Results(ds.n_elements, ds.tree.n_nodes, opts.trace_iters)
+    st = lib().oracle_run(C.byref(m.model), C.byref(opts), C.byref(b.batch), res.arr, threads)
+    if st != abi.PACC_OK:
+        raise RuntimeError("oracle_run failed: %d" % st)
+    return res
+
+
+def encode(ds, opts, e: int):
+    m = abi.ModelArgs(ds)
+    blk = np.ascontiguousarray(ds.element(e).reshape(-1))
+    L = int(ds.lengths[e])
+    N = ds.tree.n_nodes
+    tg = np.zeros(L * N, dtype=np.int8)
+    ncol = C.c_int32()
+    miss = np.zeros(N, dtype=np.uint8)
+    root = C.c_int32()
+    filt = C.c_int32()
+    st = lib().oracle_encode(C.byref(m.model), C.byref(opts), abi.ptr(blk, C.c_uint8), L, abi.ptr(tg, C.c_int8),
+                             C.byref(ncol), abi.ptr(miss, C.c_uint8), C.byref(root), C.byref(filt))
+    assert st == 0
+    return tg[:ncol.value * N].reshape(ncol.value, N), miss, root.value, filt.value
+
+
+def loglik(ds, opts, e: int, z, c_rate: float, n_rate: float) -> np.ndarray:
+    m = abi.ModelArgs(ds)
+    blk = np.ascontiguousarray(ds.element(e).reshape(-1))
+    L = int(ds.lengths[e])
+    out = np.zeros(L, dtype=np.float64)
+    ncol = C.c_int32()
+    z = np.ascontiguousarray(z, dtype=np.int32)
+    st = lib().oracle_loglik(C.byref(m.model), C.byref(opts), abi.ptr(blk, C.c_uint8), L, abi.ptr(z, C.c_int32),
+                             c_rate, n_rate, abi.ptr(out, C.c_double), C.byref(ncol))
+    assert st == 0, st
+    return out[:ncol.value]
+
+
+def pmatrix(ds, opts, d, r) -> np.ndarray:
+    m = abi.ModelArgs(ds)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    out = np.zeros((len(d), 16))
+    st = lib().oracle_pmatrix(C.byref(m.model), C.byref(opts), len(d), abi.ptr(d, C.c_double),
+                              abi.ptr(r, C.c_double), abi.ptr(out, C.c_double))
+    assert st == 0
+    return out.reshape(-1, 4, 4)
+
+
+def stream(seed: int, w0: int, n: int) -> np.ndarray:
+    out = np.zeros(n, dtype=np.uint32)
+    lib().oracle_stream(seed, w0, n, abi.ptr(out, C.c_uint32))
+    return out
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().oracle_philox(abi.ptr(c, C.c_uint32), abi.ptr(k, C.c_uint32), abi.ptr(out, C.c_uint32))
+    return out
+
+
+def sample_gamma(seed, a, b, n):
+    out = np.zeros(n)
+    lib().oracle_sample_gamma(seed, a, b, n, abi.ptr(out, C.c_double))
+    return out
+
+
+def sample_beta(seed, a, b, n):
+    out = np.zeros(n)
+    lib().oracle_sample_beta(seed, a, b, n, abi.ptr(out, C.c_double))
+    return out
+
+
+def sample_categorical(seed, p, n):
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros(n, dtype=np.int32)
+    lib().oracle_sample_categorical(seed, len(p), abi.ptr(p, C.c_double), n, abi.ptr(out, C.c_int32))
+    return out
+
+
+def eigen(Q):
+    Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1)
+    lam = np.zeros(4)
+    V = np.zeros(16)
+    Vi = np.zeros(16)
+    st = lib().oracle_eigen(*(abi.ptr(a, C.c_double) for a in (Q, lam, V, Vi)))
+    return st, lam, V.reshape(4, 4), Vi.reshape(4, 4)

@@ -1,0 +1,175 @@
+"""phyloacc-gb300: PhyloAcc-ST's per-element Bayesian MCMC on one NVIDIA GB300.
+
+Python access to the C ABI of include/pacc.h (libpaccgpu.so, built in-tree by
+phyloacc_gb300/build.py).  The compute path is the CUDA library; there is no
+Python or CPU fallback: every call fails with an exception when the library
+or a GPU is missing.
+
+    from phyloacc_gb300 import Context, default_opts
+    ctx = Context(dataset, opts)          # pacc_create
+    res = ctx.run(dataset)                # pacc_run -> abi.Results
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import default_opts  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpaccgpu.so")
+CLI_PATH = os.path.join(HERE, "_build", "phyloacc-st-gpu")
+_lib = None
+
+
+def lib():
+    """Load libpaccgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libpaccgpu.so is not built; run phyloacc_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH)
+        L.pacc_default_opts.argtypes = [C.POINTER(abi.PaccOpts)]
+        L.pacc_create.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.POINTER(C.c_int)]
+        L.pacc_create.restype = C.c_void_p
+        L.pacc_submit.argtypes = [C.c_void_p, C.POINTER(abi.PaccElementBatch)]
+        L.pacc_poll.argtypes = [C.c_void_p, C.POINTER(abi.PaccResult), C.c_int]
+        L.pacc_sync.argtypes = [C.c_void_p]
+        L.pacc_pending.argtypes = [C.c_void_p]
+        L.pacc_run.argtypes = [C.c_void_p, C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccResult)]
+        L.pacc_destroy.argtypes = [C.c_void_p]
+        L.pacc_last_error.argtypes = [C.c_void_p]
+        L.pacc_last_error.restype = C.c_char_p
+        L.pacc_get_counters.argtypes = [C.c_void_p, C.POINTER(abi.PaccCounters)]
+        L.pacc_debug_pmatrix.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
+        L.pacc_debug_loglik.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int32),
+                                        C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.pacc_debug_encode.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int8),
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int32)]
+        L.pacc_debug_stream.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint32)]
+        L.pacc_measure_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+class PaccError(RuntimeError):
+    pass
+
+
+class Context:
+    """A pacc context for one tree / rate matrix / option set."""
+
+    def __init__(self, ds, opts: abi.PaccOpts):
+        self.ds = ds
+        self.opts = opts
+        self._m = abi.ModelArgs(ds)
+        st = C.c_int(0)
+        self.h = lib().pacc_create(C.byref(self._m.model), C.byref(opts), C.byref(st))
+        if not self.h:
+            raise PaccError("pacc_create failed (%d): %s" % (st.value, lib().pacc_last_error(None).decode()))
+
+    def close(self):
+        if self.h:
+            lib().pacc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _err(self, what, st):
+        raise PaccError("%s failed (%d): %s" % (what, st, lib().pacc_last_error(self.h).decode()))
+
+    def run(self, ds=None, element_no=None) -> abi.Results:
+        ds = self.ds if ds is None else ds
+        b = abi.BatchArgs(ds, element_no)
+        res = abi.Results(ds.n_elements, ds.tree.n_nodes, self.opts.trace_iters)
+        st = lib().pacc_run(self.h, C.byref(b.batch), res.arr)
+        if st != 0:
+            self._err("pacc_run", st)
+        return res
+
+    def submit(self, ds, element_no=None):
+        b = abi.BatchArgs(ds, element_no)
+        st = lib().pacc_submit(self.h, C.byref(b.batch))
+        if st != 0:
+            self._err("pacc_submit", st)
+
+    def sync(self):
+        st = lib().pacc_sync(self.h)
+        if st != 0:
+            self._err("pacc_sync", st)
+
+    def poll(self, max_n: int) -> abi.Results:
+        res = abi.Results(max_n, self.ds.tree.n_nodes, self.opts.trace_iters)
+        k = lib().pacc_poll(self.h, res.arr, max_n)
+        if k < 0:
+            self._err("pacc_poll", -k)
+        res.n = k
+        return res
+
+    def counters(self) -> dict:
+        c = abi.PaccCounters()
+        lib().pacc_get_counters(self.h, C.byref(c))
+        return {n: getattr(c, n) for n, _ in abi.PaccCounters._fields_}
+
+    def pmatrix(self, d, r) -> np.ndarray:
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        out = np.zeros((len(d), 16))
+        st = lib().pacc_debug_pmatrix(self.h, len(d), abi.ptr(d, C.c_double), abi.ptr(r, C.c_double),
+                                      abi.ptr(out, C.c_double))
+        if st != 0:
+            self._err("pacc_debug_pmatrix", st)
+        return out.reshape(-1, 4, 4)
+
+    def loglik(self, e: int, z, c_rate: float, n_rate: float) -> np.ndarray:
+        blk = np.ascontiguousarray(self.ds.element(e).reshape(-1))
+        L = int(self.ds.lengths[e])
+        out = np.zeros(L)
+        ncol = C.c_int32()
+        z = np.ascontiguousarray(z, dtype=np.int32)
+        st = lib().pacc_debug_loglik(self.h, abi.ptr(blk, C.c_uint8), L, abi.ptr(z, C.c_int32), c_rate, n_rate,
+                                     abi.ptr(out, C.c_double), C.byref(ncol))
+        if st != 0:
+            self._err("pacc_debug_loglik", st)
+        return out[:ncol.value]
+
+    def encode(self, e: int):
+        blk = np.ascontiguousarray(self.ds.element(e).reshape(-1))
+        L = int(self.ds.lengths[e])
+        N = self.ds.tree.n_nodes
+        tg = np.zeros(L * N, dtype=np.int8)
+        ncol = C.c_int32()
+        miss = np.zeros(N, dtype=np.uint8)
+        root = C.c_int32()
+        filt = C.c_int32()
+        st = lib().pacc_debug_encode(self.h, abi.ptr(blk, C.c_uint8), L, abi.ptr(tg, C.c_int8), C.byref(ncol),
+                                     abi.ptr(miss, C.c_uint8), C.byref(root), C.byref(filt))
+        if st != 0:
+            self._err("pacc_debug_encode", st)
+        return tg[:ncol.value * N].reshape(ncol.value, N), miss, root.value, filt.value
+
+
+def stream_words(seed: int, w0: int, n: int) -> np.ndarray:
+    out = np.zeros(n, dtype=np.uint32)
+    st = lib().pacc_debug_stream(seed, w0, n, abi.ptr(out, C.c_uint32))
+    if st != 0:
+        raise PaccError("pacc_debug_stream failed (%d)" % st)
+    return out
+
+
+def measure_fma_peak(device: int = 0):
+    """Measured FP64 and FP32 FMA throughput of the GPU in FLOP/s."""
+    a, b = C.c_double(), C.c_double()
+    st = lib().pacc_measure_fma_peak(device, C.byref(a), C.byref(b))
+    if st != 0:
+        raise PaccError("pacc_measure_fma_peak failed (%d)" % st)
+    return a.value, b.value

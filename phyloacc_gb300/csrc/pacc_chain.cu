@@ -1,0 +1,1422 @@
+// pacc_chain.cu — PhyloAcc-ST's per-element MCMC as one CUDA thread block
+// per element (sm_103a).
+//
+// One CTA runs an element through M0, M1 and M2 (src/PhyloAcc-ST/main.cpp:468-494):
+// initMCMC -> Gibbs -> Eval2 -> Output_init, all on the device.  The
+// element's alignment columns are spread over the CTA's threads; every
+// chain-level step (latent-state filter, Metropolis-Hastings decisions,
+// Beta draws) is done by a few threads between block barriers.
+//
+// Numerics.  The reference keeps every partial likelihood in log space and
+// combines children with a 4x4 log-sum-exp (BPP::log_multi, bpp.hpp:427-445).
+// Here partials are linear, L_s[j] = prod_children sum_i P(j->i) L_c[i], kept
+// as mantissa * 2^scale with an integer exponent per (node, column): the
+// power-of-two rescale is exact, so the values equal the log-space ones up to
+// rounding (about 1e-16 relative per column in FP64).  Skipped children (gap
+// or missing, bpp_c.cpp:653,660) multiply by nothing, like the reference's
+// "add nothing".
+//
+// Partial re-pruning follows the reference's visited masks
+// (getUpdateNode, bpp_c.cpp:620-642, 836-858): only ancestors of changed
+// branches are recomputed.  MH proposals write the recomputed nodes to the
+// other half of a per-node double buffer (the reference's lambda_tmp,
+// bpp_c.cpp:981-989) and an accepted proposal flips the buffer index of
+// those nodes instead of copying (bpp_c.cpp:1083-1092).
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "pacc_dev.h"
+#include "pacc_rng.cuh"
+
+namespace pacc {
+
+__constant__ DevModel dM;
+
+// Workspace carve-up (per CTA).
+struct WsLayout {
+    size_t lam, scale, tg, trz, trd, hash, rep, cfg, nxt, head, first, cstat, total;
+    __host__ __device__ static WsLayout make(int n_int, int GGp, int T, int mcmc, int N, int real_bytes) {
+        WsLayout w;
+        size_t o = 0;
+        auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+        w.lam = o; o = al(o + (size_t)2 * n_int * 4 * GGp * real_bytes);
+        w.scale = o; o = al(o + (size_t)2 * n_int * GGp * 4);
+        w.tg = o; o = al(o + (size_t)n_int * GGp);
+        w.trz = o; o = al(o + (size_t)T * N);
+        w.trd = o; o = al(o + (size_t)7 * T * 8);
+        w.hash = o; o = al(o + (size_t)(mcmc + 1) * 8);
+        w.rep = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        w.cfg = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        w.nxt = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        w.head = o; o = al(o + (size_t)(mcmc + 2) * 4);
+        w.first = o; o = al(o + (size_t)(mcmc + 2) * 4);
+        w.cstat = o; o = al(o + (size_t)9 * (mcmc + 2) * 8);
+        w.total = o;
+        return w;
+    }
+};
+
+// trace_d rows
+enum { TR_LL = 0, TR_FULL = 1, TR_N = 2, TR_C = 3, TR_G = 4, TR_L = 5, TR_L2 = 6 };
+
+// Chain scalars shared by the block.
+struct ChainScalars {
+    uint64_t pos;          // next stream word
+    double rate_n, rate_c; // current rates
+    double prop_n, prop_c;
+    double loglik;         // log_lik_old
+    double maxll;
+    double proposal;
+    double mh_new;
+    int acc_n, acc_c;
+    int m, resZ, mi;
+    int max_m;
+    int skip;              // proposal rejected before the likelihood
+    int accept;
+    int any_unv;
+    int status;
+    int n_unc, n_conf, eff;
+    double vb;
+    int fallback;
+};
+
+// Shared-memory layout (dynamic, sized by N).
+template <typename Real>
+struct SmemLayout {
+    size_t ptd, ptr_, ltm, emis, beta, cnt, red, i16, i8, total;
+    __host__ __device__ static SmemLayout make(int N, int BT) {
+        SmemLayout s;
+        size_t o = 0;
+        auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        s.ptd = o; o = al(o + (size_t)4 * N * 16 * 8);                      // double P^T per class [4][N][16]
+        s.ptr_ = o; o = al(o + (sizeof(Real) == 8 ? 0 : (size_t)4 * N * 16 * sizeof(Real)));
+        s.ltm = o; o = al(o + (size_t)N * 9 * 8);                          // log_TM_Int [N][3][3]
+        s.emis = o; o = al(o + (size_t)N * 3 * 8);
+        s.beta = o; o = al(o + (size_t)N * 3 * 8);
+        s.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 4);                    // emission histogram
+        s.red = o; o = al(o + (size_t)(BT / 32 + 2) * 8 * 2);
+        s.i16 = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
+        s.i8 = o; o = al(o + (size_t)N * 8);                               // Z fixZ changed unv unvN unvC cur maxz
+        s.total = o;
+        return s;
+    }
+};
+
+enum { P_NULL = 0, P_CONS = 1, P_NEUT = 2, P_PROP = 3 };
+
+// ---------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    // deterministic: warp tree then warps in order
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x == 0) {
+        int nw = blockDim.x >> 5;
+        for (int i = 0; i < nw; i++) r += red[i];
+        red[31] = r;
+    }
+    __syncthreads();
+    r = red[31];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ int block_or(int v, int* tmp) {
+    __syncthreads();
+    if (threadIdx.x == 0) *tmp = 0;
+    __syncthreads();
+    if (v) atomicOr(tmp, 1);
+    __syncthreads();
+    int r = *tmp;
+    __syncthreads();
+    return r;
+}
+
+// Gamma(shape a, scale b) density and its log as the reference takes it (bpp_c.cpp:784,1046).
+__device__ double gamma_pdf(double x, double a, double b) {
+    if (x < 0) return 0.0;
+    if (x == 0) return (a == 1) ? 1.0 / b : 0.0;
+    double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, log(x)), __ddiv_rn(x, b)), lgamma(a)),
+                         __dmul_rn(a, log(b)));
+    return exp(t);
+}
+__device__ __forceinline__ double log_gamma_pdf(double x, double a, double b) { return log(gamma_pdf(x, a, b)); }
+__device__ __forceinline__ double lnbeta(double a, double b) {
+    return __dsub_rn(__dadd_rn(lgamma(a), lgamma(b)), lgamma(__dadd_rn(a, b)));
+}
+
+// P^T(d*r) = eigeninv * diag(exp(lambda*d*r)) * eigenvec  (bpp.hpp:375-380), FP64.
+// scaled=false uses exp(lambda*d) as the null-rate cache does (bpp.hpp:375).
+__device__ void build_pt(double d, double r, bool scaled, double* out) {
+    double e[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        double x = __dmul_rn(dM.lam[i], d);
+        if (scaled) x = __dmul_rn(x, r);
+        e[i] = exp(x);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            double s = 0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) s = __dadd_rn(s, __dmul_rn(dM.einv[a * 4 + i], __dmul_rn(dM.evec[i * 4 + b], e[i])));
+            out[a * 4 + b] = s;
+        }
+}
+
+__device__ void identity_pt(double* out) {
+#pragma unroll
+    for (int a = 0; a < 16; a++) out[a] = ((a >> 2) == (a & 3)) ? 1.0 : 0.0;
+}
+
+// Exact rescale by a power of two when the largest entry is small.
+template <typename Real> struct Rescale;
+template <> struct Rescale<double> {
+    static __device__ __forceinline__ void apply(double* a, int& sc) {
+        double mx = fmax(fmax(a[0], a[1]), fmax(a[2], a[3]));
+        if (mx < 0x1p-256 && mx > 0) {
+            do {
+#pragma unroll
+                for (int j = 0; j < 4; j++) a[j] *= 0x1p256;
+                sc -= 256;
+                mx *= 0x1p256;
+            } while (mx < 0x1p-256);
+        }
+    }
+};
+template <> struct Rescale<float> {
+    static __device__ __forceinline__ void apply(float* a, int& sc) {
+        float mx = fmaxf(fmaxf(a[0], a[1]), fmaxf(a[2], a[3]));
+        if (mx < 0x1p-60f && mx > 0) {
+            int e;
+            frexpf(mx, &e);
+            // bring the max into [0.5, 1): multiply by 2^(-e) in two exact steps
+            int k = -e;
+            float f1 = ldexpf(1.0f, k / 2), f2 = ldexpf(1.0f, k - k / 2);
+#pragma unroll
+            for (int j = 0; j < 4; j++) a[j] = (a[j] * f1) * f2;
+            sc -= k;
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// The element context held by one CTA
+// ---------------------------------------------------------------------------
+template <typename Real>
+struct Ctx {
+    // element
+    int S, N, GG, GGp, root, n_nodes, n_int, n_hlev, n_dlev, tg_draws;
+    const uint8_t* codes;     // [S][GGp]
+    const int32_t* prefix;    // [GG+1]
+    // topology in shared
+    int16_t *nodes, *internal, *c2a, *c2b, *par, *irank, *pos, *missing, *upc, *upcc, *hlev_start, *hlev_nodes,
+        *dlev_start, *dlev_nodes;
+    // shared state
+    double* ptd;              // [4][N][16]
+    Real* ptr;                // [4][N][16]
+    double* ltm;              // [N][9] log_TM_Int (zc*3+zp)
+    double* emis;             // [N][3]
+    double* beta;             // [N][3]
+    int* cnt;                 // [N][NSYM*4]
+    double* red;
+    int8_t *Z, *fixZ, *changed, *unv, *unvN, *unvC, *cur, *maxz;
+    ChainScalars* cs;
+    // workspace
+    Real* lam;                // [2][n_int][4][GGp]
+    int32_t* scl;             // [2][n_int][GGp]
+    int8_t* tg;               // [n_int][GGp] internal Tg
+    int8_t* trz;              // [T][N]
+    double* trd;              // [7][T]
+    uint64_t* hash;
+    int32_t *rep, *cfg, *nxt, *head, *first;
+    double* cstat;
+    int T, burn, mcmc;
+    DevCounters local;
+
+    __device__ __forceinline__ Real* L(int buf, int ir, int j) { return lam + (((size_t)buf * n_int + ir) * 4 + j) * GGp; }
+    __device__ __forceinline__ int32_t* SC(int buf, int ir) { return scl + ((size_t)buf * n_int + ir) * GGp; }
+    __device__ __forceinline__ int tg_of(int s, int g) {
+        // Tg of a node at column g: leaves from their code, internal nodes from the sampled state
+        if (s < S) {
+            int c = codes[(size_t)s * GGp + g];
+            return c < 4 ? c : (c == CODE_GAP ? 4 : (c == CODE_OTHER ? 5 : -1));
+        }
+        return tg[(size_t)irank[s] * GGp + g];
+    }
+};
+
+// Class of the matrix used for child c: Z 2 -> neut, 0 -> null, else cons
+// (bpp_c.cpp:661-663); in an MH proposal the proposed class uses P_PROP (bpp_c.cpp:885-906).
+__device__ __forceinline__ int mat_class(int z, int prop_class) {
+    int k = (z == 2) ? P_NEUT : (z == 0 ? P_NULL : P_CONS);
+    return (prop_class >= 0 && k == prop_class) ? P_PROP : k;
+}
+
+// Felsenstein pruning over the nodes flagged in `unv` (postorder), all columns.
+// mh = false: results overwrite the current buffer of each node (Update_Tg with
+// visited masks, bpp_c.cpp:647-671).  mh = true: results go to the other
+// buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928).  Returns the summed
+// per-column log-likelihood at the root (valid when the root is flagged).
+template <typename Real>
+__device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
+    const int BT = blockDim.x;
+    double ll_sum = 0;
+    unsigned long long e_int = 0, e_leaf = 0;
+    for (int k = 0; k < c.n_int; k++) {
+        int s = c.internal[k];
+        if (!unv[s] || c.missing[s]) continue;
+        int ir = c.irank[s];
+        int dst = mh ? (1 - c.cur[s]) : c.cur[s];
+        int ch[2] = {c.c2a[s], c.c2b[s]};
+        Real P0[16], P1[16];
+        bool use[2];
+        int csrc[2], cir[2];
+        use[0] = !c.missing[ch[0]];
+        use[1] = !c.missing[ch[1]];
+        {
+            const Real* p0 = c.ptr + ((size_t)mat_class(c.Z[ch[0]], prop_class) * c.N + ch[0]) * 16;
+            const Real* p1 = c.ptr + ((size_t)mat_class(c.Z[ch[1]], prop_class) * c.N + ch[1]) * 16;
+#pragma unroll
+            for (int i = 0; i < 16; i++) { P0[i] = p0[i]; P1[i] = p1[i]; }
+        }
+        for (int q = 0; q < 2; q++) {
+            cir[q] = ch[q] >= c.S ? c.irank[ch[q]] : -1;
+            csrc[q] = (ch[q] >= c.S) ? ((mh && unv[ch[q]]) ? 1 - c.cur[ch[q]] : c.cur[ch[q]]) : 0;
+        }
+        const bool is_root = (s == c.root);
+        Real* Ld = c.L(dst, ir, 0);
+        int32_t* Sd = c.SC(dst, ir);
+        const int8_t* tgs = c.tg + (size_t)ir * c.GGp;
+        for (int g = threadIdx.x; g < c.GG; g += BT) {
+            Real a[4] = {1, 1, 1, 1};
+            int sc = 0;
+            if (tgs[g] < KB) {
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    if (!use[q]) continue;
+                    const Real* P = q ? P1 : P0;
+                    int cc = ch[q];
+                    if (cc < c.S) {
+                        int code = c.codes[(size_t)cc * c.GGp + g];
+                        if (code == CODE_GAP || code == CODE_OTHER) continue;
+                        if (code < 4) {
+#pragma unroll
+                            for (int j = 0; j < 4; j++) a[j] *= P[code * 4 + j];
+                        } else {
+                            int msk = ambig_mask(code - CODE_R);
+                            Real v[4] = {0, 0, 0, 0};
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                                if (msk & (1 << i)) {
+#pragma unroll
+                                    for (int j = 0; j < 4; j++) v[j] += P[i * 4 + j];
+                                }
+#pragma unroll
+                            for (int j = 0; j < 4; j++) a[j] *= v[j];
+                        }
+                        e_leaf++;
+                    } else {
+                        if (c.tg[(size_t)cir[q] * c.GGp + g] >= KB) continue;
+                        const Real* Lc = c.L(csrc[q], cir[q], 0);
+                        Real x0 = Lc[g], x1 = Lc[g + c.GGp], x2 = Lc[g + 2 * c.GGp], x3 = Lc[g + 3 * c.GGp];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            Real v = P[j] * x0;
+                            v += P[4 + j] * x1;
+                            v += P[8 + j] * x2;
+                            v += P[12 + j] * x3;
+                            a[j] *= v;
+                        }
+                        sc += c.SC(csrc[q], cir[q])[g];
+                        e_int++;
+                    }
+                }
+                Rescale<Real>::apply(a, sc);
+            }
+            if (is_root) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
+                double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
+                ll_sum += log(t) + (double)sc * 0.6931471805599453;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) Ld[j * c.GGp + g] = a[j];
+            Sd[g] = sc;
+        }
+    }
+    c.local.edge_internal += e_int;
+    c.local.edge_leaf += e_leaf;
+    if (threadIdx.x < c.GG) c.local.col_ll += 0;
+    double r = block_sum(ll_sum, c.red);
+    if (threadIdx.x == 0) c.local.col_ll += c.GG;
+    return r;
+}
+
+// Build the P^T table of class k for all nodes of the pruned tree (except the
+// root) at rate r.  Branches shorter than 1e-10 keep the identity
+// (bpp_c.cpp:191-226, 1123).  force_eigen: the proposal matrices of log_f_Xz
+// (bpp_c.cpp:887-902) and the Eval2 fallback (bpp_c2.cpp:220-237) apply the
+// eigen formula whatever the branch length.
+template <typename Real>
+__device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
+    for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
+        int s = c.nodes[i];
+        double* out = c.ptd + ((size_t)k * c.N + s) * 16;
+        if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, out);
+        else identity_pt(out);
+        if (sizeof(Real) != 8) {
+            Real* o2 = c.ptr + ((size_t)k * c.N + s) * 16;
+            for (int q = 0; q < 16; q++) o2[q] = (Real)out[q];
+        }
+        c.local.pmat++;
+    }
+}
+
+template <typename Real>
+__device__ void copy_class(Ctx<Real>& c, const double* dist2, int from, int to) {
+    // accepted proposal becomes the cache; branches < 1e-10 are not rebuilt (bpp_c.cpp:1123)
+    for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
+        int s = c.nodes[i];
+        if (dist2[s] < 1e-10) continue;
+        double* a = c.ptd + ((size_t)from * c.N + s) * 16;
+        double* b = c.ptd + ((size_t)to * c.N + s) * 16;
+        for (int q = 0; q < 16; q++) b[q] = a[q];
+        if (sizeof(Real) != 8) {
+            Real* a2 = c.ptr + ((size_t)from * c.N + s) * 16;
+            Real* b2 = c.ptr + ((size_t)to * c.N + s) * 16;
+            for (int q = 0; q < 16; q++) b2[q] = a2[q];
+        }
+    }
+}
+
+// log_TM_Int from the current g, l, l2 (bpp_c.cpp:301-332, 573-599).
+template <typename Real>
+__device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool init) {
+    const double NI = -CUDART_INF;
+    for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
+        int s = c.nodes[i];
+        double* t = c.ltm + (size_t)s * 9;   // t[zc*3 + zp]
+        if (c.fixZ[s] == 1) {
+            if (init) t[0 * 3 + 1] = NI;
+            t[1 * 3 + 1] = 0;
+            t[2 * 3 + 1] = NI;
+            t[0 * 3 + 0] = log(1 - gr);
+            t[1 * 3 + 0] = log(gr);
+            t[2 * 3 + 0] = NI;
+        } else {
+            t[0 * 3 + 0] = log(1 - gr);
+            t[1 * 3 + 0] = log(gr);
+            t[2 * 3 + 0] = NI;
+            double y = 1 - lr;
+            if (init) t[0 * 3 + 1] = NI;
+            t[1 * 3 + 1] = log(y);
+            t[2 * 3 + 1] = log(1 - y);
+            if (init) t[0 * 3 + 2] = NI;
+            t[1 * 3 + 2] = log(lr2);
+            t[2 * 3 + 2] = log(1 - lr2);
+        }
+    }
+}
+
+// Internal-base sampling, top-down per column (Update_Tg with tosample,
+// bpp_c.cpp:672-733).  Column g takes its words at pos + prefix[g].
+template <typename Real>
+__device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
+    int err = 0;
+    const int rir = c.irank[c.root];
+    const int rbuf = c.cur[c.root];
+    unsigned long long draws = 0;
+    for (int g = threadIdx.x; g < c.GG; g += blockDim.x) {
+        uint64_t w = pos + (uint64_t)c.prefix[g];
+        uint64_t blk = ~0ull;
+        uint32_t words[4];
+        auto next_u = [&]() {
+            uint64_t b = w >> 2;
+            if (b != blk) {
+                philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, words);
+                blk = b;
+            }
+            double u = word_to_uniform(words[w & 3]);
+            w++;
+            return u;
+        };
+        Real p[4];
+        const Real* Lr = c.L(rbuf, rir, 0);
+#pragma unroll
+        for (int j = 0; j < 4; j++) p[j] = Lr[j * c.GGp + g];
+        int nn = categorical(4, p, next_u());
+        draws++;
+        if (nn > 3) { err = 1; nn = 0; }
+        c.tg[(size_t)rir * c.GGp + g] = (int8_t)nn;
+        for (int k = c.n_int - 2; k >= 0; k--) {
+            int s = c.internal[k];
+            int ir = c.irank[s];
+            if (c.missing[s] || c.tg[(size_t)ir * c.GGp + g] >= KB) continue;
+            int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
+            const Real* P = c.ptr + ((size_t)mat_class(c.Z[s], -1) * c.N + s) * 16;
+            const Real* Ls = c.L(c.cur[s], ir, 0);
+            Real q[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) q[i] = P[i * 4 + tp] * Ls[i * c.GGp + g];
+            int n2 = categorical(4, q, next_u());
+            draws++;
+            if (n2 > 3) { err = 1; n2 = 0; }
+            c.tg[(size_t)ir * c.GGp + g] = (int8_t)n2;
+        }
+    }
+    c.local.tg_draws += draws;
+    return err;
+}
+
+// Emission sums per branch and class (getEmission, bpp_c2.cpp:355-390) from a
+// histogram of (child symbol, parent base) pairs.
+template <typename Real>
+__device__ void emission(Ctx<Real>& c) {
+    const int NB = NSYM * 4;
+    for (int i = threadIdx.x; i < c.N * NB; i += blockDim.x) c.cnt[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    // columns are processed warp-synchronously so that equal bins of a warp
+    // are merged before the shared atomic
+    const int nW = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    for (int g0 = w * 32; g0 < c.GG; g0 += nW * 32) {
+        int g = g0 + lane;
+        bool act = g < c.GG;
+        for (int k = 0; k < c.n_nodes - 1; k++) {
+            int s = c.nodes[k];
+            if (c.missing[s]) continue;
+            int key = -1;
+            if (act) {
+                int sym;
+                if (s < c.S) {
+                    int code = c.codes[(size_t)s * c.GGp + g];
+                    sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
+                } else {
+                    int t = c.tg[(size_t)c.irank[s] * c.GGp + g];
+                    sym = t < KB ? t : -1;
+                }
+                if (sym >= 0) {
+                    int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
+                    key = sym * 4 + tp;
+                }
+            }
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            int leader = __ffs(peers) - 1;
+            if (key >= 0 && lane == leader) atomicAdd(&c.cnt[s * NB + key], __popc(peers));
+        }
+    }
+    __syncthreads();
+    // per (node, class): e = sum counts * log P
+    for (int i = threadIdx.x; i < (c.n_nodes - 1) * 3; i += blockDim.x) {
+        int s = c.nodes[i / 3];
+        int z = i % 3;
+        if (c.missing[s]) continue;
+        const double* P = c.ptd + ((size_t)(z == 0 ? P_NULL : (z == 1 ? P_CONS : P_NEUT)) * c.N + s) * 16;
+        double e = 0;
+        for (int b = 0; b < NB; b++) {
+            int n = c.cnt[s * NB + b];
+            if (!n) continue;
+            int sym = b >> 2, tp = b & 3;
+            double v;
+            if (sym < 4) v = log(P[sym * 4 + tp]);
+            else {
+                int msk = ambig_mask(sym - 4);
+                double t = 0;
+                for (int q = 0; q < 4; q++)
+                    if (msk & (1 << q)) t += P[q * 4 + tp];
+                v = log(t);
+            }
+            e += (double)n * v;
+        }
+        c.emis[s * 3 + z] = e;
+    }
+    __syncthreads();
+}
+
+// log_multi2 column zp for child s (bpp.hpp:447-460)
+__device__ __forceinline__ double msg(const double* ltm, const double* beta, int s, int zp) {
+    double t0 = ltm[s * 9 + 0 * 3 + zp] + beta[s * 3 + 0];
+    double t1 = ltm[s * 9 + 1 * 3 + zp] + beta[s * 3 + 1];
+    double t2 = ltm[s * 9 + 2 * 3 + zp] + beta[s * 3 + 2];
+    double mx = t0;
+    if (t1 > mx) mx = t1;
+    if (t2 > mx) mx = t2;
+    double sm = exp(t0 - mx) + exp(t1 - mx) + exp(t2 - mx);
+    return log(sm) + mx;
+}
+
+// Forward filter / backward sample of Z (Update_Z_subtree, bpp_c.cpp:1182-1293).
+template <typename Real>
+__device__ int update_z(Ctx<Real>& c, uint64_t pos) {
+    const double NI = -CUDART_INF;
+    for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
+        int s = c.nodes[i];
+        for (int k = 0; k < 3; k++) c.beta[s * 3 + k] = c.emis[s * 3 + k];
+        if (c.fixZ[s] == 1) c.beta[s * 3 + 2] = NI;
+        c.changed[s] = 0;
+    }
+    __syncthreads();
+    for (int h = 0; h < c.n_hlev; h++) {
+        int a = c.hlev_start[h], b = c.hlev_start[h + 1];
+        for (int i = a * 3 + threadIdx.x; i < b * 3; i += blockDim.x) {
+            int p = c.hlev_nodes[i / 3];
+            int zp = i % 3;
+            double v = c.beta[p * 3 + zp];
+            v += msg(c.ltm, c.beta, c.c2a[p], zp);
+            v += msg(c.ltm, c.beta, c.c2b[p], zp);
+            c.beta[p * 3 + zp] = v;
+        }
+        __syncthreads();
+    }
+    int err = 0;
+    if (threadIdx.x == 0) {
+        const double prior_z[3] = {log(0.5), log(0.5), NI};
+        double lp[3], pr[3];
+        for (int k = 0; k < 3; k++) lp[k] = c.beta[c.root * 3 + k] + prior_z[k];
+        double mx = lp[0];
+        if (lp[1] > mx) mx = lp[1];
+        if (lp[2] > mx) mx = lp[2];
+        for (int k = 0; k < 3; k++) pr[k] = exp(lp[k] - mx);
+        uint32_t wd[4];
+        philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
+        int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
+        if (nn > 2) { err = 1; nn = c.Z[c.root]; }
+        if (nn != c.Z[c.root]) c.changed[c.root] = 1;
+        c.Z[c.root] = (int8_t)nn;
+    }
+    __syncthreads();
+    for (int d = 0; d < c.n_dlev; d++) {
+        int a = c.dlev_start[d], b = c.dlev_start[d + 1];
+        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+            int s = c.dlev_nodes[i];
+            int zp = c.Z[c.par[s]];
+            double lt[3], pr[3];
+            for (int k = 0; k < 3; k++) lt[k] = c.ltm[s * 9 + k * 3 + zp] + c.beta[s * 3 + k];
+            double mx = lt[0];
+            if (lt[1] > mx) mx = lt[1];
+            if (lt[2] > mx) mx = lt[2];
+            for (int k = 0; k < 3; k++) pr[k] = exp(lt[k] - mx);
+            uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
+            uint32_t wd[4];
+            philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
+            int nn = categorical(3, pr, word_to_uniform(wd[w & 3]));
+            if (nn > 2) { err = 1; nn = c.Z[s]; }
+            if (nn != c.Z[s]) c.changed[s] = 1;
+            c.Z[s] = (int8_t)nn;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.local.z_draws += c.n_nodes;
+    return err;
+}
+
+// Flags of proper ancestors of flagged nodes (getUpdateNode, bpp_c.cpp:620-642).
+template <typename Real>
+__device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int mode, int* tmp) {
+    // mode 0: src = changed flags; mode 1: Z == 2 (non-missing); mode 2: Z == 1 (non-missing)
+    for (int i = threadIdx.x; i < c.N; i += blockDim.x) dst[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
+        int s = c.nodes[i];
+        bool f;
+        if (mode == 0) f = src[s];
+        else f = !c.missing[s] && c.Z[s] == (mode == 1 ? 2 : 1);
+        if (!f) continue;
+        int j = c.par[s];
+        while (j != c.N) {
+            dst[j] = 1;
+            j = c.par[j];
+        }
+    }
+    __syncthreads();
+}
+
+// One Metropolis-Hastings update of the accelerated (neut) or conserved rate
+// (sample_rate, bpp_c.cpp:930-1176), M = 1, adaptive factor 0.5.
+template <typename Real>
+__device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
+    ChainScalars* cs = c.cs;
+    const int8_t* unv = neut ? c.unvN : c.unvC;
+    const int cls = neut ? P_NEUT : P_CONS;
+    double prior_a = neut ? dM.nprior_a : dM.cprior_a;
+    double prior_b = neut ? dM.nprior_b : dM.cprior_b;
+    const int m = cs->m;
+    __syncthreads();
+    if (!unv[c.root]) {
+        // no branch in the class: draw from the prior (bpp_c.cpp:940-964)
+        if (threadIdx.x == 0) {
+            double cur = old_rate;
+            if (cs->resZ != 0) {
+                StreamReader rd;
+                rd.init(dM.seed, cs->pos);
+                cur = rd.gamma(prior_a, prior_b);
+                cs->pos = rd.pos;
+                if (neut) {
+                    if (dM.ropt == 1 && cur < dM.nlb) cur = old_rate;
+                    else if (dM.ropt == 2 && cur < c.trd[TR_C * c.T + m]) cur = old_rate;
+                } else {
+                    if (dM.ropt == 1 && cur > dM.cub) cur = old_rate;
+                    else if (dM.ropt == 2 && cur > c.trd[TR_N * c.T + m + 1]) cur = old_rate;
+                }
+            }
+            cs->proposal = cur;
+        }
+        __syncthreads();
+        double cur = cs->proposal;
+        if (cur != old_rate) build_class(c, dist2, cls, cur, true, false);
+        __syncthreads();
+        if (threadIdx.x == 0 && cur != old_rate) { if (neut) cs->acc_n++; else cs->acc_c++; }
+        old_rate = old_rate;  // (no-op, keeps the structure of the reference)
+        __syncthreads();
+        double r = cs->proposal;
+        // adaptive step below
+        if (threadIdx.x == 0) cs->mh_new = r;
+        __syncthreads();
+    } else {
+        if (threadIdx.x == 0) {
+            StreamReader rd;
+            rd.init(dM.seed, cs->pos);
+            double r = rd.uniform();
+            double proposal;
+            int skip = 0;
+            double cur = old_rate;
+            if (neut) {
+                proposal = rd.gamma(__ddiv_rn(cur, cs->prop_n), cs->prop_n);
+                if (dM.ropt == 1 && proposal < dM.nlb) skip = 1;
+                else if (dM.ropt == 2 && proposal < c.trd[TR_C * c.T + m]) skip = 1;
+            } else {
+                double ip = __ddiv_rn(1.0, cs->prop_c);
+                double u = __dadd_rn(__dmul_rn(r, __dsub_rn(cs->prop_c, ip)), ip);
+                proposal = __dmul_rn(cur, u);
+                if (dM.ropt == 1 && proposal > dM.cub) skip = 1;
+                else if (dM.ropt == 2 && proposal > c.trd[TR_N * c.T + m + 1]) skip = 1;
+            }
+            if (!skip && (proposal < 1e-12 || proposal > 1e8)) skip = 1;
+            cs->pos = rd.pos;
+            cs->proposal = proposal;
+            cs->skip = skip;
+            cs->mh_new = r;  // keep r for the decision
+            cs->accept = 0;
+        }
+        __syncthreads();
+        if (!cs->skip) {
+            build_class(c, dist2, P_PROP, cs->proposal, true, true);
+            __syncthreads();
+            double ll_new = prune(c, unv, true, cls);
+            if (threadIdx.x == 0) {
+                double proposal = cs->proposal, cur = old_rate, r = cs->mh_new;
+                double MH;
+                if (neut)
+                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
+                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                     log_gamma_pdf(cur, prior_a, prior_b)),
+                                           log_gamma_pdf(cur, __ddiv_rn(proposal, cs->prop_n), cs->prop_n)),
+                                   log_gamma_pdf(proposal, __ddiv_rn(cur, cs->prop_n), cs->prop_n));
+                else
+                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
+                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                     log_gamma_pdf(cur, prior_a, prior_b)),
+                                           log(cur)),
+                                   log(proposal));
+                if (log(r) < MH) {
+                    cs->accept = 1;
+                    cs->loglik = ll_new;
+                }
+            }
+            __syncthreads();
+            if (cs->accept) {
+                for (int i = threadIdx.x; i < c.n_int; i += blockDim.x) {
+                    int s = c.internal[i];
+                    if (unv[s] && !c.missing[s]) c.cur[s] ^= 1;
+                }
+                copy_class(c, dist2, P_PROP, cls);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double cur = cs->accept ? cs->proposal : old_rate;
+            if (cur != old_rate) { if (neut) cs->acc_n++; else cs->acc_c++; }
+            cs->mh_new = cur;
+        }
+        __syncthreads();
+    }
+    double cur = c.cs->mh_new;
+    // adaptive proposal scale (bpp_c.cpp:1145-1171)
+    if (threadIdx.x == 0 && (m + 1) % dM.adapt_freq == 0) {
+        int blocks = (m + 1) / dM.adapt_freq;
+        double step = fmin(0.5, 1 / sqrt((double)blocks));
+        double scale_adj;
+        if (neut) {
+            double rate = (double)cs->acc_n / dM.adapt_freq;
+            if (rate > 0.44) scale_adj = exp(step);
+            else if (rate < 0.23) scale_adj = exp(-step);
+            else scale_adj = 1;
+            cs->prop_n = __dmul_rn(cs->prop_n, scale_adj);
+            if (cs->prop_n > 1) cs->prop_n = 1;
+            cs->acc_n = 0;
+        } else {
+            double rate = (double)cs->acc_c / dM.adapt_freq;
+            if (rate > 0.44) scale_adj = exp(step);
+            else if (rate < 0.23) scale_adj = exp(-step);
+            else scale_adj = 1;
+            cs->prop_c = pow(cs->prop_c, scale_adj);
+            if (cs->prop_c < 1.0001) cs->prop_c = 1.0001;
+            cs->acc_c = 0;
+        }
+    }
+    __syncthreads();
+    return cur;
+}
+
+// Rank selection: the element that std::sort would put at index T/2 (bpp_c2.cpp:742-755).
+__device__ double median_of(const double* x, int T, double* red) {
+    int target = T / 2;
+    __syncthreads();
+    for (int i = threadIdx.x; i < T; i += blockDim.x) {
+        double v = x[i];
+        int lt = 0, eqb = 0;
+        for (int j = 0; j < T; j++) {
+            double u = x[j];
+            lt += (u < v);
+            eqb += (u == v && j < i);
+        }
+        int r = lt + eqb;
+        if (r == target) red[30] = v;
+    }
+    __syncthreads();
+    double r = red[30];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ uint64_t fnv_step(uint64_t h, uint8_t b) {
+    return (h ^ b) * 0x100000001b3ull;
+}
+
+// Prior of a Z configuration (bpp_c2.cpp:131-163): Beta-Binomial terms + root prior.
+template <typename Real>
+__device__ double prior_config(Ctx<Real>& c, const int8_t* z) {
+    double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int k = 0; k + 1 < c.n_nodes; k++) {
+        int s = c.nodes[k];
+        nZ[z[s]][z[c.par[s]]] += 1;
+    }
+    double pz = lnbeta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]) - lnbeta(dM.ga, dM.gb);
+    for (int k = 0; k + 1 < c.n_nodes; k++) {
+        int s = c.nodes[k];
+        if (c.fixZ[s] == 1) nZ[z[s]][z[c.par[s]]] -= 1;
+    }
+    pz += lnbeta(dM.la + nZ[2][1], dM.lb + nZ[1][1]) - lnbeta(dM.la, dM.lb);
+    if (dM.l2a > 0) pz += lnbeta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]) - lnbeta(dM.l2a, dM.l2b);
+    pz += (z[c.root] == 2) ? -CUDART_INF : log(0.5);
+    return pz;
+}
+
+// Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353).
+template <typename Real>
+__device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, int* n_conf_out) {
+    ChainScalars* cs = c.cs;
+    const int burn = c.burn, mcmc = c.mcmc, T = c.T;
+    int8_t* Zm = c.maxz;  // Max_Z
+    // uncertain nodes
+    for (int s = threadIdx.x; s < c.N; s += blockDim.x) {
+        int cnt = 0;
+        for (int i = burn; i < T; i++) cnt += (c.trz[(size_t)i * c.N + s] == Zm[s]);
+        c.changed[s] = cnt < mcmc;   // reuse: uncertain flag
+    }
+    __syncthreads();
+    // hashes of the uncertain projection
+    for (int i = burn + threadIdx.x; i < T + 1; i += blockDim.x) {
+        const int8_t* z = (i < T) ? c.trz + (size_t)i * c.N : Zm;
+        uint64_t h = 0xcbf29ce484222325ull;
+        for (int s = 0; s < c.N; s++)
+            if (c.changed[s]) h = fnv_step(h, (uint8_t)z[s]);
+        c.hash[i - burn] = h;
+    }
+    __syncthreads();
+    auto same = [&](const int8_t* a, const int8_t* b) {
+        for (int s = 0; s < c.N; s++)
+            if (c.changed[s] && a[s] != b[s]) return false;
+        return true;
+    };
+    // rep[i]: largest index >= i with the same projection; cfg[i] = -2 if it equals Max_Z's
+    for (int i = burn + threadIdx.x; i < T; i += blockDim.x) {
+        const int8_t* zi = c.trz + (size_t)i * c.N;
+        uint64_t hi = c.hash[i - burn];
+        int r = i;
+        for (int j = T - 1; j > i; j--) {
+            if (c.hash[j - burn] == hi && same(c.trz + (size_t)j * c.N, zi)) { r = j; break; }
+        }
+        c.rep[i - burn] = r;
+        c.cfg[i - burn] = (hi == c.hash[T - burn] && same(zi, Zm)) ? -2 : -1;
+    }
+    __syncthreads();
+    // configuration ids in first-occurrence order scanning from the last sample (bpp_c2.cpp:65-116)
+    if (threadIdx.x == 0) {
+        int nconf = 1;
+        c.first[0] = -1;   // Max_Z
+        c.head[0] = -1;
+        for (int i = T - 1; i >= burn; i--) {
+            int k = i - burn;
+            int j;
+            if (c.cfg[k] == -2) j = 0;
+            else if (c.rep[k] == i) { j = nconf++; c.first[j] = i; c.head[j] = -1; }
+            else j = c.cfg[c.rep[k] - burn];
+            c.cfg[k] = j;
+        }
+        // members of each config in decreasing sample index: build lists
+        for (int j = 0; j < nconf; j++) c.head[j] = -1;
+        for (int i = burn; i < T; i++) {     // prepend in increasing order -> list in decreasing order
+            int k = i - burn;
+            int j = c.cfg[k];
+            c.nxt[k] = c.head[j];
+            c.head[j] = k;
+        }
+        cs->n_conf = nconf;
+    }
+    __syncthreads();
+    const int nconf = cs->n_conf;
+    *n_conf_out = nconf;
+    // per-config sums in the reference's order (bpp_c2.cpp:105-113)
+    double* CNT = c.cstat;
+    double* VC = CNT + (mcmc + 2);
+    double* MC = VC + (mcmc + 2);
+    double* VN = MC + (mcmc + 2);
+    double* MN = VN + (mcmc + 2);
+    double* CV = MN + (mcmc + 2);
+    double* SF = CV + (mcmc + 2);
+    double* LD = SF + (mcmc + 2);
+    double* PZ = LD + (mcmc + 2);
+    const double* trN = c.trd + TR_N * T;
+    const double* trC = c.trd + TR_C * T;
+    const double* trF = c.trd + TR_FULL * T;
+    for (int j = threadIdx.x; j < nconf; j += blockDim.x) {
+        double n = 0, vc = 0, mc = 0, vn = 0, mn = 0, cv = 0, sf = 0;
+        for (int k = c.head[j]; k >= 0; k = c.nxt[k]) {
+            int i = k + burn;
+            n += 1;
+            vc = __dadd_rn(vc, __dmul_rn(trC[i], trC[i]));
+            mc = __dadd_rn(mc, trC[i]);
+            if (resZ != 0) {
+                vn = __dadd_rn(vn, __dmul_rn(trN[i], trN[i]));
+                mn = __dadd_rn(mn, trN[i]);
+                cv = __dadd_rn(cv, __dmul_rn(trC[i], trN[i]));
+            }
+            sf = __dadd_rn(sf, __ddiv_rn(trF[i], (double)mcmc));
+        }
+        CNT[j] = n; VC[j] = vc; MC[j] = mc; VN[j] = vn; MN[j] = mn; CV[j] = cv; SF[j] = sf;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nconf; j += blockDim.x) {
+        double w = CNT[j] / mcmc;
+        LD[j] = 0;
+        if (w < 0.02) continue;
+        const int8_t* z = (j == 0) ? Zm : c.trz + (size_t)c.first[j] * c.N;
+        double pz = prior_config(c, z);
+        PZ[j] = pz;
+        SF[j] = __dadd_rn(SF[j], __ddiv_rn(__dmul_rn(CNT[j], pz), (double)mcmc));
+        double nj = CNT[j];
+        double ld;
+        if (resZ == 0) {
+            ld = __dsub_rn(log(__dsub_rn(VC[j], __ddiv_rn(__dmul_rn(MC[j], MC[j]), nj))), log(nj));
+        } else {
+            double vc = __dsub_rn(VC[j], __ddiv_rn(__dmul_rn(MC[j], MC[j]), nj));
+            double vn = __dsub_rn(VN[j], __ddiv_rn(__dmul_rn(MN[j], MN[j]), nj));
+            double cov = __dsub_rn(CV[j], __ddiv_rn(__dmul_rn(MN[j], MC[j]), nj));
+            ld = __dsub_rn(log(__dsub_rn(__dmul_rn(vc, vn), __dmul_rn(cov, cov))), __dmul_rn(2.0, log(nj)));
+        }
+        LD[j] = ld;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double VB = 0;
+        int eff = 0;
+        for (int j = 0; j < nconf; j++) {
+            double w = CNT[j] / mcmc;
+            if (w < 0.02) continue;
+            if (isnan(LD[j])) continue;
+            eff += (int)CNT[j];
+            VB = __dsub_rn(VB, __dmul_rn(w, log(CNT[j])));
+            VB = __dadd_rn(VB, SF[j]);
+            VB = __dadd_rn(VB, __ddiv_rn(__dmul_rn(__dmul_rn(0.5, LD[j]), CNT[j]), (double)mcmc));
+        }
+        cs->eff = eff;
+        cs->vb = VB;
+    }
+    __syncthreads();
+    double VB = cs->vb;
+    if (cs->eff == 0) {
+        // no dominant configuration: q(r, Z) = q(r) q(Z) at the mean rates (bpp_c2.cpp:199-316)
+        double varn = 0, varc = 0, cov = 0, meann = 0, meanc = 0;
+        for (int j = 0; j < nconf; j++) {
+            varc = __dadd_rn(varc, VC[j]);
+            meanc = __dadd_rn(meanc, MC[j]);
+            if (resZ != 0) { meann = __dadd_rn(meann, MN[j]); varn = __dadd_rn(varn, VN[j]); cov = __dadd_rn(cov, CV[j]); }
+        }
+        double rn = meann / mcmc, rc = meanc / mcmc;
+        build_class(c, dist2, P_CONS, rc, true, true);
+        if (resZ != 0) build_class(c, dist2, P_NEUT, rn, true, true);
+        __syncthreads();
+        for (int j = 0; j < nconf; j++) {
+            const int8_t* z = (j == 0) ? Zm : c.trz + (size_t)c.first[j] * c.N;
+            for (int s = threadIdx.x; s < c.N; s += blockDim.x) {
+                c.Z[s] = z[s];
+                c.unv[s] = 1;
+                c.cur[s] = 0;
+            }
+            __syncthreads();
+            double pz = prior_config(c, z);
+            double ll = prune(c, c.unv, false, -1);
+            if (threadIdx.x == 0) SF[j] = __dadd_rn(ll, pz);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            double mx = SF[0];
+            for (int j = 1; j < nconf; j++) if (SF[j] > mx) mx = SF[j];
+            double v;
+            if (mx == -CUDART_INF) v = -CUDART_INF;
+            else {
+                double sm = 0;
+                for (int j = 0; j < nconf; j++) sm += exp(SF[j] - mx);
+                v = log(sm) + mx;
+            }
+            v += log_gamma_pdf(rc, dM.cprior_a, dM.cprior_b);
+            if (resZ != 0) v += log_gamma_pdf(rn, dM.nprior_a, dM.nprior_b);
+            double logdet;
+            if (resZ == 0) {
+                varc -= meanc * meanc / mcmc;
+                logdet = log(varc) - log((double)mcmc);
+                v += 0.5 * logdet + 0.5 * log(2 * CUDART_PI);
+            } else {
+                varn -= meann * meann / mcmc;
+                varc -= meanc * meanc / mcmc;
+                cov -= meann * meanc / mcmc;
+                logdet = log(varc * varn - cov * cov) - 2 * log((double)mcmc);
+                v += 0.5 * logdet + log(2 * CUDART_PI);
+            }
+            cs->vb = v;
+        }
+        __syncthreads();
+        VB = cs->vb;
+    } else {
+        double f = (double)mcmc / cs->eff;
+        if (resZ != 0) VB = VB * f + log((double)mcmc) + log(2 * CUDART_PI) + 1;
+        else VB = VB * f + log((double)mcmc) + 0.5 * (log(2 * CUDART_PI) + 1);
+    }
+    __syncthreads();
+    return VB;
+}
+
+// ---------------------------------------------------------------------------
+// The chain kernel
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ChainScalars cs_;
+    __shared__ int tmp_;
+    __shared__ int elem_;
+    __shared__ double dist2_[MAX_NODES];
+    const int N = dM.N, S = dM.S;
+    const int BT = blockDim.x;
+    SmemLayout<Real> L = SmemLayout<Real>::make(N, BT);
+    TopoLayout TL = TopoLayout::make(N);
+    Ctx<Real> c;
+    c.S = S;
+    c.N = N;
+    c.ptd = (double*)(smem + L.ptd);
+    c.ptr = (sizeof(Real) == 8) ? (Real*)c.ptd : (Real*)(smem + L.ptr_);
+    c.ltm = (double*)(smem + L.ltm);
+    c.emis = (double*)(smem + L.emis);
+    c.beta = (double*)(smem + L.beta);
+    c.cnt = (int*)(smem + L.cnt);
+    c.red = (double*)(smem + L.red);
+    int16_t* t16 = (int16_t*)(smem + L.i16);
+    c.nodes = t16 + TL.nodes; c.internal = t16 + TL.internal; c.c2a = t16 + TL.c2a; c.c2b = t16 + TL.c2b;
+    c.par = t16 + TL.par; c.irank = t16 + TL.irank; c.pos = t16 + TL.pos; c.missing = t16 + TL.missing;
+    c.upc = t16 + TL.upc; c.upcc = t16 + TL.upcc; c.hlev_start = t16 + TL.hlev_start;
+    c.hlev_nodes = t16 + TL.hlev_nodes; c.dlev_start = t16 + TL.dlev_start; c.dlev_nodes = t16 + TL.dlev_nodes;
+    int8_t* t8 = (int8_t*)(smem + L.i8);
+    c.Z = t8; c.fixZ = t8 + N; c.changed = t8 + 2 * N; c.unv = t8 + 3 * N; c.unvN = t8 + 4 * N;
+    c.unvC = t8 + 5 * N; c.cur = t8 + 6 * N; c.maxz = t8 + 7 * N;
+    c.cs = &cs_;
+    c.burn = dM.burnin;
+    c.mcmc = dM.mcmc;
+    c.T = dM.burnin + dM.mcmc;
+    const int T = c.T;
+    char* ws = P.ws + (size_t)blockIdx.x * P.ws_stride;
+    WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, T, dM.mcmc, N, sizeof(Real));
+    c.lam = (Real*)(ws + W.lam);
+    c.scl = (int32_t*)(ws + W.scale);
+    c.tg = (int8_t*)(ws + W.tg);
+    c.trz = (int8_t*)(ws + W.trz);
+    c.trd = (double*)(ws + W.trd);
+    c.hash = (uint64_t*)(ws + W.hash);
+    c.rep = (int32_t*)(ws + W.rep);
+    c.cfg = (int32_t*)(ws + W.cfg);
+    c.nxt = (int32_t*)(ws + W.nxt);
+    c.head = (int32_t*)(ws + W.head);
+    c.first = (int32_t*)(ws + W.first);
+    c.cstat = (double*)(ws + W.cstat);
+    const int TI = dM.trace_iters < T ? dM.trace_iters : T;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) elem_ = atomicAdd(P.next_elem, 1);
+        __syncthreads();
+        const int e = elem_;
+        if (e >= P.n_elem) break;
+        long long t_start = clock64();
+        const ElemHeader& H = P.hdr[e];
+        DevResult* R = P.results + e;
+        if (H.filtered) {
+            if (threadIdx.x == 0) R->status = 1;
+            continue;
+        }
+        c.local = DevCounters{0, 0, 0, 0, 0, 0, 0};
+        c.GG = H.GG; c.GGp = H.GGp; c.root = H.root; c.n_nodes = H.n_nodes; c.n_int = H.n_int;
+        c.n_hlev = H.n_hlev; c.n_dlev = H.n_dlev; c.tg_draws = H.tg_draws;
+        c.codes = P.blob + H.codes_off;
+        c.prefix = (const int32_t*)(P.blob + H.prefix_off);
+        const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
+        for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
+        {
+            const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
+            for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = d2[i];
+        }
+        {
+            const int8_t* tg0 = (const int8_t*)(P.blob + H.tg_off);
+            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = tg0[i];
+        }
+        if (threadIdx.x == 0) {
+            cs_.pos = 0;
+            cs_.acc_n = 0;
+            cs_.acc_c = 0;
+            cs_.status = 0;
+        }
+        for (int i = threadIdx.x; i < N; i += BT) c.maxz[i] = 0;
+        __syncthreads();
+        const int resZ_of[3] = {0, 2, 1};
+        for (int mi = 0; mi < 3; mi++) {
+            const int resZ = resZ_of[mi];
+            // ---------------- initMCMC (bpp_c.cpp:131-343) ----------------
+            if (threadIdx.x == 0) {
+                cs_.resZ = resZ;
+                cs_.mi = mi;
+                cs_.prop_c = 1.2;
+                cs_.prop_n = (double)1 / c.GG * 10;
+                cs_.maxll = -CUDART_INF;
+                cs_.max_m = 0;
+                c.trd[TR_N * T + 0] = dM.init_n;
+                c.trd[TR_C * T + 0] = dM.init_c;
+                c.trd[TR_L * T + 0] = dM.init_l;
+                c.trd[TR_L2 * T + 0] = (dM.l2a == 0) ? 0.0 : dM.init_l2;
+                c.trd[TR_G * T + 0] = dM.init_g;
+                cs_.rate_n = dM.init_n;
+                cs_.rate_c = dM.init_c;
+            }
+            for (int i = threadIdx.x; i < N; i += BT) { c.Z[i] = -1; c.fixZ[i] = -1; c.cur[i] = 0; }
+            __syncthreads();
+            for (int i = threadIdx.x; i < c.n_nodes; i += BT) {
+                int s = c.nodes[i];
+                c.Z[s] = (s == c.root) ? 0 : 1;
+                if (c.upc[s]) c.fixZ[s] = 1;
+                if (s == c.root) c.fixZ[s] = 1;
+                if (resZ == 2 && c.upcc[s]) c.fixZ[s] = 1;
+                if (resZ == 0 && s != c.root) c.fixZ[s] = 1;
+            }
+            __syncthreads();
+            build_class(c, dist2_, P_NULL, 1.0, false, false);
+            build_class(c, dist2_, P_NEUT, dM.init_n, true, false);
+            build_class(c, dist2_, P_CONS, dM.init_c, true, false);
+            __syncthreads();
+            build_ltm(c, c.trd[TR_G * T], c.trd[TR_L * T], c.trd[TR_L2 * T], true);
+            for (int i = threadIdx.x; i < N; i += BT) {
+                c.emis[i * 3 + 0] = 0; c.emis[i * 3 + 1] = 0; c.emis[i * 3 + 2] = 0;
+                if (c.missing[i]) { c.emis[i * 3 + 1] = log(dM.cons_to_mis); }
+                c.unv[i] = 1;
+            }
+            __syncthreads();
+            // ---------------- Gibbs (bpp_c.cpp:346-519) ----------------
+            double ll0 = prune(c, c.unv, false, -1);
+            if (threadIdx.x == 0) cs_.loglik = ll0;
+            __syncthreads();
+            for (int m = 0; m < T; m++) {
+                // MonitorChain (bpp_c.cpp:741-834)
+                for (int i = threadIdx.x; i < N; i += BT) c.trz[(size_t)m * N + i] = c.Z[i];
+                if (threadIdx.x == 0) {
+                    cs_.m = m;
+                    double ll = cs_.loglik;
+                    double full = ll + 0.0;
+                    full += log_gamma_pdf(c.trd[TR_C * T + m], dM.cprior_a, dM.cprior_b);
+                    if (resZ != 0) full += log_gamma_pdf(c.trd[TR_N * T + m], dM.nprior_a, dM.nprior_b);
+                    c.trd[TR_LL * T + m] = ll;
+                    c.trd[TR_FULL * T + m] = full;
+                    tmp_ = (m >= c.burn && full > cs_.maxll) ? 1 : 0;
+                    if (tmp_) { cs_.maxll = full; cs_.max_m = m; }
+                }
+                __syncthreads();
+                if (tmp_)
+                    for (int i = threadIdx.x; i < N; i += BT) c.maxz[i] = c.Z[i];
+                if (m == T - 1) break;
+                // internal bases
+                uint64_t pos = cs_.pos;
+                int err = sample_tg(c, pos);
+                __syncthreads();
+                if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.tg_draws;
+                if (err) atomicOr(&cs_.status, 1);
+                // latent states
+                emission(c);
+                pos = cs_.pos;
+                int zerr = update_z(c, pos);
+                if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.n_nodes;
+                if (zerr) atomicOr(&cs_.status, 1);
+                __syncthreads();
+                // partial re-prune of ancestors of changed branches (bpp_c.cpp:419-431)
+                mark_ancestors(c, c.changed, c.unv, 0, &tmp_);
+                int any_unv = block_or(c.unv[c.root], &tmp_);
+                if (any_unv) {
+                    double ll = prune(c, c.unv, false, -1);
+                    if (threadIdx.x == 0) cs_.loglik = ll;
+                }
+                __syncthreads();
+                // rates (bpp_c.cpp:434-452)
+                mark_ancestors(c, nullptr, c.unvN, 1, &tmp_);
+                mark_ancestors(c, nullptr, c.unvC, 2, &tmp_);
+                double rn = sample_rate(c, dist2_, true, c.trd[TR_N * T + m], &tmp_);
+                if (threadIdx.x == 0) c.trd[TR_N * T + m + 1] = rn;
+                __syncthreads();
+                double rc = sample_rate(c, dist2_, false, c.trd[TR_C * T + m], &tmp_);
+                if (threadIdx.x == 0) c.trd[TR_C * T + m + 1] = rc;
+                // transitions of Z (sample_transition, bpp_c.cpp:522-613)
+                if (threadIdx.x == 0) {
+                    double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                    for (int k = 0; k + 1 < c.n_nodes; k++) {
+                        int s = c.nodes[k];
+                        nZ[c.Z[s]][c.Z[c.par[s]]] += 1;
+                    }
+                    StreamReader rd;
+                    rd.init(dM.seed, cs_.pos);
+                    double gr = rd.beta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]);
+                    for (int k = 0; k + 1 < c.n_nodes; k++) {
+                        int s = c.nodes[k];
+                        if (c.fixZ[s] == 1) nZ[c.Z[s]][c.Z[c.par[s]]] -= 1;
+                    }
+                    double lr = rd.beta(dM.la + nZ[2][1], dM.lb + nZ[1][1]);
+                    double lr2 = (dM.l2a == 0) ? 0.0 : rd.beta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]);
+                    cs_.pos = rd.pos;
+                    c.trd[TR_G * T + m + 1] = gr;
+                    c.trd[TR_L * T + m + 1] = lr;
+                    c.trd[TR_L2 * T + m + 1] = lr2;
+                }
+                __syncthreads();
+                build_ltm(c, c.trd[TR_G * T + m + 1], c.trd[TR_L * T + m + 1], c.trd[TR_L2 * T + m + 1], false);
+                __syncthreads();
+                if (threadIdx.x == 0) c.local.iters++;
+            }
+            __syncthreads();
+            DevModelResult& MR = R->model[mi];
+            if (threadIdx.x == 0) MR.max_loglik = cs_.maxll;
+            // traces of the first TI iterations
+            if (TI > 0 && P.tr_d) {
+                double* td = P.tr_d + ((size_t)e * 3 + mi) * 6 * TI;
+                const int rows[6] = {TR_LL, TR_N, TR_C, TR_G, TR_L, TR_L2};
+                for (int i = threadIdx.x; i < 6 * TI; i += BT) td[i] = c.trd[rows[i / TI] * T + (i % TI)];
+                int8_t* tz = P.tr_z + ((size_t)e * 3 + mi) * TI * N;
+                for (int i = threadIdx.x; i < TI * N; i += BT) tz[i] = c.trz[i];
+            }
+            // ---------------- Eval2 ----------------
+            int nconf = 0;
+            double vb = eval2(c, dist2_, resZ, &tmp_, &nconf);
+            // ---------------- Output_init (bpp_c2.cpp:739-785) ----------------
+            double med[5];
+            const int mrow[5] = {TR_N, TR_C, TR_G, TR_L, TR_L2};
+            for (int q = 0; q < 5; q++) med[q] = median_of(c.trd + mrow[q] * T, T, c.red);
+            if (threadIdx.x == 0) {
+                MR.loglik = vb;
+                for (int q = 0; q < 5; q++) MR.rates[q] = med[q];
+                MR.failure = isnan(vb) ? 1 : 0;
+                MR.n_configs = nconf;
+                if (isnan(vb)) cs_.status |= 2;
+            }
+            int32_t* mz = P.max_z + ((size_t)e * 3 + mi) * N;
+            for (int s = threadIdx.x; s < N; s += BT) mz[s] = c.maxz[s];
+            double* pz = P.post_z + ((size_t)e * 3 + mi) * N * 4;
+            for (int s = threadIdx.x; s < N; s += BT) {
+                int cnt[4] = {0, 0, 0, 0};
+                for (int i = c.burn; i < T; i++) {
+                    int z = c.trz[(size_t)i * N + s];
+                    if (z >= -1 && z <= 2) cnt[z + 1]++;
+                }
+                if (c.missing[s]) cnt[0] = c.mcmc;
+                for (int k = 0; k < 4; k++) pz[s * 4 + k] = (double)cnt[k] / c.mcmc;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            R->status = (cs_.status & 1) ? 3 : ((cs_.status & 2) ? 2 : 0);
+            R->device_ms = (double)(clock64() - t_start);
+        }
+        // counters
+        if (P.counters) {
+            atomicAdd(&P.counters->edge_internal, c.local.edge_internal);
+            atomicAdd(&P.counters->edge_leaf, c.local.edge_leaf);
+            atomicAdd(&P.counters->tg_draws, c.local.tg_draws);
+            if (threadIdx.x == 0) {
+                atomicAdd(&P.counters->col_ll, c.local.col_ll);
+                atomicAdd(&P.counters->z_draws, c.local.z_draws);
+                atomicAdd(&P.counters->iters, c.local.iters);
+            }
+            atomicAdd(&P.counters->pmat, c.local.pmat);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel-level entry points for parity tests
+// ---------------------------------------------------------------------------
+__global__ void pmatrix_kernel(int n, const double* d, const double* r, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) build_pt(d[i], r[i], true, out + (size_t)i * 16);
+}
+
+__global__ void stream_kernel(uint32_t seed, uint64_t w0, int n, uint32_t* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        uint64_t w = w0 + i;
+        uint32_t wd[4];
+        philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, seed, 0u, wd);
+        out[i] = wd[w & 3];
+    }
+}
+
+// Per-column log-likelihood of one element for fixed Z and rates.
+template <typename Real>
+__global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, double n_rate, double* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ChainScalars cs_;
+    __shared__ double dist2_[MAX_NODES];
+    const int N = dM.N, S = dM.S;
+    const int BT = blockDim.x;
+    SmemLayout<Real> L = SmemLayout<Real>::make(N, BT);
+    TopoLayout TL = TopoLayout::make(N);
+    Ctx<Real> c;
+    c.S = S; c.N = N;
+    c.ptd = (double*)(smem + L.ptd);
+    c.ptr = (sizeof(Real) == 8) ? (Real*)c.ptd : (Real*)(smem + L.ptr_);
+    c.red = (double*)(smem + L.red);
+    int16_t* t16 = (int16_t*)(smem + L.i16);
+    c.nodes = t16 + TL.nodes; c.internal = t16 + TL.internal; c.c2a = t16 + TL.c2a; c.c2b = t16 + TL.c2b;
+    c.par = t16 + TL.par; c.irank = t16 + TL.irank; c.pos = t16 + TL.pos; c.missing = t16 + TL.missing;
+    int8_t* t8 = (int8_t*)(smem + L.i8);
+    c.Z = t8; c.unv = t8 + 3 * N; c.cur = t8 + 6 * N;
+    c.cs = &cs_;
+    const ElemHeader& H = P.hdr[0];
+    c.GG = H.GG; c.GGp = H.GGp; c.root = H.root; c.n_nodes = H.n_nodes; c.n_int = H.n_int;
+    c.codes = P.blob + H.codes_off;
+    char* ws = P.ws;
+    WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, 1, 1, N, sizeof(Real));
+    c.lam = (Real*)(ws + W.lam);
+    c.scl = (int32_t*)(ws + W.scale);
+    c.tg = (int8_t*)(ws + W.tg);
+    c.local = DevCounters{0, 0, 0, 0, 0, 0, 0};
+    const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
+    for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
+    const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
+    for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = d2[i];
+    const int8_t* tg0 = (const int8_t*)(P.blob + H.tg_off);
+    for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = tg0[i];
+    for (int i = threadIdx.x; i < N; i += BT) { c.Z[i] = (int8_t)z[i]; c.unv[i] = 1; c.cur[i] = 0; }
+    __syncthreads();
+    build_class(c, dist2_, P_NULL, 1.0, false, false);
+    build_class(c, dist2_, P_NEUT, n_rate, true, false);
+    build_class(c, dist2_, P_CONS, c_rate, true, false);
+    __syncthreads();
+    prune(c, c.unv, false, -1);
+    __syncthreads();
+    int rir = c.irank[c.root];
+    for (int g = threadIdx.x; g < c.GG; g += BT) {
+        Real* Lr = c.L(0, rir, 0);
+        double t = (double)Lr[g] + (double)Lr[g + c.GGp] + (double)Lr[g + 2 * c.GGp] + (double)Lr[g + 3 * c.GGp];
+        out[g] = log(t) + (double)c.SC(0, rir)[g] * 0.6931471805599453;
+    }
+}
+
+// FMA throughput probe: independent FMA chains per thread.
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+    T x0 = threadIdx.x * (T)1e-7, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3, x4 = x0 + (T)4, x5 = x0 + (T)5,
+      x6 = x0 + (T)6, x7 = x0 + (T)7;
+    for (int i = 0; i < iters; i++) {
+        x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+        x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+    T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == (T)-12345.0) out[blockIdx.x] = s;
+}
+
+// ---------------------------------------------------------------------------
+// Host-callable launchers (C++ linkage, used by pacc_host.cpp)
+// ---------------------------------------------------------------------------
+cudaError_t set_model(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
+
+size_t smem_bytes(int N, int BT, int prec) {
+    return prec == 0 ? SmemLayout<double>::make(N, BT).total : SmemLayout<float>::make(N, BT).total;
+}
+
+size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec) {
+    return WsLayout::make(n_int, GGp, T, mcmc, N, prec == 0 ? 8 : 4).total;
+}
+
+size_t topo_bytes(int N) { return (size_t)((TopoLayout::make(N).total * 2 + 15) & ~15) + (size_t)N * 8; }
+
+cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st) {
+    if (prec == 0) {
+        cudaFuncSetAttribute(chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        chain_kernel<double><<<grid, BT, smem, st>>>(p);
+    } else {
+        cudaFuncSetAttribute(chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        chain_kernel<float><<<grid, BT, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate, double n_rate, double* out, int BT,
+                          size_t smem, int prec, cudaStream_t st) {
+    if (prec == 0) {
+        cudaFuncSetAttribute(loglik_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        loglik_kernel<double><<<1, BT, smem, st>>>(p, z, c_rate, n_rate, out);
+    } else {
+        cudaFuncSetAttribute(loglik_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        loglik_kernel<float><<<1, BT, smem, st>>>(p, z, c_rate, n_rate, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out, cudaStream_t st) {
+    pmatrix_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, d, r, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st) {
+    stream_kernel<<<(n + 255) / 256, 256, 0, st>>>(seed, w0, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st) {
+    if (prec == 0) fma_probe_kernel<double><<<grid, BT, 0, st>>>((double*)out, iters, 0.9999999, 1e-7);
+    else fma_probe_kernel<float><<<grid, BT, 0, st>>>((float*)out, iters, 0.9999f, 1e-4f);
+    return cudaGetLastError();
+}
+
+}  // namespace pacc

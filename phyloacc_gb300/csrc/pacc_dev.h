@@ -1,0 +1,128 @@
+// pacc_dev.h — data shared between the host preprocessing and the chain kernel.
+#pragma once
+#include <stdint.h>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#endif
+
+namespace pacc {
+
+static const int KB = 4;          // bases (num_base with INDEL == 0)
+static const int NSYM = 10;       // emission symbols: 0..3 base, 4..9 ambiguity codes r y k m s w
+static const int MAX_NODES = 511; // N = 2S-1 with S <= 256
+
+// Leaf column codes (one byte per taxon and column).
+enum LeafCode : uint8_t {
+    CODE_A = 0, CODE_C = 1, CODE_G = 2, CODE_T = 3,
+    CODE_GAP = 4,   // GAPCHAR: Tg = 4 (bpp_c.hpp:259)
+    CODE_OTHER = 5, // n and anything else: Tg = 5 (bpp_c.hpp:260)
+    CODE_R = 6, CODE_Y = 7, CODE_K = 8, CODE_M = 9, CODE_S = 10, CODE_W = 11  // Tg = -1
+};
+
+// Two-hot masks of the ambiguity codes r y k m s w (bpp_c.hpp:230-248):
+// r = a|g (0x5), y = c|t (0xA), k = g|t (0xC), m = a|c (0x3), s = c|g (0x6), w = a|t (0x9).
+__host__ __device__ inline int ambig_mask(int k) { return (0x963CA5 >> (4 * k)) & 0xF; }
+
+// Model constants (one per context), copied to __constant__ memory.
+struct DevModel {
+    int S, N;
+    double lam[4];
+    double evec[16];   // eigenvec = V^T, row-major [i][b]
+    double einv[16];   // eigeninv = (V^T)^-1, row-major [a][i]
+    double pi[4];
+    double log_pi[4];
+    // options (main.cpp:36-90)
+    int burnin, mcmc, adapt_freq, ropt;
+    uint32_t seed;
+    double init_c, init_n, cprior_a, cprior_b, nprior_a, nprior_b, cub, nlb;
+    double init_l, init_l2, init_g;
+    double la, lb, ga, gb, l2a, l2b;
+    double cons_to_mis;
+    int trace_iters;
+};
+
+// Per-element topology after missing-taxon pruning (bpp_c.hpp:331-428),
+// node ids are PhyloAcc's.  Offsets are in int16 units from the start of
+// the element's topology block; see host code for the layout.
+struct ElemHeader {
+    int32_t GG;            // columns after trimming
+    int32_t GGp;           // GG rounded up to a multiple of 32
+    int32_t root;
+    int32_t n_nodes;       // |nodes| (postorder of the pruned tree)
+    int32_t n_int;         // |internal_nodes|
+    int32_t n_hlev;        // bottom-up levels (by height) of non-leaf nodes
+    int32_t n_dlev;        // top-down levels (by depth) below the root
+    int32_t tg_draws;      // stream words used by one internal-base pass (prefix[GG])
+    int64_t codes_off;     // byte offset of codes [S][GGp]
+    int64_t tg_off;        // byte offset of initial internal Tg [n_int][GGp] (int8)
+    int64_t prefix_off;    // byte offset of draw prefix [GG+1] (int32)
+    int64_t topo_off;      // byte offset of the int16 topology block
+    int64_t element_no;
+    int32_t filtered;
+    int32_t pad;
+};
+
+// Layout of the int16 topology block (each array length N unless noted).
+struct TopoLayout {
+    int nodes, internal, c2a, c2b, par, irank, pos, missing, upc, upcc, hlev_start, hlev_nodes, dlev_start,
+        dlev_nodes, total;
+    __host__ __device__ static TopoLayout make(int N) {
+        TopoLayout t;
+        int o = 0;
+        t.nodes = o; o += N;
+        t.internal = o; o += N;
+        t.c2a = o; o += N;
+        t.c2b = o; o += N;
+        t.par = o; o += N;
+        t.irank = o; o += N;
+        t.pos = o; o += N;
+        t.missing = o; o += N;
+        t.upc = o; o += N;
+        t.upcc = o; o += N;
+        t.hlev_start = o; o += N + 1;
+        t.hlev_nodes = o; o += N;
+        t.dlev_start = o; o += N + 1;
+        t.dlev_nodes = o; o += N;
+        t.total = o;
+        return t;
+    }
+};
+
+// Per-model result written by the kernel.
+struct DevModelResult {
+    double loglik, max_loglik, rates[5];
+    int32_t failure, n_configs;
+};
+
+struct DevResult {
+    DevModelResult model[3];
+    int32_t status;
+    int32_t pad;
+    double device_ms;
+};
+
+// Work counters accumulated by the kernel (atomicAdd per CTA per element).
+struct DevCounters {
+    unsigned long long edge_internal, edge_leaf, col_ll, tg_draws, z_draws, pmat, iters;
+};
+
+// Parameters of one chain-kernel launch.
+struct ChainParams {
+    const ElemHeader* hdr;     // [n_elem]
+    const uint8_t* blob;       // element data (codes, initial Tg, draw prefix, topology)
+    int n_elem;
+    int* next_elem;            // work counter (atomic)
+    DevResult* results;        // [n_elem]
+    int32_t* max_z;            // [n_elem][3][N]
+    double* post_z;            // [n_elem][3][N][4]
+    double* tr_d;              // [n_elem][3][6][TI] (loglik, n, c, g, l, l2) or null
+    int8_t* tr_z;              // [n_elem][3][TI][N] or null
+    char* ws;                  // per-CTA workspace
+    size_t ws_stride;
+    int n_int_max, GGp_max;
+    DevCounters* counters;
+};
+
+}  // namespace pacc

@@ -1,0 +1,837 @@
+// pacc_host.cpp — host side of the C ABI declared in include/pacc.h.
+//
+// Owns the context (model constants, device buffers), the per-element
+// preprocessing that PhyloAcc-ST does in the BPP_C constructor
+// (src/PhyloAcc-ST/bpp_c.hpp:143-476: column encoding, optional column
+// trimming, missing taxa, pruning of the outgroup path, node orders), the
+// packing of elements into one device blob, the kernel launches and the
+// collection of results.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <set>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/pacc.h"
+#include "eigen4.h"
+#include "pacc_dev.h"
+
+namespace pacc {
+
+cudaError_t set_model(const DevModel& m);
+size_t smem_bytes(int N, int BT, int prec);
+size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec);
+size_t topo_bytes(int N);
+cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st);
+cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate, double n_rate, double* out, int BT,
+                          size_t smem, int prec, cudaStream_t st);
+cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out, cudaStream_t st);
+cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st);
+cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// model (BPP, bpp.hpp:173-404)
+// ---------------------------------------------------------------------------
+struct HostModel {
+    int S = 0, N = 0;
+    std::vector<int> ch0, ch1, parent;
+    std::vector<double> dist;
+    std::vector<int> conserve, outgroup;
+    std::vector<char> upper, upper_conserve;  // [N]
+    DevModel dm;
+};
+
+// One preprocessed element.
+struct HostElem {
+    int64_t no = 0;
+    int filtered = 0;
+    int GG = 0, GGp = 0, root = 0, n_nodes = 0, n_int = 0, n_hlev = 0, n_dlev = 0, tg_draws = 0;
+    std::vector<uint8_t> codes;    // [S][GGp]
+    std::vector<int8_t> tg0;       // [n_int][GGp]
+    std::vector<int32_t> prefix;   // [GG+1]
+    std::vector<int16_t> topo;     // TopoLayout
+    std::vector<double> dist2;     // [N]
+    std::vector<int8_t> tg_full;   // [GG][N] (debug encode only)
+    std::vector<uint8_t> missing;  // [N]
+};
+
+static inline uint8_t encode_char(uint8_t ch, char gapchar) {
+    // bpp_c.hpp:220-261
+    switch ((char)ch) {
+        case 'a': return CODE_A;
+        case 'c': return CODE_C;
+        case 'g': return CODE_G;
+        case 't': return CODE_T;
+        case 'r': return CODE_R;
+        case 'y': return CODE_Y;
+        case 'k': return CODE_K;
+        case 'm': return CODE_M;
+        case 's': return CODE_S;
+        case 'w': return CODE_W;
+        default: return ((char)ch == gapchar) ? CODE_GAP : CODE_OTHER;
+    }
+}
+
+static inline int code_tg(uint8_t c) { return c < 4 ? c : (c == CODE_GAP ? 4 : (c == CODE_OTHER ? 5 : -1)); }
+
+// Per-element preprocessing (BPP_C ctor, bpp_c.hpp:143-476).  Returns false
+// only on invalid input; filtered elements return true with E.filtered = 1.
+static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* bases, int len, HostElem& E,
+                       bool keep_full) {
+    const int S = M.S, N = M.N;
+    E.GG = len;
+    if (len < o.min_len) { E.filtered = 1; return true; }
+    // encode (species rows, tree leaf order)
+    std::vector<uint8_t> code((size_t)S * len);
+    const char gapchar = (char)o.gapchar;
+    for (int s = 0; s < S; s++)
+        for (int g = 0; g < len; g++) code[(size_t)s * len + g] = encode_char(bases[(size_t)s * len + g], gapchar);
+    // optional column trimming (bpp_c.hpp:267-301)
+    std::vector<int> cols;
+    cols.reserve(len);
+    if (o.trim_gap_percent < 1) {
+        int nmis = 0;
+        for (int g = 0; g < len; g++) {
+            int mis = 0;
+            for (int s = 0; s < S; s++) if (code_tg(code[(size_t)s * len + g]) >= 4) mis++;
+            if (mis > S * o.trim_gap_percent) nmis++;
+            else cols.push_back(g);
+        }
+        if (len - nmis < o.min_len) { E.filtered = 1; return true; }
+    } else {
+        for (int g = 0; g < len; g++) cols.push_back(g);
+    }
+    const int GG = (int)cols.size();
+    E.GG = GG;
+    E.GGp = (GG + 31) & ~31;
+    const int GGp = E.GGp;
+    E.codes.assign((size_t)S * GGp, CODE_GAP);
+    for (int s = 0; s < S; s++)
+        for (int i = 0; i < GG; i++) E.codes[(size_t)s * GGp + i] = code[(size_t)s * len + cols[i]];
+    // gap counts and missing flags (bpp_c.hpp:303-351)
+    std::vector<int> num_missing(S, 0);
+    for (int s = 0; s < S; s++)
+        for (int i = 0; i < GG; i++) if (E.codes[(size_t)s * GGp + i] == CODE_GAP) num_missing[s]++;
+    std::vector<int> c2a = M.ch0, c2b = M.ch1, par = M.parent;
+    std::vector<double> d2 = M.dist;
+    std::vector<char> missing(N, 0);
+    for (int s = S; s < N; s++) {
+        int p[2] = {c2a[s], c2b[s]};
+        for (int q = 0; q < 2; q++)
+            if (p[q] < S && num_missing[p[q]] > o.gap_prop * GG) missing[p[q]] = 1;
+        if (missing[p[0]] && missing[p[1]]) missing[s] = 1;
+    }
+    int ct = 0;
+    for (int cidx : M.conserve) if (cidx >= 0 && cidx < N && missing[cidx]) ct++;
+    if (ct > o.conserve_prop * (double)M.conserve.size()) { E.filtered = 1; return true; }
+    // collapse missing branches on the outgroup path, or everywhere with PRUNE_TREE
+    // (getSubtree_missing, bpp_c.cpp:64-113)
+    int root = N - 1;
+    std::vector<char> up(N, 0);
+    for (int s = 0; s < N; s++) up[s] = o.prune_tree ? 1 : M.upper[s];
+    struct Walker {
+        int S;
+        std::vector<int>&c2a, &c2b, &par;
+        std::vector<double>& d2;
+        std::vector<char>&missing, &up;
+        int& root;
+        void walk(int ss, int child) {
+            if (!up[ss] || ss < S) return;
+            int s = ss;
+            while (up[s] && s >= S) {
+                int p0 = c2a[s], p1 = c2b[s];
+                int keep;
+                if (missing[p0] && !missing[p1]) { keep = p1; par[p0] = -1; }
+                else if (!missing[p0] && missing[p1]) { keep = p0; par[p1] = -1; }
+                else {
+                    walk(p0, 0);
+                    walk(p1, 1);
+                    return;
+                }
+                d2[keep] += d2[s];
+                if (s == root) root = keep;
+                else {
+                    (child == 0 ? c2a : c2b)[par[ss]] = keep;
+                    par[keep] = par[ss];
+                }
+                s = keep;
+            }
+        }
+    } wk{S, c2a, c2b, par, d2, missing, up, root};
+    wk.walk(N - 1, -1);
+    par[root] = N;
+    // postorder of the pruned tree (bpp_c.cpp:44-60)
+    std::vector<int> nodes;
+    nodes.reserve(N);
+    {
+        std::vector<std::pair<int, int>> st;
+        st.push_back({root, 0});
+        while (!st.empty()) {
+            auto& t = st.back();
+            int j = t.first;
+            if (t.second == 0) {
+                t.second = 1;
+                if (c2a[j] != -1) { st.push_back({c2a[j], 0}); continue; }
+            }
+            if (t.second == 1) {
+                t.second = 2;
+                if (c2b[j] != -1) { st.push_back({c2b[j], 0}); continue; }
+            }
+            nodes.push_back(j);
+            st.pop_back();
+        }
+    }
+    std::vector<int> internal;
+    for (int s : nodes) if (s >= S) internal.push_back(s);
+    if (internal.empty()) { E.filtered = 2; return true; }  // the whole tree collapsed to one leaf
+    const int n_int = (int)internal.size();
+    std::vector<int> irank(N, -1), pos(N, -1);
+    for (int i = 0; i < n_int; i++) irank[internal[i]] = i;
+    for (int i = 0; i < (int)nodes.size(); i++) pos[nodes[i]] = i;
+    // internal Tg = K where both children are >= K (bpp_c.hpp:417-428)
+    E.tg0.assign((size_t)n_int * GGp, 4);
+    auto tg_at = [&](int s, int g) -> int {
+        if (s < S) return code_tg(E.codes[(size_t)s * GGp + g]);
+        return E.tg0[(size_t)irank[s] * GGp + g];
+    };
+    for (int i = 0; i < n_int; i++) {
+        int s = internal[i];
+        for (int g = 0; g < GG; g++)
+            E.tg0[(size_t)i * GGp + g] = (tg_at(c2a[s], g) >= 4 && tg_at(c2b[s], g) >= 4) ? 4 : -1;
+    }
+    // stream words of one internal-base pass: per column the root and every
+    // eligible internal node (bpp_c.cpp:674-732)
+    E.prefix.assign(GG + 1, 0);
+    for (int g = 0; g < GG; g++) {
+        int cnt = 1;
+        for (int i = 0; i + 1 < n_int; i++) {
+            int s = internal[i];
+            if (!missing[s] && E.tg0[(size_t)i * GGp + g] < 4) cnt++;
+        }
+        E.prefix[g + 1] = E.prefix[g] + cnt;
+    }
+    E.tg_draws = E.prefix[GG];
+    // levels: heights of internal nodes for the upward filter, depths for sampling
+    std::vector<int> height(N, 0), depth(N, 0);
+    for (int s : nodes)
+        if (s >= S) height[s] = 1 + std::max(height[c2a[s]], height[c2b[s]]);
+    for (int i = (int)nodes.size() - 1; i >= 0; i--) {
+        int s = nodes[i];
+        depth[s] = (s == root) ? 0 : depth[par[s]] + 1;
+    }
+    TopoLayout TL = TopoLayout::make(N);
+    E.topo.assign(TL.total, 0);
+    int16_t* t = E.topo.data();
+    for (int i = 0; i < N; i++) {
+        t[TL.nodes + i] = (int16_t)(i < (int)nodes.size() ? nodes[i] : -1);
+        t[TL.internal + i] = (int16_t)(i < n_int ? internal[i] : -1);
+        t[TL.c2a + i] = (int16_t)c2a[i];
+        t[TL.c2b + i] = (int16_t)c2b[i];
+        t[TL.par + i] = (int16_t)par[i];
+        t[TL.irank + i] = (int16_t)irank[i];
+        t[TL.pos + i] = (int16_t)pos[i];
+        t[TL.missing + i] = (int16_t)missing[i];
+        t[TL.upc + i] = (int16_t)(M.upper[i] ? 1 : 0);
+        t[TL.upcc + i] = (int16_t)(M.upper_conserve[i] ? 1 : 0);
+    }
+    int maxh = 0, maxd = 0;
+    for (int s : nodes) { if (s >= S) maxh = std::max(maxh, height[s]); maxd = std::max(maxd, depth[s]); }
+    {
+        int k = 0;
+        for (int h = 1; h <= maxh; h++) {
+            t[TL.hlev_start + h - 1] = (int16_t)k;
+            for (int s : nodes) if (s >= S && height[s] == h) t[TL.hlev_nodes + k++] = (int16_t)s;
+        }
+        t[TL.hlev_start + maxh] = (int16_t)k;
+        E.n_hlev = maxh;
+        k = 0;
+        for (int d = 1; d <= maxd; d++) {
+            t[TL.dlev_start + d - 1] = (int16_t)k;
+            for (int s : nodes) if (depth[s] == d) t[TL.dlev_nodes + k++] = (int16_t)s;
+        }
+        t[TL.dlev_start + maxd] = (int16_t)k;
+        E.n_dlev = maxd;
+    }
+    E.dist2 = d2;
+    E.root = root;
+    E.n_nodes = (int)nodes.size();
+    E.n_int = n_int;
+    E.missing.assign(missing.begin(), missing.end());
+    if (keep_full) {
+        E.tg_full.assign((size_t)GG * N, -1);
+        for (int g = 0; g < GG; g++) {
+            for (int s = 0; s < S; s++) E.tg_full[(size_t)g * N + s] = (int8_t)code_tg(E.codes[(size_t)s * GGp + g]);
+            for (int i = 0; i < n_int; i++) E.tg_full[(size_t)g * N + internal[i]] = E.tg0[(size_t)i * GGp + g];
+        }
+    }
+    return true;
+}
+
+}  // namespace pacc
+
+using namespace pacc;
+
+struct pacc_ctx {
+    HostModel M;
+    pacc_opts o;
+    std::string err;
+    int device = 0;
+    int n_sm = 0;
+    bool gpu_ok = false;
+    cudaStream_t stream = nullptr;
+    // pending and finished work
+    std::vector<HostElem> pending;
+    struct Done {
+        pacc_result r;
+        std::vector<int32_t> max_z;
+        std::vector<double> post_z;
+        std::vector<double> tr_d;
+        std::vector<int8_t> tr_z;
+    };
+    std::vector<Done> done;
+    size_t done_head = 0;
+    pacc_counters counters;
+    // persistent device buffers (grown on demand)
+    void* d_ws = nullptr; size_t ws_cap = 0;
+    void* d_blob = nullptr; size_t blob_cap = 0;
+    void* d_misc = nullptr; size_t misc_cap = 0;
+};
+
+static std::string g_create_error;
+
+static bool cuda_ok(pacc_ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+static bool grow(pacc_ctx* c, void** p, size_t* cap, size_t need) {
+    if (*cap >= need) return true;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t n = std::max(need, (size_t)(*cap * 3 / 2));
+    if (!cuda_ok(c, cudaMalloc(p, n), "cudaMalloc")) return false;
+    *cap = n;
+    return true;
+}
+
+extern "C" {
+
+void pacc_default_opts(pacc_opts* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->burnin = 200; o->mcmc = 800; o->adapt_freq = 500; o->seed = 5;
+    o->init_conserve_rate = 0.5; o->init_acce_rate = 1.0;
+    o->conserve_prior_a = 5; o->conserve_prior_b = 0.04;
+    o->acce_prior_a = 10; o->acce_prior_b = 0.2;
+    o->ropt = 1; o->cub = 1; o->nlb = 0.6;
+    o->init_lrate = 0.3; o->init_lrate2 = 0.1; o->init_grate = 0.5;
+    o->hyper_lrate_a = 1; o->hyper_lrate_b = 9;
+    o->hyper_grate_a = 3; o->hyper_grate_b = 1;
+    o->hyper_lrate2_a = 1; o->hyper_lrate2_b = 9;
+    o->conserve_prop = 0.8; o->gap_prop = 0.8; o->cons_to_mis = 0.01;
+    o->gapchar = '-'; o->prune_tree = 0; o->trim_gap_percent = 1; o->min_len = 50; o->indel = 0;
+    o->precision = PACC_FP64; o->device = 0; o->memory_budget_bytes = 0; o->max_resident = 0;
+    o->sweeps_per_launch = 0; o->trace_iters = 0; o->block_threads = 0; o->use_graphs = 1;
+}
+
+pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* status) {
+    auto fail = [&](int st, const std::string& msg) -> pacc_ctx* {
+        g_create_error = msg;
+        if (status) *status = st;
+        return nullptr;
+    };
+    if (!model || !opts) return fail(PACC_EINVAL, "null model or opts");
+    const int S = model->n_species;
+    if (S < 2 || S > 256) return fail(PACC_EINVAL, "n_species must be in [2, 256]");
+    if (opts->indel != 0) return fail(PACC_EUNSUPPORTED, "INDEL > 0 (five-state model) is not supported");
+    if (opts->mcmc < 1 || opts->burnin < 0 || opts->adapt_freq < 1)
+        return fail(PACC_EINVAL, "MCMC must be >= 1, BURNIN >= 0, ADAPT_FREQ >= 1");
+    pacc_ctx* c = new pacc_ctx();
+    c->o = *opts;
+    HostModel& M = c->M;
+    M.S = S;
+    M.N = 2 * S - 1;
+    const int N = M.N;
+    M.ch0.assign(N, -1); M.ch1.assign(N, -1); M.parent.assign(N, -1);
+    M.dist.assign(model->distances, model->distances + N);
+    for (int i = 0; i < N; i++) {
+        int a = model->children[2 * i], b = model->children[2 * i + 1];
+        if ((i < S) != (a < 0) || (a < 0) != (b < 0) || a >= N || b >= N) {
+            delete c;
+            return fail(PACC_EINVAL, "children[] is not a binary tree with leaves 0..S-1");
+        }
+        M.ch0[i] = a; M.ch1[i] = b;
+        if (a >= 0) M.parent[a] = i;
+        if (b >= 0) M.parent[b] = i;
+    }
+    for (int i = 0; i < N - 1; i++)
+        if (M.parent[i] < 0) { delete c; return fail(PACC_EINVAL, "node without parent"); }
+    M.outgroup.assign(model->outgroup, model->outgroup + model->n_outgroup);
+    M.conserve.assign(model->conserve, model->conserve + model->n_conserve);
+    // upper / upper_conserve (getUppertree, bpp.cpp:486-504)
+    M.upper.assign(N, 0);
+    M.upper_conserve.assign(N, 0);
+    auto mark = [&](const std::vector<int>& grp, std::vector<char>& out) {
+        for (int p : grp) {
+            if (p < 0 || p >= N) continue;
+            while (p != N - 1 && p >= 0) { out[p] = 1; p = M.parent[p]; }
+        }
+        out[N - 1] = 1;
+    };
+    mark(M.outgroup, M.upper);
+    mark(M.conserve, M.upper_conserve);
+    // eigensystem (bpp.hpp:357-362)
+    double lam[4], V[16], Vi[16];
+    int est = pacc_eigen::decompose(4, model->rate_matrix, lam, V, Vi);
+    if (est != pacc_eigen::EIG_OK) {
+        delete c;
+        return fail(PACC_EINVAL, est == pacc_eigen::EIG_COMPLEX ? "RATE_MAT has complex eigenvalues"
+                                                                : "RATE_MAT eigendecomposition failed");
+    }
+    DevModel& dm = M.dm;
+    std::memset(&dm, 0, sizeof(dm));
+    dm.S = S; dm.N = N;
+    for (int i = 0; i < 4; i++) {
+        dm.lam[i] = lam[i];
+        dm.pi[i] = model->pi[i];
+        dm.log_pi[i] = std::log(model->pi[i]);
+        for (int j = 0; j < 4; j++) {
+            dm.evec[i * 4 + j] = V[j * 4 + i];
+            dm.einv[i * 4 + j] = Vi[j * 4 + i];
+        }
+    }
+    dm.burnin = opts->burnin; dm.mcmc = opts->mcmc; dm.adapt_freq = opts->adapt_freq; dm.ropt = opts->ropt;
+    dm.seed = opts->seed;
+    dm.init_c = opts->init_conserve_rate; dm.init_n = opts->init_acce_rate;
+    dm.cprior_a = opts->conserve_prior_a; dm.cprior_b = opts->conserve_prior_b;
+    dm.nprior_a = opts->acce_prior_a; dm.nprior_b = opts->acce_prior_b;
+    dm.cub = opts->cub; dm.nlb = opts->nlb;
+    dm.init_l = opts->init_lrate; dm.init_l2 = opts->init_lrate2; dm.init_g = opts->init_grate;
+    dm.la = opts->hyper_lrate_a; dm.lb = opts->hyper_lrate_b;
+    dm.ga = opts->hyper_grate_a; dm.gb = opts->hyper_grate_b;
+    dm.l2a = opts->hyper_lrate2_a; dm.l2b = opts->hyper_lrate2_b;
+    dm.cons_to_mis = opts->cons_to_mis;
+    dm.trace_iters = opts->trace_iters;
+    c->device = opts->device;
+    // Without a usable GPU the context still serves the host-only entry points
+    // (pacc_debug_encode); every device call then fails with PACC_ECUDA.
+    c->gpu_ok = cuda_ok(c, cudaSetDevice(c->device), "cudaSetDevice") &&
+                cuda_ok(c, cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device), "attr") &&
+                cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") &&
+                cuda_ok(c, set_model(dm), "set_model");
+    std::memset(&c->counters, 0, sizeof(c->counters));
+    if (status) *status = PACC_OK;
+    return c;
+}
+
+const char* pacc_last_error(pacc_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+void pacc_destroy(pacc_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->d_ws) cudaFree(c->d_ws);
+    if (c->d_blob) cudaFree(c->d_blob);
+    if (c->d_misc) cudaFree(c->d_misc);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
+    if (!c || !b || b->n_elements < 0) return PACC_EINVAL;
+    const int n = b->n_elements;
+    size_t base = c->pending.size();
+    c->pending.resize(base + n);
+    std::atomic<int> next(0);
+    std::atomic<int> bad(0);
+    int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), 32));
+    if (n < 64) nt = 1;
+    auto work = [&]() {
+        for (;;) {
+            int e = next.fetch_add(1);
+            if (e >= n) break;
+            HostElem& E = c->pending[base + e];
+            E.no = b->element_no ? b->element_no[e] : e;
+            if (b->lengths[e] < 0 || !preprocess(c->M, c->o, b->bases + b->offsets[e], b->lengths[e], E, false))
+                bad = 1;
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; i++) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    if (bad) { c->pending.resize(base); c->err = "invalid element"; return PACC_EINVAL; }
+    return PACC_OK;
+}
+
+static int run_pending(pacc_ctx* c) {
+    if (c->pending.empty()) return PACC_OK;
+    if (!c->gpu_ok) return PACC_ECUDA;
+    cudaSetDevice(c->device);
+    const int N = c->M.N, S = c->M.S;
+    const int n = (int)c->pending.size();
+    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    const int T = c->o.burnin + c->o.mcmc;
+    const int TI = std::min(c->o.trace_iters, T);
+    // pack the blob
+    std::vector<ElemHeader> hdr(n);
+    size_t off = 0;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    int n_int_max = 1, GGp_max = 32;
+    const size_t tb = topo_bytes(N);
+    for (int e = 0; e < n; e++) {
+        HostElem& E = c->pending[e];
+        ElemHeader& H = hdr[e];
+        std::memset(&H, 0, sizeof(H));
+        H.element_no = E.no;
+        H.filtered = E.filtered;
+        if (E.filtered) continue;
+        H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
+        H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws;
+        H.codes_off = off; off = al(off + E.codes.size());
+        H.tg_off = off; off = al(off + E.tg0.size());
+        H.prefix_off = off; off = al(off + E.prefix.size() * 4);
+        H.topo_off = off; off = al(off + tb);
+        n_int_max = std::max(n_int_max, E.n_int);
+        GGp_max = std::max(GGp_max, E.GGp);
+    }
+    std::vector<uint8_t> blob(off);
+    for (int e = 0; e < n; e++) {
+        HostElem& E = c->pending[e];
+        if (E.filtered) continue;
+        ElemHeader& H = hdr[e];
+        std::memcpy(&blob[H.codes_off], E.codes.data(), E.codes.size());
+        std::memcpy(&blob[H.tg_off], E.tg0.data(), E.tg0.size());
+        std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
+        std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
+        std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
+    }
+    // launch geometry
+    int BT = c->o.block_threads > 0 ? c->o.block_threads : 128;
+    size_t smem = smem_bytes(N, BT, prec);
+    int per_sm = 2;
+    int grid = std::max(1, std::min(n, c->n_sm * per_sm));
+    size_t ws1 = ws_bytes(n_int_max, GGp_max, T, c->o.mcmc, N, prec);
+    ws1 = (ws1 + 4095) & ~(size_t)4095;
+    // misc buffers
+    size_t o_hdr = 0;
+    size_t o_res = al(o_hdr + sizeof(ElemHeader) * n);
+    size_t o_mz = al(o_res + sizeof(DevResult) * n);
+    size_t o_pz = al(o_mz + sizeof(int32_t) * 3 * N * (size_t)n);
+    size_t o_trd = al(o_pz + sizeof(double) * 3 * N * 4 * (size_t)n);
+    size_t o_trz = al(o_trd + sizeof(double) * 3 * 6 * (size_t)TI * n);
+    size_t o_cnt = al(o_trz + (size_t)3 * TI * N * n);
+    size_t o_next = al(o_cnt + sizeof(DevCounters));
+    size_t misc = al(o_next + 256);
+    if (!grow(c, &c->d_blob, &c->blob_cap, std::max<size_t>(off, 256)) ||
+        !grow(c, &c->d_ws, &c->ws_cap, ws1 * grid) || !grow(c, &c->d_misc, &c->misc_cap, misc))
+        return PACC_OOM;
+    char* mb = (char*)c->d_misc;
+    cudaStream_t st = c->stream;
+    if (!cuda_ok(c, cudaMemcpyAsync(c->d_blob, blob.data(), off, cudaMemcpyHostToDevice, st), "H2D blob") ||
+        !cuda_ok(c, cudaMemcpyAsync(mb + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st),
+                 "H2D hdr") ||
+        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_next + 256 - o_res, st), "memset"))
+        return PACC_ECUDA;
+    ChainParams p;
+    p.hdr = (const ElemHeader*)(mb + o_hdr);
+    p.blob = (const uint8_t*)c->d_blob;
+    p.n_elem = n;
+    p.next_elem = (int*)(mb + o_next);
+    p.results = (DevResult*)(mb + o_res);
+    p.max_z = (int32_t*)(mb + o_mz);
+    p.post_z = (double*)(mb + o_pz);
+    p.tr_d = TI > 0 ? (double*)(mb + o_trd) : nullptr;
+    p.tr_z = TI > 0 ? (int8_t*)(mb + o_trz) : nullptr;
+    p.ws = (char*)c->d_ws;
+    p.ws_stride = ws1;
+    p.n_int_max = n_int_max;
+    p.GGp_max = GGp_max;
+    p.counters = (DevCounters*)(mb + o_cnt);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    if (!cuda_ok(c, launch_chain(p, grid, BT, smem, prec, st), "launch chain")) return PACC_ECUDA;
+    cudaEventRecord(e1, st);
+    std::vector<DevResult> res(n);
+    std::vector<int32_t> mz((size_t)3 * N * n);
+    std::vector<double> pz((size_t)3 * N * 4 * n);
+    std::vector<double> trd((size_t)3 * 6 * TI * n);
+    std::vector<int8_t> trz((size_t)3 * TI * N * n);
+    DevCounters dc;
+    cudaMemcpyAsync(res.data(), mb + o_res, sizeof(DevResult) * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(mz.data(), mb + o_mz, mz.size() * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pz.data(), mb + o_pz, pz.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (TI > 0) {
+        cudaMemcpyAsync(trd.data(), mb + o_trd, trd.size() * 8, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(trz.data(), mb + o_trz, trz.size(), cudaMemcpyDeviceToHost, st);
+    }
+    cudaMemcpyAsync(&dc, mb + o_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "chain kernel")) return PACC_ECUDA;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int clk_khz = 0;
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, c->device);
+    pacc_counters& pc = c->counters;
+    std::memset(&pc, 0, sizeof(pc));
+    pc.edge_updates_internal = (double)dc.edge_internal;
+    pc.edge_updates_leaf = (double)dc.edge_leaf;
+    pc.column_loglik = (double)dc.col_ll;
+    pc.tg_draws = (double)dc.tg_draws;
+    pc.z_draws = (double)dc.z_draws;
+    pc.pmatrix_builds = (double)dc.pmat;
+    pc.iterations = (double)dc.iters;
+    pc.kernel_ms = ms;
+    pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
+    for (int e = 0; e < n; e++) {
+        pacc_ctx::Done d;
+        std::memset(&d.r, 0, sizeof(d.r));
+        d.r.element_no = c->pending[e].no;
+        d.r.n_nodes = N;
+        HostElem& E = c->pending[e];
+        if (E.filtered) {
+            d.r.status = E.filtered == 2 ? PACC_SAMPLER_ERROR : PACC_FILTERED;
+            d.max_z.assign(3 * N, 0);
+            d.post_z.assign(3 * N * 4, 0.0);
+        } else {
+            const DevResult& R = res[e];
+            d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
+            for (int m = 0; m < 3; m++) {
+                pacc_model_result& mr = d.r.model[m];
+                mr.loglik = R.model[m].loglik;
+                mr.max_loglik = R.model[m].max_loglik;
+                mr.n_rate = R.model[m].rates[0];
+                mr.c_rate = R.model[m].rates[1];
+                mr.g_rate = R.model[m].rates[2];
+                mr.l_rate = R.model[m].rates[3];
+                mr.l2_rate = R.model[m].rates[4];
+                mr.failure = R.model[m].failure;
+                mr.n_configs = R.model[m].n_configs;
+            }
+            d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
+            d.max_z.assign(mz.begin() + (size_t)e * 3 * N, mz.begin() + (size_t)(e + 1) * 3 * N);
+            d.post_z.assign(pz.begin() + (size_t)e * 3 * N * 4, pz.begin() + (size_t)(e + 1) * 3 * N * 4);
+            if (TI > 0) {
+                d.tr_d.assign(trd.begin() + (size_t)e * 3 * 6 * TI, trd.begin() + (size_t)(e + 1) * 3 * 6 * TI);
+                d.tr_z.assign(trz.begin() + (size_t)e * 3 * TI * N, trz.begin() + (size_t)(e + 1) * 3 * TI * N);
+            }
+        }
+        c->done.push_back(std::move(d));
+    }
+    c->pending.clear();
+    (void)S;
+    return PACC_OK;
+}
+
+int pacc_sync(pacc_ctx* c) {
+    if (!c) return PACC_EINVAL;
+    return run_pending(c);
+}
+
+int pacc_pending(pacc_ctx* c) {
+    if (!c) return 0;
+    return (int)(c->pending.size() + (c->done.size() - c->done_head));
+}
+
+static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
+    const int N = c->M.N;
+    int32_t* mz = out->max_z;
+    double* pz = out->post_z;
+    pacc_trace tr = out->trace;
+    *out = d.r;
+    out->max_z = mz;
+    out->post_z = pz;
+    out->trace = tr;
+    if (mz) std::memcpy(mz, d.max_z.data(), sizeof(int32_t) * 3 * N);
+    if (pz) std::memcpy(pz, d.post_z.data(), sizeof(double) * 3 * N * 4);
+    const int T = c->o.burnin + c->o.mcmc;
+    const int TI = std::min(c->o.trace_iters, T);
+    const int TS = c->o.trace_iters;  // caller stride
+    if (TI > 0 && !d.tr_d.empty()) {
+        double* dst[6] = {tr.loglik, tr.n_rate, tr.c_rate, tr.g_rate, tr.l_rate, tr.l2_rate};
+        for (int m = 0; m < 3; m++)
+            for (int r = 0; r < 6; r++)
+                if (dst[r])
+                    for (int i = 0; i < TI; i++) dst[r][m * TS + i] = d.tr_d[((size_t)m * 6 + r) * TI + i];
+        if (tr.z)
+            for (int m = 0; m < 3; m++)
+                for (int i = 0; i < TI; i++)
+                    for (int s = 0; s < N; s++)
+                        tr.z[((size_t)m * TS + i) * N + s] = d.tr_z[((size_t)m * TI + i) * N + s];
+    }
+}
+
+int pacc_poll(pacc_ctx* c, pacc_result* out, int max) {
+    if (!c || (!out && max > 0)) return -PACC_EINVAL;
+    int k = 0;
+    while (k < max && c->done_head < c->done.size()) {
+        fill_result(c, c->done[c->done_head], &out[k]);
+        c->done_head++;
+        k++;
+    }
+    if (c->done_head == c->done.size()) { c->done.clear(); c->done_head = 0; }
+    return k;
+}
+
+int pacc_run(pacc_ctx* c, const pacc_element_batch* b, pacc_result* out) {
+    if (!c || !b) return PACC_EINVAL;
+    if (!c->pending.empty() || c->done_head < c->done.size()) { c->err = "pacc_run needs an idle context"; return PACC_EBUSY; }
+    int st = pacc_submit(c, b);
+    if (st != PACC_OK) return st;
+    st = pacc_sync(c);
+    if (st != PACC_OK) return st;
+    int k = pacc_poll(c, out, b->n_elements);
+    return k == b->n_elements ? PACC_OK : PACC_ECUDA;
+}
+
+int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
+    if (!c || !out) return PACC_EINVAL;
+    *out = c->counters;
+    return PACC_OK;
+}
+
+int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, double* out) {
+    if (!c || n <= 0) return PACC_EINVAL;
+    if (!c->gpu_ok) return PACC_ECUDA;
+    cudaSetDevice(c->device);
+    double *dd = nullptr, *dr = nullptr, *dout = nullptr;
+    if (!cuda_ok(c, cudaMalloc(&dd, n * 8), "malloc") || !cuda_ok(c, cudaMalloc(&dr, n * 8), "malloc") ||
+        !cuda_ok(c, cudaMalloc(&dout, (size_t)n * 128), "malloc"))
+        return PACC_OOM;
+    cudaMemcpy(dd, d, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dr, r, n * 8, cudaMemcpyHostToDevice);
+    cudaError_t e = launch_pmatrix(n, dd, dr, dout, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 128, cudaMemcpyDeviceToHost);
+    cudaFree(dd); cudaFree(dr); cudaFree(dout);
+    return cuda_ok(c, e, "pmatrix") ? PACC_OK : PACC_ECUDA;
+}
+
+int pacc_debug_encode(pacc_ctx* c, const uint8_t* bases, int32_t length, int8_t* tg_out, int32_t* n_cols,
+                      uint8_t* missing_out, int32_t* root_out, int32_t* filtered) {
+    if (!c) return PACC_EINVAL;
+    HostElem E;
+    if (!preprocess(c->M, c->o, bases, length, E, true)) return PACC_EINVAL;
+    *filtered = E.filtered ? 1 : 0;
+    if (E.filtered) { *n_cols = 0; return PACC_OK; }
+    *n_cols = E.GG;
+    std::memcpy(tg_out, E.tg_full.data(), E.tg_full.size());
+    for (int s = 0; s < c->M.N; s++) missing_out[s] = E.missing[s];
+    *root_out = E.root;
+    return PACC_OK;
+}
+
+int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const int32_t* z, double c_rate,
+                      double n_rate, double* out, int32_t* n_cols) {
+    if (!c) return PACC_EINVAL;
+    if (!c->gpu_ok) return PACC_ECUDA;
+    cudaSetDevice(c->device);
+    HostElem E;
+    if (!preprocess(c->M, c->o, bases, length, E, false)) return PACC_EINVAL;
+    if (E.filtered) { *n_cols = 0; return PACC_FILTERED; }
+    const int N = c->M.N;
+    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    ElemHeader H;
+    std::memset(&H, 0, sizeof(H));
+    H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
+    size_t off = 0;
+    H.codes_off = off; off = al(off + E.codes.size());
+    H.tg_off = off; off = al(off + E.tg0.size());
+    H.prefix_off = off; off = al(off + E.prefix.size() * 4);
+    H.topo_off = off; off = al(off + topo_bytes(N));
+    std::vector<uint8_t> blob(off);
+    std::memcpy(&blob[H.codes_off], E.codes.data(), E.codes.size());
+    std::memcpy(&blob[H.tg_off], E.tg0.data(), E.tg0.size());
+    std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
+    std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
+    std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
+    size_t ws = ws_bytes(E.n_int, E.GGp, 1, 1, N, prec);
+    void *dblob = nullptr, *dh = nullptr, *dws = nullptr, *dz = nullptr, *dout = nullptr;
+    cudaError_t e = cudaMalloc(&dblob, off);
+    if (e == cudaSuccess) e = cudaMalloc(&dh, sizeof(H));
+    if (e == cudaSuccess) e = cudaMalloc(&dws, ws);
+    if (e == cudaSuccess) e = cudaMalloc(&dz, N * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)E.GG * 8);
+    if (e == cudaSuccess) e = cudaMemcpy(dblob, blob.data(), off, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dh, &H, sizeof(H), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dz, z, N * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        ChainParams p;
+        std::memset(&p, 0, sizeof(p));
+        p.hdr = (const ElemHeader*)dh;
+        p.blob = (const uint8_t*)dblob;
+        p.n_elem = 1;
+        p.ws = (char*)dws;
+        p.ws_stride = ws;
+        p.n_int_max = E.n_int;
+        p.GGp_max = E.GGp;
+        int BT = 128;
+        e = launch_loglik(p, (const int32_t*)dz, c_rate, n_rate, (double*)dout, BT, smem_bytes(N, BT, prec), prec,
+                          c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)E.GG * 8, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dblob); cudaFree(dh); cudaFree(dws); cudaFree(dz); cudaFree(dout);
+    *n_cols = E.GG;
+    return cuda_ok(c, e, "loglik") ? PACC_OK : PACC_ECUDA;
+}
+
+int pacc_debug_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out) {
+    if (n <= 0) return PACC_EINVAL;
+    uint32_t* d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * 4) != cudaSuccess) return PACC_OOM;
+    cudaError_t e = launch_stream(seed, w0, n, d, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? PACC_OK : PACC_ECUDA;
+}
+
+int pacc_measure_fma_peak(int device, double* fp64, double* fp32) {
+    if (cudaSetDevice(device) != cudaSuccess) return PACC_ECUDA;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    void* d = nullptr;
+    if (cudaMalloc(&d, 1 << 20) != cudaSuccess) return PACC_OOM;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    double res[2] = {0, 0};
+    for (int prec = 0; prec < 2; prec++) {
+        int grid = nsm * 8, BT = 256;
+        int iters = prec == 0 ? 2000 : 40000;
+        launch_fma_probe(prec, grid, BT, iters / 10, d, 0);
+        cudaDeviceSynchronize();
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(a);
+            launch_fma_probe(prec, grid, BT, iters, d, 0);
+            cudaEventRecord(b);
+            cudaEventSynchronize(b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            best = std::min(best, ms);
+        }
+        res[prec] = (double)grid * BT * iters * 8.0 * 2.0 / (best * 1e-3);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    if (fp64) *fp64 = res[0];
+    if (fp32) *fp32 = res[1];
+    return cudaGetLastError() == cudaSuccess ? PACC_OK : PACC_ECUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,537 @@
+// phyloacc-st-gpu — drop-in replacement for the PhyloAcc-ST executable.
+//
+//     phyloacc-st-gpu <config file>
+//
+// Reads the same key-value configuration (src/PhyloAcc-ST/main.cpp:100-287),
+// the same inputs (.mod tree + rate matrix, FASTA alignment, bed segments,
+// optional id list) and writes the same tables that phyloacc.py's snakemake
+// rule expects and phyloacc_post.py reads (main.cpp:360-402, bpp.cpp:568-619,
+// bpp_c2.cpp:706-785):
+//   <PREFIX>_elem_lik.txt, <PREFIX>_M{0,1,2}_elem_Z.txt,
+//   <PREFIX>_rate_postZ_M{0,1,2}.txt, <PREFIX>_hyper.txt,
+//   <PREFIX>_species_names.txt and, with VERBOSE, <PREFIX>_mcmc_trace_M{m}_{No}.txt.
+// The MCMC itself runs on the GPU through the C ABI of include/pacc.h.
+// Extra keys (ignored by PhyloAcc-ST): GPU_PRECISION fp64|fp32, GPU_DEVICE,
+// GPU_BLOCK_THREADS, GPU_MEMORY_BUDGET_GB.
+#include <dirent.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "pacc.h"
+
+using std::string;
+using std::vector;
+
+static string trim(string s, const string& ts = " \t\n") {
+    s.erase(0, s.find_first_not_of(ts));
+    s.erase(s.find_last_not_of(ts) + 1);
+    return s;
+}
+
+static vector<string> split(const string& s, char delim) {
+    vector<string> out;
+    std::stringstream ss(s);
+    string item;
+    while (std::getline(ss, item, delim)) out.push_back(item);
+    return out;
+}
+
+static string lower(string s) {
+    for (auto& ch : s) ch = (char)std::tolower((unsigned char)ch);
+    return s;
+}
+
+[[noreturn]] static void die(const string& msg) {
+    std::cerr << msg << std::endl;
+    std::exit(1);
+}
+
+// ---------------------------------------------------------------------------
+// .mod file: BACKGROUND, RATE_MAT and a labelled Newick TREE (newick.cpp:431-517)
+// ---------------------------------------------------------------------------
+struct TNode {
+    string name;
+    double dist = 0;
+    vector<int> kids;
+    int id = -1;
+};
+
+struct Tree {
+    vector<TNode> nodes;  // parse order
+    int root = -1;
+    int S = 0;
+    vector<string> names;       // by PhyloAcc id
+    vector<double> distances;   // by id
+    vector<int> children;       // [2N]
+};
+
+// Recursive Newick parser.  Branch lengths are parsed as float like the
+// reference (newick.cpp:185,300,325); every node must carry a label
+// (newick.cpp:416-419).
+static int parse_newick(const string& s, size_t& i, Tree& T) {
+    TNode nd;
+    if (i < s.size() && s[i] == '(') {
+        i++;
+        for (;;) {
+            int k = parse_newick(s, i, T);
+            nd.kids.push_back(k);
+            if (i < s.size() && s[i] == ',') { i++; continue; }
+            if (i < s.size() && s[i] == ')') { i++; break; }
+            die("(Error. Malformed tree)");
+        }
+    }
+    size_t a = i;
+    while (i < s.size() && s[i] != ':' && s[i] != ',' && s[i] != ')' && s[i] != ';') i++;
+    nd.name = s.substr(a, i - a);
+    if (i < s.size() && s[i] == ':') {
+        i++;
+        size_t b = i;
+        while (i < s.size() && s[i] != ',' && s[i] != ')' && s[i] != ';') i++;
+        nd.dist = (double)(float)std::atof(s.substr(b, i - b).c_str());
+    }
+    T.nodes.push_back(nd);
+    return (int)T.nodes.size() - 1;
+}
+
+static void load_mod(const string& path, Tree& T, double pi[4], double Q[16]) {
+    std::ifstream in(path.c_str());
+    if (!in) die("(Error. Cannot open the phylogenetic tree input file: " + path + ")");
+    string line, newick;
+    for (int i = 0; i < 4; i++) pi[i] = 0;
+    for (int i = 0; i < 16; i++) Q[i] = 0;
+    while (std::getline(in, line)) {
+        if (line == "") break;
+        line = trim(line);
+        vector<string> sp = split(line, ' ');
+        if (sp.empty()) continue;
+        if (sp[0] == "BACKGROUND:") {
+            int k = 0;
+            for (size_t g = 1; g < sp.size() && k < 4; g++)
+                if (sp[g] != "") pi[k++] = std::atof(sp[g].c_str());
+        } else if (sp[0] == "RATE_MAT:") {
+            for (int r = 0; r < 4; r++) {
+                if (!std::getline(in, line)) die("(Error. Truncated RATE_MAT)");
+                vector<string> tk = split(trim(line), ' ');
+                int k = 0;
+                for (auto& t : tk)
+                    if (t != "" && k < 4) Q[r * 4 + k++] = std::atof(t.c_str());
+            }
+        } else if (sp[0] == "TREE:" && sp.size() > 1) {
+            newick = trim(sp[1]);
+        }
+    }
+    if (newick.empty()) die("(Error. No TREE in " + path + ")");
+    size_t i = 0;
+    T.root = parse_newick(newick, i, T);
+    // PhyloAcc ids: leaves 0..S-1, internal S..N-1, both in postorder (newick.cpp:382-400)
+    int S = 0;
+    for (auto& nd : T.nodes) if (nd.kids.empty()) S++;
+    T.S = S;
+    int N = 2 * S - 1;
+    if ((int)T.nodes.size() != N) die("(Error. The tree must be binary)");
+    int leaf = 0, br = S;
+    // T.nodes is already in postorder (children pushed before parents)
+    for (auto& nd : T.nodes) nd.id = nd.kids.empty() ? leaf++ : br++;
+    T.names.assign(N, "");
+    T.distances.assign(N, 0);
+    T.children.assign(2 * N, -1);
+    for (auto& nd : T.nodes) {
+        if (nd.name.empty()) die("\n(Error. Some nodes in the tree aren't labeled. Please label all nodes and try again!)");
+        T.names[nd.id] = nd.name;
+        T.distances[nd.id] = nd.dist;
+        vector<int> ids;
+        for (int k : nd.kids) ids.push_back(T.nodes[k].id);
+        std::sort(ids.begin(), ids.end());  // dag order (bpp.cpp:105-117)
+        for (size_t k = 0; k < ids.size() && k < 2; k++) T.children[2 * nd.id + k] = ids[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FASTA + bed (profile.cpp:17-126)
+// ---------------------------------------------------------------------------
+struct Profile {
+    vector<string> names, X, elem_names;
+    vector<std::pair<long, long>> pos;
+};
+
+static Profile load_profile(const string& fa, const string& bed) {
+    Profile P;
+    std::ifstream in(fa.c_str());
+    if (!in) die("(Error. Cannot open the phylogenetic profile input file: " + fa + ")");
+    string line, whole;
+    bool have = false;
+    size_t G = 0;
+    while (std::getline(in, line)) {
+        line = trim(line);
+        if (!line.empty() && line[0] == '>') {
+            if (have) {
+                if (P.X.empty()) G = whole.size();
+                else if (whole.size() != G) die("(Error. Sequences of unequal length in " + fa + ")");
+                P.X.push_back(lower(whole));
+            }
+            P.names.push_back(trim(line.substr(1)));
+            whole.clear();
+            have = true;
+        } else {
+            whole += line;
+        }
+    }
+    if (have) {
+        if (!P.X.empty() && whole.size() != G) die("(Error. Sequences of unequal length in " + fa + ")");
+        P.X.push_back(lower(whole));
+    }
+    std::ifstream bs(bed.c_str());
+    if (!bs) die("(Error. Cannot open the segment input file: " + bed + ")");
+    while (std::getline(bs, line)) {
+        line = trim(line);
+        vector<string> sp = split(line, '\t');
+        if (sp.size() < 3) break;
+        P.elem_names.push_back(sp[0]);
+        P.pos.push_back({std::atoi(sp[1].c_str()), std::atoi(sp[2].c_str())});
+    }
+    return P;
+}
+
+// ---------------------------------------------------------------------------
+// configuration (main.cpp:36-287)
+// ---------------------------------------------------------------------------
+struct Config {
+    string phytree, align, segment, id_path, output, prefix = "test";
+    string outgroup, target, conserve;
+    int batch = -1, chain = 0, num_thread = 1;
+    bool verbose = false, sample_hyper = false;
+    pacc_opts o;
+};
+
+static bool to_bool(const string& s) { return s == "true" || s == "1"; }
+
+static Config load_config(const string& path) {
+    Config C;
+    pacc_default_opts(&C.o);
+    std::ifstream in(path.c_str());
+    if (!in) die("Cannot open the parameters file: " + path);
+    string line;
+    int line_num = 1;
+    double lrate2_init = C.o.init_lrate2;
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        vector<string> w;
+        string word;
+        while (ls >> word) w.push_back(word);
+        if (w.empty() || w[0][0] == '#') continue;
+        if (w.size() != 2) {
+            std::cerr << "\nLine " << line_num << " in the parameter file is not formatted correctly: " << line << "\n";
+            die("Each line should contain a parameter and a value separated by a space and no other whitespace.\n");
+        }
+        const string& k = w[0];
+        const string& v = w[1];
+        pacc_opts& o = C.o;
+        if (k == "PHYTREE_FILE") C.phytree = v;
+        else if (k == "ALIGN_FILE") C.align = v;
+        else if (k == "SEG_FILE") C.segment = v;
+        else if (k == "ID_FILE") C.id_path = v;
+        else if (k == "BATCH") C.batch = std::stoi(v);
+        else if (k == "RESULT_FOLDER") C.output = v;
+        else if (k == "PREFIX") C.prefix = v;
+        else if (k == "SEED") o.seed = (uint32_t)std::stoi(v);
+        else if (k == "INIT_CONSERVE_RATE") o.init_conserve_rate = std::stod(v);
+        else if (k == "INIT_ACCE_RATE") o.init_acce_rate = std::stod(v);
+        else if (k == "CONSERVE_PRIOR_A") o.conserve_prior_a = std::stod(v);
+        else if (k == "CONSERVE_PRIOR_B") o.conserve_prior_b = std::stod(v);
+        else if (k == "ACCE_PRIOR_A") o.acce_prior_a = std::stod(v);
+        else if (k == "ACCE_PRIOR_B") o.acce_prior_b = std::stod(v);
+        else if (k == "ROPT") o.ropt = std::stoi(v);
+        else if (k == "CUB") o.cub = std::stod(v);
+        else if (k == "NLB") o.nlb = std::stod(v);
+        else if (k == "BURNIN") o.burnin = std::stoi(v);
+        else if (k == "MCMC") o.mcmc = std::stoi(v);
+        else if (k == "ADAPT_FREQ") o.adapt_freq = std::stoi(v);
+        else if (k == "INIT_LRATE") o.init_lrate = std::stod(v);
+        else if (k == "INIT_LRATE2") lrate2_init = std::stod(v);
+        else if (k == "INIT_GRATE") o.init_grate = std::stod(v);
+        else if (k == "HYPER_LRATE_A") o.hyper_lrate_a = std::stod(v);
+        else if (k == "HYPER_LRATE_B") o.hyper_lrate_b = std::stod(v);
+        else if (k == "HYPER_GRATE_A") o.hyper_grate_a = std::stod(v);
+        else if (k == "HYPER_GRATE_B") o.hyper_grate_b = std::stod(v);
+        else if (k == "HYPER_LRATE2_A") o.hyper_lrate2_a = std::stod(v);
+        else if (k == "HYPER_LRATE2_B") o.hyper_lrate2_b = std::stod(v);
+        else if (k == "CHAIN") C.chain = std::stoi(v);
+        else if (k == "OUTGROUP") C.outgroup = v;
+        else if (k == "TARGETSPECIES") C.target = v;
+        else if (k == "CONSERVE") C.conserve = v;
+        else if (k == "CONSERVE_PROP") o.conserve_prop = std::stod(v);
+        else if (k == "GAP_PROP") o.gap_prop = std::stod(v);
+        else if (k == "CONSTOMIS") o.cons_to_mis = std::stod(v);
+        else if (k == "GAPCHAR") o.gapchar = v[0];
+        else if (k == "PRUNE_TREE") o.prune_tree = to_bool(v);
+        else if (k == "TRIM_GAP_PERCENT") o.trim_gap_percent = std::stod(v);
+        else if (k == "MIN_LEN") o.min_len = std::stoi(v);
+        else if (k == "INDEL") o.indel = std::stoi(v);
+        else if (k == "INDEL2") {}
+        else if (k == "SAMPLE_INDEL") {}
+        else if (k == "SAMPLE_HYPER") C.sample_hyper = to_bool(v);
+        else if (k == "VERBOSE") C.verbose = to_bool(v);
+        else if (k == "NUM_THREAD") C.num_thread = std::stoi(v);
+        else if (k == "GPU_PRECISION") o.precision = (v == "fp32" || v == "FP32") ? PACC_FP32 : PACC_FP64;
+        else if (k == "GPU_DEVICE") o.device = std::stoi(v);
+        else if (k == "GPU_BLOCK_THREADS") o.block_threads = std::stoi(v);
+        else if (k == "GPU_MEMORY_BUDGET_GB") o.memory_budget_bytes = (int64_t)(std::stod(v) * 1e9);
+        else std::cout << "Unknown parameter: " << k << ", skipping..." << std::endl;
+        line_num++;
+    }
+    C.phytree = trim(C.phytree, " \"\t\n");
+    C.align = trim(C.align, " \"\t\n");
+    C.output = trim(C.output, " \"\t\n");
+    C.segment = trim(C.segment, " \"\t\n");
+    C.o.init_lrate2 = (C.o.hyper_lrate2_a == 0) ? 0 : lrate2_init;  // main.cpp:286
+    return C;
+}
+
+static bool dir_exists(const string& p) {
+    if (p.empty()) return false;
+    DIR* d = opendir(p.c_str());
+    if (!d) return false;
+    closedir(d);
+    return true;
+}
+
+static vector<int> species_ids(const string& list, const vector<string>& names) {
+    vector<int> out;
+    for (auto& t : split(trim(list), ';')) {
+        int pos = (int)(std::find(names.begin(), names.end(), t) - names.begin());
+        out.push_back(pos);  // a name that is not found maps to S (bpp.hpp:230-235)
+    }
+    return out;
+}
+
+int main(int argc, char** argv) {
+    auto t_start = std::chrono::steady_clock::now();
+    std::cout << std::fixed << std::setprecision(4);
+    if (argc < 2) die("Please specify the path of the parameter file.");
+    Config C = load_config(argv[1]);
+    if (!dir_exists(C.output)) {
+        std::cout << "output path doesn't exist or empty!" << std::endl;
+        return 1;
+    }
+    if (C.sample_hyper) die("SAMPLE_HYPER is not supported by this build");
+    Profile prof = load_profile(C.align, C.segment);
+    Tree T;
+    double pi[4], Q[16];
+    load_mod(C.phytree, T, pi, Q);
+    const int S = T.S, N = 2 * S - 1;
+    // MatchProfAndTree (bpp.cpp:133-184)
+    vector<int> reorder(S, -1);
+    bool matched = (int)prof.names.size() >= S;
+    for (int s = 0; s < S && matched; s++) {
+        auto it = std::find(prof.names.begin(), prof.names.end(), T.names[s]);
+        if (it == prof.names.end()) matched = false;
+        else reorder[s] = (int)(it - prof.names.begin());
+    }
+    vector<string> X(S);
+    vector<string> species_names(S);
+    if (matched) {
+        std::cout << "The species in profile and tree match perfectly. Reorder the species in profile matrix by the tree."
+                  << std::endl;
+        for (int s = 0; s < S; s++) { X[s] = prof.X[reorder[s]]; species_names[s] = T.names[s]; }
+    } else {
+        std::cout << "The species in phylogenetic profile and tree cannot be matched literally; using the order of the data."
+                  << std::endl;
+        if ((int)prof.X.size() < S) die("(Error. Fewer sequences than tree leaves)");
+        for (int s = 0; s < S; s++) { X[s] = prof.X[s]; species_names[s] = prof.names[s]; }
+    }
+    vector<int> outgroup = species_ids(C.outgroup, species_names);
+    vector<int> conserve = species_ids(C.conserve, species_names);
+    pacc_model model;
+    model.n_species = S;
+    model.children = T.children.data();
+    model.distances = T.distances.data();
+    model.pi = pi;
+    model.rate_matrix = Q;
+    model.outgroup = outgroup.data();
+    model.n_outgroup = (int)outgroup.size();
+    model.conserve = conserve.data();
+    model.n_conserve = (int)conserve.size();
+    const int Cn = (int)prof.elem_names.size();
+    vector<long> el_start(Cn), el_len(Cn);
+    {
+        long start = 0;
+        for (int c = 0; c < Cn; c++) {
+            long len = prof.pos[c].second - prof.pos[c].first;
+            el_start[c] = start;
+            el_len[c] = len;
+            start += len;  // consecutive elements (bpp.hpp:257-274)
+        }
+    }
+    // ids (main.cpp:406-440)
+    vector<int> ids;
+    if (C.id_path.empty()) {
+        if (C.batch == -1) for (int c = 0; c < Cn; c++) ids.push_back(c);
+        else {
+            int tmp = (int)std::ceil(Cn / 3);
+            for (int c = C.batch * tmp; c < (C.batch + 1) * tmp && c < Cn; c++) ids.push_back(c);
+        }
+    } else {
+        std::ifstream in(C.id_path.c_str());
+        if (!in) die("Cannot open the id file: " + C.id_path);
+        string line;
+        while (std::getline(in, line)) {
+            std::istringstream ls(line);
+            string tk;
+            ls >> tk;
+            tk = trim(tk);
+            if (tk.empty()) continue;
+            ids.push_back(std::atoi(tk.c_str()));
+        }
+    }
+    std::cout << ids.size() << " of elements to be computed" << std::endl;
+    const string out = C.output + "/" + C.prefix;
+    {
+        std::ofstream h((out + "_hyper.txt").c_str());
+        h << "iter\tnprior_a\tnprior_b\tcprior_a\tcprior_b\tprior_l_a\tprior_l_b\tprior_g_a\tprior_g_b\n";
+        h << 0 << "\t" << C.o.acce_prior_a << "\t" << C.o.acce_prior_b << "\t" << C.o.conserve_prior_a << "\t"
+          << C.o.conserve_prior_b << "\t" << C.o.hyper_lrate_a << "\t" << C.o.hyper_lrate_b << "\t" << C.o.hyper_grate_a
+          << "\t" << C.o.hyper_grate_b << std::endl;
+        std::ofstream sp((out + "_species_names.txt").c_str());
+        for (int s = 0; s < N; s++) sp << T.names[s] << std::endl;
+    }
+    const string zpath[3] = {out + "_rate_postZ_M0.txt", out + "_rate_postZ_M1.txt", out + "_rate_postZ_M2.txt"};
+    std::ofstream oz[3];
+    for (int m = 0; m < 3; m++) {
+        oz[m].open(zpath[m].c_str());
+        oz[m] << "No.\tn_rate\tc_rate\tg_rate\tl_rate\tl2_rate";
+        for (int s = 0; s < N; s++)
+            for (int k = 0; k < 4; k++) oz[m] << "\t" << T.names[s] << "_" << k;
+        oz[m] << std::endl;
+    }
+    const int Tn = C.o.burnin + C.o.mcmc;
+    if (C.verbose) C.o.trace_iters = Tn;
+    if (C.chain < 1) {
+        // CHAIN has no default in PhyloAcc-ST (main.cpp:57): nothing runs.
+        ids.clear();
+    }
+    // batch of elements in tree leaf order
+    vector<int64_t> no(ids.size());
+    vector<int32_t> lens(ids.size());
+    vector<int64_t> offs(ids.size());
+    vector<uint8_t> bases;
+    for (size_t i = 0; i < ids.size(); i++) {
+        int c = ids[i];
+        if (c < 0 || c >= Cn) die("element id out of range");
+        no[i] = c;
+        lens[i] = (int32_t)el_len[c];
+        offs[i] = (int64_t)bases.size();
+        for (int s = 0; s < S; s++) {
+            const string& row = X[s];
+            for (long g = 0; g < el_len[c]; g++) {
+                long p = el_start[c] + g;
+                bases.push_back(p < (long)row.size() ? (uint8_t)row[p] : (uint8_t)0);
+            }
+        }
+    }
+    int st = 0;
+    pacc_ctx* ctx = pacc_create(&model, &C.o, &st);
+    if (!ctx) die(string("pacc_create failed: ") + pacc_last_error(nullptr));
+    vector<pacc_result> res(ids.size());
+    vector<int32_t> maxz(ids.size() * 3 * N);
+    vector<double> postz(ids.size() * 3 * N * 4);
+    const int TI = C.o.trace_iters;
+    vector<double> tr((size_t)ids.size() * 6 * 3 * std::max(TI, 1));
+    vector<int8_t> trz((size_t)ids.size() * 3 * std::max(TI, 1) * N);
+    for (size_t i = 0; i < ids.size(); i++) {
+        std::memset(&res[i], 0, sizeof(pacc_result));
+        res[i].max_z = &maxz[i * 3 * N];
+        res[i].post_z = &postz[i * 3 * N * 4];
+        if (TI > 0) {
+            double* b = &tr[i * 6 * 3 * TI];
+            res[i].trace.loglik = b;
+            res[i].trace.n_rate = b + 3 * TI;
+            res[i].trace.c_rate = b + 6 * TI;
+            res[i].trace.g_rate = b + 9 * TI;
+            res[i].trace.l_rate = b + 12 * TI;
+            res[i].trace.l2_rate = b + 15 * TI;
+            res[i].trace.z = &trz[i * 3 * TI * N];
+        }
+    }
+    pacc_element_batch batch;
+    batch.n_elements = (int32_t)ids.size();
+    batch.element_no = no.data();
+    batch.lengths = lens.data();
+    batch.offsets = offs.data();
+    batch.bases = bases.data();
+    if (!ids.empty()) {
+        st = pacc_run(ctx, &batch, res.data());
+        if (st != PACC_OK) die(string("GPU run failed: ") + pacc_last_error(ctx));
+    }
+    // rate_postZ rows (bpp_c2.cpp:774-784), model files M0, M1 (resZ 2), M2 (resZ 1)
+    for (size_t i = 0; i < ids.size(); i++) {
+        const pacc_result& r = res[i];
+        if (r.status == PACC_FILTERED || r.status == PACC_SAMPLER_ERROR) continue;
+        for (int m = 0; m < 3; m++) {
+            const pacc_model_result& mr = r.model[m];
+            oz[m] << r.element_no << "\t" << mr.n_rate << "\t" << mr.c_rate << "\t" << mr.g_rate << "\t" << mr.l_rate
+                  << "\t" << mr.l2_rate;
+            for (int s = 0; s < N; s++)
+                for (int k = 0; k < 4; k++) oz[m] << "\t" << postz[(i * 3 + m) * N * 4 + s * 4 + k];
+            oz[m] << std::endl;
+            if (C.verbose || mr.failure) {
+                std::ofstream tf((out + "_mcmc_trace_M" + std::to_string(m) + "_" + std::to_string(r.element_no) + ".txt").c_str());
+                tf.precision(8);
+                tf << "loglik\trate_n\trate_c\tgrate\tlrate\tlrate2\t";
+                for (int s = 0; s < N; s++) tf << T.names[s] << "\t";
+                tf << std::endl;
+                const double* b = &tr[i * 6 * 3 * TI];
+                for (int it = 0; it < TI; it++) {
+                    for (int q = 0; q < 6; q++) tf << b[q * 3 * TI + m * TI + it] << "\t";
+                    for (int s = 0; s < N; s++) tf << (int)trz[((i * 3 + m) * TI + it) * N + s] << "\t";
+                    tf << std::endl;
+                }
+            }
+        }
+    }
+    // _elem_lik.txt and _M*_elem_Z.txt (bpp.cpp:568-619)
+    {
+        std::ofstream ol((out + "_elem_lik.txt").c_str());
+        ol.precision(8);
+        ol << "No.\tID\tloglik_Null\tloglik_Acc\tloglik_Full\tlogBF1\tlogBF2\tloglik_Max_M0\tloglik_Max_M1\tloglik_Max_M2"
+           << std::endl;
+        for (size_t i = 0; i < ids.size(); i++) {
+            const pacc_result& r = res[i];
+            int c = ids[i];
+            double null_ = r.model[0].loglik, acc = r.model[1].loglik, full = r.model[2].loglik;
+            ol << c << "\t" << prof.elem_names[c] << "\t" << null_ << "\t" << acc << "\t" << full << "\t";
+            ol << acc - null_ << "\t" << acc - full;
+            ol << "\t" << r.model[0].max_loglik << "\t" << r.model[1].max_loglik << "\t" << r.model[2].max_loglik;
+            ol << std::endl;
+        }
+        for (int m = 0; m < 3; m++) {
+            std::ofstream ozz((out + "_M" + std::to_string(m) + "_elem_Z.txt").c_str());
+            ozz << "No.";
+            for (int s = 0; s < N; s++) ozz << "\t" << T.names[s];
+            ozz << std::endl;
+            for (size_t i = 0; i < ids.size(); i++) {
+                ozz << ids[i];
+                for (int s = 0; s < N; s++) ozz << "\t" << maxz[(i * 3 + m) * N + s];
+                ozz << std::endl;
+            }
+        }
+    }
+    pacc_counters pc;
+    pacc_get_counters(ctx, &pc);
+    pacc_destroy(ctx);
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    std::cout << "\n\ntime used:  " << (long)(secs / 60) << " min. (" << secs << " s; GPU kernel "
+              << pc.kernel_ms / 1000.0 << " s)" << std::endl;
+    return 0;
+}

@@ -1,0 +1,102 @@
+"""Generate the golden fixtures under tests/golden/<case>/.
+
+Each case holds the PhyloAcc-ST inputs (.mod, FASTA, bed, cfg) and the output
+tables the unmodified reference wrote for them: the PhyloAcc-ST sources from
+the reference checkout compiled against the stand-in GSL/Armadillo headers of
+oracle/shim (recipe: oracle/build_oracle.py), run with VERBOSE 1 so that it
+also writes its per-iteration traces (_mcmc_trace_M*_*.txt), which are packed
+into traces.npz.
+
+    python tests/golden/make_ref_golden.py /path/to/PhyloAcc
+
+Needs the reference checkout; the fixtures it writes are committed, so the
+tests that use them run anywhere.
+"""
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from phyloacc_gb300 import synth  # noqa: E402
+from oracle.build_oracle import build_reference  # noqa: E402
+
+CASES = {
+    # name: (dataset kind, element indices, burnin, mcmc, seed, extra cfg keys)
+    "st12_default": ("st12", [0, 1, 2, 3, 85, 90, 91, 99], 100, 300, 0, {}),
+    "st12_options": ("st12", [4, 5, 86, 92], 60, 200, 3,
+                     {"PRUNE_TREE": 1, "TRIM_GAP_PERCENT": 0.4, "GAP_PROP": 0.3, "ROPT": 2,
+                      "HYPER_LRATE2_A": 0, "ADAPT_FREQ": 25, "INIT_CONSERVE_RATE": 0.3}),
+    "st43_default": ("st43", [0, 7, 12], 50, 150, 1, {}),
+}
+
+
+def mask_taxa(ds, case):
+    """Blank some taxa in some elements to exercise missing-taxon handling,
+    outgroup collapse and the conserved-species filter."""
+    S = ds.tree.n_species
+    if case == "st12_options":
+        blk = ds.element(1)
+        blk[ds.outgroup[0], :] = ord("-")          # outgroup missing -> root moves
+        blk = ds.element(2)
+        for s in ds.conserve[:2]:
+            blk[s, :] = ord("n")
+        blk = ds.element(3)
+        blk[ds.target[0], : blk.shape[1] // 2] = ord("-")
+    if case == "st43_default":
+        blk = ds.element(1)
+        blk[0, :] = ord("-")
+        blk[S - 1, :] = ord("-")
+        blk = ds.element(2)
+        blk[:, :5] = ord("r")                     # ambiguity codes in a few columns
+        blk[3, 5:9] = ord("y")
+    return ds
+
+
+def read_trace(path):
+    rows = [ln.rstrip("\n\t").split("\t") for ln in open(path)][1:]
+    a = np.array([[float(x) for x in r] for r in rows])
+    return a
+
+
+def main(ref_root):
+    exe = build_reference(ref_root)
+    if exe is None:
+        raise SystemExit("reference sources not found under " + ref_root)
+    for name, (kind, idx, burn, mcmc, seed, extra) in CASES.items():
+        d = os.path.join(HERE, name)
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+        os.makedirs(d)
+        ds = synth.make_dataset(kind, seed=0).subset(idx)
+        ds.bases = ds.bases.copy()
+        ds = mask_taxa(ds, name)
+        kv = {"VERBOSE": 1}
+        kv.update(extra)
+        cfg = synth.write_inputs(ds, d, prefix="case", burnin=burn, mcmc=mcmc, seed=seed, extra=kv,
+                                 species_order=list(range(ds.tree.n_species))[::-1])
+        # make the cfg relative to the fixture directory
+        lines = open(cfg).read().replace(d + "/", "").replace(d, ".")
+        open(cfg, "w").write(lines)
+        r = subprocess.run([exe, "case.cfg"], cwd=d, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise SystemExit(r.stdout[-2000:] + r.stderr[-2000:])
+        out = os.path.join(d, "out")
+        traces = {}
+        for f in sorted(glob.glob(os.path.join(out, "case_mcmc_trace_M*_*.txt"))):
+            tag = os.path.basename(f)[len("case_mcmc_trace_"):-4]  # M{m}_{elem}
+            traces[tag] = read_trace(f)[:200]   # the first 200 iterations are the chain-parity window
+            os.remove(f)
+        np.savez_compressed(os.path.join(d, "traces.npz"), **traces)
+        os.remove(os.path.join(out, "case_hyper.txt"))
+        print(name, "ok", sorted(os.listdir(out)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

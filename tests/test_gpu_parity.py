@@ -1,0 +1,136 @@
+"""GPU parity: every kernel of the chain against the oracle on the same
+inputs and draw stream, and the whole path against the reference's own
+outputs (tests/golden)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import phyloacc_gb300 as pg
+from golden_io import CASES, as_float, load_case, read_table, ref_tables, ref_traces
+from oracle import pyoracle as po
+from phyloacc_gb300 import abi, synth
+from test_oracle_golden import _check_tables
+
+pytestmark = pytest.mark.gpu
+
+
+def test_stream_words_match_oracle(built):
+    for seed, w0 in [(0, 0), (5, 12345), (7, 2**33 + 3)]:
+        assert (pg.stream_words(seed, w0, 4099) == po.stream(seed, w0, 4099)).all()
+
+
+def test_pmatrix_matches_oracle(built):
+    ds = synth.make_dataset("st43", n_elements=2, seed=0)
+    o = abi.default_opts()
+    ctx = pg.Context(ds, o)
+    rng = np.random.default_rng(0)
+    d = np.concatenate([ds.tree.distances[:-1], rng.uniform(1e-6, 5.0, 200)])
+    r = np.concatenate([np.full(ds.tree.n_nodes - 1, 0.35), rng.uniform(0.01, 8.0, 200)])
+    a = ctx.pmatrix(d, r)
+    b = po.pmatrix(ds, o, d, r)
+    assert np.abs(a - b).max() < 1e-14 * 4
+    assert np.abs(a.sum(1) - 1).max() < 1e-13      # P^T columns are distributions over the child base
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.PACC_FP64, 1e-12), (abi.PACC_FP32, 1e-6)])
+def test_loglik_matches_oracle(built, prec, tol):
+    for kind, elems in [("st12", [0, 1, 90, 95]), ("st43", [0, 3, 17])]:
+        ds = synth.make_dataset(kind, n_elements=100, seed=1)
+        o = abi.default_opts()
+        o.precision = prec
+        ctx = pg.Context(ds, o)
+        rng = np.random.default_rng(2)
+        for e in elems:
+            for _ in range(3):
+                z = rng.integers(0, 3, ds.tree.n_nodes).astype(np.int32)
+                rc, rn = rng.uniform(0.1, 0.9), rng.uniform(1.0, 6.0)
+                a = ctx.loglik(e, z, rc, rn)
+                b = po.loglik(ds, o, e, z, rc, rn)
+                assert abs(a.sum() - b.sum()) <= tol * abs(b.sum()), (kind, e, a.sum(), b.sum())
+                assert (np.abs(a - b) <= tol * np.maximum(1.0, np.abs(b)) * (10 if prec else 1)).all()
+
+
+def _chain_compare(ds, o, T=200):
+    o.trace_iters = T
+    g = pg.Context(ds, o).run()
+    r = po.run(ds, o, threads=0)
+    assert (g.status() == r.status()).all()
+    for e in range(ds.n_elements):
+        if r.status()[e] == abi.PACC_FILTERED:
+            continue
+        for m in range(3):
+            assert (g.tr_z[e, m] == r.tr_z[e, m]).all(), (e, m)
+            ll_g, ll_r = g.tr["loglik"][e, m], r.tr["loglik"][e, m]
+            assert (np.abs(ll_g - ll_r) <= 1e-12 * np.abs(ll_r)).all(), (e, m)
+            for k in ("n_rate", "c_rate", "g_rate", "l_rate", "l2_rate"):
+                a, b = g.tr[k][e, m], r.tr[k][e, m]
+                assert (np.abs(a - b) <= 1e-12 * np.abs(b) + 1e-300).all(), (e, m, k)
+    return g, r
+
+
+def test_chain_matches_oracle_first_200_iterations(built):
+    ds = synth.make_dataset("st12", seed=0).subset([0, 1, 2, 3, 80, 90, 91, 99])
+    o = abi.default_opts()
+    o.seed, o.burnin, o.mcmc = 0, 100, 300
+    g, r = _chain_compare(ds, o)
+    mg, mr = g.field("loglik"), r.field("loglik")
+    fin = np.isfinite(mr)
+    assert np.allclose(mg[fin], mr[fin], rtol=1e-10, atol=0)
+    assert (g.max_z == r.max_z).all()
+    assert np.abs(g.post_z - r.post_z).max() == 0
+
+
+def test_chain_matches_oracle_43_taxa(built):
+    ds = synth.make_dataset("st43", n_elements=60, seed=0).subset([0, 5, 11, 23])
+    o = abi.default_opts()
+    o.seed, o.burnin, o.mcmc = 3, 60, 140
+    _chain_compare(ds, o)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_matches_reference_golden(built, case):
+    ds, o, kv = load_case(case)
+    o.trace_iters = 200
+    res = pg.Context(ds, o).run()
+    _check_tables(res, ds, ref_tables(case))
+    tr = ref_traces(case)
+    N = ds.tree.n_nodes
+    for key, a in tr.items():
+        m, e = int(key[1]), int(key.split("_")[1])
+        T = a.shape[0]
+        mine = np.stack([res.tr[k][e, m, :T] for k in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
+        assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), (case, key)
+        assert (res.tr_z[e, m, :T] == a[:, 6:6 + N].astype(np.int8)).all(), (case, key)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cli_drop_in_matches_reference_tables(built, case, tmp_path):
+    src = os.path.join(os.path.dirname(__file__), "golden", case)
+    work = tmp_path / case
+    shutil.copytree(src, work)
+    shutil.rmtree(work / "out")
+    os.makedirs(work / "out")
+    r = subprocess.run([pg.CLI_PATH, "case.cfg"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    ref_dir = os.path.join(src, "out")
+    for f in sorted(os.listdir(ref_dir)):
+        h1, rows1 = read_table(os.path.join(ref_dir, f))
+        h2, rows2 = read_table(str(work / "out" / f))
+        assert h1 == h2, f
+        assert len(rows1) == len(rows2), f
+        for a, b in zip(rows1, rows2):
+            assert len(a) == len(b), f
+            for x, y in zip(a, b):
+                if x == y:
+                    continue
+                fx, fy = as_float(x), as_float(y)
+                assert np.isclose(fx, fy, rtol=2e-7, atol=1e-12) or (np.isnan(fx) and np.isnan(fy)), (f, x, y)
+    # VERBOSE traces
+    for key, a in ref_traces(case).items():
+        m, e = key.split("_")
+        p = work / "out" / ("case_mcmc_trace_%s_%s.txt" % (m, e))
+        got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in open(p)][1:])
+        assert np.allclose(got[:a.shape[0]], a, rtol=2e-7, atol=1e-300), key

@@ -1,0 +1,101 @@
+"""Bit-exact checks of the host preprocessing of the C ABI (column encoding,
+trimming, missing taxa, pruning of the outgroup path, bpp_c.hpp:143-476)
+against the oracle.  Runs without a GPU: pacc_create serves the host-only
+entry points when no device is present."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+import phyloacc_gb300 as pg
+from golden_io import CASES, load_case
+from oracle import pyoracle as po
+from phyloacc_gb300 import abi, synth
+
+
+def _compare(ds, o, elems):
+    ctx = pg.Context(ds, o)
+    for e in elems:
+        a = ctx.encode(e)
+        b = po.encode(ds, o, e)
+        assert a[3] == b[3], (e, "filtered")
+        if a[3]:
+            continue
+        assert a[0].shape == b[0].shape
+        assert (a[0] == b[0]).all(), e
+        assert (a[1] == b[1]).all(), e
+        assert a[2] == b[2], e
+
+
+def _edge_dataset(seed=0):
+    ds = synth.make_dataset("st12", n_elements=12, seed=seed)
+    ds.bases = ds.bases.copy()
+    S = ds.tree.n_species
+    rng = np.random.default_rng(seed)
+    for e in range(ds.n_elements):
+        blk = ds.element(e)
+        if e == 0:
+            blk[ds.outgroup[0]] = ord("-")                 # outgroup missing -> root moves
+        if e == 1:
+            blk[:, :] = ord("-")                          # everything missing -> filtered by CONSERVE_PROP
+        if e == 2:
+            for s in ds.conserve[:3]:
+                blk[s] = ord("-")
+        if e == 3:
+            blk[rng.integers(0, S, 40), rng.integers(0, blk.shape[1], 40)] = np.frombuffer(b"rykmsw" * 7, np.uint8)[:40]
+        if e == 4:
+            blk[:, ::3] = ord("n")
+        if e == 5:
+            blk[1:, :10] = ord("-")                        # columns nearly all gaps (trimmed when enabled)
+        if e == 6:
+            blk[[ds.outgroup[0], 1, 2]] = ord("-")
+        if e == 7:
+            blk[:, :] = np.frombuffer(b"ACGTX*?.", np.uint8)[rng.integers(0, 8, blk.shape)]  # upper case -> other
+    return ds
+
+
+@pytest.mark.parametrize("kv", [
+    {},
+    {"prune_tree": 1},
+    {"trim_gap_percent": 0.5},
+    {"gap_prop": 0.05, "conserve_prop": 0.5},
+    {"min_len": 160},
+    {"gapchar": ord("n")},
+])
+def test_encode_matches_oracle(kv):
+    ds = _edge_dataset()
+    o = abi.default_opts()
+    for k, v in kv.items():
+        setattr(o, k, v)
+    _compare(ds, o, range(ds.n_elements))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_encode_golden_inputs(case):
+    ds, o, _ = load_case(case)
+    _compare(ds, o, range(ds.n_elements))
+
+
+def test_encode_43_taxa():
+    ds = synth.make_dataset("st43", n_elements=40, seed=2)
+    _compare(ds, abi.default_opts(), range(ds.n_elements))
+
+
+def test_abi_exports_every_declared_symbol(built):
+    hdr = open(pg.LIB_PATH.replace("phyloacc_gb300/_build/libpaccgpu.so", "include/pacc.h")).read()
+    names = set(re.findall(r"^(?:const\s+)?[a-z_0-9]+\s*\*?\s*(pacc_[a-z_0-9]+)\(", hdr, re.M))
+    assert len(names) >= 15
+    L = C.CDLL(pg.LIB_PATH)
+    for n in sorted(names):
+        assert hasattr(L, n), n
+
+
+def test_run_without_gpu_fails_loudly(built):
+    import os
+    if os.path.exists("/dev/nvidia0"):
+        pytest.skip("a GPU is present")
+    ds = synth.make_dataset("st12", n_elements=2, seed=0)
+    ctx = pg.Context(ds, abi.default_opts())
+    with pytest.raises(pg.PaccError):
+        ctx.run()

@@ -1,0 +1,59 @@
+"""The oracle against the reference's own outputs (tests/golden, written by
+the unmodified PhyloAcc-ST sources built against the stand-in GSL/Armadillo
+of oracle/shim and fed the same draw stream)."""
+import numpy as np
+import pytest
+
+from golden_io import CASES, as_float, load_case, ref_tables, ref_traces
+from oracle import pyoracle as po
+
+
+def _check_tables(res, ds, tables, rel=6e-8):
+    # _elem_lik.txt: precision 8
+    _, rows = tables["elem_lik"]
+    for i, row in enumerate(rows):
+        assert int(row[0]) == i
+        vals = [as_float(x) for x in row[2:]]
+        m = res.field("loglik")[i]
+        mx = res.field("max_loglik")[i]
+        mine = [m[0], m[1], m[2], m[1] - m[0], m[1] - m[2], mx[0], mx[1], mx[2]]
+        for a, b in zip(mine, vals):
+            if np.isnan(b) or np.isinf(b):
+                assert (np.isnan(a) and np.isnan(b)) or a == b
+            else:
+                assert abs(a - b) <= rel * max(1.0, abs(b)), (i, mine, vals)
+    # _M*_elem_Z.txt: integers
+    for m in range(3):
+        _, rows = tables["M%d_elem_Z" % m]
+        for i, row in enumerate(rows):
+            assert [int(x) for x in row[1:]] == res.max_z[i, m].tolist()
+    # _rate_postZ_M*.txt: default precision 6
+    for m in range(3):
+        _, rows = tables["rate_postZ_M%d" % m]
+        st = res.status()
+        k = 0
+        for i in range(ds.n_elements):
+            if st[i] == 1:
+                continue
+            row = [as_float(x) for x in rows[k]]
+            k += 1
+            assert int(row[0]) == i
+            f = res.arr[i].model[m]
+            mine = [f.n_rate, f.c_rate, f.g_rate, f.l_rate, f.l2_rate] + res.post_z[i, m].reshape(-1).tolist()
+            assert np.allclose(mine, row[1:], rtol=6e-6, atol=1e-12), (i, m)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_reference(case):
+    ds, o, kv = load_case(case)
+    o.trace_iters = 200
+    res = po.run(ds, o, threads=4)
+    _check_tables(res, ds, ref_tables(case))
+    tr = ref_traces(case)
+    N = ds.tree.n_nodes
+    for key, a in tr.items():
+        m, e = int(key[1]), int(key.split("_")[1])
+        T = a.shape[0]
+        mine = np.stack([res.tr[k][e, m, :T] for k in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
+        assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), (case, key)
+        assert (res.tr_z[e, m, :T] == a[:, 6:6 + N].astype(np.int8)).all(), (case, key)
