@@ -1,0 +1,275 @@
+"""Benchmark: posterior elements/sec at 43 taxa (FP32 vs FP64 path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+A step runs one batch of the 43-taxon workload through the whole per-element
+path (M0, M1, M2: Gibbs + Eval2 + output rows, 2,000 iterations each) on the
+GPU.  The workload is synthetic with the shapes of the 43-taxon configuration:
+Yule tree with total length 2.5 and 8 target taxa in 3 clades; element lengths
+log-normal (median 250 bp, sigma 0.6, clipped 50-2000); 10% accelerated
+(r2 ~ U[1.5, 4]) and r1 ~ U[0.2, 0.6]; 5% of (taxon, element) pairs missing and
+3% gap cells; BURNIN 500 + MCMC 1500.
+
+value     = elements / kernel time of the FP32-partial path (inputs resident)
+e2e       = the same through pacc_run from host buffers (preprocessing, H2D,
+            kernel, D2H inside the timed region)
+fp64      = the plain FP64 path on a smaller batch of the same workload
+--impl reference runs the CPU oracle (the restatement of PhyloAcc-ST's
+path; the unmodified reference needs GSL/Armadillo, absent here) on all host
+cores over a bounded sample of the same workload.
+Multi-GPU: replicas (elements are independent; no collective), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "posterior elements/sec at 43 taxa (FP32 vs FP64 path); p50/p99 element latency"
+WORKLOAD = ("43-taxon Yule tree (total length 2.5, 8 targets in 3 clades); elements log-normal "
+            "(median 250 bp, sigma 0.6, clipped 50-2000), 10% accelerated; BURNIN 500 + MCMC 1500; "
+            "M0+M1+M2 with Eval2 and output rows per element")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as td
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        td.init_process_group("gloo", rank=rank, world_size=ws)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def reduce_max(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for ln in self.p.stdout:
+            self.rows.append([x.strip() for x in ln.split(",")])
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(n, seed):
+    from phyloacc_gb300 import synth
+    ds = synth.make_dataset("st43", n_elements=n, seed=seed)
+    return ds
+
+
+ITERS = {"burnin": 500, "mcmc": 1500}
+
+
+def opts_for(precision):
+    from phyloacc_gb300 import abi
+    o = abi.default_opts()
+    o.burnin, o.mcmc, o.seed = ITERS["burnin"], ITERS["mcmc"], 0
+    o.precision = precision
+    return o
+
+
+def cpu_baseline(ds, n_sample, threads):
+    from oracle import pyoracle
+    sub = ds.subset(list(range(n_sample)))
+    o = opts_for(0)
+    t = time.time()
+    pyoracle.run(sub, o, threads=threads)
+    dt = time.time() - t
+    return n_sample / dt, dt
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    ds = make_workload(max(cores, 1) * 2, seed=0)
+    vals = []
+    for step in range(args.warmup + args.steps):
+        sub = ds.subset(list(range((step % 2) * cores, (step % 2) * cores + cores)))
+        v, dt = cpu_baseline(sub, cores, cores)
+        if step >= args.warmup:
+            vals.append((v, dt))
+    v = float(np.mean([x[0] for x in vals]))
+    ms = float(np.mean([x[1] for x in vals])) * 1e3
+    sample = "%d elements per step (one per host core) of the 43-taxon workload, full 2,000 iterations x 3 models" % cores
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "elements_per_step": cores, "parallelism": "OpenMP over elements"},
+            "cpu_baseline": {"value": v, "unit": "elements/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def time_gpu(ctx, ds, steps, warmup, ws, clocks=None):
+    """Returns per-step (kernel_s, wall_s) lists (max over ranks) and the last counters."""
+    kern, wall = [], []
+    cnt = None
+    res = None
+    for step in range(warmup + steps):
+        timed = step >= warmup
+        barrier(ws)
+        if timed and clocks is not None and step == warmup:
+            clocks.start()
+        t = time.perf_counter()
+        res = ctx.run(ds)
+        dt = time.perf_counter() - t
+        c = ctx.counters()
+        if timed:
+            kern.append(reduce_max(ws, c["kernel_ms"] * 1e-3))
+            wall.append(reduce_max(ws, dt))
+            cnt = c
+    return kern, wall, cnt, res
+
+
+def run_gpu(args, ws, rank, local):
+    import phyloacc_gb300 as pg
+    from phyloacc_gb300 import abi
+    if not os.path.exists(pg.LIB_PATH):
+        from phyloacc_gb300.build import build
+        build()
+    E = args.elements
+    ds = make_workload(E, seed=100 + rank)
+    o32 = opts_for(abi.PACC_FP32)
+    o32.device = 0
+    ctx32 = pg.Context(ds, o32)
+    clocks = ClockSampler(local)
+    kern, wall, cnt, res = time_gpu(ctx32, ds, args.steps, args.warmup, ws, clocks)
+    clk = clocks.stop()
+    value = ws * E / float(np.mean(kern))
+    e2e = ws * E / float(np.mean(wall))
+    h2d = int(ds.bases.nbytes + ds.lengths.nbytes + ds.offsets.nbytes)
+    d2h = int(E * (3 * ds.tree.n_nodes * (4 + 32) + 256))
+    dev_ms = np.array([res.arr[i].device_ms for i in range(res.n)])
+    # FP64 plain path on a smaller batch of the same workload
+    E64 = args.fp64_elements
+    if args.no_fp64:
+        k64, c64, v64 = [float("nan")], {"flop": float("nan")}, float("nan")
+    else:
+        ds64 = ds.subset(list(range(E64)))
+        ctx64 = pg.Context(ds64, opts_for(abi.PACC_FP64))
+        k64, w64, c64, _ = time_gpu(ctx64, ds64, max(1, args.steps // 2), 1, ws)
+        v64 = ws * E64 / float(np.mean(k64))
+    fp64_peak, fp32_peak = pg.measure_fma_peak(0)
+    achieved = cnt["flop"] / float(np.mean(kern)) / ws * ws
+    line = {
+        "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(kern)) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32-partials+fp64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "elements_per_step": E, "precision": "FP32 partials, FP64 chain math",
+                   "l2": "working set larger than L2 (per-CTA chain state x resident CTAs)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "work": "36 flop per internal-child edge-column + 4 per leaf-child edge-column (device counters)",
+                     "peak_source": "measured FP32 FMA probe (pacc_measure_fma_peak)"},
+        "fp64": {"value": v64, "unit": "elements/s", "elements_per_step": E64,
+                 "achieved_tflops": c64["flop"] / float(np.mean(k64)) / 1e12,
+                 "peak_tflops": fp64_peak / 1e12,
+                 "frac": c64["flop"] / float(np.mean(k64)) / fp64_peak},
+        "fp32_over_fp64": value / v64,
+        "element_device_ms": {"p50": float(np.percentile(dev_ms, 50)), "p99": float(np.percentile(dev_ms, 99))},
+        "counters": {k: cnt[k] for k in ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "iterations")},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        v, dt = cpu_baseline(ds, cores, cores)
+        line["cpu_baseline"] = {"value": v, "unit": "elements/s", "cores": cores, "kind": "port",
+                                "sample": "%d elements of the same workload, one per host core, %.1f s" % (cores, dt)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--elements", type=int, default=5000)
+    ap.add_argument("--fp64-elements", type=int, default=608)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--burnin", type=int, default=500, help="profiling only: shorter chains")
+    ap.add_argument("--mcmc", type=int, default=1500, help="profiling only: shorter chains")
+    args = ap.parse_args()
+    ITERS["burnin"], ITERS["mcmc"] = args.burnin, args.mcmc
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if ws > 1 else None
+        run_gpu(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

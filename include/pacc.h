@@ -50,8 +50,10 @@ typedef enum pacc_status {
 } pacc_status;
 
 typedef enum pacc_precision {
-    PACC_FP64 = 0,              /* plain path: FP64 partials */
-    PACC_FP32 = 1               /* FP32 partials with power-of-two rescaling, FP64 sums */
+    PACC_FP64 = 0,              /* plain path: one CTA per element, FP64 partials, partial re-pruning */
+    PACC_FP32 = 1,              /* batched path: one warp per element, FP32 partials with power-of-two
+                                   rescaling, FP64 log-likelihood sums and chain arithmetic */
+    PACC_FP64_BATCHED = 2       /* the batched layout with FP64 partials (checks the layout draw for draw) */
 } pacc_precision;
 
 /* Tree, rate matrix and species sets: the content of the .mod file plus the
@@ -200,6 +202,9 @@ typedef struct pacc_counters {
     double iterations;             /* MCMC iterations run (all models) */
     double kernel_ms;              /* summed duration of the chain kernels (CUDA events) */
     double flop;                   /* algorithmic FP work of the prunes, counted from the above */
+    double phase_cycles[8];        /* batched kernel, SM cycles summed over chains: internal-base pass,
+                                      emission sums, Z filter, Z-change likelihood, accelerated-rate MH,
+                                      conserved-rate MH, monitor/transitions, model init + Eval2 + output */
 } pacc_counters;
 int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);
 

@@ -118,7 +118,9 @@ class Context:
     def counters(self) -> dict:
         c = abi.PaccCounters()
         lib().pacc_get_counters(self.h, C.byref(c))
-        return {n: getattr(c, n) for n, _ in abi.PaccCounters._fields_}
+        out = {n: getattr(c, n) for n, _ in abi.PaccCounters._fields_ if n != "phase_cycles"}
+        out["phase_cycles"] = list(c.phase_cycles)
+        return out
 
     def pmatrix(self, d, r) -> np.ndarray:
         d = np.ascontiguousarray(d, dtype=np.float64)

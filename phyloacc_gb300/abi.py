@@ -22,6 +22,7 @@ PACC_EUNSUPPORTED = 9
 
 PACC_FP64 = 0
 PACC_FP32 = 1
+PACC_FP64_BATCHED = 2
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -128,7 +129,7 @@ class PaccResult(C.Structure):
 class PaccCounters(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "edge_updates_internal", "edge_updates_leaf", "column_loglik", "tg_draws", "z_draws",
-        "pmatrix_builds", "iterations", "kernel_ms", "flop")]
+        "pmatrix_builds", "iterations", "kernel_ms", "flop")] + [("phase_cycles", C.c_double * 8)]
 
 
 def ptr(a: np.ndarray, ctype):

@@ -43,6 +43,7 @@ def build(force=False, verbose=False):
         return LIB
     objs = {
         "pacc_chain.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_chain.cu")],
+        "pacc_batch.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_batch.cu")],
         "pacc_host.o": [NVCC] + ARCH + COMMON + ["-x", "cu", "-c", os.path.join(CSRC, "pacc_host.cpp")],
     }
     cmds = []

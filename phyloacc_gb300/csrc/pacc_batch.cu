@@ -1,0 +1,1224 @@
+// pacc_batch.cu — the batched, resumable chain kernel: one warp per element
+// chain, many chains per SM, chain state resident in device memory between
+// launches.
+//
+// Same sampler as pacc_chain.cu (PhyloAcc-ST's initMCMC -> Gibbs -> Eval2 ->
+// Output_init for M0, M1, M2; src/PhyloAcc-ST/main.cpp:468-494) with a
+// layout built for many concurrent chains:
+//   * a chain is a warp; a CTA holds several chains, each with its own slice
+//     of shared memory and its own position in the element queue;
+//   * partial likelihoods are never stored between steps: every pass over the
+//     columns recomputes them column by column in a per-lane shared-memory
+//     slice (one column per lane), so the only per-iteration device-memory
+//     traffic is the element's column codes.  The reference's partial
+//     re-pruning (bpp_c.cpp:620-642) is an optimisation over stored partials
+//     and gives the same values as a full prune;
+//   * the internal-base pass samples, and counts the (child, parent) base
+//     pairs that the branch emissions need (getEmission, bpp_c2.cpp:355-390),
+//     in the same sweep over a column;
+//   * the latent-state filter runs in linear space in FP64 with per-node
+//     normalisation (the reference's log-space log_multi2, bpp.hpp:447-460,
+//     computes the same messages);
+//   * a launch advances each resident chain by a bounded number of iterations
+//     and saves its state, so a host loop can retire finished chains and admit
+//     new ones between launches (serving), and a fixed launch sequence can be
+//     captured in a CUDA graph.
+// Real = float: FP32 partials with power-of-two rescaling folded into one
+// integer exponent per column; per-column log-likelihoods are combined in
+// FP64 (mantissa products + exact exponents); exp(lambda*r*t), the MH ratio,
+// the Z filter normalisation and the chain scalars stay in FP64.
+// Real = double: the same kernel in FP64, used to check this layout against
+// the oracle draw for draw.
+#include "pacc_common.cuh"
+
+namespace pacc {
+
+// Per-slot device workspace.
+struct SlotLayout {
+    size_t Z, maxz, tbl, trz, trd, total;
+    __host__ __device__ static SlotLayout make(int N, int T) {
+        SlotLayout L;
+        size_t o = 0;
+        auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+        L.Z = o; o = al(o + N);
+        L.maxz = o; o = al(o + N);
+        L.tbl = o; o = al(o + (size_t)3 * N * 16 * 8);     // class P^T tables, FP64 [null, cons, neut][N][16]
+        L.trz = o; o = al(o + (size_t)T * N);
+        L.trd = o; o = al(o + (size_t)7 * T * 8);
+        L.total = o;
+        return L;
+    }
+};
+
+// Per-warp Eval2 scratch.
+struct GrpLayout {
+    size_t hash, rep, cfg, nxt, head, first, cstat, total;
+    __host__ __device__ static GrpLayout make(int mcmc) {
+        GrpLayout L;
+        size_t o = 0;
+        auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+        L.hash = o; o = al(o + (size_t)(mcmc + 1) * 8);
+        L.rep = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        L.cfg = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        L.nxt = o; o = al(o + (size_t)(mcmc + 1) * 4);
+        L.head = o; o = al(o + (size_t)(mcmc + 2) * 4);
+        L.first = o; o = al(o + (size_t)(mcmc + 2) * 4);
+        L.cstat = o; o = al(o + (size_t)9 * (mcmc + 2) * 8);
+        L.total = o;
+        return L;
+    }
+};
+
+// Shared memory of one warp-chain.
+template <typename Real>
+struct WarpSmem {
+    size_t ptc, part, tgv, hdf, rec, stage, cnt, topo, i8, dbl, total;
+    __host__ __device__ static WarpSmem make(int N, int NI, int S) {
+        WarpSmem w;
+        size_t o = 0;
+        auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        w.ptc = o; o = al(o + (size_t)N * 16 * sizeof(Real));        // current P^T per branch
+        size_t part_bytes = (size_t)NI * 4 * 32 * sizeof(Real);
+        size_t alias_bytes = (size_t)N * 6 * 8;                        // emis + bz alias the slice
+        w.part = o; o = al(o + (part_bytes > alias_bytes ? part_bytes : alias_bytes));
+        w.tgv = o; o = al(o + (size_t)NI * 32);
+        w.hdf = o; o = al(o + (size_t)NI * 32);
+        w.rec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
+        w.stage = o; o = al(o + (size_t)S * 32);
+        w.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 2);               // uint16 bins
+        w.topo = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
+        w.i8 = o; o = al(o + (size_t)N * 6);                            // fixZ chg unv mask maxz(unused) Zc
+        w.dbl = o; o = al(o + (size_t)N * 8 + 64 * 8);                  // dist2 + scratch
+        w.total = o;
+        return w;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// per-warp context
+// ---------------------------------------------------------------------------
+template <typename Real>
+struct W {
+    int lane, S, N, GG, GGp, root, n_nodes, n_int, n_hlev, n_dlev, tg_draws, T, burn, mcmc;
+    const uint8_t* codes;
+    const int32_t* prefix;
+    int16_t *nodes, *internal, *c2a, *c2b, *par, *irank, *pos, *missing, *upc, *upcc, *hlev_start, *hlev_nodes,
+        *dlev_start, *dlev_nodes;
+    Real* ptc;          // [N][16]
+    Real* part;         // [NI][4][32]
+    int8_t* tgv;        // [NI][32]
+    int8_t* hdf;        // [NI][32] node has data at this lane's column
+    const NodeRec* rec; // [NI]
+    uint8_t* stage;     // [S][32]
+    unsigned* cnt;      // [N][20] packed uint16 pairs
+    double* emis;       // [N][3]  (aliases part)
+    double* bz;         // [N][3]  (aliases part)
+    double* dist2;      // [N]
+    double* scr;        // 64 doubles
+    int8_t *Z, *fixZ, *chg, *unv, *mask;
+    // slot workspace
+    int8_t* sZ;
+    int8_t* smaxz;
+    double* tbl;        // [3][N][16]
+    int8_t* trz;        // [T][N]
+    double* trd;        // [7][T]
+    SlotState st;       // lane-replicated copy
+    unsigned long long e_int, e_leaf, n_tg;
+    unsigned long long ph[8];
+    long long t0;
+
+    __device__ __forceinline__ Real& P(int s, int i, int j) { return ptc[s * 16 + i * 4 + j]; }
+    __device__ __forceinline__ Real& PART(int k, int j) { return part[(k * 4 + j) * 32 + lane]; }
+};
+
+__device__ __forceinline__ void wsync() { __syncwarp(); }
+
+// Phase timer of a warp (lane 0): cycles since the previous mark go to phase i.
+#define PHASE(i)                               \
+    do {                                       \
+        if (w.lane == 0) {                     \
+            long long t_ = clock64();          \
+            w.ph[i] += (unsigned long long)(t_ - w.t0); \
+            w.t0 = t_;                         \
+        }                                      \
+    } while (0)
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_or(int v) { return __any_sync(0xffffffffu, v); }
+
+enum { TR_LL = 0, TR_FULL = 1, TR_N = 2, TR_C = 3, TR_G = 4, TR_L = 5, TR_L2 = 6 };
+enum { C_NULL = 0, C_CONS = 1, C_NEUT = 2 };
+
+// Fill the current per-branch matrices: class by Z (null / cons / neut,
+// bpp_c.cpp:661-663); with prop_class >= 0 the branches of that class get the
+// proposal matrices P(d * r_prop) (log_f_Xz, bpp_c.cpp:885-906).
+template <typename Real>
+__device__ void fill_ptc(W<Real>& w, int prop_class, double r_prop) {
+    for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
+        int s = w.nodes[i];
+        int z = w.Z[s];
+        int k = (z == 2) ? C_NEUT : (z == 0 ? C_NULL : C_CONS);
+        if (prop_class >= 0 && k == prop_class) {
+            double pt[16];
+            build_pt(w.dist2[s], r_prop, true, pt);
+            for (int q = 0; q < 16; q++) w.ptc[s * 16 + q] = (Real)pt[q];
+        } else {
+            const double* src = w.tbl + ((size_t)k * w.N + s) * 16;
+            for (int q = 0; q < 16; q++) w.ptc[s * 16 + q] = (Real)src[q];
+        }
+    }
+    wsync();
+}
+
+// Class table k at rate r for all branches of the pruned tree; branches not
+// longer than 1e-10 keep the identity (bpp_c.cpp:191-226) unless force.
+template <typename Real>
+__device__ void build_table(W<Real>& w, int k, double r, bool scaled, bool force, bool skip_short) {
+    for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
+        int s = w.nodes[i];
+        double* out = w.tbl + ((size_t)k * w.N + s) * 16;
+        if (skip_short && w.dist2[s] < 1e-10) continue;
+        if (force || w.dist2[s] > 1e-10) build_pt(w.dist2[s], r, scaled, out);
+        else identity_pt(out);
+    }
+    wsync();
+}
+
+template <typename Real> struct Resc;
+template <> struct Resc<double> {
+    static __device__ __forceinline__ void apply(double* a, int& sc) {
+        double mx = fmax(fmax(a[0], a[1]), fmax(a[2], a[3]));
+        if (mx < 0x1p-256 && mx > 0) {
+            do {
+                for (int j = 0; j < 4; j++) a[j] *= 0x1p256;
+                sc -= 256;
+                mx *= 0x1p256;
+            } while (mx < 0x1p-256);
+        }
+    }
+};
+template <> struct Resc<float> {
+    static __device__ __forceinline__ void apply(float* a, int& sc) {
+        float mx = fmaxf(fmaxf(a[0], a[1]), fmaxf(a[2], a[3]));
+        if (mx < 0x1p-40f && mx > 0) {
+            int e;
+            frexpf(mx, &e);
+            int k = -e;   // scale the max into [0.5, 1)
+            float f1 = ldexpf(1.0f, k / 2), f2 = ldexpf(1.0f, k - k / 2);
+            for (int j = 0; j < 4; j++) a[j] = (a[j] * f1) * f2;
+            sc -= k;
+        }
+    }
+};
+
+// Bottom-up pass over one column held by this lane (Update_Tg without
+// sampling, bpp_c.cpp:647-671): every internal node's partial into the slice.
+// Returns the rescale exponent accumulated over the column; the root partial
+// includes pi.  hdf: a node has data when some leaf below it is a base or an
+// ambiguity code, the complement of Tg == K (bpp_c.hpp:417-428).
+template <typename Real>
+__device__ __forceinline__ int column_up(W<Real>& w, bool act) {
+    int sc = 0;
+    const int lane = w.lane;
+    for (int k = 0; k < w.n_int; k++) {
+        const NodeRec R = w.rec[k];
+        int code0 = 0, code1 = 0;
+        bool h0, h1;
+        if (R.r0 < 0) { code0 = w.stage[R.c0 * 32 + lane]; h0 = code0 != CODE_GAP && code0 != CODE_OTHER; }
+        else h0 = w.hdf[R.r0 * 32 + lane];
+        if (R.r1 < 0) { code1 = w.stage[R.c1 * 32 + lane]; h1 = code1 != CODE_GAP && code1 != CODE_OTHER; }
+        else h1 = w.hdf[R.r1 * 32 + lane];
+        const bool hs = h0 || h1;
+        w.hdf[k * 32 + lane] = hs;
+        Real a[4] = {1, 1, 1, 1};
+        if (act && hs && !R.missing) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int c = q ? R.c1 : R.c0;
+                const int r = q ? R.r1 : R.r0;
+                const int code = q ? code1 : code0;
+                if ((q ? R.m1 : R.m0) || !(q ? h1 : h0)) continue;
+                const Real* Pc = w.ptc + c * 16;
+                if (r < 0) {
+                    if (code < 4) {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) a[j] *= Pc[code * 4 + j];
+                    } else {
+                        int msk = ambig_mask(code - CODE_R);
+                        Real v[4] = {0, 0, 0, 0};
+#pragma unroll
+                        for (int i = 0; i < 4; i++)
+                            if (msk & (1 << i))
+#pragma unroll
+                                for (int j = 0; j < 4; j++) v[j] += Pc[i * 4 + j];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) a[j] *= v[j];
+                    }
+                    w.e_leaf++;
+                } else {
+                    Real x0 = w.PART(r, 0), x1 = w.PART(r, 1), x2 = w.PART(r, 2), x3 = w.PART(r, 3);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        Real v = Pc[j] * x0;
+                        v += Pc[4 + j] * x1;
+                        v += Pc[8 + j] * x2;
+                        v += Pc[12 + j] * x3;
+                        a[j] *= v;
+                    }
+                    w.e_int++;
+                }
+            }
+            Resc<Real>::apply(a, sc);
+        }
+        if (R.is_root)
+#pragma unroll
+            for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
+#pragma unroll
+        for (int j = 0; j < 4; j++) w.PART(k, j) = a[j];
+    }
+    return sc;
+}
+
+// Load the codes of column g of every taxon into this lane's stage slots.
+template <typename Real>
+__device__ __forceinline__ void stage_column(W<Real>& w, int g, bool act) {
+    for (int s = 0; s < w.S; s++) w.stage[s * 32 + w.lane] = act ? w.codes[(size_t)s * w.GGp + g] : (uint8_t)CODE_GAP;
+}
+
+// Per-column log-likelihood accumulated as (FP64 product of root sums) x 2^exponent.
+struct LLAcc {
+    double prod;
+    long long e2;
+    __device__ void init() { prod = 1.0; e2 = 0; }
+    __device__ void add(double t, int sc) {
+        int e;
+        double m = frexp(t, &e);
+        prod *= m;
+        e2 += e + sc;
+        int e3;
+        prod = frexp(prod, &e3);
+        e2 += e3;
+    }
+    __device__ double value() const { return log(prod) + (double)e2 * 0.6931471805599453; }
+};
+
+// Full prune of all columns with the current matrices; returns the summed
+// per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).
+template <typename Real>
+__device__ double likelihood_pass(W<Real>& w) {
+    double acc = 0;
+    LLAcc ll;
+    ll.init();
+    const int rk = w.irank[w.root];
+    for (int g0 = 0; g0 < w.GG; g0 += 32) {
+        int g = g0 + w.lane;
+        bool act = g < w.GG;
+        stage_column(w, g, act);
+        int sc = column_up(w, act);
+        if (act) {
+            double t = (double)w.PART(rk, 0) + (double)w.PART(rk, 1) + (double)w.PART(rk, 2) + (double)w.PART(rk, 3);
+            if (sizeof(Real) == 8) acc += log(t) + (double)sc * 0.6931471805599453;
+            else ll.add(t, sc);
+        }
+    }
+    double v = (sizeof(Real) == 8) ? acc : ll.value();
+    return warp_sum(v);
+}
+
+// Inverse-CDF categorical draw in the partials' precision.
+template <typename Real>
+__device__ __forceinline__ int cat4(const Real* p, double u) {
+    if (sizeof(Real) == 8) return categorical(4, p, u);
+    float tot = ((float)p[0] + (float)p[1]) + ((float)p[2] + (float)p[3]);
+    float t = (float)u * tot;
+    float cum = 0;
+    for (int k = 0; k < 4; k++) {
+        cum += (float)p[k];
+        if (t < cum) return k;
+    }
+    for (int k = 3; k >= 0; k--)
+        if (p[k] > 0) return k;
+    return 4;
+}
+
+// Internal-base pass (Update_Tg with sampling, bpp_c.cpp:672-733) fused with
+// the emission histogram of (child symbol, parent base) pairs.
+template <typename Real>
+__device__ int sample_pass(W<Real>& w, uint64_t pos) {
+    const int NB = NSYM * 4;
+    for (int i = w.lane; i < w.N * NB / 2; i += 32) w.cnt[i] = 0;
+    wsync();
+    int err = 0;
+    const int rk = w.irank[w.root];
+    for (int g0 = 0; g0 < w.GG; g0 += 32) {
+        int g = g0 + w.lane;
+        bool act = g < w.GG;
+        stage_column(w, g, act);
+        column_up(w, act);
+        // top-down sampling
+        uint64_t wp = pos + (act ? (uint64_t)w.prefix[g] : 0);
+        uint64_t blk = ~0ull;
+        uint32_t words[4];
+        auto next_u = [&]() {
+            uint64_t b = wp >> 2;
+            if (b != blk) {
+                philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, words);
+                blk = b;
+            }
+            double u = word_to_uniform(words[wp & 3]);
+            wp++;
+            return u;
+        };
+        if (act) {
+            Real p[4];
+            for (int j = 0; j < 4; j++) p[j] = w.PART(rk, j);
+            int nn = cat4(p, next_u());
+            if (nn > 3) { err = 1; nn = 0; }
+            w.tgv[rk * 32 + w.lane] = (int8_t)nn;
+            w.n_tg++;
+            for (int k = w.n_int - 2; k >= 0; k--) {
+                int s = w.internal[k];
+                bool hs = w.hdf[k * 32 + w.lane];
+                if (w.missing[s] || !hs) { w.tgv[k * 32 + w.lane] = 4; continue; }
+                int tp = w.tgv[w.irank[w.par[s]] * 32 + w.lane];
+                const Real* Ps = w.ptc + s * 16;
+                Real q[4];
+                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4 + tp] * w.PART(k, i);
+                int n2 = cat4(q, next_u());
+                if (n2 > 3) { err = 1; n2 = 0; }
+                w.tgv[k * 32 + w.lane] = (int8_t)n2;
+                w.n_tg++;
+            }
+        }
+        // emission histogram, warp-aggregated
+        for (int i = 0; i < w.n_nodes - 1; i++) {
+            int s = w.nodes[i];
+            if (w.missing[s]) continue;
+            int key = -1;
+            if (act) {
+                int sym;
+                if (s < w.S) {
+                    int code = w.stage[s * 32 + w.lane];
+                    sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
+                } else {
+                    int t = w.tgv[w.irank[s] * 32 + w.lane];
+                    sym = t < 4 ? t : -1;
+                }
+                if (sym >= 0) {
+                    int tp = w.tgv[w.irank[w.par[s]] * 32 + w.lane];
+                    if (tp >= 0 && tp < 4) key = sym * 4 + tp;
+                }
+            }
+            unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (key >= 0 && w.lane == __ffs(peers) - 1) {
+                int bin = s * NB + key;
+                atomicAdd(&w.cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
+            }
+        }
+    }
+    wsync();
+    return warp_or(err);
+}
+
+// Emission sums from the histogram (getEmission, bpp_c2.cpp:355-390).
+template <typename Real>
+__device__ void emission_sums(W<Real>& w) {
+    const int NB = NSYM * 4;
+    for (int t = w.lane; t < (w.n_nodes - 1) * 3; t += 32) {
+        int s = w.nodes[t / 3];
+        int z = t % 3;
+        if (w.missing[s]) continue;
+        const double* P = w.tbl + ((size_t)z * w.N + s) * 16;
+        double e = 0;
+        for (int b = 0; b < NB; b++) {
+            int bin = s * NB + b;
+            unsigned n = (w.cnt[bin >> 1] >> (16 * (bin & 1))) & 0xFFFF;
+            if (!n) continue;
+            int sym = b >> 2, tp = b & 3;
+            double v;
+            if (sym < 4) {
+                v = (sizeof(Real) == 8) ? log(P[sym * 4 + tp]) : (double)logf((float)P[sym * 4 + tp]);
+            } else {
+                int msk = ambig_mask(sym - 4);
+                double tt = 0;
+                for (int q = 0; q < 4; q++)
+                    if (msk & (1 << q)) tt += P[q * 4 + tp];
+                v = (sizeof(Real) == 8) ? log(tt) : (double)logf((float)tt);
+            }
+            e += (double)n * v;
+        }
+        w.emis[s * 3 + z] = e;
+    }
+    wsync();
+}
+
+// Latent-state forward filter (linear FP64, normalised per node) and
+// backward sampling (Update_Z_subtree, bpp_c.cpp:1182-1293).
+template <typename Real>
+__device__ int update_z(W<Real>& w, uint64_t pos) {
+    // transition T[zc][zp] for fixed (fixZ) and free nodes from g, l, l2 (bpp_c.cpp:573-599)
+    const double gr = w.st.gr, lr = w.st.lr, lr2 = w.st.lr2;
+    double Tf[3][3] = {{1 - gr, 0, 0}, {gr, 1, 0}, {0, 0, 0}};
+    double Tn[3][3] = {{1 - gr, 0, 0}, {gr, 1 - lr, lr2}, {0, lr, 1 - lr2}};
+    // node beta := exp(emission - max) with state 2 banned for fixZ nodes
+    for (int i = w.lane; i < w.n_nodes; i += 32) {
+        int s = w.nodes[i];
+        double e0 = w.emis[s * 3 + 0], e1 = w.emis[s * 3 + 1], e2 = w.emis[s * 3 + 2];
+        bool ban = w.fixZ[s] == 1;
+        double mx = e0 > e1 ? e0 : e1;
+        if (!ban && e2 > mx) mx = e2;
+        w.bz[s * 3 + 0] = exp(e0 - mx);
+        w.bz[s * 3 + 1] = exp(e1 - mx);
+        w.bz[s * 3 + 2] = ban ? 0.0 : exp(e2 - mx);
+    }
+    wsync();
+    for (int h = 0; h < w.n_hlev; h++) {
+        int a = w.hlev_start[h], b = w.hlev_start[h + 1];
+        for (int i = a + w.lane; i < b; i += 32) {
+            int p = w.hlev_nodes[i];
+            double v[3] = {w.bz[p * 3 + 0], w.bz[p * 3 + 1], w.bz[p * 3 + 2]};
+            int ch[2] = {w.c2a[p], w.c2b[p]};
+            for (int q = 0; q < 2; q++) {
+                int c = ch[q];
+                const double(*T)[3] = (w.fixZ[c] == 1) ? Tf : Tn;
+                for (int zp = 0; zp < 3; zp++) {
+                    double m = 0;
+                    for (int zc = 0; zc < 3; zc++) m += T[zc][zp] * w.bz[c * 3 + zc];
+                    v[zp] *= m;
+                }
+            }
+            double mx = fmax(v[0], fmax(v[1], v[2]));
+            double inv = mx > 0 ? 1.0 / mx : 1.0;
+            for (int zp = 0; zp < 3; zp++) w.bz[p * 3 + zp] = v[zp] * inv;
+        }
+        wsync();
+    }
+    int err = 0;
+    if (w.lane == 0) {
+        double pr[3] = {0.5 * w.bz[w.root * 3 + 0], 0.5 * w.bz[w.root * 3 + 1], 0.0};
+        uint32_t wd[4];
+        philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
+        int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
+        if (nn > 2) { err = 1; nn = w.Z[w.root]; }
+        w.chg[w.root] = (nn != w.Z[w.root]);
+        w.Z[w.root] = (int8_t)nn;
+    }
+    wsync();
+    for (int d = 0; d < w.n_dlev; d++) {
+        int a = w.dlev_start[d], b = w.dlev_start[d + 1];
+        for (int i = a + w.lane; i < b; i += 32) {
+            int s = w.dlev_nodes[i];
+            int zp = w.Z[w.par[s]];
+            const double(*T)[3] = (w.fixZ[s] == 1) ? Tf : Tn;
+            double pr[3];
+            for (int k = 0; k < 3; k++) pr[k] = T[k][zp] * w.bz[s * 3 + k];
+            uint64_t wq = pos + 1 + (uint64_t)(w.n_nodes - 2 - w.pos[s]);
+            uint32_t wd[4];
+            philox4x32_10((uint32_t)(wq >> 2), (uint32_t)(wq >> 34), 0u, 0u, dM.seed, 0u, wd);
+            int nn = categorical(3, pr, word_to_uniform(wd[wq & 3]));
+            if (nn > 2) { err = 1; nn = w.Z[s]; }
+            w.chg[s] = (nn != w.Z[s]);
+            w.Z[s] = (int8_t)nn;
+        }
+        wsync();
+    }
+    return warp_or(err);
+}
+
+// Flags of proper ancestors (getUpdateNode, bpp_c.cpp:620-642, 836-858).
+// mode 0: of changed nodes; 1: of non-missing Z == 2; 2: of non-missing Z == 1.
+template <typename Real>
+__device__ int ancestors(W<Real>& w, int mode, int8_t* dst) {
+    for (int i = w.lane; i < w.N; i += 32) dst[i] = 0;
+    wsync();
+    for (int i = w.lane; i < w.n_nodes; i += 32) {
+        int s = w.nodes[i];
+        bool f = (mode == 0) ? (w.chg[s] != 0) : (!w.missing[s] && w.Z[s] == (mode == 1 ? 2 : 1));
+        if (!f) continue;
+        int j = w.par[s];
+        while (j >= 0 && j < w.N) {
+            dst[j] = 1;
+            j = w.par[j];
+        }
+    }
+    wsync();
+    return dst[w.root];
+}
+
+__device__ __forceinline__ double bcast(double v) { return __shfl_sync(0xffffffffu, v, 0); }
+__device__ __forceinline__ int bcast(int v) { return __shfl_sync(0xffffffffu, v, 0); }
+__device__ __forceinline__ uint64_t bcast(uint64_t v) {
+    return ((uint64_t)__shfl_sync(0xffffffffu, (unsigned)(v >> 32), 0) << 32) | __shfl_sync(0xffffffffu, (unsigned)v, 0);
+}
+
+// One MH update of the accelerated (neut) or conserved rate (sample_rate,
+// bpp_c.cpp:930-1176; M = 1, adaptive factor 0.5).  Lane 0 draws and decides,
+// the warp evaluates the proposal's likelihood.
+template <typename Real>
+__device__ double mh_rate(W<Real>& w, bool neut, double old_rate, int m) {
+    const double prior_a = neut ? dM.nprior_a : dM.cprior_a;
+    const double prior_b = neut ? dM.nprior_b : dM.cprior_b;
+    const int cls = neut ? C_NEUT : C_CONS;
+    const int resZ = w.st.resZ;
+    int any = ancestors(w, neut ? 1 : 2, w.unv);
+    double cur = old_rate;
+    if (!any) {
+        // no branch of the class: draw from the prior (bpp_c.cpp:940-964)
+        double c0 = old_rate;
+        uint64_t pos = w.st.pos;
+        if (w.lane == 0 && resZ != 0) {
+            StreamReader rd;
+            rd.init(dM.seed, pos);
+            c0 = rd.gamma(prior_a, prior_b);
+            pos = rd.pos;
+            if (neut) {
+                if (dM.ropt == 1 && c0 < dM.nlb) c0 = old_rate;
+                else if (dM.ropt == 2 && c0 < w.trd[TR_C * w.T + m]) c0 = old_rate;
+            } else {
+                if (dM.ropt == 1 && c0 > dM.cub) c0 = old_rate;
+                else if (dM.ropt == 2 && c0 > w.trd[TR_N * w.T + m + 1]) c0 = old_rate;
+            }
+        }
+        cur = bcast(c0);
+        w.st.pos = bcast(pos);
+        if (cur != old_rate) build_table(w, cls, cur, true, false, true);
+    } else {
+        double r = 0, proposal = 0;
+        int skip = 0;
+        uint64_t pos = w.st.pos;
+        if (w.lane == 0) {
+            StreamReader rd;
+            rd.init(dM.seed, pos);
+            r = rd.uniform();
+            if (neut) {
+                proposal = rd.gamma(__ddiv_rn(old_rate, w.st.prop_n), w.st.prop_n);
+                if (dM.ropt == 1 && proposal < dM.nlb) skip = 1;
+                else if (dM.ropt == 2 && proposal < w.trd[TR_C * w.T + m]) skip = 1;
+            } else {
+                double ip = __ddiv_rn(1.0, w.st.prop_c);
+                double u = __dadd_rn(__dmul_rn(r, __dsub_rn(w.st.prop_c, ip)), ip);
+                proposal = __dmul_rn(old_rate, u);
+                if (dM.ropt == 1 && proposal > dM.cub) skip = 1;
+                else if (dM.ropt == 2 && proposal > w.trd[TR_N * w.T + m + 1]) skip = 1;
+            }
+            if (!skip && (proposal < 1e-12 || proposal > 1e8)) skip = 1;
+            pos = rd.pos;
+        }
+        skip = bcast(skip);
+        proposal = bcast(proposal);
+        w.st.pos = bcast(pos);
+        if (!skip) {
+            fill_ptc(w, cls, proposal);
+            double ll_new = likelihood_pass(w);
+            int acc = 0;
+            if (w.lane == 0) {
+                double MH;
+                if (neut)
+                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, w.st.loglik),
+                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                     log_gamma_pdf(old_rate, prior_a, prior_b)),
+                                           log_gamma_pdf(old_rate, __ddiv_rn(proposal, w.st.prop_n), w.st.prop_n)),
+                                   log_gamma_pdf(proposal, __ddiv_rn(old_rate, w.st.prop_n), w.st.prop_n));
+                else
+                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, w.st.loglik),
+                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                     log_gamma_pdf(old_rate, prior_a, prior_b)),
+                                           log(old_rate)),
+                                   log(proposal));
+                acc = log(r) < MH;
+            }
+            acc = bcast(acc);
+            if (acc) {
+                cur = proposal;
+                w.st.loglik = ll_new;
+                build_table(w, cls, cur, true, false, true);
+            }
+        }
+    }
+    if (cur != old_rate) { if (neut) w.st.acc_n++; else w.st.acc_c++; }
+    // adaptive proposal scale (bpp_c.cpp:1145-1171); every lane computes the same values
+    if ((m + 1) % dM.adapt_freq == 0) {
+        int blocks = (m + 1) / dM.adapt_freq;
+        double step = fmin(0.5, 1 / sqrt((double)blocks));
+        double scale_adj;
+        if (neut) {
+            double rate = (double)w.st.acc_n / dM.adapt_freq;
+            scale_adj = rate > 0.44 ? exp(step) : (rate < 0.23 ? exp(-step) : 1.0);
+            w.st.prop_n = __dmul_rn(w.st.prop_n, scale_adj);
+            if (w.st.prop_n > 1) w.st.prop_n = 1;
+            w.st.acc_n = 0;
+        } else {
+            double rate = (double)w.st.acc_c / dM.adapt_freq;
+            scale_adj = rate > 0.44 ? exp(step) : (rate < 0.23 ? exp(-step) : 1.0);
+            w.st.prop_c = pow(w.st.prop_c, scale_adj);
+            if (w.st.prop_c < 1.0001) w.st.prop_c = 1.0001;
+            w.st.acc_c = 0;
+        }
+    }
+    return cur;
+}
+
+// Prior of a Z configuration (bpp_c2.cpp:131-163).
+template <typename Real>
+__device__ double prior_config(W<Real>& w, const int8_t* z) {
+    double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int k = 0; k + 1 < w.n_nodes; k++) {
+        int s = w.nodes[k];
+        nZ[z[s]][z[w.par[s]]] += 1;
+    }
+    double pz = lnbeta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]) - lnbeta(dM.ga, dM.gb);
+    for (int k = 0; k + 1 < w.n_nodes; k++) {
+        int s = w.nodes[k];
+        if (w.fixZ[s] == 1) nZ[z[s]][z[w.par[s]]] -= 1;
+    }
+    pz += lnbeta(dM.la + nZ[2][1], dM.lb + nZ[1][1]) - lnbeta(dM.la, dM.lb);
+    if (dM.l2a > 0) pz += lnbeta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]) - lnbeta(dM.l2a, dM.l2b);
+    pz += (z[w.root] == 2) ? -CUDART_INF : log(0.5);
+    return pz;
+}
+
+// Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353) by one warp.
+template <typename Real>
+__device__ double eval2(W<Real>& w, char* gws, int* n_conf_out) {
+    const int burn = w.burn, mcmc = w.mcmc, T = w.T, N = w.N;
+    const int resZ = w.st.resZ;
+    GrpLayout G = GrpLayout::make(mcmc);
+    uint64_t* hash = (uint64_t*)(gws + G.hash);
+    int32_t* rep = (int32_t*)(gws + G.rep);
+    int32_t* cfg = (int32_t*)(gws + G.cfg);
+    int32_t* nxt = (int32_t*)(gws + G.nxt);
+    int32_t* head = (int32_t*)(gws + G.head);
+    int32_t* first = (int32_t*)(gws + G.first);
+    double* CNT = (double*)(gws + G.cstat);
+    double* VC = CNT + (mcmc + 2);
+    double* MC = VC + (mcmc + 2);
+    double* VN = MC + (mcmc + 2);
+    double* MN = VN + (mcmc + 2);
+    double* CV = MN + (mcmc + 2);
+    double* SF = CV + (mcmc + 2);
+    double* LD = SF + (mcmc + 2);
+    const int8_t* Zm = w.smaxz;
+    int8_t* unc = w.mask;
+    for (int s = w.lane; s < N; s += 32) {
+        int c = 0;
+        for (int i = burn; i < T; i++) c += (w.trz[(size_t)i * N + s] == Zm[s]);
+        unc[s] = c < mcmc;
+    }
+    wsync();
+    for (int i = burn + w.lane; i <= T; i += 32) {
+        const int8_t* z = (i < T) ? w.trz + (size_t)i * N : Zm;
+        uint64_t h = 0xcbf29ce484222325ull;
+        for (int s = 0; s < N; s++)
+            if (unc[s]) h = fnv_step(h, (uint8_t)z[s]);
+        hash[i - burn] = h;
+    }
+    wsync();
+    auto same = [&](const int8_t* a, const int8_t* b) {
+        for (int s = 0; s < N; s++)
+            if (unc[s] && a[s] != b[s]) return false;
+        return true;
+    };
+    for (int i = burn + w.lane; i < T; i += 32) {
+        const int8_t* zi = w.trz + (size_t)i * N;
+        uint64_t hi = hash[i - burn];
+        int r = i;
+        for (int j = T - 1; j > i; j--)
+            if (hash[j - burn] == hi && same(w.trz + (size_t)j * N, zi)) { r = j; break; }
+        rep[i - burn] = r;
+        cfg[i - burn] = (hi == hash[T - burn] && same(zi, Zm)) ? -2 : -1;
+    }
+    wsync();
+    int nconf = 1;
+    if (w.lane == 0) {
+        first[0] = -1;
+        for (int i = T - 1; i >= burn; i--) {
+            int k = i - burn;
+            int j;
+            if (cfg[k] == -2) j = 0;
+            else if (rep[k] == i) { j = nconf++; first[j] = i; }
+            else j = cfg[rep[k] - burn];
+            cfg[k] = j;
+        }
+        for (int j = 0; j < nconf; j++) head[j] = -1;
+        for (int i = burn; i < T; i++) {
+            int k = i - burn;
+            nxt[k] = head[cfg[k]];
+            head[cfg[k]] = k;
+        }
+    }
+    nconf = bcast(nconf);
+    __syncwarp();
+    *n_conf_out = nconf;
+    const double* trN = w.trd + TR_N * T;
+    const double* trC = w.trd + TR_C * T;
+    const double* trF = w.trd + TR_FULL * T;
+    for (int j = w.lane; j < nconf; j += 32) {
+        double n = 0, vc = 0, mc = 0, vn = 0, mn = 0, cv = 0, sf = 0;
+        for (int k = head[j]; k >= 0; k = nxt[k]) {
+            int i = k + burn;
+            n += 1;
+            vc = __dadd_rn(vc, __dmul_rn(trC[i], trC[i]));
+            mc = __dadd_rn(mc, trC[i]);
+            if (resZ != 0) {
+                vn = __dadd_rn(vn, __dmul_rn(trN[i], trN[i]));
+                mn = __dadd_rn(mn, trN[i]);
+                cv = __dadd_rn(cv, __dmul_rn(trC[i], trN[i]));
+            }
+            sf = __dadd_rn(sf, __ddiv_rn(trF[i], (double)mcmc));
+        }
+        CNT[j] = n; VC[j] = vc; MC[j] = mc; VN[j] = vn; MN[j] = mn; CV[j] = cv; SF[j] = sf;
+        LD[j] = 0;
+        double wgt = n / mcmc;
+        if (wgt < 0.02) continue;
+        const int8_t* z = (j == 0) ? Zm : w.trz + (size_t)first[j] * N;
+        double pz = prior_config(w, z);
+        SF[j] = __dadd_rn(SF[j], __ddiv_rn(__dmul_rn(n, pz), (double)mcmc));
+        double ld;
+        if (resZ == 0) {
+            ld = __dsub_rn(log(__dsub_rn(vc, __ddiv_rn(__dmul_rn(mc, mc), n))), log(n));
+        } else {
+            double a = __dsub_rn(vc, __ddiv_rn(__dmul_rn(mc, mc), n));
+            double b = __dsub_rn(vn, __ddiv_rn(__dmul_rn(mn, mn), n));
+            double cov = __dsub_rn(cv, __ddiv_rn(__dmul_rn(mn, mc), n));
+            ld = __dsub_rn(log(__dsub_rn(__dmul_rn(a, b), __dmul_rn(cov, cov))), __dmul_rn(2.0, log(n)));
+        }
+        LD[j] = ld;
+    }
+    __syncwarp();
+    double VB = 0;
+    int eff = 0;
+    if (w.lane == 0) {
+        for (int j = 0; j < nconf; j++) {
+            double wgt = CNT[j] / mcmc;
+            if (wgt < 0.02) continue;
+            if (isnan(LD[j])) continue;
+            eff += (int)CNT[j];
+            VB = __dsub_rn(VB, __dmul_rn(wgt, log(CNT[j])));
+            VB = __dadd_rn(VB, SF[j]);
+            VB = __dadd_rn(VB, __ddiv_rn(__dmul_rn(__dmul_rn(0.5, LD[j]), CNT[j]), (double)mcmc));
+        }
+    }
+    eff = bcast(eff);
+    VB = bcast(VB);
+    if (eff == 0) {
+        // fallback: prune each configuration at the mean rates (bpp_c2.cpp:199-316)
+        double varn = 0, varc = 0, cov = 0, meann = 0, meanc = 0;
+        for (int j = 0; j < nconf; j++) {
+            varc = __dadd_rn(varc, VC[j]);
+            meanc = __dadd_rn(meanc, MC[j]);
+            if (resZ != 0) { meann = __dadd_rn(meann, MN[j]); varn = __dadd_rn(varn, VN[j]); cov = __dadd_rn(cov, CV[j]); }
+        }
+        double rn = meann / mcmc, rc = meanc / mcmc;
+        build_table(w, C_CONS, rc, true, true, false);
+        if (resZ != 0) build_table(w, C_NEUT, rn, true, true, false);
+        for (int j = 0; j < nconf; j++) {
+            const int8_t* z = (j == 0) ? Zm : w.trz + (size_t)first[j] * N;
+            for (int s = w.lane; s < N; s += 32) w.Z[s] = z[s];
+            wsync();
+            double pz = prior_config(w, z);
+            fill_ptc(w, -1, 0.0);
+            double ll = likelihood_pass(w);
+            if (w.lane == 0) SF[j] = __dadd_rn(ll, pz);
+        }
+        __syncwarp();
+        double v = 0;
+        if (w.lane == 0) {
+            double mx = SF[0];
+            for (int j = 1; j < nconf; j++) if (SF[j] > mx) mx = SF[j];
+            if (mx == -CUDART_INF) v = -CUDART_INF;
+            else {
+                double sm = 0;
+                for (int j = 0; j < nconf; j++) sm = __dadd_rn(sm, exp(__dsub_rn(SF[j], mx)));
+                v = __dadd_rn(log(sm), mx);
+            }
+            v = __dadd_rn(v, log_gamma_pdf(rc, dM.cprior_a, dM.cprior_b));
+            if (resZ != 0) v = __dadd_rn(v, log_gamma_pdf(rn, dM.nprior_a, dM.nprior_b));
+            double logdet;
+            if (resZ == 0) {
+                varc = __dsub_rn(varc, __ddiv_rn(__dmul_rn(meanc, meanc), (double)mcmc));
+                logdet = __dsub_rn(log(varc), log((double)mcmc));
+                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), __dmul_rn(0.5, log(2 * CUDART_PI))));
+            } else {
+                varn = __dsub_rn(varn, __ddiv_rn(__dmul_rn(meann, meann), (double)mcmc));
+                varc = __dsub_rn(varc, __ddiv_rn(__dmul_rn(meanc, meanc), (double)mcmc));
+                cov = __dsub_rn(cov, __ddiv_rn(__dmul_rn(meann, meanc), (double)mcmc));
+                logdet = __dsub_rn(log(__dsub_rn(__dmul_rn(varc, varn), __dmul_rn(cov, cov))),
+                                   __dmul_rn(2.0, log((double)mcmc)));
+                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), log(2 * CUDART_PI)));
+            }
+        }
+        VB = bcast(v);
+    } else {
+        double f = (double)mcmc / eff;
+        if (resZ != 0) VB = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(VB, f), log((double)mcmc)), log(2 * CUDART_PI)), 1.0);
+        else VB = __dadd_rn(__dadd_rn(__dmul_rn(VB, f), log((double)mcmc)), __dmul_rn(0.5, __dadd_rn(log(2 * CUDART_PI), 1.0)));
+    }
+    return VB;
+}
+
+// Element of rank T/2 under std::sort's order (bpp_c2.cpp:742-755).
+__device__ double warp_median(const double* x, int T) {
+    int target = T / 2;
+    double found = 0;
+    int hit = 0;
+    for (int i = threadIdx.x & 31; i < T; i += 32) {
+        double v = x[i];
+        int r = 0;
+        for (int j = 0; j < T; j++) {
+            double u = x[j];
+            r += (u < v) || (u == v && j < i);
+        }
+        if (r == target) { found = v; hit = 1; }
+    }
+    unsigned b = __ballot_sync(0xffffffffu, hit);
+    return __shfl_sync(0xffffffffu, found, __ffs(b) - 1);
+}
+
+// initMCMC for model w.st.mi (bpp_c.cpp:131-343) followed by the initial full prune.
+template <typename Real>
+__device__ void init_model(W<Real>& w) {
+    const int resZ = w.st.resZ;
+    for (int i = w.lane; i < w.N; i += 32) { w.Z[i] = -1; w.fixZ[i] = -1; }
+    wsync();
+    for (int i = w.lane; i < w.n_nodes; i += 32) {
+        int s = w.nodes[i];
+        w.Z[s] = (s == w.root) ? 0 : 1;
+        if (w.upc[s] || s == w.root) w.fixZ[s] = 1;
+        if (resZ == 2 && w.upcc[s]) w.fixZ[s] = 1;
+        if (resZ == 0 && s != w.root) w.fixZ[s] = 1;
+    }
+    wsync();
+    w.st.prop_c = 1.2;
+    w.st.prop_n = (double)1 / w.GG * 10;
+    w.st.maxll = -CUDART_INF;
+    w.st.max_m = 0;
+    w.st.m = 0;
+    w.st.rate_n = dM.init_n;
+    w.st.rate_c = dM.init_c;
+    w.st.gr = dM.init_g;
+    w.st.lr = dM.init_l;
+    w.st.lr2 = (dM.l2a == 0) ? 0.0 : dM.init_l2;
+    if (w.lane == 0) {
+        w.trd[TR_N * w.T] = w.st.rate_n;
+        w.trd[TR_C * w.T] = w.st.rate_c;
+        w.trd[TR_G * w.T] = w.st.gr;
+        w.trd[TR_L * w.T] = w.st.lr;
+        w.trd[TR_L2 * w.T] = w.st.lr2;
+    }
+    build_table(w, C_NULL, 1.0, false, false, false);
+    build_table(w, C_NEUT, dM.init_n, true, false, false);
+    build_table(w, C_CONS, dM.init_c, true, false, false);
+    fill_ptc(w, -1, 0.0);
+    w.st.loglik = likelihood_pass(w);
+    w.st.phase = PH_RUN;
+}
+
+template <typename Real>
+__device__ void write_slot_z(W<Real>& w) {
+    for (int i = w.lane; i < w.N; i += 32) w.sZ[i] = w.Z[i];
+}
+
+// ---------------------------------------------------------------------------
+// kernel
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int N = dM.N, S = dM.S;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    WarpSmem<Real> L = WarpSmem<Real>::make(N, P.n_int_max, S);
+    TopoLayout TL = TopoLayout::make(N);
+    unsigned char* base = smem + (size_t)wid * L.total;
+    W<Real> w;
+    w.lane = lane;
+    w.S = S;
+    w.N = N;
+    w.burn = dM.burnin;
+    w.mcmc = dM.mcmc;
+    w.T = dM.burnin + dM.mcmc;
+    w.ptc = (Real*)(base + L.ptc);
+    w.part = (Real*)(base + L.part);
+    w.emis = (double*)(base + L.part);
+    w.bz = w.emis + (size_t)N * 3;
+    w.tgv = (int8_t*)(base + L.tgv);
+    w.hdf = (int8_t*)(base + L.hdf);
+    NodeRec* recw = (NodeRec*)(base + L.rec);
+    w.rec = recw;
+    w.stage = (uint8_t*)(base + L.stage);
+    w.cnt = (unsigned*)(base + L.cnt);
+    int16_t* t16 = (int16_t*)(base + L.topo);
+    w.nodes = t16 + TL.nodes; w.internal = t16 + TL.internal; w.c2a = t16 + TL.c2a; w.c2b = t16 + TL.c2b;
+    w.par = t16 + TL.par; w.irank = t16 + TL.irank; w.pos = t16 + TL.pos; w.missing = t16 + TL.missing;
+    w.upc = t16 + TL.upc; w.upcc = t16 + TL.upcc; w.hlev_start = t16 + TL.hlev_start;
+    w.hlev_nodes = t16 + TL.hlev_nodes; w.dlev_start = t16 + TL.dlev_start; w.dlev_nodes = t16 + TL.dlev_nodes;
+    int8_t* f8 = (int8_t*)(base + L.i8);
+    w.fixZ = f8; w.chg = f8 + N; w.unv = f8 + 2 * N; w.mask = f8 + 3 * N; w.Z = f8 + 5 * N;
+    w.dist2 = (double*)(base + L.dbl);
+    w.scr = w.dist2 + N;
+    const int gw = blockIdx.x * nw + wid;
+    const int n_gw = gridDim.x * nw;
+    char* gws = P.grp_ws + (size_t)gw * P.grp_ws_stride;
+    const SlotLayout SL = SlotLayout::make(N, w.T);
+    const int TI = dM.trace_iters < w.T ? dM.trace_iters : w.T;
+    const int resZ_of[3] = {0, 2, 1};
+    (void)n_gw;
+    for (;;) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(P.next_slot, 1);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= P.n_slots) break;
+        SlotState* sp = P.slots + slot;
+        w.st = *sp;
+        if (w.st.phase == PH_DONE || w.st.phase == PH_EMPTY || w.st.elem < 0) continue;
+        const int e = w.st.elem;
+        const ElemHeader& H = P.hdr[e];
+        w.GG = H.GG; w.GGp = H.GGp; w.root = H.root; w.n_nodes = H.n_nodes; w.n_int = H.n_int;
+        w.n_hlev = H.n_hlev; w.n_dlev = H.n_dlev; w.tg_draws = H.tg_draws;
+        w.codes = P.blob + H.codes_off;
+        w.prefix = (const int32_t*)(P.blob + H.prefix_off);
+        {
+            const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
+            for (int i = lane; i < TL.total; i += 32) t16[i] = topo[i];
+            const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
+            for (int i = lane; i < N; i += 32) w.dist2[i] = d2[i];
+        }
+        wsync();
+        for (int k = lane; k < w.n_int; k += 32) {
+            int s = w.internal[k];
+            NodeRec R;
+            R.c0 = w.c2a[s];
+            R.c1 = w.c2b[s];
+            R.r0 = R.c0 >= S ? w.irank[R.c0] : -1;
+            R.r1 = R.c1 >= S ? w.irank[R.c1] : -1;
+            R.m0 = (int8_t)w.missing[R.c0];
+            R.m1 = (int8_t)w.missing[R.c1];
+            R.missing = (int8_t)w.missing[s];
+            R.is_root = (s == w.root);
+            R.pad = 0;
+            recw[k] = R;
+        }
+        char* sw = P.slot_ws + (size_t)slot * P.slot_ws_stride;
+        w.sZ = (int8_t*)(sw + SL.Z);
+        w.smaxz = (int8_t*)(sw + SL.maxz);
+        w.tbl = (double*)(sw + SL.tbl);
+        w.trz = (int8_t*)(sw + SL.trz);
+        w.trd = (double*)(sw + SL.trd);
+        w.e_int = w.e_leaf = w.n_tg = 0;
+        for (int q = 0; q < 8; q++) w.ph[q] = 0;
+        w.t0 = clock64();
+        if (w.st.phase == PH_INIT && w.st.mi == 0 && lane == 0) w.st.start_clock = clock64();
+        // restore Z / fixZ of a running model
+        if (w.st.phase == PH_RUN) {
+            for (int i = lane; i < N; i += 32) { w.Z[i] = w.sZ[i]; w.fixZ[i] = -1; }
+            wsync();
+            const int resZ = w.st.resZ;
+            for (int i = lane; i < w.n_nodes; i += 32) {
+                int s = w.nodes[i];
+                if (w.upc[s] || s == w.root) w.fixZ[s] = 1;
+                if (resZ == 2 && w.upcc[s]) w.fixZ[s] = 1;
+                if (resZ == 0 && s != w.root) w.fixZ[s] = 1;
+            }
+        }
+        wsync();
+        int budget = P.sweeps > 0 ? P.sweeps : 0x7fffffff;
+        int errs = 0;
+        while (budget > 0 && w.st.phase != PH_DONE) {
+            if (w.st.phase == PH_INIT) {
+                w.st.resZ = resZ_of[w.st.mi];
+                init_model(w);
+                PHASE(7);
+            }
+            const int m = w.st.m;
+            const int T = w.T;
+            // MonitorChain (bpp_c.cpp:741-834)
+            for (int i = lane; i < N; i += 32) w.trz[(size_t)m * N + i] = w.Z[i];
+            double full = w.st.loglik + 0.0;
+            full += log_gamma_pdf(w.trd[TR_C * T + m], dM.cprior_a, dM.cprior_b);
+            if (w.st.resZ != 0) full += log_gamma_pdf(w.trd[TR_N * T + m], dM.nprior_a, dM.nprior_b);
+            if (lane == 0) { w.trd[TR_LL * T + m] = w.st.loglik; w.trd[TR_FULL * T + m] = full; }
+            if (m >= w.burn && full > w.st.maxll) {
+                w.st.maxll = full;
+                w.st.max_m = m;
+                for (int i = lane; i < N; i += 32) w.smaxz[i] = w.Z[i];
+            }
+            wsync();
+            if (m == T - 1) {
+                // end of the model: Eval2 and the output row (bpp_c2.cpp:14-353, 739-785)
+                const int mi = w.st.mi;
+                DevModelResult& MR = P.results[e].model[mi];
+                if (TI > 0 && P.tr_d) {
+                    double* td = P.tr_d + ((size_t)e * 3 + mi) * 6 * TI;
+                    const int rows[6] = {TR_LL, TR_N, TR_C, TR_G, TR_L, TR_L2};
+                    for (int i = lane; i < 6 * TI; i += 32) td[i] = w.trd[rows[i / TI] * T + (i % TI)];
+                    int8_t* tz = P.tr_z + ((size_t)e * 3 + mi) * TI * N;
+                    for (int i = lane; i < TI * N; i += 32) tz[i] = w.trz[i];
+                }
+                __syncwarp();
+                int nconf = 0;
+                double vb = eval2(w, gws, &nconf);
+                const int mrow[5] = {TR_N, TR_C, TR_G, TR_L, TR_L2};
+                double med[5];
+                for (int q = 0; q < 5; q++) med[q] = warp_median(w.trd + mrow[q] * T, T);
+                if (lane == 0) {
+                    MR.loglik = vb;
+                    MR.max_loglik = w.st.maxll;
+                    for (int q = 0; q < 5; q++) MR.rates[q] = med[q];
+                    MR.failure = isnan(vb) ? 1 : 0;
+                    MR.n_configs = nconf;
+                }
+                if (isnan(vb)) w.st.status |= 2;
+                int32_t* mz = P.max_z + ((size_t)e * 3 + mi) * N;
+                for (int s = lane; s < N; s += 32) mz[s] = w.smaxz[s];
+                double* pz = P.post_z + ((size_t)e * 3 + mi) * N * 4;
+                for (int s = lane; s < N; s += 32) {
+                    int c4[4] = {0, 0, 0, 0};
+                    for (int i = w.burn; i < T; i++) {
+                        int z = w.trz[(size_t)i * N + s];
+                        if (z >= -1 && z <= 2) c4[z + 1]++;
+                    }
+                    if (w.missing[s]) c4[0] = w.mcmc;
+                    for (int k = 0; k < 4; k++) pz[s * 4 + k] = (double)c4[k] / w.mcmc;
+                }
+                PHASE(7);
+                w.st.mi++;
+                w.st.phase = (w.st.mi == 3) ? PH_DONE : PH_INIT;
+                if (w.st.phase == PH_DONE && lane == 0) {
+                    P.results[e].status = (w.st.status & 1) ? 3 : ((w.st.status & 2) ? 2 : 0);
+                    P.results[e].device_ms = (double)(clock64() - w.st.start_clock);
+                    atomicAdd(P.n_done, 1);
+                }
+                __syncwarp();
+                continue;
+            }
+            PHASE(6);
+            // internal bases + emission histogram with the matrices of the current Z
+            fill_ptc(w, -1, 0.0);
+            uint64_t pos = w.st.pos;
+            errs |= sample_pass(w, pos);
+            pos += (uint64_t)w.tg_draws;
+            PHASE(0);
+            emission_sums(w);
+            // missing nodes keep fixed emissions (bpp_c.hpp:451-474); the root has none
+            for (int i = lane; i < N; i += 32) {
+                if (w.missing[i]) { w.emis[i * 3 + 0] = 0; w.emis[i * 3 + 1] = log(dM.cons_to_mis); w.emis[i * 3 + 2] = 0; }
+            }
+            if (lane == 0) { w.emis[w.root * 3 + 0] = 0; w.emis[w.root * 3 + 1] = 0; w.emis[w.root * 3 + 2] = 0; }
+            wsync();
+            PHASE(1);
+            errs |= update_z(w, pos);
+            pos += (uint64_t)w.n_nodes;
+            w.st.pos = pos;
+            PHASE(2);
+            // log-likelihood under the new Z when a branch changed (bpp_c.cpp:419-431)
+            if (ancestors(w, 0, w.unv)) {
+                fill_ptc(w, -1, 0.0);
+                w.st.loglik = likelihood_pass(w);
+            }
+            PHASE(3);
+            // rates (bpp_c.cpp:434-452)
+            double rn = mh_rate(w, true, w.trd[TR_N * T + m], m);
+            if (lane == 0) w.trd[TR_N * T + m + 1] = rn;
+            __syncwarp();
+            PHASE(4);
+            double rc = mh_rate(w, false, w.trd[TR_C * T + m], m);
+            if (lane == 0) w.trd[TR_C * T + m + 1] = rc;
+            PHASE(5);
+            w.st.rate_n = rn;
+            w.st.rate_c = rc;
+            // transitions (sample_transition, bpp_c.cpp:522-613)
+            double gr = 0, lr = 0, lr2 = 0;
+            uint64_t p2 = w.st.pos;
+            if (lane == 0) {
+                double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                for (int k = 0; k + 1 < w.n_nodes; k++) {
+                    int s = w.nodes[k];
+                    nZ[w.Z[s]][w.Z[w.par[s]]] += 1;
+                }
+                StreamReader rd;
+                rd.init(dM.seed, p2);
+                gr = rd.beta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]);
+                for (int k = 0; k + 1 < w.n_nodes; k++) {
+                    int s = w.nodes[k];
+                    if (w.fixZ[s] == 1) nZ[w.Z[s]][w.Z[w.par[s]]] -= 1;
+                }
+                lr = rd.beta(dM.la + nZ[2][1], dM.lb + nZ[1][1]);
+                lr2 = (dM.l2a == 0) ? 0.0 : rd.beta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]);
+                p2 = rd.pos;
+                w.trd[TR_G * T + m + 1] = gr;
+                w.trd[TR_L * T + m + 1] = lr;
+                w.trd[TR_L2 * T + m + 1] = lr2;
+            }
+            w.st.gr = bcast(gr);
+            w.st.lr = bcast(lr);
+            w.st.lr2 = bcast(lr2);
+            w.st.pos = bcast(p2);
+            w.st.m = m + 1;
+            w.st.iters++;
+            budget--;
+            __syncwarp();
+        }
+        if (errs) w.st.status |= 1;
+        write_slot_z(w);
+        if (lane == 0) *sp = w.st;
+        unsigned long long ei = w.e_int, el = w.e_leaf, nt = w.n_tg;
+        for (int o = 16; o > 0; o >>= 1) {
+            ei += __shfl_xor_sync(0xffffffffu, ei, o);
+            el += __shfl_xor_sync(0xffffffffu, el, o);
+            nt += __shfl_xor_sync(0xffffffffu, nt, o);
+        }
+        if (lane == 0 && P.counters) {
+            for (int q = 0; q < 8; q++) atomicAdd(&P.counters->phase_cycles[q], w.ph[q]);
+            atomicAdd(&P.counters->edge_internal, ei);
+            atomicAdd(&P.counters->edge_leaf, el);
+            atomicAdd(&P.counters->tg_draws, nt);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-callable pieces
+// ---------------------------------------------------------------------------
+cudaError_t set_model_batch(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
+
+size_t batch_warp_smem(int N, int NI, int S, int prec) {
+    return prec == 0 ? WarpSmem<double>::make(N, NI, S).total : WarpSmem<float>::make(N, NI, S).total;
+}
+size_t batch_slot_bytes(int N, int T) { return SlotLayout::make(N, T).total; }
+size_t batch_grp_bytes(int mcmc) { return GrpLayout::make(mcmc).total; }
+size_t batch_state_bytes() { return sizeof(SlotState); }
+
+// Slot states for a fresh batch: slot i runs element elem[i].
+__global__ void init_slots_kernel(SlotState* s, const int32_t* elem, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    SlotState z;
+    memset(&z, 0, sizeof(z));
+    z.elem = elem[i];
+    z.phase = elem[i] < 0 ? PH_EMPTY : PH_INIT;
+    s[i] = z;
+}
+
+cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st) {
+    init_slots_kernel<<<(n + 127) / 128, 128, 0, st>>>((SlotState*)slots, elem, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, cudaStream_t st) {
+    const BatchParams& p = *(const BatchParams*)params;
+    if (prec == 0) {
+        cudaFuncSetAttribute(batch_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        batch_kernel<double><<<grid, warps * 32, smem, st>>>(p);
+    } else {
+        cudaFuncSetAttribute(batch_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        batch_kernel<float><<<grid, warps * 32, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+size_t batch_params_bytes() { return sizeof(BatchParams); }
+
+}  // namespace pacc

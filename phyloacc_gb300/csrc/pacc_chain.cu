@@ -26,12 +26,10 @@
 #include <math_constants.h>
 #include <stdint.h>
 
-#include "pacc_dev.h"
-#include "pacc_rng.cuh"
+#include "pacc_common.cuh"
 
 namespace pacc {
 
-__constant__ DevModel dM;
 
 // Workspace carve-up (per CTA).
 struct WsLayout {
@@ -81,6 +79,10 @@ struct ChainScalars {
     int fallback;
 };
 
+// Reduction scratch: one slot per warp (<= 32), the broadcast slot RED_SUM
+// and the median slot RED_MED.
+static const int RED_SUM = 32, RED_MED = 33, RED_SLOTS = 40;
+
 // Shared-memory layout (dynamic, sized by N).
 template <typename Real>
 struct SmemLayout {
@@ -95,7 +97,7 @@ struct SmemLayout {
         s.emis = o; o = al(o + (size_t)N * 3 * 8);
         s.beta = o; o = al(o + (size_t)N * 3 * 8);
         s.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 4);                    // emission histogram
-        s.red = o; o = al(o + (size_t)(BT / 32 + 2) * 8 * 2);
+        s.red = o; o = al(o + (size_t)RED_SLOTS * 8);                        // reduction scratch
         s.i16 = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
         s.i8 = o; o = al(o + (size_t)N * 8);                               // Z fixZ changed unv unvN unvC cur maxz
         s.total = o;
@@ -104,6 +106,7 @@ struct SmemLayout {
 };
 
 enum { P_NULL = 0, P_CONS = 1, P_NEUT = 2, P_PROP = 3 };
+
 
 // ---------------------------------------------------------------------------
 // Small helpers
@@ -119,10 +122,10 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
     if (threadIdx.x == 0) {
         int nw = blockDim.x >> 5;
         for (int i = 0; i < nw; i++) r += red[i];
-        red[31] = r;
+        red[RED_SUM] = r;
     }
     __syncthreads();
-    r = red[31];
+    r = red[RED_SUM];
     __syncthreads();
     return r;
 }
@@ -136,45 +139,6 @@ __device__ __forceinline__ int block_or(int v, int* tmp) {
     int r = *tmp;
     __syncthreads();
     return r;
-}
-
-// Gamma(shape a, scale b) density and its log as the reference takes it (bpp_c.cpp:784,1046).
-__device__ double gamma_pdf(double x, double a, double b) {
-    if (x < 0) return 0.0;
-    if (x == 0) return (a == 1) ? 1.0 / b : 0.0;
-    double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, log(x)), __ddiv_rn(x, b)), lgamma(a)),
-                         __dmul_rn(a, log(b)));
-    return exp(t);
-}
-__device__ __forceinline__ double log_gamma_pdf(double x, double a, double b) { return log(gamma_pdf(x, a, b)); }
-__device__ __forceinline__ double lnbeta(double a, double b) {
-    return __dsub_rn(__dadd_rn(lgamma(a), lgamma(b)), lgamma(__dadd_rn(a, b)));
-}
-
-// P^T(d*r) = eigeninv * diag(exp(lambda*d*r)) * eigenvec  (bpp.hpp:375-380), FP64.
-// scaled=false uses exp(lambda*d) as the null-rate cache does (bpp.hpp:375).
-__device__ void build_pt(double d, double r, bool scaled, double* out) {
-    double e[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        double x = __dmul_rn(dM.lam[i], d);
-        if (scaled) x = __dmul_rn(x, r);
-        e[i] = exp(x);
-    }
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            double s = 0;
-#pragma unroll
-            for (int i = 0; i < 4; i++) s = __dadd_rn(s, __dmul_rn(dM.einv[a * 4 + i], __dmul_rn(dM.evec[i * 4 + b], e[i])));
-            out[a * 4 + b] = s;
-        }
-}
-
-__device__ void identity_pt(double* out) {
-#pragma unroll
-    for (int a = 0; a < 16; a++) out[a] = ((a >> 2) == (a & 3)) ? 1.0 : 0.0;
 }
 
 // Exact rescale by a power of two when the largest entry is small.
@@ -507,7 +471,7 @@ __device__ void emission(Ctx<Real>& c) {
                 }
                 if (sym >= 0) {
                     int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
-                    key = sym * 4 + tp;
+                    if (tp >= 0 && tp < 4) key = sym * 4 + tp;
                 }
             }
             unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -633,7 +597,7 @@ __device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int
         else f = !c.missing[s] && c.Z[s] == (mode == 1 ? 2 : 1);
         if (!f) continue;
         int j = c.par[s];
-        while (j != c.N) {
+        while (j >= 0 && j < c.N) {
             dst[j] = 1;
             j = c.par[j];
         }
@@ -791,17 +755,14 @@ __device__ double median_of(const double* x, int T, double* red) {
             eqb += (u == v && j < i);
         }
         int r = lt + eqb;
-        if (r == target) red[30] = v;
+        if (r == target) red[RED_MED] = v;
     }
     __syncthreads();
-    double r = red[30];
+    double r = red[RED_MED];
     __syncthreads();
     return r;
 }
 
-__device__ __forceinline__ uint64_t fnv_step(uint64_t h, uint8_t b) {
-    return (h ^ b) * 0x100000001b3ull;
-}
 
 // Prior of a Z configuration (bpp_c2.cpp:131-163): Beta-Binomial terms + root prior.
 template <typename Real>

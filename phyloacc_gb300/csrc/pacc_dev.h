@@ -106,6 +106,18 @@ struct DevResult {
 // Work counters accumulated by the kernel (atomicAdd per CTA per element).
 struct DevCounters {
     unsigned long long edge_internal, edge_leaf, col_ll, tg_draws, z_draws, pmat, iters;
+    unsigned long long phase_cycles[8];  // batched kernel: cycles per phase (summed over warps)
+};
+
+// One internal node of the pruned tree, in postorder, as the batched kernel
+// reads it (one 16-byte shared-memory load per node and column).
+struct NodeRec {
+    int16_t c0, c1;      // child node ids
+    int16_t r0, r1;      // internal rank of a child (-1 for a leaf)
+    int8_t m0, m1;       // child missing (skipped by the prune)
+    int8_t missing;      // this node missing
+    int8_t is_root;
+    int32_t pad;
 };
 
 // Parameters of one chain-kernel launch.
@@ -123,6 +135,43 @@ struct ChainParams {
     size_t ws_stride;
     int n_int_max, GGp_max;
     DevCounters* counters;
+};
+
+// ---- batched (warp-per-chain) kernel ----
+enum { PH_INIT = 0, PH_RUN = 1, PH_DONE = 2, PH_EMPTY = 3 };
+
+struct SlotState {
+    int32_t elem, phase, mi, m;
+    int32_t resZ, pad0;
+    uint64_t pos;
+    double rate_n, rate_c, gr, lr, lr2;
+    double prop_n, prop_c;
+    int32_t acc_n, acc_c;
+    double loglik, maxll;
+    int32_t max_m, status;
+    int64_t start_clock;
+    int64_t iters;
+};
+
+struct BatchParams {
+    const ElemHeader* hdr;
+    const uint8_t* blob;
+    SlotState* slots;
+    int n_slots;
+    char* slot_ws;            // per-slot: Z, maxz, class tables, traces
+    size_t slot_ws_stride;
+    char* grp_ws;             // per-warp scratch for Eval2
+    size_t grp_ws_stride;
+    int sweeps;               // iterations per slot per launch (<= 0: until done)
+    DevResult* results;       // by element index
+    int32_t* max_z;
+    double* post_z;
+    double* tr_d;
+    int8_t* tr_z;
+    DevCounters* counters;
+    int* n_done;              // number of slots that reached PH_DONE in this launch
+    int* next_slot;           // slot queue (atomic)
+    int n_int_max, S_max;
 };
 
 }  // namespace pacc

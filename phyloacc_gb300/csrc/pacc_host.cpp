@@ -36,6 +36,12 @@ cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate,
 cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out, cudaStream_t st);
 cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st);
+cudaError_t set_model_batch(const DevModel& m);
+size_t batch_warp_smem(int N, int NI, int S, int prec);
+size_t batch_slot_bytes(int N, int T);
+size_t batch_grp_bytes(int mcmc);
+cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
+cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // model (BPP, bpp.hpp:173-404)
@@ -427,7 +433,7 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     c->gpu_ok = cuda_ok(c, cudaSetDevice(c->device), "cudaSetDevice") &&
                 cuda_ok(c, cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device), "attr") &&
                 cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") &&
-                cuda_ok(c, set_model(dm), "set_model");
+                cuda_ok(c, set_model(dm), "set_model") && cuda_ok(c, set_model_batch(dm), "set_model_batch");
     std::memset(&c->counters, 0, sizeof(c->counters));
     if (status) *status = PACC_OK;
     return c;
@@ -472,6 +478,51 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
     return PACC_OK;
 }
 
+static void collect_results(pacc_ctx* c, const std::vector<DevResult>& res, const std::vector<int32_t>& mz,
+                            const std::vector<double>& pz, const std::vector<double>& trd,
+                            const std::vector<int8_t>& trz, int TI, int clk_khz) {
+    const int N = c->M.N;
+    const int n = (int)c->pending.size();
+    for (int e = 0; e < n; e++) {
+        pacc_ctx::Done d;
+        std::memset(&d.r, 0, sizeof(d.r));
+        d.r.element_no = c->pending[e].no;
+        d.r.n_nodes = N;
+        HostElem& E = c->pending[e];
+        if (E.filtered) {
+            d.r.status = E.filtered == 2 ? PACC_SAMPLER_ERROR : PACC_FILTERED;
+            d.max_z.assign(3 * N, 0);
+            d.post_z.assign(3 * N * 4, 0.0);
+        } else {
+            const DevResult& R = res[e];
+            d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
+            for (int m = 0; m < 3; m++) {
+                pacc_model_result& mr = d.r.model[m];
+                mr.loglik = R.model[m].loglik;
+                mr.max_loglik = R.model[m].max_loglik;
+                mr.n_rate = R.model[m].rates[0];
+                mr.c_rate = R.model[m].rates[1];
+                mr.g_rate = R.model[m].rates[2];
+                mr.l_rate = R.model[m].rates[3];
+                mr.l2_rate = R.model[m].rates[4];
+                mr.failure = R.model[m].failure;
+                mr.n_configs = R.model[m].n_configs;
+            }
+            d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
+            d.max_z.assign(mz.begin() + (size_t)e * 3 * N, mz.begin() + (size_t)(e + 1) * 3 * N);
+            d.post_z.assign(pz.begin() + (size_t)e * 3 * N * 4, pz.begin() + (size_t)(e + 1) * 3 * N * 4);
+            if (TI > 0) {
+                d.tr_d.assign(trd.begin() + (size_t)e * 3 * 6 * TI, trd.begin() + (size_t)(e + 1) * 3 * 6 * TI);
+                d.tr_z.assign(trz.begin() + (size_t)e * 3 * TI * N, trz.begin() + (size_t)(e + 1) * 3 * TI * N);
+            }
+        }
+        c->done.push_back(std::move(d));
+    }
+}
+
+static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<uint8_t>& blob, size_t off,
+                       int n_int_max, int GGp_max);
+
 static int run_pending(pacc_ctx* c) {
     if (c->pending.empty()) return PACC_OK;
     if (!c->gpu_ok) return PACC_ECUDA;
@@ -514,6 +565,7 @@ static int run_pending(pacc_ctx* c) {
         std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
         std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
     }
+    if (c->o.precision != PACC_FP64) return run_batched(c, hdr, blob, off, n_int_max, GGp_max);
     // launch geometry
     int BT = c->o.block_threads > 0 ? c->o.block_threads : 128;
     size_t smem = smem_bytes(N, BT, prec);
@@ -594,43 +646,145 @@ static int run_pending(pacc_ctx* c) {
     pc.iterations = (double)dc.iters;
     pc.kernel_ms = ms;
     pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
-    for (int e = 0; e < n; e++) {
-        pacc_ctx::Done d;
-        std::memset(&d.r, 0, sizeof(d.r));
-        d.r.element_no = c->pending[e].no;
-        d.r.n_nodes = N;
-        HostElem& E = c->pending[e];
-        if (E.filtered) {
-            d.r.status = E.filtered == 2 ? PACC_SAMPLER_ERROR : PACC_FILTERED;
-            d.max_z.assign(3 * N, 0);
-            d.post_z.assign(3 * N * 4, 0.0);
-        } else {
-            const DevResult& R = res[e];
-            d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
-            for (int m = 0; m < 3; m++) {
-                pacc_model_result& mr = d.r.model[m];
-                mr.loglik = R.model[m].loglik;
-                mr.max_loglik = R.model[m].max_loglik;
-                mr.n_rate = R.model[m].rates[0];
-                mr.c_rate = R.model[m].rates[1];
-                mr.g_rate = R.model[m].rates[2];
-                mr.l_rate = R.model[m].rates[3];
-                mr.l2_rate = R.model[m].rates[4];
-                mr.failure = R.model[m].failure;
-                mr.n_configs = R.model[m].n_configs;
-            }
-            d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
-            d.max_z.assign(mz.begin() + (size_t)e * 3 * N, mz.begin() + (size_t)(e + 1) * 3 * N);
-            d.post_z.assign(pz.begin() + (size_t)e * 3 * N * 4, pz.begin() + (size_t)(e + 1) * 3 * N * 4);
-            if (TI > 0) {
-                d.tr_d.assign(trd.begin() + (size_t)e * 3 * 6 * TI, trd.begin() + (size_t)(e + 1) * 3 * 6 * TI);
-                d.tr_z.assign(trz.begin() + (size_t)e * 3 * TI * N, trz.begin() + (size_t)(e + 1) * 3 * TI * N);
-            }
-        }
-        c->done.push_back(std::move(d));
-    }
+    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz);
     c->pending.clear();
     (void)S;
+    return PACC_OK;
+}
+
+
+// The batched path: one warp per element chain, chain state resident in device
+// memory (pacc_batch.cu).  Every admitted element gets a slot; warps claim
+// slots from a queue and run each chain to completion.
+static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<uint8_t>& blob, size_t off,
+                       int n_int_max, int GGp_max) {
+    (void)GGp_max;
+    const int N = c->M.N, S = c->M.S;
+    const int n = (int)c->pending.size();
+    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    const int T = c->o.burnin + c->o.mcmc;
+    const int TI = std::min(c->o.trace_iters, T);
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    std::vector<int32_t> elem;
+    for (int e = 0; e < n; e++) if (!c->pending[e].filtered) elem.push_back(e);
+    const int n_slots = std::max(1, (int)elem.size());
+    if (elem.empty()) elem.push_back(-1);
+    // geometry: warps per CTA from the shared-memory footprint of one chain
+    size_t wsm = batch_warp_smem(N, n_int_max, S, prec);
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    int warps = c->o.block_threads > 0 ? std::min(4, std::max(1, c->o.block_threads / 32)) : 4;
+    while (warps > 1 && wsm * warps > (size_t)max_smem) warps--;
+    if (wsm > (size_t)max_smem) { c->err = "element tree too large for the batched kernel"; return PACC_EUNSUPPORTED; }
+    size_t smem = wsm * warps;
+    int per_sm = 0;
+    cudaFuncAttributes fa;
+    (void)fa;
+    {
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+        per_sm = std::max(1, (int)(smem_sm / (smem + 1024)));
+        per_sm = std::min(per_sm, 2048 / (warps * 32));
+    }
+    int grid = std::max(1, std::min(c->n_sm * per_sm, (n_slots + warps - 1) / warps));
+    const int n_warps = grid * warps;
+    size_t slot_b = al(batch_slot_bytes(N, T));
+    size_t grp_b = al(batch_grp_bytes(c->o.mcmc));
+    size_t o_hdr = 0;
+    size_t o_res = al(o_hdr + sizeof(ElemHeader) * n);
+    size_t o_mz = al(o_res + sizeof(DevResult) * n);
+    size_t o_pz = al(o_mz + sizeof(int32_t) * 3 * N * (size_t)n);
+    size_t o_trd = al(o_pz + sizeof(double) * 3 * N * 4 * (size_t)n);
+    size_t o_trz = al(o_trd + sizeof(double) * 3 * 6 * (size_t)TI * n);
+    size_t o_cnt = al(o_trz + (size_t)3 * TI * N * n);
+    size_t o_next = al(o_cnt + sizeof(DevCounters));
+    size_t o_elem = al(o_next + 256);
+    size_t o_slots = al(o_elem + sizeof(int32_t) * elem.size());
+    size_t o_slotws = al(o_slots + sizeof(SlotState) * n_slots);
+    size_t o_grp = al(o_slotws + slot_b * n_slots);
+    size_t misc = al(o_grp + grp_b * n_warps);
+    if (!grow(c, &c->d_blob, &c->blob_cap, std::max<size_t>(off, 256)) || !grow(c, &c->d_misc, &c->misc_cap, misc))
+        return PACC_OOM;
+    char* mb = (char*)c->d_misc;
+    cudaStream_t st = c->stream;
+    if (!cuda_ok(c, cudaMemcpyAsync(c->d_blob, blob.data(), off, cudaMemcpyHostToDevice, st), "H2D blob") ||
+        !cuda_ok(c, cudaMemcpyAsync(mb + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st), "H2D hdr") ||
+        !cuda_ok(c, cudaMemcpyAsync(mb + o_elem, elem.data(), sizeof(int32_t) * elem.size(), cudaMemcpyHostToDevice, st), "H2D elem") ||
+        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_elem - o_res, st), "memset") ||
+        !cuda_ok(c, launch_init_slots(mb + o_slots, (const int32_t*)(mb + o_elem), n_slots, st), "init slots"))
+        return PACC_ECUDA;
+    BatchParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.hdr = (const ElemHeader*)(mb + o_hdr);
+    p.blob = (const uint8_t*)c->d_blob;
+    p.slots = (SlotState*)(mb + o_slots);
+    p.n_slots = n_slots;
+    p.slot_ws = mb + o_slotws;
+    p.slot_ws_stride = slot_b;
+    p.grp_ws = mb + o_grp;
+    p.grp_ws_stride = grp_b;
+    p.sweeps = c->o.sweeps_per_launch;
+    p.results = (DevResult*)(mb + o_res);
+    p.max_z = (int32_t*)(mb + o_mz);
+    p.post_z = (double*)(mb + o_pz);
+    p.tr_d = TI > 0 ? (double*)(mb + o_trd) : nullptr;
+    p.tr_z = TI > 0 ? (int8_t*)(mb + o_trz) : nullptr;
+    p.counters = (DevCounters*)(mb + o_cnt);
+    p.n_done = (int*)(mb + o_next);
+    p.next_slot = (int*)(mb + o_next + 128);
+    p.n_int_max = n_int_max;
+    p.S_max = S;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    int launches = 0;
+    for (;;) {
+        if (!cuda_ok(c, cudaMemsetAsync(mb + o_next + 128, 0, 4, st), "memset queue") ||
+            !cuda_ok(c, launch_batch(&p, grid, warps, smem, prec, st), "launch batch"))
+            return PACC_ECUDA;
+        launches++;
+        if (p.sweeps <= 0) break;
+        int done = 0;
+        if (!cuda_ok(c, cudaMemcpyAsync(&done, mb + o_next, 4, cudaMemcpyDeviceToHost, st), "D2H done") ||
+            !cuda_ok(c, cudaStreamSynchronize(st), "batch kernel"))
+            return PACC_ECUDA;
+        if (done >= (int)elem.size() || elem[0] < 0) break;
+        if (launches > 100000000) { c->err = "batched run did not finish"; return PACC_TIMEOUT; }
+    }
+    cudaEventRecord(e1, st);
+    std::vector<DevResult> res(n);
+    std::vector<int32_t> mz((size_t)3 * N * n);
+    std::vector<double> pz((size_t)3 * N * 4 * n);
+    std::vector<double> trd((size_t)3 * 6 * TI * n);
+    std::vector<int8_t> trz((size_t)3 * TI * N * n);
+    DevCounters dc;
+    cudaMemcpyAsync(res.data(), mb + o_res, sizeof(DevResult) * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(mz.data(), mb + o_mz, mz.size() * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pz.data(), mb + o_pz, pz.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (TI > 0) {
+        cudaMemcpyAsync(trd.data(), mb + o_trd, trd.size() * 8, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(trz.data(), mb + o_trz, trz.size(), cudaMemcpyDeviceToHost, st);
+    }
+    cudaMemcpyAsync(&dc, mb + o_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "batch kernel")) return PACC_ECUDA;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int clk_khz = 0;
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, c->device);
+    pacc_counters& pc = c->counters;
+    std::memset(&pc, 0, sizeof(pc));
+    pc.edge_updates_internal = (double)dc.edge_internal;
+    pc.edge_updates_leaf = (double)dc.edge_leaf;
+    pc.tg_draws = (double)dc.tg_draws;
+    pc.kernel_ms = ms;
+    pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
+    pc.iterations = (double)launches;
+    for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
+    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz);
+    c->pending.clear();
     return PACC_OK;
 }
 
