@@ -52,11 +52,12 @@ struct SlotLayout {
 
 // Per-warp Eval2 scratch.
 struct GrpLayout {
-    size_t hash, rep, cfg, nxt, head, first, cstat, total;
-    __host__ __device__ static GrpLayout make(int mcmc) {
+    size_t hash, rep, cfg, nxt, head, first, cstat, gpart, total;
+    __host__ __device__ static GrpLayout make(int mcmc, int NI, int real_bytes) {
         GrpLayout L;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+        L.gpart = o; o = al(o + (size_t)NI * 4 * 32 * real_bytes);   // all internal partials of 32 columns
         L.hash = o; o = al(o + (size_t)(mcmc + 1) * 8);
         L.rep = o; o = al(o + (size_t)(mcmc + 1) * 4);
         L.cfg = o; o = al(o + (size_t)(mcmc + 1) * 4);
@@ -72,19 +73,21 @@ struct GrpLayout {
 // Shared memory of one warp-chain.
 template <typename Real>
 struct WarpSmem {
-    size_t ptc, part, tgv, hdf, rec, stage, cnt, topo, i8, dbl, total;
-    __host__ __device__ static WarpSmem make(int N, int NI, int S) {
+    size_t ptc, part, tgv, hdf, rec, srec, emr, stage, cnt, topo, i8, dbl, total;
+    __host__ __device__ static WarpSmem make(int N, int NI, int S, int D) {
         WarpSmem w;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
         w.ptc = o; o = al(o + (size_t)N * 16 * sizeof(Real));        // current P^T per branch
-        size_t part_bytes = (size_t)NI * 4 * 32 * sizeof(Real);
-        size_t alias_bytes = (size_t)N * 6 * 8;                        // emis + bz alias the slice
+        size_t part_bytes = (size_t)D * 4 * 32 * sizeof(Real);          // stack of pending partials
+        size_t alias_bytes = (size_t)N * 6 * 8;                        // emis + bz alias the stack
         w.part = o; o = al(o + (part_bytes > alias_bytes ? part_bytes : alias_bytes));
         w.tgv = o; o = al(o + (size_t)NI * 32);
-        w.hdf = o; o = al(o + (size_t)NI * 32);
+        w.hdf = o; o = al(o + 16);
         w.rec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
-        w.stage = o; o = al(o + (size_t)S * 32);
+        w.srec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
+        w.emr = o; o = al(o + (size_t)N * sizeof(EmRec));
+        w.stage = o; o = al(o + (size_t)((S + 15) & ~15) * 32);
         w.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 2);               // uint16 bins
         w.topo = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
         w.i8 = o; o = al(o + (size_t)N * 6);                            // fixZ chg unv mask maxz(unused) Zc
@@ -108,8 +111,13 @@ struct W {
     Real* part;         // [NI][4][32]
     int8_t* tgv;        // [NI][32]
     int8_t* hdf;        // [NI][32] node has data at this lane's column
-    const NodeRec* rec; // [NI]
-    uint8_t* stage;     // [S][32]
+    const NodeRec* rec; // [NI] internal nodes in postorder (internal_nodes)
+    const NodeRec* srec;// [NI] internal nodes in stack order
+    Real* gpart;        // [NI][4][32] per-warp device scratch: partials of the sampling pass
+    const EmRec* emr;   // [n_nodes - 1]
+    uint32_t* stage;    // [SP/4][32] words of per-lane column codes
+    const uint8_t* codes_t;  // [GGp][SP]
+    int SP;
     unsigned* cnt;      // [N][20] packed uint16 pairs
     double* emis;       // [N][3]  (aliases part)
     double* bz;         // [N][3]  (aliases part)
@@ -214,78 +222,139 @@ template <> struct Resc<float> {
     }
 };
 
+// Load the codes of column g of every taxon into this lane's stage words:
+// the column is SP contiguous bytes (codes by column), read with SP/16
+// independent 128-bit loads.  Stage layout: word ((c >> 2) * 32 + lane) holds
+// taxa c..c+3 of this lane's column.
+__device__ __forceinline__ void stage_column(const uint8_t* __restrict__ codes_t, int SP, uint32_t* __restrict__ stage,
+                                             int lane, int g, bool act) {
+    const int nv = SP >> 4;
+    if (act) {
+        const uint4* __restrict__ src = (const uint4*)(codes_t + (size_t)g * SP);
+        for (int i0 = 0; i0 < nv; i0 += 4) {   // up to 4 loads in flight (64 taxa)
+            uint4 v[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (i0 + i < nv) v[i] = src[i0 + i];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (i0 + i < nv) {
+                    const int b = 4 * (i0 + i);
+                    stage[(b + 0) * 32 + lane] = v[i].x;
+                    stage[(b + 1) * 32 + lane] = v[i].y;
+                    stage[(b + 2) * 32 + lane] = v[i].z;
+                    stage[(b + 3) * 32 + lane] = v[i].w;
+                }
+        }
+    } else {
+        for (int i = 0; i < 4 * nv; i++) stage[i * 32 + lane] = 0x04040404u;  // gaps
+    }
+}
+
+__device__ __forceinline__ int stage_code(const uint32_t* __restrict__ stage, int c, int lane) {
+    return (stage[(c >> 2) * 32 + lane] >> (8 * (c & 3))) & 0xFF;
+}
+
 // Bottom-up pass over one column held by this lane (Update_Tg without
-// sampling, bpp_c.cpp:647-671): every internal node's partial into the slice.
-// Returns the rescale exponent accumulated over the column; the root partial
-// includes pi.  hdf: a node has data when some leaf below it is a base or an
-// ambiguity code, the complement of Tg == K (bpp_c.hpp:417-428).
-template <typename Real>
-__device__ __forceinline__ int column_up(W<Real>& w, bool act) {
+// sampling, bpp_c.cpp:647-671).  Internal nodes are visited in stack order
+// (a postorder that takes the child needing more pending partials first); a
+// node pops its internal children's partials and pushes its own, so at most
+// `stack_depth` partials per lane are live.  The "has data" flag of a node
+// (some leaf below is a base or an ambiguity code: the complement of
+// Tg == K, bpp_c.hpp:417-428) travels on a register bit stack.  With STORE,
+// every partial is also written to the warp's device scratch (for the
+// top-down sampling) and the node's no-data mark to tgv.  Returns the rescale
+// exponent of the column; *root gets the root partial (pi included).
+template <typename Real, bool STORE>
+__device__ __forceinline__ int column_up(const NodeRec* __restrict__ srec, int n_int, const uint32_t* __restrict__ stage,
+                                         Real* __restrict__ stk, Real* __restrict__ gpart, int8_t* __restrict__ tgv,
+                                         const Real* __restrict__ ptc, int lane, bool act, unsigned& e_int,
+                                         unsigned& e_leaf, const Real pi[4], Real root[4]) {
     int sc = 0;
-    const int lane = w.lane;
-    for (int k = 0; k < w.n_int; k++) {
-        const NodeRec R = w.rec[k];
+    int sp = 0;
+    unsigned hbits = 0;
+    for (int k = 0; k < n_int; k++) {
+        const NodeRec R = srec[k];
         int code0 = 0, code1 = 0;
-        bool h0, h1;
-        if (R.r0 < 0) { code0 = w.stage[R.c0 * 32 + lane]; h0 = code0 != CODE_GAP && code0 != CODE_OTHER; }
-        else h0 = w.hdf[R.r0 * 32 + lane];
-        if (R.r1 < 0) { code1 = w.stage[R.c1 * 32 + lane]; h1 = code1 != CODE_GAP && code1 != CODE_OTHER; }
-        else h1 = w.hdf[R.r1 * 32 + lane];
+        bool h0 = false, h1 = false;
+        Real x0[4], x1[4];
+        // pop internal children (the child computed last is on top)
+        const bool i0 = R.r0 >= 0, i1 = R.r1 >= 0;
+        if (i0 && i1) {
+            const bool c0_top = R.prank & 1;   // flags, see NodeRec
+            Real* t = stk + (sp - 1) * 128 + lane;
+            Real* u = stk + (sp - 2) * 128 + lane;
+            const bool ht = hbits & 1, hu = (hbits >> 1) & 1;
+            hbits >>= 2;
+            sp -= 2;
+            if (c0_top) {
+                x0[0] = t[0]; x0[1] = t[32]; x0[2] = t[64]; x0[3] = t[96]; h0 = ht;
+                x1[0] = u[0]; x1[1] = u[32]; x1[2] = u[64]; x1[3] = u[96]; h1 = hu;
+            } else {
+                x1[0] = t[0]; x1[1] = t[32]; x1[2] = t[64]; x1[3] = t[96]; h1 = ht;
+                x0[0] = u[0]; x0[1] = u[32]; x0[2] = u[64]; x0[3] = u[96]; h0 = hu;
+            }
+        } else if (i0 || i1) {
+            Real* t = stk + (sp - 1) * 128 + lane;
+            const bool ht = hbits & 1;
+            hbits >>= 1;
+            sp -= 1;
+            if (i0) { x0[0] = t[0]; x0[1] = t[32]; x0[2] = t[64]; x0[3] = t[96]; h0 = ht; }
+            else { x1[0] = t[0]; x1[1] = t[32]; x1[2] = t[64]; x1[3] = t[96]; h1 = ht; }
+        }
+        if (!i0) { code0 = stage_code(stage, R.c0, lane); h0 = code0 != CODE_GAP && code0 != CODE_OTHER; }
+        if (!i1) { code1 = stage_code(stage, R.c1, lane); h1 = code1 != CODE_GAP && code1 != CODE_OTHER; }
         const bool hs = h0 || h1;
-        w.hdf[k * 32 + lane] = hs;
-        Real a[4] = {1, 1, 1, 1};
+        Real a0 = 1, a1 = 1, a2 = 1, a3 = 1;
         if (act && hs && !R.missing) {
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int c = q ? R.c1 : R.c0;
-                const int r = q ? R.r1 : R.r0;
+                const bool internal_child = q ? i1 : i0;
                 const int code = q ? code1 : code0;
                 if ((q ? R.m1 : R.m0) || !(q ? h1 : h0)) continue;
-                const Real* Pc = w.ptc + c * 16;
-                if (r < 0) {
+                const Real* __restrict__ Pc = ptc + c * 16;
+                if (!internal_child) {
                     if (code < 4) {
-#pragma unroll
-                        for (int j = 0; j < 4; j++) a[j] *= Pc[code * 4 + j];
+                        const Real* Pr = Pc + code * 4;
+                        a0 *= Pr[0]; a1 *= Pr[1]; a2 *= Pr[2]; a3 *= Pr[3];
                     } else {
                         int msk = ambig_mask(code - CODE_R);
-                        Real v[4] = {0, 0, 0, 0};
+                        Real v0 = 0, v1 = 0, v2 = 0, v3 = 0;
 #pragma unroll
                         for (int i = 0; i < 4; i++)
-                            if (msk & (1 << i))
-#pragma unroll
-                                for (int j = 0; j < 4; j++) v[j] += Pc[i * 4 + j];
-#pragma unroll
-                        for (int j = 0; j < 4; j++) a[j] *= v[j];
+                            if (msk & (1 << i)) { v0 += Pc[i * 4]; v1 += Pc[i * 4 + 1]; v2 += Pc[i * 4 + 2]; v3 += Pc[i * 4 + 3]; }
+                        a0 *= v0; a1 *= v1; a2 *= v2; a3 *= v3;
                     }
-                    w.e_leaf++;
+                    e_leaf++;
                 } else {
-                    Real x0 = w.PART(r, 0), x1 = w.PART(r, 1), x2 = w.PART(r, 2), x3 = w.PART(r, 3);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        Real v = Pc[j] * x0;
-                        v += Pc[4 + j] * x1;
-                        v += Pc[8 + j] * x2;
-                        v += Pc[12 + j] * x3;
-                        a[j] *= v;
-                    }
-                    w.e_int++;
+                    const Real* x = q ? x1 : x0;
+                    a0 *= ((Pc[0] * x[0] + Pc[4] * x[1]) + (Pc[8] * x[2] + Pc[12] * x[3]));
+                    a1 *= ((Pc[1] * x[0] + Pc[5] * x[1]) + (Pc[9] * x[2] + Pc[13] * x[3]));
+                    a2 *= ((Pc[2] * x[0] + Pc[6] * x[1]) + (Pc[10] * x[2] + Pc[14] * x[3]));
+                    a3 *= ((Pc[3] * x[0] + Pc[7] * x[1]) + (Pc[11] * x[2] + Pc[15] * x[3]));
+                    e_int++;
                 }
             }
+            Real a[4] = {a0, a1, a2, a3};
             Resc<Real>::apply(a, sc);
+            a0 = a[0]; a1 = a[1]; a2 = a[2]; a3 = a[3];
         }
-        if (R.is_root)
-#pragma unroll
-            for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
-#pragma unroll
-        for (int j = 0; j < 4; j++) w.PART(k, j) = a[j];
+        if (R.is_root) {
+            a0 *= pi[0]; a1 *= pi[1]; a2 *= pi[2]; a3 *= pi[3];
+            root[0] = a0; root[1] = a1; root[2] = a2; root[3] = a3;
+        }
+        Real* __restrict__ o = stk + sp * 128 + lane;
+        o[0] = a0; o[32] = a1; o[64] = a2; o[96] = a3;
+        sp++;
+        hbits = (hbits << 1) | (hs ? 1u : 0u);
+        if (STORE) {
+            Real* __restrict__ gp = gpart + R.self * 128 + lane;
+            gp[0] = a0; gp[32] = a1; gp[64] = a2; gp[96] = a3;
+            tgv[R.self * 32 + lane] = hs ? (int8_t)-1 : (int8_t)4;
+        }
     }
     return sc;
-}
-
-// Load the codes of column g of every taxon into this lane's stage slots.
-template <typename Real>
-__device__ __forceinline__ void stage_column(W<Real>& w, int g, bool act) {
-    for (int s = 0; s < w.S; s++) w.stage[s * 32 + w.lane] = act ? w.codes[(size_t)s * w.GGp + g] : (uint8_t)CODE_GAP;
 }
 
 // Per-column log-likelihood accumulated as (FP64 product of root sums) x 2^exponent.
@@ -308,22 +377,32 @@ struct LLAcc {
 // Full prune of all columns with the current matrices; returns the summed
 // per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).
 template <typename Real>
-__device__ double likelihood_pass(W<Real>& w) {
+__device__ __forceinline__ double likelihood_pass(W<Real>& w) {
+    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP;
+    const NodeRec* __restrict__ srec = w.srec;
+    const uint8_t* __restrict__ codes_t = w.codes_t;
+    uint32_t* __restrict__ stage = w.stage;
+    Real* __restrict__ stk = w.part;
+    const Real* __restrict__ ptc = w.ptc;
+    const Real pi[4] = {(Real)dM.pi[0], (Real)dM.pi[1], (Real)dM.pi[2], (Real)dM.pi[3]};
+    unsigned e_int = 0, e_leaf = 0;
     double acc = 0;
     LLAcc ll;
     ll.init();
-    const int rk = w.irank[w.root];
-    for (int g0 = 0; g0 < w.GG; g0 += 32) {
-        int g = g0 + w.lane;
-        bool act = g < w.GG;
-        stage_column(w, g, act);
-        int sc = column_up(w, act);
+    for (int g0 = 0; g0 < GG; g0 += 32) {
+        const int g = g0 + lane;
+        const bool act = g < GG;
+        stage_column(codes_t, SP, stage, lane, g, act);
+        Real r[4];
+        int sc = column_up<Real, false>(srec, n_int, stage, stk, nullptr, nullptr, ptc, lane, act, e_int, e_leaf, pi, r);
         if (act) {
-            double t = (double)w.PART(rk, 0) + (double)w.PART(rk, 1) + (double)w.PART(rk, 2) + (double)w.PART(rk, 3);
+            double t = (double)r[0] + (double)r[1] + (double)r[2] + (double)r[3];
             if (sizeof(Real) == 8) acc += log(t) + (double)sc * 0.6931471805599453;
             else ll.add(t, sc);
         }
     }
+    w.e_int += e_int;
+    w.e_leaf += e_leaf;
     double v = (sizeof(Real) == 8) ? acc : ll.value();
     return warp_sum(v);
 }
@@ -344,82 +423,108 @@ __device__ __forceinline__ int cat4(const Real* p, double u) {
     return 4;
 }
 
+// Uniform from a stream word in the partials' precision.
+template <typename Real>
+__device__ __forceinline__ double u_of(uint32_t w) { return word_to_uniform(w); }
+template <>
+__device__ __forceinline__ double u_of<float>(uint32_t w) {
+    return (double)(((float)(w >> 8) + 0.5f) * 5.9604644775390625e-08f);
+}
+
 // Internal-base pass (Update_Tg with sampling, bpp_c.cpp:672-733) fused with
 // the emission histogram of (child symbol, parent base) pairs.
 template <typename Real>
-__device__ int sample_pass(W<Real>& w, uint64_t pos) {
+__device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
     const int NB = NSYM * 4;
-    for (int i = w.lane; i < w.N * NB / 2; i += 32) w.cnt[i] = 0;
-    wsync();
+    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, S = w.S, N = w.N, n_nodes = w.n_nodes;
+    const NodeRec* __restrict__ rec = w.rec;
+    const NodeRec* __restrict__ srec = w.srec;
+    const uint8_t* __restrict__ codes_t = w.codes_t;
+    uint32_t* __restrict__ stage = w.stage;
+    int8_t* __restrict__ tgv = w.tgv;
+    Real* __restrict__ stk = w.part;
+    Real* __restrict__ part = w.gpart;
+    const Real* __restrict__ ptc = w.ptc;
+    unsigned* __restrict__ cnt = w.cnt;
+    const int16_t* __restrict__ nodes = w.nodes;
+    const int16_t* __restrict__ internal = w.internal;
+    const int16_t* __restrict__ irank = w.irank;
+    const int16_t* __restrict__ par = w.par;
+    const int16_t* __restrict__ missing = w.missing;
+    const int32_t* __restrict__ prefix = w.prefix;
+    const uint32_t seed = dM.seed;
+    const Real pi[4] = {(Real)dM.pi[0], (Real)dM.pi[1], (Real)dM.pi[2], (Real)dM.pi[3]};
+    for (int i = lane; i < N * NB / 2; i += 32) cnt[i] = 0;
+    __syncwarp();
     int err = 0;
-    const int rk = w.irank[w.root];
-    for (int g0 = 0; g0 < w.GG; g0 += 32) {
-        int g = g0 + w.lane;
-        bool act = g < w.GG;
-        stage_column(w, g, act);
-        column_up(w, act);
-        // top-down sampling
-        uint64_t wp = pos + (act ? (uint64_t)w.prefix[g] : 0);
-        uint64_t blk = ~0ull;
-        uint32_t words[4];
-        auto next_u = [&]() {
-            uint64_t b = wp >> 2;
-            if (b != blk) {
-                philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, words);
-                blk = b;
-            }
-            double u = word_to_uniform(words[wp & 3]);
-            wp++;
-            return u;
-        };
+    const int rk = irank[w.root];
+    unsigned e_int = 0, e_leaf = 0, n_tg = 0;
+    for (int g0 = 0; g0 < GG; g0 += 32) {
+        const int g = g0 + lane;
+        const bool act = g < GG;
+        stage_column(codes_t, SP, stage, lane, g, act);
+        Real rootp[4];
+        column_up<Real, true>(srec, n_int, stage, stk, part, tgv, ptc, lane, act, e_int, e_leaf, pi, rootp);
         if (act) {
-            Real p[4];
-            for (int j = 0; j < 4; j++) p[j] = w.PART(rk, j);
-            int nn = cat4(p, next_u());
+            uint64_t wp = pos + (uint64_t)prefix[g];
+            uint64_t blk = wp >> 2;
+            uint32_t words[4];
+            philox4x32_10((uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u, seed, 0u, words);
+            int nn = cat4(rootp, u_of<Real>(words[wp & 3]));
+            wp++;
             if (nn > 3) { err = 1; nn = 0; }
-            w.tgv[rk * 32 + w.lane] = (int8_t)nn;
-            w.n_tg++;
-            for (int k = w.n_int - 2; k >= 0; k--) {
-                int s = w.internal[k];
-                bool hs = w.hdf[k * 32 + w.lane];
-                if (w.missing[s] || !hs) { w.tgv[k * 32 + w.lane] = 4; continue; }
-                int tp = w.tgv[w.irank[w.par[s]] * 32 + w.lane];
-                const Real* Ps = w.ptc + s * 16;
+            tgv[rk * 32 + lane] = (int8_t)nn;
+            n_tg++;
+            for (int k = n_int - 2; k >= 0; k--) {
+                const NodeRec R = rec[k];
+                if (R.missing || tgv[k * 32 + lane] == 4) { tgv[k * 32 + lane] = 4; continue; }
+                const int tp = tgv[R.prank * 32 + lane];
+                const Real* __restrict__ Ps = ptc + R.self * 16 + tp;
                 Real q[4];
-                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4 + tp] * w.PART(k, i);
-                int n2 = cat4(q, next_u());
+                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4] * part[k * 128 + i * 32 + lane];
+                if ((wp >> 2) != blk) {
+                    blk = wp >> 2;
+                    philox4x32_10((uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u, seed, 0u, words);
+                }
+                int n2 = cat4(q, u_of<Real>(words[wp & 3]));
+                wp++;
                 if (n2 > 3) { err = 1; n2 = 0; }
-                w.tgv[k * 32 + w.lane] = (int8_t)n2;
-                w.n_tg++;
+                tgv[k * 32 + lane] = (int8_t)n2;
+                n_tg++;
             }
         }
         // emission histogram, warp-aggregated
-        for (int i = 0; i < w.n_nodes - 1; i++) {
-            int s = w.nodes[i];
-            if (w.missing[s]) continue;
+        const EmRec* __restrict__ emr = w.emr;
+        for (int i = 0; i < n_nodes - 1; i++) {
+            const EmRec E = emr[i];
+            if (E.missing) continue;
+            const int s = E.node;
             int key = -1;
             if (act) {
                 int sym;
-                if (s < w.S) {
-                    int code = w.stage[s * 32 + w.lane];
+                if (E.rank < 0) {
+                    int code = stage_code(stage, s, lane);
                     sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
                 } else {
-                    int t = w.tgv[w.irank[s] * 32 + w.lane];
+                    int t = tgv[E.rank * 32 + lane];
                     sym = t < 4 ? t : -1;
                 }
                 if (sym >= 0) {
-                    int tp = w.tgv[w.irank[w.par[s]] * 32 + w.lane];
+                    int tp = tgv[E.prank * 32 + lane];
                     if (tp >= 0 && tp < 4) key = sym * 4 + tp;
                 }
             }
             unsigned peers = __match_any_sync(0xffffffffu, key);
-            if (key >= 0 && w.lane == __ffs(peers) - 1) {
+            if (key >= 0 && lane == __ffs(peers) - 1) {
                 int bin = s * NB + key;
-                atomicAdd(&w.cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
+                atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
             }
         }
     }
-    wsync();
+    w.e_int += e_int;
+    w.e_leaf += e_leaf;
+    w.n_tg += n_tg;
+    __syncwarp();
     return warp_or(err);
 }
 
@@ -682,10 +787,12 @@ __device__ double prior_config(W<Real>& w, const int8_t* z) {
 
 // Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353) by one warp.
 template <typename Real>
-__device__ double eval2(W<Real>& w, char* gws, int* n_conf_out) {
+__device__ __noinline__ double eval2(W<Real>& w, char* gws, int* n_conf_out) {
     const int burn = w.burn, mcmc = w.mcmc, T = w.T, N = w.N;
     const int resZ = w.st.resZ;
-    GrpLayout G = GrpLayout::make(mcmc);
+    // Eval2 runs after the chain, so it reuses the warp scratch from its start
+    // (the sampling-pass partials are not live any more).
+    GrpLayout G = GrpLayout::make(mcmc, 0, 0);
     uint64_t* hash = (uint64_t*)(gws + G.hash);
     int32_t* rep = (int32_t*)(gws + G.rep);
     int32_t* cfg = (int32_t*)(gws + G.cfg);
@@ -860,7 +967,7 @@ __device__ double eval2(W<Real>& w, char* gws, int* n_conf_out) {
 }
 
 // Element of rank T/2 under std::sort's order (bpp_c2.cpp:742-755).
-__device__ double warp_median(const double* x, int T) {
+__device__ __noinline__ double warp_median(const double* x, int T) {
     int target = T / 2;
     double found = 0;
     int hit = 0;
@@ -879,7 +986,7 @@ __device__ double warp_median(const double* x, int T) {
 
 // initMCMC for model w.st.mi (bpp_c.cpp:131-343) followed by the initial full prune.
 template <typename Real>
-__device__ void init_model(W<Real>& w) {
+__device__ __noinline__ void init_model(W<Real>& w) {
     const int resZ = w.st.resZ;
     for (int i = w.lane; i < w.N; i += 32) { w.Z[i] = -1; w.fixZ[i] = -1; }
     wsync();
@@ -929,7 +1036,7 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int N = dM.N, S = dM.S;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    WarpSmem<Real> L = WarpSmem<Real>::make(N, P.n_int_max, S);
+    WarpSmem<Real> L = WarpSmem<Real>::make(N, P.n_int_max, S, P.stack_depth);
     TopoLayout TL = TopoLayout::make(N);
     unsigned char* base = smem + (size_t)wid * L.total;
     W<Real> w;
@@ -947,7 +1054,11 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     w.hdf = (int8_t*)(base + L.hdf);
     NodeRec* recw = (NodeRec*)(base + L.rec);
     w.rec = recw;
-    w.stage = (uint8_t*)(base + L.stage);
+    NodeRec* srecw = (NodeRec*)(base + L.srec);
+    w.srec = srecw;
+    EmRec* emrw = (EmRec*)(base + L.emr);
+    w.emr = emrw;
+    w.stage = (uint32_t*)(base + L.stage);
     w.cnt = (unsigned*)(base + L.cnt);
     int16_t* t16 = (int16_t*)(base + L.topo);
     w.nodes = t16 + TL.nodes; w.internal = t16 + TL.internal; w.c2a = t16 + TL.c2a; w.c2b = t16 + TL.c2b;
@@ -961,6 +1072,10 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     const int gw = blockIdx.x * nw + wid;
     const int n_gw = gridDim.x * nw;
     char* gws = P.grp_ws + (size_t)gw * P.grp_ws_stride;
+    {
+        GrpLayout GLy = GrpLayout::make(dM.mcmc, P.n_int_max, sizeof(Real));
+        w.gpart = (Real*)(gws + GLy.gpart);
+    }
     const SlotLayout SL = SlotLayout::make(N, w.T);
     const int TI = dM.trace_iters < w.T ? dM.trace_iters : w.T;
     const int resZ_of[3] = {0, 2, 1};
@@ -978,6 +1093,8 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
         w.GG = H.GG; w.GGp = H.GGp; w.root = H.root; w.n_nodes = H.n_nodes; w.n_int = H.n_int;
         w.n_hlev = H.n_hlev; w.n_dlev = H.n_dlev; w.tg_draws = H.tg_draws;
         w.codes = P.blob + H.codes_off;
+        w.codes_t = P.blob + H.codes_t_off;
+        w.SP = H.SP;
         w.prefix = (const int32_t*)(P.blob + H.prefix_off);
         {
             const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
@@ -997,8 +1114,38 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
             R.m1 = (int8_t)w.missing[R.c1];
             R.missing = (int8_t)w.missing[s];
             R.is_root = (s == w.root);
-            R.pad = 0;
+            R.self = (int16_t)s;
+            R.prank = (s == w.root) ? (int16_t)-1 : w.irank[w.par[s]];
             recw[k] = R;
+        }
+        {
+            const int16_t* sord = t16 + TL.sord;
+            const int16_t* sflag = t16 + TL.sflag;
+            for (int k = lane; k < w.n_int; k += 32) {
+                int s = sord[k];
+                NodeRec R;
+                R.c0 = w.c2a[s];
+                R.c1 = w.c2b[s];
+                R.r0 = R.c0 >= S ? w.irank[R.c0] : -1;
+                R.r1 = R.c1 >= S ? w.irank[R.c1] : -1;
+                R.m0 = (int8_t)w.missing[R.c0];
+                R.m1 = (int8_t)w.missing[R.c1];
+                R.missing = (int8_t)w.missing[s];
+                R.is_root = (s == w.root);
+                R.self = w.irank[s];      // stack order: self = internal rank (scratch row)
+                R.prank = sflag[s];       // stack order: bit 0 = first child's partial on top
+                srecw[k] = R;
+            }
+        }
+        for (int i = lane; i < w.n_nodes - 1; i += 32) {
+            int s = w.nodes[i];
+            EmRec E;
+            E.node = (int16_t)s;
+            E.rank = s >= S ? w.irank[s] : (int16_t)-1;
+            E.prank = w.irank[w.par[s]];
+            E.missing = (int8_t)w.missing[s];
+            E.pad = 0;
+            emrw[i] = E;
         }
         char* sw = P.slot_ws + (size_t)slot * P.slot_ws_stride;
         w.sZ = (int8_t*)(sw + SL.Z);
@@ -1023,7 +1170,13 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
             }
         }
         wsync();
-        int budget = P.sweeps > 0 ? P.sweeps : 0x7fffffff;
+        // iterations this launch: `sweeps` for a 256-column element, scaled by
+        // 256 / GG so that every chain's share of a launch costs about the same
+        int budget = 0x7fffffff;
+        if (P.sweeps > 0) {
+            long long b = (long long)P.sweeps * 256 / (w.GG > 0 ? w.GG : 1);
+            budget = (int)(b < 1 ? 1 : (b > 0x7fffffff ? 0x7fffffff : b));
+        }
         int errs = 0;
         while (budget > 0 && w.st.phase != PH_DONE) {
             if (w.st.phase == PH_INIT) {
@@ -1088,7 +1241,8 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
                 if (w.st.phase == PH_DONE && lane == 0) {
                     P.results[e].status = (w.st.status & 1) ? 3 : ((w.st.status & 2) ? 2 : 0);
                     P.results[e].device_ms = (double)(clock64() - w.st.start_clock);
-                    atomicAdd(P.n_done, 1);
+                    int di = atomicAdd(P.n_done, 1);
+                    if (P.done_list) P.done_list[di] = slot;
                 }
                 __syncwarp();
                 continue;
@@ -1184,11 +1338,11 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
 // ---------------------------------------------------------------------------
 cudaError_t set_model_batch(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
 
-size_t batch_warp_smem(int N, int NI, int S, int prec) {
-    return prec == 0 ? WarpSmem<double>::make(N, NI, S).total : WarpSmem<float>::make(N, NI, S).total;
+size_t batch_warp_smem(int N, int NI, int S, int D, int prec) {
+    return prec == 0 ? WarpSmem<double>::make(N, NI, S, D).total : WarpSmem<float>::make(N, NI, S, D).total;
 }
 size_t batch_slot_bytes(int N, int T) { return SlotLayout::make(N, T).total; }
-size_t batch_grp_bytes(int mcmc) { return GrpLayout::make(mcmc).total; }
+size_t batch_grp_bytes(int mcmc, int NI, int prec) { return GrpLayout::make(mcmc, NI, prec == 0 ? 8 : 4).total; }
 size_t batch_state_bytes() { return sizeof(SlotState); }
 
 // Slot states for a fresh batch: slot i runs element elem[i].

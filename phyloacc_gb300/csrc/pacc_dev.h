@@ -56,18 +56,21 @@ struct ElemHeader {
     int32_t n_dlev;        // top-down levels (by depth) below the root
     int32_t tg_draws;      // stream words used by one internal-base pass (prefix[GG])
     int64_t codes_off;     // byte offset of codes [S][GGp]
+    int64_t codes_t_off;   // byte offset of codes by column [GGp][SP] (SP = S rounded up to 16)
     int64_t tg_off;        // byte offset of initial internal Tg [n_int][GGp] (int8)
     int64_t prefix_off;    // byte offset of draw prefix [GG+1] (int32)
     int64_t topo_off;      // byte offset of the int16 topology block
     int64_t element_no;
     int32_t filtered;
-    int32_t pad;
+    int32_t SP;            // taxa per column row in codes_t (multiple of 16)
+    int32_t stack_depth;   // partials pending at once in the stack-order traversal
+    int32_t pad2;
 };
 
 // Layout of the int16 topology block (each array length N unless noted).
 struct TopoLayout {
     int nodes, internal, c2a, c2b, par, irank, pos, missing, upc, upcc, hlev_start, hlev_nodes, dlev_start,
-        dlev_nodes, total;
+        dlev_nodes, sord, sflag, total;
     __host__ __device__ static TopoLayout make(int N) {
         TopoLayout t;
         int o = 0;
@@ -85,6 +88,8 @@ struct TopoLayout {
         t.hlev_nodes = o; o += N;
         t.dlev_start = o; o += N + 1;
         t.dlev_nodes = o; o += N;
+        t.sord = o; o += N;    // internal nodes in a postorder that visits the child needing more stack first
+        t.sflag = o; o += N;   // bit 0: the first child's (c2a) partial is on top of the stack at its parent
         t.total = o;
         return t;
     }
@@ -117,7 +122,17 @@ struct NodeRec {
     int8_t m0, m1;       // child missing (skipped by the prune)
     int8_t missing;      // this node missing
     int8_t is_root;
-    int32_t pad;
+    int16_t self;        // node id
+    int16_t prank;       // internal rank of the parent (-1 for the root)
+};
+
+// One non-root node of the pruned tree for the emission histogram.
+struct EmRec {
+    int16_t node;        // node id
+    int16_t rank;        // internal rank, -1 for a leaf
+    int16_t prank;       // internal rank of the parent
+    int8_t missing;
+    int8_t pad;
 };
 
 // Parameters of one chain-kernel launch.
@@ -171,7 +186,9 @@ struct BatchParams {
     DevCounters* counters;
     int* n_done;              // number of slots that reached PH_DONE in this launch
     int* next_slot;           // slot queue (atomic)
+    int* done_list;           // slots that reached PH_DONE in this launch (n_done entries), or null
     int n_int_max, S_max;
+    int stack_depth;          // max over admitted elements
 };
 
 }  // namespace pacc

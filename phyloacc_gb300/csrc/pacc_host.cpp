@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <deque>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -37,9 +38,9 @@ cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out,
 cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st);
 cudaError_t set_model_batch(const DevModel& m);
-size_t batch_warp_smem(int N, int NI, int S, int prec);
+size_t batch_warp_smem(int N, int NI, int S, int D, int prec);
 size_t batch_slot_bytes(int N, int T);
-size_t batch_grp_bytes(int mcmc);
+size_t batch_grp_bytes(int mcmc, int NI, int prec);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
 cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, cudaStream_t st);
 
@@ -61,12 +62,15 @@ struct HostElem {
     int filtered = 0;
     int GG = 0, GGp = 0, root = 0, n_nodes = 0, n_int = 0, n_hlev = 0, n_dlev = 0, tg_draws = 0;
     std::vector<uint8_t> codes;    // [S][GGp]
+    std::vector<uint8_t> codes_t;  // [GGp][SP] column-major copy for 128-bit per-column loads
     std::vector<int8_t> tg0;       // [n_int][GGp]
     std::vector<int32_t> prefix;   // [GG+1]
     std::vector<int16_t> topo;     // TopoLayout
     std::vector<double> dist2;     // [N]
     std::vector<int8_t> tg_full;   // [GG][N] (debug encode only)
     std::vector<uint8_t> missing;  // [N]
+    std::vector<int> sord, sflag;  // stack order of internal nodes, pop-order flags
+    int stack_depth = 0;
 };
 
 static inline uint8_t encode_char(uint8_t ch, char gapchar) {
@@ -122,6 +126,10 @@ static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* ba
     E.codes.assign((size_t)S * GGp, CODE_GAP);
     for (int s = 0; s < S; s++)
         for (int i = 0; i < GG; i++) E.codes[(size_t)s * GGp + i] = code[(size_t)s * len + cols[i]];
+    const int SP = (S + 15) & ~15;
+    E.codes_t.assign((size_t)GGp * SP, CODE_GAP);
+    for (int i = 0; i < GG; i++)
+        for (int s = 0; s < S; s++) E.codes_t[(size_t)i * SP + s] = E.codes[(size_t)s * GGp + i];
     // gap counts and missing flags (bpp_c.hpp:303-351)
     std::vector<int> num_missing(S, 0);
     for (int s = 0; s < S; s++)
@@ -266,6 +274,46 @@ static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* ba
         t[TL.dlev_start + maxd] = (int16_t)k;
         E.n_dlev = maxd;
     }
+    // stack order for the batched kernel: a postorder that visits the child
+    // subtree needing more pending partials first (Sethi-Ullman), so that at
+    // most E.stack_depth partials are pending at once
+    {
+        std::vector<int> need(N, 0);
+        for (int s : nodes) {
+            if (s < S) continue;
+            int a = c2a[s], b = c2b[s];
+            int na = a >= S ? need[a] : 0, nb = b >= S ? need[b] : 0;
+            if (a < S && b < S) need[s] = 1;
+            else if (a < S) need[s] = std::max(nb, 1);
+            else if (b < S) need[s] = std::max(na, 1);
+            else need[s] = std::max(std::max(na, nb), 1 + std::min(na, nb));
+        }
+        E.stack_depth = need[root];
+        std::vector<int> sord;
+        std::vector<int> sflag(N, 0);
+        std::vector<std::pair<int, int>> st;  // (node, state)
+        st.push_back({root, 0});
+        while (!st.empty()) {
+            auto cur = st.back();
+            st.pop_back();
+            int s = cur.first;
+            if (s < S) continue;
+            if (cur.second == 1) { sord.push_back(s); continue; }
+            int a = c2a[s], b = c2b[s];
+            bool a_int = a >= S, b_int = b >= S;
+            int first = a, second = b;
+            if (a_int && b_int && need[b] > need[a]) { first = b; second = a; sflag[s] = 1; }
+            st.push_back({s, 1});
+            st.push_back({second, 0});
+            st.push_back({first, 0});
+        }
+        E.sord = sord;
+        E.sflag = sflag;
+    }
+    for (int i = 0; i < N; i++) {
+        t[TL.sord + i] = (int16_t)(i < (int)E.sord.size() ? E.sord[i] : -1);
+        t[TL.sflag + i] = (int16_t)E.sflag[i];
+    }
     E.dist2 = d2;
     E.root = root;
     E.n_nodes = (int)nodes.size();
@@ -284,6 +332,37 @@ static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* ba
 }  // namespace pacc
 
 using namespace pacc;
+
+// Serving state: chain slots resident on the device, admitted from a host
+// queue as slots free up, advanced by a CUDA-graph-captured sweep step.
+struct Server {
+    bool ready = false;
+    int n_slots = 0, warps = 4, grid = 0, prec = 1, D = 1, n_int_max = 1, GG_cap = 0, SP = 16;
+    size_t smem = 0, slot_b = 0, grp_b = 0, blob_b = 0, tb = 0, o_prefix = 0, o_codes = 0;
+    char* dev = nullptr;
+    ElemHeader* d_hdr = nullptr;
+    char* d_blob = nullptr;
+    SlotState* d_slots = nullptr;
+    char* d_slotws = nullptr;
+    char* d_grp = nullptr;
+    DevResult* d_res = nullptr;
+    int32_t* d_mz = nullptr;
+    double* d_pz = nullptr;
+    DevCounters* d_cnt = nullptr;
+    int* d_ctr = nullptr;       // [0] n_done, [32] next_slot
+    int* d_done = nullptr;
+    int* h_done = nullptr;      // pinned: [0] count, [1..] slots
+    BatchParams p;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<int> free_slots;
+    std::vector<int64_t> slot_no;
+    std::vector<double> slot_t0;
+    std::deque<std::pair<HostElem, double>> queue;
+    int resident = 0;
+    long long steps = 0;
+    double kernel_ms = 0;
+};
 
 struct pacc_ctx {
     HostModel M;
@@ -309,6 +388,7 @@ struct pacc_ctx {
     void* d_ws = nullptr; size_t ws_cap = 0;
     void* d_blob = nullptr; size_t blob_cap = 0;
     void* d_misc = nullptr; size_t misc_cap = 0;
+    Server srv;
 };
 
 static std::string g_create_error;
@@ -447,8 +527,314 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->d_ws) cudaFree(c->d_ws);
     if (c->d_blob) cudaFree(c->d_blob);
     if (c->d_misc) cudaFree(c->d_misc);
+    if (c->srv.gexec) cudaGraphExecDestroy(c->srv.gexec);
+    if (c->srv.graph) cudaGraphDestroy(c->srv.graph);
+    if (c->srv.dev) cudaFree(c->srv.dev);
+    if (c->srv.h_done) cudaFreeHost(c->srv.h_done);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+// ---------------------------------------------------------------------------
+// serving: resident chain slots, continuous admission (batched kernel only)
+// ---------------------------------------------------------------------------
+static bool serving(const pacc_ctx* c) { return c->o.sweeps_per_launch > 0 && c->o.precision != PACC_FP64; }
+
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Stack depth bound of the unpruned tree: pruning only removes nodes.
+static int tree_stack_depth(const HostModel& M) {
+    std::vector<int> need(M.N, 0);
+    for (int s = M.S; s < M.N; s++) {  // ids are postorder: children before parents
+        int a = M.ch0[s], b = M.ch1[s];
+        int na = a >= M.S ? need[a] : 0, nb = b >= M.S ? need[b] : 0;
+        if (a < M.S && b < M.S) need[s] = 1;
+        else if (a < M.S) need[s] = std::max(nb, 1);
+        else if (b < M.S) need[s] = std::max(na, 1);
+        else need[s] = std::max(std::max(na, nb), 1 + std::min(na, nb));
+    }
+    return std::max(1, need[M.N - 1]);
+}
+
+static int server_setup(pacc_ctx* c, int GG_needed) {
+    Server& v = c->srv;
+    if (v.ready) return PACC_OK;
+    const int N = c->M.N, S = c->M.S;
+    const int T = c->o.burnin + c->o.mcmc;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    v.prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    v.D = tree_stack_depth(c->M);
+    v.n_int_max = S - 1;
+    v.SP = (S + 15) & ~15;
+    v.GG_cap = std::max(5120, (GG_needed + 31) & ~31);
+    v.warps = 4;
+    size_t wsm = batch_warp_smem(N, v.n_int_max, S, v.D, v.prec);
+    int max_smem = 0, smem_sm = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+    while (v.warps > 1 && wsm * v.warps > (size_t)max_smem) v.warps--;
+    if (wsm > (size_t)max_smem) { c->err = "element tree too large for the batched kernel"; return PACC_EUNSUPPORTED; }
+    v.smem = wsm * v.warps;
+    int per_sm = std::max(1, std::min((int)(smem_sm / (v.smem + 1024)), 2048 / (v.warps * 32)));
+    v.grid = c->n_sm * per_sm;
+    const int n_warps = v.grid * v.warps;
+    v.tb = al(topo_bytes(N));
+    v.o_prefix = v.tb;
+    v.o_codes = al(v.o_prefix + (size_t)(v.GG_cap + 1) * 4);
+    v.blob_b = al(v.o_codes + (size_t)v.GG_cap * v.SP);
+    v.slot_b = al(batch_slot_bytes(N, T));
+    v.grp_b = al(batch_grp_bytes(c->o.mcmc, v.n_int_max, v.prec));
+    size_t per_slot = v.blob_b + v.slot_b + al(sizeof(ElemHeader)) + al(sizeof(SlotState)) + al(sizeof(DevResult)) +
+                      al(3 * N * 4) + al(3 * N * 4 * 8) + 8;
+    size_t budget = (size_t)c->o.memory_budget_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = fr / 4;
+    }
+    int want = c->o.max_resident > 0 ? c->o.max_resident : 2 * n_warps;
+    size_t fixed = (size_t)n_warps * v.grp_b + (1 << 20);
+    if (budget <= fixed + per_slot) { c->err = "memory budget too small for one chain slot"; return PACC_OOM; }
+    v.n_slots = (int)std::min<size_t>((size_t)want, (budget - fixed) / per_slot);
+    const int ns = v.n_slots;
+    size_t o = 0;
+    size_t o_hdr = o; o = al(o + sizeof(ElemHeader) * ns);
+    size_t o_blob = o; o = al(o + v.blob_b * ns);
+    size_t o_slots = o; o = al(o + sizeof(SlotState) * ns);
+    size_t o_sws = o; o = al(o + v.slot_b * ns);
+    size_t o_grp = o; o = al(o + v.grp_b * n_warps);
+    size_t o_res = o; o = al(o + sizeof(DevResult) * ns);
+    size_t o_mz = o; o = al(o + sizeof(int32_t) * 3 * N * (size_t)ns);
+    size_t o_pz = o; o = al(o + sizeof(double) * 3 * N * 4 * (size_t)ns);
+    size_t o_cnt = o; o = al(o + sizeof(DevCounters));
+    size_t o_ctr = o; o = al(o + 256);
+    size_t o_done = o; o = al(o + sizeof(int) * (ns + 1));
+    if (!cuda_ok(c, cudaMalloc((void**)&v.dev, o), "cudaMalloc (serving slots)")) return PACC_OOM;
+    if (!cuda_ok(c, cudaMallocHost((void**)&v.h_done, sizeof(int) * (ns + 2)), "cudaMallocHost")) return PACC_OOM;
+    v.d_hdr = (ElemHeader*)(v.dev + o_hdr);
+    v.d_blob = v.dev + o_blob;
+    v.d_slots = (SlotState*)(v.dev + o_slots);
+    v.d_slotws = v.dev + o_sws;
+    v.d_grp = v.dev + o_grp;
+    v.d_res = (DevResult*)(v.dev + o_res);
+    v.d_mz = (int32_t*)(v.dev + o_mz);
+    v.d_pz = (double*)(v.dev + o_pz);
+    v.d_cnt = (DevCounters*)(v.dev + o_cnt);
+    v.d_ctr = (int*)(v.dev + o_ctr);
+    v.d_done = (int*)(v.dev + o_done);
+    cudaStream_t st = c->stream;
+    if (!cuda_ok(c, cudaMemsetAsync(v.dev, 0, o, st), "memset slots")) return PACC_ECUDA;
+    // every slot starts empty
+    std::vector<int32_t> empty(ns, -1);
+    int32_t* d_e = nullptr;
+    if (!cuda_ok(c, cudaMalloc((void**)&d_e, sizeof(int32_t) * ns), "cudaMalloc") ||
+        !cuda_ok(c, cudaMemcpyAsync(d_e, empty.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, st), "H2D") ||
+        !cuda_ok(c, launch_init_slots(v.d_slots, d_e, ns, st), "init slots") ||
+        !cuda_ok(c, cudaStreamSynchronize(st), "init slots"))
+        return PACC_ECUDA;
+    cudaFree(d_e);
+    std::memset(&v.p, 0, sizeof(v.p));
+    v.p.hdr = v.d_hdr;
+    v.p.blob = (const uint8_t*)v.d_blob;
+    v.p.slots = v.d_slots;
+    v.p.n_slots = ns;
+    v.p.slot_ws = v.d_slotws;
+    v.p.slot_ws_stride = v.slot_b;
+    v.p.grp_ws = v.d_grp;
+    v.p.grp_ws_stride = v.grp_b;
+    v.p.sweeps = c->o.sweeps_per_launch;
+    v.p.results = v.d_res;
+    v.p.max_z = v.d_mz;
+    v.p.post_z = v.d_pz;
+    v.p.counters = v.d_cnt;
+    v.p.n_done = v.d_ctr;
+    v.p.next_slot = v.d_ctr + 32;
+    v.p.done_list = v.d_done;
+    v.p.n_int_max = v.n_int_max;
+    v.p.S_max = S;
+    v.p.stack_depth = v.D;
+    // the sweep step: reset the queue counters, advance every resident chain,
+    // copy the list of chains that finished back to pinned host memory
+    auto record = [&](cudaStream_t s2) -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(v.d_ctr, 0, 256, s2);
+        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, s2);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, s2);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * ns, cudaMemcpyDeviceToHost, s2);
+        return e;
+    };
+    // one step over the empty slots outside capture: sets the kernel's
+    // shared-memory attribute and checks the launch geometry
+    if (!cuda_ok(c, record(st), "first sweep step") || !cuda_ok(c, cudaStreamSynchronize(st), "first sweep step"))
+        return PACC_ECUDA;
+    if (c->o.use_graphs) {
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = record(st);
+        cudaError_t e2 = cudaStreamEndCapture(st, &v.graph);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&v.gexec, v.graph, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (v.graph) { cudaGraphDestroy(v.graph); v.graph = nullptr; }
+            v.gexec = nullptr;
+        }
+    }
+    v.free_slots.clear();
+    for (int i = ns - 1; i >= 0; i--) v.free_slots.push_back(i);
+    v.slot_no.assign(ns, 0);
+    v.slot_t0.assign(ns, 0);
+    v.resident = 0;
+    v.ready = true;
+    return PACC_OK;
+}
+
+// Move queued elements into free slots.
+static int server_admit(pacc_ctx* c) {
+    Server& v = c->srv;
+    const int N = c->M.N;
+    cudaStream_t st = c->stream;
+    std::vector<std::pair<int, std::pair<HostElem, double>>> adm;
+    while (!v.free_slots.empty() && !v.queue.empty()) {
+        int slot = v.free_slots.back();
+        v.free_slots.pop_back();
+        adm.push_back({slot, std::move(v.queue.front())});
+        v.queue.pop_front();
+    }
+    if (adm.empty()) return PACC_OK;
+    // stage every admitted element contiguously in pinned memory, then copy
+    size_t tot = 0;
+    for (auto& a : adm) {
+        const HostElem& E = a.second.first;
+        tot += v.tb + E.prefix.size() * 4 + E.codes_t.size() + sizeof(ElemHeader) + sizeof(SlotState) + 64;
+    }
+    char* hs = nullptr;
+    if (!cuda_ok(c, cudaMallocHost((void**)&hs, tot), "cudaMallocHost")) return PACC_OOM;
+    size_t off = 0;
+    for (auto& a : adm) {
+        const int slot = a.first;
+        const HostElem& E = a.second.first;
+        char* reg = v.d_blob + (size_t)slot * v.blob_b;
+        ElemHeader H;
+        std::memset(&H, 0, sizeof(H));
+        H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
+        H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws; H.stack_depth = E.stack_depth;
+        H.element_no = E.no;
+        H.SP = v.SP;
+        H.topo_off = (int64_t)(reg - v.d_blob);
+        H.prefix_off = H.topo_off + (int64_t)v.o_prefix;
+        H.codes_t_off = H.topo_off + (int64_t)v.o_codes;
+        H.codes_off = H.codes_t_off;
+        H.tg_off = 0;
+        char* p0 = hs + off;
+        std::memcpy(p0, E.topo.data(), E.topo.size() * 2);
+        std::memcpy(p0 + ((E.topo.size() * 2 + 15) & ~(size_t)15), E.dist2.data(), N * 8);
+        char* p1 = p0 + v.tb;
+        std::memcpy(p1, E.prefix.data(), E.prefix.size() * 4);
+        char* p2 = p1 + E.prefix.size() * 4;
+        std::memcpy(p2, E.codes_t.data(), E.codes_t.size());
+        char* p3 = p2 + E.codes_t.size();
+        std::memcpy(p3, &H, sizeof(H));
+        SlotState S0;
+        std::memset(&S0, 0, sizeof(S0));
+        S0.elem = slot;
+        S0.phase = 0;  // PH_INIT
+        char* p4 = p3 + sizeof(H);
+        std::memcpy(p4, &S0, sizeof(S0));
+        bool ok = cuda_ok(c, cudaMemcpyAsync(reg, p0, v.tb, cudaMemcpyHostToDevice, st), "H2D topo") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_prefix, p1, E.prefix.size() * 4, cudaMemcpyHostToDevice, st), "H2D prefix") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_codes, p2, E.codes_t.size(), cudaMemcpyHostToDevice, st), "H2D codes") &&
+                  cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, p3, sizeof(H), cudaMemcpyHostToDevice, st), "H2D header") &&
+                  cuda_ok(c, cudaMemcpyAsync(v.d_slots + slot, p4, sizeof(S0), cudaMemcpyHostToDevice, st), "H2D slot") &&
+                  cuda_ok(c, cudaMemsetAsync(v.d_res + slot, 0, sizeof(DevResult), st), "memset result");
+        if (!ok) { cudaFreeHost(hs); return PACC_ECUDA; }
+        off += v.tb + E.prefix.size() * 4 + E.codes_t.size() + sizeof(H) + sizeof(S0) + 64;
+        v.slot_no[slot] = E.no;
+        v.slot_t0[slot] = a.second.second;
+        v.resident++;
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFreeHost(hs);
+    return cuda_ok(c, e, "admission") ? PACC_OK : PACC_ECUDA;
+}
+
+// One sweep step over the resident chains; finished chains become results.
+static int server_step(pacc_ctx* c) {
+    Server& v = c->srv;
+    const int N = c->M.N;
+    int st0 = server_admit(c);
+    if (st0 != PACC_OK) return st0;
+    if (v.resident == 0) return PACC_OK;
+    cudaStream_t st = c->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    cudaError_t e;
+    if (v.gexec) e = cudaGraphLaunch(v.gexec, st);
+    else {
+        e = cudaMemsetAsync(v.d_ctr, 0, 256, st);
+        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * v.n_slots, cudaMemcpyDeviceToHost, st);
+    }
+    cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (!cuda_ok(c, e, "sweep step")) return PACC_ECUDA;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    v.kernel_ms += ms;
+    v.steps++;
+    const int nd = v.h_done[0];
+    if (nd <= 0) return PACC_OK;
+    int clk_khz = 0;
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, c->device);
+    std::vector<DevResult> res(nd);
+    std::vector<int32_t> mz((size_t)nd * 3 * N);
+    std::vector<double> pz((size_t)nd * 3 * N * 4);
+    for (int i = 0; i < nd; i++) {
+        int slot = v.h_done[1 + i];
+        cudaMemcpyAsync(&res[i], v.d_res + slot, sizeof(DevResult), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&mz[(size_t)i * 3 * N], v.d_mz + (size_t)slot * 3 * N, sizeof(int32_t) * 3 * N,
+                        cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&pz[(size_t)i * 3 * N * 4], v.d_pz + (size_t)slot * 3 * N * 4, sizeof(double) * 3 * N * 4,
+                        cudaMemcpyDeviceToHost, st);
+    }
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "D2H results")) return PACC_ECUDA;
+    const double t = now_ms();
+    for (int i = 0; i < nd; i++) {
+        int slot = v.h_done[1 + i];
+        pacc_ctx::Done d;
+        std::memset(&d.r, 0, sizeof(d.r));
+        d.r.element_no = v.slot_no[slot];
+        d.r.n_nodes = N;
+        const DevResult& R = res[i];
+        d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
+        for (int m = 0; m < 3; m++) {
+            pacc_model_result& mr = d.r.model[m];
+            mr.loglik = R.model[m].loglik;
+            mr.max_loglik = R.model[m].max_loglik;
+            mr.n_rate = R.model[m].rates[0];
+            mr.c_rate = R.model[m].rates[1];
+            mr.g_rate = R.model[m].rates[2];
+            mr.l_rate = R.model[m].rates[3];
+            mr.l2_rate = R.model[m].rates[4];
+            mr.failure = R.model[m].failure;
+            mr.n_configs = R.model[m].n_configs;
+        }
+        d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
+        d.r.latency_ms = t - v.slot_t0[slot];
+        d.max_z.assign(mz.begin() + (size_t)i * 3 * N, mz.begin() + (size_t)(i + 1) * 3 * N);
+        d.post_z.assign(pz.begin() + (size_t)i * 3 * N * 4, pz.begin() + (size_t)(i + 1) * 3 * N * 4);
+        c->done.push_back(std::move(d));
+        // the slot's device state is PH_DONE, which the kernel skips until re-admission
+        v.free_slots.push_back(slot);
+        v.resident--;
+    }
+    return PACC_OK;
 }
 
 int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
@@ -475,6 +861,31 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
     work();
     for (auto& t : th) t.join();
     if (bad) { c->pending.resize(base); c->err = "invalid element"; return PACC_EINVAL; }
+    if (serving(c)) {
+        if (!c->gpu_ok) return PACC_ECUDA;
+        int gmax = 0;
+        for (size_t i = base; i < c->pending.size(); i++) gmax = std::max(gmax, c->pending[i].GG);
+        int st = server_setup(c, gmax);
+        if (st != PACC_OK) return st;
+        const double t = now_ms();
+        for (size_t i = base; i < c->pending.size(); i++) {
+            HostElem& E = c->pending[i];
+            if (E.filtered) {
+                pacc_ctx::Done d;
+                std::memset(&d.r, 0, sizeof(d.r));
+                d.r.element_no = E.no;
+                d.r.n_nodes = c->M.N;
+                d.r.status = E.filtered == 2 ? PACC_SAMPLER_ERROR : PACC_FILTERED;
+                d.max_z.assign(3 * c->M.N, 0);
+                d.post_z.assign(3 * c->M.N * 4, 0.0);
+                c->done.push_back(std::move(d));
+                continue;
+            }
+            if (E.GG > c->srv.GG_cap) { c->err = "element longer than the serving slot capacity"; return PACC_EINVAL; }
+            c->srv.queue.push_back({std::move(E), t});
+        }
+        c->pending.resize(base);
+    }
     return PACC_OK;
 }
 
@@ -547,7 +958,10 @@ static int run_pending(pacc_ctx* c) {
         if (E.filtered) continue;
         H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
         H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws;
+        H.stack_depth = E.stack_depth;
         H.codes_off = off; off = al(off + E.codes.size());
+        H.codes_t_off = off; off = al(off + E.codes_t.size());
+        H.SP = (S + 15) & ~15;
         H.tg_off = off; off = al(off + E.tg0.size());
         H.prefix_off = off; off = al(off + E.prefix.size() * 4);
         H.topo_off = off; off = al(off + tb);
@@ -560,6 +974,7 @@ static int run_pending(pacc_ctx* c) {
         if (E.filtered) continue;
         ElemHeader& H = hdr[e];
         std::memcpy(&blob[H.codes_off], E.codes.data(), E.codes.size());
+        std::memcpy(&blob[H.codes_t_off], E.codes_t.data(), E.codes_t.size());
         std::memcpy(&blob[H.tg_off], E.tg0.data(), E.tg0.size());
         std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
         std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
@@ -667,10 +1082,15 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     std::vector<int32_t> elem;
     for (int e = 0; e < n; e++) if (!c->pending[e].filtered) elem.push_back(e);
+    // longest elements first: the last chains to start are the short ones
+    std::stable_sort(elem.begin(), elem.end(),
+                     [&](int a, int b) { return c->pending[a].GG > c->pending[b].GG; });
     const int n_slots = std::max(1, (int)elem.size());
     if (elem.empty()) elem.push_back(-1);
+    int D = 1;
+    for (int e = 0; e < n; e++) if (!c->pending[e].filtered) D = std::max(D, c->pending[e].stack_depth);
     // geometry: warps per CTA from the shared-memory footprint of one chain
-    size_t wsm = batch_warp_smem(N, n_int_max, S, prec);
+    size_t wsm = batch_warp_smem(N, n_int_max, S, D, prec);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     int warps = c->o.block_threads > 0 ? std::min(4, std::max(1, c->o.block_threads / 32)) : 4;
@@ -689,7 +1109,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     int grid = std::max(1, std::min(c->n_sm * per_sm, (n_slots + warps - 1) / warps));
     const int n_warps = grid * warps;
     size_t slot_b = al(batch_slot_bytes(N, T));
-    size_t grp_b = al(batch_grp_bytes(c->o.mcmc));
+    size_t grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec));
     size_t o_hdr = 0;
     size_t o_res = al(o_hdr + sizeof(ElemHeader) * n);
     size_t o_mz = al(o_res + sizeof(DevResult) * n);
@@ -734,6 +1154,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     p.next_slot = (int*)(mb + o_next + 128);
     p.n_int_max = n_int_max;
     p.S_max = S;
+    p.stack_depth = D;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -790,12 +1211,19 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
 
 int pacc_sync(pacc_ctx* c) {
     if (!c) return PACC_EINVAL;
+    if (serving(c)) {
+        while (!c->srv.queue.empty() || c->srv.resident > 0) {
+            int st = server_step(c);
+            if (st != PACC_OK) return st;
+        }
+        return PACC_OK;
+    }
     return run_pending(c);
 }
 
 int pacc_pending(pacc_ctx* c) {
     if (!c) return 0;
-    return (int)(c->pending.size() + (c->done.size() - c->done_head));
+    return (int)(c->pending.size() + c->srv.queue.size() + c->srv.resident + (c->done.size() - c->done_head));
 }
 
 static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
@@ -828,6 +1256,10 @@ static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
 
 int pacc_poll(pacc_ctx* c, pacc_result* out, int max) {
     if (!c || (!out && max > 0)) return -PACC_EINVAL;
+    if (serving(c) && c->done_head == c->done.size() && (!c->srv.queue.empty() || c->srv.resident > 0)) {
+        int st = server_step(c);
+        if (st != PACC_OK) return -st;
+    }
     int k = 0;
     while (k < max && c->done_head < c->done.size()) {
         fill_result(c, c->done[c->done_head], &out[k]);
@@ -845,12 +1277,59 @@ int pacc_run(pacc_ctx* c, const pacc_element_batch* b, pacc_result* out) {
     if (st != PACC_OK) return st;
     st = pacc_sync(c);
     if (st != PACC_OK) return st;
+    if (serving(c)) {
+        // results arrive in completion order: put them back in batch order
+        std::vector<pacc_result> tmp(b->n_elements);
+        const int N = c->M.N;
+        std::vector<int32_t> mz((size_t)b->n_elements * 3 * N);
+        std::vector<double> pz((size_t)b->n_elements * 3 * N * 4);
+        for (int i = 0; i < b->n_elements; i++) {
+            std::memset(&tmp[i], 0, sizeof(pacc_result));
+            tmp[i].max_z = &mz[(size_t)i * 3 * N];
+            tmp[i].post_z = &pz[(size_t)i * 3 * N * 4];
+        }
+        int k = pacc_poll(c, tmp.data(), b->n_elements);
+        if (k != b->n_elements) return PACC_ECUDA;
+        std::vector<int> pos(b->n_elements, -1);
+        for (int i = 0; i < b->n_elements; i++) {
+            int64_t no = b->element_no ? b->element_no[i] : i;
+            for (int j = 0; j < k; j++)
+                if (tmp[j].element_no == no && pos[j] < 0) { pos[j] = i; break; }
+        }
+        for (int j = 0; j < k; j++) {
+            int i = pos[j];
+            if (i < 0) return PACC_ECUDA;
+            int32_t* omz = out[i].max_z;
+            double* opz = out[i].post_z;
+            pacc_trace tr = out[i].trace;
+            out[i] = tmp[j];
+            out[i].max_z = omz;
+            out[i].post_z = opz;
+            out[i].trace = tr;
+            if (omz) std::memcpy(omz, tmp[j].max_z, sizeof(int32_t) * 3 * N);
+            if (opz) std::memcpy(opz, tmp[j].post_z, sizeof(double) * 3 * N * 4);
+        }
+        return PACC_OK;
+    }
     int k = pacc_poll(c, out, b->n_elements);
     return k == b->n_elements ? PACC_OK : PACC_ECUDA;
 }
 
 int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
     if (!c || !out) return PACC_EINVAL;
+    if (serving(c) && c->srv.ready) {
+        DevCounters dc;
+        if (cudaMemcpy(&dc, c->srv.d_cnt, sizeof(dc), cudaMemcpyDeviceToHost) != cudaSuccess) return PACC_ECUDA;
+        pacc_counters& pc = c->counters;
+        std::memset(&pc, 0, sizeof(pc));
+        pc.edge_updates_internal = (double)dc.edge_internal;
+        pc.edge_updates_leaf = (double)dc.edge_leaf;
+        pc.tg_draws = (double)dc.tg_draws;
+        pc.kernel_ms = c->srv.kernel_ms;
+        pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
+        pc.iterations = (double)c->srv.steps;
+        for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
+    }
     *out = c->counters;
     return PACC_OK;
 }
