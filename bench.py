@@ -185,6 +185,59 @@ def time_gpu(ctx, ds, steps, warmup, ws, clocks=None):
     return kern, wall, cnt, res
 
 
+def serve_latency(ds, throughput, seconds, sweeps, seed=1):
+    """Open-loop serving at 80% of the batch throughput.
+
+    Elements arrive as a Poisson process (rate 0.8 x throughput, cycling
+    through the workload); each poll runs one sweep step of the resident
+    chains and retires the finished ones.  Latency = time the result came back
+    minus the element's scheduled arrival time, for elements arriving in the
+    last two thirds of the window (after the slots have filled)."""
+    import phyloacc_gb300 as pg
+    from phyloacc_gb300 import abi
+    o = opts_for(abi.PACC_FP32)
+    o.sweeps_per_launch = sweeps
+    ctx = pg.Context(ds, o)
+    rate = 0.8 * throughput
+    rng = np.random.default_rng(seed)
+    n_max = int(rate * seconds * 1.5) + 16
+    arrive = np.cumsum(rng.exponential(1.0 / rate, n_max))
+    arrive = arrive[arrive < seconds]
+    E = ds.n_elements
+    measured = {k for k in range(len(arrive)) if arrive[k] >= seconds / 3}
+    lat = {}
+    k_next = 0
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        k_end = int(np.searchsorted(arrive, now, side="right"))
+        if k_end > k_next:
+            idx = [k % E for k in range(k_next, k_end)]
+            ctx.submit(ds.subset(idx), element_no=np.arange(k_next, k_end))
+            k_next = k_end
+        if ctx.pending() > 0:
+            r = ctx.poll(4096)
+            t = time.perf_counter() - t0
+            for i in range(r.n):
+                k = int(r.arr[i].element_no)
+                if k in measured:
+                    lat[k] = (t - arrive[k]) * 1e3
+        else:
+            time.sleep(0.001)
+        if k_next >= len(arrive) and measured.issubset(lat.keys()):
+            break
+        if time.perf_counter() - t0 > 6 * seconds + 600:
+            break
+    wall = time.perf_counter() - t0
+    ctx.close()
+    v = np.array(list(lat.values()))
+    return {"load": 0.8, "arrival_rate": rate, "window_s": seconds, "sweeps_per_launch": sweeps,
+            "elements_measured": int(len(v)), "elements_submitted": int(k_next),
+            "p50_ms": float(np.percentile(v, 50)) if len(v) else None,
+            "p99_ms": float(np.percentile(v, 99)) if len(v) else None,
+            "wall_s": wall}
+
+
 def run_gpu(args, ws, rank, local):
     import phyloacc_gb300 as pg
     from phyloacc_gb300 import abi
@@ -237,6 +290,9 @@ def run_gpu(args, ws, rank, local):
         "counters": {k: cnt[k] for k in ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "iterations")},
         "clocks": clk,
     }
+    if args.serve_seconds > 0:
+        line["serving"] = serve_latency(ds, value / ws, args.serve_seconds, args.serve_sweeps)
+        line["latency_ms"] = {"p50": line["serving"]["p50_ms"], "p99": line["serving"]["p99_ms"]}
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
         v, dt = cpu_baseline(ds, cores, cores)
@@ -256,6 +312,10 @@ def main():
     ap.add_argument("--fp64-elements", type=int, default=608)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="arrival window of the 80%%-load serving run (0: skip)")
+    ap.add_argument("--serve-sweeps", type=int, default=32,
+                    help="sweep budget per serving step (x256 columns per chain)")
     ap.add_argument("--burnin", type=int, default=500, help="profiling only: shorter chains")
     ap.add_argument("--mcmc", type=int, default=1500, help="profiling only: shorter chains")
     args = ap.parse_args()

@@ -109,6 +109,8 @@ typedef struct pacc_opts {
     int32_t trace_iters;          /* record the first trace_iters iterations of every model (0 = off) */
     int32_t block_threads;        /* threads per chain CTA (0 = autotuned) */
     int32_t use_graphs;           /* capture the sweep launches in a CUDA graph (1) */
+    int32_t columns_per_lane;     /* batched kernel: alignment columns each lane carries (1, 2 or 4;
+                                     0 = autotuned) */
 } pacc_opts;
 
 /* A batch of elements.  Element e's alignment block is n_species rows of

@@ -115,6 +115,10 @@ class Context:
         res.n = k
         return res
 
+    def pending(self) -> int:
+        """Elements submitted and not yet returned by poll()."""
+        return lib().pacc_pending(self.h)
+
     def counters(self) -> dict:
         c = abi.PaccCounters()
         lib().pacc_get_counters(self.h, C.byref(c))

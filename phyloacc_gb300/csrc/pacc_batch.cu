@@ -57,7 +57,7 @@ struct GrpLayout {
         GrpLayout L;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-        L.gpart = o; o = al(o + (size_t)NI * 4 * 32 * real_bytes);   // all internal partials of 32 columns
+        L.gpart = o; o = al(o + (size_t)NI * 4 * 32 * real_bytes);   // all internal partials of 32 x C columns (NI = internal nodes x C)
         L.hash = o; o = al(o + (size_t)(mcmc + 1) * 8);
         L.rep = o; o = al(o + (size_t)(mcmc + 1) * 4);
         L.cfg = o; o = al(o + (size_t)(mcmc + 1) * 4);
@@ -70,24 +70,24 @@ struct GrpLayout {
     }
 };
 
-// Shared memory of one warp-chain.
+// Shared memory of one warp-chain; every lane carries C columns.
 template <typename Real>
 struct WarpSmem {
     size_t ptc, part, tgv, hdf, rec, srec, emr, stage, cnt, topo, i8, dbl, total;
-    __host__ __device__ static WarpSmem make(int N, int NI, int S, int D) {
+    __host__ __device__ static WarpSmem make(int N, int NI, int S, int D, int C) {
         WarpSmem w;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
         w.ptc = o; o = al(o + (size_t)N * 16 * sizeof(Real));        // current P^T per branch
-        size_t part_bytes = (size_t)D * 4 * 32 * sizeof(Real);          // stack of pending partials
+        size_t part_bytes = (size_t)D * C * 4 * 32 * sizeof(Real);      // stack of pending partials
         size_t alias_bytes = (size_t)N * 6 * 8;                        // emis + bz alias the stack
         w.part = o; o = al(o + (part_bytes > alias_bytes ? part_bytes : alias_bytes));
-        w.tgv = o; o = al(o + (size_t)NI * 32);
+        w.tgv = o; o = al(o + (size_t)NI * C * 32);
         w.hdf = o; o = al(o + 16);
         w.rec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
         w.srec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
         w.emr = o; o = al(o + (size_t)N * sizeof(EmRec));
-        w.stage = o; o = al(o + (size_t)((S + 15) & ~15) * 32);
+        w.stage = o; o = al(o + (size_t)C * ((S + 15) & ~15) * 32);
         w.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 2);               // uint16 bins
         w.topo = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
         w.i8 = o; o = al(o + (size_t)N * 6);                            // fixZ chg unv mask maxz(unused) Zc
@@ -100,7 +100,7 @@ struct WarpSmem {
 // ---------------------------------------------------------------------------
 // per-warp context
 // ---------------------------------------------------------------------------
-template <typename Real>
+template <typename Real, int C>
 struct W {
     int lane, S, N, GG, GGp, root, n_nodes, n_int, n_hlev, n_dlev, tg_draws, T, burn, mcmc;
     const uint8_t* codes;
@@ -108,14 +108,14 @@ struct W {
     int16_t *nodes, *internal, *c2a, *c2b, *par, *irank, *pos, *missing, *upc, *upcc, *hlev_start, *hlev_nodes,
         *dlev_start, *dlev_nodes;
     Real* ptc;          // [N][16]
-    Real* part;         // [NI][4][32]
-    int8_t* tgv;        // [NI][32]
+    Real* part;         // stack of pending partials [D][C][4][32]
+    int8_t* tgv;        // [NI][C][32] sampled base (or 4: no data) per internal node and column
     int8_t* hdf;        // [NI][32] node has data at this lane's column
     const NodeRec* rec; // [NI] internal nodes in postorder (internal_nodes)
     const NodeRec* srec;// [NI] internal nodes in stack order
-    Real* gpart;        // [NI][4][32] per-warp device scratch: partials of the sampling pass
+    Real* gpart;        // [NI][C][4][32] per-warp device scratch: partials of the sampling pass
     const EmRec* emr;   // [n_nodes - 1]
-    uint32_t* stage;    // [SP/4][32] words of per-lane column codes
+    uint32_t* stage;    // [C][SP/4][32] words of per-lane column codes
     const uint8_t* codes_t;  // [GGp][SP]
     int SP;
     unsigned* cnt;      // [N][20] packed uint16 pairs
@@ -163,8 +163,8 @@ enum { C_NULL = 0, C_CONS = 1, C_NEUT = 2 };
 // Fill the current per-branch matrices: class by Z (null / cons / neut,
 // bpp_c.cpp:661-663); with prop_class >= 0 the branches of that class get the
 // proposal matrices P(d * r_prop) (log_f_Xz, bpp_c.cpp:885-906).
-template <typename Real>
-__device__ void fill_ptc(W<Real>& w, int prop_class, double r_prop) {
+template <typename Real, int C>
+__device__ void fill_ptc(W<Real, C>& w, int prop_class, double r_prop) {
     for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
         int s = w.nodes[i];
         int z = w.Z[s];
@@ -183,8 +183,8 @@ __device__ void fill_ptc(W<Real>& w, int prop_class, double r_prop) {
 
 // Class table k at rate r for all branches of the pruned tree; branches not
 // longer than 1e-10 keep the identity (bpp_c.cpp:191-226) unless force.
-template <typename Real>
-__device__ void build_table(W<Real>& w, int k, double r, bool scaled, bool force, bool skip_short) {
+template <typename Real, int C>
+__device__ void build_table(W<Real, C>& w, int k, double r, bool scaled, bool force, bool skip_short) {
     for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
         int s = w.nodes[i];
         double* out = w.tbl + ((size_t)k * w.N + s) * 16;
@@ -255,106 +255,153 @@ __device__ __forceinline__ int stage_code(const uint32_t* __restrict__ stage, in
     return (stage[(c >> 2) * 32 + lane] >> (8 * (c & 3))) & 0xFF;
 }
 
-// Bottom-up pass over one column held by this lane (Update_Tg without
-// sampling, bpp_c.cpp:647-671).  Internal nodes are visited in stack order
-// (a postorder that takes the child needing more pending partials first); a
-// node pops its internal children's partials and pushes its own, so at most
-// `stack_depth` partials per lane are live.  The "has data" flag of a node
-// (some leaf below is a base or an ambiguity code: the complement of
-// Tg == K, bpp_c.hpp:417-428) travels on a register bit stack.  With STORE,
-// every partial is also written to the warp's device scratch (for the
-// top-down sampling) and the node's no-data mark to tgv.  Returns the rescale
-// exponent of the column; *root gets the root partial (pi included).
-template <typename Real, bool STORE>
-__device__ __forceinline__ int column_up(const NodeRec* __restrict__ srec, int n_int, const uint32_t* __restrict__ stage,
-                                         Real* __restrict__ stk, Real* __restrict__ gpart, int8_t* __restrict__ tgv,
-                                         const Real* __restrict__ ptc, int lane, bool act, unsigned& e_int,
-                                         unsigned& e_leaf, const Real pi[4], Real root[4]) {
-    int sc = 0;
+// Bottom-up pass over the C columns held by this lane (Update_Tg without
+// sampling, bpp_c.cpp:647-671); column j of the lane is stage set j.  Internal
+// nodes are visited in stack order (a postorder that takes the child needing
+// more pending partials first); a node pops its internal children's partials
+// and pushes its own, so at most `stack_depth` partials per column are live.
+// The C columns share every node record and every matrix load, and their
+// arithmetic is independent, which hides the latency of each.  The "has
+// data" flag of a node (some leaf below is a base or an ambiguity code: the
+// complement of Tg == K, bpp_c.hpp:417-428) travels on a register bit stack
+// per column.  With STORE, every partial is also written to the warp's device
+// scratch (for the top-down sampling) and the node's no-data mark to tgv.
+// sc[j] gets the rescale exponent of column j and root[j] its root partial
+// (pi included).
+template <typename Real, int C, bool STORE>
+__device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int n_int,
+                                          const uint32_t* __restrict__ stage, int sstride, Real* __restrict__ stk,
+                                          Real* __restrict__ gpart, int8_t* __restrict__ tgv,
+                                          const Real* __restrict__ ptc, int lane, const bool (&act)[C],
+                                          unsigned& e_int, unsigned& e_leaf, const Real pi[4], Real (&root)[C][4],
+                                          int (&sc)[C]) {
     int sp = 0;
-    unsigned hbits = 0;
+    unsigned hbits[C];
+#pragma unroll
+    for (int j = 0; j < C; j++) { hbits[j] = 0; sc[j] = 0; }
     for (int k = 0; k < n_int; k++) {
         const NodeRec R = srec[k];
-        int code0 = 0, code1 = 0;
-        bool h0 = false, h1 = false;
-        Real x0[4], x1[4];
-        // pop internal children (the child computed last is on top)
         const bool i0 = R.r0 >= 0, i1 = R.r1 >= 0;
+        Real x0[C][4], x1[C][4];
+        bool h0[C], h1[C];
+        int code0[C], code1[C];
+        // pop internal children (the child computed last is on top)
         if (i0 && i1) {
             const bool c0_top = R.prank & 1;   // flags, see NodeRec
-            Real* t = stk + (sp - 1) * 128 + lane;
-            Real* u = stk + (sp - 2) * 128 + lane;
-            const bool ht = hbits & 1, hu = (hbits >> 1) & 1;
-            hbits >>= 2;
+            const Real* t = stk + (sp - 1) * (C * 128) + lane;
+            const Real* u = stk + (sp - 2) * (C * 128) + lane;
             sp -= 2;
-            if (c0_top) {
-                x0[0] = t[0]; x0[1] = t[32]; x0[2] = t[64]; x0[3] = t[96]; h0 = ht;
-                x1[0] = u[0]; x1[1] = u[32]; x1[2] = u[64]; x1[3] = u[96]; h1 = hu;
-            } else {
-                x1[0] = t[0]; x1[1] = t[32]; x1[2] = t[64]; x1[3] = t[96]; h1 = ht;
-                x0[0] = u[0]; x0[1] = u[32]; x0[2] = u[64]; x0[3] = u[96]; h0 = hu;
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                const bool ht = hbits[j] & 1, hu = (hbits[j] >> 1) & 1;
+                hbits[j] >>= 2;
+                Real tt[4], uu[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) { tt[i] = t[j * 128 + i * 32]; uu[i] = u[j * 128 + i * 32]; }
+#pragma unroll
+                for (int i = 0; i < 4; i++) { x0[j][i] = c0_top ? tt[i] : uu[i]; x1[j][i] = c0_top ? uu[i] : tt[i]; }
+                h0[j] = c0_top ? ht : hu;
+                h1[j] = c0_top ? hu : ht;
             }
         } else if (i0 || i1) {
-            Real* t = stk + (sp - 1) * 128 + lane;
-            const bool ht = hbits & 1;
-            hbits >>= 1;
+            const Real* t = stk + (sp - 1) * (C * 128) + lane;
             sp -= 1;
-            if (i0) { x0[0] = t[0]; x0[1] = t[32]; x0[2] = t[64]; x0[3] = t[96]; h0 = ht; }
-            else { x1[0] = t[0]; x1[1] = t[32]; x1[2] = t[64]; x1[3] = t[96]; h1 = ht; }
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                const bool ht = hbits[j] & 1;
+                hbits[j] >>= 1;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const Real v = t[j * 128 + i * 32];
+                    x0[j][i] = v;
+                    x1[j][i] = v;
+                }
+                h0[j] = ht;
+                h1[j] = ht;
+            }
         }
-        if (!i0) { code0 = stage_code(stage, R.c0, lane); h0 = code0 != CODE_GAP && code0 != CODE_OTHER; }
-        if (!i1) { code1 = stage_code(stage, R.c1, lane); h1 = code1 != CODE_GAP && code1 != CODE_OTHER; }
-        const bool hs = h0 || h1;
-        Real a0 = 1, a1 = 1, a2 = 1, a3 = 1;
-        if (act && hs && !R.missing) {
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            code0[j] = 0;
+            code1[j] = 0;
+            if (!i0) { code0[j] = stage_code(stage + j * sstride, R.c0, lane); h0[j] = code0[j] != CODE_GAP && code0[j] != CODE_OTHER; }
+            if (!i1) { code1[j] = stage_code(stage + j * sstride, R.c1, lane); h1[j] = code1[j] != CODE_GAP && code1[j] != CODE_OTHER; }
+        }
+        Real a[C][4];
+        bool hs[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            hs[j] = h0[j] || h1[j];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[j][i] = 1;
+        }
+        if (!R.missing) {
 #pragma unroll
             for (int q = 0; q < 2; q++) {
+                if (q ? R.m1 : R.m0) continue;
                 const int c = q ? R.c1 : R.c0;
-                const bool internal_child = q ? i1 : i0;
-                const int code = q ? code1 : code0;
-                if ((q ? R.m1 : R.m0) || !(q ? h1 : h0)) continue;
                 const Real* __restrict__ Pc = ptc + c * 16;
-                if (!internal_child) {
-                    if (code < 4) {
-                        const Real* Pr = Pc + code * 4;
-                        a0 *= Pr[0]; a1 *= Pr[1]; a2 *= Pr[2]; a3 *= Pr[3];
-                    } else {
-                        int msk = ambig_mask(code - CODE_R);
-                        Real v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+                if (q ? i1 : i0) {
+                    // internal child: one matrix load serves all C columns
+                    Real p[16];
 #pragma unroll
-                        for (int i = 0; i < 4; i++)
-                            if (msk & (1 << i)) { v0 += Pc[i * 4]; v1 += Pc[i * 4 + 1]; v2 += Pc[i * 4 + 2]; v3 += Pc[i * 4 + 3]; }
-                        a0 *= v0; a1 *= v1; a2 *= v2; a3 *= v3;
+                    for (int i = 0; i < 16; i++) p[i] = Pc[i];
+#pragma unroll
+                    for (int j = 0; j < C; j++) {
+                        const Real* x = q ? x1[j] : x0[j];
+                        const bool use = act[j] && hs[j] && (q ? h1[j] : h0[j]);
+                        const Real d0 = (p[0] * x[0] + p[4] * x[1]) + (p[8] * x[2] + p[12] * x[3]);
+                        const Real d1 = (p[1] * x[0] + p[5] * x[1]) + (p[9] * x[2] + p[13] * x[3]);
+                        const Real d2 = (p[2] * x[0] + p[6] * x[1]) + (p[10] * x[2] + p[14] * x[3]);
+                        const Real d3 = (p[3] * x[0] + p[7] * x[1]) + (p[11] * x[2] + p[15] * x[3]);
+                        if (use) {
+                            a[j][0] *= d0; a[j][1] *= d1; a[j][2] *= d2; a[j][3] *= d3;
+                            e_int++;
+                        }
                     }
-                    e_leaf++;
                 } else {
-                    const Real* x = q ? x1 : x0;
-                    a0 *= ((Pc[0] * x[0] + Pc[4] * x[1]) + (Pc[8] * x[2] + Pc[12] * x[3]));
-                    a1 *= ((Pc[1] * x[0] + Pc[5] * x[1]) + (Pc[9] * x[2] + Pc[13] * x[3]));
-                    a2 *= ((Pc[2] * x[0] + Pc[6] * x[1]) + (Pc[10] * x[2] + Pc[14] * x[3]));
-                    a3 *= ((Pc[3] * x[0] + Pc[7] * x[1]) + (Pc[11] * x[2] + Pc[15] * x[3]));
-                    e_int++;
+#pragma unroll
+                    for (int j = 0; j < C; j++) {
+                        const int code = q ? code1[j] : code0[j];
+                        if (!(act[j] && hs[j] && (q ? h1[j] : h0[j]))) continue;
+                        if (code < 4) {
+                            const Real* Pr = Pc + code * 4;
+                            a[j][0] *= Pr[0]; a[j][1] *= Pr[1]; a[j][2] *= Pr[2]; a[j][3] *= Pr[3];
+                        } else {
+                            int msk = ambig_mask(code - CODE_R);
+                            Real v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                                if (msk & (1 << i)) { v0 += Pc[i * 4]; v1 += Pc[i * 4 + 1]; v2 += Pc[i * 4 + 2]; v3 += Pc[i * 4 + 3]; }
+                            a[j][0] *= v0; a[j][1] *= v1; a[j][2] *= v2; a[j][3] *= v3;
+                        }
+                        e_leaf++;
+                    }
                 }
             }
-            Real a[4] = {a0, a1, a2, a3};
-            Resc<Real>::apply(a, sc);
-            a0 = a[0]; a1 = a[1]; a2 = a[2]; a3 = a[3];
+#pragma unroll
+            for (int j = 0; j < C; j++)
+                if (act[j] && hs[j]) Resc<Real>::apply(a[j], sc[j]);
         }
-        if (R.is_root) {
-            a0 *= pi[0]; a1 *= pi[1]; a2 *= pi[2]; a3 *= pi[3];
-            root[0] = a0; root[1] = a1; root[2] = a2; root[3] = a3;
-        }
-        Real* __restrict__ o = stk + sp * 128 + lane;
-        o[0] = a0; o[32] = a1; o[64] = a2; o[96] = a3;
+        Real* __restrict__ o = stk + sp * (C * 128) + lane;
         sp++;
-        hbits = (hbits << 1) | (hs ? 1u : 0u);
-        if (STORE) {
-            Real* __restrict__ gp = gpart + R.self * 128 + lane;
-            gp[0] = a0; gp[32] = a1; gp[64] = a2; gp[96] = a3;
-            tgv[R.self * 32 + lane] = hs ? (int8_t)-1 : (int8_t)4;
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (R.is_root) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) { a[j][i] *= pi[i]; root[j][i] = a[j][i]; }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) o[j * 128 + i * 32] = a[j][i];
+            hbits[j] = (hbits[j] << 1) | (hs[j] ? 1u : 0u);
+            if (STORE) {
+                Real* __restrict__ gp = gpart + (R.self * C + j) * 128 + lane;
+#pragma unroll
+                for (int i = 0; i < 4; i++) gp[i * 32] = a[j][i];
+                tgv[(R.self * C + j) * 32 + lane] = hs[j] ? (int8_t)-1 : (int8_t)4;
+            }
         }
     }
-    return sc;
 }
 
 // Per-column log-likelihood accumulated as (FP64 product of root sums) x 2^exponent.
@@ -375,10 +422,12 @@ struct LLAcc {
 };
 
 // Full prune of all columns with the current matrices; returns the summed
-// per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).
-template <typename Real>
-__device__ __forceinline__ double likelihood_pass(W<Real>& w) {
+// per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).  A pass
+// covers 32 x C columns: lane l takes columns g0 + 32 j + l.
+template <typename Real, int C>
+__device__ __forceinline__ double likelihood_pass(W<Real, C>& w) {
     const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP;
+    const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ srec = w.srec;
     const uint8_t* __restrict__ codes_t = w.codes_t;
     uint32_t* __restrict__ stage = w.stage;
@@ -389,16 +438,25 @@ __device__ __forceinline__ double likelihood_pass(W<Real>& w) {
     double acc = 0;
     LLAcc ll;
     ll.init();
-    for (int g0 = 0; g0 < GG; g0 += 32) {
-        const int g = g0 + lane;
-        const bool act = g < GG;
-        stage_column(codes_t, SP, stage, lane, g, act);
-        Real r[4];
-        int sc = column_up<Real, false>(srec, n_int, stage, stk, nullptr, nullptr, ptc, lane, act, e_int, e_leaf, pi, r);
-        if (act) {
-            double t = (double)r[0] + (double)r[1] + (double)r[2] + (double)r[3];
-            if (sizeof(Real) == 8) acc += log(t) + (double)sc * 0.6931471805599453;
-            else ll.add(t, sc);
+    for (int g0 = 0; g0 < GG; g0 += 32 * C) {
+        bool act[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int g = g0 + 32 * j + lane;
+            act[j] = g < GG;
+            stage_column(codes_t, SP, stage + j * sstride, lane, g, act[j]);
+        }
+        Real r[C][4];
+        int sc[C];
+        column_up<Real, C, false>(srec, n_int, stage, sstride, stk, nullptr, nullptr, ptc, lane, act, e_int, e_leaf,
+                                  pi, r, sc);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (act[j]) {
+                double t = (double)r[j][0] + (double)r[j][1] + (double)r[j][2] + (double)r[j][3];
+                if (sizeof(Real) == 8) acc += log(t) + (double)sc[j] * 0.6931471805599453;
+                else ll.add(t, sc[j]);
+            }
         }
     }
     w.e_int += e_int;
@@ -432,11 +490,14 @@ __device__ __forceinline__ double u_of<float>(uint32_t w) {
 }
 
 // Internal-base pass (Update_Tg with sampling, bpp_c.cpp:672-733) fused with
-// the emission histogram of (child symbol, parent base) pairs.
-template <typename Real>
-__device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
+// the emission histogram of (child symbol, parent base) pairs.  Each column
+// draws from its own words of the stream (prefix[g] words before it), so the
+// draws do not depend on how columns are spread over lanes.
+template <typename Real, int C>
+__device__ __forceinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
     const int NB = NSYM * 4;
-    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, S = w.S, N = w.N, n_nodes = w.n_nodes;
+    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, N = w.N, n_nodes = w.n_nodes;
+    const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ rec = w.rec;
     const NodeRec* __restrict__ srec = w.srec;
     const uint8_t* __restrict__ codes_t = w.codes_t;
@@ -446,11 +507,7 @@ __device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
     Real* __restrict__ part = w.gpart;
     const Real* __restrict__ ptc = w.ptc;
     unsigned* __restrict__ cnt = w.cnt;
-    const int16_t* __restrict__ nodes = w.nodes;
-    const int16_t* __restrict__ internal = w.internal;
     const int16_t* __restrict__ irank = w.irank;
-    const int16_t* __restrict__ par = w.par;
-    const int16_t* __restrict__ missing = w.missing;
     const int32_t* __restrict__ prefix = w.prefix;
     const uint32_t seed = dM.seed;
     const Real pi[4] = {(Real)dM.pi[0], (Real)dM.pi[1], (Real)dM.pi[2], (Real)dM.pi[3]};
@@ -459,37 +516,54 @@ __device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
     int err = 0;
     const int rk = irank[w.root];
     unsigned e_int = 0, e_leaf = 0, n_tg = 0;
-    for (int g0 = 0; g0 < GG; g0 += 32) {
-        const int g = g0 + lane;
-        const bool act = g < GG;
-        stage_column(codes_t, SP, stage, lane, g, act);
-        Real rootp[4];
-        column_up<Real, true>(srec, n_int, stage, stk, part, tgv, ptc, lane, act, e_int, e_leaf, pi, rootp);
-        if (act) {
-            uint64_t wp = pos + (uint64_t)prefix[g];
-            uint64_t blk = wp >> 2;
-            uint32_t words[4];
-            philox4x32_10((uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u, seed, 0u, words);
-            int nn = cat4(rootp, u_of<Real>(words[wp & 3]));
-            wp++;
+    for (int g0 = 0; g0 < GG; g0 += 32 * C) {
+        bool act[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int g = g0 + 32 * j + lane;
+            act[j] = g < GG;
+            stage_column(codes_t, SP, stage + j * sstride, lane, g, act[j]);
+        }
+        Real rootp[C][4];
+        int sc[C];
+        column_up<Real, C, true>(srec, n_int, stage, sstride, stk, part, tgv, ptc, lane, act, e_int, e_leaf, pi,
+                                 rootp, sc);
+        // top-down draws, the C columns interleaved
+        uint64_t wp[C], blk[C];
+        uint32_t words[C][4];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (!act[j]) continue;
+            wp[j] = pos + (uint64_t)prefix[g0 + 32 * j + lane];
+            blk[j] = wp[j] >> 2;
+            philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
+            int nn = cat4(rootp[j], u_of<Real>(words[j][wp[j] & 3]));
+            wp[j]++;
             if (nn > 3) { err = 1; nn = 0; }
-            tgv[rk * 32 + lane] = (int8_t)nn;
+            tgv[(rk * C + j) * 32 + lane] = (int8_t)nn;
             n_tg++;
-            for (int k = n_int - 2; k >= 0; k--) {
-                const NodeRec R = rec[k];
-                if (R.missing || tgv[k * 32 + lane] == 4) { tgv[k * 32 + lane] = 4; continue; }
-                const int tp = tgv[R.prank * 32 + lane];
+        }
+        for (int k = n_int - 2; k >= 0; k--) {
+            const NodeRec R = rec[k];
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                if (!act[j]) continue;
+                int8_t* tk = tgv + (k * C + j) * 32 + lane;
+                if (R.missing || *tk == 4) { *tk = 4; continue; }
+                const int tp = tgv[(R.prank * C + j) * 32 + lane];
                 const Real* __restrict__ Ps = ptc + R.self * 16 + tp;
+                const Real* __restrict__ pk = part + (k * C + j) * 128 + lane;
                 Real q[4];
-                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4] * part[k * 128 + i * 32 + lane];
-                if ((wp >> 2) != blk) {
-                    blk = wp >> 2;
-                    philox4x32_10((uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u, seed, 0u, words);
+#pragma unroll
+                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4] * pk[i * 32];
+                if ((wp[j] >> 2) != blk[j]) {
+                    blk[j] = wp[j] >> 2;
+                    philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
                 }
-                int n2 = cat4(q, u_of<Real>(words[wp & 3]));
-                wp++;
+                int n2 = cat4(q, u_of<Real>(words[j][wp[j] & 3]));
+                wp[j]++;
                 if (n2 > 3) { err = 1; n2 = 0; }
-                tgv[k * 32 + lane] = (int8_t)n2;
+                *tk = (int8_t)n2;
                 n_tg++;
             }
         }
@@ -499,25 +573,28 @@ __device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
             const EmRec E = emr[i];
             if (E.missing) continue;
             const int s = E.node;
-            int key = -1;
-            if (act) {
-                int sym;
-                if (E.rank < 0) {
-                    int code = stage_code(stage, s, lane);
-                    sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
-                } else {
-                    int t = tgv[E.rank * 32 + lane];
-                    sym = t < 4 ? t : -1;
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                int key = -1;
+                if (act[j]) {
+                    int sym;
+                    if (E.rank < 0) {
+                        int code = stage_code(stage + j * sstride, s, lane);
+                        sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
+                    } else {
+                        int t = tgv[(E.rank * C + j) * 32 + lane];
+                        sym = t < 4 ? t : -1;
+                    }
+                    if (sym >= 0) {
+                        int tp = tgv[(E.prank * C + j) * 32 + lane];
+                        if (tp >= 0 && tp < 4) key = sym * 4 + tp;
+                    }
                 }
-                if (sym >= 0) {
-                    int tp = tgv[E.prank * 32 + lane];
-                    if (tp >= 0 && tp < 4) key = sym * 4 + tp;
+                unsigned peers = __match_any_sync(0xffffffffu, key);
+                if (key >= 0 && lane == __ffs(peers) - 1) {
+                    int bin = s * NB + key;
+                    atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
                 }
-            }
-            unsigned peers = __match_any_sync(0xffffffffu, key);
-            if (key >= 0 && lane == __ffs(peers) - 1) {
-                int bin = s * NB + key;
-                atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
             }
         }
     }
@@ -529,8 +606,8 @@ __device__ __forceinline__ int sample_pass(W<Real>& w, uint64_t pos) {
 }
 
 // Emission sums from the histogram (getEmission, bpp_c2.cpp:355-390).
-template <typename Real>
-__device__ void emission_sums(W<Real>& w) {
+template <typename Real, int C>
+__device__ void emission_sums(W<Real, C>& w) {
     const int NB = NSYM * 4;
     for (int t = w.lane; t < (w.n_nodes - 1) * 3; t += 32) {
         int s = w.nodes[t / 3];
@@ -562,8 +639,8 @@ __device__ void emission_sums(W<Real>& w) {
 
 // Latent-state forward filter (linear FP64, normalised per node) and
 // backward sampling (Update_Z_subtree, bpp_c.cpp:1182-1293).
-template <typename Real>
-__device__ int update_z(W<Real>& w, uint64_t pos) {
+template <typename Real, int C>
+__device__ int update_z(W<Real, C>& w, uint64_t pos) {
     // transition T[zc][zp] for fixed (fixZ) and free nodes from g, l, l2 (bpp_c.cpp:573-599)
     const double gr = w.st.gr, lr = w.st.lr, lr2 = w.st.lr2;
     double Tf[3][3] = {{1 - gr, 0, 0}, {gr, 1, 0}, {0, 0, 0}};
@@ -635,8 +712,8 @@ __device__ int update_z(W<Real>& w, uint64_t pos) {
 
 // Flags of proper ancestors (getUpdateNode, bpp_c.cpp:620-642, 836-858).
 // mode 0: of changed nodes; 1: of non-missing Z == 2; 2: of non-missing Z == 1.
-template <typename Real>
-__device__ int ancestors(W<Real>& w, int mode, int8_t* dst) {
+template <typename Real, int C>
+__device__ int ancestors(W<Real, C>& w, int mode, int8_t* dst) {
     for (int i = w.lane; i < w.N; i += 32) dst[i] = 0;
     wsync();
     for (int i = w.lane; i < w.n_nodes; i += 32) {
@@ -662,8 +739,8 @@ __device__ __forceinline__ uint64_t bcast(uint64_t v) {
 // One MH update of the accelerated (neut) or conserved rate (sample_rate,
 // bpp_c.cpp:930-1176; M = 1, adaptive factor 0.5).  Lane 0 draws and decides,
 // the warp evaluates the proposal's likelihood.
-template <typename Real>
-__device__ double mh_rate(W<Real>& w, bool neut, double old_rate, int m) {
+template <typename Real, int C>
+__device__ double mh_rate(W<Real, C>& w, bool neut, double old_rate, int m) {
     const double prior_a = neut ? dM.nprior_a : dM.cprior_a;
     const double prior_b = neut ? dM.nprior_b : dM.cprior_b;
     const int cls = neut ? C_NEUT : C_CONS;
@@ -767,8 +844,8 @@ __device__ double mh_rate(W<Real>& w, bool neut, double old_rate, int m) {
 }
 
 // Prior of a Z configuration (bpp_c2.cpp:131-163).
-template <typename Real>
-__device__ double prior_config(W<Real>& w, const int8_t* z) {
+template <typename Real, int C>
+__device__ double prior_config(W<Real, C>& w, const int8_t* z) {
     double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int k = 0; k + 1 < w.n_nodes; k++) {
         int s = w.nodes[k];
@@ -786,8 +863,8 @@ __device__ double prior_config(W<Real>& w, const int8_t* z) {
 }
 
 // Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353) by one warp.
-template <typename Real>
-__device__ __noinline__ double eval2(W<Real>& w, char* gws, int* n_conf_out) {
+template <typename Real, int C>
+__device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) {
     const int burn = w.burn, mcmc = w.mcmc, T = w.T, N = w.N;
     const int resZ = w.st.resZ;
     // Eval2 runs after the chain, so it reuses the warp scratch from its start
@@ -985,8 +1062,8 @@ __device__ __noinline__ double warp_median(const double* x, int T) {
 }
 
 // initMCMC for model w.st.mi (bpp_c.cpp:131-343) followed by the initial full prune.
-template <typename Real>
-__device__ __noinline__ void init_model(W<Real>& w) {
+template <typename Real, int C>
+__device__ __noinline__ void init_model(W<Real, C>& w) {
     const int resZ = w.st.resZ;
     for (int i = w.lane; i < w.N; i += 32) { w.Z[i] = -1; w.fixZ[i] = -1; }
     wsync();
@@ -1023,23 +1100,23 @@ __device__ __noinline__ void init_model(W<Real>& w) {
     w.st.phase = PH_RUN;
 }
 
-template <typename Real>
-__device__ void write_slot_z(W<Real>& w) {
+template <typename Real, int C>
+__device__ void write_slot_z(W<Real, C>& w) {
     for (int i = w.lane; i < w.N; i += 32) w.sZ[i] = w.Z[i];
 }
 
 // ---------------------------------------------------------------------------
 // kernel
 // ---------------------------------------------------------------------------
-template <typename Real>
+template <typename Real, int C>
 __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int N = dM.N, S = dM.S;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    WarpSmem<Real> L = WarpSmem<Real>::make(N, P.n_int_max, S, P.stack_depth);
+    WarpSmem<Real> L = WarpSmem<Real>::make(N, P.n_int_max, S, P.stack_depth, C);
     TopoLayout TL = TopoLayout::make(N);
     unsigned char* base = smem + (size_t)wid * L.total;
-    W<Real> w;
+    W<Real, C> w;
     w.lane = lane;
     w.S = S;
     w.N = N;
@@ -1073,7 +1150,7 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     const int n_gw = gridDim.x * nw;
     char* gws = P.grp_ws + (size_t)gw * P.grp_ws_stride;
     {
-        GrpLayout GLy = GrpLayout::make(dM.mcmc, P.n_int_max, sizeof(Real));
+        GrpLayout GLy = GrpLayout::make(dM.mcmc, P.n_int_max * C, sizeof(Real));
         w.gpart = (Real*)(gws + GLy.gpart);
     }
     const SlotLayout SL = SlotLayout::make(N, w.T);
@@ -1338,11 +1415,13 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
 // ---------------------------------------------------------------------------
 cudaError_t set_model_batch(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
 
-size_t batch_warp_smem(int N, int NI, int S, int D, int prec) {
-    return prec == 0 ? WarpSmem<double>::make(N, NI, S, D).total : WarpSmem<float>::make(N, NI, S, D).total;
+size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C) {
+    return prec == 0 ? WarpSmem<double>::make(N, NI, S, D, C).total : WarpSmem<float>::make(N, NI, S, D, C).total;
 }
 size_t batch_slot_bytes(int N, int T) { return SlotLayout::make(N, T).total; }
-size_t batch_grp_bytes(int mcmc, int NI, int prec) { return GrpLayout::make(mcmc, NI, prec == 0 ? 8 : 4).total; }
+size_t batch_grp_bytes(int mcmc, int NI, int prec, int C) {
+    return GrpLayout::make(mcmc, NI * C, prec == 0 ? 8 : 4).total;
+}
 size_t batch_state_bytes() { return sizeof(SlotState); }
 
 // Slot states for a fresh batch: slot i runs element elem[i].
@@ -1361,16 +1440,28 @@ cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStrea
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, cudaStream_t st) {
+template <typename Real, int C>
+static cudaError_t launch_batch_t(const BatchParams& p, int grid, int warps, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(batch_kernel<Real, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    batch_kernel<Real, C><<<grid, warps * 32, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+// Column counts per lane that are compiled: FP32 1, 2, 4; FP64 1, 2.
+bool batch_supports(int prec, int C) { return prec == 0 ? (C == 1 || C == 2) : (C == 1 || C == 2 || C == 4); }
+
+cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st) {
     const BatchParams& p = *(const BatchParams*)params;
     if (prec == 0) {
-        cudaFuncSetAttribute(batch_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        batch_kernel<double><<<grid, warps * 32, smem, st>>>(p);
+        if (C == 1) return launch_batch_t<double, 1>(p, grid, warps, smem, st);
+        if (C == 2) return launch_batch_t<double, 2>(p, grid, warps, smem, st);
     } else {
-        cudaFuncSetAttribute(batch_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        batch_kernel<float><<<grid, warps * 32, smem, st>>>(p);
+        if (C == 1) return launch_batch_t<float, 1>(p, grid, warps, smem, st);
+        if (C == 2) return launch_batch_t<float, 2>(p, grid, warps, smem, st);
+        if (C == 4) return launch_batch_t<float, 4>(p, grid, warps, smem, st);
     }
-    return cudaGetLastError();
+    return cudaErrorInvalidValue;
 }
 
 size_t batch_params_bytes() { return sizeof(BatchParams); }

@@ -12,6 +12,7 @@
 #include <atomic>
 #include <chrono>
 #include <deque>
+#include <unordered_map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -38,11 +39,12 @@ cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out,
 cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st);
 cudaError_t set_model_batch(const DevModel& m);
-size_t batch_warp_smem(int N, int NI, int S, int D, int prec);
+size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C);
 size_t batch_slot_bytes(int N, int T);
-size_t batch_grp_bytes(int mcmc, int NI, int prec);
+size_t batch_grp_bytes(int mcmc, int NI, int prec, int C);
+bool batch_supports(int prec, int C);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
-cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, cudaStream_t st);
+cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // model (BPP, bpp.hpp:173-404)
@@ -337,7 +339,7 @@ using namespace pacc;
 // queue as slots free up, advanced by a CUDA-graph-captured sweep step.
 struct Server {
     bool ready = false;
-    int n_slots = 0, warps = 4, grid = 0, prec = 1, D = 1, n_int_max = 1, GG_cap = 0, SP = 16;
+    int n_slots = 0, warps = 4, grid = 0, prec = 1, C = 1, D = 1, n_int_max = 1, GG_cap = 0, SP = 16;
     size_t smem = 0, slot_b = 0, grp_b = 0, blob_b = 0, tb = 0, o_prefix = 0, o_codes = 0;
     char* dev = nullptr;
     ElemHeader* d_hdr = nullptr;
@@ -349,6 +351,9 @@ struct Server {
     int32_t* d_mz = nullptr;
     double* d_pz = nullptr;
     DevCounters* d_cnt = nullptr;
+    double* d_trd = nullptr;
+    int8_t* d_trz = nullptr;
+    int TI = 0;
     int* d_ctr = nullptr;       // [0] n_done, [32] next_slot
     int* d_done = nullptr;
     int* h_done = nullptr;      // pinned: [0] count, [1..] slots
@@ -427,6 +432,24 @@ void pacc_default_opts(pacc_opts* o) {
     o->gapchar = '-'; o->prune_tree = 0; o->trim_gap_percent = 1; o->min_len = 50; o->indel = 0;
     o->precision = PACC_FP64; o->device = 0; o->memory_budget_bytes = 0; o->max_resident = 0;
     o->sweeps_per_launch = 0; o->trace_iters = 0; o->block_threads = 0; o->use_graphs = 1;
+    o->columns_per_lane = 0;
+}
+
+// The device model (eigensystem, priors, options) lives in constant memory,
+// one copy per device.  A context uploads its own before it launches when
+// another context's model is there.  Contexts that share a device are driven
+// from one host thread at a time (every entry point returns with its work done).
+static std::mutex g_model_mu;
+static const pacc_ctx* g_model_owner[64];
+
+static bool ensure_model(pacc_ctx* c) {
+    std::lock_guard<std::mutex> lk(g_model_mu);
+    const int d = c->device;
+    if (d >= 0 && d < 64 && g_model_owner[d] == c) return true;
+    if (!cuda_ok(c, set_model(c->M.dm), "set_model") || !cuda_ok(c, set_model_batch(c->M.dm), "set_model_batch"))
+        return false;
+    if (d >= 0 && d < 64) g_model_owner[d] = c;
+    return true;
 }
 
 pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* status) {
@@ -513,7 +536,7 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     c->gpu_ok = cuda_ok(c, cudaSetDevice(c->device), "cudaSetDevice") &&
                 cuda_ok(c, cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device), "attr") &&
                 cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") &&
-                cuda_ok(c, set_model(dm), "set_model") && cuda_ok(c, set_model_batch(dm), "set_model_batch");
+                ensure_model(c);
     std::memset(&c->counters, 0, sizeof(c->counters));
     if (status) *status = PACC_OK;
     return c;
@@ -523,6 +546,10 @@ const char* pacc_last_error(pacc_ctx* c) { return c ? c->err.c_str() : g_create_
 
 void pacc_destroy(pacc_ctx* c) {
     if (!c) return;
+    {
+        std::lock_guard<std::mutex> lk(g_model_mu);
+        if (c->device >= 0 && c->device < 64 && g_model_owner[c->device] == c) g_model_owner[c->device] = nullptr;
+    }
     cudaSetDevice(c->device);
     if (c->d_ws) cudaFree(c->d_ws);
     if (c->d_blob) cudaFree(c->d_blob);
@@ -544,10 +571,28 @@ static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Columns each lane of the batched kernel carries: the caller's choice, else
+// the tuned value for this precision.
+static int batch_columns(const pacc_ctx* c, int prec) {
+    int C = c->o.columns_per_lane;
+    if (C <= 0) C = 1;
+    while (C > 1 && !batch_supports(prec, C)) C >>= 1;
+    return C;
+}
+
 // Stack depth bound of the unpruned tree: pruning only removes nodes.
 static int tree_stack_depth(const HostModel& M) {
-    std::vector<int> need(M.N, 0);
-    for (int s = M.S; s < M.N; s++) {  // ids are postorder: children before parents
+    std::vector<int> need(M.N, 0), order, todo{M.N - 1};
+    while (!todo.empty()) {  // preorder; reversed below it visits children first
+        int s = todo.back();
+        todo.pop_back();
+        if (s < M.S) continue;
+        order.push_back(s);
+        todo.push_back(M.ch0[s]);
+        todo.push_back(M.ch1[s]);
+    }
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const int s = *it;
         int a = M.ch0[s], b = M.ch1[s];
         int na = a >= M.S ? need[a] : 0, nb = b >= M.S ? need[b] : 0;
         if (a < M.S && b < M.S) need[s] = 1;
@@ -561,16 +606,19 @@ static int tree_stack_depth(const HostModel& M) {
 static int server_setup(pacc_ctx* c, int GG_needed) {
     Server& v = c->srv;
     if (v.ready) return PACC_OK;
+    cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
     const int N = c->M.N, S = c->M.S;
     const int T = c->o.burnin + c->o.mcmc;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     v.prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    v.C = batch_columns(c, v.prec);
     v.D = tree_stack_depth(c->M);
     v.n_int_max = S - 1;
     v.SP = (S + 15) & ~15;
     v.GG_cap = std::max(5120, (GG_needed + 31) & ~31);
     v.warps = 4;
-    size_t wsm = batch_warp_smem(N, v.n_int_max, S, v.D, v.prec);
+    size_t wsm = batch_warp_smem(N, v.n_int_max, S, v.D, v.prec, v.C);
     int max_smem = 0, smem_sm = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
@@ -585,16 +633,19 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.o_codes = al(v.o_prefix + (size_t)(v.GG_cap + 1) * 4);
     v.blob_b = al(v.o_codes + (size_t)v.GG_cap * v.SP);
     v.slot_b = al(batch_slot_bytes(N, T));
-    v.grp_b = al(batch_grp_bytes(c->o.mcmc, v.n_int_max, v.prec));
-    size_t per_slot = v.blob_b + v.slot_b + al(sizeof(ElemHeader)) + al(sizeof(SlotState)) + al(sizeof(DevResult)) +
-                      al(3 * N * 4) + al(3 * N * 4 * 8) + 8;
+    v.grp_b = al(batch_grp_bytes(c->o.mcmc, v.n_int_max, v.prec, v.C));
+    v.TI = std::min(c->o.trace_iters, T);
+    size_t per_slot = v.blob_b + v.slot_b + sizeof(ElemHeader) + sizeof(SlotState) + sizeof(DevResult) +
+                      3 * N * 4 + 3 * N * 4 * 8 + sizeof(double) * 3 * 6 * (size_t)v.TI + (size_t)3 * v.TI * N + 8;
     size_t budget = (size_t)c->o.memory_budget_bytes;
     if (budget == 0) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
         budget = fr / 4;
     }
-    int want = c->o.max_resident > 0 ? c->o.max_resident : 2 * n_warps;
+    // one resident chain per warp: every chain advances in every step, so
+    // latency is the chain's own length; more slots would only queue on warps
+    int want = c->o.max_resident > 0 ? c->o.max_resident : n_warps;
     size_t fixed = (size_t)n_warps * v.grp_b + (1 << 20);
     if (budget <= fixed + per_slot) { c->err = "memory budget too small for one chain slot"; return PACC_OOM; }
     v.n_slots = (int)std::min<size_t>((size_t)want, (budget - fixed) / per_slot);
@@ -608,6 +659,8 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     size_t o_res = o; o = al(o + sizeof(DevResult) * ns);
     size_t o_mz = o; o = al(o + sizeof(int32_t) * 3 * N * (size_t)ns);
     size_t o_pz = o; o = al(o + sizeof(double) * 3 * N * 4 * (size_t)ns);
+    size_t o_trd = o; o = al(o + sizeof(double) * 3 * 6 * (size_t)v.TI * ns);
+    size_t o_trz = o; o = al(o + (size_t)3 * v.TI * N * ns);
     size_t o_cnt = o; o = al(o + sizeof(DevCounters));
     size_t o_ctr = o; o = al(o + 256);
     size_t o_done = o; o = al(o + sizeof(int) * (ns + 1));
@@ -621,6 +674,8 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.d_res = (DevResult*)(v.dev + o_res);
     v.d_mz = (int32_t*)(v.dev + o_mz);
     v.d_pz = (double*)(v.dev + o_pz);
+    v.d_trd = v.TI > 0 ? (double*)(v.dev + o_trd) : nullptr;
+    v.d_trz = v.TI > 0 ? (int8_t*)(v.dev + o_trz) : nullptr;
     v.d_cnt = (DevCounters*)(v.dev + o_cnt);
     v.d_ctr = (int*)(v.dev + o_ctr);
     v.d_done = (int*)(v.dev + o_done);
@@ -648,6 +703,8 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.p.results = v.d_res;
     v.p.max_z = v.d_mz;
     v.p.post_z = v.d_pz;
+    v.p.tr_d = v.d_trd;
+    v.p.tr_z = v.d_trz;
     v.p.counters = v.d_cnt;
     v.p.n_done = v.d_ctr;
     v.p.next_slot = v.d_ctr + 32;
@@ -659,7 +716,7 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     // copy the list of chains that finished back to pinned host memory
     auto record = [&](cudaStream_t s2) -> cudaError_t {
         cudaError_t e = cudaMemsetAsync(v.d_ctr, 0, 256, s2);
-        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, s2);
+        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, v.C, s2);
         if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, s2);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * ns, cudaMemcpyDeviceToHost, s2);
@@ -762,6 +819,8 @@ static int server_admit(pacc_ctx* c) {
 // One sweep step over the resident chains; finished chains become results.
 static int server_step(pacc_ctx* c) {
     Server& v = c->srv;
+    cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
     const int N = c->M.N;
     int st0 = server_admit(c);
     if (st0 != PACC_OK) return st0;
@@ -775,7 +834,7 @@ static int server_step(pacc_ctx* c) {
     if (v.gexec) e = cudaGraphLaunch(v.gexec, st);
     else {
         e = cudaMemsetAsync(v.d_ctr, 0, 256, st);
-        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, st);
+        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, v.C, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * v.n_slots, cudaMemcpyDeviceToHost, st);
     }
@@ -803,6 +862,15 @@ static int server_step(pacc_ctx* c) {
         cudaMemcpyAsync(&pz[(size_t)i * 3 * N * 4], v.d_pz + (size_t)slot * 3 * N * 4, sizeof(double) * 3 * N * 4,
                         cudaMemcpyDeviceToHost, st);
     }
+    const size_t trd_n = (size_t)3 * 6 * v.TI, trz_n = (size_t)3 * v.TI * N;
+    std::vector<double> trd(trd_n * nd);
+    std::vector<int8_t> trz(trz_n * nd);
+    if (v.TI > 0)
+        for (int i = 0; i < nd; i++) {
+            int slot = v.h_done[1 + i];
+            cudaMemcpyAsync(&trd[trd_n * i], v.d_trd + trd_n * slot, sizeof(double) * trd_n, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&trz[trz_n * i], v.d_trz + trz_n * slot, trz_n, cudaMemcpyDeviceToHost, st);
+        }
     if (!cuda_ok(c, cudaStreamSynchronize(st), "D2H results")) return PACC_ECUDA;
     const double t = now_ms();
     for (int i = 0; i < nd; i++) {
@@ -829,6 +897,10 @@ static int server_step(pacc_ctx* c) {
         d.r.latency_ms = t - v.slot_t0[slot];
         d.max_z.assign(mz.begin() + (size_t)i * 3 * N, mz.begin() + (size_t)(i + 1) * 3 * N);
         d.post_z.assign(pz.begin() + (size_t)i * 3 * N * 4, pz.begin() + (size_t)(i + 1) * 3 * N * 4);
+        if (v.TI > 0) {
+            d.tr_d.assign(trd.begin() + trd_n * i, trd.begin() + trd_n * (i + 1));
+            d.tr_z.assign(trz.begin() + trz_n * i, trz.begin() + trz_n * (i + 1));
+        }
         c->done.push_back(std::move(d));
         // the slot's device state is PH_DONE, which the kernel skips until re-admission
         v.free_slots.push_back(slot);
@@ -866,7 +938,7 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
         int gmax = 0;
         for (size_t i = base; i < c->pending.size(); i++) gmax = std::max(gmax, c->pending[i].GG);
         int st = server_setup(c, gmax);
-        if (st != PACC_OK) return st;
+        if (st != PACC_OK) { c->pending.resize(base); return st; }
         const double t = now_ms();
         for (size_t i = base; i < c->pending.size(); i++) {
             HostElem& E = c->pending[i];
@@ -881,7 +953,16 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
                 c->done.push_back(std::move(d));
                 continue;
             }
-            if (E.GG > c->srv.GG_cap) { c->err = "element longer than the serving slot capacity"; return PACC_EINVAL; }
+            if (E.GG > c->srv.GG_cap) {
+                c->pending.resize(base);
+                c->err = "element longer than the serving slot capacity";
+                return PACC_EINVAL;
+            }
+            if (E.stack_depth > c->srv.D || E.n_int > c->srv.n_int_max) {
+                c->pending.resize(base);
+                c->err = "element tree exceeds the serving slot geometry";
+                return PACC_EUNSUPPORTED;
+            }
             c->srv.queue.push_back({std::move(E), t});
         }
         c->pending.resize(base);
@@ -938,6 +1019,7 @@ static int run_pending(pacc_ctx* c) {
     if (c->pending.empty()) return PACC_OK;
     if (!c->gpu_ok) return PACC_ECUDA;
     cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
     const int N = c->M.N, S = c->M.S;
     const int n = (int)c->pending.size();
     const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
@@ -1090,7 +1172,8 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     int D = 1;
     for (int e = 0; e < n; e++) if (!c->pending[e].filtered) D = std::max(D, c->pending[e].stack_depth);
     // geometry: warps per CTA from the shared-memory footprint of one chain
-    size_t wsm = batch_warp_smem(N, n_int_max, S, D, prec);
+    const int C = batch_columns(c, prec);
+    size_t wsm = batch_warp_smem(N, n_int_max, S, D, prec, C);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     int warps = c->o.block_threads > 0 ? std::min(4, std::max(1, c->o.block_threads / 32)) : 4;
@@ -1109,7 +1192,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     int grid = std::max(1, std::min(c->n_sm * per_sm, (n_slots + warps - 1) / warps));
     const int n_warps = grid * warps;
     size_t slot_b = al(batch_slot_bytes(N, T));
-    size_t grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec));
+    size_t grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec, C));
     size_t o_hdr = 0;
     size_t o_res = al(o_hdr + sizeof(ElemHeader) * n);
     size_t o_mz = al(o_res + sizeof(DevResult) * n);
@@ -1162,7 +1245,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     int launches = 0;
     for (;;) {
         if (!cuda_ok(c, cudaMemsetAsync(mb + o_next + 128, 0, 4, st), "memset queue") ||
-            !cuda_ok(c, launch_batch(&p, grid, warps, smem, prec, st), "launch batch"))
+            !cuda_ok(c, launch_batch(&p, grid, warps, smem, prec, C, st), "launch batch"))
             return PACC_ECUDA;
         launches++;
         if (p.sweeps <= 0) break;
@@ -1279,37 +1362,18 @@ int pacc_run(pacc_ctx* c, const pacc_element_batch* b, pacc_result* out) {
     if (st != PACC_OK) return st;
     if (serving(c)) {
         // results arrive in completion order: put them back in batch order
-        std::vector<pacc_result> tmp(b->n_elements);
-        const int N = c->M.N;
-        std::vector<int32_t> mz((size_t)b->n_elements * 3 * N);
-        std::vector<double> pz((size_t)b->n_elements * 3 * N * 4);
-        for (int i = 0; i < b->n_elements; i++) {
-            std::memset(&tmp[i], 0, sizeof(pacc_result));
-            tmp[i].max_z = &mz[(size_t)i * 3 * N];
-            tmp[i].post_z = &pz[(size_t)i * 3 * N * 4];
+        std::unordered_map<int64_t, std::deque<int>> where;
+        for (int i = 0; i < b->n_elements; i++) where[b->element_no ? b->element_no[i] : i].push_back(i);
+        const size_t n0 = c->done_head;
+        if (c->done.size() - n0 != (size_t)b->n_elements) { c->err = "served results lost"; return PACC_ECUDA; }
+        std::vector<pacc_ctx::Done> ord(b->n_elements);
+        for (size_t j = n0; j < c->done.size(); j++) {
+            auto it = where.find(c->done[j].r.element_no);
+            if (it == where.end() || it->second.empty()) { c->err = "served results lost"; return PACC_ECUDA; }
+            ord[it->second.front()] = std::move(c->done[j]);
+            it->second.pop_front();
         }
-        int k = pacc_poll(c, tmp.data(), b->n_elements);
-        if (k != b->n_elements) return PACC_ECUDA;
-        std::vector<int> pos(b->n_elements, -1);
-        for (int i = 0; i < b->n_elements; i++) {
-            int64_t no = b->element_no ? b->element_no[i] : i;
-            for (int j = 0; j < k; j++)
-                if (tmp[j].element_no == no && pos[j] < 0) { pos[j] = i; break; }
-        }
-        for (int j = 0; j < k; j++) {
-            int i = pos[j];
-            if (i < 0) return PACC_ECUDA;
-            int32_t* omz = out[i].max_z;
-            double* opz = out[i].post_z;
-            pacc_trace tr = out[i].trace;
-            out[i] = tmp[j];
-            out[i].max_z = omz;
-            out[i].post_z = opz;
-            out[i].trace = tr;
-            if (omz) std::memcpy(omz, tmp[j].max_z, sizeof(int32_t) * 3 * N);
-            if (opz) std::memcpy(opz, tmp[j].post_z, sizeof(double) * 3 * N * 4);
-        }
-        return PACC_OK;
+        for (int i = 0; i < b->n_elements; i++) c->done[n0 + i] = std::move(ord[i]);
     }
     int k = pacc_poll(c, out, b->n_elements);
     return k == b->n_elements ? PACC_OK : PACC_ECUDA;
@@ -1338,6 +1402,7 @@ int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, dou
     if (!c || n <= 0) return PACC_EINVAL;
     if (!c->gpu_ok) return PACC_ECUDA;
     cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
     double *dd = nullptr, *dr = nullptr, *dout = nullptr;
     if (!cuda_ok(c, cudaMalloc(&dd, n * 8), "malloc") || !cuda_ok(c, cudaMalloc(&dr, n * 8), "malloc") ||
         !cuda_ok(c, cudaMalloc(&dout, (size_t)n * 128), "malloc"))
@@ -1370,6 +1435,7 @@ int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const i
     if (!c) return PACC_EINVAL;
     if (!c->gpu_ok) return PACC_ECUDA;
     cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
     HostElem E;
     if (!preprocess(c->M, c->o, bases, length, E, false)) return PACC_EINVAL;
     if (E.filtered) { *n_cols = 0; return PACC_FILTERED; }

@@ -287,6 +287,7 @@ static Config load_config(const string& path) {
         else if (k == "GPU_PRECISION") o.precision = (v == "fp32" || v == "FP32") ? PACC_FP32 : PACC_FP64;
         else if (k == "GPU_DEVICE") o.device = std::stoi(v);
         else if (k == "GPU_BLOCK_THREADS") o.block_threads = std::stoi(v);
+        else if (k == "GPU_COLUMNS_PER_LANE") o.columns_per_lane = std::stoi(v);
         else if (k == "GPU_MEMORY_BUDGET_GB") o.memory_budget_bytes = (int64_t)(std::stod(v) * 1e9);
         else std::cout << "Unknown parameter: " << k << ", skipping..." << std::endl;
         line_num++;

@@ -136,12 +136,15 @@ def test_cli_drop_in_matches_reference_tables(built, case, tmp_path):
         assert np.allclose(got[:a.shape[0]], a, rtol=2e-7, atol=1e-300), key
 
 
-def test_batched_layout_fp64_matches_oracle(built):
-    """The warp-per-chain layout with FP64 partials reproduces the oracle's chains."""
+@pytest.mark.parametrize("cols", [1, 2])
+def test_batched_layout_fp64_matches_oracle(built, cols):
+    """The warp-per-chain layout with FP64 partials reproduces the oracle's
+    chains, with one or two alignment columns per lane."""
     ds = synth.make_dataset("st12", seed=0).subset([0, 1, 2, 3, 80, 90, 91, 99])
     o = abi.default_opts()
     o.seed, o.burnin, o.mcmc = 0, 100, 300
     o.precision = abi.PACC_FP64_BATCHED
+    o.columns_per_lane = cols
     g, r = _chain_compare(ds, o)
     mg, mr = g.field("loglik"), r.field("loglik")
     fin = np.isfinite(mr)
@@ -160,3 +163,20 @@ def test_batched_layout_fp64_43_taxa_resumable(built):
     g2 = pg.Context(ds, o).run()
     assert (g2.tr_z == g1.tr_z).all()
     assert np.array_equal(g2.field("loglik"), g1.field("loglik"))
+
+
+def test_contexts_with_different_models_interleave(built):
+    """Each context launches with its own tree and rate matrix, whatever
+    context ran last on the device."""
+    a = synth.make_dataset("st12", seed=0).subset([0, 1, 2])
+    b = synth.make_dataset("st43", n_elements=3, seed=1)
+    o = abi.default_opts()
+    o.seed, o.burnin, o.mcmc = 1, 20, 40
+    ca, cb = pg.Context(a, o), pg.Context(b, o)
+    r1 = ca.run()
+    cb.run()
+    r2 = ca.run()
+    assert np.array_equal(r1.field("loglik"), r2.field("loglik"))
+    assert np.array_equal(r1.post_z, r2.post_z)
+    assert np.allclose(ca.pmatrix(a.tree.distances[:4], np.ones(4)), po.pmatrix(a, o, a.tree.distances[:4], np.ones(4)),
+                       rtol=0, atol=1e-14)
