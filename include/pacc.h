@@ -216,6 +216,28 @@ int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);
  * d[i] and rates r[i], FP64 on the device.  out: [n][16] row-major (child, parent). */
 int pacc_debug_pmatrix(pacc_ctx* ctx, int n, const double* d, const double* r, double* out);
 
+/* The same P^T matrices as pacc_debug_pmatrix, computed without allocating.
+ * This entry point has no counterpart in the reference (PhyloAcc-ST builds
+ * its matrices on the host with Armadillo); it exists for callers that must
+ * not allocate device memory at that moment: a process whose device memory
+ * is fully committed (a serving context holding its whole budget in chain
+ * slots), or one that cannot afford the device-wide synchronisation that
+ * cudaFree implies while other streams are busy.
+ * Working memory is a fixed file-scope device array of PACC_NOALLOC_MAX_PAIRS
+ * (distance, rate) pairs and their matrices (about 590 KB per device); larger
+ * requests return PACC_EINVAL.  Nothing in the scratch has to start at zero:
+ * the kernel writes every matrix that is copied back.
+ * Set-up: the first call on a device looks the scratch up with
+ * cudaGetSymbolAddress (which loads the module on that device); later calls
+ * reuse the address.  Make the first call from ordinary code, before any
+ * stream capture.
+ * The scratch is shared by every context on a device: calls that overlap on
+ * one device (two threads, or two contexts' streams) race on it.
+ * n: 1..PACC_NOALLOC_MAX_PAIRS; d, r, out: host arrays as for pacc_debug_pmatrix.
+ * Returns when out is written. */
+#define PACC_NOALLOC_MAX_PAIRS 4096
+int pacc_pmatrix_noalloc(pacc_ctx* ctx, int n, const double* d, const double* r, double* out);
+
 /* (b) Per-column log-likelihood of one element for a given Z (int32 [N]) and
  * conserved/accelerated rates, using the chosen precision's pruning kernel.
  * out: [columns after trimming]; returns the column count via *n_cols. */

@@ -46,6 +46,8 @@ def lib():
         L.pacc_get_counters.argtypes = [C.c_void_p, C.POINTER(abi.PaccCounters)]
         L.pacc_debug_pmatrix.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]
+        L.pacc_pmatrix_noalloc.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double)]
         L.pacc_debug_loglik.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int32),
                                         C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
         L.pacc_debug_encode.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int8),
@@ -134,6 +136,18 @@ class Context:
                                       abi.ptr(out, C.c_double))
         if st != 0:
             self._err("pacc_debug_pmatrix", st)
+        return out.reshape(-1, 4, 4)
+
+    def pmatrix_noalloc(self, d, r) -> np.ndarray:
+        """pmatrix() through the allocation-free entry point (at most
+        PACC_NOALLOC_MAX_PAIRS pairs per call)."""
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        out = np.zeros((len(d), 16))
+        st = lib().pacc_pmatrix_noalloc(self.h, len(d), abi.ptr(d, C.c_double), abi.ptr(r, C.c_double),
+                                        abi.ptr(out, C.c_double))
+        if st != 0:
+            self._err("pacc_pmatrix_noalloc", st)
         return out.reshape(-1, 4, 4)
 
     def loglik(self, e: int, z, c_rate: float, n_rate: float) -> np.ndarray:

@@ -45,6 +45,7 @@ def build(force=False, verbose=False):
         "pacc_chain.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_chain.cu")],
         "pacc_batch.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_batch.cu")],
         "pacc_host.o": [NVCC] + ARCH + COMMON + ["-x", "cu", "-c", os.path.join(CSRC, "pacc_host.cpp")],
+        "pacc_noalloc.o": [NVCC] + ARCH + COMMON + ["-c", os.path.join(CSRC, "pacc_noalloc.cu")],
     }
     cmds = []
     for name, cmd in objs.items():

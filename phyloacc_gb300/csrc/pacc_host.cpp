@@ -42,6 +42,7 @@ cudaError_t set_model_batch(const DevModel& m);
 size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C);
 size_t batch_slot_bytes(int N, int T);
 size_t batch_grp_bytes(int mcmc, int NI, int prec, int C);
+cudaError_t noalloc_scratch_address(double** p);
 bool batch_supports(int prec, int C);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
 cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st);
@@ -1414,6 +1415,38 @@ int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, dou
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 128, cudaMemcpyDeviceToHost);
     cudaFree(dd); cudaFree(dr); cudaFree(dout);
     return cuda_ok(c, e, "pmatrix") ? PACC_OK : PACC_ECUDA;
+}
+
+// Scratch address per device, looked up once (pacc_noalloc.cu).
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_base[64];
+
+int pacc_pmatrix_noalloc(pacc_ctx* c, int n, const double* d, const double* r, double* out) {
+    if (!c || n <= 0 || n > PACC_NOALLOC_MAX_PAIRS || !d || !r || !out) return PACC_EINVAL;
+    if (!c->gpu_ok || c->device < 0 || c->device >= 64) return PACC_ECUDA;
+    if (cudaSetDevice(c->device) != cudaSuccess) return PACC_ECUDA;
+    if (!ensure_model(c)) return PACC_ECUDA;
+    double* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_base[c->device]) {
+            double* p = nullptr;
+            if (noalloc_scratch_address(&p) != cudaSuccess || !p) return PACC_ECUDA;
+            g_noalloc_base[c->device] = p;
+        }
+        base = g_noalloc_base[c->device];
+    }
+    const size_t M = PACC_NOALLOC_MAX_PAIRS;
+    double* sd = base;
+    double* sr = base + M;
+    double* so = base + 2 * M;
+    cudaStream_t st = c->stream;
+    cudaError_t e = cudaMemcpyAsync(sd, d, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sr, r, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_pmatrix(n, sd, sr, so, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, so, sizeof(double) * 16 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? PACC_OK : PACC_ECUDA;
 }
 
 int pacc_debug_encode(pacc_ctx* c, const uint8_t* bases, int32_t length, int8_t* tg_out, int32_t* n_cols,
