@@ -264,7 +264,8 @@ def run_gpu(args, ws, rank, local):
     else:
         ds64 = ds.subset(list(range(E64)))
         ctx64 = pg.Context(ds64, opts_for(abi.PACC_FP64))
-        k64, w64, c64, _ = time_gpu(ctx64, ds64, max(1, args.steps // 2), 1, ws)
+        ctx64.run(ds.subset(list(range(E64, E64 + 152))))    # warm-up on one element per SM
+        k64, w64, c64, _ = time_gpu(ctx64, ds64, 1, 0, ws)
         v64 = ws * E64 / float(np.mean(k64))
     fp64_peak, fp32_peak = pg.measure_fma_peak(0)
     achieved = cnt["flop"] / float(np.mean(kern)) / ws * ws
@@ -308,7 +309,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--elements", type=int, default=5000)
+    ap.add_argument("--elements", type=int, default=2432,
+                    help="elements per step (default: two per resident chain warp)")
     ap.add_argument("--fp64-elements", type=int, default=608)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

@@ -73,7 +73,7 @@ struct GrpLayout {
 // Shared memory of one warp-chain; every lane carries C columns.
 template <typename Real>
 struct WarpSmem {
-    size_t ptc, part, tgv, hdf, rec, srec, emr, stage, cnt, topo, i8, dbl, total;
+    size_t ptc, part, tgv, hdf, rec, srec, stage, cnt, topo, i8, dbl, total;
     __host__ __device__ static WarpSmem make(int N, int NI, int S, int D, int C) {
         WarpSmem w;
         size_t o = 0;
@@ -86,7 +86,6 @@ struct WarpSmem {
         w.hdf = o; o = al(o + 16);
         w.rec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
         w.srec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
-        w.emr = o; o = al(o + (size_t)N * sizeof(EmRec));
         w.stage = o; o = al(o + (size_t)C * ((S + 15) & ~15) * 32);
         w.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 2);               // uint16 bins
         w.topo = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
@@ -114,7 +113,6 @@ struct W {
     const NodeRec* rec; // [NI] internal nodes in postorder (internal_nodes)
     const NodeRec* srec;// [NI] internal nodes in stack order
     Real* gpart;        // [NI][C][4][32] per-warp device scratch: partials of the sampling pass
-    const EmRec* emr;   // [n_nodes - 1]
     uint32_t* stage;    // [C][SP/4][32] words of per-lane column codes
     const uint8_t* codes_t;  // [GGp][SP]
     int SP;
@@ -136,10 +134,38 @@ struct W {
     long long t0;
 
     __device__ __forceinline__ Real& P(int s, int i, int j) { return ptc[s * 16 + i * 4 + j]; }
-    __device__ __forceinline__ Real& PART(int k, int j) { return part[(k * 4 + j) * 32 + lane]; }
 };
 
 __device__ __forceinline__ void wsync() { __syncwarp(); }
+
+// 4-state vectors and 4x4 matrices move as 16-byte accesses: a partial of
+// lane l lives at [.. * 32 + l][4], a matrix row-major in 16 contiguous words.
+__device__ __forceinline__ void ld4(const float* __restrict__ p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* __restrict__ p, double (&x)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, const float (&x)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void st4(double* __restrict__ p, const double (&x)[4]) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(x[0], x[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(x[2], x[3]);
+}
+template <typename Real>
+__device__ __forceinline__ void ld16(const Real* __restrict__ p, Real (&m)[16]) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        Real t[4];
+        ld4(p + 4 * r, t);
+#pragma unroll
+        for (int i = 0; i < 4; i++) m[4 * r + i] = t[i];
+    }
+}
+
 
 // Phase timer of a warp (lane 0): cycles since the previous mark go to phase i.
 #define PHASE(i)                               \
@@ -164,18 +190,29 @@ enum { C_NULL = 0, C_CONS = 1, C_NEUT = 2 };
 // bpp_c.cpp:661-663); with prop_class >= 0 the branches of that class get the
 // proposal matrices P(d * r_prop) (log_f_Xz, bpp_c.cpp:885-906).
 template <typename Real, int C>
-__device__ void fill_ptc(W<Real, C>& w, int prop_class, double r_prop) {
-    for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
-        int s = w.nodes[i];
-        int z = w.Z[s];
-        int k = (z == 2) ? C_NEUT : (z == 0 ? C_NULL : C_CONS);
-        if (prop_class >= 0 && k == prop_class) {
+__device__ __noinline__ void fill_ptc(W<Real, C>& w, int prop_class, double r_prop) {
+    // branches that take a class table: one matrix row (4 words) per lane and
+    // step, so that consecutive lanes write consecutive 16-byte chunks
+    const int nb = w.n_nodes - 1;
+    for (int idx = w.lane; idx < nb * 4; idx += 32) {
+        const int s = w.nodes[idx >> 2], row = idx & 3;
+        const int z = w.Z[s];
+        const int k = (z == 2) ? C_NEUT : (z == 0 ? C_NULL : C_CONS);
+        if (prop_class >= 0 && k == prop_class) continue;
+        const double* src = w.tbl + ((size_t)k * w.N + s) * 16 + row * 4;
+        const Real v[4] = {(Real)src[0], (Real)src[1], (Real)src[2], (Real)src[3]};
+        st4(w.ptc + s * 16 + row * 4, v);
+    }
+    // branches of the proposal class: P(d * r_prop) built per lane
+    if (prop_class >= 0) {
+        for (int i = w.lane; i < nb; i += 32) {
+            const int s = w.nodes[i];
+            const int z = w.Z[s];
+            const int k = (z == 2) ? C_NEUT : (z == 0 ? C_NULL : C_CONS);
+            if (k != prop_class) continue;
             double pt[16];
             build_pt(w.dist2[s], r_prop, true, pt);
             for (int q = 0; q < 16; q++) w.ptc[s * 16 + q] = (Real)pt[q];
-        } else {
-            const double* src = w.tbl + ((size_t)k * w.N + s) * 16;
-            for (int q = 0; q < 16; q++) w.ptc[s * 16 + q] = (Real)src[q];
         }
     }
     wsync();
@@ -184,7 +221,7 @@ __device__ void fill_ptc(W<Real, C>& w, int prop_class, double r_prop) {
 // Class table k at rate r for all branches of the pruned tree; branches not
 // longer than 1e-10 keep the identity (bpp_c.cpp:191-226) unless force.
 template <typename Real, int C>
-__device__ void build_table(W<Real, C>& w, int k, double r, bool scaled, bool force, bool skip_short) {
+__device__ __noinline__ void build_table(W<Real, C>& w, int k, double r, bool scaled, bool force, bool skip_short) {
     for (int i = w.lane; i < w.n_nodes - 1; i += 32) {
         int s = w.nodes[i];
         double* out = w.tbl + ((size_t)k * w.N + s) * 16;
@@ -288,34 +325,31 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
         // pop internal children (the child computed last is on top)
         if (i0 && i1) {
             const bool c0_top = R.prank & 1;   // flags, see NodeRec
-            const Real* t = stk + (sp - 1) * (C * 128) + lane;
-            const Real* u = stk + (sp - 2) * (C * 128) + lane;
+            const Real* t = stk + (sp - 1) * (C * 128) + lane * 4;
+            const Real* u = stk + (sp - 2) * (C * 128) + lane * 4;
             sp -= 2;
 #pragma unroll
             for (int j = 0; j < C; j++) {
                 const bool ht = hbits[j] & 1, hu = (hbits[j] >> 1) & 1;
                 hbits[j] >>= 2;
                 Real tt[4], uu[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) { tt[i] = t[j * 128 + i * 32]; uu[i] = u[j * 128 + i * 32]; }
+                ld4(t + j * 128, tt);
+                ld4(u + j * 128, uu);
 #pragma unroll
                 for (int i = 0; i < 4; i++) { x0[j][i] = c0_top ? tt[i] : uu[i]; x1[j][i] = c0_top ? uu[i] : tt[i]; }
                 h0[j] = c0_top ? ht : hu;
                 h1[j] = c0_top ? hu : ht;
             }
         } else if (i0 || i1) {
-            const Real* t = stk + (sp - 1) * (C * 128) + lane;
+            const Real* t = stk + (sp - 1) * (C * 128) + lane * 4;
             sp -= 1;
 #pragma unroll
             for (int j = 0; j < C; j++) {
                 const bool ht = hbits[j] & 1;
                 hbits[j] >>= 1;
+                ld4(t + j * 128, x0[j]);
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const Real v = t[j * 128 + i * 32];
-                    x0[j][i] = v;
-                    x1[j][i] = v;
-                }
+                for (int i = 0; i < 4; i++) x1[j][i] = x0[j][i];
                 h0[j] = ht;
                 h1[j] = ht;
             }
@@ -344,8 +378,7 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
                 if (q ? i1 : i0) {
                     // internal child: one matrix load serves all C columns
                     Real p[16];
-#pragma unroll
-                    for (int i = 0; i < 16; i++) p[i] = Pc[i];
+                    ld16(Pc, p);
 #pragma unroll
                     for (int j = 0; j < C; j++) {
                         const Real* x = q ? x1[j] : x0[j];
@@ -365,8 +398,9 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
                         const int code = q ? code1[j] : code0[j];
                         if (!(act[j] && hs[j] && (q ? h1[j] : h0[j]))) continue;
                         if (code < 4) {
-                            const Real* Pr = Pc + code * 4;
-                            a[j][0] *= Pr[0]; a[j][1] *= Pr[1]; a[j][2] *= Pr[2]; a[j][3] *= Pr[3];
+                            Real pr[4];
+                            ld4(Pc + code * 4, pr);
+                            a[j][0] *= pr[0]; a[j][1] *= pr[1]; a[j][2] *= pr[2]; a[j][3] *= pr[3];
                         } else {
                             int msk = ambig_mask(code - CODE_R);
                             Real v0 = 0, v1 = 0, v2 = 0, v3 = 0;
@@ -383,7 +417,7 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
             for (int j = 0; j < C; j++)
                 if (act[j] && hs[j]) Resc<Real>::apply(a[j], sc[j]);
         }
-        Real* __restrict__ o = stk + sp * (C * 128) + lane;
+        Real* __restrict__ o = stk + sp * (C * 128) + lane * 4;
         sp++;
 #pragma unroll
         for (int j = 0; j < C; j++) {
@@ -391,13 +425,10 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
 #pragma unroll
                 for (int i = 0; i < 4; i++) { a[j][i] *= pi[i]; root[j][i] = a[j][i]; }
             }
-#pragma unroll
-            for (int i = 0; i < 4; i++) o[j * 128 + i * 32] = a[j][i];
+            st4(o + j * 128, a[j]);
             hbits[j] = (hbits[j] << 1) | (hs[j] ? 1u : 0u);
             if (STORE) {
-                Real* __restrict__ gp = gpart + (R.self * C + j) * 128 + lane;
-#pragma unroll
-                for (int i = 0; i < 4; i++) gp[i * 32] = a[j][i];
+                st4(gpart + (R.self * C + j) * 128 + lane * 4, a[j]);
                 tgv[(R.self * C + j) * 32 + lane] = hs[j] ? (int8_t)-1 : (int8_t)4;
             }
         }
@@ -425,7 +456,7 @@ struct LLAcc {
 // per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).  A pass
 // covers 32 x C columns: lane l takes columns g0 + 32 j + l.
 template <typename Real, int C>
-__device__ __forceinline__ double likelihood_pass(W<Real, C>& w) {
+__device__ __noinline__ double likelihood_pass(W<Real, C>& w) {
     const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP;
     const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ srec = w.srec;
@@ -494,9 +525,9 @@ __device__ __forceinline__ double u_of<float>(uint32_t w) {
 // draws from its own words of the stream (prefix[g] words before it), so the
 // draws do not depend on how columns are spread over lanes.
 template <typename Real, int C>
-__device__ __forceinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
+__device__ __noinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
     const int NB = NSYM * 4;
-    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, N = w.N, n_nodes = w.n_nodes;
+    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, N = w.N;
     const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ rec = w.rec;
     const NodeRec* __restrict__ srec = w.srec;
@@ -528,74 +559,95 @@ __device__ __forceinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
         int sc[C];
         column_up<Real, C, true>(srec, n_int, stage, sstride, stk, part, tgv, ptc, lane, act, e_int, e_leaf, pi,
                                  rootp, sc);
-        // top-down draws, the C columns interleaved
+        // Top-down draws, the C columns interleaved, fused with the emission
+        // histogram: once a node's base is drawn, the (base, parent base) pair
+        // of its own branch and the (code, base) pairs of its leaf children are
+        // counted (warp-aggregated with match-any; every non-root node of the
+        // pruned tree is the child of exactly one internal node).
+        auto hist = [&](int node, int key) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (key >= 0 && lane == __ffs(peers) - 1) {
+                const int bin = node * NB + key;
+                atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
+            }
+        };
+        auto leaf_pairs = [&](const NodeRec& R, int j, int base) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int c = q ? R.c1 : R.c0;
+                if ((q ? R.r1 : R.r0) >= 0 || (q ? R.m1 : R.m0)) continue;
+                int key = -1;
+                if (act[j] && base < 4) {
+                    const int code = stage_code(stage + j * sstride, c, lane);
+                    const int sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
+                    if (sym >= 0) key = sym * 4 + base;
+                }
+                hist(c, key);
+            }
+        };
         uint64_t wp[C], blk[C];
         uint32_t words[C][4];
+        {
+            const NodeRec RR = rec[rk];
 #pragma unroll
-        for (int j = 0; j < C; j++) {
-            if (!act[j]) continue;
-            wp[j] = pos + (uint64_t)prefix[g0 + 32 * j + lane];
-            blk[j] = wp[j] >> 2;
-            philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
-            int nn = cat4(rootp[j], u_of<Real>(words[j][wp[j] & 3]));
-            wp[j]++;
-            if (nn > 3) { err = 1; nn = 0; }
-            tgv[(rk * C + j) * 32 + lane] = (int8_t)nn;
-            n_tg++;
+            for (int j = 0; j < C; j++) {
+                int nn = 4;
+                if (act[j]) {
+                    wp[j] = pos + (uint64_t)prefix[g0 + 32 * j + lane];
+                    blk[j] = wp[j] >> 2;
+                    philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
+                    nn = cat4(rootp[j], u_of<Real>(words[j][wp[j] & 3]));
+                    wp[j]++;
+                    if (nn > 3) { err = 1; nn = 0; }
+                    tgv[(rk * C + j) * 32 + lane] = (int8_t)nn;
+                    n_tg++;
+                }
+                leaf_pairs(RR, j, nn);
+            }
         }
+        // the partials of a node are read two nodes ahead: the loads come from
+        // L2 and their latency overlaps the draws of the nodes in between
+        Real cur[C][4], nx1[C][4], nx2[C][4];
+        auto load_part = [&](Real (&dst)[C][4], int k) {
+#pragma unroll
+            for (int j = 0; j < C; j++) ld4(part + (k * C + j) * 128 + lane * 4, dst[j]);
+        };
+        if (n_int >= 2) load_part(cur, n_int - 2);
+        if (n_int >= 3) load_part(nx1, n_int - 3);
         for (int k = n_int - 2; k >= 0; k--) {
+            if (k >= 2) load_part(nx2, k - 2);
             const NodeRec R = rec[k];
 #pragma unroll
             for (int j = 0; j < C; j++) {
-                if (!act[j]) continue;
-                int8_t* tk = tgv + (k * C + j) * 32 + lane;
-                if (R.missing || *tk == 4) { *tk = 4; continue; }
-                const int tp = tgv[(R.prank * C + j) * 32 + lane];
-                const Real* __restrict__ Ps = ptc + R.self * 16 + tp;
-                const Real* __restrict__ pk = part + (k * C + j) * 128 + lane;
-                Real q[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) q[i] = Ps[i * 4] * pk[i * 32];
-                if ((wp[j] >> 2) != blk[j]) {
-                    blk[j] = wp[j] >> 2;
-                    philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
-                }
-                int n2 = cat4(q, u_of<Real>(words[j][wp[j] & 3]));
-                wp[j]++;
-                if (n2 > 3) { err = 1; n2 = 0; }
-                *tk = (int8_t)n2;
-                n_tg++;
-            }
-        }
-        // emission histogram, warp-aggregated
-        const EmRec* __restrict__ emr = w.emr;
-        for (int i = 0; i < n_nodes - 1; i++) {
-            const EmRec E = emr[i];
-            if (E.missing) continue;
-            const int s = E.node;
-#pragma unroll
-            for (int j = 0; j < C; j++) {
-                int key = -1;
+                int n2 = 4, tp = 4;
                 if (act[j]) {
-                    int sym;
-                    if (E.rank < 0) {
-                        int code = stage_code(stage + j * sstride, s, lane);
-                        sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
+                    int8_t* tk = tgv + (k * C + j) * 32 + lane;
+                    if (R.missing || *tk == 4) {
+                        *tk = 4;
                     } else {
-                        int t = tgv[(E.rank * C + j) * 32 + lane];
-                        sym = t < 4 ? t : -1;
-                    }
-                    if (sym >= 0) {
-                        int tp = tgv[(E.prank * C + j) * 32 + lane];
-                        if (tp >= 0 && tp < 4) key = sym * 4 + tp;
+                        tp = tgv[(R.prank * C + j) * 32 + lane];
+                        const Real* __restrict__ Ps = ptc + R.self * 16 + tp;
+                        Real q[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) q[i] = Ps[i * 4] * cur[j][i];
+                        if ((wp[j] >> 2) != blk[j]) {
+                            blk[j] = wp[j] >> 2;
+                            philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
+                        }
+                        n2 = cat4(q, u_of<Real>(words[j][wp[j] & 3]));
+                        wp[j]++;
+                        if (n2 > 3) { err = 1; n2 = 0; }
+                        *tk = (int8_t)n2;
+                        n_tg++;
                     }
                 }
-                unsigned peers = __match_any_sync(0xffffffffu, key);
-                if (key >= 0 && lane == __ffs(peers) - 1) {
-                    int bin = s * NB + key;
-                    atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
-                }
+                hist(R.self, (n2 < 4 && tp < 4) ? n2 * 4 + tp : -1);
+                leaf_pairs(R, j, n2);
             }
+#pragma unroll
+            for (int j = 0; j < C; j++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) { cur[j][i] = nx1[j][i]; nx1[j][i] = nx2[j][i]; }
         }
     }
     w.e_int += e_int;
@@ -607,7 +659,7 @@ __device__ __forceinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
 
 // Emission sums from the histogram (getEmission, bpp_c2.cpp:355-390).
 template <typename Real, int C>
-__device__ void emission_sums(W<Real, C>& w) {
+__device__ __noinline__ void emission_sums(W<Real, C>& w) {
     const int NB = NSYM * 4;
     for (int t = w.lane; t < (w.n_nodes - 1) * 3; t += 32) {
         int s = w.nodes[t / 3];
@@ -640,7 +692,7 @@ __device__ void emission_sums(W<Real, C>& w) {
 // Latent-state forward filter (linear FP64, normalised per node) and
 // backward sampling (Update_Z_subtree, bpp_c.cpp:1182-1293).
 template <typename Real, int C>
-__device__ int update_z(W<Real, C>& w, uint64_t pos) {
+__device__ __noinline__ int update_z(W<Real, C>& w, uint64_t pos) {
     // transition T[zc][zp] for fixed (fixZ) and free nodes from g, l, l2 (bpp_c.cpp:573-599)
     const double gr = w.st.gr, lr = w.st.lr, lr2 = w.st.lr2;
     double Tf[3][3] = {{1 - gr, 0, 0}, {gr, 1, 0}, {0, 0, 0}};
@@ -713,7 +765,7 @@ __device__ int update_z(W<Real, C>& w, uint64_t pos) {
 // Flags of proper ancestors (getUpdateNode, bpp_c.cpp:620-642, 836-858).
 // mode 0: of changed nodes; 1: of non-missing Z == 2; 2: of non-missing Z == 1.
 template <typename Real, int C>
-__device__ int ancestors(W<Real, C>& w, int mode, int8_t* dst) {
+__device__ __noinline__ int ancestors(W<Real, C>& w, int mode, int8_t* dst) {
     for (int i = w.lane; i < w.N; i += 32) dst[i] = 0;
     wsync();
     for (int i = w.lane; i < w.n_nodes; i += 32) {
@@ -740,7 +792,7 @@ __device__ __forceinline__ uint64_t bcast(uint64_t v) {
 // bpp_c.cpp:930-1176; M = 1, adaptive factor 0.5).  Lane 0 draws and decides,
 // the warp evaluates the proposal's likelihood.
 template <typename Real, int C>
-__device__ double mh_rate(W<Real, C>& w, bool neut, double old_rate, int m) {
+__device__ __noinline__ double mh_rate(W<Real, C>& w, bool neut, double old_rate, int m) {
     const double prior_a = neut ? dM.nprior_a : dM.cprior_a;
     const double prior_b = neut ? dM.nprior_b : dM.cprior_b;
     const int cls = neut ? C_NEUT : C_CONS;
@@ -845,7 +897,7 @@ __device__ double mh_rate(W<Real, C>& w, bool neut, double old_rate, int m) {
 
 // Prior of a Z configuration (bpp_c2.cpp:131-163).
 template <typename Real, int C>
-__device__ double prior_config(W<Real, C>& w, const int8_t* z) {
+__device__ __noinline__ double prior_config(W<Real, C>& w, const int8_t* z) {
     double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int k = 0; k + 1 < w.n_nodes; k++) {
         int s = w.nodes[k];
@@ -1101,7 +1153,7 @@ __device__ __noinline__ void init_model(W<Real, C>& w) {
 }
 
 template <typename Real, int C>
-__device__ void write_slot_z(W<Real, C>& w) {
+__device__ __noinline__ void write_slot_z(W<Real, C>& w) {
     for (int i = w.lane; i < w.N; i += 32) w.sZ[i] = w.Z[i];
 }
 
@@ -1133,8 +1185,6 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     w.rec = recw;
     NodeRec* srecw = (NodeRec*)(base + L.srec);
     w.srec = srecw;
-    EmRec* emrw = (EmRec*)(base + L.emr);
-    w.emr = emrw;
     w.stage = (uint32_t*)(base + L.stage);
     w.cnt = (unsigned*)(base + L.cnt);
     int16_t* t16 = (int16_t*)(base + L.topo);
@@ -1213,16 +1263,6 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
                 R.prank = sflag[s];       // stack order: bit 0 = first child's partial on top
                 srecw[k] = R;
             }
-        }
-        for (int i = lane; i < w.n_nodes - 1; i += 32) {
-            int s = w.nodes[i];
-            EmRec E;
-            E.node = (int16_t)s;
-            E.rank = s >= S ? w.irank[s] : (int16_t)-1;
-            E.prank = w.irank[w.par[s]];
-            E.missing = (int8_t)w.missing[s];
-            E.pad = 0;
-            emrw[i] = E;
         }
         char* sw = P.slot_ws + (size_t)slot * P.slot_ws_stride;
         w.sZ = (int8_t*)(sw + SL.Z);
@@ -1413,7 +1453,11 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
 // ---------------------------------------------------------------------------
 // host-callable pieces
 // ---------------------------------------------------------------------------
-cudaError_t set_model_batch(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
+// The model is copied on the stream the kernels run on, so that a launch
+// that follows on that stream sees it.
+cudaError_t set_model_batch(const DevModel& m, cudaStream_t st) {
+    return cudaMemcpyToSymbolAsync(dM, &m, sizeof(DevModel), 0, cudaMemcpyHostToDevice, st);
+}
 
 size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C) {
     return prec == 0 ? WarpSmem<double>::make(N, NI, S, D, C).total : WarpSmem<float>::make(N, NI, S, D, C).total;
@@ -1446,6 +1490,30 @@ static cudaError_t launch_batch_t(const BatchParams& p, int grid, int warps, siz
     if (e != cudaSuccess) return e;
     batch_kernel<Real, C><<<grid, warps * 32, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+template <typename Real, int C>
+static int occupancy_t(int warps, size_t smem) {
+    if (cudaFuncSetAttribute(batch_kernel<Real, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_kernel<Real, C>, warps * 32, smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+// Resident CTAs per SM of the batched kernel for this shape (0 if it cannot run).
+int batch_occupancy(int prec, int C, int warps, size_t smem) {
+    if (prec == 0) {
+        if (C == 1) return occupancy_t<double, 1>(warps, smem);
+        if (C == 2) return occupancy_t<double, 2>(warps, smem);
+    } else {
+        if (C == 1) return occupancy_t<float, 1>(warps, smem);
+        if (C == 2) return occupancy_t<float, 2>(warps, smem);
+        if (C == 4) return occupancy_t<float, 4>(warps, smem);
+    }
+    return 0;
 }
 
 // Column counts per lane that are compiled: FP32 1, 2, 4; FP64 1, 2.

@@ -1329,7 +1329,11 @@ __global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
 // ---------------------------------------------------------------------------
 // Host-callable launchers (C++ linkage, used by pacc_host.cpp)
 // ---------------------------------------------------------------------------
-cudaError_t set_model(const DevModel& m) { return cudaMemcpyToSymbol(dM, &m, sizeof(DevModel)); }
+// The model is copied on the stream the kernels run on, so that a launch
+// that follows on that stream sees it.
+cudaError_t set_model(const DevModel& m, cudaStream_t st) {
+    return cudaMemcpyToSymbolAsync(dM, &m, sizeof(DevModel), 0, cudaMemcpyHostToDevice, st);
+}
 
 size_t smem_bytes(int N, int BT, int prec) {
     return prec == 0 ? SmemLayout<double>::make(N, BT).total : SmemLayout<float>::make(N, BT).total;

@@ -14,7 +14,7 @@ namespace pacc {
 static __constant__ DevModel dM;
 
 // Gamma(shape a, scale b) density and its log as the reference takes it (bpp_c.cpp:784,1046).
-static __device__ double gamma_pdf(double x, double a, double b) {
+static __device__ __noinline__ double gamma_pdf(double x, double a, double b) {
     if (x < 0) return 0.0;
     if (x == 0) return (a == 1) ? 1.0 / b : 0.0;
     double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, log(x)), __ddiv_rn(x, b)), lgamma(a)),

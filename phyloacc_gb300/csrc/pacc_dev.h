@@ -126,15 +126,6 @@ struct NodeRec {
     int16_t prank;       // internal rank of the parent (-1 for the root)
 };
 
-// One non-root node of the pruned tree for the emission histogram.
-struct EmRec {
-    int16_t node;        // node id
-    int16_t rank;        // internal rank, -1 for a leaf
-    int16_t prank;       // internal rank of the parent
-    int8_t missing;
-    int8_t pad;
-};
-
 // Parameters of one chain-kernel launch.
 struct ChainParams {
     const ElemHeader* hdr;     // [n_elem]

@@ -11,7 +11,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <array>
 #include <deque>
+#include <map>
 #include <unordered_map>
 #include <cmath>
 #include <cstdio>
@@ -28,7 +30,7 @@
 
 namespace pacc {
 
-cudaError_t set_model(const DevModel& m);
+cudaError_t set_model(const DevModel& m, cudaStream_t st);
 size_t smem_bytes(int N, int BT, int prec);
 size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec);
 size_t topo_bytes(int N);
@@ -38,12 +40,13 @@ cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate,
 cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out, cudaStream_t st);
 cudaError_t launch_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, cudaStream_t st);
-cudaError_t set_model_batch(const DevModel& m);
+cudaError_t set_model_batch(const DevModel& m, cudaStream_t st);
 size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C);
 size_t batch_slot_bytes(int N, int T);
 size_t batch_grp_bytes(int mcmc, int NI, int prec, int C);
 cudaError_t noalloc_scratch_address(double** p);
 bool batch_supports(int prec, int C);
+int batch_occupancy(int prec, int C, int warps, size_t smem);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
 cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st);
 
@@ -380,6 +383,8 @@ struct pacc_ctx {
     cudaStream_t stream = nullptr;
     // pending and finished work
     std::vector<HostElem> pending;
+    size_t tune_grp_b = 0;   // per-warp scratch of the batched kernel (largest candidate)
+    int tune_warps = 0;      // resident warps of the batched kernel (largest candidate)
     struct Done {
         pacc_result r;
         std::vector<int32_t> max_z;
@@ -447,7 +452,9 @@ static bool ensure_model(pacc_ctx* c) {
     std::lock_guard<std::mutex> lk(g_model_mu);
     const int d = c->device;
     if (d >= 0 && d < 64 && g_model_owner[d] == c) return true;
-    if (!cuda_ok(c, set_model(c->M.dm), "set_model") || !cuda_ok(c, set_model_batch(c->M.dm), "set_model_batch"))
+    if (!cuda_ok(c, set_model(c->M.dm, c->stream), "set_model") ||
+        !cuda_ok(c, set_model_batch(c->M.dm, c->stream), "set_model_batch") ||
+        !cuda_ok(c, cudaStreamSynchronize(c->stream), "set_model"))
         return false;
     if (d >= 0 && d < 64) g_model_owner[d] = c;
     return true;
@@ -572,13 +579,121 @@ static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Columns each lane of the batched kernel carries: the caller's choice, else
-// the tuned value for this precision.
-static int batch_columns(const pacc_ctx* c, int prec) {
-    int C = c->o.columns_per_lane;
-    if (C <= 0) C = 1;
-    while (C > 1 && !batch_supports(prec, C)) C >>= 1;
-    return C;
+// ---------------------------------------------------------------------------
+// batched-kernel geometry and the column-count tuner
+// ---------------------------------------------------------------------------
+struct BatchGeom {
+    int C = 1, warps = 4, grid = 1, per_sm = 1;
+    size_t wsm = 0, smem = 0, grp_b = 0;
+};
+
+// Column counts to consider: the caller's (if compiled), else every compiled one.
+static std::vector<int> batch_candidates(const pacc_ctx* c, int prec) {
+    int want = c->o.columns_per_lane;
+    if (want > 0) {
+        while (want > 1 && !batch_supports(prec, want)) want >>= 1;
+        return {want};
+    }
+    std::vector<int> v;
+    for (int C = 1; C <= 4; C <<= 1)
+        if (batch_supports(prec, C)) v.push_back(C);
+    return v;
+}
+
+// Warps per CTA (4, 2 or 1) that keep the most warps resident per SM for
+// column count C, from the kernel's occupancy (registers and shared memory).
+static bool batch_geom(pacc_ctx* c, int prec, int C, int n_int_max, int D, int n_slots, BatchGeom& g) {
+    const int N = c->M.N, S = c->M.S;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    g.C = C;
+    g.wsm = batch_warp_smem(N, n_int_max, S, D, prec, C);
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    const int wmax = c->o.block_threads > 0 ? std::min(4, std::max(1, c->o.block_threads / 32)) : 4;
+    int best = 0;
+    for (int w = wmax; w >= 1; w >>= 1) {
+        const size_t sm = g.wsm * w;
+        if (sm > (size_t)max_smem) continue;
+        const int nb = batch_occupancy(prec, C, w, sm);
+        if (nb * w > best) { best = nb * w; g.warps = w; g.smem = sm; g.per_sm = nb; }
+    }
+    if (best == 0) return false;
+    g.grid = std::max(1, std::min(c->n_sm * g.per_sm, (std::max(n_slots, 1) + g.warps - 1) / g.warps));
+    g.grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec, C));
+    return true;
+}
+
+// Tuned column counts, per (device, taxa, precision, stack depth).
+static std::mutex g_tune_mu;
+static std::map<std::array<int, 4>, int> g_tuned;
+
+static int tuned_columns(const pacc_ctx* c, int prec, int D) {
+    auto cands = batch_candidates(c, prec);
+    if (cands.size() == 1) return cands[0];
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find({c->device, c->M.S, prec, D});
+    return it == g_tuned.end() ? 0 : it->second;
+}
+
+// Picks the column count for this batch.  Without a tuned value and with at
+// least a device-full of chains, each candidate runs the same sample of
+// chains (every k-th element of the batch) for a few sweeps from a fresh
+// start and the fastest is kept for every later batch of this shape.  The
+// trial launches use the batch's own buffers before they are initialised for
+// the real run.
+static int tune_columns(pacc_ctx* c, int prec, int D, int n_int_max, const std::vector<int32_t>& elem, BatchParams& p,
+                        char* d_elem, char* d_ctr, int& C) {
+    C = tuned_columns(c, prec, D);
+    if (C > 0) return PACC_OK;
+    C = 1;
+    const int n_real = elem.empty() || elem[0] < 0 ? 0 : (int)elem.size();
+    BatchGeom g1;
+    if (!batch_geom(c, prec, 1, n_int_max, D, n_real, g1)) return PACC_OK;
+    const int n_trial = c->n_sm * g1.per_sm * g1.warps;
+    if (n_real < n_trial) return PACC_OK;   // too few chains to fill the device: keep 1, decide later
+    std::vector<int32_t> trial(n_trial);
+    for (int i = 0; i < n_trial; i++) trial[i] = elem[(size_t)i * n_real / n_trial];
+    cudaStream_t st = c->stream;
+    if (!cuda_ok(c, cudaMemcpyAsync(d_elem, trial.data(), sizeof(int32_t) * n_trial, cudaMemcpyHostToDevice, st),
+                 "H2D trial"))
+        return PACC_ECUDA;
+    const int save_sweeps = p.sweeps;
+    const int save_slots = p.n_slots;
+    p.n_slots = n_trial;
+    p.sweeps = 6;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0;
+    auto cands = batch_candidates(c, prec);
+    for (int rep = 0; rep < 2; rep++) {   // the first round warms the device up
+        for (int Cc : cands) {
+            BatchGeom g;
+            if (!batch_geom(c, prec, Cc, n_int_max, D, n_trial, g)) continue;
+            float ms = 0;
+            bool ok = cuda_ok(c, launch_init_slots(p.slots, (const int32_t*)d_elem, n_trial, st), "trial slots") &&
+                      cuda_ok(c, cudaMemsetAsync(d_ctr, 0, 256, st), "trial queue") &&
+                      cuda_ok(c, cudaEventRecord(e0, st), "event") &&
+                      cuda_ok(c, launch_batch(&p, g.grid, g.warps, g.smem, prec, Cc, st), "trial launch") &&
+                      cuda_ok(c, cudaEventRecord(e1, st), "event") &&
+                      cuda_ok(c, cudaStreamSynchronize(st), "trial launch") &&
+                      cuda_ok(c, cudaEventElapsedTime(&ms, e0, e1), "event");
+            if (!ok) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return PACC_ECUDA;
+            }
+            if (rep == 1 && (best == 0 || ms < best)) { best = ms; C = Cc; }
+        }
+        if (cands.size() == 1) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p.sweeps = save_sweeps;
+    p.n_slots = save_slots;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[{c->device, c->M.S, prec, D}] = C;
+    return PACC_OK;
 }
 
 // Stack depth bound of the unpruned tree: pruning only removes nodes.
@@ -613,21 +728,21 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     const int T = c->o.burnin + c->o.mcmc;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     v.prec = c->o.precision == PACC_FP32 ? 1 : 0;
-    v.C = batch_columns(c, v.prec);
     v.D = tree_stack_depth(c->M);
     v.n_int_max = S - 1;
     v.SP = (S + 15) & ~15;
     v.GG_cap = std::max(5120, (GG_needed + 31) & ~31);
-    v.warps = 4;
-    size_t wsm = batch_warp_smem(N, v.n_int_max, S, v.D, v.prec, v.C);
-    int max_smem = 0, smem_sm = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-    while (v.warps > 1 && wsm * v.warps > (size_t)max_smem) v.warps--;
-    if (wsm > (size_t)max_smem) { c->err = "element tree too large for the batched kernel"; return PACC_EUNSUPPORTED; }
-    v.smem = wsm * v.warps;
-    int per_sm = std::max(1, std::min((int)(smem_sm / (v.smem + 1024)), 2048 / (v.warps * 32)));
-    v.grid = c->n_sm * per_sm;
+    // the column count tuned by an earlier batch of this shape, else 1
+    v.C = tuned_columns(c, v.prec, v.D);
+    if (v.C <= 0) v.C = 1;
+    BatchGeom g;
+    if (!batch_geom(c, v.prec, v.C, v.n_int_max, v.D, 1 << 30, g)) {
+        c->err = "element tree too large for the batched kernel";
+        return PACC_EUNSUPPORTED;
+    }
+    v.warps = g.warps;
+    v.smem = g.smem;
+    v.grid = g.grid;
     const int n_warps = v.grid * v.warps;
     v.tb = al(topo_bytes(N));
     v.o_prefix = v.tb;
@@ -1172,28 +1287,24 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     if (elem.empty()) elem.push_back(-1);
     int D = 1;
     for (int e = 0; e < n; e++) if (!c->pending[e].filtered) D = std::max(D, c->pending[e].stack_depth);
-    // geometry: warps per CTA from the shared-memory footprint of one chain
-    const int C = batch_columns(c, prec);
-    size_t wsm = batch_warp_smem(N, n_int_max, S, D, prec, C);
-    int max_smem = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    int warps = c->o.block_threads > 0 ? std::min(4, std::max(1, c->o.block_threads / 32)) : 4;
-    while (warps > 1 && wsm * warps > (size_t)max_smem) warps--;
-    if (wsm > (size_t)max_smem) { c->err = "element tree too large for the batched kernel"; return PACC_EUNSUPPORTED; }
-    size_t smem = wsm * warps;
-    int per_sm = 0;
-    cudaFuncAttributes fa;
-    (void)fa;
+    // geometry per column count; the column count itself is tuned (or the caller's)
     {
-        int smem_sm = 0;
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
-        per_sm = std::max(1, (int)(smem_sm / (smem + 1024)));
-        per_sm = std::min(per_sm, 2048 / (warps * 32));
+        std::vector<int> cands = batch_candidates(c, prec);
+        size_t grp_max = 0;
+        int warps_max = 0;
+        for (int Cc : cands) {
+            BatchGeom g;
+            if (!batch_geom(c, prec, Cc, n_int_max, D, n_slots, g)) continue;
+            grp_max = std::max(grp_max, g.grp_b);
+            warps_max = std::max(warps_max, g.grid * g.warps);
+        }
+        if (warps_max == 0) { c->err = "element tree too large for the batched kernel"; return PACC_EUNSUPPORTED; }
+        c->tune_grp_b = grp_max;
+        c->tune_warps = warps_max;
     }
-    int grid = std::max(1, std::min(c->n_sm * per_sm, (n_slots + warps - 1) / warps));
-    const int n_warps = grid * warps;
+    const size_t grp_b = c->tune_grp_b;
+    const int n_warps = c->tune_warps;
     size_t slot_b = al(batch_slot_bytes(N, T));
-    size_t grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec, C));
     size_t o_hdr = 0;
     size_t o_res = al(o_hdr + sizeof(ElemHeader) * n);
     size_t o_mz = al(o_res + sizeof(DevResult) * n);
@@ -1212,10 +1323,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     char* mb = (char*)c->d_misc;
     cudaStream_t st = c->stream;
     if (!cuda_ok(c, cudaMemcpyAsync(c->d_blob, blob.data(), off, cudaMemcpyHostToDevice, st), "H2D blob") ||
-        !cuda_ok(c, cudaMemcpyAsync(mb + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st), "H2D hdr") ||
-        !cuda_ok(c, cudaMemcpyAsync(mb + o_elem, elem.data(), sizeof(int32_t) * elem.size(), cudaMemcpyHostToDevice, st), "H2D elem") ||
-        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_elem - o_res, st), "memset") ||
-        !cuda_ok(c, launch_init_slots(mb + o_slots, (const int32_t*)(mb + o_elem), n_slots, st), "init slots"))
+        !cuda_ok(c, cudaMemcpyAsync(mb + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st), "H2D hdr"))
         return PACC_ECUDA;
     BatchParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1239,6 +1347,23 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     p.n_int_max = n_int_max;
     p.S_max = S;
     p.stack_depth = D;
+    // column count: the caller's, the tuned one for this tree and precision,
+    // or tuned now on a sample of this batch
+    int C = 0;
+    {
+        int st_t = tune_columns(c, prec, D, n_int_max, elem, p, mb + o_elem, mb + o_next, C);
+        if (st_t != PACC_OK) return st_t;
+    }
+    BatchGeom g;
+    batch_geom(c, prec, C, n_int_max, D, n_slots, g);
+    const int warps = g.warps, grid = g.grid;
+    const size_t smem = g.smem;
+    if (!cuda_ok(c, cudaMemcpyAsync(mb + o_elem, elem.data(), sizeof(int32_t) * elem.size(), cudaMemcpyHostToDevice, st), "H2D elem") ||
+        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_elem - o_res, st), "memset") ||
+        !cuda_ok(c, launch_init_slots(mb + o_slots, (const int32_t*)(mb + o_elem), n_slots, st), "init slots"))
+        return PACC_ECUDA;
+    p.n_slots = n_slots;
+    p.sweeps = c->o.sweeps_per_launch;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1408,8 +1533,10 @@ int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, dou
     if (!cuda_ok(c, cudaMalloc(&dd, n * 8), "malloc") || !cuda_ok(c, cudaMalloc(&dr, n * 8), "malloc") ||
         !cuda_ok(c, cudaMalloc(&dout, (size_t)n * 128), "malloc"))
         return PACC_OOM;
-    cudaMemcpy(dd, d, n * 8, cudaMemcpyHostToDevice);
-    cudaMemcpy(dr, r, n * 8, cudaMemcpyHostToDevice);
+    // inputs on the kernel's stream: a plain cudaMemcpy from pageable memory
+    // may still be in flight when a kernel on a non-blocking stream starts
+    cudaMemcpyAsync(dd, d, n * 8, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dr, r, n * 8, cudaMemcpyHostToDevice, c->stream);
     cudaError_t e = launch_pmatrix(n, dd, dr, dout, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 128, cudaMemcpyDeviceToHost);
@@ -1496,9 +1623,9 @@ int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const i
     if (e == cudaSuccess) e = cudaMalloc(&dws, ws);
     if (e == cudaSuccess) e = cudaMalloc(&dz, N * 4);
     if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)E.GG * 8);
-    if (e == cudaSuccess) e = cudaMemcpy(dblob, blob.data(), off, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dh, &H, sizeof(H), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dz, z, N * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dblob, blob.data(), off, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dh, &H, sizeof(H), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z, N * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) {
         ChainParams p;
         std::memset(&p, 0, sizeof(p));

@@ -56,12 +56,12 @@ struct StreamReader {
         return cache[w & 3];
     }
     __device__ double uniform() { return word_to_uniform(word_at(pos++)); }
-    __device__ double normal() {
+    __device__ __noinline__ double normal() {
         double u1 = uniform();
         double u2 = uniform();
         return __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, log(u1))), cos(__dmul_rn(6.283185307179586, u2)));
     }
-    __device__ double gamma(double a, double b) {
+    __device__ __noinline__ double gamma(double a, double b) {
         if (a < 1.0) {
             double g = gamma_ge1(__dadd_rn(a, 1.0), 1.0);
             double u = uniform();
@@ -70,7 +70,7 @@ struct StreamReader {
         return gamma_ge1(a, b);
     }
     // Marsaglia-Tsang for shape >= 1; returns (b*d)*v.
-    __device__ double gamma_ge1(double a, double b) {
+    __device__ __noinline__ double gamma_ge1(double a, double b) {
         double d = __dsub_rn(a, 1.0 / 3.0);
         double c = __ddiv_rn(1.0, __dsqrt_rn(__dmul_rn(9.0, d)));
         double x, v;
@@ -87,7 +87,7 @@ struct StreamReader {
         }
         return __dmul_rn(__dmul_rn(b, d), v);
     }
-    __device__ double beta(double a, double b) {
+    __device__ __noinline__ double beta(double a, double b) {
         double x = gamma(a, 1.0);
         double y = gamma(b, 1.0);
         return __ddiv_rn(x, __dadd_rn(x, y));
