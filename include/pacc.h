@@ -53,7 +53,8 @@ typedef enum pacc_precision {
     PACC_FP64 = 0,              /* plain path: one CTA per element, FP64 partials, partial re-pruning */
     PACC_FP32 = 1,              /* batched path: one warp per element, FP32 partials with power-of-two
                                    rescaling, FP64 log-likelihood sums and chain arithmetic */
-    PACC_FP64_BATCHED = 2       /* the batched layout with FP64 partials (checks the layout draw for draw) */
+    PACC_FP64_BATCHED = 2,      /* the batched layout with FP64 partials (checks the layout draw for draw) */
+    PACC_FP32_PLAIN = 3         /* the plain layout (one CTA per element) with FP32 partials */
 } pacc_precision;
 
 /* Tree, rate matrix and species sets: the content of the .mod file plus the
@@ -250,6 +251,13 @@ int pacc_debug_loglik(pacc_ctx* ctx, const uint8_t* bases, int32_t length, const
  * pruned-tree root.  For bit-exact checks of the host preprocessing. */
 int pacc_debug_encode(pacc_ctx* ctx, const uint8_t* bases, int32_t length, int8_t* tg_out,
                       int32_t* n_cols, uint8_t* missing_out, int32_t* root_out, int32_t* filtered);
+
+/* Site patterns of one element after trimming: pattern_of[g] (int32 [n_cols])
+ * is the pattern of column g, patterns numbered in order of first occurrence;
+ * weights[p] (int32, room for n_cols) counts the columns of pattern p.
+ * Host only; for bit-exact checks of the compression. */
+int pacc_debug_patterns(pacc_ctx* ctx, const uint8_t* bases, int32_t length, int32_t* pattern_of,
+                        int32_t* weights, int32_t* n_cols, int32_t* n_patterns);
 
 /* Philox stream words w0 .. w0+n-1 generated on the device. */
 int pacc_debug_stream(uint32_t seed, uint64_t w0, int n, uint32_t* out);

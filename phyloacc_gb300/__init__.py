@@ -53,6 +53,8 @@ def lib():
         L.pacc_debug_encode.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int8),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32)]
+        L.pacc_debug_patterns.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.pacc_debug_stream.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint32)]
         L.pacc_measure_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
@@ -109,8 +111,10 @@ class Context:
         if st != 0:
             self._err("pacc_sync", st)
 
-    def poll(self, max_n: int) -> abi.Results:
-        res = abi.Results(max_n, self.ds.tree.n_nodes, self.opts.trace_iters)
+    def poll(self, max_n: int, buffers: bool = True) -> abi.Results:
+        """Up to max_n finished results.  In serving mode one call also runs
+        one sweep step.  buffers=False leaves out max_z / post_z / traces."""
+        res = abi.Results(max_n, self.ds.tree.n_nodes, self.opts.trace_iters if buffers else 0, buffers)
         k = lib().pacc_poll(self.h, res.arr, max_n)
         if k < 0:
             self._err("pacc_poll", -k)
@@ -161,6 +165,19 @@ class Context:
         if st != 0:
             self._err("pacc_debug_loglik", st)
         return out[:ncol.value]
+
+    def patterns(self, e: int):
+        """(pattern_of [n_cols], weights [n_patterns]) of element e (host only)."""
+        blk = np.ascontiguousarray(self.ds.element(e).reshape(-1))
+        L = int(self.ds.lengths[e])
+        po = np.zeros(max(L, 1), dtype=np.int32)
+        wt = np.zeros(max(L, 1), dtype=np.int32)
+        nc, npat = C.c_int32(), C.c_int32()
+        st = lib().pacc_debug_patterns(self.h, abi.ptr(blk, C.c_uint8), L, abi.ptr(po, C.c_int32),
+                                       abi.ptr(wt, C.c_int32), C.byref(nc), C.byref(npat))
+        if st not in (0, abi.PACC_FILTERED):
+            self._err("pacc_debug_patterns", st)
+        return po[:nc.value], wt[:npat.value]
 
     def encode(self, e: int):
         blk = np.ascontiguousarray(self.ds.element(e).reshape(-1))

@@ -23,6 +23,7 @@ PACC_EUNSUPPORTED = 9
 PACC_FP64 = 0
 PACC_FP32 = 1
 PACC_FP64_BATCHED = 2
+PACC_FP32_PLAIN = 3
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -181,11 +182,14 @@ class BatchArgs:
 class Results:
     """Result array with caller-owned max_z / post_z / trace buffers."""
 
-    def __init__(self, n: int, n_nodes: int, trace_iters: int = 0):
+    def __init__(self, n: int, n_nodes: int, trace_iters: int = 0, buffers: bool = True):
         self.n = n
         self.N = n_nodes
         self.T = trace_iters
         self.arr = (PaccResult * max(n, 1))()
+        if not buffers:      # scalar fields only (max_z / post_z / traces not copied)
+            self.max_z = self.post_z = self.tr = self.tr_z = None
+            return
         self.max_z = np.zeros((max(n, 1), 3, n_nodes), dtype=np.int32)
         self.post_z = np.zeros((max(n, 1), 3, n_nodes, 4), dtype=np.float64)
         T = max(trace_iters, 1)

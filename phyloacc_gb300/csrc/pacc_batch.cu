@@ -52,12 +52,15 @@ struct SlotLayout {
 
 // Per-warp Eval2 scratch.
 struct GrpLayout {
-    size_t hash, rep, cfg, nxt, head, first, cstat, gpart, total;
-    __host__ __device__ static GrpLayout make(int mcmc, int NI, int real_bytes) {
+    size_t hash, rep, cfg, nxt, head, first, cstat, pst, amb, total;
+    __host__ __device__ static GrpLayout make(int mcmc, int NI, int real_bytes, int GGuP, int NZ) {
         GrpLayout L;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-        L.gpart = o; o = al(o + (size_t)NI * 4 * 32 * real_bytes);   // all internal partials of 32 x C columns (NI = internal nodes x C)
+        // the chain's internal partials per site pattern, two buffers (current
+        // state / proposal): [2][NI][GGuP][4]
+        L.pst = o; o = al(o + (size_t)2 * NI * GGuP * 4 * real_bytes);
+        L.amb = o; o = al(o + (size_t)NZ * 24 * 4);        // (ambiguity code, parent base) counts of leaves
         L.hash = o; o = al(o + (size_t)(mcmc + 1) * 8);
         L.rep = o; o = al(o + (size_t)(mcmc + 1) * 4);
         L.cfg = o; o = al(o + (size_t)(mcmc + 1) * 4);
@@ -73,24 +76,23 @@ struct GrpLayout {
 // Shared memory of one warp-chain; every lane carries C columns.
 template <typename Real>
 struct WarpSmem {
-    size_t ptc, part, tgv, hdf, rec, srec, stage, cnt, topo, i8, dbl, total;
+    size_t ptc, part, tgv, rec, srec, stage, cnt, topo, i8, dbl, total;
     __host__ __device__ static WarpSmem make(int N, int NI, int S, int D, int C) {
         WarpSmem w;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
         w.ptc = o; o = al(o + (size_t)N * 16 * sizeof(Real));        // current P^T per branch
         size_t part_bytes = (size_t)D * C * 4 * 32 * sizeof(Real);      // stack of pending partials
-        size_t alias_bytes = (size_t)N * 6 * 8;                        // emis + bz alias the stack
+        size_t alias_bytes = (size_t)N * 6 * 8;                        // emissions + Z filter alias the stack
         w.part = o; o = al(o + (part_bytes > alias_bytes ? part_bytes : alias_bytes));
         w.tgv = o; o = al(o + (size_t)NI * C * 32);
-        w.hdf = o; o = al(o + 16);
         w.rec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
         w.srec = o; o = al(o + (size_t)NI * sizeof(NodeRec));
         w.stage = o; o = al(o + (size_t)C * ((S + 15) & ~15) * 32);
-        w.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 2);               // uint16 bins
+        w.cnt = o; o = al(o + (size_t)N * 16 * 2);                      // uint16 bins (base, parent base)
         w.topo = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
-        w.i8 = o; o = al(o + (size_t)N * 6);                            // fixZ chg unv mask maxz(unused) Zc
-        w.dbl = o; o = al(o + (size_t)N * 8 + 64 * 8);                  // dist2 + scratch
+        w.i8 = o; o = al(o + (size_t)N * 6);                            // fixZ chg unv mask (unused) Z
+        w.dbl = o; o = al(o + (size_t)N * 8);                           // branch lengths of the pruned tree
         w.total = o;
         return w;
     }
@@ -109,18 +111,24 @@ struct W {
     Real* ptc;          // [N][16]
     Real* part;         // stack of pending partials [D][C][4][32]
     int8_t* tgv;        // [NI][C][32] sampled base (or 4: no data) per internal node and column
-    int8_t* hdf;        // [NI][32] node has data at this lane's column
     const NodeRec* rec; // [NI] internal nodes in postorder (internal_nodes)
     const NodeRec* srec;// [NI] internal nodes in stack order
-    Real* gpart;        // [NI][C][4][32] per-warp device scratch: partials of the sampling pass
+    Real* pst[2];       // per-warp device scratch [2][NI][GGuP][4]: partials per pattern, by buffer
+    int GGuP;           // pattern stride of pst
+    int n_int_max;      // row count of pst
+    int cur;            // buffer of pst that holds the current state's partials
+    const int32_t* pof; // [GG] pattern of each column
     uint32_t* stage;    // [C][SP/4][32] words of per-lane column codes
     const uint8_t* codes_t;  // [GGp][SP]
+    const uint8_t* pcodes_t; // [GGu rounded up to 32][SP] site patterns
+    const int32_t* pw;       // [GGu] pattern weights
+    int GGu;
     int SP;
-    unsigned* cnt;      // [N][20] packed uint16 pairs
+    unsigned* cnt;      // [N][8] packed uint16 pairs: (base, parent base) counts per branch
+    unsigned* amb;      // [N][24] (ambiguity code, parent base) counts of leaf branches (device memory)
     double* emis;       // [N][3]  (aliases part)
     double* bz;         // [N][3]  (aliases part)
     double* dist2;      // [N]
-    double* scr;        // 64 doubles
     int8_t *Z, *fixZ, *chg, *unv, *mask;
     // slot workspace
     int8_t* sZ;
@@ -301,14 +309,15 @@ __device__ __forceinline__ int stage_code(const uint32_t* __restrict__ stage, in
 // arithmetic is independent, which hides the latency of each.  The "has
 // data" flag of a node (some leaf below is a base or an ambiguity code: the
 // complement of Tg == K, bpp_c.hpp:417-428) travels on a register bit stack
-// per column.  With STORE, every partial is also written to the warp's device
-// scratch (for the top-down sampling) and the node's no-data mark to tgv.
+// per column.  With STORE, every partial is also written to the chain's
+// partial buffer (rows by internal rank, columns by pattern g0 + 32 j + lane)
+// for the top-down sampling.
 // sc[j] gets the rescale exponent of column j and root[j] its root partial
 // (pi included).
 template <typename Real, int C, bool STORE>
 __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int n_int,
                                           const uint32_t* __restrict__ stage, int sstride, Real* __restrict__ stk,
-                                          Real* __restrict__ gpart, int8_t* __restrict__ tgv,
+                                          Real* __restrict__ pout, int GGuP, int g0,
                                           const Real* __restrict__ ptc, int lane, const bool (&act)[C],
                                           unsigned& e_int, unsigned& e_leaf, const Real pi[4], Real (&root)[C][4],
                                           int (&sc)[C]) {
@@ -427,9 +436,16 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
             }
             st4(o + j * 128, a[j]);
             hbits[j] = (hbits[j] << 1) | (hs[j] ? 1u : 0u);
-            if (STORE) {
-                st4(gpart + (R.self * C + j) * 128 + lane * 4, a[j]);
-                tgv[(R.self * C + j) * 32 + lane] = hs[j] ? (int8_t)-1 : (int8_t)4;
+            if (STORE && act[j]) {
+                // a node without data below it (other than the root, which is
+                // always drawn) is kept as (-1,-1,-1,-1): the sampling pass
+                // reads the mark with the partial
+                const size_t at = (size_t)R.self * GGuP + g0 + 32 * j + lane;
+                if (hs[j] || R.is_root) st4(pout + at * 4, a[j]);
+                else {
+                    const Real m[4] = {-1, -1, -1, -1};
+                    st4(pout + at * 4, m);
+                }
             }
         }
     }
@@ -439,7 +455,14 @@ __device__ __forceinline__ void column_up(const NodeRec* __restrict__ srec, int 
 struct LLAcc {
     double prod;
     long long e2;
-    __device__ void init() { prod = 1.0; e2 = 0; }
+    double lsum;   // weighted site patterns: FP64 sum of w log(mantissa)
+    __device__ void init() { prod = 1.0; e2 = 0; lsum = 0; }
+    __device__ void add_weighted(double t, int sc, int wgt) {
+        int e;
+        const double m = frexp(t, &e);
+        lsum += (double)wgt * d_log(m);
+        e2 += (long long)wgt * (e + sc);
+    }
     __device__ void add(double t, int sc) {
         int e;
         double m = frexp(t, &e);
@@ -449,44 +472,52 @@ struct LLAcc {
         prod = frexp(prod, &e3);
         e2 += e3;
     }
-    __device__ double value() const { return log(prod) + (double)e2 * 0.6931471805599453; }
+    __device__ double value() const { return d_log(prod) + lsum + (double)e2 * 0.6931471805599453; }
 };
 
-// Full prune of all columns with the current matrices; returns the summed
-// per-column log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).  A pass
-// covers 32 x C columns: lane l takes columns g0 + 32 j + l.
+// Full prune with the current matrices; returns the summed per-column
+// log-likelihood (log_exp_sum at the root, bpp_c.cpp:429).  The pass runs over
+// the element's site patterns and weights each pattern by its column count.
+// A pass covers 32 x C patterns: lane l takes patterns g0 + 32 j + l.  Every
+// internal partial is kept in partial buffer buf (0 or 1; the reference
+// keeps lambda / lambda_tmp the same way, bpp_c.cpp:981-989,1115).
 template <typename Real, int C>
-__device__ __noinline__ double likelihood_pass(W<Real, C>& w) {
-    const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP;
+__device__ __noinline__ double likelihood_pass(W<Real, C>& w, int buf) {
+    const int lane = w.lane, n_int = w.n_int, GU = w.GGu, SP = w.SP;
     const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ srec = w.srec;
-    const uint8_t* __restrict__ codes_t = w.codes_t;
+    const uint8_t* __restrict__ codes_t = w.pcodes_t;
+    const int32_t* __restrict__ pw = w.pw;
     uint32_t* __restrict__ stage = w.stage;
     Real* __restrict__ stk = w.part;
     const Real* __restrict__ ptc = w.ptc;
+    Real* __restrict__ pout = w.pst[buf];
+    const int GGuP = w.GGuP;
     const Real pi[4] = {(Real)dM.pi[0], (Real)dM.pi[1], (Real)dM.pi[2], (Real)dM.pi[3]};
     unsigned e_int = 0, e_leaf = 0;
     double acc = 0;
     LLAcc ll;
     ll.init();
-    for (int g0 = 0; g0 < GG; g0 += 32 * C) {
+    for (int g0 = 0; g0 < GU; g0 += 32 * C) {
         bool act[C];
 #pragma unroll
         for (int j = 0; j < C; j++) {
             const int g = g0 + 32 * j + lane;
-            act[j] = g < GG;
+            act[j] = g < GU;
             stage_column(codes_t, SP, stage + j * sstride, lane, g, act[j]);
         }
         Real r[C][4];
         int sc[C];
-        column_up<Real, C, false>(srec, n_int, stage, sstride, stk, nullptr, nullptr, ptc, lane, act, e_int, e_leaf,
-                                  pi, r, sc);
+        column_up<Real, C, true>(srec, n_int, stage, sstride, stk, pout, GGuP, g0, ptc, lane, act, e_int, e_leaf,
+                                 pi, r, sc);
 #pragma unroll
         for (int j = 0; j < C; j++) {
             if (act[j]) {
+                const int wgt = pw[g0 + 32 * j + lane];
                 double t = (double)r[j][0] + (double)r[j][1] + (double)r[j][2] + (double)r[j][3];
-                if (sizeof(Real) == 8) acc += log(t) + (double)sc[j] * 0.6931471805599453;
-                else ll.add(t, sc[j]);
+                if (sizeof(Real) == 8) acc += (double)wgt * (d_log(t) + (double)sc[j] * 0.6931471805599453);
+                else if (wgt == 1) ll.add(t, sc[j]);
+                else ll.add_weighted(t, sc[j], wgt);
             }
         }
     }
@@ -521,56 +552,59 @@ __device__ __forceinline__ double u_of<float>(uint32_t w) {
 }
 
 // Internal-base pass (Update_Tg with sampling, bpp_c.cpp:672-733) fused with
-// the emission histogram of (child symbol, parent base) pairs.  Each column
-// draws from its own words of the stream (prefix[g] words before it), so the
-// draws do not depend on how columns are spread over lanes.
+// the emission histogram.  The partials are those of the current state, kept
+// by the last likelihood pass in buffer w.cur (per site pattern); column g
+// reads the row of its pattern.  Each column draws from its own words of the
+// stream (prefix[g] words before it), so the draws do not depend on how
+// columns are spread over lanes.
 template <typename Real, int C>
 __device__ __noinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
-    const int NB = NSYM * 4;
     const int lane = w.lane, n_int = w.n_int, GG = w.GG, SP = w.SP, N = w.N;
     const int sstride = (SP >> 2) * 32;
     const NodeRec* __restrict__ rec = w.rec;
-    const NodeRec* __restrict__ srec = w.srec;
     const uint8_t* __restrict__ codes_t = w.codes_t;
     uint32_t* __restrict__ stage = w.stage;
     int8_t* __restrict__ tgv = w.tgv;
-    Real* __restrict__ stk = w.part;
-    Real* __restrict__ part = w.gpart;
+    const Real* __restrict__ part = w.pst[w.cur];
+    const int GGuP = w.GGuP;
+    const int32_t* __restrict__ pof = w.pof;
     const Real* __restrict__ ptc = w.ptc;
     unsigned* __restrict__ cnt = w.cnt;
     const int16_t* __restrict__ irank = w.irank;
     const int32_t* __restrict__ prefix = w.prefix;
     const uint32_t seed = dM.seed;
-    const Real pi[4] = {(Real)dM.pi[0], (Real)dM.pi[1], (Real)dM.pi[2], (Real)dM.pi[3]};
-    for (int i = lane; i < N * NB / 2; i += 32) cnt[i] = 0;
+    unsigned* __restrict__ amb = w.amb;
+    for (int i = lane; i < N * 8; i += 32) cnt[i] = 0;
+    for (int i = lane; i < w.S * 24; i += 32) amb[i] = 0;
     __syncwarp();
     int err = 0;
     const int rk = irank[w.root];
-    unsigned e_int = 0, e_leaf = 0, n_tg = 0;
+    unsigned n_tg = 0;
+    // Emission histogram: once a node's base is drawn, the (base, parent base)
+    // pair of its own branch and the (code, base) pairs of its leaf children
+    // are counted (warp-aggregated with match-any; every non-root node of the
+    // pruned tree is the child of exactly one internal node).
+    auto hist = [&](int node, int key) {
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (key >= 0 && lane == __ffs(peers) - 1) {
+            if (key < 16) {
+                const int bin = node * 16 + key;
+                atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
+            } else {
+                atomicAdd(&amb[node * 24 + key - 16], (unsigned)__popc(peers));   // leaves only, rare
+            }
+        }
+    };
     for (int g0 = 0; g0 < GG; g0 += 32 * C) {
         bool act[C];
+        int pat[C];
 #pragma unroll
         for (int j = 0; j < C; j++) {
             const int g = g0 + 32 * j + lane;
             act[j] = g < GG;
+            pat[j] = act[j] ? pof[g] : 0;
             stage_column(codes_t, SP, stage + j * sstride, lane, g, act[j]);
         }
-        Real rootp[C][4];
-        int sc[C];
-        column_up<Real, C, true>(srec, n_int, stage, sstride, stk, part, tgv, ptc, lane, act, e_int, e_leaf, pi,
-                                 rootp, sc);
-        // Top-down draws, the C columns interleaved, fused with the emission
-        // histogram: once a node's base is drawn, the (base, parent base) pair
-        // of its own branch and the (code, base) pairs of its leaf children are
-        // counted (warp-aggregated with match-any; every non-root node of the
-        // pruned tree is the child of exactly one internal node).
-        auto hist = [&](int node, int key) {
-            const unsigned peers = __match_any_sync(0xffffffffu, key);
-            if (key >= 0 && lane == __ffs(peers) - 1) {
-                const int bin = node * NB + key;
-                atomicAdd(&cnt[bin >> 1], (unsigned)__popc(peers) << (16 * (bin & 1)));
-            }
-        };
         auto leaf_pairs = [&](const NodeRec& R, int j, int base) {
 #pragma unroll
             for (int q = 0; q < 2; q++) {
@@ -593,10 +627,12 @@ __device__ __noinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
             for (int j = 0; j < C; j++) {
                 int nn = 4;
                 if (act[j]) {
+                    Real rootp[4];
+                    ld4(part + ((size_t)rk * GGuP + pat[j]) * 4, rootp);
                     wp[j] = pos + (uint64_t)prefix[g0 + 32 * j + lane];
                     blk[j] = wp[j] >> 2;
                     philox4x32_10((uint32_t)blk[j], (uint32_t)(blk[j] >> 32), 0u, 0u, seed, 0u, words[j]);
-                    nn = cat4(rootp[j], u_of<Real>(words[j][wp[j] & 3]));
+                    nn = cat4(rootp, u_of<Real>(words[j][wp[j] & 3]));
                     wp[j]++;
                     if (nn > 3) { err = 1; nn = 0; }
                     tgv[(rk * C + j) * 32 + lane] = (int8_t)nn;
@@ -605,24 +641,26 @@ __device__ __noinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
                 leaf_pairs(RR, j, nn);
             }
         }
-        // the partials of a node are read two nodes ahead: the loads come from
-        // L2 and their latency overlaps the draws of the nodes in between
-        Real cur[C][4], nx1[C][4], nx2[C][4];
+        // the partials of a node are read three nodes ahead: the loads are
+        // gathers by pattern from L2 or HBM and their latency overlaps the
+        // draws of the nodes in between
+        Real cur[C][4], nx1[C][4], nx2[C][4], nx3[C][4];
         auto load_part = [&](Real (&dst)[C][4], int k) {
 #pragma unroll
-            for (int j = 0; j < C; j++) ld4(part + (k * C + j) * 128 + lane * 4, dst[j]);
+            for (int j = 0; j < C; j++) ld4(part + ((size_t)k * GGuP + pat[j]) * 4, dst[j]);
         };
         if (n_int >= 2) load_part(cur, n_int - 2);
         if (n_int >= 3) load_part(nx1, n_int - 3);
+        if (n_int >= 4) load_part(nx2, n_int - 4);
         for (int k = n_int - 2; k >= 0; k--) {
-            if (k >= 2) load_part(nx2, k - 2);
+            if (k >= 3) load_part(nx3, k - 3);
             const NodeRec R = rec[k];
 #pragma unroll
             for (int j = 0; j < C; j++) {
                 int n2 = 4, tp = 4;
                 if (act[j]) {
                     int8_t* tk = tgv + (k * C + j) * 32 + lane;
-                    if (R.missing || *tk == 4) {
+                    if (R.missing || cur[j][0] < 0) {   // no data below the node (see column_up)
                         *tk = 4;
                     } else {
                         tp = tgv[(R.prank * C + j) * 32 + lane];
@@ -647,11 +685,13 @@ __device__ __noinline__ int sample_pass(W<Real, C>& w, uint64_t pos) {
 #pragma unroll
             for (int j = 0; j < C; j++)
 #pragma unroll
-                for (int i = 0; i < 4; i++) { cur[j][i] = nx1[j][i]; nx1[j][i] = nx2[j][i]; }
+                for (int i = 0; i < 4; i++) {
+                    cur[j][i] = nx1[j][i];
+                    nx1[j][i] = nx2[j][i];
+                    nx2[j][i] = nx3[j][i];
+                }
         }
     }
-    w.e_int += e_int;
-    w.e_leaf += e_leaf;
     w.n_tg += n_tg;
     __syncwarp();
     return warp_or(err);
@@ -667,20 +707,29 @@ __device__ __noinline__ void emission_sums(W<Real, C>& w) {
         if (w.missing[s]) continue;
         const double* P = w.tbl + ((size_t)z * w.N + s) * 16;
         double e = 0;
-        for (int b = 0; b < NB; b++) {
-            int bin = s * NB + b;
-            unsigned n = (w.cnt[bin >> 1] >> (16 * (bin & 1))) & 0xFFFF;
+        // bins 0..15 are packed pairs in shared memory; only leaves can carry
+        // ambiguity codes (bins 16..39, device memory)
+        const int nb = s >= w.S ? 16 : NB;
+        for (int b = 0; b < nb; b++) {
+            unsigned n;
+            if (b < 16) {
+                const unsigned word = w.cnt[(s * 16 + b) >> 1];
+                if (!word) { b |= 1; continue; }   // both bins of the pair are empty
+                n = (word >> (16 * (b & 1))) & 0xFFFF;
+            } else {
+                n = w.amb[s * 24 + b - 16];
+            }
             if (!n) continue;
             int sym = b >> 2, tp = b & 3;
             double v;
             if (sym < 4) {
-                v = (sizeof(Real) == 8) ? log(P[sym * 4 + tp]) : (double)logf((float)P[sym * 4 + tp]);
+                v = (sizeof(Real) == 8) ? d_log(P[sym * 4 + tp]) : (double)f_log((float)P[sym * 4 + tp]);
             } else {
                 int msk = ambig_mask(sym - 4);
                 double tt = 0;
                 for (int q = 0; q < 4; q++)
                     if (msk & (1 << q)) tt += P[q * 4 + tp];
-                v = (sizeof(Real) == 8) ? log(tt) : (double)logf((float)tt);
+                v = (sizeof(Real) == 8) ? d_log(tt) : (double)f_log((float)tt);
             }
             e += (double)n * v;
         }
@@ -704,9 +753,9 @@ __device__ __noinline__ int update_z(W<Real, C>& w, uint64_t pos) {
         bool ban = w.fixZ[s] == 1;
         double mx = e0 > e1 ? e0 : e1;
         if (!ban && e2 > mx) mx = e2;
-        w.bz[s * 3 + 0] = exp(e0 - mx);
-        w.bz[s * 3 + 1] = exp(e1 - mx);
-        w.bz[s * 3 + 2] = ban ? 0.0 : exp(e2 - mx);
+        w.bz[s * 3 + 0] = d_exp(e0 - mx);
+        w.bz[s * 3 + 1] = d_exp(e1 - mx);
+        w.bz[s * 3 + 2] = ban ? 0.0 : d_exp(e2 - mx);
     }
     wsync();
     for (int h = 0; h < w.n_hlev; h++) {
@@ -768,11 +817,13 @@ template <typename Real, int C>
 __device__ __noinline__ int ancestors(W<Real, C>& w, int mode, int8_t* dst) {
     for (int i = w.lane; i < w.N; i += 32) dst[i] = 0;
     wsync();
+#pragma unroll 1
     for (int i = w.lane; i < w.n_nodes; i += 32) {
         int s = w.nodes[i];
         bool f = (mode == 0) ? (w.chg[s] != 0) : (!w.missing[s] && w.Z[s] == (mode == 1 ? 2 : 1));
         if (!f) continue;
         int j = w.par[s];
+#pragma unroll 1
         while (j >= 0 && j < w.N) {
             dst[j] = 1;
             j = w.par[j];
@@ -846,7 +897,7 @@ __device__ __noinline__ double mh_rate(W<Real, C>& w, bool neut, double old_rate
         w.st.pos = bcast(pos);
         if (!skip) {
             fill_ptc(w, cls, proposal);
-            double ll_new = likelihood_pass(w);
+            double ll_new = likelihood_pass(w, w.cur ^ 1);   // proposal partials into the other buffer
             int acc = 0;
             if (w.lane == 0) {
                 double MH;
@@ -860,14 +911,15 @@ __device__ __noinline__ double mh_rate(W<Real, C>& w, bool neut, double old_rate
                     MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, w.st.loglik),
                                                                log_gamma_pdf(proposal, prior_a, prior_b)),
                                                      log_gamma_pdf(old_rate, prior_a, prior_b)),
-                                           log(old_rate)),
-                                   log(proposal));
-                acc = log(r) < MH;
+                                           d_log(old_rate)),
+                                   d_log(proposal));
+                acc = d_log(r) < MH;
             }
             acc = bcast(acc);
             if (acc) {
                 cur = proposal;
                 w.st.loglik = ll_new;
+                w.cur ^= 1;   // the proposal's partials become the current ones
                 build_table(w, cls, cur, true, false, true);
             }
         }
@@ -880,14 +932,14 @@ __device__ __noinline__ double mh_rate(W<Real, C>& w, bool neut, double old_rate
         double scale_adj;
         if (neut) {
             double rate = (double)w.st.acc_n / dM.adapt_freq;
-            scale_adj = rate > 0.44 ? exp(step) : (rate < 0.23 ? exp(-step) : 1.0);
+            scale_adj = rate > 0.44 ? d_exp(step) : (rate < 0.23 ? d_exp(-step) : 1.0);
             w.st.prop_n = __dmul_rn(w.st.prop_n, scale_adj);
             if (w.st.prop_n > 1) w.st.prop_n = 1;
             w.st.acc_n = 0;
         } else {
             double rate = (double)w.st.acc_c / dM.adapt_freq;
-            scale_adj = rate > 0.44 ? exp(step) : (rate < 0.23 ? exp(-step) : 1.0);
-            w.st.prop_c = pow(w.st.prop_c, scale_adj);
+            scale_adj = rate > 0.44 ? d_exp(step) : (rate < 0.23 ? d_exp(-step) : 1.0);
+            w.st.prop_c = d_pow(w.st.prop_c, scale_adj);
             if (w.st.prop_c < 1.0001) w.st.prop_c = 1.0001;
             w.st.acc_c = 0;
         }
@@ -910,7 +962,7 @@ __device__ __noinline__ double prior_config(W<Real, C>& w, const int8_t* z) {
     }
     pz += lnbeta(dM.la + nZ[2][1], dM.lb + nZ[1][1]) - lnbeta(dM.la, dM.lb);
     if (dM.l2a > 0) pz += lnbeta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]) - lnbeta(dM.l2a, dM.l2b);
-    pz += (z[w.root] == 2) ? -CUDART_INF : log(0.5);
+    pz += (z[w.root] == 2) ? -CUDART_INF : d_log(0.5);
     return pz;
 }
 
@@ -919,9 +971,7 @@ template <typename Real, int C>
 __device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) {
     const int burn = w.burn, mcmc = w.mcmc, T = w.T, N = w.N;
     const int resZ = w.st.resZ;
-    // Eval2 runs after the chain, so it reuses the warp scratch from its start
-    // (the sampling-pass partials are not live any more).
-    GrpLayout G = GrpLayout::make(mcmc, 0, 0);
+    GrpLayout G = GrpLayout::make(mcmc, w.n_int_max, sizeof(Real), w.GGuP, N);
     uint64_t* hash = (uint64_t*)(gws + G.hash);
     int32_t* rep = (int32_t*)(gws + G.rep);
     int32_t* cfg = (int32_t*)(gws + G.cfg);
@@ -1014,12 +1064,12 @@ __device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) 
         SF[j] = __dadd_rn(SF[j], __ddiv_rn(__dmul_rn(n, pz), (double)mcmc));
         double ld;
         if (resZ == 0) {
-            ld = __dsub_rn(log(__dsub_rn(vc, __ddiv_rn(__dmul_rn(mc, mc), n))), log(n));
+            ld = __dsub_rn(d_log(__dsub_rn(vc, __ddiv_rn(__dmul_rn(mc, mc), n))), d_log(n));
         } else {
             double a = __dsub_rn(vc, __ddiv_rn(__dmul_rn(mc, mc), n));
             double b = __dsub_rn(vn, __ddiv_rn(__dmul_rn(mn, mn), n));
             double cov = __dsub_rn(cv, __ddiv_rn(__dmul_rn(mn, mc), n));
-            ld = __dsub_rn(log(__dsub_rn(__dmul_rn(a, b), __dmul_rn(cov, cov))), __dmul_rn(2.0, log(n)));
+            ld = __dsub_rn(d_log(__dsub_rn(__dmul_rn(a, b), __dmul_rn(cov, cov))), __dmul_rn(2.0, d_log(n)));
         }
         LD[j] = ld;
     }
@@ -1032,7 +1082,7 @@ __device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) 
             if (wgt < 0.02) continue;
             if (isnan(LD[j])) continue;
             eff += (int)CNT[j];
-            VB = __dsub_rn(VB, __dmul_rn(wgt, log(CNT[j])));
+            VB = __dsub_rn(VB, __dmul_rn(wgt, d_log(CNT[j])));
             VB = __dadd_rn(VB, SF[j]);
             VB = __dadd_rn(VB, __ddiv_rn(__dmul_rn(__dmul_rn(0.5, LD[j]), CNT[j]), (double)mcmc));
         }
@@ -1056,7 +1106,7 @@ __device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) 
             wsync();
             double pz = prior_config(w, z);
             fill_ptc(w, -1, 0.0);
-            double ll = likelihood_pass(w);
+            double ll = likelihood_pass(w, w.cur ^ 1);   // the chain is over: either buffer may be overwritten
             if (w.lane == 0) SF[j] = __dadd_rn(ll, pz);
         }
         __syncwarp();
@@ -1067,30 +1117,30 @@ __device__ __noinline__ double eval2(W<Real, C>& w, char* gws, int* n_conf_out) 
             if (mx == -CUDART_INF) v = -CUDART_INF;
             else {
                 double sm = 0;
-                for (int j = 0; j < nconf; j++) sm = __dadd_rn(sm, exp(__dsub_rn(SF[j], mx)));
-                v = __dadd_rn(log(sm), mx);
+                for (int j = 0; j < nconf; j++) sm = __dadd_rn(sm, d_exp(__dsub_rn(SF[j], mx)));
+                v = __dadd_rn(d_log(sm), mx);
             }
             v = __dadd_rn(v, log_gamma_pdf(rc, dM.cprior_a, dM.cprior_b));
             if (resZ != 0) v = __dadd_rn(v, log_gamma_pdf(rn, dM.nprior_a, dM.nprior_b));
             double logdet;
             if (resZ == 0) {
                 varc = __dsub_rn(varc, __ddiv_rn(__dmul_rn(meanc, meanc), (double)mcmc));
-                logdet = __dsub_rn(log(varc), log((double)mcmc));
-                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), __dmul_rn(0.5, log(2 * CUDART_PI))));
+                logdet = __dsub_rn(d_log(varc), d_log((double)mcmc));
+                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), __dmul_rn(0.5, d_log(2 * CUDART_PI))));
             } else {
                 varn = __dsub_rn(varn, __ddiv_rn(__dmul_rn(meann, meann), (double)mcmc));
                 varc = __dsub_rn(varc, __ddiv_rn(__dmul_rn(meanc, meanc), (double)mcmc));
                 cov = __dsub_rn(cov, __ddiv_rn(__dmul_rn(meann, meanc), (double)mcmc));
-                logdet = __dsub_rn(log(__dsub_rn(__dmul_rn(varc, varn), __dmul_rn(cov, cov))),
-                                   __dmul_rn(2.0, log((double)mcmc)));
-                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), log(2 * CUDART_PI)));
+                logdet = __dsub_rn(d_log(__dsub_rn(__dmul_rn(varc, varn), __dmul_rn(cov, cov))),
+                                   __dmul_rn(2.0, d_log((double)mcmc)));
+                v = __dadd_rn(v, __dadd_rn(__dmul_rn(0.5, logdet), d_log(2 * CUDART_PI)));
             }
         }
         VB = bcast(v);
     } else {
         double f = (double)mcmc / eff;
-        if (resZ != 0) VB = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(VB, f), log((double)mcmc)), log(2 * CUDART_PI)), 1.0);
-        else VB = __dadd_rn(__dadd_rn(__dmul_rn(VB, f), log((double)mcmc)), __dmul_rn(0.5, __dadd_rn(log(2 * CUDART_PI), 1.0)));
+        if (resZ != 0) VB = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(VB, f), d_log((double)mcmc)), d_log(2 * CUDART_PI)), 1.0);
+        else VB = __dadd_rn(__dadd_rn(__dmul_rn(VB, f), d_log((double)mcmc)), __dmul_rn(0.5, __dadd_rn(d_log(2 * CUDART_PI), 1.0)));
     }
     return VB;
 }
@@ -1148,7 +1198,8 @@ __device__ __noinline__ void init_model(W<Real, C>& w) {
     build_table(w, C_NEUT, dM.init_n, true, false, false);
     build_table(w, C_CONS, dM.init_c, true, false, false);
     fill_ptc(w, -1, 0.0);
-    w.st.loglik = likelihood_pass(w);
+    w.cur = 0;
+    w.st.loglik = likelihood_pass(w, w.cur);
     w.st.phase = PH_RUN;
 }
 
@@ -1180,28 +1231,30 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
     w.emis = (double*)(base + L.part);
     w.bz = w.emis + (size_t)N * 3;
     w.tgv = (int8_t*)(base + L.tgv);
-    w.hdf = (int8_t*)(base + L.hdf);
+    int16_t* t16 = (int16_t*)(base + L.topo);
+    w.nodes = t16 + TL.nodes; w.internal = t16 + TL.internal; w.c2a = t16 + TL.c2a; w.c2b = t16 + TL.c2b;
+    w.par = t16 + TL.par; w.irank = t16 + TL.irank; w.pos = t16 + TL.pos; w.missing = t16 + TL.missing;
+    w.upc = t16 + TL.upc; w.upcc = t16 + TL.upcc; w.hlev_start = t16 + TL.hlev_start;
+    w.hlev_nodes = t16 + TL.hlev_nodes; w.dlev_start = t16 + TL.dlev_start; w.dlev_nodes = t16 + TL.dlev_nodes;
+    w.dist2 = (double*)(base + L.dbl);
     NodeRec* recw = (NodeRec*)(base + L.rec);
     w.rec = recw;
     NodeRec* srecw = (NodeRec*)(base + L.srec);
     w.srec = srecw;
     w.stage = (uint32_t*)(base + L.stage);
     w.cnt = (unsigned*)(base + L.cnt);
-    int16_t* t16 = (int16_t*)(base + L.topo);
-    w.nodes = t16 + TL.nodes; w.internal = t16 + TL.internal; w.c2a = t16 + TL.c2a; w.c2b = t16 + TL.c2b;
-    w.par = t16 + TL.par; w.irank = t16 + TL.irank; w.pos = t16 + TL.pos; w.missing = t16 + TL.missing;
-    w.upc = t16 + TL.upc; w.upcc = t16 + TL.upcc; w.hlev_start = t16 + TL.hlev_start;
-    w.hlev_nodes = t16 + TL.hlev_nodes; w.dlev_start = t16 + TL.dlev_start; w.dlev_nodes = t16 + TL.dlev_nodes;
     int8_t* f8 = (int8_t*)(base + L.i8);
     w.fixZ = f8; w.chg = f8 + N; w.unv = f8 + 2 * N; w.mask = f8 + 3 * N; w.Z = f8 + 5 * N;
-    w.dist2 = (double*)(base + L.dbl);
-    w.scr = w.dist2 + N;
     const int gw = blockIdx.x * nw + wid;
     const int n_gw = gridDim.x * nw;
     char* gws = P.grp_ws + (size_t)gw * P.grp_ws_stride;
     {
-        GrpLayout GLy = GrpLayout::make(dM.mcmc, P.n_int_max * C, sizeof(Real));
-        w.gpart = (Real*)(gws + GLy.gpart);
+        GrpLayout GLy = GrpLayout::make(dM.mcmc, P.n_int_max, sizeof(Real), P.GGuP_max, N);
+        w.pst[0] = (Real*)(gws + GLy.pst);
+        w.pst[1] = w.pst[0] + (size_t)P.n_int_max * P.GGuP_max * 4;
+        w.GGuP = P.GGuP_max;
+        w.n_int_max = P.n_int_max;
+        w.amb = (unsigned*)(gws + GLy.amb);
     }
     const SlotLayout SL = SlotLayout::make(N, w.T);
     const int TI = dM.trace_iters < w.T ? dM.trace_iters : w.T;
@@ -1221,6 +1274,11 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
         w.n_hlev = H.n_hlev; w.n_dlev = H.n_dlev; w.tg_draws = H.tg_draws;
         w.codes = P.blob + H.codes_off;
         w.codes_t = P.blob + H.codes_t_off;
+        w.pof = (const int32_t*)(P.blob + H.pof_off);
+        w.cur = 0;
+        w.pcodes_t = P.blob + H.pcodes_off;
+        w.pw = (const int32_t*)(P.blob + H.pw_off);
+        w.GGu = H.GGu;
         w.SP = H.SP;
         w.prefix = (const int32_t*)(P.blob + H.prefix_off);
         {
@@ -1285,6 +1343,11 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
                 if (resZ == 2 && w.upcc[s]) w.fixZ[s] = 1;
                 if (resZ == 0 && s != w.root) w.fixZ[s] = 1;
             }
+            wsync();
+            // the partial buffers belong to the warp, not the slot: rebuild the
+            // current state's partials (the log-likelihood itself is kept)
+            fill_ptc(w, -1, 0.0);
+            likelihood_pass(w, w.cur);
         }
         wsync();
         // iterations this launch: `sweeps` for a 256-column element, scaled by
@@ -1374,7 +1437,7 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
             emission_sums(w);
             // missing nodes keep fixed emissions (bpp_c.hpp:451-474); the root has none
             for (int i = lane; i < N; i += 32) {
-                if (w.missing[i]) { w.emis[i * 3 + 0] = 0; w.emis[i * 3 + 1] = log(dM.cons_to_mis); w.emis[i * 3 + 2] = 0; }
+                if (w.missing[i]) { w.emis[i * 3 + 0] = 0; w.emis[i * 3 + 1] = d_log(dM.cons_to_mis); w.emis[i * 3 + 2] = 0; }
             }
             if (lane == 0) { w.emis[w.root * 3 + 0] = 0; w.emis[w.root * 3 + 1] = 0; w.emis[w.root * 3 + 2] = 0; }
             wsync();
@@ -1386,7 +1449,7 @@ __global__ void __launch_bounds__(128) batch_kernel(BatchParams P) {
             // log-likelihood under the new Z when a branch changed (bpp_c.cpp:419-431)
             if (ancestors(w, 0, w.unv)) {
                 fill_ptc(w, -1, 0.0);
-                w.st.loglik = likelihood_pass(w);
+                w.st.loglik = likelihood_pass(w, w.cur);
             }
             PHASE(3);
             // rates (bpp_c.cpp:434-452)
@@ -1463,8 +1526,8 @@ size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C) {
     return prec == 0 ? WarpSmem<double>::make(N, NI, S, D, C).total : WarpSmem<float>::make(N, NI, S, D, C).total;
 }
 size_t batch_slot_bytes(int N, int T) { return SlotLayout::make(N, T).total; }
-size_t batch_grp_bytes(int mcmc, int NI, int prec, int C) {
-    return GrpLayout::make(mcmc, NI * C, prec == 0 ? 8 : 4).total;
+size_t batch_grp_bytes(int mcmc, int NI, int prec, int GGuP, int N) {
+    return GrpLayout::make(mcmc, NI, prec == 0 ? 8 : 4, GGuP, N).total;
 }
 size_t batch_state_bytes() { return sizeof(SlotState); }
 

@@ -1033,7 +1033,10 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
 
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) elem_ = atomicAdd(P.next_elem, 1);
+        if (threadIdx.x == 0) {
+            const int i = atomicAdd(P.next_elem, 1);
+            elem_ = (i < P.n_elem && P.order) ? P.order[i] : i;
+        }
         __syncthreads();
         const int e = elem_;
         if (e >= P.n_elem) break;

@@ -17,24 +17,24 @@ static __constant__ DevModel dM;
 static __device__ __noinline__ double gamma_pdf(double x, double a, double b) {
     if (x < 0) return 0.0;
     if (x == 0) return (a == 1) ? 1.0 / b : 0.0;
-    double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, log(x)), __ddiv_rn(x, b)), lgamma(a)),
-                         __dmul_rn(a, log(b)));
-    return exp(t);
+    double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, d_log(x)), __ddiv_rn(x, b)), d_lgamma(a)),
+                         __dmul_rn(a, d_log(b)));
+    return d_exp(t);
 }
-static __device__ __forceinline__ double log_gamma_pdf(double x, double a, double b) { return log(gamma_pdf(x, a, b)); }
+static __device__ __forceinline__ double log_gamma_pdf(double x, double a, double b) { return d_log(gamma_pdf(x, a, b)); }
 static __device__ __forceinline__ double lnbeta(double a, double b) {
-    return __dsub_rn(__dadd_rn(lgamma(a), lgamma(b)), lgamma(__dadd_rn(a, b)));
+    return __dsub_rn(__dadd_rn(d_lgamma(a), d_lgamma(b)), d_lgamma(__dadd_rn(a, b)));
 }
 
 // P^T(d*r) = eigeninv * diag(exp(lambda*d*r)) * eigenvec  (bpp.hpp:375-380), FP64.
 // scaled=false uses exp(lambda*d) as the null-rate cache does (bpp.hpp:375).
-static __device__ void build_pt(double d, double r, bool scaled, double* out) {
+static __device__ __noinline__ void build_pt(double d, double r, bool scaled, double* out) {
     double e[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         double x = __dmul_rn(dM.lam[i], d);
         if (scaled) x = __dmul_rn(x, r);
-        e[i] = exp(x);
+        e[i] = d_exp(x);
     }
 #pragma unroll
     for (int a = 0; a < 4; a++)

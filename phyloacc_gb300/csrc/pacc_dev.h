@@ -64,7 +64,10 @@ struct ElemHeader {
     int32_t filtered;
     int32_t SP;            // taxa per column row in codes_t (multiple of 16)
     int32_t stack_depth;   // partials pending at once in the stack-order traversal
-    int32_t pad2;
+    int32_t GGu;           // distinct site patterns among the GG columns
+    int64_t pcodes_off;    // byte offset of the patterns by column [GGu rounded up to 32][SP]
+    int64_t pw_off;        // byte offset of the pattern weights [GGu] (int32)
+    int64_t pof_off;       // byte offset of the pattern of each column [GG] (int32)
 };
 
 // Layout of the int16 topology block (each array length N unless noted).
@@ -132,6 +135,7 @@ struct ChainParams {
     const uint8_t* blob;       // element data (codes, initial Tg, draw prefix, topology)
     int n_elem;
     int* next_elem;            // work counter (atomic)
+    const int32_t* order;      // element claimed by work item i (longest first), or null
     DevResult* results;        // [n_elem]
     int32_t* max_z;            // [n_elem][3][N]
     double* post_z;            // [n_elem][3][N][4]
@@ -180,6 +184,7 @@ struct BatchParams {
     int* done_list;           // slots that reached PH_DONE in this launch (n_done entries), or null
     int n_int_max, S_max;
     int stack_depth;          // max over admitted elements
+    int GGuP_max;             // pattern capacity of the per-warp partial buffers (multiple of 32)
 };
 
 }  // namespace pacc

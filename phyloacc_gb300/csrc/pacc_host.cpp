@@ -43,7 +43,7 @@ cudaError_t launch_fma_probe(int prec, int grid, int BT, int iters, void* out, c
 cudaError_t set_model_batch(const DevModel& m, cudaStream_t st);
 size_t batch_warp_smem(int N, int NI, int S, int D, int prec, int C);
 size_t batch_slot_bytes(int N, int T);
-size_t batch_grp_bytes(int mcmc, int NI, int prec, int C);
+size_t batch_grp_bytes(int mcmc, int NI, int prec, int GGuP, int N);
 cudaError_t noalloc_scratch_address(double** p);
 bool batch_supports(int prec, int C);
 int batch_occupancy(int prec, int C, int warps, size_t smem);
@@ -69,6 +69,10 @@ struct HostElem {
     int GG = 0, GGp = 0, root = 0, n_nodes = 0, n_int = 0, n_hlev = 0, n_dlev = 0, tg_draws = 0;
     std::vector<uint8_t> codes;    // [S][GGp]
     std::vector<uint8_t> codes_t;  // [GGp][SP] column-major copy for 128-bit per-column loads
+    int GGu = 0;                   // distinct site patterns
+    std::vector<uint8_t> pcodes_t; // [GGu rounded up to 32][SP] the patterns in first-occurrence order
+    std::vector<int32_t> pw;       // [GGu] columns per pattern
+    std::vector<int32_t> pattern_of;  // [GG] pattern of each column
     std::vector<int8_t> tg0;       // [n_int][GGp]
     std::vector<int32_t> prefix;   // [GG+1]
     std::vector<int16_t> topo;     // TopoLayout
@@ -97,6 +101,45 @@ static inline uint8_t encode_char(uint8_t ch, char gapchar) {
 }
 
 static inline int code_tg(uint8_t c) { return c < 4 ? c : (c == CODE_GAP ? 4 : (c == CODE_OTHER ? 5 : -1)); }
+
+// Site patterns: the distinct columns (all taxa's codes equal) in order of
+// first occurrence, with the number of columns of each.  A column's
+// likelihood depends only on its codes, so the likelihood passes run once per
+// pattern and weight it; the internal-base draws still run per column.
+static void compress_patterns(HostElem& E, int SP) {
+    const int GG = E.GG;
+    size_t cap = 16;
+    while (cap < (size_t)GG * 2) cap <<= 1;
+    std::vector<int32_t> slot(cap, -1);  // open addressing: pattern id
+    std::vector<int32_t> first;          // first column of each pattern
+    E.pattern_of.assign(GG, 0);
+    E.pw.clear();
+    for (int g = 0; g < GG; g++) {
+        const uint8_t* col = &E.codes_t[(size_t)g * SP];
+        uint64_t h = 1469598103934665603ull;
+        for (int s = 0; s < SP; s++) h = (h ^ col[s]) * 1099511628211ull;
+        size_t i = (size_t)(h ^ (h >> 29)) & (cap - 1);
+        int pid = -1;
+        while (slot[i] >= 0) {
+            const int q = slot[i];
+            if (std::memcmp(&E.codes_t[(size_t)first[q] * SP], col, SP) == 0) { pid = q; break; }
+            i = (i + 1) & (cap - 1);
+        }
+        if (pid < 0) {
+            pid = (int)first.size();
+            first.push_back(g);
+            E.pw.push_back(0);
+            slot[i] = pid;
+        }
+        E.pattern_of[g] = pid;
+        E.pw[pid]++;
+    }
+    E.GGu = (int)first.size();
+    const int GGuP = (E.GGu + 31) & ~31;
+    E.pcodes_t.assign((size_t)std::max(GGuP, 32) * SP, CODE_GAP);
+    for (int p = 0; p < E.GGu; p++)
+        std::memcpy(&E.pcodes_t[(size_t)p * SP], &E.codes_t[(size_t)first[p] * SP], SP);
+}
 
 // Per-element preprocessing (BPP_C ctor, bpp_c.hpp:143-476).  Returns false
 // only on invalid input; filtered elements return true with E.filtered = 1.
@@ -136,6 +179,7 @@ static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* ba
     E.codes_t.assign((size_t)GGp * SP, CODE_GAP);
     for (int i = 0; i < GG; i++)
         for (int s = 0; s < S; s++) E.codes_t[(size_t)i * SP + s] = E.codes[(size_t)s * GGp + i];
+    compress_patterns(E, SP);
     // gap counts and missing flags (bpp_c.hpp:303-351)
     std::vector<int> num_missing(S, 0);
     for (int s = 0; s < S; s++)
@@ -344,7 +388,12 @@ using namespace pacc;
 struct Server {
     bool ready = false;
     int n_slots = 0, warps = 4, grid = 0, prec = 1, C = 1, D = 1, n_int_max = 1, GG_cap = 0, SP = 16;
-    size_t smem = 0, slot_b = 0, grp_b = 0, blob_b = 0, tb = 0, o_prefix = 0, o_codes = 0;
+    size_t smem = 0, slot_b = 0, grp_b = 0, blob_b = 0, tb = 0, o_prefix = 0, o_codes = 0, o_pcodes = 0, o_pw = 0,
+           o_pof = 0;
+    char* h_stage = nullptr;   // pinned staging of admitted elements
+    size_t h_stage_cap = 0;
+    bool inflight = false;     // a sweep was launched and not yet retired
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     char* dev = nullptr;
     ElemHeader* d_hdr = nullptr;
     char* d_blob = nullptr;
@@ -452,6 +501,9 @@ static bool ensure_model(pacc_ctx* c) {
     std::lock_guard<std::mutex> lk(g_model_mu);
     const int d = c->device;
     if (d >= 0 && d < 64 && g_model_owner[d] == c) return true;
+    // a kernel of the context whose model is there may still run (serving)
+    if (d >= 0 && d < 64 && g_model_owner[d] && g_model_owner[d]->stream)
+        cudaStreamSynchronize(g_model_owner[d]->stream);
     if (!cuda_ok(c, set_model(c->M.dm, c->stream), "set_model") ||
         !cuda_ok(c, set_model_batch(c->M.dm, c->stream), "set_model_batch") ||
         !cuda_ok(c, cudaStreamSynchronize(c->stream), "set_model"))
@@ -554,6 +606,10 @@ const char* pacc_last_error(pacc_ctx* c) { return c ? c->err.c_str() : g_create_
 
 void pacc_destroy(pacc_ctx* c) {
     if (!c) return;
+    if (c->gpu_ok && c->stream) {
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->stream);   // a serving sweep may still be in flight
+    }
     {
         std::lock_guard<std::mutex> lk(g_model_mu);
         if (c->device >= 0 && c->device < 64 && g_model_owner[c->device] == c) g_model_owner[c->device] = nullptr;
@@ -566,6 +622,9 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->srv.graph) cudaGraphDestroy(c->srv.graph);
     if (c->srv.dev) cudaFree(c->srv.dev);
     if (c->srv.h_done) cudaFreeHost(c->srv.h_done);
+    if (c->srv.h_stage) cudaFreeHost(c->srv.h_stage);
+    if (c->srv.ev0) cudaEventDestroy(c->srv.ev0);
+    if (c->srv.ev1) cudaEventDestroy(c->srv.ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -573,7 +632,10 @@ void pacc_destroy(pacc_ctx* c) {
 // ---------------------------------------------------------------------------
 // serving: resident chain slots, continuous admission (batched kernel only)
 // ---------------------------------------------------------------------------
-static bool serving(const pacc_ctx* c) { return c->o.sweeps_per_launch > 0 && c->o.precision != PACC_FP64; }
+static bool batched_layout(const pacc_ctx* c) {
+    return c->o.precision == PACC_FP32 || c->o.precision == PACC_FP64_BATCHED;
+}
+static bool serving(const pacc_ctx* c) { return c->o.sweeps_per_launch > 0 && batched_layout(c); }
 
 static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -602,7 +664,7 @@ static std::vector<int> batch_candidates(const pacc_ctx* c, int prec) {
 
 // Warps per CTA (4, 2 or 1) that keep the most warps resident per SM for
 // column count C, from the kernel's occupancy (registers and shared memory).
-static bool batch_geom(pacc_ctx* c, int prec, int C, int n_int_max, int D, int n_slots, BatchGeom& g) {
+static bool batch_geom(pacc_ctx* c, int prec, int C, int n_int_max, int D, int n_slots, int GGuP, BatchGeom& g) {
     const int N = c->M.N, S = c->M.S;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     g.C = C;
@@ -619,7 +681,7 @@ static bool batch_geom(pacc_ctx* c, int prec, int C, int n_int_max, int D, int n
     }
     if (best == 0) return false;
     g.grid = std::max(1, std::min(c->n_sm * g.per_sm, (std::max(n_slots, 1) + g.warps - 1) / g.warps));
-    g.grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec, C));
+    g.grp_b = al(batch_grp_bytes(c->o.mcmc, n_int_max, prec, GGuP, c->M.N));
     return true;
 }
 
@@ -641,14 +703,14 @@ static int tuned_columns(const pacc_ctx* c, int prec, int D) {
 // start and the fastest is kept for every later batch of this shape.  The
 // trial launches use the batch's own buffers before they are initialised for
 // the real run.
-static int tune_columns(pacc_ctx* c, int prec, int D, int n_int_max, const std::vector<int32_t>& elem, BatchParams& p,
-                        char* d_elem, char* d_ctr, int& C) {
+static int tune_columns(pacc_ctx* c, int prec, int D, int n_int_max, int GGuP, const std::vector<int32_t>& elem,
+                        BatchParams& p, char* d_elem, char* d_ctr, int& C) {
     C = tuned_columns(c, prec, D);
     if (C > 0) return PACC_OK;
     C = 1;
     const int n_real = elem.empty() || elem[0] < 0 ? 0 : (int)elem.size();
     BatchGeom g1;
-    if (!batch_geom(c, prec, 1, n_int_max, D, n_real, g1)) return PACC_OK;
+    if (!batch_geom(c, prec, 1, n_int_max, D, n_real, GGuP, g1)) return PACC_OK;
     const int n_trial = c->n_sm * g1.per_sm * g1.warps;
     if (n_real < n_trial) return PACC_OK;   // too few chains to fill the device: keep 1, decide later
     std::vector<int32_t> trial(n_trial);
@@ -669,7 +731,7 @@ static int tune_columns(pacc_ctx* c, int prec, int D, int n_int_max, const std::
     for (int rep = 0; rep < 2; rep++) {   // the first round warms the device up
         for (int Cc : cands) {
             BatchGeom g;
-            if (!batch_geom(c, prec, Cc, n_int_max, D, n_trial, g)) continue;
+            if (!batch_geom(c, prec, Cc, n_int_max, D, n_trial, GGuP, g)) continue;
             float ms = 0;
             bool ok = cuda_ok(c, launch_init_slots(p.slots, (const int32_t*)d_elem, n_trial, st), "trial slots") &&
                       cuda_ok(c, cudaMemsetAsync(d_ctr, 0, 256, st), "trial queue") &&
@@ -736,7 +798,7 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.C = tuned_columns(c, v.prec, v.D);
     if (v.C <= 0) v.C = 1;
     BatchGeom g;
-    if (!batch_geom(c, v.prec, v.C, v.n_int_max, v.D, 1 << 30, g)) {
+    if (!batch_geom(c, v.prec, v.C, v.n_int_max, v.D, 1 << 30, v.GG_cap, g)) {
         c->err = "element tree too large for the batched kernel";
         return PACC_EUNSUPPORTED;
     }
@@ -747,9 +809,12 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.tb = al(topo_bytes(N));
     v.o_prefix = v.tb;
     v.o_codes = al(v.o_prefix + (size_t)(v.GG_cap + 1) * 4);
-    v.blob_b = al(v.o_codes + (size_t)v.GG_cap * v.SP);
+    v.o_pcodes = al(v.o_codes + (size_t)v.GG_cap * v.SP);
+    v.o_pw = al(v.o_pcodes + (size_t)v.GG_cap * v.SP);
+    v.o_pof = al(v.o_pw + (size_t)v.GG_cap * 4);
+    v.blob_b = al(v.o_pof + (size_t)v.GG_cap * 4);
     v.slot_b = al(batch_slot_bytes(N, T));
-    v.grp_b = al(batch_grp_bytes(c->o.mcmc, v.n_int_max, v.prec, v.C));
+    v.grp_b = al(batch_grp_bytes(c->o.mcmc, v.n_int_max, v.prec, v.GG_cap, N));
     v.TI = std::min(c->o.trace_iters, T);
     size_t per_slot = v.blob_b + v.slot_b + sizeof(ElemHeader) + sizeof(SlotState) + sizeof(DevResult) +
                       3 * N * 4 + 3 * N * 4 * 8 + sizeof(double) * 3 * 6 * (size_t)v.TI + (size_t)3 * v.TI * N + 8;
@@ -782,6 +847,8 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     size_t o_done = o; o = al(o + sizeof(int) * (ns + 1));
     if (!cuda_ok(c, cudaMalloc((void**)&v.dev, o), "cudaMalloc (serving slots)")) return PACC_OOM;
     if (!cuda_ok(c, cudaMallocHost((void**)&v.h_done, sizeof(int) * (ns + 2)), "cudaMallocHost")) return PACC_OOM;
+    if (!cuda_ok(c, cudaEventCreate(&v.ev0), "event") || !cuda_ok(c, cudaEventCreate(&v.ev1), "event"))
+        return PACC_ECUDA;
     v.d_hdr = (ElemHeader*)(v.dev + o_hdr);
     v.d_blob = v.dev + o_blob;
     v.d_slots = (SlotState*)(v.dev + o_slots);
@@ -828,6 +895,7 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     v.p.n_int_max = v.n_int_max;
     v.p.S_max = S;
     v.p.stack_depth = v.D;
+    v.p.GGuP_max = v.GG_cap;
     // the sweep step: reset the queue counters, advance every resident chain,
     // copy the list of chains that finished back to pinned host memory
     auto record = [&](cudaStream_t s2) -> cudaError_t {
@@ -877,13 +945,20 @@ static int server_admit(pacc_ctx* c) {
     }
     if (adm.empty()) return PACC_OK;
     // stage every admitted element contiguously in pinned memory, then copy
+    auto staged = [&](const HostElem& E) {
+        return v.tb + E.prefix.size() * 4 + E.codes_t.size() + E.pcodes_t.size() + E.pw.size() * 4 +
+               E.pattern_of.size() * 4 + sizeof(ElemHeader) + sizeof(SlotState) + 64;
+    };
     size_t tot = 0;
-    for (auto& a : adm) {
-        const HostElem& E = a.second.first;
-        tot += v.tb + E.prefix.size() * 4 + E.codes_t.size() + sizeof(ElemHeader) + sizeof(SlotState) + 64;
+    for (auto& a : adm) tot += staged(a.second.first);
+    if (tot > v.h_stage_cap) {
+        if (v.h_stage) cudaFreeHost(v.h_stage);
+        v.h_stage = nullptr;
+        v.h_stage_cap = 0;
+        if (!cuda_ok(c, cudaMallocHost((void**)&v.h_stage, tot * 2), "cudaMallocHost")) return PACC_OOM;
+        v.h_stage_cap = tot * 2;
     }
-    char* hs = nullptr;
-    if (!cuda_ok(c, cudaMallocHost((void**)&hs, tot), "cudaMallocHost")) return PACC_OOM;
+    char* hs = v.h_stage;
     size_t off = 0;
     for (auto& a : adm) {
         const int slot = a.first;
@@ -900,6 +975,10 @@ static int server_admit(pacc_ctx* c) {
         H.codes_t_off = H.topo_off + (int64_t)v.o_codes;
         H.codes_off = H.codes_t_off;
         H.tg_off = 0;
+        H.GGu = E.GGu;
+        H.pcodes_off = H.topo_off + (int64_t)v.o_pcodes;
+        H.pw_off = H.topo_off + (int64_t)v.o_pw;
+        H.pof_off = H.topo_off + (int64_t)v.o_pof;
         char* p0 = hs + off;
         std::memcpy(p0, E.topo.data(), E.topo.size() * 2);
         std::memcpy(p0 + ((E.topo.size() * 2 + 15) & ~(size_t)15), E.dist2.data(), N * 8);
@@ -907,7 +986,13 @@ static int server_admit(pacc_ctx* c) {
         std::memcpy(p1, E.prefix.data(), E.prefix.size() * 4);
         char* p2 = p1 + E.prefix.size() * 4;
         std::memcpy(p2, E.codes_t.data(), E.codes_t.size());
-        char* p3 = p2 + E.codes_t.size();
+        char* p5 = p2 + E.codes_t.size();
+        std::memcpy(p5, E.pcodes_t.data(), E.pcodes_t.size());
+        char* p6 = p5 + E.pcodes_t.size();
+        std::memcpy(p6, E.pw.data(), E.pw.size() * 4);
+        char* p7 = p6 + E.pw.size() * 4;
+        std::memcpy(p7, E.pattern_of.data(), E.pattern_of.size() * 4);
+        char* p3 = p7 + E.pattern_of.size() * 4;
         std::memcpy(p3, &H, sizeof(H));
         SlotState S0;
         std::memset(&S0, 0, sizeof(S0));
@@ -918,49 +1003,34 @@ static int server_admit(pacc_ctx* c) {
         bool ok = cuda_ok(c, cudaMemcpyAsync(reg, p0, v.tb, cudaMemcpyHostToDevice, st), "H2D topo") &&
                   cuda_ok(c, cudaMemcpyAsync(reg + v.o_prefix, p1, E.prefix.size() * 4, cudaMemcpyHostToDevice, st), "H2D prefix") &&
                   cuda_ok(c, cudaMemcpyAsync(reg + v.o_codes, p2, E.codes_t.size(), cudaMemcpyHostToDevice, st), "H2D codes") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_pcodes, p5, E.pcodes_t.size(), cudaMemcpyHostToDevice, st), "H2D patterns") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_pw, p6, E.pw.size() * 4, cudaMemcpyHostToDevice, st), "H2D weights") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_pof, p7, E.pattern_of.size() * 4, cudaMemcpyHostToDevice, st), "H2D pattern map") &&
                   cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, p3, sizeof(H), cudaMemcpyHostToDevice, st), "H2D header") &&
                   cuda_ok(c, cudaMemcpyAsync(v.d_slots + slot, p4, sizeof(S0), cudaMemcpyHostToDevice, st), "H2D slot") &&
                   cuda_ok(c, cudaMemsetAsync(v.d_res + slot, 0, sizeof(DevResult), st), "memset result");
-        if (!ok) { cudaFreeHost(hs); return PACC_ECUDA; }
-        off += v.tb + E.prefix.size() * 4 + E.codes_t.size() + sizeof(H) + sizeof(S0) + 64;
+        if (!ok) return PACC_ECUDA;
+        off += staged(E);
         v.slot_no[slot] = E.no;
         v.slot_t0[slot] = a.second.second;
         v.resident++;
     }
     cudaError_t e = cudaStreamSynchronize(st);
-    cudaFreeHost(hs);
     return cuda_ok(c, e, "admission") ? PACC_OK : PACC_ECUDA;
 }
 
 // One sweep step over the resident chains; finished chains become results.
-static int server_step(pacc_ctx* c) {
+// Retires the sweep in flight, if any: waits for it, copies the finished
+// chains' results back and frees their slots.
+static int server_retire(pacc_ctx* c) {
     Server& v = c->srv;
-    cudaSetDevice(c->device);
-    if (!ensure_model(c)) return PACC_ECUDA;
+    if (!v.inflight) return PACC_OK;
+    v.inflight = false;
     const int N = c->M.N;
-    int st0 = server_admit(c);
-    if (st0 != PACC_OK) return st0;
-    if (v.resident == 0) return PACC_OK;
     cudaStream_t st = c->stream;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
-    cudaError_t e;
-    if (v.gexec) e = cudaGraphLaunch(v.gexec, st);
-    else {
-        e = cudaMemsetAsync(v.d_ctr, 0, 256, st);
-        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, v.C, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * v.n_slots, cudaMemcpyDeviceToHost, st);
-    }
-    cudaEventRecord(e1, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (!cuda_ok(c, e, "sweep step")) return PACC_ECUDA;
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "sweep step")) return PACC_ECUDA;
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    cudaEventElapsedTime(&ms, v.ev0, v.ev1);
     v.kernel_ms += ms;
     v.steps++;
     const int nd = v.h_done[0];
@@ -1025,6 +1095,35 @@ static int server_step(pacc_ctx* c) {
     return PACC_OK;
 }
 
+// One serving step: retire the previous sweep, admit queued elements into the
+// free slots, and launch the next sweep (the graph: queue reset, batched
+// kernel, copy of the finished-slot list) without waiting for it, so that the
+// caller's work until the next step overlaps the device's.
+static int server_step(pacc_ctx* c) {
+    Server& v = c->srv;
+    cudaSetDevice(c->device);
+    int st0 = server_retire(c);
+    if (st0 != PACC_OK) return st0;
+    if (!ensure_model(c)) return PACC_ECUDA;
+    st0 = server_admit(c);
+    if (st0 != PACC_OK) return st0;
+    if (v.resident == 0) return PACC_OK;
+    cudaStream_t st = c->stream;
+    cudaEventRecord(v.ev0, st);
+    cudaError_t e;
+    if (v.gexec) e = cudaGraphLaunch(v.gexec, st);
+    else {
+        e = cudaMemsetAsync(v.d_ctr, 0, 256, st);
+        if (e == cudaSuccess) e = launch_batch(&v.p, v.grid, v.warps, v.smem, v.prec, v.C, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done, v.d_ctr, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v.h_done + 1, v.d_done, sizeof(int) * v.n_slots, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(v.ev1, st);
+    if (!cuda_ok(c, e, "sweep launch")) return PACC_ECUDA;
+    v.inflight = true;
+    return PACC_OK;
+}
+
 int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
     if (!c || !b || b->n_elements < 0) return PACC_EINVAL;
     const int n = b->n_elements;
@@ -1056,7 +1155,12 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
         int st = server_setup(c, gmax);
         if (st != PACC_OK) { c->pending.resize(base); return st; }
         const double t = now_ms();
-        for (size_t i = base; i < c->pending.size(); i++) {
+        // within one submitted batch the longest elements are admitted first
+        std::vector<size_t> ord;
+        for (size_t i = base; i < c->pending.size(); i++) ord.push_back(i);
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](size_t a, size_t b) { return c->pending[a].GG > c->pending[b].GG; });
+        for (size_t i : ord) {
             HostElem& E = c->pending[i];
             if (E.filtered) {
                 pacc_ctx::Done d;
@@ -1129,7 +1233,7 @@ static void collect_results(pacc_ctx* c, const std::vector<DevResult>& res, cons
 }
 
 static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<uint8_t>& blob, size_t off,
-                       int n_int_max, int GGp_max);
+                       int n_int_max, int GGuP_max);
 
 static int run_pending(pacc_ctx* c) {
     if (c->pending.empty()) return PACC_OK;
@@ -1138,14 +1242,14 @@ static int run_pending(pacc_ctx* c) {
     if (!ensure_model(c)) return PACC_ECUDA;
     const int N = c->M.N, S = c->M.S;
     const int n = (int)c->pending.size();
-    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_PLAIN) ? 1 : 0;
     const int T = c->o.burnin + c->o.mcmc;
     const int TI = std::min(c->o.trace_iters, T);
     // pack the blob
     std::vector<ElemHeader> hdr(n);
     size_t off = 0;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    int n_int_max = 1, GGp_max = 32;
+    int n_int_max = 1, GGp_max = 32, GGuP_max = 32;
     const size_t tb = topo_bytes(N);
     for (int e = 0; e < n; e++) {
         HostElem& E = c->pending[e];
@@ -1163,7 +1267,12 @@ static int run_pending(pacc_ctx* c) {
         H.tg_off = off; off = al(off + E.tg0.size());
         H.prefix_off = off; off = al(off + E.prefix.size() * 4);
         H.topo_off = off; off = al(off + tb);
+        H.GGu = E.GGu;
+        H.pcodes_off = off; off = al(off + E.pcodes_t.size());
+        H.pw_off = off; off = al(off + E.pw.size() * 4);
+        H.pof_off = off; off = al(off + E.pattern_of.size() * 4);
         n_int_max = std::max(n_int_max, E.n_int);
+        GGuP_max = std::max(GGuP_max, (E.GGu + 31) & ~31);
         GGp_max = std::max(GGp_max, E.GGp);
     }
     std::vector<uint8_t> blob(off);
@@ -1177,8 +1286,11 @@ static int run_pending(pacc_ctx* c) {
         std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
         std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
         std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
+        std::memcpy(&blob[H.pcodes_off], E.pcodes_t.data(), E.pcodes_t.size());
+        std::memcpy(&blob[H.pw_off], E.pw.data(), E.pw.size() * 4);
+        std::memcpy(&blob[H.pof_off], E.pattern_of.data(), E.pattern_of.size() * 4);
     }
-    if (c->o.precision != PACC_FP64) return run_batched(c, hdr, blob, off, n_int_max, GGp_max);
+    if (batched_layout(c)) return run_batched(c, hdr, blob, off, n_int_max, GGuP_max);
     // launch geometry
     int BT = c->o.block_threads > 0 ? c->o.block_threads : 128;
     size_t smem = smem_bytes(N, BT, prec);
@@ -1195,22 +1307,31 @@ static int run_pending(pacc_ctx* c) {
     size_t o_trz = al(o_trd + sizeof(double) * 3 * 6 * (size_t)TI * n);
     size_t o_cnt = al(o_trz + (size_t)3 * TI * N * n);
     size_t o_next = al(o_cnt + sizeof(DevCounters));
-    size_t misc = al(o_next + 256);
+    size_t o_order = al(o_next + 256);
+    size_t misc = al(o_order + sizeof(int32_t) * n);
     if (!grow(c, &c->d_blob, &c->blob_cap, std::max<size_t>(off, 256)) ||
         !grow(c, &c->d_ws, &c->ws_cap, ws1 * grid) || !grow(c, &c->d_misc, &c->misc_cap, misc))
         return PACC_OOM;
+    // CTAs claim the longest elements first, so that the last chains to start are short
+    std::vector<int32_t> order(n);
+    for (int e = 0; e < n; e++) order[e] = e;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return c->pending[a].GG > c->pending[b].GG; });
     char* mb = (char*)c->d_misc;
     cudaStream_t st = c->stream;
     if (!cuda_ok(c, cudaMemcpyAsync(c->d_blob, blob.data(), off, cudaMemcpyHostToDevice, st), "H2D blob") ||
         !cuda_ok(c, cudaMemcpyAsync(mb + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st),
                  "H2D hdr") ||
-        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_next + 256 - o_res, st), "memset"))
+        !cuda_ok(c, cudaMemsetAsync(mb + o_res, 0, o_next + 256 - o_res, st), "memset") ||
+        !cuda_ok(c, cudaMemcpyAsync(mb + o_order, order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
+                 "H2D order"))
         return PACC_ECUDA;
     ChainParams p;
     p.hdr = (const ElemHeader*)(mb + o_hdr);
     p.blob = (const uint8_t*)c->d_blob;
     p.n_elem = n;
     p.next_elem = (int*)(mb + o_next);
+    p.order = (const int32_t*)(mb + o_order);
     p.results = (DevResult*)(mb + o_res);
     p.max_z = (int32_t*)(mb + o_mz);
     p.post_z = (double*)(mb + o_pz);
@@ -1270,8 +1391,7 @@ static int run_pending(pacc_ctx* c) {
 // memory (pacc_batch.cu).  Every admitted element gets a slot; warps claim
 // slots from a queue and run each chain to completion.
 static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<uint8_t>& blob, size_t off,
-                       int n_int_max, int GGp_max) {
-    (void)GGp_max;
+                       int n_int_max, int GGuP_max) {
     const int N = c->M.N, S = c->M.S;
     const int n = (int)c->pending.size();
     const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
@@ -1294,7 +1414,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
         int warps_max = 0;
         for (int Cc : cands) {
             BatchGeom g;
-            if (!batch_geom(c, prec, Cc, n_int_max, D, n_slots, g)) continue;
+            if (!batch_geom(c, prec, Cc, n_int_max, D, n_slots, GGuP_max, g)) continue;
             grp_max = std::max(grp_max, g.grp_b);
             warps_max = std::max(warps_max, g.grid * g.warps);
         }
@@ -1347,15 +1467,16 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     p.n_int_max = n_int_max;
     p.S_max = S;
     p.stack_depth = D;
+    p.GGuP_max = GGuP_max;
     // column count: the caller's, the tuned one for this tree and precision,
     // or tuned now on a sample of this batch
     int C = 0;
     {
-        int st_t = tune_columns(c, prec, D, n_int_max, elem, p, mb + o_elem, mb + o_next, C);
+        int st_t = tune_columns(c, prec, D, n_int_max, GGuP_max, elem, p, mb + o_elem, mb + o_next, C);
         if (st_t != PACC_OK) return st_t;
     }
     BatchGeom g;
-    batch_geom(c, prec, C, n_int_max, D, n_slots, g);
+    batch_geom(c, prec, C, n_int_max, D, n_slots, GGuP_max, g);
     const int warps = g.warps, grid = g.grid;
     const size_t smem = g.smem;
     if (!cuda_ok(c, cudaMemcpyAsync(mb + o_elem, elem.data(), sizeof(int32_t) * elem.size(), cudaMemcpyHostToDevice, st), "H2D elem") ||
@@ -1421,7 +1542,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
 int pacc_sync(pacc_ctx* c) {
     if (!c) return PACC_EINVAL;
     if (serving(c)) {
-        while (!c->srv.queue.empty() || c->srv.resident > 0) {
+        while (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight) {
             int st = server_step(c);
             if (st != PACC_OK) return st;
         }
@@ -1465,7 +1586,8 @@ static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
 
 int pacc_poll(pacc_ctx* c, pacc_result* out, int max) {
     if (!c || (!out && max > 0)) return -PACC_EINVAL;
-    if (serving(c) && c->done_head == c->done.size() && (!c->srv.queue.empty() || c->srv.resident > 0)) {
+    if (serving(c) && c->done_head == c->done.size() &&
+        (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight)) {
         int st = server_step(c);
         if (st != PACC_OK) return -st;
     }
@@ -1508,6 +1630,7 @@ int pacc_run(pacc_ctx* c, const pacc_element_batch* b, pacc_result* out) {
 int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
     if (!c || !out) return PACC_EINVAL;
     if (serving(c) && c->srv.ready) {
+        if (c->srv.inflight) cudaStreamSynchronize(c->stream);
         DevCounters dc;
         if (cudaMemcpy(&dc, c->srv.d_cnt, sizeof(dc), cudaMemcpyDeviceToHost) != cudaSuccess) return PACC_ECUDA;
         pacc_counters& pc = c->counters;
@@ -1590,6 +1713,19 @@ int pacc_debug_encode(pacc_ctx* c, const uint8_t* bases, int32_t length, int8_t*
     return PACC_OK;
 }
 
+int pacc_debug_patterns(pacc_ctx* c, const uint8_t* bases, int32_t length, int32_t* pattern_of, int32_t* weights,
+                        int32_t* n_cols, int32_t* n_patterns) {
+    if (!c || !bases || !pattern_of || !weights || !n_cols || !n_patterns) return PACC_EINVAL;
+    HostElem E;
+    if (!preprocess(c->M, c->o, bases, length, E, false)) return PACC_EINVAL;
+    if (E.filtered) { *n_cols = 0; *n_patterns = 0; return PACC_FILTERED; }
+    *n_cols = E.GG;
+    *n_patterns = E.GGu;
+    std::memcpy(pattern_of, E.pattern_of.data(), sizeof(int32_t) * E.GG);
+    std::memcpy(weights, E.pw.data(), sizeof(int32_t) * E.GGu);
+    return PACC_OK;
+}
+
 int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const int32_t* z, double c_rate,
                       double n_rate, double* out, int32_t* n_cols) {
     if (!c) return PACC_EINVAL;
@@ -1600,7 +1736,7 @@ int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const i
     if (!preprocess(c->M, c->o, bases, length, E, false)) return PACC_EINVAL;
     if (E.filtered) { *n_cols = 0; return PACC_FILTERED; }
     const int N = c->M.N;
-    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_PLAIN) ? 1 : 0;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     ElemHeader H;
     std::memset(&H, 0, sizeof(H));

@@ -21,6 +21,17 @@
 
 namespace pacc {
 
+// Out-of-line math: the chain's scalar code calls these from many places, and
+// one copy of each library routine (instead of one inlined per call site)
+// keeps the kernels small enough for the instruction caches.  The values are
+// those of the library functions they wrap.
+static __device__ __noinline__ double d_log(double x) { return log(x); }
+static __device__ __noinline__ double d_exp(double x) { return exp(x); }
+static __device__ __noinline__ double d_pow(double x, double y) { return pow(x, y); }
+static __device__ __noinline__ double d_lgamma(double x) { return lgamma(x); }
+static __device__ __noinline__ double d_cos(double x) { return cos(x); }
+static __device__ __noinline__ float f_log(float x) { return logf(x); }
+
 __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
                                               uint32_t k1, uint32_t out[4]) {
 #pragma unroll
@@ -59,13 +70,13 @@ struct StreamReader {
     __device__ __noinline__ double normal() {
         double u1 = uniform();
         double u2 = uniform();
-        return __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, log(u1))), cos(__dmul_rn(6.283185307179586, u2)));
+        return __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, d_log(u1))), d_cos(__dmul_rn(6.283185307179586, u2)));
     }
     __device__ __noinline__ double gamma(double a, double b) {
         if (a < 1.0) {
             double g = gamma_ge1(__dadd_rn(a, 1.0), 1.0);
             double u = uniform();
-            return __dmul_rn(__dmul_rn(b, g), pow(u, __ddiv_rn(1.0, a)));
+            return __dmul_rn(__dmul_rn(b, g), d_pow(u, __ddiv_rn(1.0, a)));
         }
         return gamma_ge1(a, b);
     }
@@ -83,7 +94,7 @@ struct StreamReader {
             double u = uniform();
             double x2 = __dmul_rn(x, x);
             if (u < __dsub_rn(1.0, __dmul_rn(__dmul_rn(0.0331, x2), x2))) break;
-            if (log(u) < __dadd_rn(__dmul_rn(0.5, x2), __dmul_rn(d, __dadd_rn(__dsub_rn(1.0, v), log(v))))) break;
+            if (d_log(u) < __dadd_rn(__dmul_rn(0.5, x2), __dmul_rn(d, __dadd_rn(__dsub_rn(1.0, v), d_log(v))))) break;
         }
         return __dmul_rn(__dmul_rn(b, d), v);
     }

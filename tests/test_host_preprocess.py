@@ -99,3 +99,44 @@ def test_run_without_gpu_fails_loudly(built):
     ctx = pg.Context(ds, abi.default_opts())
     with pytest.raises(pg.PaccError):
         ctx.run()
+
+
+def _patterns_numpy(blk, gapchar=ord("-")):
+    """Site patterns restated: encoded columns, distinct ones numbered in order
+    of first occurrence, with their column counts."""
+    lut = np.full(256, 5, dtype=np.uint8)
+    for i, ch in enumerate(b"acgt"):
+        lut[ch] = i
+    for i, ch in enumerate(b"rykmsw"):
+        lut[ch] = 6 + i
+    lut[gapchar] = 4
+    codes = lut[np.asarray(blk, dtype=np.uint8)]
+    ids, of, weights = {}, [], []
+    for col in codes.T:
+        key = col.tobytes()
+        if key not in ids:
+            ids[key] = len(ids)
+            weights.append(0)
+        of.append(ids[key])
+        weights[ids[key]] += 1
+    return np.array(of, dtype=np.int32), np.array(weights, dtype=np.int32)
+
+
+@pytest.mark.parametrize("kind", ["edge", "st43"])
+def test_site_patterns_bit_exact(kind):
+    ds = _edge_dataset(3) if kind == "edge" else synth.make_dataset("st43", n_elements=20, seed=4)
+    if kind == "edge":
+        blk = ds.element(8)
+        blk[:, 1::2] = blk[:, 0:1]        # many repeated columns
+    ctx = pg.Context(ds, abi.default_opts())
+    n_checked = 0
+    for e in range(ds.n_elements):
+        of, wt = ctx.patterns(e)
+        if len(of) == 0:
+            continue                      # filtered
+        ref_of, ref_wt = _patterns_numpy(ds.element(e))
+        assert np.array_equal(of, ref_of), e
+        assert np.array_equal(wt, ref_wt), e
+        assert wt.sum() == len(of)
+        n_checked += 1
+    assert n_checked >= 5
