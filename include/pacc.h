@@ -50,11 +50,11 @@ typedef enum pacc_status {
 } pacc_status;
 
 typedef enum pacc_precision {
-    PACC_FP64 = 0,              /* plain path: one CTA per element, FP64 partials, partial re-pruning */
-    PACC_FP32 = 1,              /* batched path: one warp per element, FP32 partials with power-of-two
-                                   rescaling, FP64 log-likelihood sums and chain arithmetic */
-    PACC_FP64_BATCHED = 2,      /* the batched layout with FP64 partials (checks the layout draw for draw) */
-    PACC_FP32_PLAIN = 3         /* the plain layout (one CTA per element) with FP32 partials */
+    PACC_FP64 = 0,              /* plain path: one CTA per element chain, FP64 partials, partial re-pruning */
+    PACC_FP32 = 1,              /* the same layout with FP32 partials (power-of-two rescaling, integer
+                                   exponents), FP64 log-likelihood sums and chain arithmetic */
+    PACC_FP64_BATCHED = 2,      /* warp-per-chain layout with FP64 partials (checks it draw for draw) */
+    PACC_FP32_WARP = 3          /* warp-per-chain layout with FP32 partials */
 } pacc_precision;
 
 /* Tree, rate matrix and species sets: the content of the .mod file plus the

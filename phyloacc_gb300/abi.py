@@ -23,7 +23,7 @@ PACC_EUNSUPPORTED = 9
 PACC_FP64 = 0
 PACC_FP32 = 1
 PACC_FP64_BATCHED = 2
-PACC_FP32_PLAIN = 3
+PACC_FP32_WARP = 3
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)

@@ -30,10 +30,16 @@
 
 namespace pacc {
 
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
 
 // Workspace carve-up (per CTA).
 struct WsLayout {
-    size_t lam, scale, tg, trz, trd, hash, rep, cfg, nxt, head, first, cstat, total;
+    size_t lam, scale, tg, trz, trd, hash, rep, cfg, nxt, head, first, cstat, codes, prefix, total;
     __host__ __device__ static WsLayout make(int n_int, int GGp, int T, int mcmc, int N, int real_bytes) {
         WsLayout w;
         size_t o = 0;
@@ -50,6 +56,8 @@ struct WsLayout {
         w.head = o; o = al(o + (size_t)(mcmc + 2) * 4);
         w.first = o; o = al(o + (size_t)(mcmc + 2) * 4);
         w.cstat = o; o = al(o + (size_t)9 * (mcmc + 2) * 8);
+        w.codes = o; o = al(o + (size_t)N * GGp);          // stream mode: the element's codes [S][GGp]
+        w.prefix = o; o = al(o + (size_t)(GGp + 1) * 4);   // stream mode: its draw prefix
         w.total = o;
         return w;
     }
@@ -231,7 +239,7 @@ __device__ __forceinline__ int mat_class(int z, int prop_class) {
 // buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928).  Returns the summed
 // per-column log-likelihood at the root (valid when the root is flagged).
 template <typename Real>
-__device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
+__device__ __noinline__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
     const int BT = blockDim.x;
     double ll_sum = 0;
     unsigned long long e_int = 0, e_leaf = 0;
@@ -310,7 +318,7 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
 #pragma unroll
                 for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
                 double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
-                ll_sum += log(t) + (double)sc * 0.6931471805599453;
+                ll_sum += d_log(t) + (double)sc * 0.6931471805599453;
             }
 #pragma unroll
             for (int j = 0; j < 4; j++) Ld[j * c.GGp + g] = a[j];
@@ -331,7 +339,7 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
 // (bpp_c.cpp:887-902) and the Eval2 fallback (bpp_c2.cpp:220-237) apply the
 // eigen formula whatever the branch length.
 template <typename Real>
-__device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
+__device__ __noinline__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
         int s = c.nodes[i];
         double* out = c.ptd + ((size_t)k * c.N + s) * 16;
@@ -370,23 +378,30 @@ __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool i
         int s = c.nodes[i];
         double* t = c.ltm + (size_t)s * 9;   // t[zc*3 + zp]
         if (c.fixZ[s] == 1) {
-            if (init) t[0 * 3 + 1] = NI;
+            if (init) {
+                t[0 * 3 + 1] = NI;
+                // parent state 2 never occurs above a fixed node; the
+                // reference's matrix keeps its initial zeros there
+                t[0 * 3 + 2] = 0;
+                t[1 * 3 + 2] = 0;
+                t[2 * 3 + 2] = 0;
+            }
             t[1 * 3 + 1] = 0;
             t[2 * 3 + 1] = NI;
-            t[0 * 3 + 0] = log(1 - gr);
-            t[1 * 3 + 0] = log(gr);
+            t[0 * 3 + 0] = d_log(1 - gr);
+            t[1 * 3 + 0] = d_log(gr);
             t[2 * 3 + 0] = NI;
         } else {
-            t[0 * 3 + 0] = log(1 - gr);
-            t[1 * 3 + 0] = log(gr);
+            t[0 * 3 + 0] = d_log(1 - gr);
+            t[1 * 3 + 0] = d_log(gr);
             t[2 * 3 + 0] = NI;
             double y = 1 - lr;
             if (init) t[0 * 3 + 1] = NI;
-            t[1 * 3 + 1] = log(y);
-            t[2 * 3 + 1] = log(1 - y);
+            t[1 * 3 + 1] = d_log(y);
+            t[2 * 3 + 1] = d_log(1 - y);
             if (init) t[0 * 3 + 2] = NI;
-            t[1 * 3 + 2] = log(lr2);
-            t[2 * 3 + 2] = log(1 - lr2);
+            t[1 * 3 + 2] = d_log(lr2);
+            t[2 * 3 + 2] = d_log(1 - lr2);
         }
     }
 }
@@ -394,7 +409,7 @@ __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool i
 // Internal-base sampling, top-down per column (Update_Tg with tosample,
 // bpp_c.cpp:672-733).  Column g takes its words at pos + prefix[g].
 template <typename Real>
-__device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
+__device__ __noinline__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
     int err = 0;
     const int rir = c.irank[c.root];
     const int rbuf = c.cur[c.root];
@@ -444,7 +459,7 @@ __device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
 // Emission sums per branch and class (getEmission, bpp_c2.cpp:355-390) from a
 // histogram of (child symbol, parent base) pairs.
 template <typename Real>
-__device__ void emission(Ctx<Real>& c) {
+__device__ __noinline__ void emission(Ctx<Real>& c) {
     const int NB = NSYM * 4;
     for (int i = threadIdx.x; i < c.N * NB; i += blockDim.x) c.cnt[i] = 0;
     __syncthreads();
@@ -492,13 +507,13 @@ __device__ void emission(Ctx<Real>& c) {
             if (!n) continue;
             int sym = b >> 2, tp = b & 3;
             double v;
-            if (sym < 4) v = log(P[sym * 4 + tp]);
+            if (sym < 4) v = d_log(P[sym * 4 + tp]);
             else {
                 int msk = ambig_mask(sym - 4);
                 double t = 0;
                 for (int q = 0; q < 4; q++)
                     if (msk & (1 << q)) t += P[q * 4 + tp];
-                v = log(t);
+                v = d_log(t);
             }
             e += (double)n * v;
         }
@@ -515,13 +530,13 @@ __device__ __forceinline__ double msg(const double* ltm, const double* beta, int
     double mx = t0;
     if (t1 > mx) mx = t1;
     if (t2 > mx) mx = t2;
-    double sm = exp(t0 - mx) + exp(t1 - mx) + exp(t2 - mx);
-    return log(sm) + mx;
+    double sm = d_exp(t0 - mx) + d_exp(t1 - mx) + d_exp(t2 - mx);
+    return d_log(sm) + mx;
 }
 
 // Forward filter / backward sample of Z (Update_Z_subtree, bpp_c.cpp:1182-1293).
 template <typename Real>
-__device__ int update_z(Ctx<Real>& c, uint64_t pos) {
+__device__ __noinline__ int update_z(Ctx<Real>& c, uint64_t pos) {
     const double NI = -CUDART_INF;
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         int s = c.nodes[i];
@@ -544,13 +559,13 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
     }
     int err = 0;
     if (threadIdx.x == 0) {
-        const double prior_z[3] = {log(0.5), log(0.5), NI};
+        const double prior_z[3] = {d_log(0.5), d_log(0.5), NI};
         double lp[3], pr[3];
         for (int k = 0; k < 3; k++) lp[k] = c.beta[c.root * 3 + k] + prior_z[k];
         double mx = lp[0];
         if (lp[1] > mx) mx = lp[1];
         if (lp[2] > mx) mx = lp[2];
-        for (int k = 0; k < 3; k++) pr[k] = exp(lp[k] - mx);
+        for (int k = 0; k < 3; k++) pr[k] = d_exp(lp[k] - mx);
         uint32_t wd[4];
         philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
         int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
@@ -569,7 +584,7 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
             double mx = lt[0];
             if (lt[1] > mx) mx = lt[1];
             if (lt[2] > mx) mx = lt[2];
-            for (int k = 0; k < 3; k++) pr[k] = exp(lt[k] - mx);
+            for (int k = 0; k < 3; k++) pr[k] = d_exp(lt[k] - mx);
             uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
             uint32_t wd[4];
             philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
@@ -586,7 +601,7 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
 
 // Flags of proper ancestors of flagged nodes (getUpdateNode, bpp_c.cpp:620-642).
 template <typename Real>
-__device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int mode, int* tmp) {
+__device__ __noinline__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int mode, int* tmp) {
     // mode 0: src = changed flags; mode 1: Z == 2 (non-missing); mode 2: Z == 1 (non-missing)
     for (int i = threadIdx.x; i < c.N; i += blockDim.x) dst[i] = 0;
     __syncthreads();
@@ -608,7 +623,7 @@ __device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int
 // One Metropolis-Hastings update of the accelerated (neut) or conserved rate
 // (sample_rate, bpp_c.cpp:930-1176), M = 1, adaptive factor 0.5.
 template <typename Real>
-__device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
+__device__ __noinline__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
     ChainScalars* cs = c.cs;
     const int8_t* unv = neut ? c.unvN : c.unvC;
     const int cls = neut ? P_NEUT : P_CONS;
@@ -690,9 +705,9 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
                     MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
                                                                log_gamma_pdf(proposal, prior_a, prior_b)),
                                                      log_gamma_pdf(cur, prior_a, prior_b)),
-                                           log(cur)),
-                                   log(proposal));
-                if (log(r) < MH) {
+                                           d_log(cur)),
+                                   d_log(proposal));
+                if (d_log(r) < MH) {
                     cs->accept = 1;
                     cs->loglik = ll_new;
                 }
@@ -722,18 +737,18 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
         double scale_adj;
         if (neut) {
             double rate = (double)cs->acc_n / dM.adapt_freq;
-            if (rate > 0.44) scale_adj = exp(step);
-            else if (rate < 0.23) scale_adj = exp(-step);
+            if (rate > 0.44) scale_adj = d_exp(step);
+            else if (rate < 0.23) scale_adj = d_exp(-step);
             else scale_adj = 1;
             cs->prop_n = __dmul_rn(cs->prop_n, scale_adj);
             if (cs->prop_n > 1) cs->prop_n = 1;
             cs->acc_n = 0;
         } else {
             double rate = (double)cs->acc_c / dM.adapt_freq;
-            if (rate > 0.44) scale_adj = exp(step);
-            else if (rate < 0.23) scale_adj = exp(-step);
+            if (rate > 0.44) scale_adj = d_exp(step);
+            else if (rate < 0.23) scale_adj = d_exp(-step);
             else scale_adj = 1;
-            cs->prop_c = pow(cs->prop_c, scale_adj);
+            cs->prop_c = d_pow(cs->prop_c, scale_adj);
             if (cs->prop_c < 1.0001) cs->prop_c = 1.0001;
             cs->acc_c = 0;
         }
@@ -743,7 +758,7 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
 }
 
 // Rank selection: the element that std::sort would put at index T/2 (bpp_c2.cpp:742-755).
-__device__ double median_of(const double* x, int T, double* red) {
+__device__ __noinline__ double median_of(const double* x, int T, double* red) {
     int target = T / 2;
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += blockDim.x) {
@@ -766,7 +781,7 @@ __device__ double median_of(const double* x, int T, double* red) {
 
 // Prior of a Z configuration (bpp_c2.cpp:131-163): Beta-Binomial terms + root prior.
 template <typename Real>
-__device__ double prior_config(Ctx<Real>& c, const int8_t* z) {
+__device__ __noinline__ double prior_config(Ctx<Real>& c, const int8_t* z) {
     double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int k = 0; k + 1 < c.n_nodes; k++) {
         int s = c.nodes[k];
@@ -779,13 +794,13 @@ __device__ double prior_config(Ctx<Real>& c, const int8_t* z) {
     }
     pz += lnbeta(dM.la + nZ[2][1], dM.lb + nZ[1][1]) - lnbeta(dM.la, dM.lb);
     if (dM.l2a > 0) pz += lnbeta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]) - lnbeta(dM.l2a, dM.l2b);
-    pz += (z[c.root] == 2) ? -CUDART_INF : log(0.5);
+    pz += (z[c.root] == 2) ? -CUDART_INF : d_log(0.5);
     return pz;
 }
 
 // Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353).
 template <typename Real>
-__device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, int* n_conf_out) {
+__device__ __noinline__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, int* n_conf_out) {
     ChainScalars* cs = c.cs;
     const int burn = c.burn, mcmc = c.mcmc, T = c.T;
     int8_t* Zm = c.maxz;  // Max_Z
@@ -889,12 +904,12 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
         double nj = CNT[j];
         double ld;
         if (resZ == 0) {
-            ld = __dsub_rn(log(__dsub_rn(VC[j], __ddiv_rn(__dmul_rn(MC[j], MC[j]), nj))), log(nj));
+            ld = __dsub_rn(d_log(__dsub_rn(VC[j], __ddiv_rn(__dmul_rn(MC[j], MC[j]), nj))), d_log(nj));
         } else {
             double vc = __dsub_rn(VC[j], __ddiv_rn(__dmul_rn(MC[j], MC[j]), nj));
             double vn = __dsub_rn(VN[j], __ddiv_rn(__dmul_rn(MN[j], MN[j]), nj));
             double cov = __dsub_rn(CV[j], __ddiv_rn(__dmul_rn(MN[j], MC[j]), nj));
-            ld = __dsub_rn(log(__dsub_rn(__dmul_rn(vc, vn), __dmul_rn(cov, cov))), __dmul_rn(2.0, log(nj)));
+            ld = __dsub_rn(d_log(__dsub_rn(__dmul_rn(vc, vn), __dmul_rn(cov, cov))), __dmul_rn(2.0, d_log(nj)));
         }
         LD[j] = ld;
     }
@@ -907,7 +922,7 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
             if (w < 0.02) continue;
             if (isnan(LD[j])) continue;
             eff += (int)CNT[j];
-            VB = __dsub_rn(VB, __dmul_rn(w, log(CNT[j])));
+            VB = __dsub_rn(VB, __dmul_rn(w, d_log(CNT[j])));
             VB = __dadd_rn(VB, SF[j]);
             VB = __dadd_rn(VB, __ddiv_rn(__dmul_rn(__dmul_rn(0.5, LD[j]), CNT[j]), (double)mcmc));
         }
@@ -948,22 +963,22 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
             if (mx == -CUDART_INF) v = -CUDART_INF;
             else {
                 double sm = 0;
-                for (int j = 0; j < nconf; j++) sm += exp(SF[j] - mx);
-                v = log(sm) + mx;
+                for (int j = 0; j < nconf; j++) sm += d_exp(SF[j] - mx);
+                v = d_log(sm) + mx;
             }
             v += log_gamma_pdf(rc, dM.cprior_a, dM.cprior_b);
             if (resZ != 0) v += log_gamma_pdf(rn, dM.nprior_a, dM.nprior_b);
             double logdet;
             if (resZ == 0) {
                 varc -= meanc * meanc / mcmc;
-                logdet = log(varc) - log((double)mcmc);
-                v += 0.5 * logdet + 0.5 * log(2 * CUDART_PI);
+                logdet = d_log(varc) - d_log((double)mcmc);
+                v += 0.5 * logdet + 0.5 * d_log(2 * CUDART_PI);
             } else {
                 varn -= meann * meann / mcmc;
                 varc -= meanc * meanc / mcmc;
                 cov -= meann * meanc / mcmc;
-                logdet = log(varc * varn - cov * cov) - 2 * log((double)mcmc);
-                v += 0.5 * logdet + log(2 * CUDART_PI);
+                logdet = d_log(varc * varn - cov * cov) - 2 * d_log((double)mcmc);
+                v += 0.5 * logdet + d_log(2 * CUDART_PI);
             }
             cs->vb = v;
         }
@@ -971,8 +986,8 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
         VB = cs->vb;
     } else {
         double f = (double)mcmc / cs->eff;
-        if (resZ != 0) VB = VB * f + log((double)mcmc) + log(2 * CUDART_PI) + 1;
-        else VB = VB * f + log((double)mcmc) + 0.5 * (log(2 * CUDART_PI) + 1);
+        if (resZ != 0) VB = VB * f + d_log((double)mcmc) + d_log(2 * CUDART_PI) + 1;
+        else VB = VB * f + d_log((double)mcmc) + 0.5 * (d_log(2 * CUDART_PI) + 1);
     }
     __syncthreads();
     return VB;
@@ -1034,14 +1049,43 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            const int i = atomicAdd(P.next_elem, 1);
-            elem_ = (i < P.n_elem && P.order) ? P.order[i] : i;
+            if (!P.stream) {
+                const int i = atomicAdd(P.next_elem, 1);
+                elem_ = (i < P.n_elem && P.order) ? P.order[i] : i;
+            } else {
+                // take the next published queue position; give up after idle_ns
+                // without work (the host launches the kernel again when needed)
+                elem_ = P.n_elem;
+                const unsigned long long t0 = globaltimer_ns();
+                for (;;) {
+                    const int h = *(volatile int*)P.q_head;
+                    const int t = *P.q_tail;
+                    if (h < t) {
+                        if (atomicCAS(P.q_head, h, h + 1) == h) {
+                            __threadfence_system();   // the slot id and its data after the tail
+                            elem_ = P.q_slot[h % P.q_cap];
+                            break;
+                        }
+                        continue;
+                    }
+                    if ((long long)(globaltimer_ns() - t0) > P.idle_ns) break;
+                    __nanosleep(4000);
+                }
+            }
         }
         __syncthreads();
         const int e = elem_;
-        if (e >= P.n_elem) break;
+        if (e < 0 || e >= P.n_elem) break;
         long long t_start = clock64();
-        const ElemHeader& H = P.hdr[e];
+        ElemHeader H;
+        if (P.stream) {
+            // the host rewrote this slot while the kernel ran: read it past L1
+            const int* src = (const int*)(P.hdr + e);
+            int* dst = (int*)&H;
+            for (int i = 0; i < (int)(sizeof(ElemHeader) / 4); i++) dst[i] = __ldcg(src + i);
+        } else {
+            H = P.hdr[e];
+        }
         DevResult* R = P.results + e;
         if (H.filtered) {
             if (threadIdx.x == 0) R->status = 1;
@@ -1053,14 +1097,25 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
         c.codes = P.blob + H.codes_off;
         c.prefix = (const int32_t*)(P.blob + H.prefix_off);
         const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
-        for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
-        {
-            const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
+        const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
+        const int8_t* tg0 = (const int8_t*)(P.blob + H.tg_off);
+        if (!P.stream) {
+            for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
             for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = d2[i];
-        }
-        {
-            const int8_t* tg0 = (const int8_t*)(P.blob + H.tg_off);
             for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = tg0[i];
+        } else {
+            // element data of a queue slot: copied past L1 into shared memory
+            // and this CTA's workspace, which the chain then reads
+            for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = __ldcg(topo + i);
+            for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = __ldcg(d2 + i);
+            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = __ldcg(tg0 + i);
+            const int nw = (int)(((size_t)S * c.GGp) / 4);
+            const int* csrc = (const int*)c.codes;
+            int* cdst = (int*)(ws + W.codes);
+            for (int i = threadIdx.x; i < nw; i += BT) cdst[i] = __ldcg(csrc + i);
+            for (int i = threadIdx.x; i <= c.GG; i += BT) ((int32_t*)(ws + W.prefix))[i] = __ldcg(c.prefix + i);
+            c.codes = (const uint8_t*)(ws + W.codes);
+            c.prefix = (const int32_t*)(ws + W.prefix);
         }
         if (threadIdx.x == 0) {
             cs_.pos = 0;
@@ -1107,7 +1162,7 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
             build_ltm(c, c.trd[TR_G * T], c.trd[TR_L * T], c.trd[TR_L2 * T], true);
             for (int i = threadIdx.x; i < N; i += BT) {
                 c.emis[i * 3 + 0] = 0; c.emis[i * 3 + 1] = 0; c.emis[i * 3 + 2] = 0;
-                if (c.missing[i]) { c.emis[i * 3 + 1] = log(dM.cons_to_mis); }
+                if (c.missing[i]) { c.emis[i * 3 + 1] = d_log(dM.cons_to_mis); }
                 c.unv[i] = 1;
             }
             __syncthreads();
@@ -1231,6 +1286,12 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
             R->status = (cs_.status & 1) ? 3 : ((cs_.status & 2) ? 2 : 0);
             R->device_ms = (double)(clock64() - t_start);
         }
+        if (P.stream) {
+            // publish the slot once every thread's result writes are visible
+            __threadfence_system();
+            __syncthreads();
+            if (threadIdx.x == 0) P.done_flag[e] = 1;
+        }
         // counters
         if (P.counters) {
             atomicAdd(&P.counters->edge_internal, c.local.edge_internal);
@@ -1312,7 +1373,7 @@ __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, do
     for (int g = threadIdx.x; g < c.GG; g += BT) {
         Real* Lr = c.L(0, rir, 0);
         double t = (double)Lr[g] + (double)Lr[g + c.GGp] + (double)Lr[g + 2 * c.GGp] + (double)Lr[g + 3 * c.GGp];
-        out[g] = log(t) + (double)c.SC(0, rir)[g] * 0.6931471805599453;
+        out[g] = d_log(t) + (double)c.SC(0, rir)[g] * 0.6931471805599453;
     }
 }
 
@@ -1347,6 +1408,20 @@ size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec) {
 }
 
 size_t topo_bytes(int N) { return (size_t)((TopoLayout::make(N).total * 2 + 15) & ~15) + (size_t)N * 8; }
+
+// Resident CTAs per SM of the chain kernel for this block size and shared memory.
+int chain_occupancy(int prec, int BT, size_t smem) {
+    int nb = 0;
+    cudaError_t e;
+    if (prec == 0) {
+        e = cudaFuncSetAttribute(chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, chain_kernel<double>, BT, smem);
+    } else {
+        e = cudaFuncSetAttribute(chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, chain_kernel<float>, BT, smem);
+    }
+    return e == cudaSuccess ? nb : 0;
+}
 
 cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st) {
     if (prec == 0) {

@@ -145,6 +145,15 @@ struct ChainParams {
     size_t ws_stride;
     int n_int_max, GGp_max;
     DevCounters* counters;
+    // stream mode (serving): CTAs take slots from a queue the host appends to
+    // while the kernel runs; element data and results are indexed by slot.
+    int stream;                      // 0: the n_elem elements of this launch; 1: the queue
+    int* q_head;                     // device: next queue position to take (atomic)
+    const volatile int* q_tail;      // host-mapped: queue positions published so far
+    const volatile int* q_slot;      // host-mapped: slot of queue position i (ring of q_cap)
+    int q_cap;
+    volatile int* done_flag;         // host-mapped, per slot: set to 1 once the slot's results are written
+    long long idle_ns;               // a CTA without work for this long returns
 };
 
 // ---- batched (warp-per-chain) kernel ----

@@ -32,6 +32,7 @@ namespace pacc {
 
 cudaError_t set_model(const DevModel& m, cudaStream_t st);
 size_t smem_bytes(int N, int BT, int prec);
+int chain_occupancy(int prec, int BT, size_t smem);
 size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec);
 size_t topo_bytes(int N);
 cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st);
@@ -422,6 +423,46 @@ struct Server {
     double kernel_ms = 0;
 };
 
+// Serving with the CTA-per-chain kernel: one persistent launch whose CTAs
+// take element slots from a queue in host-mapped memory that the host appends
+// to while the kernel runs, so chains of new requests start as soon as a CTA
+// is free (continuous batching without relaunches).  A CTA that finds no work
+// for a while returns; the host launches again when work arrives.
+struct StreamServer {
+    bool ready = false;
+    int n_slots = 0, grid = 0, BT = 128, prec = 0, GG_cap = 0, GGp_cap = 0, n_int_cap = 0, TI = 0;
+    size_t smem = 0, ws1 = 0, blob_b = 0, o_tg = 0, o_prefix = 0, o_topo = 0;
+    char* dev = nullptr;
+    ElemHeader* d_hdr = nullptr;
+    char* d_blob = nullptr;
+    DevResult* d_res = nullptr;
+    int32_t* d_mz = nullptr;
+    double* d_pz = nullptr;
+    double* d_trd = nullptr;
+    int8_t* d_trz = nullptr;
+    DevCounters* d_cnt = nullptr;
+    int* d_head = nullptr;
+    char* d_ws = nullptr;
+    int* h_map = nullptr;           // host-mapped: [0] tail, [64, 64+n) slot ring, [64+n, 64+2n) done flags
+    volatile int* h_tail = nullptr;
+    volatile int* h_qslot = nullptr;
+    volatile int* h_done = nullptr;
+    cudaStream_t copy = nullptr;    // admission and result copies, beside the running kernel
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool running = false;
+    char* h_stage = nullptr;
+    size_t h_stage_cap = 0;
+    ChainParams p;
+    std::vector<int> free_slots;
+    std::vector<char> busy;
+    std::vector<int64_t> slot_no;
+    std::vector<double> slot_t0;
+    std::deque<std::pair<HostElem, double>> queue;
+    int resident = 0, tail = 0;
+    long long launches = 0;
+    double kernel_ms = 0;
+};
+
 struct pacc_ctx {
     HostModel M;
     pacc_opts o;
@@ -449,6 +490,7 @@ struct pacc_ctx {
     void* d_blob = nullptr; size_t blob_cap = 0;
     void* d_misc = nullptr; size_t misc_cap = 0;
     Server srv;
+    StreamServer ss;
 };
 
 static std::string g_create_error;
@@ -625,6 +667,12 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->srv.h_stage) cudaFreeHost(c->srv.h_stage);
     if (c->srv.ev0) cudaEventDestroy(c->srv.ev0);
     if (c->srv.ev1) cudaEventDestroy(c->srv.ev1);
+    if (c->ss.dev) cudaFree(c->ss.dev);
+    if (c->ss.h_map) cudaFreeHost(c->ss.h_map);
+    if (c->ss.h_stage) cudaFreeHost(c->ss.h_stage);
+    if (c->ss.copy) cudaStreamDestroy(c->ss.copy);
+    if (c->ss.ev0) cudaEventDestroy(c->ss.ev0);
+    if (c->ss.ev1) cudaEventDestroy(c->ss.ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -632,10 +680,13 @@ void pacc_destroy(pacc_ctx* c) {
 // ---------------------------------------------------------------------------
 // serving: resident chain slots, continuous admission (batched kernel only)
 // ---------------------------------------------------------------------------
+// Warp-per-chain layout (pacc_batch.cu) or CTA-per-chain layout (pacc_chain.cu).
 static bool batched_layout(const pacc_ctx* c) {
-    return c->o.precision == PACC_FP32 || c->o.precision == PACC_FP64_BATCHED;
+    return c->o.precision == PACC_FP32_WARP || c->o.precision == PACC_FP64_BATCHED;
 }
-static bool serving(const pacc_ctx* c) { return c->o.sweeps_per_launch > 0 && batched_layout(c); }
+// Serving (continuous batching): sweep-step slots for the warp layout, the
+// persistent queue kernel for the CTA layout.
+static bool serving(const pacc_ctx* c) { return c->o.sweeps_per_launch > 0; }
 
 static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -789,7 +840,7 @@ static int server_setup(pacc_ctx* c, int GG_needed) {
     const int N = c->M.N, S = c->M.S;
     const int T = c->o.burnin + c->o.mcmc;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    v.prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    v.prec = c->o.precision == PACC_FP32_WARP ? 1 : 0;
     v.D = tree_stack_depth(c->M);
     v.n_int_max = S - 1;
     v.SP = (S + 15) & ~15;
@@ -1124,6 +1175,301 @@ static int server_step(pacc_ctx* c) {
     return PACC_OK;
 }
 
+// Threads per chain of the CTA-per-chain kernel: the caller's, else 256 with
+// FP32 partials (two chains per SM at 128 registers a thread) and 128 with
+// FP64 (238 registers a thread: two chains per SM).
+static int plain_block_threads(const pacc_ctx* c, int prec) {
+    if (c->o.block_threads > 0) return c->o.block_threads;
+    return prec == 1 ? 256 : 128;
+}
+
+// ---------------------------------------------------------------------------
+// serving with the CTA-per-chain kernel (stream mode)
+// ---------------------------------------------------------------------------
+static int stream_setup(pacc_ctx* c, int GG_needed) {
+    StreamServer& v = c->ss;
+    if (v.ready) return PACC_OK;
+    cudaSetDevice(c->device);
+    if (!ensure_model(c)) return PACC_ECUDA;
+    const int N = c->M.N, S = c->M.S;
+    const int T = c->o.burnin + c->o.mcmc;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    v.prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    v.GG_cap = std::max(5120, (GG_needed + 31) & ~31);
+    v.GGp_cap = v.GG_cap;
+    v.n_int_cap = S - 1;
+    v.TI = std::min(c->o.trace_iters, T);
+    v.BT = plain_block_threads(c, v.prec);
+    v.smem = smem_bytes(N, v.BT, v.prec);
+    const int per_sm = std::max(1, chain_occupancy(v.prec, v.BT, v.smem));
+    v.grid = c->n_sm * per_sm;
+    v.ws1 = (ws_bytes(v.n_int_cap, v.GGp_cap, T, c->o.mcmc, N, v.prec) + 4095) & ~(size_t)4095;
+    const size_t tb = al(topo_bytes(N));
+    v.o_tg = al((size_t)S * v.GGp_cap);
+    v.o_prefix = al(v.o_tg + (size_t)v.n_int_cap * v.GGp_cap);
+    v.o_topo = al(v.o_prefix + (size_t)(v.GGp_cap + 1) * 4);
+    v.blob_b = al(v.o_topo + tb);
+    const size_t per_slot = v.blob_b + sizeof(ElemHeader) + sizeof(DevResult) + 3 * N * 4 + 3 * N * 4 * 8 +
+                            sizeof(double) * 3 * 6 * (size_t)v.TI + (size_t)3 * v.TI * N + 64;
+    size_t budget = (size_t)c->o.memory_budget_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = fr / 4;
+    }
+    const size_t fixed = v.ws1 * v.grid + (1 << 20);
+    if (budget <= fixed + per_slot) { c->err = "memory budget too small for the serving workspaces"; return PACC_OOM; }
+    // two queued chains per resident CTA keep every CTA busy between host polls
+    const int want = c->o.max_resident > 0 ? c->o.max_resident : 2 * v.grid;
+    v.n_slots = (int)std::min<size_t>((size_t)want, (budget - fixed) / per_slot);
+    const int ns = v.n_slots;
+    size_t o = 0;
+    size_t o_hdr = o; o = al(o + sizeof(ElemHeader) * ns);
+    size_t o_blob = o; o = al(o + v.blob_b * ns);
+    size_t o_res = o; o = al(o + sizeof(DevResult) * ns);
+    size_t o_mz = o; o = al(o + sizeof(int32_t) * 3 * N * (size_t)ns);
+    size_t o_pz = o; o = al(o + sizeof(double) * 3 * N * 4 * (size_t)ns);
+    size_t o_trd = o; o = al(o + sizeof(double) * 3 * 6 * (size_t)v.TI * ns);
+    size_t o_trz = o; o = al(o + (size_t)3 * v.TI * N * ns);
+    size_t o_cnt = o; o = al(o + sizeof(DevCounters));
+    size_t o_head = o; o = al(o + 256);
+    size_t o_ws = o; o = al(o + v.ws1 * v.grid);
+    if (!cuda_ok(c, cudaMalloc((void**)&v.dev, o), "cudaMalloc (serving)")) return PACC_OOM;
+    if (!cuda_ok(c, cudaMemset(v.dev, 0, o_ws), "memset")) return PACC_ECUDA;
+    const size_t map_b = sizeof(int) * (64 + 2 * (size_t)ns);
+    if (!cuda_ok(c, cudaHostAlloc((void**)&v.h_map, map_b, cudaHostAllocMapped), "cudaHostAlloc")) return PACC_OOM;
+    std::memset(v.h_map, 0, map_b);
+    int* d_map = nullptr;
+    if (!cuda_ok(c, cudaHostGetDevicePointer((void**)&d_map, v.h_map, 0), "cudaHostGetDevicePointer"))
+        return PACC_ECUDA;
+    v.h_tail = v.h_map;
+    v.h_qslot = v.h_map + 64;
+    v.h_done = v.h_map + 64 + ns;
+    if (!cuda_ok(c, cudaStreamCreateWithFlags(&v.copy, cudaStreamNonBlocking), "stream") ||
+        !cuda_ok(c, cudaEventCreate(&v.ev0), "event") || !cuda_ok(c, cudaEventCreate(&v.ev1), "event"))
+        return PACC_ECUDA;
+    v.d_hdr = (ElemHeader*)(v.dev + o_hdr);
+    v.d_blob = v.dev + o_blob;
+    v.d_res = (DevResult*)(v.dev + o_res);
+    v.d_mz = (int32_t*)(v.dev + o_mz);
+    v.d_pz = (double*)(v.dev + o_pz);
+    v.d_trd = v.TI > 0 ? (double*)(v.dev + o_trd) : nullptr;
+    v.d_trz = v.TI > 0 ? (int8_t*)(v.dev + o_trz) : nullptr;
+    v.d_cnt = (DevCounters*)(v.dev + o_cnt);
+    v.d_head = (int*)(v.dev + o_head);
+    v.d_ws = v.dev + o_ws;
+    std::memset(&v.p, 0, sizeof(v.p));
+    v.p.hdr = v.d_hdr;
+    v.p.blob = (const uint8_t*)v.d_blob;
+    v.p.n_elem = ns;
+    v.p.results = v.d_res;
+    v.p.max_z = v.d_mz;
+    v.p.post_z = v.d_pz;
+    v.p.tr_d = v.d_trd;
+    v.p.tr_z = v.d_trz;
+    v.p.ws = v.d_ws;
+    v.p.ws_stride = v.ws1;
+    v.p.n_int_max = v.n_int_cap;
+    v.p.GGp_max = v.GGp_cap;
+    v.p.counters = v.d_cnt;
+    v.p.stream = 1;
+    v.p.q_head = v.d_head;
+    v.p.q_tail = d_map;
+    v.p.q_slot = d_map + 64;
+    v.p.q_cap = ns;
+    v.p.done_flag = d_map + 64 + ns;
+    v.p.idle_ns = 20000000;   // 20 ms
+    v.free_slots.clear();
+    for (int i = ns - 1; i >= 0; i--) v.free_slots.push_back(i);
+    v.busy.assign(ns, 0);
+    v.slot_no.assign(ns, 0);
+    v.slot_t0.assign(ns, 0);
+    v.resident = 0;
+    v.tail = 0;
+    v.ready = true;
+    return PACC_OK;
+}
+
+// Copies queued elements into free slots and publishes them to the queue.
+static int stream_admit(pacc_ctx* c) {
+    StreamServer& v = c->ss;
+    const int N = c->M.N, S = c->M.S;
+    std::vector<std::pair<int, std::pair<HostElem, double>>> adm;
+    while (!v.free_slots.empty() && !v.queue.empty()) {
+        int slot = v.free_slots.back();
+        v.free_slots.pop_back();
+        adm.push_back({slot, std::move(v.queue.front())});
+        v.queue.pop_front();
+    }
+    if (adm.empty()) return PACC_OK;
+    const size_t tb = topo_bytes(N);
+    auto staged = [&](const HostElem& E) {
+        return E.codes.size() + E.tg0.size() + E.prefix.size() * 4 + tb + sizeof(ElemHeader) + 64;
+    };
+    size_t tot = 0;
+    for (auto& a : adm) tot += staged(a.second.first);
+    if (tot > v.h_stage_cap) {
+        if (v.h_stage) cudaFreeHost(v.h_stage);
+        v.h_stage = nullptr;
+        v.h_stage_cap = 0;
+        if (!cuda_ok(c, cudaMallocHost((void**)&v.h_stage, tot * 2), "cudaMallocHost")) return PACC_OOM;
+        v.h_stage_cap = tot * 2;
+    }
+    size_t off = 0;
+    cudaStream_t st = v.copy;
+    for (auto& a : adm) {
+        const int slot = a.first;
+        const HostElem& E = a.second.first;
+        char* reg = v.d_blob + (size_t)slot * v.blob_b;
+        ElemHeader H;
+        std::memset(&H, 0, sizeof(H));
+        H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
+        H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws; H.stack_depth = E.stack_depth;
+        H.element_no = E.no;
+        H.SP = (S + 15) & ~15;
+        H.codes_off = reg - v.d_blob;
+        H.tg_off = H.codes_off + (int64_t)v.o_tg;
+        H.prefix_off = H.codes_off + (int64_t)v.o_prefix;
+        H.topo_off = H.codes_off + (int64_t)v.o_topo;
+        char* p0 = v.h_stage + off;
+        std::memcpy(p0, E.codes.data(), E.codes.size());
+        char* p1 = p0 + E.codes.size();
+        std::memcpy(p1, E.tg0.data(), E.tg0.size());
+        char* p2 = p1 + E.tg0.size();
+        std::memcpy(p2, E.prefix.data(), E.prefix.size() * 4);
+        char* p3 = p2 + E.prefix.size() * 4;
+        std::memcpy(p3, E.topo.data(), E.topo.size() * 2);
+        std::memcpy(p3 + ((E.topo.size() * 2 + 15) & ~(size_t)15), E.dist2.data(), N * 8);
+        char* p4 = p3 + tb;
+        std::memcpy(p4, &H, sizeof(H));
+        bool ok = cuda_ok(c, cudaMemcpyAsync(reg, p0, E.codes.size(), cudaMemcpyHostToDevice, st), "H2D codes") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_tg, p1, E.tg0.size(), cudaMemcpyHostToDevice, st), "H2D tg") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_prefix, p2, E.prefix.size() * 4, cudaMemcpyHostToDevice, st), "H2D prefix") &&
+                  cuda_ok(c, cudaMemcpyAsync(reg + v.o_topo, p3, tb, cudaMemcpyHostToDevice, st), "H2D topo") &&
+                  cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, p4, sizeof(H), cudaMemcpyHostToDevice, st), "H2D header") &&
+                  cuda_ok(c, cudaMemsetAsync(v.d_res + slot, 0, sizeof(DevResult), st), "memset result");
+        if (!ok) return PACC_ECUDA;
+        off += staged(E);
+        v.slot_no[slot] = E.no;
+        v.slot_t0[slot] = a.second.second;
+        v.busy[slot] = 1;
+        v.resident++;
+    }
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "admission")) return PACC_ECUDA;
+    // the slots' data is in device memory: publish them
+    for (auto& a : adm) {
+        v.h_done[a.first] = 0;
+        v.h_qslot[v.tail % v.n_slots] = a.first;
+        v.tail++;
+    }
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    *v.h_tail = v.tail;
+    return PACC_OK;
+}
+
+// Collects the results of the slots whose chains finished.
+static int stream_retire(pacc_ctx* c) {
+    StreamServer& v = c->ss;
+    const int N = c->M.N;
+    std::vector<int> fin;
+    for (int s = 0; s < v.n_slots; s++)
+        if (v.busy[s] && v.h_done[s]) fin.push_back(s);
+    if (fin.empty()) return PACC_OK;
+    std::atomic_thread_fence(std::memory_order_seq_cst);
+    const int nd = (int)fin.size();
+    cudaStream_t st = v.copy;
+    std::vector<DevResult> res(nd);
+    std::vector<int32_t> mz((size_t)nd * 3 * N);
+    std::vector<double> pz((size_t)nd * 3 * N * 4);
+    const size_t trd_n = (size_t)3 * 6 * v.TI, trz_n = (size_t)3 * v.TI * N;
+    std::vector<double> trd(trd_n * nd);
+    std::vector<int8_t> trz(trz_n * nd);
+    for (int i = 0; i < nd; i++) {
+        const int slot = fin[i];
+        cudaMemcpyAsync(&res[i], v.d_res + slot, sizeof(DevResult), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&mz[(size_t)i * 3 * N], v.d_mz + (size_t)slot * 3 * N, sizeof(int32_t) * 3 * N,
+                        cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&pz[(size_t)i * 3 * N * 4], v.d_pz + (size_t)slot * 3 * N * 4, sizeof(double) * 3 * N * 4,
+                        cudaMemcpyDeviceToHost, st);
+        if (v.TI > 0) {
+            cudaMemcpyAsync(&trd[trd_n * i], v.d_trd + trd_n * slot, sizeof(double) * trd_n, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&trz[trz_n * i], v.d_trz + trz_n * slot, trz_n, cudaMemcpyDeviceToHost, st);
+        }
+    }
+    if (!cuda_ok(c, cudaStreamSynchronize(st), "D2H results")) return PACC_ECUDA;
+    int clk_khz = 0;
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, c->device);
+    const double t = now_ms();
+    for (int i = 0; i < nd; i++) {
+        const int slot = fin[i];
+        pacc_ctx::Done d;
+        std::memset(&d.r, 0, sizeof(d.r));
+        d.r.element_no = v.slot_no[slot];
+        d.r.n_nodes = N;
+        const DevResult& R = res[i];
+        d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
+        for (int m = 0; m < 3; m++) {
+            pacc_model_result& mr = d.r.model[m];
+            mr.loglik = R.model[m].loglik;
+            mr.max_loglik = R.model[m].max_loglik;
+            mr.n_rate = R.model[m].rates[0];
+            mr.c_rate = R.model[m].rates[1];
+            mr.g_rate = R.model[m].rates[2];
+            mr.l_rate = R.model[m].rates[3];
+            mr.l2_rate = R.model[m].rates[4];
+            mr.failure = R.model[m].failure;
+            mr.n_configs = R.model[m].n_configs;
+        }
+        d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
+        d.r.latency_ms = t - v.slot_t0[slot];
+        d.max_z.assign(mz.begin() + (size_t)i * 3 * N, mz.begin() + (size_t)(i + 1) * 3 * N);
+        d.post_z.assign(pz.begin() + (size_t)i * 3 * N * 4, pz.begin() + (size_t)(i + 1) * 3 * N * 4);
+        if (v.TI > 0) {
+            d.tr_d.assign(trd.begin() + trd_n * i, trd.begin() + trd_n * (i + 1));
+            d.tr_z.assign(trz.begin() + trz_n * i, trz.begin() + trz_n * (i + 1));
+        }
+        c->done.push_back(std::move(d));
+        v.busy[slot] = 0;
+        v.free_slots.push_back(slot);
+        v.resident--;
+    }
+    return PACC_OK;
+}
+
+// One host step of stream serving: collect finished chains, admit queued
+// elements, and (re)launch the persistent kernel when chains wait and no
+// launch is running.
+static int stream_step(pacc_ctx* c) {
+    StreamServer& v = c->ss;
+    cudaSetDevice(c->device);
+    int st = stream_retire(c);
+    if (st != PACC_OK) return st;
+    if (!ensure_model(c)) return PACC_ECUDA;
+    st = stream_admit(c);
+    if (st != PACC_OK) return st;
+    if (v.running) {
+        cudaError_t q = cudaEventQuery(v.ev1);
+        if (q == cudaSuccess) {
+            v.running = false;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, v.ev0, v.ev1);
+            v.kernel_ms += ms;
+        } else if (q != cudaErrorNotReady) {
+            return cuda_ok(c, q, "serving kernel") ? PACC_OK : PACC_ECUDA;
+        }
+    }
+    if (!v.running && v.resident > 0) {
+        cudaStream_t ks = c->stream;
+        if (!cuda_ok(c, cudaEventRecord(v.ev0, ks), "event") ||
+            !cuda_ok(c, launch_chain(v.p, v.grid, v.BT, v.smem, v.prec, ks), "launch (serving)") ||
+            !cuda_ok(c, cudaEventRecord(v.ev1, ks), "event"))
+            return PACC_ECUDA;
+        v.running = true;
+        v.launches++;
+    }
+    return PACC_OK;
+}
+
 int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
     if (!c || !b || b->n_elements < 0) return PACC_EINVAL;
     const int n = b->n_elements;
@@ -1152,8 +1498,11 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
         if (!c->gpu_ok) return PACC_ECUDA;
         int gmax = 0;
         for (size_t i = base; i < c->pending.size(); i++) gmax = std::max(gmax, c->pending[i].GG);
-        int st = server_setup(c, gmax);
+        const bool warp = batched_layout(c);
+        int st = warp ? server_setup(c, gmax) : stream_setup(c, gmax);
         if (st != PACC_OK) { c->pending.resize(base); return st; }
+        const int cap = warp ? c->srv.GG_cap : c->ss.GG_cap;
+        auto& queue = warp ? c->srv.queue : c->ss.queue;
         const double t = now_ms();
         // within one submitted batch the longest elements are admitted first
         std::vector<size_t> ord;
@@ -1173,17 +1522,17 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
                 c->done.push_back(std::move(d));
                 continue;
             }
-            if (E.GG > c->srv.GG_cap) {
+            if (E.GG > cap) {
                 c->pending.resize(base);
                 c->err = "element longer than the serving slot capacity";
                 return PACC_EINVAL;
             }
-            if (E.stack_depth > c->srv.D || E.n_int > c->srv.n_int_max) {
+            if (warp && (E.stack_depth > c->srv.D || E.n_int > c->srv.n_int_max)) {
                 c->pending.resize(base);
                 c->err = "element tree exceeds the serving slot geometry";
                 return PACC_EUNSUPPORTED;
             }
-            c->srv.queue.push_back({std::move(E), t});
+            queue.push_back({std::move(E), t});
         }
         c->pending.resize(base);
     }
@@ -1242,7 +1591,7 @@ static int run_pending(pacc_ctx* c) {
     if (!ensure_model(c)) return PACC_ECUDA;
     const int N = c->M.N, S = c->M.S;
     const int n = (int)c->pending.size();
-    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_PLAIN) ? 1 : 0;
+    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
     const int T = c->o.burnin + c->o.mcmc;
     const int TI = std::min(c->o.trace_iters, T);
     // pack the blob
@@ -1292,9 +1641,10 @@ static int run_pending(pacc_ctx* c) {
     }
     if (batched_layout(c)) return run_batched(c, hdr, blob, off, n_int_max, GGuP_max);
     // launch geometry
-    int BT = c->o.block_threads > 0 ? c->o.block_threads : 128;
+    const int BT = plain_block_threads(c, prec);
     size_t smem = smem_bytes(N, BT, prec);
-    int per_sm = 2;
+    // resident CTAs per SM from the kernel's registers and shared memory
+    int per_sm = std::max(1, chain_occupancy(prec, BT, smem));
     int grid = std::max(1, std::min(n, c->n_sm * per_sm));
     size_t ws1 = ws_bytes(n_int_max, GGp_max, T, c->o.mcmc, N, prec);
     ws1 = (ws1 + 4095) & ~(size_t)4095;
@@ -1327,6 +1677,7 @@ static int run_pending(pacc_ctx* c) {
                  "H2D order"))
         return PACC_ECUDA;
     ChainParams p;
+    std::memset(&p, 0, sizeof(p));
     p.hdr = (const ElemHeader*)(mb + o_hdr);
     p.blob = (const uint8_t*)c->d_blob;
     p.n_elem = n;
@@ -1394,7 +1745,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
                        int n_int_max, int GGuP_max) {
     const int N = c->M.N, S = c->M.S;
     const int n = (int)c->pending.size();
-    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    const int prec = c->o.precision == PACC_FP32_WARP ? 1 : 0;
     const int T = c->o.burnin + c->o.mcmc;
     const int TI = std::min(c->o.trace_iters, T);
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -1542,9 +1893,18 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
 int pacc_sync(pacc_ctx* c) {
     if (!c) return PACC_EINVAL;
     if (serving(c)) {
-        while (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight) {
-            int st = server_step(c);
-            if (st != PACC_OK) return st;
+        if (batched_layout(c)) {
+            while (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight) {
+                int st = server_step(c);
+                if (st != PACC_OK) return st;
+            }
+        } else {
+            while (!c->ss.queue.empty() || c->ss.resident > 0) {
+                const size_t nd = c->done.size();
+                int st = stream_step(c);
+                if (st != PACC_OK) return st;
+                if (c->done.size() == nd) std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
         }
         return PACC_OK;
     }
@@ -1553,7 +1913,8 @@ int pacc_sync(pacc_ctx* c) {
 
 int pacc_pending(pacc_ctx* c) {
     if (!c) return 0;
-    return (int)(c->pending.size() + c->srv.queue.size() + c->srv.resident + (c->done.size() - c->done_head));
+    return (int)(c->pending.size() + c->srv.queue.size() + c->srv.resident + c->ss.queue.size() + c->ss.resident +
+                 (c->done.size() - c->done_head));
 }
 
 static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
@@ -1586,10 +1947,21 @@ static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
 
 int pacc_poll(pacc_ctx* c, pacc_result* out, int max) {
     if (!c || (!out && max > 0)) return -PACC_EINVAL;
-    if (serving(c) && c->done_head == c->done.size() &&
-        (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight)) {
-        int st = server_step(c);
-        if (st != PACC_OK) return -st;
+    if (serving(c) && c->done_head == c->done.size()) {
+        if (batched_layout(c)) {
+            if (!c->srv.queue.empty() || c->srv.resident > 0 || c->srv.inflight) {
+                int st = server_step(c);
+                if (st != PACC_OK) return -st;
+            }
+        } else if (!c->ss.queue.empty() || c->ss.resident > 0) {
+            int st = stream_step(c);
+            if (st != PACC_OK) return -st;
+            if (c->done_head == c->done.size()) {   // nothing finished yet: do not spin the caller
+                std::this_thread::sleep_for(std::chrono::microseconds(200));
+                st = stream_step(c);
+                if (st != PACC_OK) return -st;
+            }
+        }
     }
     int k = 0;
     while (k < max && c->done_head < c->done.size()) {
@@ -1629,7 +2001,35 @@ int pacc_run(pacc_ctx* c, const pacc_element_batch* b, pacc_result* out) {
 
 int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
     if (!c || !out) return PACC_EINVAL;
-    if (serving(c) && c->srv.ready) {
+    if (serving(c) && !batched_layout(c) && c->ss.ready) {
+        DevCounters dc;
+        if (cudaMemcpyAsync(&dc, c->ss.d_cnt, sizeof(dc), cudaMemcpyDeviceToHost, c->ss.copy) != cudaSuccess ||
+            cudaStreamSynchronize(c->ss.copy) != cudaSuccess)
+            return PACC_ECUDA;
+        pacc_counters& pc = c->counters;
+        std::memset(&pc, 0, sizeof(pc));
+        pc.edge_updates_internal = (double)dc.edge_internal;
+        pc.edge_updates_leaf = (double)dc.edge_leaf;
+        pc.column_loglik = (double)dc.col_ll;
+        pc.tg_draws = (double)dc.tg_draws;
+        pc.z_draws = (double)dc.z_draws;
+        pc.pmatrix_builds = (double)dc.pmat;
+        double running_ms = 0;
+        if (c->ss.running && cudaEventQuery(c->ss.ev0) == cudaSuccess) {
+            // the launch in progress: time from its start event to now
+            cudaEvent_t now;
+            cudaEventCreate(&now);
+            cudaEventRecord(now, c->ss.copy);
+            cudaEventSynchronize(now);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->ss.ev0, now);
+            cudaEventDestroy(now);
+            running_ms = ms;
+        }
+        pc.kernel_ms = c->ss.kernel_ms + running_ms;
+        pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
+        pc.iterations = (double)c->ss.launches;
+    } else if (serving(c) && c->srv.ready) {
         if (c->srv.inflight) cudaStreamSynchronize(c->stream);
         DevCounters dc;
         if (cudaMemcpy(&dc, c->srv.d_cnt, sizeof(dc), cudaMemcpyDeviceToHost) != cudaSuccess) return PACC_ECUDA;
@@ -1736,7 +2136,7 @@ int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const i
     if (!preprocess(c->M, c->o, bases, length, E, false)) return PACC_EINVAL;
     if (E.filtered) { *n_cols = 0; return PACC_FILTERED; }
     const int N = c->M.N;
-    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_PLAIN) ? 1 : 0;
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     ElemHeader H;
     std::memset(&H, 0, sizeof(H));

@@ -1,6 +1,8 @@
-"""Serving mode: chains stay resident in device slots, queued elements are
-admitted as slots free up, and finished chains are retired after every sweep
-step.  An element's chain depends only on the element, the model and SEED
+"""Serving mode (continuous batching).  CTA-per-chain layout: a persistent
+kernel takes element slots from a queue the host appends to while it runs.
+Warp-per-chain layout: chains stay resident in device slots, are advanced by
+sweep steps, queued elements are admitted as slots free up and finished
+chains are retired after every step.  An element's chain depends only on the element, the model and SEED
 (every element restarts the same draw stream), so a served element must give
 bit-identical results to the same element run in a batch, whatever else is
 resident beside it and whenever it was admitted."""
@@ -58,7 +60,10 @@ def _serve(ds, o, chunks, polls_between=2):
     return _index(got)
 
 
-@pytest.mark.parametrize("prec", [abi.PACC_FP32, abi.PACC_FP64_BATCHED])
+ALL = [abi.PACC_FP32, abi.PACC_FP64, abi.PACC_FP32_WARP, abi.PACC_FP64_BATCHED]
+
+
+@pytest.mark.parametrize("prec", ALL)
 def test_served_equals_batched(built, prec):
     ds = synth.make_dataset("st43", n_elements=30, seed=5)
     ref = pg.Context(ds, _opts(prec)).run()
@@ -72,29 +77,32 @@ def test_served_equals_batched(built, prec):
             assert r.arr[i].latency_ms > 0
 
 
-def test_alone_equals_mixed(built):
+@pytest.mark.parametrize("prec", [abi.PACC_FP32, abi.PACC_FP32_WARP])
+def test_alone_equals_mixed(built, prec):
     ds = synth.make_dataset("st43", n_elements=40, seed=6)
     x = 17
-    alone = _serve(ds, _opts(abi.PACC_FP32, sweeps=5), [[x]])
-    mixed = _serve(ds, _opts(abi.PACC_FP32, sweeps=5, max_resident=12),
+    alone = _serve(ds, _opts(prec, sweeps=5), [[x]])
+    mixed = _serve(ds, _opts(prec, sweeps=5, max_resident=12),
                    [list(range(0, 10)), [x] + list(range(20, 40)), list(range(10, 17))])
     a, ia = alone[x]
     b, ib = mixed[x]
     _same(a, ia, b, ib)
 
 
-def test_memory_budget_too_small_is_refused(built):
+@pytest.mark.parametrize("prec", [abi.PACC_FP32, abi.PACC_FP32_WARP])
+def test_memory_budget_too_small_is_refused(built, prec):
     ds = synth.make_dataset("st43", n_elements=4, seed=7)
-    o = _opts(abi.PACC_FP32, sweeps=3)
+    o = _opts(prec, sweeps=3)
     o.memory_budget_bytes = 1 << 20
     ctx = pg.Context(ds, o)
     with pytest.raises(pg.PaccError):
         ctx.submit(ds)
 
 
-def test_served_filtered_elements_return_at_once(built):
+@pytest.mark.parametrize("prec", [abi.PACC_FP32, abi.PACC_FP32_WARP])
+def test_served_filtered_elements_return_at_once(built, prec):
     ds = synth.make_dataset("st43", n_elements=12, seed=8)
-    o = _opts(abi.PACC_FP32, sweeps=4)
+    o = _opts(prec, sweeps=4)
     o.min_len = 10**6          # every element is filtered before it reaches a slot
     ctx = pg.Context(ds, o)
     ctx.submit(ds)
