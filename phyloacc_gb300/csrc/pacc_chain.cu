@@ -239,9 +239,14 @@ __device__ __forceinline__ int mat_class(int z, int prop_class) {
 // buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928).  Returns the summed
 // per-column log-likelihood at the root (valid when the root is flagged).
 template <typename Real>
-__device__ __noinline__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
+__device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
     const int BT = blockDim.x;
     double ll_sum = 0;
+    // FP32 partials: the thread's columns are combined as an FP64 product of
+    // root-sum mantissas with an exact integer exponent, and one log at the
+    // end, instead of one FP64 log per column
+    double mprod = 1.0;
+    long long mexp = 0;
     unsigned long long e_int = 0, e_leaf = 0;
     for (int k = 0; k < c.n_int; k++) {
         int s = c.internal[k];
@@ -318,7 +323,14 @@ __device__ __noinline__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, i
 #pragma unroll
                 for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
                 double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
-                ll_sum += d_log(t) + (double)sc * 0.6931471805599453;
+                if (sizeof(Real) == 8) {
+                    ll_sum += d_log(t) + (double)sc * 0.6931471805599453;
+                } else {
+                    int e1, e2;
+                    mprod *= frexp(t, &e1);
+                    mprod = frexp(mprod, &e2);
+                    mexp += (long long)e1 + e2 + sc;
+                }
             }
 #pragma unroll
             for (int j = 0; j < 4; j++) Ld[j * c.GGp + g] = a[j];
@@ -327,7 +339,7 @@ __device__ __noinline__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, i
     }
     c.local.edge_internal += e_int;
     c.local.edge_leaf += e_leaf;
-    if (threadIdx.x < c.GG) c.local.col_ll += 0;
+    if (sizeof(Real) != 8) ll_sum = d_log(mprod) + (double)mexp * 0.6931471805599453;
     double r = block_sum(ll_sum, c.red);
     if (threadIdx.x == 0) c.local.col_ll += c.GG;
     return r;
@@ -339,7 +351,7 @@ __device__ __noinline__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, i
 // (bpp_c.cpp:887-902) and the Eval2 fallback (bpp_c2.cpp:220-237) apply the
 // eigen formula whatever the branch length.
 template <typename Real>
-__device__ __noinline__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
+__device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
         int s = c.nodes[i];
         double* out = c.ptd + ((size_t)k * c.N + s) * 16;
@@ -409,7 +421,7 @@ __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool i
 // Internal-base sampling, top-down per column (Update_Tg with tosample,
 // bpp_c.cpp:672-733).  Column g takes its words at pos + prefix[g].
 template <typename Real>
-__device__ __noinline__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
+__device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
     int err = 0;
     const int rir = c.irank[c.root];
     const int rbuf = c.cur[c.root];
@@ -459,7 +471,7 @@ __device__ __noinline__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
 // Emission sums per branch and class (getEmission, bpp_c2.cpp:355-390) from a
 // histogram of (child symbol, parent base) pairs.
 template <typename Real>
-__device__ __noinline__ void emission(Ctx<Real>& c) {
+__device__ void emission(Ctx<Real>& c) {
     const int NB = NSYM * 4;
     for (int i = threadIdx.x; i < c.N * NB; i += blockDim.x) c.cnt[i] = 0;
     __syncthreads();
@@ -536,7 +548,7 @@ __device__ __forceinline__ double msg(const double* ltm, const double* beta, int
 
 // Forward filter / backward sample of Z (Update_Z_subtree, bpp_c.cpp:1182-1293).
 template <typename Real>
-__device__ __noinline__ int update_z(Ctx<Real>& c, uint64_t pos) {
+__device__ int update_z(Ctx<Real>& c, uint64_t pos) {
     const double NI = -CUDART_INF;
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         int s = c.nodes[i];
@@ -601,7 +613,7 @@ __device__ __noinline__ int update_z(Ctx<Real>& c, uint64_t pos) {
 
 // Flags of proper ancestors of flagged nodes (getUpdateNode, bpp_c.cpp:620-642).
 template <typename Real>
-__device__ __noinline__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int mode, int* tmp) {
+__device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int mode, int* tmp) {
     // mode 0: src = changed flags; mode 1: Z == 2 (non-missing); mode 2: Z == 1 (non-missing)
     for (int i = threadIdx.x; i < c.N; i += blockDim.x) dst[i] = 0;
     __syncthreads();
@@ -623,7 +635,7 @@ __device__ __noinline__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int
 // One Metropolis-Hastings update of the accelerated (neut) or conserved rate
 // (sample_rate, bpp_c.cpp:930-1176), M = 1, adaptive factor 0.5.
 template <typename Real>
-__device__ __noinline__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
+__device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
     ChainScalars* cs = c.cs;
     const int8_t* unv = neut ? c.unvN : c.unvC;
     const int cls = neut ? P_NEUT : P_CONS;
@@ -758,7 +770,7 @@ __device__ __noinline__ double sample_rate(Ctx<Real>& c, const double* dist2, bo
 }
 
 // Rank selection: the element that std::sort would put at index T/2 (bpp_c2.cpp:742-755).
-__device__ __noinline__ double median_of(const double* x, int T, double* red) {
+__device__ double median_of(const double* x, int T, double* red) {
     int target = T / 2;
     __syncthreads();
     for (int i = threadIdx.x; i < T; i += blockDim.x) {
@@ -781,7 +793,7 @@ __device__ __noinline__ double median_of(const double* x, int T, double* red) {
 
 // Prior of a Z configuration (bpp_c2.cpp:131-163): Beta-Binomial terms + root prior.
 template <typename Real>
-__device__ __noinline__ double prior_config(Ctx<Real>& c, const int8_t* z) {
+__device__ double prior_config(Ctx<Real>& c, const int8_t* z) {
     double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     for (int k = 0; k + 1 < c.n_nodes; k++) {
         int s = c.nodes[k];
@@ -800,7 +812,7 @@ __device__ __noinline__ double prior_config(Ctx<Real>& c, const int8_t* z) {
 
 // Marginal likelihood of one model (Eval2, bpp_c2.cpp:14-353).
 template <typename Real>
-__device__ __noinline__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, int* n_conf_out) {
+__device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, int* n_conf_out) {
     ChainScalars* cs = c.cs;
     const int burn = c.burn, mcmc = c.mcmc, T = c.T;
     int8_t* Zm = c.maxz;  // Max_Z
@@ -1053,13 +1065,15 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
                 const int i = atomicAdd(P.next_elem, 1);
                 elem_ = (i < P.n_elem && P.order) ? P.order[i] : i;
             } else {
-                // take the next published queue position; give up after idle_ns
-                // without work (the host launches the kernel again when needed)
+                // take the next published queue position; return when the host
+                // asks the idle blocks to stop (q_stop), or after idle_ns
+                // without work at the latest (the host launches again when needed)
                 elem_ = P.n_elem;
                 const unsigned long long t0 = globaltimer_ns();
                 for (;;) {
                     const int h = *(volatile int*)P.q_head;
                     const int t = *P.q_tail;
+                    if (h >= t && *P.q_stop) break;
                     if (h < t) {
                         if (atomicCAS(P.q_head, h, h + 1) == h) {
                             __threadfence_system();   // the slot id and its data after the tail

@@ -153,7 +153,8 @@ struct ChainParams {
     const volatile int* q_slot;      // host-mapped: slot of queue position i (ring of q_cap)
     int q_cap;
     volatile int* done_flag;         // host-mapped, per slot: set to 1 once the slot's results are written
-    long long idle_ns;               // a CTA without work for this long returns
+    const volatile int* q_stop;      // host-mapped: nonzero asks the blocks to return when idle
+    long long idle_ns;               // safety bound: a block idle this long returns even without q_stop
 };
 
 // ---- batched (warp-per-chain) kernel ----

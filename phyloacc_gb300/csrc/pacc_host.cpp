@@ -443,8 +443,10 @@ struct StreamServer {
     DevCounters* d_cnt = nullptr;
     int* d_head = nullptr;
     char* d_ws = nullptr;
-    int* h_map = nullptr;           // host-mapped: [0] tail, [64, 64+n) slot ring, [64+n, 64+2n) done flags
+    int* h_map = nullptr;           // host-mapped: [0] tail, [1] stop, [64, 64+n) slot ring, [64+n, 64+2n) done flags
     volatile int* h_tail = nullptr;
+    volatile int* h_stop = nullptr;
+    bool stopping = false;          // the idle blocks were asked to return
     volatile int* h_qslot = nullptr;
     volatile int* h_done = nullptr;
     cudaStream_t copy = nullptr;    // admission and result copies, beside the running kernel
@@ -543,9 +545,12 @@ static bool ensure_model(pacc_ctx* c) {
     std::lock_guard<std::mutex> lk(g_model_mu);
     const int d = c->device;
     if (d >= 0 && d < 64 && g_model_owner[d] == c) return true;
-    // a kernel of the context whose model is there may still run (serving)
-    if (d >= 0 && d < 64 && g_model_owner[d] && g_model_owner[d]->stream)
+    // a kernel of the context whose model is there may still run (serving):
+    // its idle blocks are asked to return, then its launch is waited for
+    if (d >= 0 && d < 64 && g_model_owner[d] && g_model_owner[d]->stream) {
+        if (g_model_owner[d]->ss.h_stop) *g_model_owner[d]->ss.h_stop = 1;
         cudaStreamSynchronize(g_model_owner[d]->stream);
+    }
     if (!cuda_ok(c, set_model(c->M.dm, c->stream), "set_model") ||
         !cuda_ok(c, set_model_batch(c->M.dm, c->stream), "set_model_batch") ||
         !cuda_ok(c, cudaStreamSynchronize(c->stream), "set_model"))
@@ -650,7 +655,8 @@ void pacc_destroy(pacc_ctx* c) {
     if (!c) return;
     if (c->gpu_ok && c->stream) {
         cudaSetDevice(c->device);
-        cudaStreamSynchronize(c->stream);   // a serving sweep may still be in flight
+        if (c->ss.h_stop) *c->ss.h_stop = 1;   // idle serving blocks return
+        cudaStreamSynchronize(c->stream);      // a serving launch may still be in flight
     }
     {
         std::lock_guard<std::mutex> lk(g_model_mu);
@@ -1243,6 +1249,7 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     if (!cuda_ok(c, cudaHostGetDevicePointer((void**)&d_map, v.h_map, 0), "cudaHostGetDevicePointer"))
         return PACC_ECUDA;
     v.h_tail = v.h_map;
+    v.h_stop = v.h_map + 1;
     v.h_qslot = v.h_map + 64;
     v.h_done = v.h_map + 64 + ns;
     if (!cuda_ok(c, cudaStreamCreateWithFlags(&v.copy, cudaStreamNonBlocking), "stream") ||
@@ -1278,7 +1285,8 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.p.q_slot = d_map + 64;
     v.p.q_cap = ns;
     v.p.done_flag = d_map + 64 + ns;
-    v.p.idle_ns = 20000000;   // 20 ms
+    v.p.q_stop = d_map + 1;
+    v.p.idle_ns = 30000000000LL;   // 30 s: only a safety bound, q_stop ends idle launches
     v.free_slots.clear();
     for (int i = ns - 1; i >= 0; i--) v.free_slots.push_back(i);
     v.busy.assign(ns, 0);
@@ -1449,6 +1457,7 @@ static int stream_step(pacc_ctx* c) {
     if (st != PACC_OK) return st;
     if (v.running) {
         cudaError_t q = cudaEventQuery(v.ev1);
+        if (q == cudaErrorNotReady && v.stopping && v.resident > 0) q = cudaEventSynchronize(v.ev1);
         if (q == cudaSuccess) {
             v.running = false;
             float ms = 0;
@@ -1458,7 +1467,16 @@ static int stream_step(pacc_ctx* c) {
             return cuda_ok(c, q, "serving kernel") ? PACC_OK : PACC_ECUDA;
         }
     }
+    // no chain left: let the idle blocks return (every block of a launch
+    // stays until then, so a launch never runs on part of its blocks)
+    if (v.running && v.resident == 0 && v.queue.empty() && !v.stopping) {
+        *v.h_stop = 1;
+        v.stopping = true;
+    }
     if (!v.running && v.resident > 0) {
+        *v.h_stop = 0;
+        v.stopping = false;
+        std::atomic_thread_fence(std::memory_order_seq_cst);
         cudaStream_t ks = c->stream;
         if (!cuda_ok(c, cudaEventRecord(v.ev0, ks), "event") ||
             !cuda_ok(c, launch_chain(v.p, v.grid, v.BT, v.smem, v.prec, ks), "launch (serving)") ||
@@ -1905,6 +1923,8 @@ int pacc_sync(pacc_ctx* c) {
                 if (st != PACC_OK) return st;
                 if (c->done.size() == nd) std::this_thread::sleep_for(std::chrono::microseconds(200));
             }
+            int st = stream_step(c);   // asks the idle blocks to return
+            if (st != PACC_OK) return st;
         }
         return PACC_OK;
     }

@@ -11,13 +11,14 @@
 //   <PREFIX>_rate_postZ_M{0,1,2}.txt, <PREFIX>_hyper.txt,
 //   <PREFIX>_species_names.txt and, with VERBOSE, <PREFIX>_mcmc_trace_M{m}_{No}.txt.
 // The MCMC itself runs on the GPU through the C ABI of include/pacc.h.
-// Extra keys (ignored by PhyloAcc-ST): GPU_PRECISION fp64|fp32, GPU_DEVICE,
+// Extra keys (ignored by PhyloAcc-ST): GPU_PRECISION fp64|fp32|fp32_warp|fp64_warp, GPU_DEVICE,
 // GPU_BLOCK_THREADS, GPU_MEMORY_BUDGET_GB.
 #include <dirent.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -284,7 +285,12 @@ static Config load_config(const string& path) {
         else if (k == "SAMPLE_HYPER") C.sample_hyper = to_bool(v);
         else if (k == "VERBOSE") C.verbose = to_bool(v);
         else if (k == "NUM_THREAD") C.num_thread = std::stoi(v);
-        else if (k == "GPU_PRECISION") o.precision = (v == "fp32" || v == "FP32") ? PACC_FP32 : PACC_FP64;
+        else if (k == "GPU_PRECISION") {
+            std::string u = v;
+            for (auto& ch : u) ch = (char)std::tolower((unsigned char)ch);
+            o.precision = u == "fp32" ? PACC_FP32 : u == "fp32_warp" ? PACC_FP32_WARP
+                        : u == "fp64_warp" ? PACC_FP64_BATCHED : PACC_FP64;
+        }
         else if (k == "GPU_DEVICE") o.device = std::stoi(v);
         else if (k == "GPU_BLOCK_THREADS") o.block_threads = std::stoi(v);
         else if (k == "GPU_COLUMNS_PER_LANE") o.columns_per_lane = std::stoi(v);
