@@ -386,6 +386,11 @@ __device__ void copy_class(Ctx<Real>& c, const double* dist2, int from, int to) 
 template <typename Real>
 __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool init) {
     const double NI = -CUDART_INF;
+    // the six logs depend on g, l and l2 only: one evaluation each
+    const double lg0 = d_log(1 - gr), lg1 = d_log(gr);
+    const double y = 1 - lr;
+    const double ll1 = d_log(y), ll2 = d_log(1 - y);
+    const double lm1 = d_log(lr2), lm2 = d_log(1 - lr2);
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         int s = c.nodes[i];
         double* t = c.ltm + (size_t)s * 9;   // t[zc*3 + zp]
@@ -400,20 +405,19 @@ __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool i
             }
             t[1 * 3 + 1] = 0;
             t[2 * 3 + 1] = NI;
-            t[0 * 3 + 0] = d_log(1 - gr);
-            t[1 * 3 + 0] = d_log(gr);
+            t[0 * 3 + 0] = lg0;
+            t[1 * 3 + 0] = lg1;
             t[2 * 3 + 0] = NI;
         } else {
-            t[0 * 3 + 0] = d_log(1 - gr);
-            t[1 * 3 + 0] = d_log(gr);
+            t[0 * 3 + 0] = lg0;
+            t[1 * 3 + 0] = lg1;
             t[2 * 3 + 0] = NI;
-            double y = 1 - lr;
             if (init) t[0 * 3 + 1] = NI;
-            t[1 * 3 + 1] = d_log(y);
-            t[2 * 3 + 1] = d_log(1 - y);
+            t[1 * 3 + 1] = ll1;
+            t[2 * 3 + 1] = ll2;
             if (init) t[0 * 3 + 2] = NI;
-            t[1 * 3 + 2] = d_log(lr2);
-            t[2 * 3 + 2] = d_log(1 - lr2);
+            t[1 * 3 + 2] = lm1;
+            t[2 * 3 + 2] = lm2;
         }
     }
 }
@@ -518,15 +522,17 @@ __device__ void emission(Ctx<Real>& c) {
             int n = c.cnt[s * NB + b];
             if (!n) continue;
             int sym = b >> 2, tp = b & 3;
-            double v;
-            if (sym < 4) v = d_log(P[sym * 4 + tp]);
+            double t;
+            if (sym < 4) t = P[sym * 4 + tp];
             else {
                 int msk = ambig_mask(sym - 4);
-                double t = 0;
+                t = 0;
                 for (int q = 0; q < 4; q++)
                     if (msk & (1 << q)) t += P[q * 4 + tp];
-                v = d_log(t);
             }
+            // with FP32 partials the log of the entry is taken in FP32 (the
+            // emissions feed the Z filter, whose normalisation stays FP64)
+            const double v = (sizeof(Real) == 8) ? d_log(t) : (double)f_log((float)t);
             e += (double)n * v;
         }
         c.emis[s * 3 + z] = e;
@@ -547,8 +553,86 @@ __device__ __forceinline__ double msg(const double* ltm, const double* beta, int
 }
 
 // Forward filter / backward sample of Z (Update_Z_subtree, bpp_c.cpp:1182-1293).
+// Z filter of the FP32-partial path: linear FP64 values normalised per node
+// (the log-space filter below needs three exp and a log per message; here one
+// exp per node and state).  Transition matrix T[zc][zp] from g, l, l2
+// (bpp_c.cpp:573-599); fixed nodes cannot be in state 2.  Draws use the same
+// stream words as the log-space filter.
+template <typename Real>
+__device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
+    const int T = c.T, m = c.cs->m;
+    const double gr = c.trd[TR_G * T + m], lr = c.trd[TR_L * T + m], lr2 = c.trd[TR_L2 * T + m];
+    const double Tf[3][3] = {{1 - gr, 0, 0}, {gr, 1, 0}, {0, 0, 0}};
+    const double Tn[3][3] = {{1 - gr, 0, 0}, {gr, 1 - lr, lr2}, {0, lr, 1 - lr2}};
+    for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
+        const int s = c.nodes[i];
+        const double e0 = c.emis[s * 3 + 0], e1 = c.emis[s * 3 + 1], e2 = c.emis[s * 3 + 2];
+        const bool ban = c.fixZ[s] == 1;
+        double mx = e0 > e1 ? e0 : e1;
+        if (!ban && e2 > mx) mx = e2;
+        c.beta[s * 3 + 0] = d_exp(e0 - mx);
+        c.beta[s * 3 + 1] = d_exp(e1 - mx);
+        c.beta[s * 3 + 2] = ban ? 0.0 : d_exp(e2 - mx);
+        c.changed[s] = 0;
+    }
+    __syncthreads();
+    for (int h = 0; h < c.n_hlev; h++) {
+        const int a = c.hlev_start[h], b = c.hlev_start[h + 1];
+        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+            const int p = c.hlev_nodes[i];
+            double v[3] = {c.beta[p * 3 + 0], c.beta[p * 3 + 1], c.beta[p * 3 + 2]};
+            const int ch[2] = {c.c2a[p], c.c2b[p]};
+            for (int q = 0; q < 2; q++) {
+                const int ci = ch[q];
+                const double(*Tm)[3] = (c.fixZ[ci] == 1) ? Tf : Tn;
+                for (int zp = 0; zp < 3; zp++) {
+                    double mm = 0;
+                    for (int zc = 0; zc < 3; zc++) mm += Tm[zc][zp] * c.beta[ci * 3 + zc];
+                    v[zp] *= mm;
+                }
+            }
+            const double mx = fmax(v[0], fmax(v[1], v[2]));
+            const double inv = mx > 0 ? 1.0 / mx : 1.0;
+            for (int zp = 0; zp < 3; zp++) c.beta[p * 3 + zp] = v[zp] * inv;
+        }
+        __syncthreads();
+    }
+    int err = 0;
+    if (threadIdx.x == 0) {
+        double pr[3] = {0.5 * c.beta[c.root * 3 + 0], 0.5 * c.beta[c.root * 3 + 1], 0.0};
+        uint32_t wd[4];
+        philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
+        int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
+        if (nn > 2) { err = 1; nn = c.Z[c.root]; }
+        if (nn != c.Z[c.root]) c.changed[c.root] = 1;
+        c.Z[c.root] = (int8_t)nn;
+    }
+    __syncthreads();
+    for (int d = 0; d < c.n_dlev; d++) {
+        const int a = c.dlev_start[d], b = c.dlev_start[d + 1];
+        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+            const int s = c.dlev_nodes[i];
+            const int zp = c.Z[c.par[s]];
+            const double(*Tm)[3] = (c.fixZ[s] == 1) ? Tf : Tn;
+            double pr[3];
+            for (int k = 0; k < 3; k++) pr[k] = Tm[k][zp] * c.beta[s * 3 + k];
+            const uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
+            uint32_t wd[4];
+            philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
+            int nn = categorical(3, pr, word_to_uniform(wd[w & 3]));
+            if (nn > 2) { err = 1; nn = c.Z[s]; }
+            if (nn != c.Z[s]) c.changed[s] = 1;
+            c.Z[s] = (int8_t)nn;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.local.z_draws += c.n_nodes;
+    return err;
+}
+
 template <typename Real>
 __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
+    if (sizeof(Real) == 4) return update_z_linear(c, pos);
     const double NI = -CUDART_INF;
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         int s = c.nodes[i];
@@ -1184,6 +1268,15 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
             double ll0 = prune(c, c.unv, false, -1);
             if (threadIdx.x == 0) cs_.loglik = ll0;
             __syncthreads();
+            long long tph = clock64();   // phase timer (thread 0): cycles per phase into the counters
+#define V1_PHASE(i)                                          \
+    do {                                                     \
+        if (threadIdx.x == 0) {                              \
+            const long long t_ = clock64();                  \
+            c.local.phase_cycles[i] += (unsigned long long)(t_ - tph); \
+            tph = t_;                                        \
+        }                                                    \
+    } while (0)
             for (int m = 0; m < T; m++) {
                 // MonitorChain (bpp_c.cpp:741-834)
                 for (int i = threadIdx.x; i < N; i += BT) c.trz[(size_t)m * N + i] = c.Z[i];
@@ -1202,19 +1295,23 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
                 if (tmp_)
                     for (int i = threadIdx.x; i < N; i += BT) c.maxz[i] = c.Z[i];
                 if (m == T - 1) break;
+                V1_PHASE(0);
                 // internal bases
                 uint64_t pos = cs_.pos;
                 int err = sample_tg(c, pos);
                 __syncthreads();
+                V1_PHASE(1);
                 if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.tg_draws;
                 if (err) atomicOr(&cs_.status, 1);
                 // latent states
                 emission(c);
+                V1_PHASE(2);
                 pos = cs_.pos;
                 int zerr = update_z(c, pos);
                 if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.n_nodes;
                 if (zerr) atomicOr(&cs_.status, 1);
                 __syncthreads();
+                V1_PHASE(3);
                 // partial re-prune of ancestors of changed branches (bpp_c.cpp:419-431)
                 mark_ancestors(c, c.changed, c.unv, 0, &tmp_);
                 int any_unv = block_or(c.unv[c.root], &tmp_);
@@ -1223,28 +1320,40 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
                     if (threadIdx.x == 0) cs_.loglik = ll;
                 }
                 __syncthreads();
+                V1_PHASE(4);
                 // rates (bpp_c.cpp:434-452)
                 mark_ancestors(c, nullptr, c.unvN, 1, &tmp_);
                 mark_ancestors(c, nullptr, c.unvC, 2, &tmp_);
                 double rn = sample_rate(c, dist2_, true, c.trd[TR_N * T + m], &tmp_);
                 if (threadIdx.x == 0) c.trd[TR_N * T + m + 1] = rn;
                 __syncthreads();
+                V1_PHASE(5);
                 double rc = sample_rate(c, dist2_, false, c.trd[TR_C * T + m], &tmp_);
                 if (threadIdx.x == 0) c.trd[TR_C * T + m + 1] = rc;
-                // transitions of Z (sample_transition, bpp_c.cpp:522-613)
+                __syncthreads();
+                V1_PHASE(6);
+                // transitions of Z (sample_transition, bpp_c.cpp:522-613): the
+                // (child, parent) state counts in parallel (exact integers),
+                // then the three Beta draws on one thread
+                int* zcount = c.cnt;   // free until the next emission pass
+                if (threadIdx.x < 18) zcount[threadIdx.x] = 0;
+                __syncthreads();
+                for (int k = threadIdx.x; k + 1 < c.n_nodes; k += BT) {
+                    const int s = c.nodes[k];
+                    const int b = c.Z[s] * 3 + c.Z[c.par[s]];
+                    atomicAdd(&zcount[b], 1);
+                    if (c.fixZ[s] == 1) atomicAdd(&zcount[9 + b], 1);
+                }
+                __syncthreads();
                 if (threadIdx.x == 0) {
-                    double nZ[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-                    for (int k = 0; k + 1 < c.n_nodes; k++) {
-                        int s = c.nodes[k];
-                        nZ[c.Z[s]][c.Z[c.par[s]]] += 1;
-                    }
+                    double nZ[3][3];
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) nZ[a][b] = (double)zcount[a * 3 + b];
                     StreamReader rd;
                     rd.init(dM.seed, cs_.pos);
                     double gr = rd.beta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]);
-                    for (int k = 0; k + 1 < c.n_nodes; k++) {
-                        int s = c.nodes[k];
-                        if (c.fixZ[s] == 1) nZ[c.Z[s]][c.Z[c.par[s]]] -= 1;
-                    }
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) nZ[a][b] -= (double)zcount[9 + a * 3 + b];
                     double lr = rd.beta(dM.la + nZ[2][1], dM.lb + nZ[1][1]);
                     double lr2 = (dM.l2a == 0) ? 0.0 : rd.beta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]);
                     cs_.pos = rd.pos;
@@ -1255,8 +1364,10 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
                 __syncthreads();
                 build_ltm(c, c.trd[TR_G * T + m + 1], c.trd[TR_L * T + m + 1], c.trd[TR_L2 * T + m + 1], false);
                 __syncthreads();
+                V1_PHASE(7);
                 if (threadIdx.x == 0) c.local.iters++;
             }
+#undef V1_PHASE
             __syncthreads();
             DevModelResult& MR = R->model[mi];
             if (threadIdx.x == 0) MR.max_loglik = cs_.maxll;
@@ -1315,6 +1426,7 @@ __global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
                 atomicAdd(&P.counters->col_ll, c.local.col_ll);
                 atomicAdd(&P.counters->z_draws, c.local.z_draws);
                 atomicAdd(&P.counters->iters, c.local.iters);
+                for (int q = 0; q < 8; q++) atomicAdd(&P.counters->phase_cycles[q], c.local.phase_cycles[q]);
             }
             atomicAdd(&P.counters->pmat, c.local.pmat);
         }

@@ -1747,6 +1747,7 @@ static int run_pending(pacc_ctx* c) {
     pc.z_draws = (double)dc.z_draws;
     pc.pmatrix_builds = (double)dc.pmat;
     pc.iterations = (double)dc.iters;
+    for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
     pc.kernel_ms = ms;
     pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
     collect_results(c, res, mz, pz, trd, trz, TI, clk_khz);
@@ -2046,6 +2047,7 @@ int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
             cudaEventDestroy(now);
             running_ms = ms;
         }
+        for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
         pc.kernel_ms = c->ss.kernel_ms + running_ms;
         pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
         pc.iterations = (double)c->ss.launches;
