@@ -352,6 +352,8 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
 // eigen formula whatever the branch length.
 template <typename Real>
 __device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
+    // FP64 throughout: the eigen products cancel for the small entries of
+    // short branches, which FP32 arithmetic would not resolve
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
         int s = c.nodes[i];
         double* out = c.ptd + ((size_t)k * c.N + s) * 16;
@@ -434,35 +436,59 @@ __device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
         uint64_t w = pos + (uint64_t)c.prefix[g];
         uint64_t blk = ~0ull;
         uint32_t words[4];
-        auto next_u = [&]() {
+        auto next_word = [&]() {
             uint64_t b = w >> 2;
             if (b != blk) {
                 philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, words);
                 blk = b;
             }
-            double u = word_to_uniform(words[w & 3]);
-            w++;
-            return u;
+            return words[(w++) & 3];
+        };
+        // the draw: FP64 for FP64 partials (as the oracle), FP32 for FP32 partials
+        auto draw4 = [&](const Real* q) -> int {
+            const uint32_t wd = next_word();
+            if (sizeof(Real) == 8) return categorical(4, q, word_to_uniform(wd));
+            const float u = ((float)(wd >> 8) + 0.5f) * 5.9604644775390625e-08f;
+            const float tot = ((float)q[0] + (float)q[1]) + ((float)q[2] + (float)q[3]);
+            const float t = u * tot;
+            float cum = 0;
+            for (int k = 0; k < 4; k++) {
+                cum += (float)q[k];
+                if (t < cum) return k;
+            }
+            for (int k = 3; k >= 0; k--)
+                if (q[k] > 0) return k;
+            return 4;
         };
         Real p[4];
         const Real* Lr = c.L(rbuf, rir, 0);
 #pragma unroll
         for (int j = 0; j < 4; j++) p[j] = Lr[j * c.GGp + g];
-        int nn = categorical(4, p, next_u());
+        int nn = draw4(p);
         draws++;
         if (nn > 3) { err = 1; nn = 0; }
         c.tg[(size_t)rir * c.GGp + g] = (int8_t)nn;
+        // the partials of the next node are loaded while this one is drawn
+        auto load_part = [&](int k, Real (&x)[4]) {
+            const int sk = c.internal[k];
+            const Real* Lk = c.L(c.cur[sk], c.irank[sk], 0);
+#pragma unroll
+            for (int i = 0; i < 4; i++) x[i] = Lk[i * c.GGp + g];
+        };
+        Real nxt[4] = {0, 0, 0, 0};
+        if (c.n_int >= 2) load_part(c.n_int - 2, nxt);
         for (int k = c.n_int - 2; k >= 0; k--) {
+            Real lsv[4] = {nxt[0], nxt[1], nxt[2], nxt[3]};
+            if (k >= 1) load_part(k - 1, nxt);
             int s = c.internal[k];
             int ir = c.irank[s];
             if (c.missing[s] || c.tg[(size_t)ir * c.GGp + g] >= KB) continue;
             int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
             const Real* P = c.ptr + ((size_t)mat_class(c.Z[s], -1) * c.N + s) * 16;
-            const Real* Ls = c.L(c.cur[s], ir, 0);
             Real q[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) q[i] = P[i * 4 + tp] * Ls[i * c.GGp + g];
-            int n2 = categorical(4, q, next_u());
+            for (int i = 0; i < 4; i++) q[i] = P[i * 4 + tp] * lsv[i];
+            int n2 = draw4(q);
             draws++;
             if (n2 > 3) { err = 1; n2 = 0; }
             c.tg[(size_t)ir * c.GGp + g] = (int8_t)n2;
@@ -516,7 +542,8 @@ __device__ void emission(Ctx<Real>& c) {
         int s = c.nodes[i / 3];
         int z = i % 3;
         if (c.missing[s]) continue;
-        const double* P = c.ptd + ((size_t)(z == 0 ? P_NULL : (z == 1 ? P_CONS : P_NEUT)) * c.N + s) * 16;
+        const int cls = z == 0 ? P_NULL : (z == 1 ? P_CONS : P_NEUT);
+        const Real* P = c.ptr + ((size_t)cls * c.N + s) * 16;
         double e = 0;
         for (int b = 0; b < NB; b++) {
             int n = c.cnt[s * NB + b];

@@ -452,8 +452,12 @@ struct StreamServer {
     cudaStream_t copy = nullptr;    // admission and result copies, beside the running kernel
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool running = false;
+    // pinned staging, allocated once at setup: cudaFreeHost / cudaMallocHost
+    // synchronise the device, which would wait for the persistent launch
     char* h_stage = nullptr;
     size_t h_stage_cap = 0;
+    char* h_out = nullptr;          // result staging for out_chunk slots
+    int out_chunk = 0;
     ChainParams p;
     std::vector<int> free_slots;
     std::vector<char> busy;
@@ -676,6 +680,7 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->ss.dev) cudaFree(c->ss.dev);
     if (c->ss.h_map) cudaFreeHost(c->ss.h_map);
     if (c->ss.h_stage) cudaFreeHost(c->ss.h_stage);
+    if (c->ss.h_out) cudaFreeHost(c->ss.h_out);
     if (c->ss.copy) cudaStreamDestroy(c->ss.copy);
     if (c->ss.ev0) cudaEventDestroy(c->ss.ev0);
     if (c->ss.ev1) cudaEventDestroy(c->ss.ev1);
@@ -1192,6 +1197,21 @@ static int plain_block_threads(const pacc_ctx* c, int prec) {
 // ---------------------------------------------------------------------------
 // serving with the CTA-per-chain kernel (stream mode)
 // ---------------------------------------------------------------------------
+// Layout of one finished slot's results in the pinned staging (each part
+// 16-byte aligned): result | Max_Z | P(Z) | rate traces | Z traces.
+struct OutLayout {
+    size_t mz, pz, trd, trz, bytes;
+    OutLayout(const StreamServer& v, int N) {
+        auto r16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        mz = r16(sizeof(DevResult));
+        pz = mz + r16(sizeof(int32_t) * 3 * N);
+        trd = pz + r16(sizeof(double) * 3 * N * 4);
+        trz = trd + r16(sizeof(double) * 3 * 6 * (size_t)v.TI);
+        bytes = trz + r16((size_t)3 * v.TI * N);
+    }
+};
+static size_t stream_out_bytes(const StreamServer& v, int N) { return OutLayout(v, N).bytes; }
+
 static int stream_setup(pacc_ctx* c, int GG_needed) {
     StreamServer& v = c->ss;
     if (v.ready) return PACC_OK;
@@ -1252,6 +1272,12 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.h_stop = v.h_map + 1;
     v.h_qslot = v.h_map + 64;
     v.h_done = v.h_map + 64 + ns;
+    // admission staging: at least four elements of the largest size
+    v.h_stage_cap = std::max((size_t)32 << 20, 4 * (v.blob_b + sizeof(ElemHeader) + 64));
+    if (!cuda_ok(c, cudaMallocHost((void**)&v.h_stage, v.h_stage_cap), "cudaMallocHost")) return PACC_OOM;
+    v.out_chunk = (int)std::max<size_t>(1, std::min<size_t>(ns, ((size_t)16 << 20) / stream_out_bytes(v, N)));
+    if (!cuda_ok(c, cudaMallocHost((void**)&v.h_out, stream_out_bytes(v, N) * v.out_chunk), "cudaMallocHost"))
+        return PACC_OOM;
     if (!cuda_ok(c, cudaStreamCreateWithFlags(&v.copy, cudaStreamNonBlocking), "stream") ||
         !cuda_ok(c, cudaEventCreate(&v.ev0), "event") || !cuda_ok(c, cudaEventCreate(&v.ev1), "event"))
         return PACC_ECUDA;
@@ -1314,20 +1340,16 @@ static int stream_admit(pacc_ctx* c) {
     auto staged = [&](const HostElem& E) {
         return E.codes.size() + E.tg0.size() + E.prefix.size() * 4 + tb + sizeof(ElemHeader) + 64;
     };
-    size_t tot = 0;
-    for (auto& a : adm) tot += staged(a.second.first);
-    if (tot > v.h_stage_cap) {
-        if (v.h_stage) cudaFreeHost(v.h_stage);
-        v.h_stage = nullptr;
-        v.h_stage_cap = 0;
-        if (!cuda_ok(c, cudaMallocHost((void**)&v.h_stage, tot * 2), "cudaMallocHost")) return PACC_OOM;
-        v.h_stage_cap = tot * 2;
-    }
     size_t off = 0;
     cudaStream_t st = v.copy;
     for (auto& a : adm) {
         const int slot = a.first;
         const HostElem& E = a.second.first;
+        if (off + staged(E) > v.h_stage_cap) {
+            // staging full: wait for its copies, then reuse it
+            if (!cuda_ok(c, cudaStreamSynchronize(st), "admission")) return PACC_ECUDA;
+            off = 0;
+        }
         char* reg = v.d_blob + (size_t)slot * v.blob_b;
         ElemHeader H;
         std::memset(&H, 0, sizeof(H));
@@ -1354,8 +1376,10 @@ static int stream_admit(pacc_ctx* c) {
                   cuda_ok(c, cudaMemcpyAsync(reg + v.o_tg, p1, E.tg0.size(), cudaMemcpyHostToDevice, st), "H2D tg") &&
                   cuda_ok(c, cudaMemcpyAsync(reg + v.o_prefix, p2, E.prefix.size() * 4, cudaMemcpyHostToDevice, st), "H2D prefix") &&
                   cuda_ok(c, cudaMemcpyAsync(reg + v.o_topo, p3, tb, cudaMemcpyHostToDevice, st), "H2D topo") &&
-                  cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, p4, sizeof(H), cudaMemcpyHostToDevice, st), "H2D header") &&
-                  cuda_ok(c, cudaMemsetAsync(v.d_res + slot, 0, sizeof(DevResult), st), "memset result");
+                  cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, p4, sizeof(H), cudaMemcpyHostToDevice, st), "H2D header");
+        // (no memset here: a memset is a kernel, which would wait for the
+        // persistent launch to leave room on the SMs; the kernel writes every
+        // result field of the slot before it raises the slot's flag)
         if (!ok) return PACC_ECUDA;
         off += staged(E);
         v.slot_no[slot] = E.no;
@@ -1386,60 +1410,65 @@ static int stream_retire(pacc_ctx* c) {
     std::atomic_thread_fence(std::memory_order_seq_cst);
     const int nd = (int)fin.size();
     cudaStream_t st = v.copy;
-    std::vector<DevResult> res(nd);
-    std::vector<int32_t> mz((size_t)nd * 3 * N);
-    std::vector<double> pz((size_t)nd * 3 * N * 4);
     const size_t trd_n = (size_t)3 * 6 * v.TI, trz_n = (size_t)3 * v.TI * N;
-    std::vector<double> trd(trd_n * nd);
-    std::vector<int8_t> trz(trz_n * nd);
-    for (int i = 0; i < nd; i++) {
-        const int slot = fin[i];
-        cudaMemcpyAsync(&res[i], v.d_res + slot, sizeof(DevResult), cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(&mz[(size_t)i * 3 * N], v.d_mz + (size_t)slot * 3 * N, sizeof(int32_t) * 3 * N,
-                        cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(&pz[(size_t)i * 3 * N * 4], v.d_pz + (size_t)slot * 3 * N * 4, sizeof(double) * 3 * N * 4,
-                        cudaMemcpyDeviceToHost, st);
-        if (v.TI > 0) {
-            cudaMemcpyAsync(&trd[trd_n * i], v.d_trd + trd_n * slot, sizeof(double) * trd_n, cudaMemcpyDeviceToHost, st);
-            cudaMemcpyAsync(&trz[trz_n * i], v.d_trz + trz_n * slot, trz_n, cudaMemcpyDeviceToHost, st);
-        }
-    }
-    if (!cuda_ok(c, cudaStreamSynchronize(st), "D2H results")) return PACC_ECUDA;
+    const OutLayout L(v, N);
+    const size_t ob = L.bytes;
     int clk_khz = 0;
     cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, c->device);
-    const double t = now_ms();
-    for (int i = 0; i < nd; i++) {
-        const int slot = fin[i];
-        pacc_ctx::Done d;
-        std::memset(&d.r, 0, sizeof(d.r));
-        d.r.element_no = v.slot_no[slot];
-        d.r.n_nodes = N;
-        const DevResult& R = res[i];
-        d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
-        for (int m = 0; m < 3; m++) {
-            pacc_model_result& mr = d.r.model[m];
-            mr.loglik = R.model[m].loglik;
-            mr.max_loglik = R.model[m].max_loglik;
-            mr.n_rate = R.model[m].rates[0];
-            mr.c_rate = R.model[m].rates[1];
-            mr.g_rate = R.model[m].rates[2];
-            mr.l_rate = R.model[m].rates[3];
-            mr.l2_rate = R.model[m].rates[4];
-            mr.failure = R.model[m].failure;
-            mr.n_configs = R.model[m].n_configs;
+    for (int i0 = 0; i0 < nd; i0 += v.out_chunk) {
+        const int n = std::min(v.out_chunk, nd - i0);
+        // per slot in the pinned staging: result | Max_Z | P(Z) | traces
+        auto res_of = [&](int i) { return (DevResult*)(v.h_out + ob * i); };
+        auto mz_of = [&](int i) { return (int32_t*)(v.h_out + ob * i + L.mz); };
+        auto pz_of = [&](int i) { return (double*)(v.h_out + ob * i + L.pz); };
+        auto trd_of = [&](int i) { return (double*)(v.h_out + ob * i + L.trd); };
+        auto trz_of = [&](int i) { return (int8_t*)(v.h_out + ob * i + L.trz); };
+        for (int i = 0; i < n; i++) {
+            const int slot = fin[i0 + i];
+            cudaMemcpyAsync(res_of(i), v.d_res + slot, sizeof(DevResult), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(mz_of(i), v.d_mz + (size_t)slot * 3 * N, sizeof(int32_t) * 3 * N, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(pz_of(i), v.d_pz + (size_t)slot * 3 * N * 4, sizeof(double) * 3 * N * 4,
+                            cudaMemcpyDeviceToHost, st);
+            if (v.TI > 0) {
+                cudaMemcpyAsync(trd_of(i), v.d_trd + trd_n * slot, sizeof(double) * trd_n, cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(trz_of(i), v.d_trz + trz_n * slot, trz_n, cudaMemcpyDeviceToHost, st);
+            }
         }
-        d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
-        d.r.latency_ms = t - v.slot_t0[slot];
-        d.max_z.assign(mz.begin() + (size_t)i * 3 * N, mz.begin() + (size_t)(i + 1) * 3 * N);
-        d.post_z.assign(pz.begin() + (size_t)i * 3 * N * 4, pz.begin() + (size_t)(i + 1) * 3 * N * 4);
-        if (v.TI > 0) {
-            d.tr_d.assign(trd.begin() + trd_n * i, trd.begin() + trd_n * (i + 1));
-            d.tr_z.assign(trz.begin() + trz_n * i, trz.begin() + trz_n * (i + 1));
+        if (!cuda_ok(c, cudaStreamSynchronize(st), "D2H results")) return PACC_ECUDA;
+        const double t = now_ms();
+        for (int i = 0; i < n; i++) {
+            const int slot = fin[i0 + i];
+            pacc_ctx::Done d;
+            std::memset(&d.r, 0, sizeof(d.r));
+            d.r.element_no = v.slot_no[slot];
+            d.r.n_nodes = N;
+            const DevResult& R = *res_of(i);
+            d.r.status = R.status == 0 ? PACC_OK : (R.status == 2 ? PACC_NAN_LIKELIHOOD : PACC_SAMPLER_ERROR);
+            for (int m = 0; m < 3; m++) {
+                pacc_model_result& mr = d.r.model[m];
+                mr.loglik = R.model[m].loglik;
+                mr.max_loglik = R.model[m].max_loglik;
+                mr.n_rate = R.model[m].rates[0];
+                mr.c_rate = R.model[m].rates[1];
+                mr.g_rate = R.model[m].rates[2];
+                mr.l_rate = R.model[m].rates[3];
+                mr.l2_rate = R.model[m].rates[4];
+                mr.failure = R.model[m].failure;
+                mr.n_configs = R.model[m].n_configs;
+            }
+            d.r.device_ms = clk_khz > 0 ? R.device_ms / (double)clk_khz : 0.0;
+            d.r.latency_ms = t - v.slot_t0[slot];
+            d.max_z.assign(mz_of(i), mz_of(i) + 3 * N);
+            d.post_z.assign(pz_of(i), pz_of(i) + 3 * N * 4);
+            if (v.TI > 0) {
+                d.tr_d.assign(trd_of(i), trd_of(i) + trd_n);
+                d.tr_z.assign(trz_of(i), trz_of(i) + trz_n);
+            }
+            c->done.push_back(std::move(d));
+            v.busy[slot] = 0;
+            v.free_slots.push_back(slot);
+            v.resident--;
         }
-        c->done.push_back(std::move(d));
-        v.busy[slot] = 0;
-        v.free_slots.push_back(slot);
-        v.resident--;
     }
     return PACC_OK;
 }
