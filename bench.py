@@ -281,14 +281,24 @@ def run_gpu(args, ws, rank, local):
     o32.device = 0
     o32.sweeps_per_launch = args.serve_sweeps
     ctx32 = pg.Context(ds, o32)
-    serve_stream(ctx32, ds, W, ws)                       # W warm-up steps
     clocks = ClockSampler(local)
-    clocks.start()
-    c0 = ctx32.counters()
-    dev, wall, got = serve_stream(ctx32, ds, K, ws)      # K timed steps
-    clk = clocks.stop()
-    c1 = ctx32.counters()
-    cnt = {k: c1[k] - c0[k] for k in ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "flop")}
+    keys = ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "flop")
+    if args.serve_sweeps > 0:
+        serve_stream(ctx32, ds, W, ws)                   # W warm-up steps
+        clocks.start()
+        c0 = ctx32.counters()
+        dev, wall, got = serve_stream(ctx32, ds, K, ws)  # K timed steps
+        clk = clocks.stop()
+        c1 = ctx32.counters()
+        cnt = {k: c1[k] - c0[k] for k in keys}
+        launches = int(c1["iterations"] - c0["iterations"])
+    else:
+        # the same kernel without serving: one launch per batch of E elements
+        kern, walls, c_last, res = time_gpu(ctx32, ds, K, W, ws, clocks)
+        clk = clocks.stop()
+        dev, wall, got = float(np.sum(kern)), float(np.sum(walls)), [res]
+        cnt = {k: c_last[k] * K for k in keys}          # every step runs the same batch
+        launches = K
     value = ws * E * K / dev
     e2e = ws * E * K / wall
     h2d = int(ds.bases.nbytes + ds.lengths.nbytes + ds.offsets.nbytes)
@@ -311,12 +321,13 @@ def run_gpu(args, ws, rank, local):
         "warmup": W, "ms_per_step": dev / K * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32-partials+fp64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "elements_per_step": E,
-                   "path": "FP32 partials, served and batched: one CTA per chain, a persistent kernel taking "
-                           "elements from a host-fed queue (continuous batching)",
+                   "path": ("FP32 partials, served and batched: one CTA per chain, a persistent kernel taking "
+                            "elements from a host-fed queue (continuous batching)") if args.serve_sweeps > 0 else
+                           "FP32 partials, batched: one CTA per chain, one launch per batch",
                    "l2": "inputs larger than L2 (resident chain state and partial buffers)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(c1["iterations"] - c0["iterations"]),
+        "gpu_launches": launches,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": None,
                      "work": "36 flop per internal-child edge-column + 4 per leaf-child edge-column (device counters)",
@@ -358,7 +369,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the 80%%-load serving run (0: skip)")
     ap.add_argument("--serve-sweeps", type=int, default=64,
-                    help="sweep budget per serving step (x256 columns per chain)")
+                    help="serving on (>0) or off (0: one batched launch per step, the form an ncu "
+                         "capture can replay)")
     ap.add_argument("--burnin", type=int, default=500, help="profiling only: shorter chains")
     ap.add_argument("--mcmc", type=int, default=1500, help="profiling only: shorter chains")
     args = ap.parse_args()

@@ -237,6 +237,17 @@ __device__ __forceinline__ int mat_class(int z, int prop_class) {
 // mh = false: results overwrite the current buffer of each node (Update_Tg with
 // visited masks, bpp_c.cpp:647-671).  mh = true: results go to the other
 // buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928).  Returns the summed
+// One row of a 4x4 matrix (16-byte aligned rows: matrices are 16 entries
+// apart from an aligned base).
+__device__ __forceinline__ void ld_row(const float* p, float (&r)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+}
+__device__ __forceinline__ void ld_row(const double* p, double (&r)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
+}
+
 // per-column log-likelihood at the root (valid when the root is flagged).
 template <typename Real>
 __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
@@ -254,16 +265,19 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
         int ir = c.irank[s];
         int dst = mh ? (1 - c.cur[s]) : c.cur[s];
         int ch[2] = {c.c2a[s], c.c2b[s]};
+        // FP32: the children's matrices are read row by row from shared
+        // memory (broadcast loads) rather than held in registers; FP64 holds
+        // them in registers.  No register array is indexed by a runtime value.
         Real P0[16], P1[16];
         bool use[2];
         int csrc[2], cir[2];
         use[0] = !c.missing[ch[0]];
         use[1] = !c.missing[ch[1]];
-        {
-            const Real* p0 = c.ptr + ((size_t)mat_class(c.Z[ch[0]], prop_class) * c.N + ch[0]) * 16;
-            const Real* p1 = c.ptr + ((size_t)mat_class(c.Z[ch[1]], prop_class) * c.N + ch[1]) * 16;
+        const Real* pm0 = c.ptr + ((size_t)mat_class(c.Z[ch[0]], prop_class) * c.N + ch[0]) * 16;
+        const Real* pm1 = c.ptr + ((size_t)mat_class(c.Z[ch[1]], prop_class) * c.N + ch[1]) * 16;
+        if (sizeof(Real) == 8) {
 #pragma unroll
-            for (int i = 0; i < 16; i++) { P0[i] = p0[i]; P1[i] = p1[i]; }
+            for (int i = 0; i < 16; i++) { P0[i] = pm0[i]; P1[i] = pm1[i]; }
         }
         for (int q = 0; q < 2; q++) {
             cir[q] = ch[q] >= c.S ? c.irank[ch[q]] : -1;
@@ -280,14 +294,16 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     if (!use[q]) continue;
-                    const Real* P = q ? P1 : P0;
+                    const Real* PM = q ? pm1 : pm0;
                     int cc = ch[q];
                     if (cc < c.S) {
                         int code = c.codes[(size_t)cc * c.GGp + g];
                         if (code == CODE_GAP || code == CODE_OTHER) continue;
                         if (code < 4) {
+                            Real r[4];
+                            ld_row(PM + code * 4, r);
 #pragma unroll
-                            for (int j = 0; j < 4; j++) a[j] *= P[code * 4 + j];
+                            for (int j = 0; j < 4; j++) a[j] *= r[j];
                         } else {
                             int msk = ambig_mask(code - CODE_R);
                             Real v[4] = {0, 0, 0, 0};
@@ -295,7 +311,7 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
                             for (int i = 0; i < 4; i++)
                                 if (msk & (1 << i)) {
 #pragma unroll
-                                    for (int j = 0; j < 4; j++) v[j] += P[i * 4 + j];
+                                    for (int j = 0; j < 4; j++) v[j] += PM[i * 4 + j];
                                 }
 #pragma unroll
                             for (int j = 0; j < 4; j++) a[j] *= v[j];
@@ -305,12 +321,20 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
                         if (c.tg[(size_t)cir[q] * c.GGp + g] >= KB) continue;
                         const Real* Lc = c.L(csrc[q], cir[q], 0);
                         Real x0 = Lc[g], x1 = Lc[g + c.GGp], x2 = Lc[g + 2 * c.GGp], x3 = Lc[g + 3 * c.GGp];
+                        Real r0[4], r1[4], r2[4], r3[4];
+                        if (sizeof(Real) == 8) {
+                            const Real* P = q ? P1 : P0;
+#pragma unroll
+                            for (int j = 0; j < 4; j++) { r0[j] = P[j]; r1[j] = P[4 + j]; r2[j] = P[8 + j]; r3[j] = P[12 + j]; }
+                        } else {
+                            ld_row(PM, r0); ld_row(PM + 4, r1); ld_row(PM + 8, r2); ld_row(PM + 12, r3);
+                        }
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            Real v = P[j] * x0;
-                            v += P[4 + j] * x1;
-                            v += P[8 + j] * x2;
-                            v += P[12 + j] * x3;
+                            Real v = r0[j] * x0;
+                            v += r1[j] * x1;
+                            v += r2[j] * x2;
+                            v += r3[j] * x3;
                             a[j] *= v;
                         }
                         sc += c.SC(csrc[q], cir[q])[g];
@@ -435,14 +459,19 @@ __device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
     for (int g = threadIdx.x; g < c.GG; g += blockDim.x) {
         uint64_t w = pos + (uint64_t)c.prefix[g];
         uint64_t blk = ~0ull;
-        uint32_t words[4];
+        // the block's four words in scalars (an array indexed by w & 3 would
+        // live in local memory)
+        uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
         auto next_word = [&]() {
             uint64_t b = w >> 2;
             if (b != blk) {
-                philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, words);
+                uint32_t o[4];
+                philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, o);
+                w0 = o[0]; w1 = o[1]; w2 = o[2]; w3 = o[3];
                 blk = b;
             }
-            return words[(w++) & 3];
+            const int i = (int)(w++ & 3);
+            return i == 0 ? w0 : (i == 1 ? w1 : (i == 2 ? w2 : w3));
         };
         // the draw: FP64 for FP64 partials (as the oracle), FP32 for FP32 partials
         auto draw4 = [&](const Real* q) -> int {
@@ -1119,8 +1148,10 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
 // ---------------------------------------------------------------------------
 // The chain kernel
 // ---------------------------------------------------------------------------
+// FP32 runs 256 threads with two blocks per SM (128 registers a thread);
+// FP64 runs 128 threads and may use more registers.
 template <typename Real>
-__global__ void __launch_bounds__(256) chain_kernel(ChainParams P) {
+__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(ChainParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ChainScalars cs_;
     __shared__ int tmp_;
