@@ -99,7 +99,9 @@ struct SmemLayout {
         SmemLayout s;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
-        s.ptd = o; o = al(o + (size_t)4 * N * 16 * 8);                      // double P^T per class [4][N][16]
+        // P^T per class [4][N][16]: FP64 for FP64 partials; FP32 partials keep
+        // only the FP32 copy (the FP64 product is formed in registers)
+        s.ptd = o; o = al(o + (sizeof(Real) == 8 ? (size_t)4 * N * 16 * 8 : 0));
         s.ptr_ = o; o = al(o + (sizeof(Real) == 8 ? 0 : (size_t)4 * N * 16 * sizeof(Real)));
         s.ltm = o; o = al(o + (size_t)N * 9 * 8);                          // log_TM_Int [N][3][3]
         s.emis = o; o = al(o + (size_t)N * 3 * 8);
@@ -193,7 +195,7 @@ struct Ctx {
     int16_t *nodes, *internal, *c2a, *c2b, *par, *irank, *pos, *missing, *upc, *upcc, *hlev_start, *hlev_nodes,
         *dlev_start, *dlev_nodes;
     // shared state
-    double* ptd;              // [4][N][16]
+    double* ptd;              // [4][N][16] (FP64 partials only; null for FP32)
     Real* ptr;                // [4][N][16]
     double* ltm;              // [N][9] log_TM_Int (zc*3+zp)
     double* emis;             // [N][3]
@@ -380,12 +382,17 @@ __device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, 
     // short branches, which FP32 arithmetic would not resolve
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
         int s = c.nodes[i];
-        double* out = c.ptd + ((size_t)k * c.N + s) * 16;
-        if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, out);
-        else identity_pt(out);
-        if (sizeof(Real) != 8) {
+        if (sizeof(Real) == 8) {
+            double* out = c.ptd + ((size_t)k * c.N + s) * 16;
+            if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, out);
+            else identity_pt(out);
+        } else {
+            double tmp[16];
+            if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, tmp);
+            else identity_pt(tmp);
             Real* o2 = c.ptr + ((size_t)k * c.N + s) * 16;
-            for (int q = 0; q < 16; q++) o2[q] = (Real)out[q];
+#pragma unroll
+            for (int q = 0; q < 16; q++) o2[q] = (Real)tmp[q];
         }
         c.local.pmat++;
     }
@@ -397,14 +404,9 @@ __device__ void copy_class(Ctx<Real>& c, const double* dist2, int from, int to) 
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
         int s = c.nodes[i];
         if (dist2[s] < 1e-10) continue;
-        double* a = c.ptd + ((size_t)from * c.N + s) * 16;
-        double* b = c.ptd + ((size_t)to * c.N + s) * 16;
+        const Real* a = c.ptr + ((size_t)from * c.N + s) * 16;
+        Real* b = c.ptr + ((size_t)to * c.N + s) * 16;
         for (int q = 0; q < 16; q++) b[q] = a[q];
-        if (sizeof(Real) != 8) {
-            Real* a2 = c.ptr + ((size_t)from * c.N + s) * 16;
-            Real* b2 = c.ptr + ((size_t)to * c.N + s) * 16;
-            for (int q = 0; q < 16; q++) b2[q] = a2[q];
-        }
     }
 }
 
@@ -1164,8 +1166,8 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
     Ctx<Real> c;
     c.S = S;
     c.N = N;
-    c.ptd = (double*)(smem + L.ptd);
-    c.ptr = (sizeof(Real) == 8) ? (Real*)c.ptd : (Real*)(smem + L.ptr_);
+    c.ptd = (sizeof(Real) == 8) ? (double*)(smem + L.ptd) : nullptr;
+    c.ptr = (sizeof(Real) == 8) ? (Real*)(smem + L.ptd) : (Real*)(smem + L.ptr_);
     c.ltm = (double*)(smem + L.ltm);
     c.emis = (double*)(smem + L.emis);
     c.beta = (double*)(smem + L.beta);
@@ -1521,8 +1523,8 @@ __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, do
     TopoLayout TL = TopoLayout::make(N);
     Ctx<Real> c;
     c.S = S; c.N = N;
-    c.ptd = (double*)(smem + L.ptd);
-    c.ptr = (sizeof(Real) == 8) ? (Real*)c.ptd : (Real*)(smem + L.ptr_);
+    c.ptd = (sizeof(Real) == 8) ? (double*)(smem + L.ptd) : nullptr;
+    c.ptr = (sizeof(Real) == 8) ? (Real*)(smem + L.ptd) : (Real*)(smem + L.ptr_);
     c.red = (double*)(smem + L.red);
     int16_t* t16 = (int16_t*)(smem + L.i16);
     c.nodes = t16 + TL.nodes; c.internal = t16 + TL.internal; c.c2a = t16 + TL.c2a; c.c2b = t16 + TL.c2b;

@@ -1186,12 +1186,15 @@ static int server_step(pacc_ctx* c) {
     return PACC_OK;
 }
 
-// Threads per chain of the CTA-per-chain kernel: the caller's, else 256 with
-// FP32 partials (two chains per SM at 128 registers a thread) and 128 with
-// FP64 (238 registers a thread: two chains per SM).
+// Threads per chain of the CTA-per-chain kernel: the caller's, else 128.
+// With FP32 partials that fits four chains per SM (128 registers a thread,
+// about 54 KB of shared memory a chain at 43 taxa); with FP64 partials two
+// (214 registers a thread).  More chains per SM hide the chain's serial
+// steps better than more threads per chain.
 static int plain_block_threads(const pacc_ctx* c, int prec) {
+    (void)prec;
     if (c->o.block_threads > 0) return c->o.block_threads;
-    return prec == 1 ? 256 : 128;
+    return 128;
 }
 
 // ---------------------------------------------------------------------------
