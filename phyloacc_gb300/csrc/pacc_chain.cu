@@ -289,17 +289,49 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
         Real* Ld = c.L(dst, ir, 0);
         int32_t* Sd = c.SC(dst, ir);
         const int8_t* tgs = c.tg + (size_t)ir * c.GGp;
+        // per child: its codes (leaf) or its bases, partials and scales
+        // (internal node); the branch conditions are the same for the whole block
+        // row offsets (32-bit, fewer registers than pointers): a leaf child's
+        // codes row, or an internal child's base row and partial/scale row
+        const bool leaf0 = ch[0] < c.S, leaf1 = ch[1] < c.S;
+        const int GGp = c.GGp;
+        const int r0 = (leaf0 ? ch[0] : cir[0]) * GGp, r1 = (leaf1 ? ch[1] : cir[1]) * GGp;
+        const int q0 = leaf0 ? 0 : (csrc[0] * c.n_int + cir[0]) * GGp;
+        const int q1 = leaf1 ? 0 : (csrc[1] * c.n_int + cir[1]) * GGp;
         for (int g = threadIdx.x; g < c.GG; g += BT) {
+            // every load of the column is issued before any is used, so that
+            // their latencies overlap (the node's base, then the children's
+            // data, would otherwise be three dependent round trips)
+            const int ts = tgs[g];
+            int k0 = 0, k1 = 0, s0 = 0, s1 = 0;
+            Real x0[4] = {0, 0, 0, 0}, x1[4] = {0, 0, 0, 0};
+            if (use[0]) {
+                if (leaf0) k0 = c.codes[r0 + g];
+                else {
+                    k0 = c.tg[r0 + g];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) x0[i] = c.lam[4 * q0 + i * GGp + g];
+                    s0 = c.scl[q0 + g];
+                }
+            }
+            if (use[1]) {
+                if (leaf1) k1 = c.codes[r1 + g];
+                else {
+                    k1 = c.tg[r1 + g];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) x1[i] = c.lam[4 * q1 + i * GGp + g];
+                    s1 = c.scl[q1 + g];
+                }
+            }
             Real a[4] = {1, 1, 1, 1};
             int sc = 0;
-            if (tgs[g] < KB) {
+            if (ts < KB) {
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     if (!use[q]) continue;
                     const Real* PM = q ? pm1 : pm0;
-                    int cc = ch[q];
-                    if (cc < c.S) {
-                        int code = c.codes[(size_t)cc * c.GGp + g];
+                    if (q ? leaf1 : leaf0) {
+                        const int code = q ? k1 : k0;
                         if (code == CODE_GAP || code == CODE_OTHER) continue;
                         if (code < 4) {
                             Real r[4];
@@ -320,9 +352,8 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
                         }
                         e_leaf++;
                     } else {
-                        if (c.tg[(size_t)cir[q] * c.GGp + g] >= KB) continue;
-                        const Real* Lc = c.L(csrc[q], cir[q], 0);
-                        Real x0 = Lc[g], x1 = Lc[g + c.GGp], x2 = Lc[g + 2 * c.GGp], x3 = Lc[g + 3 * c.GGp];
+                        if ((q ? k1 : k0) >= KB) continue;
+                        const Real* x = q ? x1 : x0;
                         Real r0[4], r1[4], r2[4], r3[4];
                         if (sizeof(Real) == 8) {
                             const Real* P = q ? P1 : P0;
@@ -333,13 +364,13 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
                         }
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
-                            Real v = r0[j] * x0;
-                            v += r1[j] * x1;
-                            v += r2[j] * x2;
-                            v += r3[j] * x3;
+                            Real v = r0[j] * x[0];
+                            v += r1[j] * x[1];
+                            v += r2[j] * x[2];
+                            v += r3[j] * x[3];
                             a[j] *= v;
                         }
-                        sc += c.SC(csrc[q], cir[q])[g];
+                        sc += q ? s1 : s0;
                         e_int++;
                     }
                 }
@@ -549,18 +580,14 @@ __device__ void emission(Ctx<Real>& c) {
             if (c.missing[s]) continue;
             int key = -1;
             if (act) {
+                // both loads before either is used (independent round trips)
+                const int own = (s < c.S) ? (int)c.codes[(size_t)s * c.GGp + g]
+                                          : (int)c.tg[(size_t)c.irank[s] * c.GGp + g];
+                const int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
                 int sym;
-                if (s < c.S) {
-                    int code = c.codes[(size_t)s * c.GGp + g];
-                    sym = code < 4 ? code : (code >= CODE_R ? code - 2 : -1);
-                } else {
-                    int t = c.tg[(size_t)c.irank[s] * c.GGp + g];
-                    sym = t < KB ? t : -1;
-                }
-                if (sym >= 0) {
-                    int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
-                    if (tp >= 0 && tp < 4) key = sym * 4 + tp;
-                }
+                if (s < c.S) sym = own < 4 ? own : (own >= CODE_R ? own - 2 : -1);
+                else sym = own < KB ? own : -1;
+                if (sym >= 0 && tp >= 0 && tp < 4) key = sym * 4 + tp;
             }
             unsigned peers = __match_any_sync(0xffffffffu, key);
             int leader = __ffs(peers) - 1;

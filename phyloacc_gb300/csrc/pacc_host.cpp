@@ -1537,6 +1537,9 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
             E.no = b->element_no ? b->element_no[e] : e;
             if (b->lengths[e] < 0 || !preprocess(c->M, c->o, b->bases + b->offsets[e], b->lengths[e], E, false))
                 bad = 1;
+            // the chain kernels index an element's partials with 32-bit offsets
+            else if ((size_t)8 * c->M.S * (size_t)E.GGp >= (size_t)INT32_MAX)
+                bad = 1;
         }
     };
     std::vector<std::thread> th;
