@@ -544,8 +544,11 @@ __device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
             if (k >= 1) load_part(k - 1, nxt);
             int s = c.internal[k];
             int ir = c.irank[s];
-            if (c.missing[s] || c.tg[(size_t)ir * c.GGp + g] >= KB) continue;
-            int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
+            if (c.missing[s]) continue;
+            // the node's and its parent's bases: both loads before either is used
+            const int own = c.tg[(size_t)ir * c.GGp + g];
+            const int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
+            if (own >= KB) continue;
             const Real* P = c.ptr + ((size_t)mat_class(c.Z[s], -1) * c.N + s) * 16;
             Real q[4];
 #pragma unroll
@@ -1124,16 +1127,27 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
         build_class(c, dist2, P_CONS, rc, true, true);
         if (resZ != 0) build_class(c, dist2, P_NEUT, rn, true, true);
         __syncthreads();
+        // one likelihood per configuration.  After the first (a full pass),
+        // only the proper ancestors of branches whose class changed since the
+        // previous configuration are pruned again: a node's partial depends
+        // on its children's classes alone, so every partial, and the
+        // likelihood, is that of a full pass.  When only the root's class
+        // changed no partial changes and the likelihood is the previous one.
+        double ll = 0;
         for (int j = 0; j < nconf; j++) {
             const int8_t* z = (j == 0) ? Zm : c.trz + (size_t)c.first[j] * c.N;
             for (int s = threadIdx.x; s < c.N; s += blockDim.x) {
+                c.unvN[s] = (j == 0) || (c.Z[s] != z[s]);   // free after the chain
                 c.Z[s] = z[s];
-                c.unv[s] = 1;
-                c.cur[s] = 0;
+                if (j == 0) {
+                    c.unv[s] = 1;
+                    c.cur[s] = 0;
+                }
             }
             __syncthreads();
+            if (j > 0) mark_ancestors(c, c.unvN, c.unv, 0, tmp);
             double pz = prior_config(c, z);
-            double ll = prune(c, c.unv, false, -1);
+            if (c.unv[c.root]) ll = prune(c, c.unv, false, -1);
             if (threadIdx.x == 0) SF[j] = __dadd_rn(ll, pz);
             __syncthreads();
         }
