@@ -131,6 +131,20 @@ def make_workload(n, seed):
 ITERS = {"burnin": 500, "mcmc": 1500}
 
 
+# DRAM bytes per column-node update of chain_kernel<float> (ncu capture of
+# 608 elements x 60 iterations: 61.1 GB over 1.666e9 updates)
+DRAM_BYTES_PER_UPDATE = 36.7
+
+
+def hbm_peak_gbs():
+    """The measured copy bandwidth of this machine's GPUs, else the fallback."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s)"
+
+
 def opts_for(precision):
     from phyloacc_gb300 import abi
     o = abi.default_opts()
@@ -316,6 +330,13 @@ def run_gpu(args, ws, rank, local):
         v64 = ws * E64 / float(np.mean(k64))
     fp64_peak, fp32_peak = pg.measure_fma_peak(0)
     achieved = cnt["flop"] / dev
+    updates = (cnt["edge_updates_internal"] + cnt["edge_updates_leaf"]) / 2
+    # DRAM traffic of the launch: bytes per column-node update from one ncu
+    # capture of this kernel on a smaller case of the same workload
+    # (dram__bytes_read.sum + dram__bytes_write.sum, 608 elements x 60
+    # iterations), scaled by the updates this launch made
+    traffic = DRAM_BYTES_PER_UPDATE * updates
+    hbm_peak, hbm_src = hbm_peak_gbs()
     line = {
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": dev / K * 1e3, "higher_is_better": True,
@@ -329,10 +350,14 @@ def run_gpu(args, ws, rank, local):
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
+                     "frac": achieved / fp32_peak, "traffic": traffic,
                      "work": "36 flop per internal-child edge-column + 4 per leaf-child edge-column (device counters)",
-                     "peak_source": "measured FP32 FMA rate of this GPU (pacc_measure_fma_peak)"},
-        "column_node_updates_per_s": (cnt["edge_updates_internal"] + cnt["edge_updates_leaf"]) / 2 / dev,
+                     "peak_source": "measured FP32 FMA rate of this GPU (pacc_measure_fma_peak)",
+                     "traffic_source": "%.1f DRAM bytes per column-node update (ncu, 608 elements x 60 iterations) "
+                                       "x the launch's updates" % DRAM_BYTES_PER_UPDATE,
+                     "hbm": {"achieved": traffic / dev / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": traffic / dev / 1e9 / hbm_peak, "peak_source": hbm_src}},
+        "column_node_updates_per_s": updates / dev,
         "fp64": {"value": v64, "unit": "elements/s", "elements_per_step": E64,
                  "path": "plain FP64, one CTA per chain, one launch",
                  "achieved_tflops": c64["flop"] / float(np.mean(k64)) / 1e12,
