@@ -10,13 +10,14 @@ log-normal (median 250 bp, sigma 0.6, clipped 50-2000); 10% accelerated
 (r2 ~ U[1.5, 4]) and r1 ~ U[0.2, 0.6]; 5% of (taxon, element) pairs missing and
 3% gap cells; BURNIN 500 + MCMC 1500.
 
-A step is one batch of E elements (default 1,216, one per resident chain warp)
-of the FP32-partial path, served and batched: the W warm-up batches and then
-the K timed batches are each submitted at once to a serving context; chains
-are admitted into resident device slots as slots free up and advanced by
-CUDA-graph-captured sweep steps, so a batch's tail overlaps the next batch.
+A step is one batch of E elements (default 1,216: two per resident chain, four
+chains per SM) of the FP32-partial path, served and batched: the W warm-up
+batches and then the K timed batches are each submitted at once to a serving
+context, whose persistent kernel (one CTA per chain) takes elements from a
+host-fed queue as chains finish, so a batch's tail overlaps the next batch.
+--serve-sweeps 0 runs the same kernel as one batched launch per step instead.
 
-value     = K * E / device time of the sweep steps (inputs resident)
+value     = K * E / device time of the persistent launch (inputs resident)
 e2e       = K * E / wall time through pacc_submit/pacc_poll from host buffers
             (preprocessing, H2D admission, sweeps, D2H of results inside)
 fp64      = the plain FP64 path (one CTA per chain, one launch) on a batch of
@@ -387,7 +388,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--elements", type=int, default=1216,
-                    help="elements per step (default: one per resident chain warp, 8 per SM)")
+                    help="elements per step (default: two per resident chain, four chains per SM)")
     ap.add_argument("--fp64-elements", type=int, default=912)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

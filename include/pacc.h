@@ -108,7 +108,7 @@ typedef struct pacc_opts {
     int32_t max_resident;         /* max chains resident at once (0 = derived from the budget) */
     int32_t sweeps_per_launch;    /* MCMC iterations per kernel launch (0 = run chains to completion) */
     int32_t trace_iters;          /* record the first trace_iters iterations of every model (0 = off) */
-    int32_t block_threads;        /* threads per chain CTA (0 = autotuned) */
+    int32_t block_threads;        /* threads per chain CTA (0 = 128) */
     int32_t use_graphs;           /* capture the sweep launches in a CUDA graph (1) */
     int32_t columns_per_lane;     /* batched kernel: alignment columns each lane carries (1, 2 or 4;
                                      0 = autotuned) */
