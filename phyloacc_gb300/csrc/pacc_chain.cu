@@ -103,7 +103,7 @@ struct SmemLayout {
         // only the FP32 copy (the FP64 product is formed in registers)
         s.ptd = o; o = al(o + (sizeof(Real) == 8 ? (size_t)4 * N * 16 * 8 : 0));
         s.ptr_ = o; o = al(o + (sizeof(Real) == 8 ? 0 : (size_t)4 * N * 16 * sizeof(Real)));
-        s.ltm = o; o = al(o + (size_t)N * 9 * 8);                          // log_TM_Int [N][3][3]
+        s.ltm = o; o = al(o + (sizeof(Real) == 8 ? (size_t)N * 9 * 8 : 0));  // log_TM_Int [N][3][3] (FP64 path)
         s.emis = o; o = al(o + (size_t)N * 3 * 8);
         s.beta = o; o = al(o + (size_t)N * 3 * 8);
         s.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 4);                    // emission histogram
@@ -442,8 +442,11 @@ __device__ void copy_class(Ctx<Real>& c, const double* dist2, int from, int to) 
 }
 
 // log_TM_Int from the current g, l, l2 (bpp_c.cpp:301-332, 573-599).
+// Only the log-space Z filter of the FP64 path reads it; the FP32 path's
+// linear filter forms its transition matrix from g, l and l2 directly.
 template <typename Real>
 __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool init) {
+    if (sizeof(Real) != 8) return;
     const double NI = -CUDART_INF;
     // the six logs depend on g, l and l2 only: one evaluation each
     const double lg0 = d_log(1 - gr), lg1 = d_log(gr);
