@@ -333,6 +333,9 @@ int main(int argc, char** argv) {
         return 1;
     }
     if (C.sample_hyper) die("SAMPLE_HYPER is not supported by this build");
+    // CHAIN > 1 continues every element's chains from the last state of the
+    // previous chain (main.cpp:445, bpp_c.cpp:138-151,475-485): not built
+    if (C.chain > 1) die("CHAIN > 1 (continued chains) is not supported by this build");
     Profile prof = load_profile(C.align, C.segment);
     Tree T;
     double pi[4], Q[16];

@@ -3,6 +3,7 @@ trimming, missing taxa, pruning of the outgroup path, bpp_c.hpp:143-476)
 against the oracle.  Runs without a GPU: pacc_create serves the host-only
 entry points when no device is present."""
 import ctypes as C
+import os
 import re
 
 import numpy as np
@@ -140,3 +141,22 @@ def test_site_patterns_bit_exact(kind):
         assert wt.sum() == len(of)
         n_checked += 1
     assert n_checked >= 5
+
+
+@pytest.mark.parametrize("key,value,message", [("CHAIN", "2", "CHAIN > 1"), ("SAMPLE_HYPER", "1", "SAMPLE_HYPER")])
+def test_cli_rejects_unbuilt_modes(tmp_path, key, value, message):
+    """Modes that are not built fail loudly before any device work, instead of
+    running something else."""
+    import shutil
+    import subprocess
+    from phyloacc_gb300.build import build, CLI
+    build()
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "st12_default")
+    for f in ("case.mod", "case.bed", "case.fa"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    (tmp_path / "out").mkdir()
+    lines = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines() if not ln.startswith(key + " ")]
+    (tmp_path / "case.cfg").write_text("\n".join(lines + ["%s %s" % (key, value)]) + "\n")
+    r = subprocess.run([CLI, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert message in r.stderr
