@@ -407,15 +407,24 @@ struct Element {
         }
     }
 
-    // initMCMC (bpp_c.cpp:131-343), iter == 0
-    void initMCMC(int resZ) {
+    // initMCMC (bpp_c.cpp:131-343).  chain == 0: Z = 1 on the tree's nodes,
+    // 0 at the root, -1 elsewhere (bpp_c.cpp:138-146).  A later chain takes
+    // bpp.cur_Z[resZ][CC] (bpp_c.cpp:150), which only SAMPLE_HYPER updates
+    // (bpp_c.cpp:475-477): without it that is the zero vector of bpp.cpp:201,
+    // so the chain starts from Z = 0 on every node.  Everything else (rates,
+    // proposal scales, the draw stream from SEED) starts as in chain 0.
+    void initMCMC(int resZ, int chain = 0) {
         const pacc_opts& o = M.o;
         failure = false;
         prop_c = 1.2;
         prop_n = (double)1 / GG * 10;
-        Z.assign(N, -1);
-        for (int s : nodes) Z[s] = 1;
-        Z[root] = 0;
+        if (chain == 0) {
+            Z.assign(N, -1);
+            for (int s : nodes) Z[s] = 1;
+            Z[root] = 0;
+        } else {
+            Z.assign(N, 0);
+        }
         fixZ.assign(N, -1);
         for (int s : upper_c) fixZ[s] = 1;
         fixZ[root] = 1;
@@ -1008,7 +1017,7 @@ struct Element {
     }
 };
 
-void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* res) {
+void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* res, int chain = 0) {
     const pacc_opts& o = M.o;
     const int N = M.N;
     res->element_no = b->element_no ? b->element_no[e] : e;
@@ -1026,7 +1035,7 @@ void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* re
         for (int mi = 0; mi < 3; mi++) {
             int resZ = resZ_of[mi];
             ModelOut out;
-            E.initMCMC(resZ);
+            E.initMCMC(resZ, chain);
             std::vector<int> maxz;
             double maxll;
             E.Gibbs(resZ, maxll, maxz);
@@ -1084,6 +1093,22 @@ int oracle_run(const pacc_model* model, const pacc_opts* opts, const pacc_elemen
 #pragma omp parallel for schedule(guided) num_threads(n_threads)
 #endif
     for (int e = 0; e < batch->n_elements; e++) run_one(M, batch, e, &out[e]);
+    return PACC_OK;
+}
+
+// The same for chain `chain` of a CHAIN > 1 run (main.cpp:445): each element
+// runs again from SEED with the continued-chain start of initMCMC.
+int oracle_run_chain(const pacc_model* model, const pacc_opts* opts, const pacc_element_batch* batch,
+                     pacc_result* out, int n_threads, int chain) {
+    Model M;
+    if (!build_model(model, opts, M)) return PACC_EINVAL;
+    if (opts->indel != 0) return PACC_EUNSUPPORTED;
+    if (chain < 0) return PACC_EINVAL;
+#ifdef _OPENMP
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel for schedule(guided) num_threads(n_threads)
+#endif
+    for (int e = 0; e < batch->n_elements; e++) run_one(M, batch, e, &out[e], chain);
     return PACC_OK;
 }
 

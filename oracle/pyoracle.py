@@ -25,6 +25,10 @@ def lib():
         L.oracle_run.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts),
                                  C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccResult), C.c_int]
         L.oracle_run.restype = C.c_int
+        L.oracle_run_chain.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts),
+                                       C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccResult), C.c_int,
+                                       C.c_int]
+        L.oracle_run_chain.restype = C.c_int
         L.oracle_encode.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.POINTER(C.c_uint8),
                                     C.c_int32, C.POINTER(C.c_int8), C.POINTER(C.c_int32), C.POINTER(C.c_uint8),
                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
@@ -48,11 +52,16 @@ def lib():
     return _lib
 
 
-def run(ds, opts: abi.PaccOpts, threads: int = 0, element_no=None) -> abi.Results:
+def run(ds, opts: abi.PaccOpts, threads: int = 0, element_no=None, chain: int = 0) -> abi.Results:
+    """Every element through M0, M1, M2 on the CPU.  chain > 0: a later chain
+    of a CHAIN > 1 run (it starts from Z = 0 on every node)."""
     m = abi.ModelArgs(ds)
     b = abi.BatchArgs(ds, element_no)
     res = abi.Results(ds.n_elements, ds.tree.n_nodes, opts.trace_iters)
-    st = lib().oracle_run(C.byref(m.model), C.byref(opts), C.byref(b.batch), res.arr, threads)
+    if chain == 0:
+        st = lib().oracle_run(C.byref(m.model), C.byref(opts), C.byref(b.batch), res.arr, threads)
+    else:
+        st = lib().oracle_run_chain(C.byref(m.model), C.byref(opts), C.byref(b.batch), res.arr, threads, chain)
     if st != abi.PACC_OK:
         raise RuntimeError("oracle_run failed: %d" % st)
     return res

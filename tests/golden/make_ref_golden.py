@@ -7,10 +7,13 @@ oracle/shim (recipe: oracle/build_oracle.py), run with VERBOSE 1 so that it
 also writes its per-iteration traces (_mcmc_trace_M*_*.txt), which are packed
 into traces.npz.
 
-    python tests/golden/make_ref_golden.py /path/to/PhyloAcc
+    python tests/golden/make_ref_golden.py /path/to/PhyloAcc [case ...]
 
-Needs the reference checkout; the fixtures it writes are committed, so the
-tests that use them run anywhere.
+(all cases, or only the named ones).  Needs the reference checkout; the
+fixtures it writes are committed, so the tests that use them run anywhere.
+With CHAIN > 1 the reference appends every chain's rows to the same trace
+file; they are stored per chain (key M{m}_{e} for the first chain,
+M{m}_{e}_c{k} for chain k).
 """
 import glob
 import os
@@ -34,6 +37,8 @@ CASES = {
                      {"PRUNE_TREE": 1, "TRIM_GAP_PERCENT": 0.4, "GAP_PROP": 0.3, "ROPT": 2,
                       "HYPER_LRATE2_A": 0, "ADAPT_FREQ": 25, "INIT_CONSERVE_RATE": 0.3}),
     "st43_default": ("st43", [0, 7, 12], 50, 150, 1, {}),
+    # two chains: the second starts every element from Z = 0 (main.cpp:445, bpp_c.cpp:150)
+    "st12_chain2": ("st12", [0, 85, 90], 60, 150, 2, {"CHAIN": 2}),
 }
 
 
@@ -65,11 +70,13 @@ def read_trace(path):
     return a
 
 
-def main(ref_root):
+def main(ref_root, only=None):
     exe = build_reference(ref_root)
     if exe is None:
         raise SystemExit("reference sources not found under " + ref_root)
     for name, (kind, idx, burn, mcmc, seed, extra) in CASES.items():
+        if only and name not in only:
+            continue
         d = os.path.join(HERE, name)
         if os.path.isdir(d):
             shutil.rmtree(d)
@@ -89,9 +96,13 @@ def main(ref_root):
             raise SystemExit(r.stdout[-2000:] + r.stderr[-2000:])
         out = os.path.join(d, "out")
         traces = {}
+        T = burn + mcmc
         for f in sorted(glob.glob(os.path.join(out, "case_mcmc_trace_M*_*.txt"))):
             tag = os.path.basename(f)[len("case_mcmc_trace_"):-4]  # M{m}_{elem}
-            traces[tag] = read_trace(f)[:200]   # the first 200 iterations are the chain-parity window
+            rows = read_trace(f)
+            for k in range(int(extra.get("CHAIN", 1))):
+                # the first 200 iterations of each chain are the chain-parity window
+                traces[tag + ("_c%d" % k if k else "")] = rows[k * T:k * T + min(T, 200)]
             os.remove(f)
         np.savez_compressed(os.path.join(d, "traces.npz"), **traces)
         os.remove(os.path.join(out, "case_hyper.txt"))
@@ -99,4 +110,4 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])

@@ -8,7 +8,13 @@ from golden_io import CASES, as_float, load_case, ref_tables, ref_traces
 from oracle import pyoracle as po
 
 
-def _check_tables(res, ds, tables, rel=6e-8):
+def _check_tables(res, ds, tables, rel=6e-8, postz_only=False):
+    if not postz_only:
+        _check_lik_and_maxz(res, tables, rel)
+    _check_postz(res, ds, tables)
+
+
+def _check_lik_and_maxz(res, tables, rel):
     # _elem_lik.txt: precision 8
     _, rows = tables["elem_lik"]
     for i, row in enumerate(rows):
@@ -27,6 +33,9 @@ def _check_tables(res, ds, tables, rel=6e-8):
         _, rows = tables["M%d_elem_Z" % m]
         for i, row in enumerate(rows):
             assert [int(x) for x in row[1:]] == res.max_z[i, m].tolist()
+
+
+def _check_postz(res, ds, tables):
     # _rate_postZ_M*.txt: default precision 6
     for m in range(3):
         _, rows = tables["rate_postZ_M%d" % m]
@@ -57,3 +66,36 @@ def test_oracle_matches_reference(case):
         mine = np.stack([res.tr[k][e, m, :T] for k in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
         assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), (case, key)
         assert (res.tr_z[e, m, :T] == a[:, 6:6 + N].astype(np.int8)).all(), (case, key)
+
+
+def test_oracle_matches_reference_continued_chain():
+    """CHAIN 2: the reference runs every element again from SEED, starting
+    from Z = 0 on every node; it appends the second chain's _rate_postZ rows
+    and trace rows and rewrites _elem_lik / _elem_Z with the second chain's."""
+    case = "st12_chain2"
+    ds, o, kv = load_case(case)
+    assert kv["CHAIN"] == "2"
+    o.trace_iters = 200
+    res = [po.run(ds, o, threads=4, chain=k) for k in range(2)]
+    tables = ref_tables(case)
+    n = int(sum(res[0].status() != 1))
+    for k in range(2):
+        part = dict(tables)
+        for m in range(3):
+            hdr, rows = tables["rate_postZ_M%d" % m]
+            assert len(rows) == 2 * n
+            part["rate_postZ_M%d" % m] = (hdr, rows[k * n:(k + 1) * n])
+        _check_tables(res[k], ds, part, postz_only=(k == 0))
+    N = ds.tree.n_nodes
+    tr = ref_traces(case)
+    assert any(key.endswith("_c1") for key in tr)
+    for key, a in tr.items():
+        k = 1 if key.endswith("_c1") else 0
+        m, e = int(key[1]), int(key.split("_")[1])
+        r = res[k]
+        T = a.shape[0]
+        mine = np.stack([r.tr[f][e, m, :T] for f in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
+        assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), (case, key)
+        assert (r.tr_z[e, m, :T] == a[:, 6:6 + N].astype(np.int8)).all(), (case, key)
+    # the second chain really starts elsewhere: Z = 0 on every node at iteration 0
+    assert (res[1].tr_z[:, :, 0] == 0).all()
