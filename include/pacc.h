@@ -112,6 +112,10 @@ typedef struct pacc_opts {
     int32_t use_graphs;           /* capture the sweep launches in a CUDA graph (1) */
     int32_t columns_per_lane;     /* batched kernel: alignment columns each lane carries (1, 2 or 4;
                                      0 = autotuned) */
+    int32_t chain;                /* CHAIN > 1: index of this chain, 0 = the first.  A later chain
+                                     runs every element again from SEED, starting from Z = 0 on
+                                     every node (main.cpp:445, bpp_c.cpp:138-151); PACC_FP64 and
+                                     PACC_FP32 only */
 } pacc_opts;
 
 /* A batch of elements.  Element e's alignment block is n_species rows of

@@ -63,6 +63,7 @@ class PaccOpts(C.Structure):
         ("precision", C.c_int32), ("device", C.c_int32), ("memory_budget_bytes", C.c_int64),
         ("max_resident", C.c_int32), ("sweeps_per_launch", C.c_int32), ("trace_iters", C.c_int32),
         ("block_threads", C.c_int32), ("use_graphs", C.c_int32), ("columns_per_lane", C.c_int32),
+        ("chain", C.c_int32),
     ]
 
 
@@ -83,7 +84,7 @@ def default_opts() -> PaccOpts:
     o.gapchar, o.prune_tree, o.trim_gap_percent, o.min_len, o.indel = ord("-"), 0, 1.0, 50, 0.0
     o.precision, o.device, o.memory_budget_bytes = PACC_FP64, 0, 0
     o.max_resident, o.sweeps_per_launch, o.trace_iters = 0, 0, 0
-    o.block_threads, o.use_graphs, o.columns_per_lane = 0, 1, 0
+    o.block_threads, o.use_graphs, o.columns_per_lane, o.chain = 0, 1, 0, 0
     return o
 
 

@@ -1357,6 +1357,12 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 if (resZ == 0 && s != c.root) c.fixZ[s] = 1;
             }
             __syncthreads();
+            if (P.z_start_zero) {
+                // a later chain starts from bpp.cur_Z, the zero vector unless
+                // SAMPLE_HYPER updates it (bpp_c.cpp:148-151, bpp.cpp:201)
+                for (int i = threadIdx.x; i < N; i += BT) c.Z[i] = 0;
+                __syncthreads();
+            }
             build_class(c, dist2_, P_NULL, 1.0, false, false);
             build_class(c, dist2_, P_NEUT, dM.init_n, true, false);
             build_class(c, dist2_, P_CONS, dM.init_c, true, false);

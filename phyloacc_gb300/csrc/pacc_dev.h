@@ -155,6 +155,7 @@ struct ChainParams {
     volatile int* done_flag;         // host-mapped, per slot: set to 1 once the slot's results are written
     const volatile int* q_stop;      // host-mapped: nonzero asks the blocks to return when idle
     long long idle_ns;               // safety bound: a block idle this long returns even without q_stop
+    int z_start_zero;                // a later chain of a CHAIN > 1 run: Z starts at 0 on every node
 };
 
 // ---- batched (warp-per-chain) kernel ----

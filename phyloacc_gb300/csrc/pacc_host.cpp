@@ -536,6 +536,7 @@ void pacc_default_opts(pacc_opts* o) {
     o->precision = PACC_FP64; o->device = 0; o->memory_budget_bytes = 0; o->max_resident = 0;
     o->sweeps_per_launch = 0; o->trace_iters = 0; o->block_threads = 0; o->use_graphs = 1;
     o->columns_per_lane = 0;
+    o->chain = 0;
 }
 
 // The device model (eigensystem, priors, options) lives in constant memory,
@@ -573,6 +574,9 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     const int S = model->n_species;
     if (S < 2 || S > 256) return fail(PACC_EINVAL, "n_species must be in [2, 256]");
     if (opts->indel != 0) return fail(PACC_EUNSUPPORTED, "INDEL > 0 (five-state model) is not supported");
+    if (opts->chain < 0) return fail(PACC_EINVAL, "chain must be >= 0");
+    if (opts->chain > 0 && opts->precision != PACC_FP64 && opts->precision != PACC_FP32)
+        return fail(PACC_EUNSUPPORTED, "a later chain (chain > 0) needs PACC_FP64 or PACC_FP32");
     if (opts->mcmc < 1 || opts->burnin < 0 || opts->adapt_freq < 1)
         return fail(PACC_EINVAL, "MCMC must be >= 1, BURNIN >= 0, ADAPT_FREQ >= 1");
     pacc_ctx* c = new pacc_ctx();
@@ -1316,6 +1320,7 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.p.done_flag = d_map + 64 + ns;
     v.p.q_stop = d_map + 1;
     v.p.idle_ns = 30000000000LL;   // 30 s: only a safety bound, q_stop ends idle launches
+    v.p.z_start_zero = c->o.chain > 0 ? 1 : 0;
     v.free_slots.clear();
     for (int i = ns - 1; i >= 0; i--) v.free_slots.push_back(i);
     v.busy.assign(ns, 0);
@@ -1746,6 +1751,7 @@ static int run_pending(pacc_ctx* c) {
     p.n_int_max = n_int_max;
     p.GGp_max = GGp_max;
     p.counters = (DevCounters*)(mb + o_cnt);
+    p.z_start_zero = c->o.chain > 0 ? 1 : 0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

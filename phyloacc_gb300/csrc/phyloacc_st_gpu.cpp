@@ -333,9 +333,6 @@ int main(int argc, char** argv) {
         return 1;
     }
     if (C.sample_hyper) die("SAMPLE_HYPER is not supported by this build");
-    // CHAIN > 1 continues every element's chains from the last state of the
-    // previous chain (main.cpp:445, bpp_c.cpp:138-151,475-485): not built
-    if (C.chain > 1) die("CHAIN > 1 (continued chains) is not supported by this build");
     Profile prof = load_profile(C.align, C.segment);
     Tree T;
     double pi[4], Q[16];
@@ -450,65 +447,82 @@ int main(int argc, char** argv) {
             }
         }
     }
-    int st = 0;
-    pacc_ctx* ctx = pacc_create(&model, &C.o, &st);
-    if (!ctx) die(string("pacc_create failed: ") + pacc_last_error(nullptr));
     vector<pacc_result> res(ids.size());
     vector<int32_t> maxz(ids.size() * 3 * N);
     vector<double> postz(ids.size() * 3 * N * 4);
     const int TI = C.o.trace_iters;
     vector<double> tr((size_t)ids.size() * 6 * 3 * std::max(TI, 1));
     vector<int8_t> trz((size_t)ids.size() * 3 * std::max(TI, 1) * N);
-    for (size_t i = 0; i < ids.size(); i++) {
-        std::memset(&res[i], 0, sizeof(pacc_result));
-        res[i].max_z = &maxz[i * 3 * N];
-        res[i].post_z = &postz[i * 3 * N * 4];
-        if (TI > 0) {
-            double* b = &tr[i * 6 * 3 * TI];
-            res[i].trace.loglik = b;
-            res[i].trace.n_rate = b + 3 * TI;
-            res[i].trace.c_rate = b + 6 * TI;
-            res[i].trace.g_rate = b + 9 * TI;
-            res[i].trace.l_rate = b + 12 * TI;
-            res[i].trace.l2_rate = b + 15 * TI;
-            res[i].trace.z = &trz[i * 3 * TI * N];
-        }
-    }
     pacc_element_batch batch;
     batch.n_elements = (int32_t)ids.size();
     batch.element_no = no.data();
     batch.lengths = lens.data();
     batch.offsets = offs.data();
     batch.bases = bases.data();
-    if (!ids.empty()) {
-        st = pacc_run(ctx, &batch, res.data());
-        if (st != PACC_OK) die(string("GPU run failed: ") + pacc_last_error(ctx));
-    }
-    // rate_postZ rows (bpp_c2.cpp:774-784), model files M0, M1 (resZ 2), M2 (resZ 1)
-    for (size_t i = 0; i < ids.size(); i++) {
-        const pacc_result& r = res[i];
-        if (r.status == PACC_FILTERED || r.status == PACC_SAMPLER_ERROR) continue;
-        for (int m = 0; m < 3; m++) {
-            const pacc_model_result& mr = r.model[m];
-            oz[m] << r.element_no << "\t" << mr.n_rate << "\t" << mr.c_rate << "\t" << mr.g_rate << "\t" << mr.l_rate
-                  << "\t" << mr.l2_rate;
-            for (int s = 0; s < N; s++)
-                for (int k = 0; k < 4; k++) oz[m] << "\t" << postz[(i * 3 + m) * N * 4 + s * 4 + k];
-            oz[m] << std::endl;
-            if (C.verbose || mr.failure) {
-                std::ofstream tf((out + "_mcmc_trace_M" + std::to_string(m) + "_" + std::to_string(r.element_no) + ".txt").c_str());
-                tf.precision(8);
-                tf << "loglik\trate_n\trate_c\tgrate\tlrate\tlrate2\t";
-                for (int s = 0; s < N; s++) tf << T.names[s] << "\t";
-                tf << std::endl;
-                const double* b = &tr[i * 6 * 3 * TI];
-                for (int it = 0; it < TI; it++) {
-                    for (int q = 0; q < 6; q++) tf << b[q * 3 * TI + m * TI + it] << "\t";
-                    for (int s = 0; s < N; s++) tf << (int)trz[((i * 3 + m) * TI + it) * N + s] << "\t";
-                    tf << std::endl;
+    double kernel_ms = 0;
+    // CHAIN chains (main.cpp:445): each runs every element from SEED; a later
+    // chain starts from Z = 0 (bpp_c.cpp:148-151).  _rate_postZ rows and
+    // traces are appended per chain, _elem_lik / _elem_Z are the last chain's.
+    for (int chain = 0; chain < std::max(1, C.chain); chain++) {
+        C.o.chain = chain;
+        int st = 0;
+        pacc_ctx* ctx = pacc_create(&model, &C.o, &st);
+        if (!ctx) die(string("pacc_create failed: ") + pacc_last_error(nullptr));
+        for (size_t i = 0; i < ids.size(); i++) {
+            std::memset(&res[i], 0, sizeof(pacc_result));
+            res[i].max_z = &maxz[i * 3 * N];
+            res[i].post_z = &postz[i * 3 * N * 4];
+            if (TI > 0) {
+                double* b = &tr[i * 6 * 3 * TI];
+                res[i].trace.loglik = b;
+                res[i].trace.n_rate = b + 3 * TI;
+                res[i].trace.c_rate = b + 6 * TI;
+                res[i].trace.g_rate = b + 9 * TI;
+                res[i].trace.l_rate = b + 12 * TI;
+                res[i].trace.l2_rate = b + 15 * TI;
+                res[i].trace.z = &trz[i * 3 * TI * N];
+            }
+        }
+        if (!ids.empty()) {
+            st = pacc_run(ctx, &batch, res.data());
+            if (st != PACC_OK) die(string("GPU run failed: ") + pacc_last_error(ctx));
+        }
+        // rate_postZ rows (bpp_c2.cpp:774-784), model files M0, M1 (resZ 2), M2 (resZ 1)
+        for (size_t i = 0; i < ids.size(); i++) {
+            const pacc_result& r = res[i];
+            if (r.status == PACC_FILTERED || r.status == PACC_SAMPLER_ERROR) continue;
+            for (int m = 0; m < 3; m++) {
+                const pacc_model_result& mr = r.model[m];
+                oz[m] << r.element_no << "\t" << mr.n_rate << "\t" << mr.c_rate << "\t" << mr.g_rate << "\t"
+                      << mr.l_rate << "\t" << mr.l2_rate;
+                for (int s = 0; s < N; s++)
+                    for (int k = 0; k < 4; k++) oz[m] << "\t" << postz[(i * 3 + m) * N * 4 + s * 4 + k];
+                oz[m] << std::endl;
+                if (C.verbose || mr.failure) {
+                    // Output_sampling (bpp_c2.cpp:706-736): header with the first chain,
+                    // later chains appended
+                    const string path = out + "_mcmc_trace_M" + std::to_string(m) + "_" +
+                                        std::to_string(r.element_no) + ".txt";
+                    std::ofstream tf(path.c_str(), chain == 0 ? std::ios::out : std::ios::app);
+                    tf.precision(8);
+                    if (chain == 0) {
+                        tf << "loglik\trate_n\trate_c\tgrate\tlrate\tlrate2\t";
+                        for (int s = 0; s < N; s++) tf << T.names[s] << "\t";
+                        tf << std::endl;
+                    }
+                    const double* b = &tr[i * 6 * 3 * TI];
+                    for (int it = 0; it < TI; it++) {
+                        for (int q = 0; q < 6; q++) tf << b[q * 3 * TI + m * TI + it] << "\t";
+                        for (int s = 0; s < N; s++) tf << (int)trz[((i * 3 + m) * TI + it) * N + s] << "\t";
+                        tf << std::endl;
+                    }
                 }
             }
         }
+        pacc_counters pc;
+        pacc_get_counters(ctx, &pc);
+        kernel_ms += pc.kernel_ms;
+        pacc_destroy(ctx);
     }
     // _elem_lik.txt and _M*_elem_Z.txt (bpp.cpp:568-619)
     {
@@ -537,11 +551,8 @@ int main(int argc, char** argv) {
             }
         }
     }
-    pacc_counters pc;
-    pacc_get_counters(ctx, &pc);
-    pacc_destroy(ctx);
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     std::cout << "\n\ntime used:  " << (long)(secs / 60) << " min. (" << secs << " s; GPU kernel "
-              << pc.kernel_ms / 1000.0 << " s)" << std::endl;
+              << kernel_ms / 1000.0 << " s)" << std::endl;
     return 0;
 }

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import phyloacc_gb300 as pg
-from golden_io import CASES, as_float, load_case, read_table, ref_tables, ref_traces
+from golden_io import CASES, as_float, load_case, read_cfg, read_table, ref_tables, ref_traces
 from oracle import pyoracle as po
 from phyloacc_gb300 import abi, synth
 from test_oracle_golden import _check_tables
@@ -134,6 +134,59 @@ def test_cli_drop_in_matches_reference_tables(built, case, tmp_path):
         p = work / "out" / ("case_mcmc_trace_%s_%s.txt" % (m, e))
         got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
         assert np.allclose(got[:a.shape[0]], a, rtol=2e-7, atol=1e-300), key
+
+
+def test_later_chain_matches_oracle(built):
+    """A later chain of a CHAIN > 1 run (every element again from SEED,
+    starting from Z = 0 on every node) reproduces the oracle's chains."""
+    ds, o, kv = load_case("st12_chain2")
+    o.trace_iters = 200
+    o.chain = 1
+    g = pg.Context(ds, o).run()
+    r = po.run(ds, o, threads=4, chain=1)
+    assert (g.tr_z[:, :, 0] == 0).all()
+    assert (g.tr_z == r.tr_z).all()
+    rel = np.abs(g.tr["loglik"] - r.tr["loglik"]) / np.abs(r.tr["loglik"])
+    assert rel.max() < 1e-12
+    mg, mr = g.field("loglik"), r.field("loglik")
+    assert (np.isclose(mg, mr, rtol=1e-10, atol=0) | (np.isinf(mg) & np.isinf(mr))).all()
+    assert (g.max_z == r.max_z).all()
+
+
+def test_cli_two_chains_match_reference(built, tmp_path):
+    """CHAIN 2 through phyloacc-st-gpu: the reference's tables (the second
+    chain's _elem_lik and _elem_Z, both chains' _rate_postZ rows) and both
+    chains' trace rows."""
+    case = "st12_chain2"
+    src = os.path.join(os.path.dirname(__file__), "golden", case)
+    work = tmp_path / case
+    shutil.copytree(src, work)
+    shutil.rmtree(work / "out")
+    os.makedirs(work / "out")
+    r = subprocess.run([pg.CLI_PATH, "case.cfg"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    ref_dir = os.path.join(src, "out")
+    for f in sorted(os.listdir(ref_dir)):
+        h1, rows1 = read_table(os.path.join(ref_dir, f))
+        h2, rows2 = read_table(str(work / "out" / f))
+        assert h1 == h2, f
+        assert len(rows1) == len(rows2), f
+        for a, b in zip(rows1, rows2):
+            assert len(a) == len(b), f
+            for x, y in zip(a, b):
+                if x == y:
+                    continue
+                fx, fy = as_float(x), as_float(y)
+                assert np.isclose(fx, fy, rtol=2e-7, atol=1e-12) or (np.isnan(fx) and np.isnan(fy)), (f, x, y)
+    kv = read_cfg(str(work / "case.cfg"))
+    T = int(kv["BURNIN"]) + int(kv["MCMC"])
+    for key, a in ref_traces(case).items():
+        w = key.split("_")
+        k = 1 if len(w) == 3 else 0
+        p = work / "out" / ("case_mcmc_trace_%s_%s.txt" % (w[0], w[1]))
+        got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
+        assert got.shape[0] == 2 * T
+        assert np.allclose(got[k * T:k * T + a.shape[0]], a, rtol=2e-7, atol=1e-300), key
 
 
 @pytest.mark.parametrize("cols", [1, 2])

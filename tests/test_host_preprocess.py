@@ -143,7 +143,7 @@ def test_site_patterns_bit_exact(kind):
     assert n_checked >= 5
 
 
-@pytest.mark.parametrize("key,value,message", [("CHAIN", "2", "CHAIN > 1"), ("SAMPLE_HYPER", "1", "SAMPLE_HYPER")])
+@pytest.mark.parametrize("key,value,message", [("SAMPLE_HYPER", "1", "SAMPLE_HYPER")])
 def test_cli_rejects_unbuilt_modes(tmp_path, key, value, message):
     """Modes that are not built fail loudly before any device work, instead of
     running something else."""
