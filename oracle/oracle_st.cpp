@@ -202,6 +202,15 @@ struct ModelOut {
 // ---------------------------------------------------------------------------
 // BPP_C: one element (bpp_c.hpp:40-516, bpp_c.cpp, bpp_c2.cpp)
 // ---------------------------------------------------------------------------
+// One element's chain state carried from one SAMPLE_HYPER chain to the next:
+// bpp.cur_Z[1][CC] and bpp.cur_{n,c,g,l,l2}rate[CC] (bpp.hpp:105,137-142),
+// written at the end of Gibbs when UpHyper is set (bpp_c.cpp:475-485).  Z
+// empty: the first chain's start (bpp_c.cpp:138-146).
+struct CarryState {
+    std::vector<int> Z;
+    double n = 0, c = 0, g = 0, l = 0, l2 = 0;
+};
+
 struct Element {
     const Model& M;
     int S, N, GG = 0, CC = 0, root = 0;
@@ -413,12 +422,16 @@ struct Element {
     // (bpp_c.cpp:475-477): without it that is the zero vector of bpp.cpp:201,
     // so the chain starts from Z = 0 on every node.  Everything else (rates,
     // proposal scales, the draw stream from SEED) starts as in chain 0.
-    void initMCMC(int resZ, int chain = 0) {
+    // carry: SAMPLE_HYPER's state (bpp_c.cpp:150,165-177): its Z, when set,
+    // and its rates replace the start values.
+    void initMCMC(int resZ, int chain = 0, const CarryState* carry = nullptr) {
         const pacc_opts& o = M.o;
         failure = false;
         prop_c = 1.2;
         prop_n = (double)1 / GG * 10;
-        if (chain == 0) {
+        if (carry && !carry->Z.empty()) {
+            Z = carry->Z;
+        } else if (chain == 0) {
             Z.assign(N, -1);
             for (int s : nodes) Z[s] = 1;
             Z[root] = 0;
@@ -429,19 +442,19 @@ struct Element {
         for (int s : upper_c) fixZ[s] = 1;
         fixZ[root] = 1;
         MaxLoglik = LOG_ZERO;
-        trace_n_rate[0] = o.init_acce_rate;
-        trace_c_rate[0] = o.init_conserve_rate;
         double init_lrate2 = (o.hyper_lrate2_a == 0) ? 0.0 : o.init_lrate2;  // main.cpp:286
-        trace_l_rate[0] = o.init_lrate;
-        trace_l2_rate[0] = init_lrate2;
-        trace_g_rate[0] = o.init_grate;
+        trace_n_rate[0] = carry ? carry->n : o.init_acce_rate;
+        trace_c_rate[0] = carry ? carry->c : o.init_conserve_rate;
+        trace_l_rate[0] = carry ? carry->l : o.init_lrate;
+        trace_l2_rate[0] = carry ? carry->l2 : init_lrate2;
+        trace_g_rate[0] = carry ? carry->g : o.init_grate;
         for (int s = 0; s < N; s++) tm_null[s] = M.log_cache_TM_null[s];
         for (size_t i = 0; i + 1 < nodes.size(); i++) {
             int s = nodes[i];
             if (distances2[s] > 1e-10) {
                 if (distances2[s] != M.distances[s]) tm_null[s] = log_tm(M, distances2[s], 1.0, false);
-                tm_neut[s] = log_tm(M, distances2[s], o.init_acce_rate, true);
-                tm_cons[s] = log_tm(M, distances2[s], o.init_conserve_rate, true);
+                tm_neut[s] = log_tm(M, distances2[s], trace_n_rate[0], true);
+                tm_cons[s] = log_tm(M, distances2[s], trace_c_rate[0], true);
             } else {
                 tm_cons[s] = tm_null[s];
                 tm_neut[s] = tm_null[s];
@@ -1017,7 +1030,10 @@ struct Element {
     }
 };
 
-void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* res, int chain = 0) {
+// carry set: a SAMPLE_HYPER chain — only the full model M2 runs
+// (main.cpp:466-494), from the carried state, which it then updates.
+void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* res, int chain = 0,
+             CarryState* carry = nullptr) {
     const pacc_opts& o = M.o;
     const int N = M.N;
     res->element_no = b->element_no ? b->element_no[e] : e;
@@ -1032,13 +1048,21 @@ void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* re
     // main.cpp:468-494: M0 (resZ 0), M1 (resZ 2), M2 (resZ 1)
     const int resZ_of[3] = {0, 2, 1};
     try {
-        for (int mi = 0; mi < 3; mi++) {
+        for (int mi = carry ? 2 : 0; mi < 3; mi++) {
             int resZ = resZ_of[mi];
             ModelOut out;
-            E.initMCMC(resZ, chain);
+            E.initMCMC(resZ, chain, carry);
             std::vector<int> maxz;
             double maxll;
             E.Gibbs(resZ, maxll, maxz);
+            if (carry) {   // bpp_c.cpp:475-485: the state where Gibbs stopped
+                carry->Z = E.Z;
+                carry->n = E.trace_n_rate[E.m];
+                carry->c = E.trace_c_rate[E.m];
+                carry->g = E.trace_g_rate[E.m];
+                carry->l = E.trace_l_rate[E.m];
+                carry->l2 = E.trace_l2_rate[E.m];
+            }
             if (o.trace_iters > 0) E.record_trace(out, o.trace_iters);
             bool fail = false;
             int nconf = 0;
@@ -1109,6 +1133,105 @@ int oracle_run_chain(const pacc_model* model, const pacc_opts* opts, const pacc_
 #pragma omp parallel for schedule(guided) num_threads(n_threads)
 #endif
     for (int e = 0; e < batch->n_elements; e++) run_one(M, batch, e, &out[e], chain);
+    return PACC_OK;
+}
+
+// SAMPLE_HYPER: CHAIN chains of M2 over the batch, each from the state the
+// previous one left (main.cpp:445-509), with the hyper-parameters drawn
+// between chains by BPP::sample_hyperparam (bpp.cpp:324-477) from the model's
+// own generator (seeded with SEED, bpp.hpp:177-178).  out: [n_chains][n]
+// results (model[2] filled); hyper: [n_chains + 1][10] = (nprior_a, nprior_b,
+// cprior_a, cprior_b, prior_l_a, prior_l_b, prior_g_a, prior_g_b, prior_l2_a,
+// prior_l2_b), row 0 the starting values and row k + 1 those after chain k.
+int oracle_run_hyper(const pacc_model* model, const pacc_opts* opts, const pacc_element_batch* batch,
+                     int n_chains, pacc_result* out, double* hyper, int n_threads) {
+    Model M0;
+    if (!build_model(model, opts, M0)) return PACC_EINVAL;
+    if (opts->indel != 0) return PACC_EUNSUPPORTED;
+    const int n = batch->n_elements;
+    double h[10] = {opts->acce_prior_a, opts->acce_prior_b, opts->conserve_prior_a, opts->conserve_prior_b,
+                    opts->hyper_lrate_a, opts->hyper_lrate_b, opts->hyper_grate_a, opts->hyper_grate_b,
+                    opts->hyper_lrate2_a, opts->hyper_lrate2_b};
+    for (int q = 0; q < 10; q++) hyper[q] = h[q];
+    // bpp.cpp:215-220: every element starts from the INIT_* values
+    std::vector<CarryState> st(n);
+    for (auto& c : st) {
+        c.n = opts->init_acce_rate;
+        c.c = opts->init_conserve_rate;
+        c.g = opts->init_grate;
+        c.l = opts->init_lrate;
+        c.l2 = (opts->hyper_lrate2_a == 0) ? 0.0 : opts->init_lrate2;   // main.cpp:286
+    }
+    oracle_rng::Stream rng;
+    rng.set(opts->seed);
+#ifdef _OPENMP
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#endif
+    for (int chain = 0; chain < n_chains; chain++) {
+        pacc_opts oc = *opts;
+        oc.acce_prior_a = h[0]; oc.acce_prior_b = h[1];
+        oc.conserve_prior_a = h[2]; oc.conserve_prior_b = h[3];
+        oc.hyper_lrate_a = h[4]; oc.hyper_lrate_b = h[5];
+        oc.hyper_grate_a = h[6]; oc.hyper_grate_b = h[7];
+        oc.hyper_lrate2_a = h[8]; oc.hyper_lrate2_b = h[9];
+        Model M;
+        if (!build_model(model, &oc, M)) return PACC_EINVAL;
+        pacc_result* res = out + (size_t)chain * n;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(guided) num_threads(n_threads)
+#endif
+        for (int e = 0; e < n; e++) run_one(M, batch, e, &res[e], chain, &st[e]);
+        // sample_hyperparam (bpp.cpp:324-477): independent MH on each pair,
+        // sums over the batch's elements in order (filtered ones included
+        // with the values they started from)
+        const double p = 1, r = 1, q = 0.1, s = 0.1;
+        const double vna = 100, vnb = 100, vca = 100, vcb = 100;
+        const double ne = (double)n;
+        double nap = rng.gamma(vna, h[0] / vna);
+        double cap = rng.gamma(vca, h[2] / vca);
+        double nbp = rng.gamma(vnb, h[1] / vnb);
+        double cbp = rng.gamma(vcb, h[3] / vcb);
+        auto rate_ratio = [&](double ap, double bp, double a, double b, double sum_r, double lpr) {
+            double mr = (ap - 1) * (std::log(p) + lpr) - (q + sum_r) / bp - (ne + r) * std::lgamma(ap) -
+                        std::log(bp) * ap * (s + ne);
+            mr -= (a - 1) * (std::log(p) + lpr) - (q + sum_r) / b - (ne + r) * std::lgamma(a) -
+                  std::log(b) * a * (s + ne);
+            return mr;
+        };
+        {
+            double sum_r = 0, lpr = 0;
+            for (int e = 0; e < n; e++) { sum_r += st[e].n; lpr += std::log(st[e].n); }
+            double mr = rate_ratio(nap, nbp, h[0], h[1], sum_r, lpr);
+            double hr = std::log(gamma_pdf(h[0], vna, nap / vna)) - std::log(gamma_pdf(nap, vna, h[0] / vna)) +
+                        std::log(gamma_pdf(h[1], vnb, nbp / vnb)) - std::log(gamma_pdf(nbp, vnb, h[1] / vnb));
+            if (std::log(rng.uniform()) < mr + hr) { h[0] = nap; h[1] = nbp; }
+        }
+        {
+            double sum_r = 0, lpr = 0;
+            for (int e = 0; e < n; e++) { sum_r += st[e].c; lpr += std::log(st[e].c); }
+            double mr = rate_ratio(cap, cbp, h[2], h[3], sum_r, lpr);
+            double hr = std::log(gamma_pdf(h[2], vca, cap / vca)) - std::log(gamma_pdf(cap, vca, h[2] / vca)) +
+                        std::log(gamma_pdf(h[3], vcb, cbp / vcb)) - std::log(gamma_pdf(cbp, vcb, h[3] / vcb));
+            if (std::log(rng.uniform()) < mr + hr) { h[2] = cap; h[3] = cbp; }
+        }
+        // Beta hyper-parameters of l, l2, g: multiplicative U(0.7, 1.3) proposals
+        auto beta_pair = [&](double& a, double& b, double CarryState::*f) {
+            double u = rng.uniform() * (1.3 - 0.7) + 0.7;
+            double ap = a * u;
+            u = rng.uniform() * (1.3 - 0.7) + 0.7;
+            double bp = b * u;
+            double log_p = 0, log_pc = 0;
+            for (int e = 0; e < n; e++) { log_p += std::log(st[e].*f); log_pc += std::log(1 - st[e].*f); }
+            double mr = (ap - a) * (log_p - 1) + (bp - b) * (log_pc - 1);
+            mr += ne * (lnbeta(a, b) - lnbeta(ap, bp));
+            double hr = std::log(a) - std::log(ap) + std::log(b) - std::log(bp);
+            if (std::log(rng.uniform()) < mr + hr) { a = ap; b = bp; }
+        };
+        beta_pair(h[4], h[5], &CarryState::l);
+        beta_pair(h[8], h[9], &CarryState::l2);
+        beta_pair(h[6], h[7], &CarryState::g);
+        for (int k = 0; k < 10; k++) hyper[(size_t)(chain + 1) * 10 + k] = h[k];
+    }
     return PACC_OK;
 }
 

@@ -29,6 +29,10 @@ def lib():
                                        C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccResult), C.c_int,
                                        C.c_int]
         L.oracle_run_chain.restype = C.c_int
+        L.oracle_run_hyper.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts),
+                                       C.POINTER(abi.PaccElementBatch), C.c_int, C.POINTER(abi.PaccResult),
+                                       C.POINTER(C.c_double), C.c_int]
+        L.oracle_run_hyper.restype = C.c_int
         L.oracle_encode.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccOpts), C.POINTER(C.c_uint8),
                                     C.c_int32, C.POINTER(C.c_int8), C.POINTER(C.c_int32), C.POINTER(C.c_uint8),
                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
@@ -65,6 +69,24 @@ def run(ds, opts: abi.PaccOpts, threads: int = 0, element_no=None, chain: int = 
     if st != abi.PACC_OK:
         raise RuntimeError("oracle_run failed: %d" % st)
     return res
+
+
+def run_hyper(ds, opts: abi.PaccOpts, n_chains: int, threads: int = 0, element_no=None):
+    """SAMPLE_HYPER: n_chains chains of M2 over the batch with the
+    hyper-parameters drawn between chains.  Returns (results, hyper): results
+    holds n_chains * n entries, chain k at [k * n, (k + 1) * n) (model 2
+    filled); hyper is [n_chains + 1, 10] (nprior_a, nprior_b, cprior_a,
+    cprior_b, prior_l_a, prior_l_b, prior_g_a, prior_g_b, prior_l2_a,
+    prior_l2_b), row 0 the starting values."""
+    m = abi.ModelArgs(ds)
+    b = abi.BatchArgs(ds, element_no)
+    res = abi.Results(n_chains * ds.n_elements, ds.tree.n_nodes, opts.trace_iters)
+    hyper = np.zeros((n_chains + 1, 10))
+    st = lib().oracle_run_hyper(C.byref(m.model), C.byref(opts), C.byref(b.batch), n_chains, res.arr,
+                                abi.ptr(hyper, C.c_double), threads)
+    if st != abi.PACC_OK:
+        raise RuntimeError("oracle_run_hyper failed: %d" % st)
+    return res, hyper
 
 
 def encode(ds, opts, e: int):

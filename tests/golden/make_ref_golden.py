@@ -39,6 +39,8 @@ CASES = {
     "st43_default": ("st43", [0, 7, 12], 50, 150, 1, {}),
     # two chains: the second starts every element from Z = 0 (main.cpp:445, bpp_c.cpp:150)
     "st12_chain2": ("st12", [0, 85, 90], 60, 150, 2, {"CHAIN": 2}),
+    # SAMPLE_HYPER: three chains of M2, hyper-parameters drawn between chains
+    "st12_hyper": ("st12", [0, 1, 85, 90], 60, 150, 4, {"CHAIN": 3, "SAMPLE_HYPER": 1}),
 }
 
 
@@ -105,7 +107,8 @@ def main(ref_root, only=None):
                 traces[tag + ("_c%d" % k if k else "")] = rows[k * T:k * T + min(T, 200)]
             os.remove(f)
         np.savez_compressed(os.path.join(d, "traces.npz"), **traces)
-        os.remove(os.path.join(out, "case_hyper.txt"))
+        if not extra.get("SAMPLE_HYPER"):
+            os.remove(os.path.join(out, "case_hyper.txt"))   # only the starting values
         print(name, "ok", sorted(os.listdir(out)))
 
 

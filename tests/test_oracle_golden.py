@@ -99,3 +99,59 @@ def test_oracle_matches_reference_continued_chain():
         assert (r.tr_z[e, m, :T] == a[:, 6:6 + N].astype(np.int8)).all(), (case, key)
     # the second chain really starts elsewhere: Z = 0 on every node at iteration 0
     assert (res[1].tr_z[:, :, 0] == 0).all()
+
+
+def test_oracle_matches_reference_sample_hyper():
+    """SAMPLE_HYPER with CHAIN 3: only M2 runs, each chain from the state the
+    previous one left, and the hyper-parameters are drawn between chains.
+    The reference appends per chain a _hyper.txt row, an _elem_lik.txt row
+    per element (No, ID, loglik_all, loglik_Max) and the _rate_postZ_M2 rows."""
+    case = "st12_hyper"
+    ds, o, kv = load_case(case)
+    assert kv["SAMPLE_HYPER"] == "1"
+    K, n, N = int(kv["CHAIN"]), ds.n_elements, ds.tree.n_nodes
+    o.trace_iters = 200
+    res, hyper = po.run_hyper(ds, o, K, threads=4)
+    tables = ref_tables(case)
+    _, rows = tables["hyper"]
+    assert len(rows) == K + 1
+    assert np.allclose([as_float(x) for x in rows[0][1:]], hyper[0, :8])
+    for k in range(K):
+        row = [as_float(x) for x in rows[k + 1]]
+        assert int(row[0]) == k
+        assert np.allclose(row[1:], hyper[k + 1], rtol=6e-6, atol=0), (k, row, hyper[k + 1])
+    assert not np.allclose(hyper[K], hyper[0])          # some proposals were accepted
+    _, rows = tables["elem_lik"]
+    assert len(rows) == K * n
+    st = res.status()
+    for k in range(K):
+        for i in range(n):
+            row = rows[k * n + i]
+            r = res.arr[k * n + i]
+            assert int(row[0]) == i
+            for a, b in zip([r.model[2].loglik, r.model[2].max_loglik], [as_float(x) for x in row[2:]]):
+                if st[k * n + i] == 1:
+                    assert b == 0                           # filtered: the slot's initial zero
+                elif np.isinf(b) or np.isnan(b):
+                    assert a == b or (np.isnan(a) and np.isnan(b))
+                else:
+                    assert abs(a - b) <= 6e-8 * max(1.0, abs(b)), (k, i, a, b)
+    for m in (0, 1):
+        assert tables["rate_postZ_M%d" % m][1] == []
+    _, rows = tables["rate_postZ_M2"]
+    kept = [j for j in range(K * n) if st[j] != 1]
+    assert len(rows) == len(kept)
+    for row, j in zip(rows, kept):
+        row = [as_float(x) for x in row]
+        f = res.arr[j].model[2]
+        mine = [f.n_rate, f.c_rate, f.g_rate, f.l_rate, f.l2_rate] + res.post_z[j, 2].reshape(-1).tolist()
+        assert int(row[0]) == j % n
+        assert np.allclose(mine, row[1:], rtol=6e-6, atol=1e-12), j
+    for key, a in ref_traces(case).items():
+        w = key.split("_")
+        k = int(w[2][1:]) if len(w) == 3 else 0
+        j = k * n + int(w[1])
+        T = a.shape[0]
+        mine = np.stack([res.tr[f][j, 2, :T] for f in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
+        assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), key
+        assert (res.tr_z[j, 2, :T] == a[:, 6:6 + N].astype(np.int8)).all(), key
