@@ -116,6 +116,9 @@ typedef struct pacc_opts {
                                      runs every element again from SEED, starting from Z = 0 on
                                      every node (main.cpp:445, bpp_c.cpp:138-151); PACC_FP64 and
                                      PACC_FP32 only */
+    int32_t sample_hyper;         /* SAMPLE_HYPER chain (main.cpp:466-494): only the full model M2
+                                     runs, from the batch's start states, and every result returns
+                                     its end state; PACC_FP64 and PACC_FP32 without serving */
 } pacc_opts;
 
 /* A batch of elements.  Element e's alignment block is n_species rows of
@@ -128,6 +131,11 @@ typedef struct pacc_element_batch {
     const int32_t* lengths;       /* [n] alignment columns of each element */
     const int64_t* offsets;       /* [n] byte offset of each block in `bases` */
     const uint8_t* bases;
+    /* SAMPLE_HYPER chains (opts.sample_hyper): each element's start state, the
+       bpp.cur_Z[1] / cur_*rate of bpp_c.cpp:148-177, or NULL for the first
+       chain's start (Z = 1 on the tree's nodes; the INIT_* rates) */
+    const int8_t* start_z;        /* [n*N] */
+    const double* start_rates;    /* [n*5]: n, c, g, l, l2 */
 } pacc_element_batch;
 
 /* Per-model summary (one row of _rate_postZ_M*.txt plus _elem_lik.txt fields). */
@@ -160,6 +168,9 @@ typedef struct pacc_result {
     pacc_trace trace;             /* caller buffers or NULL pointers */
     double latency_ms;            /* submit -> result available (serving) */
     double device_ms;             /* time the element's chain spent on the device */
+    /* SAMPLE_HYPER chains: the state where M2's chain stopped (bpp_c.cpp:475-485) */
+    int8_t* end_z;                /* caller buffer [N] or NULL */
+    double end_rates[5];          /* n, c, g, l, l2 */
 } pacc_result;
 
 typedef struct pacc_ctx pacc_ctx;

@@ -1062,6 +1062,10 @@ void run_one(const Model& M, const pacc_element_batch* b, int e, pacc_result* re
                 carry->g = E.trace_g_rate[E.m];
                 carry->l = E.trace_l_rate[E.m];
                 carry->l2 = E.trace_l2_rate[E.m];
+                if (res->end_z)
+                    for (int s = 0; s < N; s++) res->end_z[s] = (int8_t)carry->Z[s];
+                const double v[5] = {carry->n, carry->c, carry->g, carry->l, carry->l2};
+                for (int q = 0; q < 5; q++) res->end_rates[q] = v[q];
             }
             if (o.trace_iters > 0) E.record_trace(out, o.trace_iters);
             bool fail = false;

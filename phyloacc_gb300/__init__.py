@@ -91,9 +91,11 @@ class Context:
     def _err(self, what, st):
         raise PaccError("%s failed (%d): %s" % (what, st, lib().pacc_last_error(self.h).decode()))
 
-    def run(self, ds=None, element_no=None) -> abi.Results:
+    def run(self, ds=None, element_no=None, start_z=None, start_rates=None) -> abi.Results:
+        """Runs a batch to completion.  start_z [n, N] / start_rates [n, 5]:
+        the SAMPLE_HYPER start states (opts.sample_hyper)."""
         ds = self.ds if ds is None else ds
-        b = abi.BatchArgs(ds, element_no)
+        b = abi.BatchArgs(ds, element_no, start_z, start_rates)
         res = abi.Results(ds.n_elements, ds.tree.n_nodes, self.opts.trace_iters)
         st = lib().pacc_run(self.h, C.byref(b.batch), res.arr)
         if st != 0:

@@ -63,7 +63,7 @@ class PaccOpts(C.Structure):
         ("precision", C.c_int32), ("device", C.c_int32), ("memory_budget_bytes", C.c_int64),
         ("max_resident", C.c_int32), ("sweeps_per_launch", C.c_int32), ("trace_iters", C.c_int32),
         ("block_threads", C.c_int32), ("use_graphs", C.c_int32), ("columns_per_lane", C.c_int32),
-        ("chain", C.c_int32),
+        ("chain", C.c_int32), ("sample_hyper", C.c_int32),
     ]
 
 
@@ -84,7 +84,7 @@ def default_opts() -> PaccOpts:
     o.gapchar, o.prune_tree, o.trim_gap_percent, o.min_len, o.indel = ord("-"), 0, 1.0, 50, 0.0
     o.precision, o.device, o.memory_budget_bytes = PACC_FP64, 0, 0
     o.max_resident, o.sweeps_per_launch, o.trace_iters = 0, 0, 0
-    o.block_threads, o.use_graphs, o.columns_per_lane, o.chain = 0, 1, 0, 0
+    o.block_threads, o.use_graphs, o.columns_per_lane, o.chain, o.sample_hyper = 0, 1, 0, 0, 0
     return o
 
 
@@ -95,6 +95,8 @@ class PaccElementBatch(C.Structure):
         ("lengths", _i32p),
         ("offsets", _i64p),
         ("bases", _u8p),
+        ("start_z", C.POINTER(C.c_int8)),
+        ("start_rates", C.POINTER(C.c_double)),
     ]
 
 
@@ -125,6 +127,8 @@ class PaccResult(C.Structure):
         ("trace", PaccTrace),
         ("latency_ms", C.c_double),
         ("device_ms", C.c_double),
+        ("end_z", C.POINTER(C.c_int8)),
+        ("end_rates", C.c_double * 5),
     ]
 
 
@@ -165,7 +169,7 @@ class ModelArgs:
 class BatchArgs:
     """Keeps the numpy buffers behind a PaccElementBatch alive."""
 
-    def __init__(self, ds, element_no=None):
+    def __init__(self, ds, element_no=None, start_z=None, start_rates=None):
         E = ds.n_elements
         self.element_no = np.ascontiguousarray(np.arange(E) if element_no is None else element_no, dtype=np.int64)
         self.lengths = np.ascontiguousarray(ds.lengths, dtype=np.int32)
@@ -177,6 +181,12 @@ class BatchArgs:
         b.lengths = ptr(self.lengths, C.c_int32)
         b.offsets = ptr(self.offsets, C.c_int64)
         b.bases = ptr(self.bases, C.c_uint8)
+        self.start_z = None if start_z is None else np.ascontiguousarray(start_z, dtype=np.int8)
+        self.start_rates = None if start_rates is None else np.ascontiguousarray(start_rates, dtype=np.float64)
+        if self.start_z is not None:
+            b.start_z = ptr(self.start_z, C.c_int8)
+        if self.start_rates is not None:
+            b.start_rates = ptr(self.start_rates, C.c_double)
         self.batch = b
 
 
@@ -197,10 +207,12 @@ class Results:
         self.tr = {k: np.zeros((max(n, 1), 3, T), dtype=np.float64)
                    for k in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")}
         self.tr_z = np.zeros((max(n, 1), 3, T, n_nodes), dtype=np.int8)
+        self.end_z = np.zeros((max(n, 1), n_nodes), dtype=np.int8)
         for i in range(n):
             r = self.arr[i]
             r.max_z = ptr(self.max_z[i], C.c_int32)
             r.post_z = ptr(self.post_z[i], C.c_double)
+            r.end_z = ptr(self.end_z[i], C.c_int8)
             if trace_iters > 0:
                 for k, a in self.tr.items():
                     setattr(r.trace, k, ptr(a[i], C.c_double))

@@ -61,7 +61,8 @@ def build(force=False, verbose=False):
     cli_src = os.path.join(CSRC, "phyloacc_st_gpu.cpp")
     if os.path.exists(cli_src):
         tmp = CLI + ".tmp"
-        _run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", tmp,
+        # -ffp-contract=off: the host's hyper-parameter MH rounds like the oracle's
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", tmp,
               "-L" + OUT, "-lpaccgpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
         os.replace(tmp, CLI)
     return LIB

@@ -1328,7 +1328,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
         for (int i = threadIdx.x; i < N; i += BT) c.maxz[i] = 0;
         __syncthreads();
         const int resZ_of[3] = {0, 2, 1};
-        for (int mi = 0; mi < 3; mi++) {
+        for (int mi = P.first_model; mi < 3; mi++) {
             const int resZ = resZ_of[mi];
             // ---------------- initMCMC (bpp_c.cpp:131-343) ----------------
             if (threadIdx.x == 0) {
@@ -1343,8 +1343,17 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 c.trd[TR_L * T + 0] = dM.init_l;
                 c.trd[TR_L2 * T + 0] = (dM.l2a == 0) ? 0.0 : dM.init_l2;
                 c.trd[TR_G * T + 0] = dM.init_g;
-                cs_.rate_n = dM.init_n;
-                cs_.rate_c = dM.init_c;
+                if (P.start_rates) {
+                    // SAMPLE_HYPER: the rates the previous chain stopped at (bpp_c.cpp:165-177)
+                    const double* sr = P.start_rates + (size_t)e * 5;
+                    c.trd[TR_N * T + 0] = sr[0];
+                    c.trd[TR_C * T + 0] = sr[1];
+                    c.trd[TR_G * T + 0] = sr[2];
+                    c.trd[TR_L * T + 0] = sr[3];
+                    c.trd[TR_L2 * T + 0] = sr[4];
+                }
+                cs_.rate_n = c.trd[TR_N * T + 0];
+                cs_.rate_c = c.trd[TR_C * T + 0];
             }
             for (int i = threadIdx.x; i < N; i += BT) { c.Z[i] = -1; c.fixZ[i] = -1; c.cur[i] = 0; }
             __syncthreads();
@@ -1363,9 +1372,14 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 for (int i = threadIdx.x; i < N; i += BT) c.Z[i] = 0;
                 __syncthreads();
             }
+            if (P.start_z && P.start_z[(size_t)e * N] != -128) {
+                // SAMPLE_HYPER: the Z the previous chain stopped at (bpp_c.cpp:150)
+                for (int i = threadIdx.x; i < N; i += BT) c.Z[i] = P.start_z[(size_t)e * N + i];
+                __syncthreads();
+            }
             build_class(c, dist2_, P_NULL, 1.0, false, false);
-            build_class(c, dist2_, P_NEUT, dM.init_n, true, false);
-            build_class(c, dist2_, P_CONS, dM.init_c, true, false);
+            build_class(c, dist2_, P_NEUT, c.trd[TR_N * T + 0], true, false);
+            build_class(c, dist2_, P_CONS, c.trd[TR_C * T + 0], true, false);
             __syncthreads();
             build_ltm(c, c.trd[TR_G * T], c.trd[TR_L * T], c.trd[TR_L2 * T], true);
             for (int i = threadIdx.x; i < N; i += BT) {
@@ -1479,6 +1493,16 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
             }
 #undef V1_PHASE
             __syncthreads();
+            if (P.end_z) {
+                // the state where the chain stopped (bpp_c.cpp:475-485), before
+                // Eval2 reuses Z
+                for (int i = threadIdx.x; i < N; i += BT) P.end_z[(size_t)e * N + i] = c.Z[i];
+                if (threadIdx.x == 0) {
+                    const int rws[5] = {TR_N, TR_C, TR_G, TR_L, TR_L2};
+                    for (int q = 0; q < 5; q++) P.end_rates[(size_t)e * 5 + q] = c.trd[rws[q] * T + (T - 1)];
+                }
+                __syncthreads();
+            }
             DevModelResult& MR = R->model[mi];
             if (threadIdx.x == 0) MR.max_loglik = cs_.maxll;
             // traces of the first TI iterations

@@ -156,6 +156,14 @@ struct ChainParams {
     const volatile int* q_stop;      // host-mapped: nonzero asks the blocks to return when idle
     long long idle_ns;               // safety bound: a block idle this long returns even without q_stop
     int z_start_zero;                // a later chain of a CHAIN > 1 run: Z starts at 0 on every node
+    // SAMPLE_HYPER chains: models from first_model (2: M2 only); per element
+    // the start state (start_z[e*N] == -128: the first chain's Z) and the
+    // state where M2's chain stopped
+    int first_model;
+    const int8_t* start_z;           // [n][N]
+    const double* start_rates;       // [n][5] n, c, g, l, l2
+    int8_t* end_z;                   // [n][N]
+    double* end_rates;               // [n][5]
 };
 
 // ---- batched (warp-per-chain) kernel ----

@@ -82,6 +82,8 @@ struct HostElem {
     std::vector<uint8_t> missing;  // [N]
     std::vector<int> sord, sflag;  // stack order of internal nodes, pop-order flags
     int stack_depth = 0;
+    std::vector<int8_t> start_z;   // SAMPLE_HYPER start state ([N], empty: the first chain's start)
+    std::vector<double> start_rates;  // [5] n, c, g, l, l2 (empty: the INIT_* values)
 };
 
 static inline uint8_t encode_char(uint8_t ch, char gapchar) {
@@ -487,6 +489,7 @@ struct pacc_ctx {
         std::vector<double> post_z;
         std::vector<double> tr_d;
         std::vector<int8_t> tr_z;
+        std::vector<int8_t> end_z;
     };
     std::vector<Done> done;
     size_t done_head = 0;
@@ -577,6 +580,9 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     if (opts->chain < 0) return fail(PACC_EINVAL, "chain must be >= 0");
     if (opts->chain > 0 && opts->precision != PACC_FP64 && opts->precision != PACC_FP32)
         return fail(PACC_EUNSUPPORTED, "a later chain (chain > 0) needs PACC_FP64 or PACC_FP32");
+    if (opts->sample_hyper &&
+        ((opts->precision != PACC_FP64 && opts->precision != PACC_FP32) || opts->sweeps_per_launch > 0))
+        return fail(PACC_EUNSUPPORTED, "SAMPLE_HYPER chains need PACC_FP64 or PACC_FP32 without serving");
     if (opts->mcmc < 1 || opts->burnin < 0 || opts->adapt_freq < 1)
         return fail(PACC_EINVAL, "MCMC must be >= 1, BURNIN >= 0, ADAPT_FREQ >= 1");
     pacc_ctx* c = new pacc_ctx();
@@ -1545,6 +1551,12 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
             // the chain kernels index an element's partials with 32-bit offsets
             else if ((size_t)8 * c->M.S * (size_t)E.GGp >= (size_t)INT32_MAX)
                 bad = 1;
+            if (c->o.sample_hyper) {
+                const int N = c->M.N;
+                if (b->start_z) E.start_z.assign(b->start_z + (size_t)e * N, b->start_z + (size_t)(e + 1) * N);
+                if (b->start_rates)
+                    E.start_rates.assign(b->start_rates + (size_t)e * 5, b->start_rates + (size_t)(e + 1) * 5);
+            }
         }
     };
     std::vector<std::thread> th;
@@ -1599,7 +1611,8 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
 
 static void collect_results(pacc_ctx* c, const std::vector<DevResult>& res, const std::vector<int32_t>& mz,
                             const std::vector<double>& pz, const std::vector<double>& trd,
-                            const std::vector<int8_t>& trz, int TI, int clk_khz) {
+                            const std::vector<int8_t>& trz, int TI, int clk_khz,
+                            const std::vector<int8_t>& ez, const std::vector<double>& er) {
     const int N = c->M.N;
     const int n = (int)c->pending.size();
     for (int e = 0; e < n; e++) {
@@ -1633,6 +1646,10 @@ static void collect_results(pacc_ctx* c, const std::vector<DevResult>& res, cons
             if (TI > 0) {
                 d.tr_d.assign(trd.begin() + (size_t)e * 3 * 6 * TI, trd.begin() + (size_t)(e + 1) * 3 * 6 * TI);
                 d.tr_z.assign(trz.begin() + (size_t)e * 3 * TI * N, trz.begin() + (size_t)(e + 1) * 3 * TI * N);
+            }
+            if (!ez.empty()) {
+                d.end_z.assign(ez.begin() + (size_t)e * N, ez.begin() + (size_t)(e + 1) * N);
+                for (int q = 0; q < 5; q++) d.r.end_rates[q] = er[(size_t)e * 5 + q];
             }
         }
         c->done.push_back(std::move(d));
@@ -1716,7 +1733,13 @@ static int run_pending(pacc_ctx* c) {
     size_t o_cnt = al(o_trz + (size_t)3 * TI * N * n);
     size_t o_next = al(o_cnt + sizeof(DevCounters));
     size_t o_order = al(o_next + 256);
-    size_t misc = al(o_order + sizeof(int32_t) * n);
+    // SAMPLE_HYPER: start and end states
+    const bool hyp = c->o.sample_hyper != 0;
+    size_t o_sz = al(o_order + sizeof(int32_t) * n);
+    size_t o_sr = al(o_sz + (hyp ? (size_t)N * n : 0));
+    size_t o_ez = al(o_sr + (hyp ? sizeof(double) * 5 * n : 0));
+    size_t o_er = al(o_ez + (hyp ? (size_t)N * n : 0));
+    size_t misc = al(o_er + (hyp ? sizeof(double) * 5 * n : 0));
     if (!grow(c, &c->d_blob, &c->blob_cap, std::max<size_t>(off, 256)) ||
         !grow(c, &c->d_ws, &c->ws_cap, ws1 * grid) || !grow(c, &c->d_misc, &c->misc_cap, misc))
         return PACC_OOM;
@@ -1734,6 +1757,33 @@ static int run_pending(pacc_ctx* c) {
         !cuda_ok(c, cudaMemcpyAsync(mb + o_order, order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
                  "H2D order"))
         return PACC_ECUDA;
+    std::vector<int8_t> sz, ez;
+    std::vector<double> sr, er;
+    if (hyp) {
+        // start states: the caller's, else the first chain's (Z marked -128,
+        // rates from INIT_*, main.cpp:286 for l2)
+        sz.assign((size_t)N * n, 0);
+        sr.assign((size_t)5 * n, 0.0);
+        for (int e = 0; e < n; e++) {
+            const HostElem& E = c->pending[e];
+            if ((int)E.start_z.size() == N) std::memcpy(&sz[(size_t)e * N], E.start_z.data(), N);
+            else sz[(size_t)e * N] = -128;
+            if (E.start_rates.size() == 5) {
+                for (int q = 0; q < 5; q++) sr[(size_t)e * 5 + q] = E.start_rates[q];
+            } else {
+                const pacc_opts& o = c->o;
+                const double l2 = (o.hyper_lrate2_a == 0) ? 0.0 : o.init_lrate2;
+                const double v[5] = {o.init_acce_rate, o.init_conserve_rate, o.init_grate, o.init_lrate, l2};
+                for (int q = 0; q < 5; q++) sr[(size_t)e * 5 + q] = v[q];
+            }
+        }
+        ez.assign((size_t)N * n, 0);
+        er.assign((size_t)5 * n, 0.0);
+        if (!cuda_ok(c, cudaMemcpyAsync(mb + o_sz, sz.data(), sz.size(), cudaMemcpyHostToDevice, st), "H2D start Z") ||
+            !cuda_ok(c, cudaMemcpyAsync(mb + o_sr, sr.data(), sr.size() * 8, cudaMemcpyHostToDevice, st),
+                     "H2D start rates"))
+            return PACC_ECUDA;
+    }
     ChainParams p;
     std::memset(&p, 0, sizeof(p));
     p.hdr = (const ElemHeader*)(mb + o_hdr);
@@ -1752,6 +1802,13 @@ static int run_pending(pacc_ctx* c) {
     p.GGp_max = GGp_max;
     p.counters = (DevCounters*)(mb + o_cnt);
     p.z_start_zero = c->o.chain > 0 ? 1 : 0;
+    if (hyp) {
+        p.first_model = 2;
+        p.start_z = (const int8_t*)(mb + o_sz);
+        p.start_rates = (const double*)(mb + o_sr);
+        p.end_z = (int8_t*)(mb + o_ez);
+        p.end_rates = (double*)(mb + o_er);
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1772,6 +1829,10 @@ static int run_pending(pacc_ctx* c) {
         cudaMemcpyAsync(trz.data(), mb + o_trz, trz.size(), cudaMemcpyDeviceToHost, st);
     }
     cudaMemcpyAsync(&dc, mb + o_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, st);
+    if (hyp) {
+        cudaMemcpyAsync(ez.data(), mb + o_ez, ez.size(), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(er.data(), mb + o_er, er.size() * 8, cudaMemcpyDeviceToHost, st);
+    }
     if (!cuda_ok(c, cudaStreamSynchronize(st), "chain kernel")) return PACC_ECUDA;
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -1791,7 +1852,7 @@ static int run_pending(pacc_ctx* c) {
     for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
     pc.kernel_ms = ms;
     pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
-    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz);
+    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz, ez, er);
     c->pending.clear();
     (void)S;
     return PACC_OK;
@@ -1945,7 +2006,7 @@ static int run_batched(pacc_ctx* c, std::vector<ElemHeader>& hdr, std::vector<ui
     pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
     pc.iterations = (double)launches;
     for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
-    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz);
+    collect_results(c, res, mz, pz, trd, trz, TI, clk_khz, {}, {});
     c->pending.clear();
     return PACC_OK;
 }
@@ -1984,10 +2045,13 @@ static void fill_result(pacc_ctx* c, pacc_ctx::Done& d, pacc_result* out) {
     int32_t* mz = out->max_z;
     double* pz = out->post_z;
     pacc_trace tr = out->trace;
+    int8_t* ez = out->end_z;
     *out = d.r;
     out->max_z = mz;
     out->post_z = pz;
     out->trace = tr;
+    out->end_z = ez;
+    if (ez && !d.end_z.empty()) std::memcpy(ez, d.end_z.data(), (size_t)N);
     if (mz) std::memcpy(mz, d.max_z.data(), sizeof(int32_t) * 3 * N);
     if (pz) std::memcpy(pz, d.post_z.data(), sizeof(double) * 3 * N * 4);
     const int T = c->o.burnin + c->o.mcmc;

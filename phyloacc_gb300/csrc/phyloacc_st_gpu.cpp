@@ -323,6 +323,112 @@ static vector<int> species_ids(const string& list, const vector<string>& names) 
     return out;
 }
 
+// ---------------------------------------------------------------------------
+// SAMPLE_HYPER: the hyper-parameter MH between chains (BPP::sample_hyperparam,
+// bpp.cpp:324-477) on the host.  Its draws come from the model's own
+// generator, seeded with SEED (bpp.hpp:177-178): here a Philox4x32-10 word
+// stream from SEED (Salmon et al., SC'11), the same stream layout and
+// samplers as the chains' (uniform (w + 0.5) 2^-32, Box-Muller normal,
+// Marsaglia-Tsang gamma with the a < 1 boost).
+// ---------------------------------------------------------------------------
+struct HostStream {
+    uint32_t seed = 0;
+    uint64_t pos = 0, blk = ~0ull;
+    uint32_t cache[4] = {0, 0, 0, 0};
+    uint32_t word() {
+        const uint64_t b = pos >> 2;
+        if (b != blk) {
+            uint32_t c0 = (uint32_t)b, c1 = (uint32_t)(b >> 32), c2 = 0, c3 = 0, k0 = seed, k1 = 0;
+            for (int r = 0; r < 10; r++) {
+                const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+                const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+                c1 = (uint32_t)p1; c3 = (uint32_t)p0; c0 = n0; c2 = n2;
+                k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+            }
+            cache[0] = c0; cache[1] = c1; cache[2] = c2; cache[3] = c3;
+            blk = b;
+        }
+        return cache[pos++ & 3];
+    }
+    double uniform() { return ((double)word() + 0.5) * 2.3283064365386963e-10; }
+    double normal() {
+        const double u1 = uniform(), u2 = uniform();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+    double gamma(double a, double b) {
+        if (a < 1.0) {
+            const double g = gamma(a + 1.0, 1.0);
+            const double u = uniform();
+            return b * g * std::pow(u, 1.0 / a);
+        }
+        const double d = a - 1.0 / 3.0, c = 1.0 / std::sqrt(9.0 * d);
+        double x, v;
+        for (;;) {
+            do {
+                x = normal();
+                v = 1.0 + c * x;
+            } while (v <= 0.0);
+            v = v * v * v;
+            const double u = uniform(), x2 = x * x;
+            if (u < 1.0 - 0.0331 * x2 * x2) break;
+            if (std::log(u) < 0.5 * x2 + d * (1.0 - v + std::log(v))) break;
+        }
+        return b * d * v;
+    }
+};
+
+static double gamma_density(double x, double a, double b) {   // the Gamma(a, scale b) density
+    if (x < 0) return 0.0;
+    if (x == 0) return (a == 1) ? 1.0 / b : 0.0;
+    return std::exp((a - 1) * std::log(x) - x / b - std::lgamma(a) - a * std::log(b));
+}
+static double ln_beta(double a, double b) { return std::lgamma(a) + std::lgamma(b) - std::lgamma(a + b); }
+
+// h: nprior_a, nprior_b, cprior_a, cprior_b, prior_l_a, prior_l_b, prior_g_a,
+// prior_g_b, prior_l2_a, prior_l2_b.  rates: [n][5] n, c, g, l, l2 of every
+// element of the run (in id order; filtered elements with their start values).
+static void sample_hyperparam(HostStream& rng, double* h, const vector<double>& rates, int n) {
+    const double p = 1, r = 1, q = 0.1, s = 0.1, ne = (double)n;
+    const double vna = 100, vnb = 100, vca = 100, vcb = 100;
+    const double nap = rng.gamma(vna, h[0] / vna);
+    const double cap = rng.gamma(vca, h[2] / vca);
+    const double nbp = rng.gamma(vnb, h[1] / vnb);
+    const double cbp = rng.gamma(vcb, h[3] / vcb);
+    auto shape_scale = [&](int col, double ap, double bp, double& a, double& b, double va, double vb) {
+        double sum_r = 0, lpr = 0;
+        for (int e = 0; e < n; e++) {
+            sum_r += rates[(size_t)e * 5 + col];
+            lpr += std::log(rates[(size_t)e * 5 + col]);
+        }
+        double mr = (ap - 1) * (std::log(p) + lpr) - (q + sum_r) / bp - (ne + r) * std::lgamma(ap) -
+                    std::log(bp) * ap * (s + ne);
+        mr -= (a - 1) * (std::log(p) + lpr) - (q + sum_r) / b - (ne + r) * std::lgamma(a) - std::log(b) * a * (s + ne);
+        const double hr = std::log(gamma_density(a, va, ap / va)) - std::log(gamma_density(ap, va, a / va)) +
+                          std::log(gamma_density(b, vb, bp / vb)) - std::log(gamma_density(bp, vb, b / vb));
+        if (std::log(rng.uniform()) < mr + hr) { a = ap; b = bp; }
+    };
+    shape_scale(0, nap, nbp, h[0], h[1], vna, vnb);   // accelerated-rate prior
+    shape_scale(1, cap, cbp, h[2], h[3], vca, vcb);   // conserved-rate prior
+    auto beta_pair = [&](int col, double& a, double& b) {
+        double u = rng.uniform() * (1.3 - 0.7) + 0.7;
+        const double ap = a * u;
+        u = rng.uniform() * (1.3 - 0.7) + 0.7;
+        const double bp = b * u;
+        double log_p = 0, log_pc = 0;
+        for (int e = 0; e < n; e++) {
+            log_p += std::log(rates[(size_t)e * 5 + col]);
+            log_pc += std::log(1 - rates[(size_t)e * 5 + col]);
+        }
+        double mr = (ap - a) * (log_p - 1) + (bp - b) * (log_pc - 1);
+        mr += ne * (ln_beta(a, b) - ln_beta(ap, bp));
+        const double hr = std::log(a) - std::log(ap) + std::log(b) - std::log(bp);
+        if (std::log(rng.uniform()) < mr + hr) { a = ap; b = bp; }
+    };
+    beta_pair(3, h[4], h[5]);   // l
+    beta_pair(4, h[8], h[9]);   // l2
+    beta_pair(2, h[6], h[7]);   // g
+}
+
 int main(int argc, char** argv) {
     auto t_start = std::chrono::steady_clock::now();
     std::cout << std::fixed << std::setprecision(4);
@@ -332,7 +438,8 @@ int main(int argc, char** argv) {
         std::cout << "output path doesn't exist or empty!" << std::endl;
         return 1;
     }
-    if (C.sample_hyper) die("SAMPLE_HYPER is not supported by this build");
+    if (C.chain > 1 && !C.sample_hyper && C.o.precision != PACC_FP64 && C.o.precision != PACC_FP32)
+        die("CHAIN > 1: a later chain needs GPU_PRECISION fp64 or fp32");
     Profile prof = load_profile(C.align, C.segment);
     Tree T;
     double pi[4], Q[16];
@@ -460,11 +567,45 @@ int main(int argc, char** argv) {
     batch.offsets = offs.data();
     batch.bases = bases.data();
     double kernel_ms = 0;
-    // CHAIN chains (main.cpp:445): each runs every element from SEED; a later
-    // chain starts from Z = 0 (bpp_c.cpp:148-151).  _rate_postZ rows and
-    // traces are appended per chain, _elem_lik / _elem_Z are the last chain's.
+    // SAMPLE_HYPER (main.cpp:466-509): only M2 runs, each chain from the state
+    // the previous one left (bpp_c.cpp:148-177,475-485); the hyper-parameters
+    // are drawn between chains; _elem_lik.txt gets (loglik_all, loglik_Max)
+    // rows per chain (bpp.cpp:622-634) and no _elem_Z files are written.
+    const bool hyp = C.sample_hyper;
+    C.o.sample_hyper = hyp ? 1 : 0;
+    double hyper[10] = {C.o.acce_prior_a, C.o.acce_prior_b, C.o.conserve_prior_a, C.o.conserve_prior_b,
+                        C.o.hyper_lrate_a, C.o.hyper_lrate_b, C.o.hyper_grate_a, C.o.hyper_grate_b,
+                        C.o.hyper_lrate2_a, C.o.hyper_lrate2_b};
+    HostStream hyper_rng;
+    hyper_rng.seed = C.o.seed;
+    vector<int8_t> state_z, end_z;
+    vector<double> state_rates;
+    if (hyp) {
+        end_z.assign(ids.size() * N, 0);
+        state_rates.resize(ids.size() * 5);
+        for (size_t i = 0; i < ids.size(); i++) {   // bpp.cpp:215-220
+            const double v[5] = {C.o.init_acce_rate, C.o.init_conserve_rate, C.o.init_grate, C.o.init_lrate,
+                                 C.o.init_lrate2};
+            for (int q = 0; q < 5; q++) state_rates[i * 5 + q] = v[q];
+        }
+        std::ofstream ol((out + "_elem_lik.txt").c_str());
+        ol << "No.\tID\tloglik_all\tloglik_Max" << std::endl;
+    }
+    // CHAIN chains (main.cpp:445): each runs every element from SEED; without
+    // SAMPLE_HYPER a later chain starts from Z = 0 (bpp_c.cpp:148-151).
+    // _rate_postZ rows and traces are appended per chain, _elem_lik / _elem_Z
+    // are the last chain's.
     for (int chain = 0; chain < std::max(1, C.chain); chain++) {
-        C.o.chain = chain;
+        C.o.chain = hyp ? 0 : chain;
+        if (hyp) {
+            C.o.acce_prior_a = hyper[0]; C.o.acce_prior_b = hyper[1];
+            C.o.conserve_prior_a = hyper[2]; C.o.conserve_prior_b = hyper[3];
+            C.o.hyper_lrate_a = hyper[4]; C.o.hyper_lrate_b = hyper[5];
+            C.o.hyper_grate_a = hyper[6]; C.o.hyper_grate_b = hyper[7];
+            C.o.hyper_lrate2_a = hyper[8]; C.o.hyper_lrate2_b = hyper[9];
+            batch.start_z = chain > 0 ? state_z.data() : nullptr;
+            batch.start_rates = state_rates.data();
+        }
         int st = 0;
         pacc_ctx* ctx = pacc_create(&model, &C.o, &st);
         if (!ctx) die(string("pacc_create failed: ") + pacc_last_error(nullptr));
@@ -472,6 +613,7 @@ int main(int argc, char** argv) {
             std::memset(&res[i], 0, sizeof(pacc_result));
             res[i].max_z = &maxz[i * 3 * N];
             res[i].post_z = &postz[i * 3 * N * 4];
+            if (hyp) res[i].end_z = &end_z[i * N];
             if (TI > 0) {
                 double* b = &tr[i * 6 * 3 * TI];
                 res[i].trace.loglik = b;
@@ -491,7 +633,7 @@ int main(int argc, char** argv) {
         for (size_t i = 0; i < ids.size(); i++) {
             const pacc_result& r = res[i];
             if (r.status == PACC_FILTERED || r.status == PACC_SAMPLER_ERROR) continue;
-            for (int m = 0; m < 3; m++) {
+            for (int m = hyp ? 2 : 0; m < 3; m++) {
                 const pacc_model_result& mr = r.model[m];
                 oz[m] << r.element_no << "\t" << mr.n_rate << "\t" << mr.c_rate << "\t" << mr.g_rate << "\t"
                       << mr.l_rate << "\t" << mr.l2_rate;
@@ -523,9 +665,29 @@ int main(int argc, char** argv) {
         pacc_get_counters(ctx, &pc);
         kernel_ms += pc.kernel_ms;
         pacc_destroy(ctx);
+        if (hyp) {
+            // the chains' end states become the next start (elements that did
+            // not run keep theirs), then the hyper-parameter MH and the rows
+            if (state_z.empty()) state_z.assign(ids.size() * N, -128);
+            for (size_t i = 0; i < ids.size(); i++) {
+                if (res[i].status == PACC_FILTERED || res[i].status == PACC_SAMPLER_ERROR) continue;
+                std::memcpy(&state_z[i * N], &end_z[i * N], N);
+                for (int q = 0; q < 5; q++) state_rates[i * 5 + q] = res[i].end_rates[q];
+            }
+            sample_hyperparam(hyper_rng, hyper, state_rates, (int)ids.size());
+            std::ofstream h((out + "_hyper.txt").c_str(), std::ios::app);
+            h << chain;
+            for (int q = 0; q < 10; q++) h << "\t" << hyper[q];
+            h << std::endl;
+            std::ofstream ol((out + "_elem_lik.txt").c_str(), std::ios::app);
+            ol.precision(8);
+            for (size_t i = 0; i < ids.size(); i++)
+                ol << ids[i] << "\t" << prof.elem_names[ids[i]] << "\t" << res[i].model[2].loglik << "\t"
+                   << res[i].model[2].max_loglik << std::endl;
+        }
     }
     // _elem_lik.txt and _M*_elem_Z.txt (bpp.cpp:568-619)
-    {
+    if (!hyp) {
         std::ofstream ol((out + "_elem_lik.txt").c_str());
         ol.precision(8);
         ol << "No.\tID\tloglik_Null\tloglik_Acc\tloglik_Full\tlogBF1\tlogBF2\tloglik_Max_M0\tloglik_Max_M1\tloglik_Max_M2"

@@ -189,6 +189,76 @@ def test_cli_two_chains_match_reference(built, tmp_path):
         assert np.allclose(got[k * T:k * T + a.shape[0]], a, rtol=2e-7, atol=1e-300), key
 
 
+def test_sample_hyper_chains_match_oracle(built):
+    """SAMPLE_HYPER chains through the API: M2 only, each chain from the end
+    state the previous one returned, with the priors the oracle's
+    hyper-parameter MH drew; traces, marginal likelihoods and end states equal
+    the oracle's."""
+    ds, o, kv = load_case("st12_hyper")
+    K, n, N = int(kv["CHAIN"]), ds.n_elements, ds.tree.n_nodes
+    o.trace_iters = 200
+    ref, hyper = po.run_hyper(ds, o, K, threads=4)
+    o.sample_hyper = 1
+    start_z, start_rates = None, None
+    for k in range(K):
+        ok = o
+        (ok.acce_prior_a, ok.acce_prior_b, ok.conserve_prior_a, ok.conserve_prior_b, ok.hyper_lrate_a,
+         ok.hyper_lrate_b, ok.hyper_grate_a, ok.hyper_grate_b, ok.hyper_lrate2_a, ok.hyper_lrate2_b) = hyper[k]
+        g = pg.Context(ds, ok).run(start_z=start_z, start_rates=start_rates)
+        for i in range(n):
+            j = k * n + i
+            assert (g.tr_z[i, 2] == ref.tr_z[j, 2]).all(), (k, i)
+            rel = np.abs(g.tr["loglik"][i, 2] - ref.tr["loglik"][j, 2]) / np.abs(ref.tr["loglik"][j, 2])
+            assert rel.max() < 1e-12, (k, i)
+            a, b = g.arr[i].model[2].loglik, ref.arr[j].model[2].loglik
+            assert np.isclose(a, b, rtol=1e-10, atol=0) or (np.isinf(a) and a == b), (k, i, a, b)
+            assert (g.end_z[i] == ref.end_z[j]).all(), (k, i)
+            assert np.allclose(list(g.arr[i].end_rates), list(ref.arr[j].end_rates), rtol=1e-12, atol=0), (k, i)
+            assert g.arr[i].model[0].loglik == 0 and g.arr[i].model[1].loglik == 0
+        start_z = g.end_z[:n].copy()
+        start_rates = np.array([list(g.arr[i].end_rates) for i in range(n)])
+
+
+def _cli_tables_match(src, work):
+    ref_dir = os.path.join(src, "out")
+    for f in sorted(os.listdir(ref_dir)):
+        h1, rows1 = read_table(os.path.join(ref_dir, f))
+        h2, rows2 = read_table(str(work / "out" / f))
+        assert h1 == h2, f
+        assert len(rows1) == len(rows2), f
+        for a, b in zip(rows1, rows2):
+            assert len(a) == len(b), f
+            for x, y in zip(a, b):
+                if x == y:
+                    continue
+                fx, fy = as_float(x), as_float(y)
+                assert np.isclose(fx, fy, rtol=2e-7, atol=1e-12) or (np.isnan(fx) and np.isnan(fy)), (f, x, y)
+
+
+def test_cli_sample_hyper_matches_reference(built, tmp_path):
+    """SAMPLE_HYPER with CHAIN 3 through phyloacc-st-gpu: the reference's
+    _hyper.txt rows, per-chain _elem_lik.txt and _rate_postZ_M2.txt rows, and
+    every chain's M2 trace."""
+    case = "st12_hyper"
+    src = os.path.join(os.path.dirname(__file__), "golden", case)
+    work = tmp_path / case
+    shutil.copytree(src, work)
+    shutil.rmtree(work / "out")
+    os.makedirs(work / "out")
+    r = subprocess.run([pg.CLI_PATH, "case.cfg"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    _cli_tables_match(src, work)
+    kv = read_cfg(str(work / "case.cfg"))
+    T, K = int(kv["BURNIN"]) + int(kv["MCMC"]), int(kv["CHAIN"])
+    for key, a in ref_traces(case).items():
+        w = key.split("_")
+        k = int(w[2][1:]) if len(w) == 3 else 0
+        p = work / "out" / ("case_mcmc_trace_%s_%s.txt" % (w[0], w[1]))
+        got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
+        assert got.shape[0] == K * T
+        assert np.allclose(got[k * T:k * T + a.shape[0]], a, rtol=2e-7, atol=1e-300), key
+
+
 @pytest.mark.parametrize("cols", [1, 2])
 def test_batched_layout_fp64_matches_oracle(built, cols):
     """The warp-per-chain layout with FP64 partials reproduces the oracle's

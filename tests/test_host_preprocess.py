@@ -143,8 +143,12 @@ def test_site_patterns_bit_exact(kind):
     assert n_checked >= 5
 
 
-@pytest.mark.parametrize("key,value,message", [("SAMPLE_HYPER", "1", "SAMPLE_HYPER")])
-def test_cli_rejects_unbuilt_modes(tmp_path, key, value, message):
+@pytest.mark.parametrize("extra,message", [
+    ({"INDEL": "1"}, "INDEL > 0"),
+    ({"SAMPLE_HYPER": "1", "GPU_PRECISION": "fp32_warp"}, "SAMPLE_HYPER chains need"),
+    ({"CHAIN": "2", "GPU_PRECISION": "fp64_warp"}, "a later chain"),
+])
+def test_cli_rejects_unbuilt_modes(tmp_path, extra, message):
     """Modes that are not built fail loudly before any device work, instead of
     running something else."""
     import shutil
@@ -155,8 +159,9 @@ def test_cli_rejects_unbuilt_modes(tmp_path, key, value, message):
     for f in ("case.mod", "case.bed", "case.fa"):
         shutil.copy(os.path.join(src, f), tmp_path / f)
     (tmp_path / "out").mkdir()
-    lines = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines() if not ln.startswith(key + " ")]
-    (tmp_path / "case.cfg").write_text("\n".join(lines + ["%s %s" % (key, value)]) + "\n")
+    lines = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines()
+             if ln.split(" ")[0] not in extra]
+    (tmp_path / "case.cfg").write_text("\n".join(lines + ["%s %s" % kv for kv in extra.items()]) + "\n")
     r = subprocess.run([CLI, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0
     assert message in r.stderr
