@@ -3,7 +3,7 @@ and, where the PhyloAcc sources are present, the reference itself compiled
 against the stand-in GSL/Armadillo headers of oracle/shim (oracle/_ref/).
 
     python oracle/build_oracle.py            # oracle only
-    python oracle/build_oracle.py --ref DIR  # also build DIR/src/PhyloAcc-ST
+    python oracle/build_oracle.py --ref DIR  # also build DIR/src/PhyloAcc-ST and PhyloAcc-ST-GBGC
 """
 import os
 import subprocess
@@ -62,7 +62,32 @@ def build_reference(ref_root, force=False):
     return out
 
 
+def build_reference_gbgc(ref_root, force=False):
+    """The unmodified PhyloAcc-ST-GBGC sources (the gBGC model) with the same
+    stand-in headers.  Output: oracle/_ref/PhyloAcc-gBGC (git-ignored).  The
+    prebuilt binary shipped beside those sources is not used."""
+    src_dir = os.path.join(ref_root, "src", "PhyloAcc-ST-GBGC", "SRC")
+    if not os.path.isdir(src_dir):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "PhyloAcc-gBGC")
+    shim = os.path.join(HERE, "shim")
+    srcs = [os.path.join(src_dir, s) for s in REF_SOURCES]
+    shim_files = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs]
+    if not force and _newer(out, srcs + shim_files + [os.path.join(HERE, "oracle_rng.h")]):
+        return out
+    cmd = [CXX, "-O2", "-std=c++14", "-ffp-contract=off", "-fopenmp", "-w",
+           "-I" + shim, "-I" + HERE, "-I" + os.path.join(ROOT, "phyloacc_gb300", "csrc")] + srcs + \
+          [os.path.join(shim, "shim_impl.cpp"), "-o", out + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     if "--ref" in sys.argv:
-        print(build_reference(sys.argv[sys.argv.index("--ref") + 1], force="--force" in sys.argv))
+        ref = sys.argv[sys.argv.index("--ref") + 1]
+        print(build_reference(ref, force="--force" in sys.argv))
+        print(build_reference_gbgc(ref, force="--force" in sys.argv))

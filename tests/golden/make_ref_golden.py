@@ -28,7 +28,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from phyloacc_gb300 import synth  # noqa: E402
-from oracle.build_oracle import build_reference  # noqa: E402
+from oracle.build_oracle import build_reference, build_reference_gbgc  # noqa: E402
 
 CASES = {
     # name: (dataset kind, element indices, burnin, mcmc, seed, extra cfg keys)
@@ -41,7 +41,10 @@ CASES = {
     "st12_chain2": ("st12", [0, 85, 90], 60, 150, 2, {"CHAIN": 2}),
     # SAMPLE_HYPER: three chains of M2, hyper-parameters drawn between chains
     "st12_hyper": ("st12", [0, 1, 85, 90], 60, 150, 4, {"CHAIN": 3, "SAMPLE_HYPER": 1}),
+    # the gBGC model (src/PhyloAcc-ST-GBGC): same inputs, its own outputs and traces
+    "gbgc12_default": ("st12", [0, 1, 85, 90], 20, 60, 0, {}),
 }
+GBGC_CASES = {"gbgc12_default"}
 
 
 def mask_taxa(ds, case):
@@ -73,12 +76,14 @@ def read_trace(path):
 
 
 def main(ref_root, only=None):
-    exe = build_reference(ref_root)
-    if exe is None:
+    exe_st = build_reference(ref_root)
+    exe_gbgc = build_reference_gbgc(ref_root)
+    if exe_st is None or exe_gbgc is None:
         raise SystemExit("reference sources not found under " + ref_root)
     for name, (kind, idx, burn, mcmc, seed, extra) in CASES.items():
         if only and name not in only:
             continue
+        exe = exe_gbgc if name in GBGC_CASES else exe_st
         d = os.path.join(HERE, name)
         if os.path.isdir(d):
             shutil.rmtree(d)
@@ -99,8 +104,8 @@ def main(ref_root, only=None):
         out = os.path.join(d, "out")
         traces = {}
         T = burn + mcmc
-        for f in sorted(glob.glob(os.path.join(out, "case_mcmc_trace_M*_*.txt"))):
-            tag = os.path.basename(f)[len("case_mcmc_trace_"):-4]  # M{m}_{elem}
+        for f in sorted(glob.glob(os.path.join(out, "case_mcmc_trace_*_*.txt"))):
+            tag = os.path.basename(f)[len("case_mcmc_trace_"):-4]  # M{m}_{elem} (gBGC: {m}_{elem})
             rows = read_trace(f)
             for k in range(int(extra.get("CHAIN", 1))):
                 # the first 200 iterations of each chain are the chain-parity window

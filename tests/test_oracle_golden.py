@@ -155,3 +155,23 @@ def test_oracle_matches_reference_sample_hyper():
         mine = np.stack([res.tr[f][j, 2, :T] for f in ("loglik", "n_rate", "c_rate", "g_rate", "l_rate", "l2_rate")], 1)
         assert np.allclose(mine, a[:, :6], rtol=6e-8, atol=1e-300), key
         assert (res.tr_z[j, 2, :T] == a[:, 6:6 + N].astype(np.int8)).all(), key
+
+
+def test_gbgc_fixture_layout():
+    """The gBGC fixture (src/PhyloAcc-ST-GBGC run on the 12-taxon inputs):
+    per-iteration traces (loglik, rate_n, rate_c, GB, then B and Z of every
+    node) and per-element tables, kept for the gBGC oracle and kernels."""
+    ds, o, kv = load_case("gbgc12_default")
+    N, n = ds.tree.n_nodes, ds.n_elements
+    T = int(kv["BURNIN"]) + int(kv["MCMC"])
+    tr = ref_traces("gbgc12_default")
+    assert sorted(tr) == sorted("%d_%d" % (m, e) for m in range(3) for e in range(n))
+    for a in tr.values():
+        assert a.shape == (T, 4 + 2 * N)
+        assert np.isfinite(a[:, 0]).all()
+        assert set(np.unique(a[:, 4 + N:])) <= {-1, 0, 1, 2}
+    tables = ref_tables("gbgc12_default")
+    hdr, rows = tables["elem_lik"]
+    assert hdr[:3] == ["No.", "ID", "loglik_NUll"] and len(rows) == n
+    hdr, rows = tables["1_elem_Z"]
+    assert len(rows) == n and hdr[0] == ds.tree.names[0] + "_B"
