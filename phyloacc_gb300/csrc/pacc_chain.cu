@@ -1393,7 +1393,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
             if (threadIdx.x == 0) cs_.loglik = ll0;
             __syncthreads();
             long long tph = clock64();   // phase timer (thread 0): cycles per phase into the counters
-#define V1_PHASE(i)                                          \
+#define CHAIN_PHASE(i)                                          \
     do {                                                     \
         if (threadIdx.x == 0) {                              \
             const long long t_ = clock64();                  \
@@ -1419,23 +1419,23 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 if (tmp_)
                     for (int i = threadIdx.x; i < N; i += BT) c.maxz[i] = c.Z[i];
                 if (m == T - 1) break;
-                V1_PHASE(0);
+                CHAIN_PHASE(0);
                 // internal bases
                 uint64_t pos = cs_.pos;
                 int err = sample_tg(c, pos);
                 __syncthreads();
-                V1_PHASE(1);
+                CHAIN_PHASE(1);
                 if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.tg_draws;
                 if (err) atomicOr(&cs_.status, 1);
                 // latent states
                 emission(c);
-                V1_PHASE(2);
+                CHAIN_PHASE(2);
                 pos = cs_.pos;
                 int zerr = update_z(c, pos);
                 if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.n_nodes;
                 if (zerr) atomicOr(&cs_.status, 1);
                 __syncthreads();
-                V1_PHASE(3);
+                CHAIN_PHASE(3);
                 // partial re-prune of ancestors of changed branches (bpp_c.cpp:419-431)
                 mark_ancestors(c, c.changed, c.unv, 0, &tmp_);
                 int any_unv = block_or(c.unv[c.root], &tmp_);
@@ -1444,18 +1444,18 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                     if (threadIdx.x == 0) cs_.loglik = ll;
                 }
                 __syncthreads();
-                V1_PHASE(4);
+                CHAIN_PHASE(4);
                 // rates (bpp_c.cpp:434-452)
                 mark_ancestors(c, nullptr, c.unvN, 1, &tmp_);
                 mark_ancestors(c, nullptr, c.unvC, 2, &tmp_);
                 double rn = sample_rate(c, dist2_, true, c.trd[TR_N * T + m], &tmp_);
                 if (threadIdx.x == 0) c.trd[TR_N * T + m + 1] = rn;
                 __syncthreads();
-                V1_PHASE(5);
+                CHAIN_PHASE(5);
                 double rc = sample_rate(c, dist2_, false, c.trd[TR_C * T + m], &tmp_);
                 if (threadIdx.x == 0) c.trd[TR_C * T + m + 1] = rc;
                 __syncthreads();
-                V1_PHASE(6);
+                CHAIN_PHASE(6);
                 // transitions of Z (sample_transition, bpp_c.cpp:522-613): the
                 // (child, parent) state counts in parallel (exact integers),
                 // then the three Beta draws on one thread
@@ -1488,10 +1488,10 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 __syncthreads();
                 build_ltm(c, c.trd[TR_G * T + m + 1], c.trd[TR_L * T + m + 1], c.trd[TR_L2 * T + m + 1], false);
                 __syncthreads();
-                V1_PHASE(7);
+                CHAIN_PHASE(7);
                 if (threadIdx.x == 0) c.local.iters++;
             }
-#undef V1_PHASE
+#undef CHAIN_PHASE
             __syncthreads();
             if (P.end_z) {
                 // the state where the chain stopped (bpp_c.cpp:475-485), before
