@@ -531,10 +531,8 @@ int main(int argc, char** argv) {
     }
     const int Tn = C.o.burnin + C.o.mcmc;
     if (C.verbose) C.o.trace_iters = Tn;
-    if (C.chain < 1) {
-        // CHAIN has no default in PhyloAcc-ST (main.cpp:57): nothing runs.
-        ids.clear();
-    }
+    // CHAIN has no default in PhyloAcc-ST (main.cpp:57): with CHAIN < 1 no
+    // chain runs and only the headers above are written (main.cpp:445-509)
     // batch of elements in tree leaf order
     vector<int64_t> no(ids.size());
     vector<int32_t> lens(ids.size());
@@ -595,7 +593,7 @@ int main(int argc, char** argv) {
     // SAMPLE_HYPER a later chain starts from Z = 0 (bpp_c.cpp:148-151).
     // _rate_postZ rows and traces are appended per chain, _elem_lik / _elem_Z
     // are the last chain's.
-    for (int chain = 0; chain < std::max(1, C.chain); chain++) {
+    for (int chain = 0; chain < C.chain; chain++) {
         C.o.chain = hyp ? 0 : chain;
         if (hyp) {
             C.o.acce_prior_a = hyper[0]; C.o.acce_prior_b = hyper[1];
@@ -687,7 +685,7 @@ int main(int argc, char** argv) {
         }
     }
     // _elem_lik.txt and _M*_elem_Z.txt (bpp.cpp:568-619)
-    if (!hyp) {
+    if (!hyp && C.chain >= 1) {
         std::ofstream ol((out + "_elem_lik.txt").c_str());
         ol.precision(8);
         ol << "No.\tID\tloglik_Null\tloglik_Acc\tloglik_Full\tlogBF1\tlogBF2\tloglik_Max_M0\tloglik_Max_M1\tloglik_Max_M2"

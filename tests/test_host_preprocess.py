@@ -165,3 +165,25 @@ def test_cli_rejects_unbuilt_modes(tmp_path, extra, message):
     r = subprocess.run([CLI, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0
     assert message in r.stderr
+
+
+def test_cli_chain_zero_writes_headers_only(tmp_path):
+    """CHAIN 0 (the reference has no default for CHAIN, main.cpp:57): no chain
+    runs, so only _hyper.txt, _species_names.txt and the _rate_postZ headers
+    are written, as PhyloAcc-ST does; no device is touched."""
+    import shutil
+    import subprocess
+    from phyloacc_gb300.build import build, CLI
+    build()
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "st12_default")
+    for f in ("case.mod", "case.bed", "case.fa"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    (tmp_path / "out").mkdir()
+    lines = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines() if not ln.startswith("CHAIN ")]
+    (tmp_path / "case.cfg").write_text("\n".join(lines + ["CHAIN 0"]) + "\n")
+    r = subprocess.run([CLI, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert sorted(os.listdir(tmp_path / "out")) == ["case_hyper.txt", "case_rate_postZ_M0.txt", "case_rate_postZ_M1.txt",
+                                                   "case_rate_postZ_M2.txt", "case_species_names.txt"]
+    for m in range(3):
+        assert len(open(tmp_path / "out" / ("case_rate_postZ_M%d.txt" % m)).read().splitlines()) == 1
