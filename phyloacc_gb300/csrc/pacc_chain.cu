@@ -85,20 +85,69 @@ struct ChainScalars {
     int n_unc, n_conf, eff;
     double vb;
     int fallback;
+    int n_list;            // entries of the current pass's node list
 };
 
 // Reduction scratch: one slot per warp (<= 32), the broadcast slot RED_SUM
 // and the median slot RED_MED.
 static const int RED_SUM = 32, RED_MED = 33, RED_SLOTS = 40;
 
-// Shared-memory layout (dynamic, sized by N).
+// Slots of the sampling pass's ring of column data copied ahead into
+// shared memory (cp.async): the nodes up to RING-1 steps ahead are in
+// flight while a node is drawn.
+static const int RING = 3;
+
+// One internal node of a pruning pass (the nodes flagged for the pass, in
+// the element's stack order: every node after its children, the child whose
+// subtree needs more pending partials first).  Child slot 0 is the child
+// visited second, whose partial is on top of the stack when both children
+// were computed in the same pass.
+enum { K_SKIP = 0, K_LEAF = 1, K_MEM = 2, K_STACK = 3 };
+struct __align__(16) PNode {
+    int32_t dst;        // row of the result: (buffer * n_int + rank) * GGp
+    int32_t src[2];     // leaf child: codes row (leaf * GGp); K_MEM child: its partial row; else -1
+    int32_t act[2];     // internal child: its activity row (rank * GGp); leaf: -1
+    int16_t mat[2];     // the child's transition matrix: class * N + child
+    int8_t kind[2];     // K_SKIP (missing child), K_LEAF, K_MEM (internal, unchanged in this pass), K_STACK
+    int8_t push;        // the parent is in the pass: the result goes on the stack
+    int8_t is_root;
+    int32_t pad;
+};
+
+// One internal node of the sampling pass (root first, then the internal
+// nodes in reverse postorder, so a parent's base is drawn before its
+// children's).
+struct __align__(16) SNode {
+    int32_t part;       // partial row of the node in its current buffer: (cur * n_int + rank) * GGp
+    int32_t act;        // activity row (rank * GGp); -1: a missing node (never drawn)
+    int16_t mat;        // matrix of the node's own branch: class(Z) * N + node
+    int16_t rank;       // base slot of the node
+    int16_t prank;      // base slot of the parent (-1 for the root)
+    int16_t node;       // emission row of the node's branch (-1: the root or a missing node)
+    int16_t leaf[2];    // leaf children whose branches emit under this node (-1: none or missing)
+    int32_t pad[2];
+};
+
+// Shared-memory layout (dynamic, sized by N, the block size and the
+// prune's stack depth D).
 template <typename Real>
 struct SmemLayout {
-    size_t ptd, ptr_, ltm, emis, beta, cnt, red, i16, i8, total;
-    __host__ __device__ static SmemLayout make(int N, int BT) {
+    size_t ptd, ptr_, ltm, emis, beta, cnt, red, i16, i8, dist, scr, ring, stks, desc, total;
+    __host__ __device__ static SmemLayout make(int N, int BT, int D) {
         SmemLayout s;
         size_t o = 0;
         auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+        const int n_int = (N + 1) / 2 - 1 > 0 ? (N + 1) / 2 - 1 : 1;   // internal nodes of a binary tree
+        // column scratch of one pass, per thread: the internal bases of its
+        // column and the ring of prefetched partials (sampling pass), or the
+        // stack of pending partials and their scales (prune)
+        const size_t sb = al((size_t)n_int * BT) + (size_t)RING * BT * (4 * sizeof(Real) + 12);
+        const size_t sk = al((size_t)D * BT * 4 * sizeof(Real)) + (size_t)D * BT * 4;
+        s.scr = o; o = al(o + (sb > sk ? sb : sk));
+        s.ring = s.scr + al((size_t)n_int * BT);
+        s.stks = s.scr + al((size_t)D * BT * 4 * sizeof(Real));
+        s.desc = o; o = al(o + (size_t)n_int * 32);                              // PNode / SNode list
+        s.dist = o; o = al(o + (size_t)N * 8);                                   // branch lengths
         // P^T per class [4][N][16]: FP64 for FP64 partials; FP32 partials keep
         // only the FP32 copy (the FP64 product is formed in registers)
         s.ptd = o; o = al(o + (sizeof(Real) == 8 ? (size_t)4 * N * 16 * 8 : 0));
@@ -106,7 +155,7 @@ struct SmemLayout {
         s.ltm = o; o = al(o + (sizeof(Real) == 8 ? (size_t)N * 9 * 8 : 0));  // log_TM_Int [N][3][3] (FP64 path)
         s.emis = o; o = al(o + (size_t)N * 3 * 8);
         s.beta = o; o = al(o + (size_t)N * 3 * 8);
-        s.cnt = o; o = al(o + (size_t)N * NSYM * 4 * 4);                    // emission histogram
+        s.cnt = o; o = al(o + (size_t)N * NSYM * 2 * 4);                    // emission histogram (16-bit bins)
         s.red = o; o = al(o + (size_t)RED_SLOTS * 8);                        // reduction scratch
         s.i16 = o; o = al(o + (size_t)TopoLayout::make(N).total * 2);
         s.i8 = o; o = al(o + (size_t)N * 8);                               // Z fixZ changed unv unvN unvC cur maxz
@@ -194,20 +243,30 @@ struct Ctx {
     // topology in shared
     int16_t *nodes, *internal, *c2a, *c2b, *par, *irank, *pos, *missing, *upc, *upcc, *hlev_start, *hlev_nodes,
         *dlev_start, *dlev_nodes;
+    int16_t *sord, *sflag;
     // shared state
     double* ptd;              // [4][N][16] (FP64 partials only; null for FP32)
     Real* ptr;                // [4][N][16]
     double* ltm;              // [N][9] log_TM_Int (zc*3+zp)
     double* emis;             // [N][3]
     double* beta;             // [N][3]
-    int* cnt;                 // [N][NSYM*4]
+    unsigned* cnt;            // [N][NSYM*2]: (child symbol, parent base) counts, two 16-bit bins a word
     double* red;
     int8_t *Z, *fixZ, *changed, *unv, *unvN, *unvC, *cur, *maxz;
     ChainScalars* cs;
+    int8_t* bases;            // sampling pass: [n_int][BT] internal bases of each thread's column
+    Real* ring;               // sampling pass: [RING][BT][4] partials copied ahead, then [RING][3][BT]
+                              // words holding the activity byte and two leaf codes
+    Real* stk;                // prune: [D][BT][4] pending partials
+    int32_t* stks;            // prune: [D][BT] their scales
+    PNode* pn;                // the pass's node list
+    SNode* sn;
+    int D;                    // stack rows
     // workspace
-    Real* lam;                // [2][n_int][4][GGp]
-    int32_t* scl;             // [2][n_int][GGp]
-    int8_t* tg;               // [n_int][GGp] internal Tg
+    Real* lam;                // [2][n_int][GGp][4] partials, one 4-vector per (node, column)
+    int32_t* scl;             // [2][n_int][GGp] their power-of-two exponents
+    int8_t* act;              // [n_int][GGp] static: < 4 where an internal node is sampled and pruned
+                              // (the initial Tg; 4 where both children are gaps or missing)
     int8_t* trz;              // [T][N]
     double* trd;              // [7][T]
     uint64_t* hash;
@@ -215,18 +274,24 @@ struct Ctx {
     double* cstat;
     int T, burn, mcmc;
     DevCounters local;
-
-    __device__ __forceinline__ Real* L(int buf, int ir, int j) { return lam + (((size_t)buf * n_int + ir) * 4 + j) * GGp; }
-    __device__ __forceinline__ int32_t* SC(int buf, int ir) { return scl + ((size_t)buf * n_int + ir) * GGp; }
-    __device__ __forceinline__ int tg_of(int s, int g) {
-        // Tg of a node at column g: leaves from their code, internal nodes from the sampled state
-        if (s < S) {
-            int c = codes[(size_t)s * GGp + g];
-            return c < 4 ? c : (c == CODE_GAP ? 4 : (c == CODE_OTHER ? 5 : -1));
-        }
-        return tg[(size_t)irank[s] * GGp + g];
-    }
 };
+
+// One partial 4-vector: 16-byte (FP32) or two 16-byte (FP64) accesses.
+__device__ __forceinline__ void ld4(const float* p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&x)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&x)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&x)[4]) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(x[0], x[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(x[2], x[3]);
+}
 
 // Class of the matrix used for child c: Z 2 -> neut, 0 -> null, else cons
 // (bpp_c.cpp:661-663); in an MH proposal the proposed class uses P_PROP (bpp_c.cpp:885-906).
@@ -235,10 +300,6 @@ __device__ __forceinline__ int mat_class(int z, int prop_class) {
     return (prop_class >= 0 && k == prop_class) ? P_PROP : k;
 }
 
-// Felsenstein pruning over the nodes flagged in `unv` (postorder), all columns.
-// mh = false: results overwrite the current buffer of each node (Update_Tg with
-// visited masks, bpp_c.cpp:647-671).  mh = true: results go to the other
-// buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928).  Returns the summed
 // One row of a 4x4 matrix (16-byte aligned rows: matrices are 16 entries
 // apart from an aligned base).
 __device__ __forceinline__ void ld_row(const float* p, float (&r)[4]) {
@@ -250,10 +311,104 @@ __device__ __forceinline__ void ld_row(const double* p, double (&r)[4]) {
     r[0] = a.x; r[1] = a.y; r[2] = b.x; r[3] = b.y;
 }
 
-// per-column log-likelihood at the root (valid when the root is flagged).
+// The pass's node list for a prune over the nodes flagged in `unv`: the
+// flagged, non-missing internal nodes in stack order, with their children
+// resolved (data source, matrix, stack use).  Built by warp 0 with a ballot
+// compaction, so the column loop reads one 32-byte entry per node.
+// mh = false: results overwrite the current buffer of each node (Update_Tg
+// with visited masks, bpp_c.cpp:647-671).  mh = true: results go to the other
+// buffer (log_f_Xz into lambda_tmp, bpp_c.cpp:860-928), and the children in
+// class prop_class take the proposal's matrices (bpp_c.cpp:885-906).
+// The flagged sets of every pass are closed upwards (ancestors of changed
+// branches, getUpdateNode), so every pushed partial is popped by its parent.
+template <typename Real>
+__device__ int build_prune_list(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int base = 0;
+        for (int k0 = 0; k0 < c.n_int; k0 += 32) {
+            const int k = k0 + lane;
+            int s = -1;
+            bool f = false;
+            if (k < c.n_int) {
+                s = c.sord[k];
+                f = unv[s] && !c.missing[s];
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, f);
+            if (f) {
+                PNode d;
+                const int ir = c.irank[s];
+                const int dbuf = mh ? 1 - c.cur[s] : c.cur[s];
+                d.dst = (dbuf * c.n_int + ir) * c.GGp;
+                d.is_root = (s == c.root);
+                const int ps = c.par[s];
+                d.push = (s != c.root && ps >= 0 && ps < c.N && unv[ps] && !c.missing[ps]) ? 1 : 0;
+                // slot 0: the child visited second (top of the stack)
+                const int a = c.c2a[s], bb = c.c2b[s];
+                const int chs[2] = {c.sflag[s] ? a : bb, c.sflag[s] ? bb : a};
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const int ch = chs[q];
+                    d.mat[q] = (int16_t)(mat_class(c.Z[ch], prop_class) * c.N + ch);
+                    if (c.missing[ch]) {
+                        d.kind[q] = K_SKIP; d.src[q] = -1; d.act[q] = -1;
+                    } else if (ch < c.S) {
+                        d.kind[q] = K_LEAF; d.src[q] = ch * c.GGp; d.act[q] = -1;
+                    } else {
+                        const int cir = c.irank[ch];
+                        d.act[q] = cir * c.GGp;
+                        if (unv[ch]) { d.kind[q] = K_STACK; d.src[q] = -1; }
+                        else { d.kind[q] = K_MEM; d.src[q] = (c.cur[ch] * c.n_int + cir) * c.GGp; }
+                    }
+                }
+                d.pad = 0;
+                c.pn[base + __popc(b & ((1u << lane) - 1u))] = d;
+            }
+            base += __popc(b);
+        }
+        if (lane == 0) c.cs->n_list = base;
+    }
+    __syncthreads();
+    return c.cs->n_list;
+}
+
+// What a column needs of one child before the arithmetic: issued for the
+// next node while the current one is computed (none of it depends on the
+// pass's own results).
+template <typename Real>
+struct ChildCol {
+    Real x[4];
+    int code;     // leaf: column code; internal: activity (< 4 = active)
+    int sc;
+};
+
+template <typename Real>
+__device__ __forceinline__ void load_child(const Ctx<Real>& c, const PNode& d, int q, int g, ChildCol<Real>& o) {
+    o.sc = 0;
+    o.code = 4;
+    const int kd = d.kind[q];
+    if (kd == K_LEAF) {
+        o.code = c.codes[d.src[q] + g];
+    } else if (kd >= K_MEM) {
+        o.code = c.act[d.act[q] + g];
+        if (kd == K_MEM) {
+            ld4(c.lam + ((size_t)d.src[q] + g) * 4, o.x);
+            o.sc = c.scl[d.src[q] + g];
+        }
+    }
+}
+
+// Felsenstein pruning over the flagged nodes (see build_prune_list), all
+// columns; returns the summed per-column log-likelihood at the root (valid
+// when the root is flagged).  A thread walks its column through the list:
+// partials computed in this pass are passed to the parent through a
+// shared-memory stack of depth D (the element's stack order bounds it), and
+// only unchanged children are read from the partial buffers.
 template <typename Real>
 __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
-    const int BT = blockDim.x;
+    const int n = build_prune_list(c, unv, mh, prop_class);
+    const int BT = blockDim.x, tid = threadIdx.x;
     double ll_sum = 0;
     // FP32 partials: the thread's columns are combined as an FP64 product of
     // root-sum mantissas with an exact integer exponent, and one log at the
@@ -261,122 +416,77 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
     double mprod = 1.0;
     long long mexp = 0;
     unsigned long long e_int = 0, e_leaf = 0;
-    for (int k = 0; k < c.n_int; k++) {
-        int s = c.internal[k];
-        if (!unv[s] || c.missing[s]) continue;
-        int ir = c.irank[s];
-        int dst = mh ? (1 - c.cur[s]) : c.cur[s];
-        int ch[2] = {c.c2a[s], c.c2b[s]};
-        // FP32: the children's matrices are read row by row from shared
-        // memory (broadcast loads) rather than held in registers; FP64 holds
-        // them in registers.  No register array is indexed by a runtime value.
-        Real P0[16], P1[16];
-        bool use[2];
-        int csrc[2], cir[2];
-        use[0] = !c.missing[ch[0]];
-        use[1] = !c.missing[ch[1]];
-        const Real* pm0 = c.ptr + ((size_t)mat_class(c.Z[ch[0]], prop_class) * c.N + ch[0]) * 16;
-        const Real* pm1 = c.ptr + ((size_t)mat_class(c.Z[ch[1]], prop_class) * c.N + ch[1]) * 16;
-        if (sizeof(Real) == 8) {
-#pragma unroll
-            for (int i = 0; i < 16; i++) { P0[i] = pm0[i]; P1[i] = pm1[i]; }
-        }
-        for (int q = 0; q < 2; q++) {
-            cir[q] = ch[q] >= c.S ? c.irank[ch[q]] : -1;
-            csrc[q] = (ch[q] >= c.S) ? ((mh && unv[ch[q]]) ? 1 - c.cur[ch[q]] : c.cur[ch[q]]) : 0;
-        }
-        const bool is_root = (s == c.root);
-        Real* Ld = c.L(dst, ir, 0);
-        int32_t* Sd = c.SC(dst, ir);
-        const int8_t* tgs = c.tg + (size_t)ir * c.GGp;
-        // per child: its codes (leaf) or its bases, partials and scales
-        // (internal node); the branch conditions are the same for the whole block
-        // row offsets (32-bit, fewer registers than pointers): a leaf child's
-        // codes row, or an internal child's base row and partial/scale row
-        const bool leaf0 = ch[0] < c.S, leaf1 = ch[1] < c.S;
-        const int GGp = c.GGp;
-        const int r0 = (leaf0 ? ch[0] : cir[0]) * GGp, r1 = (leaf1 ? ch[1] : cir[1]) * GGp;
-        const int q0 = leaf0 ? 0 : (csrc[0] * c.n_int + cir[0]) * GGp;
-        const int q1 = leaf1 ? 0 : (csrc[1] * c.n_int + cir[1]) * GGp;
-        for (int g = threadIdx.x; g < c.GG; g += BT) {
-            // every load of the column is issued before any is used, so that
-            // their latencies overlap (the node's base, then the children's
-            // data, would otherwise be three dependent round trips)
-            const int ts = tgs[g];
-            int k0 = 0, k1 = 0, s0 = 0, s1 = 0;
-            Real x0[4] = {0, 0, 0, 0}, x1[4] = {0, 0, 0, 0};
-            if (use[0]) {
-                if (leaf0) k0 = c.codes[r0 + g];
-                else {
-                    k0 = c.tg[r0 + g];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) x0[i] = c.lam[4 * q0 + i * GGp + g];
-                    s0 = c.scl[q0 + g];
-                }
-            }
-            if (use[1]) {
-                if (leaf1) k1 = c.codes[r1 + g];
-                else {
-                    k1 = c.tg[r1 + g];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) x1[i] = c.lam[4 * q1 + i * GGp + g];
-                    s1 = c.scl[q1 + g];
-                }
+    int overflow = 0;
+    for (int g = tid; g < c.GG; g += BT) {
+        int sp = 0;
+        PNode dn = c.pn[0];
+        ChildCol<Real> n0, n1;
+        if (n > 0) { load_child(c, dn, 0, g, n0); load_child(c, dn, 1, g, n1); }
+        for (int k = 0; k < n; k++) {
+            const PNode d = dn;
+            ChildCol<Real> ch[2] = {n0, n1};
+            if (k + 1 < n) {
+                dn = c.pn[k + 1];
+                load_child(c, dn, 0, g, n0);
+                load_child(c, dn, 1, g, n1);
             }
             Real a[4] = {1, 1, 1, 1};
             int sc = 0;
-            if (ts < KB) {
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    if (!use[q]) continue;
-                    const Real* PM = q ? pm1 : pm0;
-                    if (q ? leaf1 : leaf0) {
-                        const int code = q ? k1 : k0;
-                        if (code == CODE_GAP || code == CODE_OTHER) continue;
-                        if (code < 4) {
-                            Real r[4];
-                            ld_row(PM + code * 4, r);
+            for (int q = 0; q < 2; q++) {
+                const int kd = d.kind[q];
+                if (kd == K_SKIP) continue;
+                const Real* PM = c.ptr + (size_t)d.mat[q] * 16;
+                if (kd == K_LEAF) {
+                    const int code = ch[q].code;
+                    if (code == CODE_GAP || code == CODE_OTHER) continue;
+                    if (code < 4) {
+                        Real r[4];
+                        ld_row(PM + code * 4, r);
 #pragma unroll
-                            for (int j = 0; j < 4; j++) a[j] *= r[j];
-                        } else {
-                            int msk = ambig_mask(code - CODE_R);
-                            Real v[4] = {0, 0, 0, 0};
-#pragma unroll
-                            for (int i = 0; i < 4; i++)
-                                if (msk & (1 << i)) {
-#pragma unroll
-                                    for (int j = 0; j < 4; j++) v[j] += PM[i * 4 + j];
-                                }
-#pragma unroll
-                            for (int j = 0; j < 4; j++) a[j] *= v[j];
-                        }
-                        e_leaf++;
+                        for (int j = 0; j < 4; j++) a[j] *= r[j];
                     } else {
-                        if ((q ? k1 : k0) >= KB) continue;
-                        const Real* x = q ? x1 : x0;
-                        Real r0[4], r1[4], r2[4], r3[4];
-                        if (sizeof(Real) == 8) {
-                            const Real* P = q ? P1 : P0;
+                        const int msk = ambig_mask(code - CODE_R);
+                        Real v[4] = {0, 0, 0, 0};
 #pragma unroll
-                            for (int j = 0; j < 4; j++) { r0[j] = P[j]; r1[j] = P[4 + j]; r2[j] = P[8 + j]; r3[j] = P[12 + j]; }
-                        } else {
-                            ld_row(PM, r0); ld_row(PM + 4, r1); ld_row(PM + 8, r2); ld_row(PM + 12, r3);
-                        }
+                        for (int i = 0; i < 4; i++)
+                            if (msk & (1 << i)) {
 #pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            Real v = r0[j] * x[0];
-                            v += r1[j] * x[1];
-                            v += r2[j] * x[2];
-                            v += r3[j] * x[3];
-                            a[j] *= v;
-                        }
-                        sc += q ? s1 : s0;
-                        e_int++;
+                                for (int j = 0; j < 4; j++) v[j] += PM[i * 4 + j];
+                            }
+#pragma unroll
+                        for (int j = 0; j < 4; j++) a[j] *= v[j];
                     }
+                    e_leaf++;
+                } else {
+                    if (kd == K_STACK) {
+                        // the child's partial of this pass (on top of the stack)
+                        if (sp > 0) {
+                            sp--;
+                            ld4(c.stk + ((size_t)sp * BT + tid) * 4, ch[q].x);
+                            ch[q].sc = c.stks[sp * BT + tid];
+                        } else {
+                            overflow = 1;
+                        }
+                    }
+                    if (ch[q].code >= KB) continue;
+                    Real r0[4], r1[4], r2[4], r3[4];
+                    ld_row(PM, r0); ld_row(PM + 4, r1); ld_row(PM + 8, r2); ld_row(PM + 12, r3);
+                    const Real* x = ch[q].x;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        Real v = r0[j] * x[0];
+                        v += r1[j] * x[1];
+                        v += r2[j] * x[2];
+                        v += r3[j] * x[3];
+                        a[j] *= v;
+                    }
+                    sc += ch[q].sc;
+                    e_int++;
                 }
-                Rescale<Real>::apply(a, sc);
             }
-            if (is_root) {
+            Rescale<Real>::apply(a, sc);
+            if (d.is_root) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
                 double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
@@ -389,11 +499,20 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
                     mexp += (long long)e1 + e2 + sc;
                 }
             }
-#pragma unroll
-            for (int j = 0; j < 4; j++) Ld[j * c.GGp + g] = a[j];
-            Sd[g] = sc;
+            st4(c.lam + ((size_t)d.dst + g) * 4, a);
+            c.scl[d.dst + g] = sc;
+            if (d.push) {
+                if (sp < c.D) {
+                    st4(c.stk + ((size_t)sp * BT + tid) * 4, a);
+                    c.stks[sp * BT + tid] = sc;
+                } else {
+                    overflow = 1;
+                }
+                sp++;
+            }
         }
     }
+    if (overflow) atomicOr(&c.cs->status, 1);
     c.local.edge_internal += e_int;
     c.local.edge_leaf += e_leaf;
     if (sizeof(Real) != 8) ll_sum = d_log(mprod) + (double)mexp * 0.6931471805599453;
@@ -484,22 +603,116 @@ __device__ void build_ltm(Ctx<Real>& c, double gr, double lr, double lr2, bool i
     }
 }
 
-// Internal-base sampling, top-down per column (Update_Tg with tosample,
-// bpp_c.cpp:672-733).  Column g takes its words at pos + prefix[g].
+// The sampling pass's node list: the root, then the internal nodes in
+// reverse postorder (internal[n_int-2] .. internal[0]), each with its
+// partial row in the current buffer, the matrix of its branch and the
+// leaf children whose branch emissions are counted under it.
 template <typename Real>
-__device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
+__device__ void build_sample_list(Ctx<Real>& c) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < c.n_int; i += blockDim.x) {
+        const int s = c.internal[c.n_int - 1 - i];
+        const int ir = c.irank[s];
+        SNode d;
+        d.part = (c.cur[s] * c.n_int + ir) * c.GGp;
+        const bool miss = c.missing[s] != 0;
+        d.act = miss ? -1 : ir * c.GGp;
+        d.mat = (int16_t)(mat_class(c.Z[s], -1) * c.N + s);
+        d.rank = (int16_t)ir;
+        d.prank = (int16_t)(s == c.root ? -1 : c.irank[c.par[s]]);
+        d.node = (int16_t)((s == c.root || miss) ? -1 : s);
+        const int a = c.c2a[s], b = c.c2b[s];
+        d.leaf[0] = (int16_t)((a >= 0 && a < c.S && !c.missing[a]) ? a : -1);
+        d.leaf[1] = (int16_t)((b >= 0 && b < c.S && !c.missing[b]) ? b : -1);
+        d.pad[0] = d.pad[1] = 0;
+        c.sn[i] = d;
+    }
+    for (int i = threadIdx.x; i < c.N * NSYM * 2; i += blockDim.x) c.cnt[i] = 0;
+    __syncthreads();
+}
+
+// One histogram count for the branch above `row`: lanes of the warp with
+// the same key are merged before the shared atomic.  Bins are 16 bits, two
+// to a word (a branch counts at most one pair per column, and elements have
+// fewer than 65,536 columns).  Called by all 32 lanes.
+__device__ __forceinline__ void emit_key(unsigned* cnt, int row, int key) {
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicAdd(&cnt[row * (NSYM * 2) + (key >> 1)], (unsigned)__popc(peers) << (16 * (key & 1)));
+}
+__device__ __forceinline__ int bin_count(const unsigned* cnt, int row, int key) {
+    return (int)((cnt[row * (NSYM * 2) + (key >> 1)] >> (16 * (key & 1))) & 0xffffu);
+}
+
+// Asynchronous 16-byte global -> shared copies (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+// One partial 4-vector (16 or 32 bytes).
+__device__ __forceinline__ void cp_part(float* sdst, const float* gsrc) { cp_async16(sdst, gsrc); }
+__device__ __forceinline__ void cp_part(double* sdst, const double* gsrc) {
+    cp_async16(sdst, gsrc);
+    cp_async16(sdst + 2, gsrc + 2);
+}
+
+// Emission symbol of a leaf code: bases 0..3, ambiguity codes 4..9, else -1.
+__device__ __forceinline__ int leaf_sym(int code) { return code < 4 ? code : (code >= CODE_R ? code - 2 : -1); }
+
+// Internal-base sampling, top-down per column (Update_Tg with tosample,
+// bpp_c.cpp:672-733), fused with the histogram of (child symbol, parent
+// base) pairs of every branch that the emissions are summed from
+// (getEmission, bpp_c2.cpp:355-390).  Column g takes its stream words at
+// pos + prefix[g].  A thread keeps the bases of its column in shared memory
+// (the parent's base is read there, not from device memory), loads the next
+// node's partial while the current node is drawn, and the histogram counts
+// are integers, so the order of the adds does not matter.  Each internal
+// node's base is drawn afresh from the current partials, so bases need not
+// outlive the pass: which nodes are drawn (and pruned) at a column is the
+// static activity row.
+template <typename Real>
+__device__ int sample_emit(Ctx<Real>& c, uint64_t pos) {
+    build_sample_list(c);
     int err = 0;
-    const int rir = c.irank[c.root];
-    const int rbuf = c.cur[c.root];
+    const int BT = blockDim.x, tid = threadIdx.x;
     unsigned long long draws = 0;
-    for (int g = threadIdx.x; g < c.GG; g += blockDim.x) {
-        uint64_t w = pos + (uint64_t)c.prefix[g];
+    int8_t* bs = c.bases;
+    const int n = c.n_int;
+    // ring slot q of this thread: the partial, and the 4-byte words holding
+    // the activity byte and the two leaf codes of the node RING-1 steps ahead
+    Real* rp = c.ring;
+    unsigned* rw = (unsigned*)(c.ring + (size_t)RING * BT * 4);
+    for (int gb = 0; gb < c.GG; gb += BT) {
+        const int g = gb + tid;
+        const bool on = g < c.GG;
+        const int gw = g & ~3, sh = 8 * (g & 3);
+        // copies of node i's column data into ring slot i % RING
+        auto issue = [&](int i) {
+            if (on && i < n) {
+                const SNode e = c.sn[i];
+                const int q = i % RING;
+                cp_part(rp + ((size_t)q * BT + tid) * 4, c.lam + ((size_t)e.part + g) * 4);
+                if (e.act >= 0) cp_async4(rw + (q * 3 + 0) * BT + tid, c.act + e.act + gw);
+                if (e.leaf[0] >= 0) cp_async4(rw + (q * 3 + 1) * BT + tid, c.codes + (size_t)e.leaf[0] * c.GGp + gw);
+                if (e.leaf[1] >= 0) cp_async4(rw + (q * 3 + 2) * BT + tid, c.codes + (size_t)e.leaf[1] * c.GGp + gw);
+            }
+            cp_async_commit();
+        };
+        for (int i = 0; i < RING - 1; i++) issue(i);
+        uint64_t w = on ? pos + (uint64_t)c.prefix[g] : 0;
         uint64_t blk = ~0ull;
         // the block's four words in scalars (an array indexed by w & 3 would
         // live in local memory)
         uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
         auto next_word = [&]() {
-            uint64_t b = w >> 2;
+            const uint64_t b = w >> 2;
             if (b != blk) {
                 uint32_t o[4];
                 philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, dM.seed, 0u, o);
@@ -525,83 +738,60 @@ __device__ int sample_tg(Ctx<Real>& c, uint64_t pos) {
                 if (q[k] > 0) return k;
             return 4;
         };
-        Real p[4];
-        const Real* Lr = c.L(rbuf, rir, 0);
+        // node i = 0 is the root (always drawn), then the internal nodes top-down
+        for (int i = 0; i < n; i++) {
+            issue(i + RING - 1);
+            cp_async_wait<RING - 1>();   // node i's copies have landed
+            const SNode d = c.sn[i];
+            const int q = i % RING;
+            Real x[4];
+            ld4(rp + ((size_t)q * BT + tid) * 4, x);
+            const int a = (d.act >= 0 && i > 0) ? (int)((rw[(q * 3 + 0) * BT + tid] >> sh) & 0xff) : 0;
+            const int lc0 = d.leaf[0] >= 0 ? (int)((rw[(q * 3 + 1) * BT + tid] >> sh) & 0xff) : 4;
+            const int lc1 = d.leaf[1] >= 0 ? (int)((rw[(q * 3 + 2) * BT + tid] >> sh) & 0xff) : 4;
+            int tp = 0, nb = 4;
+            if (i == 0) {
+                if (on) {
+                    nb = draw4(x);
+                    draws++;
+                    if (nb > 3) { err = 1; nb = 0; }
+                }
+            } else {
+                const bool drawn = on && d.act >= 0 && (int8_t)a < KB;
+                tp = bs[d.prank * BT + tid];
+                if (drawn) {
+                    const Real* P = c.ptr + (size_t)d.mat * 16;
+                    Real qv[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) p[j] = Lr[j * c.GGp + g];
-        int nn = draw4(p);
-        draws++;
-        if (nn > 3) { err = 1; nn = 0; }
-        c.tg[(size_t)rir * c.GGp + g] = (int8_t)nn;
-        // the partials of the next node are loaded while this one is drawn
-        auto load_part = [&](int k, Real (&x)[4]) {
-            const int sk = c.internal[k];
-            const Real* Lk = c.L(c.cur[sk], c.irank[sk], 0);
-#pragma unroll
-            for (int i = 0; i < 4; i++) x[i] = Lk[i * c.GGp + g];
-        };
-        Real nxt[4] = {0, 0, 0, 0};
-        if (c.n_int >= 2) load_part(c.n_int - 2, nxt);
-        for (int k = c.n_int - 2; k >= 0; k--) {
-            Real lsv[4] = {nxt[0], nxt[1], nxt[2], nxt[3]};
-            if (k >= 1) load_part(k - 1, nxt);
-            int s = c.internal[k];
-            int ir = c.irank[s];
-            if (c.missing[s]) continue;
-            // the node's and its parent's bases: both loads before either is used
-            const int own = c.tg[(size_t)ir * c.GGp + g];
-            const int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
-            if (own >= KB) continue;
-            const Real* P = c.ptr + ((size_t)mat_class(c.Z[s], -1) * c.N + s) * 16;
-            Real q[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) q[i] = P[i * 4 + tp] * lsv[i];
-            int n2 = draw4(q);
-            draws++;
-            if (n2 > 3) { err = 1; n2 = 0; }
-            c.tg[(size_t)ir * c.GGp + g] = (int8_t)n2;
+                    for (int k = 0; k < 4; k++) qv[k] = P[k * 4 + tp] * x[k];
+                    nb = draw4(qv);
+                    draws++;
+                    if (nb > 3) { err = 1; nb = 0; }
+                }
+            }
+            bs[d.rank * BT + tid] = (int8_t)nb;
+            if (d.node >= 0) emit_key(c.cnt, d.node, (on && nb < KB && tp < KB) ? nb * 4 + tp : -1);
+            if (d.leaf[0] >= 0) {
+                const int sy = leaf_sym(lc0);
+                emit_key(c.cnt, d.leaf[0], (on && sy >= 0 && nb < KB) ? sy * 4 + nb : -1);
+            }
+            if (d.leaf[1] >= 0) {
+                const int sy = leaf_sym(lc1);
+                emit_key(c.cnt, d.leaf[1], (on && sy >= 0 && nb < KB) ? sy * 4 + nb : -1);
+            }
         }
+        cp_async_wait<0>();
     }
     c.local.tg_draws += draws;
+    __syncthreads();
     return err;
 }
 
-// Emission sums per branch and class (getEmission, bpp_c2.cpp:355-390) from a
-// histogram of (child symbol, parent base) pairs.
+// Emission sums per branch and class (getEmission, bpp_c2.cpp:355-390) from
+// the histogram of the sampling pass: e_s[z] = sum of counts * log P^T_z.
 template <typename Real>
 __device__ void emission(Ctx<Real>& c) {
     const int NB = NSYM * 4;
-    for (int i = threadIdx.x; i < c.N * NB; i += blockDim.x) c.cnt[i] = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    // columns are processed warp-synchronously so that equal bins of a warp
-    // are merged before the shared atomic
-    const int nW = blockDim.x >> 5;
-    const int w = threadIdx.x >> 5;
-    for (int g0 = w * 32; g0 < c.GG; g0 += nW * 32) {
-        int g = g0 + lane;
-        bool act = g < c.GG;
-        for (int k = 0; k < c.n_nodes - 1; k++) {
-            int s = c.nodes[k];
-            if (c.missing[s]) continue;
-            int key = -1;
-            if (act) {
-                // both loads before either is used (independent round trips)
-                const int own = (s < c.S) ? (int)c.codes[(size_t)s * c.GGp + g]
-                                          : (int)c.tg[(size_t)c.irank[s] * c.GGp + g];
-                const int tp = c.tg[(size_t)c.irank[c.par[s]] * c.GGp + g];
-                int sym;
-                if (s < c.S) sym = own < 4 ? own : (own >= CODE_R ? own - 2 : -1);
-                else sym = own < KB ? own : -1;
-                if (sym >= 0 && tp >= 0 && tp < 4) key = sym * 4 + tp;
-            }
-            unsigned peers = __match_any_sync(0xffffffffu, key);
-            int leader = __ffs(peers) - 1;
-            if (key >= 0 && lane == leader) atomicAdd(&c.cnt[s * NB + key], __popc(peers));
-        }
-    }
-    __syncthreads();
-    // per (node, class): e = sum counts * log P
     for (int i = threadIdx.x; i < (c.n_nodes - 1) * 3; i += blockDim.x) {
         int s = c.nodes[i / 3];
         int z = i % 3;
@@ -610,7 +800,7 @@ __device__ void emission(Ctx<Real>& c) {
         const Real* P = c.ptr + ((size_t)cls * c.N + s) * 16;
         double e = 0;
         for (int b = 0; b < NB; b++) {
-            int n = c.cnt[s * NB + b];
+            int n = bin_count(c.cnt, s, b);
             if (!n) continue;
             int sym = b >> 2, tp = b & 3;
             double t;
@@ -1196,35 +1386,53 @@ __device__ double eval2(Ctx<Real>& c, const double* dist2, int resZ, int* tmp, i
 // ---------------------------------------------------------------------------
 // FP32 runs 256 threads with two blocks per SM (128 registers a thread);
 // FP64 runs 128 threads and may use more registers.
+// Shared-memory pointers of a chain context (layout SmemLayout).
 template <typename Real>
-__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(ChainParams P) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ ChainScalars cs_;
-    __shared__ int tmp_;
-    __shared__ int elem_;
-    __shared__ double dist2_[MAX_NODES];
-    const int N = dM.N, S = dM.S;
-    const int BT = blockDim.x;
-    SmemLayout<Real> L = SmemLayout<Real>::make(N, BT);
+__device__ void bind_smem(Ctx<Real>& c, unsigned char* smem, int N, int BT, int D) {
+    SmemLayout<Real> L = SmemLayout<Real>::make(N, BT, D);
     TopoLayout TL = TopoLayout::make(N);
-    Ctx<Real> c;
-    c.S = S;
     c.N = N;
+    c.D = D;
     c.ptd = (sizeof(Real) == 8) ? (double*)(smem + L.ptd) : nullptr;
     c.ptr = (sizeof(Real) == 8) ? (Real*)(smem + L.ptd) : (Real*)(smem + L.ptr_);
     c.ltm = (double*)(smem + L.ltm);
     c.emis = (double*)(smem + L.emis);
     c.beta = (double*)(smem + L.beta);
-    c.cnt = (int*)(smem + L.cnt);
+    c.cnt = (unsigned*)(smem + L.cnt);
     c.red = (double*)(smem + L.red);
     int16_t* t16 = (int16_t*)(smem + L.i16);
     c.nodes = t16 + TL.nodes; c.internal = t16 + TL.internal; c.c2a = t16 + TL.c2a; c.c2b = t16 + TL.c2b;
     c.par = t16 + TL.par; c.irank = t16 + TL.irank; c.pos = t16 + TL.pos; c.missing = t16 + TL.missing;
     c.upc = t16 + TL.upc; c.upcc = t16 + TL.upcc; c.hlev_start = t16 + TL.hlev_start;
     c.hlev_nodes = t16 + TL.hlev_nodes; c.dlev_start = t16 + TL.dlev_start; c.dlev_nodes = t16 + TL.dlev_nodes;
+    c.sord = t16 + TL.sord; c.sflag = t16 + TL.sflag;
     int8_t* t8 = (int8_t*)(smem + L.i8);
     c.Z = t8; c.fixZ = t8 + N; c.changed = t8 + 2 * N; c.unv = t8 + 3 * N; c.unvN = t8 + 4 * N;
     c.unvC = t8 + 5 * N; c.cur = t8 + 6 * N; c.maxz = t8 + 7 * N;
+    c.bases = (int8_t*)(smem + L.scr);
+    c.ring = (Real*)(smem + L.ring);
+    c.stk = (Real*)(smem + L.scr);
+    c.stks = (int32_t*)(smem + L.stks);
+    c.pn = (PNode*)(smem + L.desc);
+    c.sn = (SNode*)(smem + L.desc);
+}
+
+// FP32 runs up to 256 threads with two blocks per SM (128 registers a
+// thread); FP64 may use more registers.
+template <typename Real>
+__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(ChainParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ChainScalars cs_;
+    __shared__ int tmp_;
+    __shared__ int elem_;
+    const int N = dM.N, S = dM.S;
+    const int BT = blockDim.x;
+    TopoLayout TL = TopoLayout::make(N);
+    Ctx<Real> c;
+    c.S = S;
+    bind_smem(c, smem, N, BT, P.stack_cap);
+    int16_t* t16 = c.nodes;
+    double* dist2_ = (double*)(smem + SmemLayout<Real>::make(N, BT, P.stack_cap).dist);
     c.cs = &cs_;
     c.burn = dM.burnin;
     c.mcmc = dM.mcmc;
@@ -1234,7 +1442,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
     WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, T, dM.mcmc, N, sizeof(Real));
     c.lam = (Real*)(ws + W.lam);
     c.scl = (int32_t*)(ws + W.scale);
-    c.tg = (int8_t*)(ws + W.tg);
+    c.act = (int8_t*)(ws + W.tg);
     c.trz = (int8_t*)(ws + W.trz);
     c.trd = (double*)(ws + W.trd);
     c.hash = (uint64_t*)(ws + W.hash);
@@ -1304,13 +1512,13 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
         if (!P.stream) {
             for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
             for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = d2[i];
-            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = tg0[i];
+            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.act[i] = tg0[i];
         } else {
             // element data of a queue slot: copied past L1 into shared memory
             // and this CTA's workspace, which the chain then reads
             for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = __ldcg(topo + i);
             for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = __ldcg(d2 + i);
-            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = __ldcg(tg0 + i);
+            for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.act[i] = __ldcg(tg0 + i);
             const int nw = (int)(((size_t)S * c.GGp) / 4);
             const int* csrc = (const int*)c.codes;
             int* cdst = (int*)(ws + W.codes);
@@ -1422,8 +1630,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 CHAIN_PHASE(0);
                 // internal bases
                 uint64_t pos = cs_.pos;
-                int err = sample_tg(c, pos);
-                __syncthreads();
+                int err = sample_emit(c, pos);
                 CHAIN_PHASE(1);
                 if (threadIdx.x == 0) cs_.pos = pos + (uint64_t)c.tg_draws;
                 if (err) atomicOr(&cs_.status, 1);
@@ -1459,7 +1666,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 // transitions of Z (sample_transition, bpp_c.cpp:522-613): the
                 // (child, parent) state counts in parallel (exact integers),
                 // then the three Beta draws on one thread
-                int* zcount = c.cnt;   // free until the next emission pass
+                int* zcount = (int*)c.cnt;   // free until the next sampling pass
                 if (threadIdx.x < 18) zcount[threadIdx.x] = 0;
                 __syncthreads();
                 for (int k = threadIdx.x; k + 1 < c.n_nodes; k += BT) {
@@ -1590,21 +1797,13 @@ template <typename Real>
 __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, double n_rate, double* out) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ChainScalars cs_;
-    __shared__ double dist2_[MAX_NODES];
     const int N = dM.N, S = dM.S;
     const int BT = blockDim.x;
-    SmemLayout<Real> L = SmemLayout<Real>::make(N, BT);
     TopoLayout TL = TopoLayout::make(N);
     Ctx<Real> c;
-    c.S = S; c.N = N;
-    c.ptd = (sizeof(Real) == 8) ? (double*)(smem + L.ptd) : nullptr;
-    c.ptr = (sizeof(Real) == 8) ? (Real*)(smem + L.ptd) : (Real*)(smem + L.ptr_);
-    c.red = (double*)(smem + L.red);
-    int16_t* t16 = (int16_t*)(smem + L.i16);
-    c.nodes = t16 + TL.nodes; c.internal = t16 + TL.internal; c.c2a = t16 + TL.c2a; c.c2b = t16 + TL.c2b;
-    c.par = t16 + TL.par; c.irank = t16 + TL.irank; c.pos = t16 + TL.pos; c.missing = t16 + TL.missing;
-    int8_t* t8 = (int8_t*)(smem + L.i8);
-    c.Z = t8; c.unv = t8 + 3 * N; c.cur = t8 + 6 * N;
+    c.S = S;
+    bind_smem(c, smem, N, BT, P.stack_cap);
+    double* dist2_ = (double*)(smem + SmemLayout<Real>::make(N, BT, P.stack_cap).dist);
     c.cs = &cs_;
     const ElemHeader& H = P.hdr[0];
     c.GG = H.GG; c.GGp = H.GGp; c.root = H.root; c.n_nodes = H.n_nodes; c.n_int = H.n_int;
@@ -1613,15 +1812,16 @@ __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, do
     WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, 1, 1, N, sizeof(Real));
     c.lam = (Real*)(ws + W.lam);
     c.scl = (int32_t*)(ws + W.scale);
-    c.tg = (int8_t*)(ws + W.tg);
+    c.act = (int8_t*)(ws + W.tg);
     c.local = DevCounters{0, 0, 0, 0, 0, 0, 0};
     const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
-    for (int i = threadIdx.x; i < TL.total; i += BT) t16[i] = topo[i];
+    for (int i = threadIdx.x; i < TL.total; i += BT) c.nodes[i] = topo[i];
     const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
     for (int i = threadIdx.x; i < N; i += BT) dist2_[i] = d2[i];
     const int8_t* tg0 = (const int8_t*)(P.blob + H.tg_off);
-    for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.tg[i] = tg0[i];
+    for (size_t i = threadIdx.x; i < (size_t)c.n_int * c.GGp; i += BT) c.act[i] = tg0[i];
     for (int i = threadIdx.x; i < N; i += BT) { c.Z[i] = (int8_t)z[i]; c.unv[i] = 1; c.cur[i] = 0; }
+    if (threadIdx.x == 0) cs_.status = 0;
     __syncthreads();
     build_class(c, dist2_, P_NULL, 1.0, false, false);
     build_class(c, dist2_, P_NEUT, n_rate, true, false);
@@ -1629,11 +1829,13 @@ __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, do
     __syncthreads();
     prune(c, c.unv, false, -1);
     __syncthreads();
-    int rir = c.irank[c.root];
+    const int rir = c.irank[c.root];
     for (int g = threadIdx.x; g < c.GG; g += BT) {
-        Real* Lr = c.L(0, rir, 0);
-        double t = (double)Lr[g] + (double)Lr[g + c.GGp] + (double)Lr[g + 2 * c.GGp] + (double)Lr[g + 3 * c.GGp];
-        out[g] = d_log(t) + (double)c.SC(0, rir)[g] * 0.6931471805599453;
+        Real a[4];
+        const size_t row = (size_t)rir * c.GGp + g;
+        ld4(c.lam + row * 4, a);
+        double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
+        out[g] = d_log(t) + (double)c.scl[row] * 0.6931471805599453;
     }
 }
 
@@ -1659,8 +1861,8 @@ cudaError_t set_model(const DevModel& m, cudaStream_t st) {
     return cudaMemcpyToSymbolAsync(dM, &m, sizeof(DevModel), 0, cudaMemcpyHostToDevice, st);
 }
 
-size_t smem_bytes(int N, int BT, int prec) {
-    return prec == 0 ? SmemLayout<double>::make(N, BT).total : SmemLayout<float>::make(N, BT).total;
+size_t smem_bytes(int N, int BT, int prec, int D) {
+    return prec == 0 ? SmemLayout<double>::make(N, BT, D).total : SmemLayout<float>::make(N, BT, D).total;
 }
 
 size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec) {

@@ -144,6 +144,7 @@ struct ChainParams {
     char* ws;                  // per-CTA workspace
     size_t ws_stride;
     int n_int_max, GGp_max;
+    int stack_cap;             // rows of the prune's shared-memory stack (>= every element's stack_depth)
     DevCounters* counters;
     // stream mode (serving): CTAs take slots from a queue the host appends to
     // while the kernel runs; element data and results are indexed by slot.

@@ -31,7 +31,7 @@
 namespace pacc {
 
 cudaError_t set_model(const DevModel& m, cudaStream_t st);
-size_t smem_bytes(int N, int BT, int prec);
+size_t smem_bytes(int N, int BT, int prec, int D);
 int chain_occupancy(int prec, int BT, size_t smem);
 size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec);
 size_t topo_bytes(int N);
@@ -477,6 +477,7 @@ struct pacc_ctx {
     std::string err;
     int device = 0;
     int n_sm = 0;
+    int stack_cap = 1;       // pending partials of the CTA kernel's prune (the full tree's stack order)
     bool gpu_ok = false;
     cudaStream_t stream = nullptr;
     // pending and finished work
@@ -605,6 +606,21 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     }
     for (int i = 0; i < N - 1; i++)
         if (M.parent[i] < 0) { delete c; return fail(PACC_EINVAL, "node without parent"); }
+    {
+        // pending partials of a stack-order prune of the full tree (the
+        // child needing more first, Sethi-Ullman): an element's pruned tree
+        // is a minor of the full tree and never needs more
+        std::vector<int> need(N, 0);
+        for (int s = S; s < N; s++) {
+            const int a = M.ch0[s], b = M.ch1[s];
+            const int na = a >= S ? need[a] : 0, nb = b >= S ? need[b] : 0;
+            if (a < S && b < S) need[s] = 1;
+            else if (a < S) need[s] = std::max(nb, 1);
+            else if (b < S) need[s] = std::max(na, 1);
+            else need[s] = std::max(std::max(na, nb), 1 + std::min(na, nb));
+        }
+        c->stack_cap = std::max(1, need[N - 1]);
+    }
     M.outgroup.assign(model->outgroup, model->outgroup + model->n_outgroup);
     M.conserve.assign(model->conserve, model->conserve + model->n_conserve);
     // upper / upper_conserve (getUppertree, bpp.cpp:486-504)
@@ -1239,7 +1255,7 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.n_int_cap = S - 1;
     v.TI = std::min(c->o.trace_iters, T);
     v.BT = plain_block_threads(c, v.prec);
-    v.smem = smem_bytes(N, v.BT, v.prec);
+    v.smem = smem_bytes(N, v.BT, v.prec, c->stack_cap);
     const int per_sm = std::max(1, chain_occupancy(v.prec, v.BT, v.smem));
     v.grid = c->n_sm * per_sm;
     v.ws1 = (ws_bytes(v.n_int_cap, v.GGp_cap, T, c->o.mcmc, N, v.prec) + 4095) & ~(size_t)4095;
@@ -1317,6 +1333,7 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.p.ws_stride = v.ws1;
     v.p.n_int_max = v.n_int_cap;
     v.p.GGp_max = v.GGp_cap;
+    v.p.stack_cap = c->stack_cap;
     v.p.counters = v.d_cnt;
     v.p.stream = 1;
     v.p.q_head = v.d_head;
@@ -1717,7 +1734,7 @@ static int run_pending(pacc_ctx* c) {
     if (batched_layout(c)) return run_batched(c, hdr, blob, off, n_int_max, GGuP_max);
     // launch geometry
     const int BT = plain_block_threads(c, prec);
-    size_t smem = smem_bytes(N, BT, prec);
+    size_t smem = smem_bytes(N, BT, prec, c->stack_cap);
     // resident CTAs per SM from the kernel's registers and shared memory
     int per_sm = std::max(1, chain_occupancy(prec, BT, smem));
     int grid = std::max(1, std::min(n, c->n_sm * per_sm));
@@ -1800,6 +1817,7 @@ static int run_pending(pacc_ctx* c) {
     p.ws_stride = ws1;
     p.n_int_max = n_int_max;
     p.GGp_max = GGp_max;
+    p.stack_cap = c->stack_cap;
     p.counters = (DevCounters*)(mb + o_cnt);
     p.z_start_zero = c->o.chain > 0 ? 1 : 0;
     if (hyp) {
@@ -2299,8 +2317,9 @@ int pacc_debug_loglik(pacc_ctx* c, const uint8_t* bases, int32_t length, const i
         p.ws_stride = ws;
         p.n_int_max = E.n_int;
         p.GGp_max = E.GGp;
+        p.stack_cap = c->stack_cap;
         int BT = 128;
-        e = launch_loglik(p, (const int32_t*)dz, c_rate, n_rate, (double*)dout, BT, smem_bytes(N, BT, prec), prec,
+        e = launch_loglik(p, (const int32_t*)dz, c_rate, n_rate, (double*)dout, BT, smem_bytes(N, BT, prec, c->stack_cap), prec,
                           c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)E.GG * 8, cudaMemcpyDeviceToHost);
