@@ -86,6 +86,12 @@ struct ChainScalars {
     double vb;
     int fallback;
     int n_list;            // entries of the current pass's node list
+    // FP32-partial path: logs kept with the rates so the monitor and the MH
+    // ratios need at most two new logarithms per step
+    double lcur_n, lcur_c; // log rate_n, log rate_c
+    double lpn;            // log prop_n
+    double lgn;            // lgamma(rate_n / prop_n), valid when lgn_ok
+    int lgn_ok;
 };
 
 // Reduction scratch: one slot per warp (<= 32), the broadcast slot RED_SUM
@@ -521,42 +527,87 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
     return r;
 }
 
-// Build the P^T table of class k for all nodes of the pruned tree (except the
-// root) at rate r.  Branches shorter than 1e-10 keep the identity
-// (bpp_c.cpp:191-226, 1123).  force_eigen: the proposal matrices of log_f_Xz
-// (bpp_c.cpp:887-902) and the Eval2 fallback (bpp_c2.cpp:220-237) apply the
-// eigen formula whatever the branch length.
-template <typename Real>
-__device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
-    // FP64 throughout: the eigen products cancel for the small entries of
-    // short branches, which FP32 arithmetic would not resolve
-    for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
-        int s = c.nodes[i];
-        if (sizeof(Real) == 8) {
-            double* out = c.ptd + ((size_t)k * c.N + s) * 16;
-            if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, out);
-            else identity_pt(out);
-        } else {
-            double tmp[16];
-            if (force_eigen || dist2[s] > 1e-10) build_pt(dist2[s], r, scaled, tmp);
-            else identity_pt(tmp);
-            Real* o2 = c.ptr + ((size_t)k * c.N + s) * 16;
+// P^T(d r) of the FP32-partial path: the exponentials exp(lambda_i d r) in
+// FP64, then the 4x4 product in FP32 as I + sum_i A_i (exp(lambda_i d r) - 1)
+// with A_i = eigeninv[:, i] eigenvec[i, :].  Its terms are of the size of the
+// result, so the small entries of short branches do not come from
+// cancelling O(1) terms (as they would in eigeninv diag(e) eigenvec).
+static __device__ __noinline__ void build_pt32(double d, double r, bool scaled, float* out) {
+    float em1[4];
 #pragma unroll
-            for (int q = 0; q < 16; q++) o2[q] = (Real)tmp[q];
-        }
-        c.local.pmat++;
+    for (int i = 0; i < 4; i++) {
+        double x = __dmul_rn(dM.lam[i], d);
+        if (scaled) x = __dmul_rn(x, r);
+        em1[i] = (float)(d_exp(x) - 1.0);
+    }
+#pragma unroll
+    for (int ab = 0; ab < 16; ab++) {
+        const float* A = dM.a32 + ab * 4;
+        float s = A[0] * em1[0];
+        s = fmaf(A[1], em1[1], s);
+        s = fmaf(A[2], em1[2], s);
+        s = fmaf(A[3], em1[3], s);
+        out[ab] = s + (((ab >> 2) == (ab & 3)) ? 1.0f : 0.0f);
     }
 }
 
+// P^T of class k for node s at rate r.  Branches shorter than 1e-10 keep the
+// identity (bpp_c.cpp:191-226, 1123) unless force_eigen: the proposal
+// matrices of log_f_Xz (bpp_c.cpp:887-902) and the Eval2 fallback
+// (bpp_c2.cpp:220-237) apply the eigen formula whatever the branch length.
 template <typename Real>
-__device__ void copy_class(Ctx<Real>& c, const double* dist2, int from, int to) {
-    // accepted proposal becomes the cache; branches < 1e-10 are not rebuilt (bpp_c.cpp:1123)
+__device__ __forceinline__ void build_one(Ctx<Real>& c, const double* dist2, int k, int s, double r, bool scaled,
+                                          bool force_eigen) {
+    const bool eig = force_eigen || dist2[s] > 1e-10;
+    if (sizeof(Real) == 8) {
+        double* out = c.ptd + ((size_t)k * c.N + s) * 16;
+        if (eig) build_pt(dist2[s], r, scaled, out);
+        else identity_pt(out);
+    } else {
+        float* out = (float*)c.ptr + ((size_t)k * c.N + s) * 16;
+        if (eig) build_pt32(dist2[s], r, scaled, out);
+        else {
+#pragma unroll
+            for (int q = 0; q < 16; q++) out[q] = ((q >> 2) == (q & 3)) ? 1.0f : 0.0f;
+        }
+    }
+    c.local.pmat++;
+}
+
+// The P^T table of class k for all nodes of the pruned tree (except the root).
+template <typename Real>
+__device__ void build_class(Ctx<Real>& c, const double* dist2, int k, double r, bool scaled, bool force_eigen) {
+    for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) build_one(c, dist2, k, c.nodes[i], r, scaled, force_eigen);
+}
+
+// The proposal's matrices (log_f_Xz, bpp_c.cpp:885-906) for the branches a
+// proposal of class cls changes: those whose Z puts them in the class.  The
+// prune reads the proposal's matrices for exactly these children.
+template <typename Real>
+__device__ void build_prop(Ctx<Real>& c, const double* dist2, int cls, double r) {
     for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
-        int s = c.nodes[i];
+        const int s = c.nodes[i];
+        if (mat_class(c.Z[s], -1) == cls) build_one(c, dist2, P_PROP, s, r, true, true);
+    }
+}
+
+// An accepted proposal becomes the class's cache (bpp_c.cpp:1115-1131): the
+// branches that took the proposal's matrices keep them, the others get the
+// same matrices at the new rate; branches shorter than 1e-10 are not rebuilt
+// (bpp_c.cpp:1123).
+template <typename Real>
+__device__ void accept_class(Ctx<Real>& c, const double* dist2, int cls, double r) {
+    for (int i = threadIdx.x; i < c.n_nodes - 1; i += blockDim.x) {
+        const int s = c.nodes[i];
         if (dist2[s] < 1e-10) continue;
-        const Real* a = c.ptr + ((size_t)from * c.N + s) * 16;
-        Real* b = c.ptr + ((size_t)to * c.N + s) * 16;
-        for (int q = 0; q < 16; q++) b[q] = a[q];
+        if (mat_class(c.Z[s], -1) == cls) {
+            const Real* a = c.ptr + ((size_t)P_PROP * c.N + s) * 16;
+            Real* b = c.ptr + ((size_t)cls * c.N + s) * 16;
+#pragma unroll
+            for (int q = 0; q < 16; q++) b[q] = a[q];
+        } else {
+            build_one(c, dist2, cls, s, r, true, true);
+        }
     }
 }
 
@@ -997,11 +1048,22 @@ __device__ void mark_ancestors(Ctx<Real>& c, const int8_t* src, int8_t* dst, int
     __syncthreads();
 }
 
+// Log density of Gamma(shape a, scale b) at x > 0 without the exp/log round
+// trip: (a - 1) log x - x / b - lgamma(a) - a log b, with log x given.
+__device__ __forceinline__ double lgamma_pdf_lx(double x, double lx, double a, double b, double lga_alogb) {
+    return (a - 1.0) * lx - x / b - lga_alogb;
+}
+
 // One Metropolis-Hastings update of the accelerated (neut) or conserved rate
 // (sample_rate, bpp_c.cpp:930-1176), M = 1, adaptive factor 0.5.
+// FP64 partials follow the reference's arithmetic term by term.  FP32
+// partials keep the MH ratio in FP64 but evaluate it from cached logs of the
+// current rate and proposal scale (one new log per proposal, plus one lgamma
+// for the accelerated rate's Gamma proposal), and draw the proposal in FP32.
 template <typename Real>
 __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, double old_rate, int* tmp) {
     ChainScalars* cs = c.cs;
+    const bool f32 = sizeof(Real) == 4;
     const int8_t* unv = neut ? c.unvN : c.unvC;
     const int cls = neut ? P_NEUT : P_CONS;
     double prior_a = neut ? dM.nprior_a : dM.cprior_a;
@@ -1013,10 +1075,17 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
         if (threadIdx.x == 0) {
             double cur = old_rate;
             if (cs->resZ != 0) {
-                StreamReader rd;
-                rd.init(dM.seed, cs->pos);
-                cur = rd.gamma(prior_a, prior_b);
-                cs->pos = rd.pos;
+                if (f32) {
+                    StreamReader32 rd;
+                    rd.init(dM.seed, cs->pos);
+                    cur = (double)rd.gamma((float)prior_a, (float)prior_b);
+                    cs->pos = rd.pos;
+                } else {
+                    StreamReader rd;
+                    rd.init(dM.seed, cs->pos);
+                    cur = rd.gamma(prior_a, prior_b);
+                    cs->pos = rd.pos;
+                }
                 if (neut) {
                     if (dM.ropt == 1 && cur < dM.nlb) cur = old_rate;
                     else if (dM.ropt == 2 && cur < c.trd[TR_C * c.T + m]) cur = old_rate;
@@ -1026,13 +1095,16 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
                 }
             }
             cs->proposal = cur;
+            if (f32 && cur != old_rate) {
+                if (neut) { cs->lcur_n = d_log(cur); cs->lgn_ok = 0; }
+                else cs->lcur_c = d_log(cur);
+            }
         }
         __syncthreads();
         double cur = cs->proposal;
         if (cur != old_rate) build_class(c, dist2, cls, cur, true, false);
         __syncthreads();
         if (threadIdx.x == 0 && cur != old_rate) { if (neut) cs->acc_n++; else cs->acc_c++; }
-        old_rate = old_rate;  // (no-op, keeps the structure of the reference)
         __syncthreads();
         double r = cs->proposal;
         // adaptive step below
@@ -1040,25 +1112,40 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
         __syncthreads();
     } else {
         if (threadIdx.x == 0) {
-            StreamReader rd;
-            rd.init(dM.seed, cs->pos);
-            double r = rd.uniform();
-            double proposal;
+            double r, proposal;
             int skip = 0;
             double cur = old_rate;
+            if (f32) {
+                StreamReader32 rd;
+                rd.init(dM.seed, cs->pos);
+                r = word_to_uniform(rd.word_at(rd.pos++));
+                if (neut) proposal = (double)rd.gamma((float)(cur / cs->prop_n), (float)cs->prop_n);
+                else {
+                    double ip = 1.0 / cs->prop_c;
+                    proposal = cur * (r * (cs->prop_c - ip) + ip);
+                }
+                cs->pos = rd.pos;
+            } else {
+                StreamReader rd;
+                rd.init(dM.seed, cs->pos);
+                r = rd.uniform();
+                if (neut) {
+                    proposal = rd.gamma(__ddiv_rn(cur, cs->prop_n), cs->prop_n);
+                } else {
+                    double ip = __ddiv_rn(1.0, cs->prop_c);
+                    double u = __dadd_rn(__dmul_rn(r, __dsub_rn(cs->prop_c, ip)), ip);
+                    proposal = __dmul_rn(cur, u);
+                }
+                cs->pos = rd.pos;
+            }
             if (neut) {
-                proposal = rd.gamma(__ddiv_rn(cur, cs->prop_n), cs->prop_n);
                 if (dM.ropt == 1 && proposal < dM.nlb) skip = 1;
                 else if (dM.ropt == 2 && proposal < c.trd[TR_C * c.T + m]) skip = 1;
             } else {
-                double ip = __ddiv_rn(1.0, cs->prop_c);
-                double u = __dadd_rn(__dmul_rn(r, __dsub_rn(cs->prop_c, ip)), ip);
-                proposal = __dmul_rn(cur, u);
                 if (dM.ropt == 1 && proposal > dM.cub) skip = 1;
                 else if (dM.ropt == 2 && proposal > c.trd[TR_N * c.T + m + 1]) skip = 1;
             }
             if (!skip && (proposal < 1e-12 || proposal > 1e8)) skip = 1;
-            cs->pos = rd.pos;
             cs->proposal = proposal;
             cs->skip = skip;
             cs->mh_new = r;  // keep r for the decision
@@ -1066,27 +1153,59 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
         }
         __syncthreads();
         if (!cs->skip) {
-            build_class(c, dist2, P_PROP, cs->proposal, true, true);
+            build_prop(c, dist2, cls, cs->proposal);
             __syncthreads();
             double ll_new = prune(c, unv, true, cls);
             if (threadIdx.x == 0) {
                 double proposal = cs->proposal, cur = old_rate, r = cs->mh_new;
                 double MH;
-                if (neut)
-                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
-                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
-                                                     log_gamma_pdf(cur, prior_a, prior_b)),
-                                           log_gamma_pdf(cur, __ddiv_rn(proposal, cs->prop_n), cs->prop_n)),
-                                   log_gamma_pdf(proposal, __ddiv_rn(cur, cs->prop_n), cs->prop_n));
-                else
-                    MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
-                                                               log_gamma_pdf(proposal, prior_a, prior_b)),
-                                                     log_gamma_pdf(cur, prior_a, prior_b)),
-                                           d_log(cur)),
-                                   d_log(proposal));
-                if (d_log(r) < MH) {
-                    cs->accept = 1;
-                    cs->loglik = ll_new;
+                if (f32) {
+                    const double lp = d_log(proposal);
+                    if (neut) {
+                        const double pn = cs->prop_n, lpn = cs->lpn, lc = cs->lcur_n;
+                        const double s1 = proposal / pn, s2 = cur / pn;
+                        const double lg1 = d_lgamma(s1);
+                        const double lg2 = cs->lgn_ok ? cs->lgn : d_lgamma(s2);
+                        MH = (ll_new - cs->loglik) + lgamma_pdf_lx(proposal, lp, prior_a, prior_b, dM.kn) -
+                             lgamma_pdf_lx(cur, lc, prior_a, prior_b, dM.kn) +
+                             lgamma_pdf_lx(cur, lc, s1, pn, lg1 + s1 * lpn) -
+                             lgamma_pdf_lx(proposal, lp, s2, pn, lg2 + s2 * lpn);
+                        if (d_log(r) < MH) {
+                            cs->accept = 1;
+                            cs->loglik = ll_new;
+                            cs->lcur_n = lp;
+                            cs->lgn = lg1;
+                        } else {
+                            cs->lgn = lg2;
+                        }
+                        cs->lgn_ok = 1;
+                    } else {
+                        const double lc = cs->lcur_c;
+                        MH = (ll_new - cs->loglik) + lgamma_pdf_lx(proposal, lp, prior_a, prior_b, dM.kc) -
+                             lgamma_pdf_lx(cur, lc, prior_a, prior_b, dM.kc) + lc - lp;
+                        if (d_log(r) < MH) {
+                            cs->accept = 1;
+                            cs->loglik = ll_new;
+                            cs->lcur_c = lp;
+                        }
+                    }
+                } else {
+                    if (neut)
+                        MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
+                                                                   log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                         log_gamma_pdf(cur, prior_a, prior_b)),
+                                               log_gamma_pdf(cur, __ddiv_rn(proposal, cs->prop_n), cs->prop_n)),
+                                       log_gamma_pdf(proposal, __ddiv_rn(cur, cs->prop_n), cs->prop_n));
+                    else
+                        MH = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(ll_new, cs->loglik),
+                                                                   log_gamma_pdf(proposal, prior_a, prior_b)),
+                                                         log_gamma_pdf(cur, prior_a, prior_b)),
+                                               d_log(cur)),
+                                       d_log(proposal));
+                    if (d_log(r) < MH) {
+                        cs->accept = 1;
+                        cs->loglik = ll_new;
+                    }
                 }
             }
             __syncthreads();
@@ -1095,7 +1214,7 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
                     int s = c.internal[i];
                     if (unv[s] && !c.missing[s]) c.cur[s] ^= 1;
                 }
-                copy_class(c, dist2, P_PROP, cls);
+                accept_class(c, dist2, cls, cs->proposal);
             }
         }
         __syncthreads();
@@ -1120,6 +1239,7 @@ __device__ double sample_rate(Ctx<Real>& c, const double* dist2, bool neut, doub
             cs->prop_n = __dmul_rn(cs->prop_n, scale_adj);
             if (cs->prop_n > 1) cs->prop_n = 1;
             cs->acc_n = 0;
+            if (f32) { cs->lpn = d_log(cs->prop_n); cs->lgn_ok = 0; }
         } else {
             double rate = (double)cs->acc_c / dM.adapt_freq;
             if (rate > 0.44) scale_adj = d_exp(step);
@@ -1562,6 +1682,12 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 }
                 cs_.rate_n = c.trd[TR_N * T + 0];
                 cs_.rate_c = c.trd[TR_C * T + 0];
+                if (sizeof(Real) == 4) {
+                    cs_.lcur_n = d_log(cs_.rate_n);
+                    cs_.lcur_c = d_log(cs_.rate_c);
+                    cs_.lpn = d_log(cs_.prop_n);
+                    cs_.lgn_ok = 0;
+                }
             }
             for (int i = threadIdx.x; i < N; i += BT) { c.Z[i] = -1; c.fixZ[i] = -1; c.cur[i] = 0; }
             __syncthreads();
@@ -1616,8 +1742,15 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                     cs_.m = m;
                     double ll = cs_.loglik;
                     double full = ll + 0.0;
-                    full += log_gamma_pdf(c.trd[TR_C * T + m], dM.cprior_a, dM.cprior_b);
-                    if (resZ != 0) full += log_gamma_pdf(c.trd[TR_N * T + m], dM.nprior_a, dM.nprior_b);
+                    if (sizeof(Real) == 4) {
+                        // the rates' log priors from the logs kept with them
+                        full += lgamma_pdf_lx(c.trd[TR_C * T + m], cs_.lcur_c, dM.cprior_a, dM.cprior_b, dM.kc);
+                        if (resZ != 0)
+                            full += lgamma_pdf_lx(c.trd[TR_N * T + m], cs_.lcur_n, dM.nprior_a, dM.nprior_b, dM.kn);
+                    } else {
+                        full += log_gamma_pdf(c.trd[TR_C * T + m], dM.cprior_a, dM.cprior_b);
+                        if (resZ != 0) full += log_gamma_pdf(c.trd[TR_N * T + m], dM.nprior_a, dM.nprior_b);
+                    }
                     c.trd[TR_LL * T + m] = ll;
                     c.trd[TR_FULL * T + m] = full;
                     tmp_ = (m >= c.burn && full > cs_.maxll) ? 1 : 0;
@@ -1680,14 +1813,27 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                     double nZ[3][3];
                     for (int a = 0; a < 3; a++)
                         for (int b = 0; b < 3; b++) nZ[a][b] = (double)zcount[a * 3 + b];
-                    StreamReader rd;
-                    rd.init(dM.seed, cs_.pos);
-                    double gr = rd.beta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]);
-                    for (int a = 0; a < 3; a++)
-                        for (int b = 0; b < 3; b++) nZ[a][b] -= (double)zcount[9 + a * 3 + b];
-                    double lr = rd.beta(dM.la + nZ[2][1], dM.lb + nZ[1][1]);
-                    double lr2 = (dM.l2a == 0) ? 0.0 : rd.beta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]);
-                    cs_.pos = rd.pos;
+                    double gr, lr, lr2;
+                    if (sizeof(Real) == 4) {
+                        // FP32 draws (the transition rates feed the Z filter)
+                        StreamReader32 rd;
+                        rd.init(dM.seed, cs_.pos);
+                        gr = (double)rd.beta((float)(dM.ga + nZ[1][0] + nZ[2][0]), (float)(dM.gb + nZ[0][0]));
+                        for (int a = 0; a < 3; a++)
+                            for (int b = 0; b < 3; b++) nZ[a][b] -= (double)zcount[9 + a * 3 + b];
+                        lr = (double)rd.beta((float)(dM.la + nZ[2][1]), (float)(dM.lb + nZ[1][1]));
+                        lr2 = (dM.l2a == 0) ? 0.0 : (double)rd.beta((float)(dM.l2a + nZ[1][2]), (float)(dM.l2b + nZ[2][2]));
+                        cs_.pos = rd.pos;
+                    } else {
+                        StreamReader rd;
+                        rd.init(dM.seed, cs_.pos);
+                        gr = rd.beta(dM.ga + nZ[1][0] + nZ[2][0], dM.gb + nZ[0][0]);
+                        for (int a = 0; a < 3; a++)
+                            for (int b = 0; b < 3; b++) nZ[a][b] -= (double)zcount[9 + a * 3 + b];
+                        lr = rd.beta(dM.la + nZ[2][1], dM.lb + nZ[1][1]);
+                        lr2 = (dM.l2a == 0) ? 0.0 : rd.beta(dM.l2a + nZ[1][2], dM.l2b + nZ[2][2]);
+                        cs_.pos = rd.pos;
+                    }
                     c.trd[TR_G * T + m + 1] = gr;
                     c.trd[TR_L * T + m + 1] = lr;
                     c.trd[TR_L2 * T + m + 1] = lr2;

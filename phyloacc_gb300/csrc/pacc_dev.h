@@ -41,6 +41,11 @@ struct DevModel {
     double la, lb, ga, gb, l2a, l2b;
     double cons_to_mis;
     int trace_iters;
+    // FP32-partial path: P^T(d r)[a][b] = [a == b] + sum_i A[a][b][i] (exp(lambda_i d r) - 1)
+    // with A[a][b][i] = eigeninv[a][i] * eigenvec[i][b] rounded to FP32
+    float a32[64];
+    // log normalisers lgamma(a) + a log(b) of the conserved and accelerated rate priors
+    double kc, kn;
 };
 
 // Per-element topology after missing-taxon pruning (bpp_c.hpp:331-428),

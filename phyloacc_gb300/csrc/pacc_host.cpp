@@ -667,6 +667,11 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     dm.l2a = opts->hyper_lrate2_a; dm.l2b = opts->hyper_lrate2_b;
     dm.cons_to_mis = opts->cons_to_mis;
     dm.trace_iters = opts->trace_iters;
+    for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 4; b++)
+            for (int i = 0; i < 4; i++) dm.a32[(a * 4 + b) * 4 + i] = (float)(dm.einv[a * 4 + i] * dm.evec[i * 4 + b]);
+    dm.kc = std::lgamma(dm.cprior_a) + dm.cprior_a * std::log(dm.cprior_b);
+    dm.kn = std::lgamma(dm.nprior_a) + dm.nprior_a * std::log(dm.nprior_b);
     c->device = opts->device;
     // Without a usable GPU the context still serves the host-only entry points
     // (pacc_debug_encode); every device call then fails with PACC_ECUDA.

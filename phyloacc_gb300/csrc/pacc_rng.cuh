@@ -105,6 +105,62 @@ struct StreamReader {
     }
 };
 
+// The same samplers in FP32 arithmetic, for the FP32-partial path (its
+// rate proposals and transition-rate draws; the MH ratio stays FP64).
+// Uniforms take the top 24 bits of a word: ((w >> 8) + 0.5) * 2^-24.
+struct StreamReader32 {
+    uint32_t seed;
+    uint64_t pos;
+    uint64_t blk;
+    uint32_t cache[4];
+    __device__ void init(uint32_t s, uint64_t p) { seed = s; pos = p; blk = ~0ull; }
+    __device__ uint32_t word_at(uint64_t w) {
+        const uint64_t b = w >> 2;
+        if (b != blk) {
+            philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), 0u, 0u, seed, 0u, cache);
+            blk = b;
+        }
+        return cache[w & 3];
+    }
+    __device__ float uniform() { return ((float)(word_at(pos++) >> 8) + 0.5f) * 5.9604644775390625e-08f; }
+    __device__ float normal() {
+        const float u1 = uniform();
+        const float u2 = uniform();
+        return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+    }
+    // Marsaglia-Tsang for shape >= 1; returns (b*d)*v.
+    __device__ float gamma_ge1(float a, float b) {
+        const float d = a - 1.0f / 3.0f;
+        const float c = 1.0f / sqrtf(9.0f * d);
+        float x, v;
+        for (int guard = 0; guard < 100000; guard++) {
+            do {
+                x = normal();
+                v = 1.0f + c * x;
+            } while (v <= 0.0f);
+            v = v * v * v;
+            const float u = uniform();
+            const float x2 = x * x;
+            if (u < 1.0f - 0.0331f * x2 * x2) break;
+            if (logf(u) < 0.5f * x2 + d * (1.0f - v + logf(v))) break;
+        }
+        return b * d * v;
+    }
+    __device__ __noinline__ float gamma(float a, float b) {
+        if (a < 1.0f) {
+            const float g = gamma_ge1(a + 1.0f, 1.0f);
+            const float u = uniform();
+            return b * g * powf(u, 1.0f / a);
+        }
+        return gamma_ge1(a, b);
+    }
+    __device__ float beta(float a, float b) {
+        const float x = gamma(a, 1.0f);
+        const float y = gamma(b, 1.0f);
+        return x / (x + y);
+    }
+};
+
 // Inverse-CDF categorical draw over K unnormalised weights (K <= 4).
 template <typename T>
 __device__ __forceinline__ int categorical(int K, const T* p, double u) {

@@ -40,8 +40,10 @@ def test_fp32_loglik_underflow_stress(built):
                                        (abi.PACC_FP32_WARP, 4)])
 def test_fp32_chain_tracks_fp64_on_stress_set(built, prec, cols):
     """While the FP32 and FP64 chains agree on Z and on every rate (the same
-    draws and decisions), their log-likelihoods agree to 1e-6 relative; the
-    chains may part later on a near-tie decision."""
+    draws and decisions; the CTA FP32 path draws its Gamma/Beta variates in
+    FP32, so its rates agree to about 1e-7 relative), their log-likelihoods
+    agree to 1e-6 relative; the chains may part later on a near-tie
+    decision."""
     ds = synth.make_dataset("st43_stress", n_elements=4, seed=5)
     o = abi.default_opts()
     o.seed, o.burnin, o.mcmc, o.trace_iters = 2, 20, 40, 60
@@ -55,7 +57,7 @@ def test_fp32_chain_tracks_fp64_on_stress_set(built, prec, cols):
         for m in range(3):
             same = (g32.tr_z[e, m] == g64.tr_z[e, m]).all(axis=1)
             for k in ("n_rate", "c_rate", "g_rate", "l_rate"):
-                same &= g32.tr[k][e, m] == g64.tr[k][e, m]
+                same &= np.abs(g32.tr[k][e, m] - g64.tr[k][e, m]) <= 1e-5 * np.abs(g64.tr[k][e, m])
             upto = len(same) if same.all() else int(np.argmin(same))
             a, b = g32.tr["loglik"][e, m, :upto], g64.tr["loglik"][e, m, :upto]
             assert (np.abs(a - b) <= TOL_LL * np.abs(b)).all(), (e, m)
