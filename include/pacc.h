@@ -108,7 +108,11 @@ typedef struct pacc_opts {
     int32_t max_resident;         /* max chains resident at once (0 = derived from the budget) */
     int32_t sweeps_per_launch;    /* MCMC iterations per kernel launch (0 = run chains to completion) */
     int32_t trace_iters;          /* record the first trace_iters iterations of every model (0 = off) */
-    int32_t block_threads;        /* threads per chain CTA (0 = 128) */
+    int32_t block_threads;        /* threads per chain CTA (0 = chosen by the trial-launch tuner:
+                                     the fastest of a few threads-per-chain / registers-a-thread /
+                                     chains-per-SM shapes on a short trial of the first batch,
+                                     remembered per device, taxon count and precision; results do
+                                     not depend on the shape) */
     int32_t use_graphs;           /* capture the sweep launches in a CUDA graph (1) */
     int32_t columns_per_lane;     /* batched kernel: alignment columns each lane carries (1, 2 or 4;
                                      0 = autotuned) */
@@ -119,6 +123,13 @@ typedef struct pacc_opts {
     int32_t sample_hyper;         /* SAMPLE_HYPER chain (main.cpp:466-494): only the full model M2
                                      runs, from the batch's start states, and every result returns
                                      its end state; PACC_FP64 and PACC_FP32 without serving */
+    int64_t serve_idle_ns;        /* serving on the CTA layout: a block of the persistent launch that
+                                     has waited this long for work returns (0 = 30 s); elements
+                                     published after every block left are taken by the next launch */
+    int32_t register_budget;      /* CTA kernel with FP32 partials: registers a thread, 128 (four
+                                     128-thread chains per SM), 168 (three) or 255 (two); 0 = chosen
+                                     together with block_threads by a trial-launch tuner */
+    int32_t reserved0;
 } pacc_opts;
 
 /* A batch of elements.  Element e's alignment block is n_species rows of
@@ -220,11 +231,23 @@ typedef struct pacc_counters {
     double iterations;             /* MCMC iterations run (all models) */
     double kernel_ms;              /* summed duration of the chain kernels (CUDA events) */
     double flop;                   /* algorithmic FP work of the prunes, counted from the above */
-    double phase_cycles[8];        /* batched kernel, SM cycles summed over chains: internal-base pass,
-                                      emission sums, Z filter, Z-change likelihood, accelerated-rate MH,
-                                      conserved-rate MH, monitor/transitions, model init + Eval2 + output */
+    double phase_cycles[8];        /* SM cycles summed over chains.  CTA kernel: monitor, internal-base
+                                      pass (with the emission histogram), emission sums, Z filter,
+                                      Z-change likelihood, accelerated-rate MH, conserved-rate MH,
+                                      transitions.  Warp kernel: internal-base pass, emission sums, Z
+                                      filter, Z-change likelihood, accelerated-rate MH, conserved-rate
+                                      MH, monitor/transitions, model init + Eval2 + output */
+    double serve_idle_exits;       /* serving (CTA layout): blocks that left a launch on the idle bound */
 } pacc_counters;
 int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);
+
+/* Launch shape of the CTA-per-chain kernel (no counterpart in the reference):
+ * threads per chain, registers a thread, resident chains per SM and the
+ * duration of the tuner's trial launches (0 when the shape was fixed by the
+ * options or taken from an earlier context).  Zeros before the first launch
+ * or on the warp-per-chain layouts. */
+int pacc_get_launch_shape(pacc_ctx* ctx, int32_t* block_threads, int32_t* registers, int32_t* chains_per_sm,
+                          double* trial_ms);
 
 /* --- Kernel-level entry points used by parity tests (same kernels as the chain) --- */
 

@@ -57,6 +57,8 @@ def lib():
                                           C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.pacc_debug_stream.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint32)]
         L.pacc_measure_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.pacc_get_launch_shape.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -133,6 +135,16 @@ class Context:
         out = {n: getattr(c, n) for n, _ in abi.PaccCounters._fields_ if n != "phase_cycles"}
         out["phase_cycles"] = list(c.phase_cycles)
         return out
+
+    def launch_shape(self) -> dict:
+        """Threads per chain, registers a thread and chains per SM of the
+        CTA kernel (the tuner's choice), and the tuner's trial time in ms."""
+        bt, regs, per_sm, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        st = lib().pacc_get_launch_shape(self.h, C.byref(bt), C.byref(regs), C.byref(per_sm), C.byref(ms))
+        if st != 0:
+            self._err("pacc_get_launch_shape", st)
+        return {"block_threads": bt.value, "registers": regs.value, "chains_per_sm": per_sm.value,
+                "tuner_trial_ms": ms.value}
 
     def pmatrix(self, d, r) -> np.ndarray:
         d = np.ascontiguousarray(d, dtype=np.float64)

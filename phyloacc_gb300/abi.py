@@ -64,6 +64,7 @@ class PaccOpts(C.Structure):
         ("max_resident", C.c_int32), ("sweeps_per_launch", C.c_int32), ("trace_iters", C.c_int32),
         ("block_threads", C.c_int32), ("use_graphs", C.c_int32), ("columns_per_lane", C.c_int32),
         ("chain", C.c_int32), ("sample_hyper", C.c_int32),
+        ("serve_idle_ns", C.c_int64), ("register_budget", C.c_int32), ("reserved0", C.c_int32),
     ]
 
 
@@ -85,6 +86,7 @@ def default_opts() -> PaccOpts:
     o.precision, o.device, o.memory_budget_bytes = PACC_FP64, 0, 0
     o.max_resident, o.sweeps_per_launch, o.trace_iters = 0, 0, 0
     o.block_threads, o.use_graphs, o.columns_per_lane, o.chain, o.sample_hyper = 0, 1, 0, 0, 0
+    o.serve_idle_ns, o.register_budget = 0, 0
     return o
 
 
@@ -135,7 +137,8 @@ class PaccResult(C.Structure):
 class PaccCounters(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "edge_updates_internal", "edge_updates_leaf", "column_loglik", "tg_draws", "z_draws",
-        "pmatrix_builds", "iterations", "kernel_ms", "flop")] + [("phase_cycles", C.c_double * 8)]
+        "pmatrix_builds", "iterations", "kernel_ms", "flop")] + [("phase_cycles", C.c_double * 8),
+                                                                  ("serve_idle_exits", C.c_double)]
 
 
 def ptr(a: np.ndarray, ctype):

@@ -96,7 +96,7 @@ struct ChainScalars {
 
 // Reduction scratch: one slot per warp (<= 32), the broadcast slot RED_SUM
 // and the median slot RED_MED.
-static const int RED_SUM = 32, RED_MED = 33, RED_SLOTS = 40;
+static const int RED_SUM = 80, RED_MED = 81, RED_SLOTS = 88;
 
 // Slots of the sampling pass's ring of column data copied ahead into
 // shared memory (cp.async): the nodes up to RING-1 steps ahead are in
@@ -176,23 +176,70 @@ enum { P_NULL = 0, P_CONS = 1, P_NEUT = 2, P_PROP = 3 };
 // ---------------------------------------------------------------------------
 // Small helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double block_sum(double v, double* red) {
-    // deterministic: warp tree then warps in order
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+// Exact sum of per-column log-likelihoods.  Each column's FP64 value v is
+// held exactly in 64.64 fixed point (floor(v) and the 64-bit fraction
+// (v - floor(v)) * 2^64; exact for |v| >= 2^-12, below that the bits under
+// 2^-64 are dropped) and added in 128-bit integers, which is associative: the
+// total does not depend on how columns are spread over threads, and it is
+// the exact sum of the column values rounded once (more than the Kahan
+// compensation of an FP64 running sum gives).  A column of -inf or NaN makes
+// the total -inf or NaN, as log-sum-exp accumulation does.
+struct ColSum {
+    __int128 acc;
+    int bad;      // bit 0: a -inf column; bit 1: a NaN or +inf column
+    __device__ __forceinline__ void init() { acc = 0; bad = 0; }
+    __device__ __forceinline__ void add(double v) {
+        if (!(v > -CUDART_INF && v < CUDART_INF)) {
+            bad |= (v == -CUDART_INF) ? 1 : 2;
+            return;
+        }
+        const double h = floor(v);
+        const long long hi = (long long)h;
+        const unsigned long long lo = (unsigned long long)((v - h) * 18446744073709551616.0);
+        acc += ((__int128)hi << 64) + (__int128)lo;
+    }
+};
+
+// Block-wide total of the threads' ColSums (every thread gets the result).
+__device__ __forceinline__ double block_colsum(ColSum s, double* red) {
+    unsigned long long lo = (unsigned long long)s.acc;
+    long long hi = (long long)(s.acc >> 64);
+    int bad = s.bad;
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long lo2 = __shfl_down_sync(0xffffffffu, lo, o);
+        const long long hi2 = __shfl_down_sync(0xffffffffu, hi, o);
+        bad |= __shfl_down_sync(0xffffffffu, bad, o);
+        const __int128 t = (((__int128)hi << 64) | lo) + (((__int128)hi2 << 64) | lo2);
+        lo = (unsigned long long)t;
+        hi = (long long)(t >> 64);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    unsigned long long* r64 = (unsigned long long*)red;   // [warp][lo, hi], then the flags
+    int* rbad = (int*)(r64 + 2 * 32);
     __syncthreads();
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    double r = 0;
-    if (threadIdx.x == 0) {
-        int nw = blockDim.x >> 5;
-        for (int i = 0; i < nw; i++) r += red[i];
-        red[RED_SUM] = r;
+    if (l == 0) {
+        r64[2 * w] = lo;
+        r64[2 * w + 1] = (unsigned long long)hi;
+        rbad[w] = bad;
     }
     __syncthreads();
-    r = red[RED_SUM];
+    if (threadIdx.x == 0) {
+        __int128 t = 0;
+        int b = 0;
+        const int nw = blockDim.x >> 5;
+        for (int i = 0; i < nw; i++) {
+            t += ((__int128)(long long)r64[2 * i + 1] << 64) | r64[2 * i];
+            b |= rbad[i];
+        }
+        double v = (double)(long long)(t >> 64) + (double)(unsigned long long)t * 0x1p-64;
+        if (b & 2) v = CUDART_NAN;
+        else if (b & 1) v = -CUDART_INF;
+        red[RED_SUM] = v;
+    }
     __syncthreads();
-    return r;
+    const double v = red[RED_SUM];
+    __syncthreads();
+    return v;
 }
 
 __device__ __forceinline__ int block_or(int v, int* tmp) {
@@ -415,12 +462,8 @@ template <typename Real>
 __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class) {
     const int n = build_prune_list(c, unv, mh, prop_class);
     const int BT = blockDim.x, tid = threadIdx.x;
-    double ll_sum = 0;
-    // FP32 partials: the thread's columns are combined as an FP64 product of
-    // root-sum mantissas with an exact integer exponent, and one log at the
-    // end, instead of one FP64 log per column
-    double mprod = 1.0;
-    long long mexp = 0;
+    ColSum ll;
+    ll.init();
     unsigned long long e_int = 0, e_leaf = 0;
     int overflow = 0;
     for (int g = tid; g < c.GG; g += BT) {
@@ -495,14 +538,17 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
             if (d.is_root) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) a[j] *= (Real)dM.pi[j];
-                double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
+                const double t = (double)a[0] + (double)a[1] + (double)a[2] + (double)a[3];
                 if (sizeof(Real) == 8) {
-                    ll_sum += d_log(t) + (double)sc * 0.6931471805599453;
+                    ll.add(d_log(t) + (double)sc * 0.6931471805599453);
                 } else {
-                    int e1, e2;
-                    mprod *= frexp(t, &e1);
-                    mprod = frexp(mprod, &e2);
-                    mexp += (long long)e1 + e2 + sc;
+                    // FP32 partials: the column's log from its FP64 root sum
+                    // t = m 2^e as (e + scale) ln 2 + log m, log m in FP32 (the
+                    // partials carry FP32 rounding already)
+                    int e1;
+                    const double mt = frexp(t, &e1);
+                    ll.add(t > 0 ? (double)(e1 + sc) * 0.6931471805599453 + (double)logf((float)mt)
+                                 : (t == 0 ? -CUDART_INF : CUDART_NAN));
                 }
             }
             st4(c.lam + ((size_t)d.dst + g) * 4, a);
@@ -521,8 +567,7 @@ __device__ double prune(Ctx<Real>& c, const int8_t* unv, bool mh, int prop_class
     if (overflow) atomicOr(&c.cs->status, 1);
     c.local.edge_internal += e_int;
     c.local.edge_leaf += e_leaf;
-    if (sizeof(Real) != 8) ll_sum = d_log(mprod) + (double)mexp * 0.6931471805599453;
-    double r = block_sum(ll_sum, c.red);
+    double r = block_colsum(ll, c.red);
     if (threadIdx.x == 0) c.local.col_ll += c.GG;
     return r;
 }
@@ -780,11 +825,9 @@ __device__ int sample_emit(Ctx<Real>& c, uint64_t pos) {
             const float u = ((float)(wd >> 8) + 0.5f) * 5.9604644775390625e-08f;
             const float tot = ((float)q[0] + (float)q[1]) + ((float)q[2] + (float)q[3]);
             const float t = u * tot;
-            float cum = 0;
-            for (int k = 0; k < 4; k++) {
-                cum += (float)q[k];
-                if (t < cum) return k;
-            }
+            // the first k with t < cum_k, from three compares (cum is non-decreasing)
+            const float c0 = (float)q[0], c1 = c0 + (float)q[1], c2 = c1 + (float)q[2], c3 = c2 + (float)q[3];
+            if (t < c3) return (t >= c0) + (t >= c1) + (t >= c2);
             for (int k = 3; k >= 0; k--)
                 if (q[k] > 0) return k;
             return 4;
@@ -1537,10 +1580,12 @@ __device__ void bind_smem(Ctx<Real>& c, unsigned char* smem, int N, int BT, int 
     c.sn = (SNode*)(smem + L.desc);
 }
 
-// FP32 runs up to 256 threads with two blocks per SM (128 registers a
-// thread); FP64 may use more registers.
-template <typename Real>
-__global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(ChainParams P) {
+// Register budgets (launch bounds MAXT threads, MINB blocks per SM): FP32
+// partials come in three (128 registers: four 128-thread chains per SM; 168:
+// three; 255: two, or one of 256 threads), chosen per taxon count by the
+// host's trial-launch tuner; FP64 partials use one (255).
+template <typename Real, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) chain_kernel(ChainParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ChainScalars cs_;
     __shared__ int tmp_;
@@ -1554,12 +1599,12 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
     int16_t* t16 = c.nodes;
     double* dist2_ = (double*)(smem + SmemLayout<Real>::make(N, BT, P.stack_cap).dist);
     c.cs = &cs_;
-    c.burn = dM.burnin;
-    c.mcmc = dM.mcmc;
-    c.T = dM.burnin + dM.mcmc;
+    c.burn = P.trial_mcmc > 0 ? P.trial_burn : dM.burnin;
+    c.mcmc = P.trial_mcmc > 0 ? P.trial_mcmc : dM.mcmc;
+    c.T = c.burn + c.mcmc;
     const int T = c.T;
     char* ws = P.ws + (size_t)blockIdx.x * P.ws_stride;
-    WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, T, dM.mcmc, N, sizeof(Real));
+    WsLayout W = WsLayout::make(P.n_int_max, P.GGp_max, T, c.mcmc, N, sizeof(Real));
     c.lam = (Real*)(ws + W.lam);
     c.scl = (int32_t*)(ws + W.scale);
     c.act = (int8_t*)(ws + W.tg);
@@ -1598,7 +1643,10 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                         }
                         continue;
                     }
-                    if ((long long)(globaltimer_ns() - t0) > P.idle_ns) break;
+                    if ((long long)(globaltimer_ns() - t0) > P.idle_ns) {
+                        if (P.counters) atomicAdd(&P.counters->idle_exits, 1ull);
+                        break;
+                    }
                     __nanosleep(4000);
                 }
             }
@@ -1621,7 +1669,7 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
             if (threadIdx.x == 0) R->status = 1;
             continue;
         }
-        c.local = DevCounters{0, 0, 0, 0, 0, 0, 0};
+        c.local = DevCounters{};
         c.GG = H.GG; c.GGp = H.GGp; c.root = H.root; c.n_nodes = H.n_nodes; c.n_int = H.n_int;
         c.n_hlev = H.n_hlev; c.n_dlev = H.n_dlev; c.tg_draws = H.tg_draws;
         c.codes = P.blob + H.codes_off;
@@ -1788,14 +1836,17 @@ __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? 2 : 1) chain_kernel(C
                 // rates (bpp_c.cpp:434-452)
                 mark_ancestors(c, nullptr, c.unvN, 1, &tmp_);
                 mark_ancestors(c, nullptr, c.unvC, 2, &tmp_);
-                double rn = sample_rate(c, dist2_, true, c.trd[TR_N * T + m], &tmp_);
-                if (threadIdx.x == 0) c.trd[TR_N * T + m + 1] = rn;
-                __syncthreads();
-                CHAIN_PHASE(5);
-                double rc = sample_rate(c, dist2_, false, c.trd[TR_C * T + m], &tmp_);
-                if (threadIdx.x == 0) c.trd[TR_C * T + m + 1] = rc;
-                __syncthreads();
-                CHAIN_PHASE(6);
+                // accelerated, then conserved rate: one copy of the MH code
+                // (and its prune) serves both
+#pragma unroll 1
+                for (int q = 0; q < 2; q++) {
+                    const int row = q == 0 ? TR_N : TR_C;
+                    const double rr = sample_rate(c, dist2_, q == 0, c.trd[row * T + m], &tmp_);
+                    if (threadIdx.x == 0) c.trd[row * T + m + 1] = rr;
+                    __syncthreads();
+                    if (q == 0) CHAIN_PHASE(5);
+                    else CHAIN_PHASE(6);
+                }
                 // transitions of Z (sample_transition, bpp_c.cpp:522-613): the
                 // (child, parent) state counts in parallel (exact integers),
                 // then the three Beta draws on one thread
@@ -1959,7 +2010,7 @@ __global__ void loglik_kernel(ChainParams P, const int32_t* z, double c_rate, do
     c.lam = (Real*)(ws + W.lam);
     c.scl = (int32_t*)(ws + W.scale);
     c.act = (int8_t*)(ws + W.tg);
-    c.local = DevCounters{0, 0, 0, 0, 0, 0, 0};
+    c.local = DevCounters{};
     const int16_t* topo = (const int16_t*)(P.blob + H.topo_off);
     for (int i = threadIdx.x; i < TL.total; i += BT) c.nodes[i] = topo[i];
     const double* d2 = (const double*)(P.blob + H.topo_off + (size_t)((TL.total * 2 + 15) & ~15));
@@ -2017,29 +2068,42 @@ size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec) {
 
 size_t topo_bytes(int N) { return (size_t)((TopoLayout::make(N).total * 2 + 15) & ~15) + (size_t)N * 8; }
 
-// Resident CTAs per SM of the chain kernel for this block size and shared memory.
-int chain_occupancy(int prec, int BT, size_t smem) {
+// Kernel instances: FP64 partials one register budget, FP32 partials three
+// (variant 0: 128 registers, 1: 168, 2: 255).
+int chain_variants(int prec) { return prec == 0 ? 1 : 3; }
+int chain_variant_max_threads(int prec, int v) { return (prec == 0 || v == 2) ? 256 : 128; }
+
+template <typename K>
+static int occupancy_of(K k, int BT, size_t smem) {
     int nb = 0;
-    cudaError_t e;
-    if (prec == 0) {
-        e = cudaFuncSetAttribute(chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, chain_kernel<double>, BT, smem);
-    } else {
-        e = cudaFuncSetAttribute(chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, chain_kernel<float>, BT, smem);
-    }
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, BT, smem);
     return e == cudaSuccess ? nb : 0;
 }
 
-cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st) {
-    if (prec == 0) {
-        cudaFuncSetAttribute(chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        chain_kernel<double><<<grid, BT, smem, st>>>(p);
-    } else {
-        cudaFuncSetAttribute(chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        chain_kernel<float><<<grid, BT, smem, st>>>(p);
-    }
+// Resident CTAs per SM of a chain kernel instance for this block size and shared memory.
+int chain_occupancy(int prec, int variant, int BT, size_t smem) {
+    if (BT > chain_variant_max_threads(prec, variant)) return 0;
+    if (prec == 0) return occupancy_of(chain_kernel<double, 256, 1>, BT, smem);
+    if (variant == 0) return occupancy_of(chain_kernel<float, 128, 4>, BT, smem);
+    if (variant == 1) return occupancy_of(chain_kernel<float, 128, 3>, BT, smem);
+    return occupancy_of(chain_kernel<float, 256, 1>, BT, smem);
+}
+
+template <typename K>
+static cudaError_t launch_of(K k, const ChainParams& p, int grid, int BT, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, BT, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, int variant, cudaStream_t st) {
+    if (BT > chain_variant_max_threads(prec, variant)) return cudaErrorInvalidConfiguration;
+    if (prec == 0) return launch_of(chain_kernel<double, 256, 1>, p, grid, BT, smem, st);
+    if (variant == 0) return launch_of(chain_kernel<float, 128, 4>, p, grid, BT, smem, st);
+    if (variant == 1) return launch_of(chain_kernel<float, 128, 3>, p, grid, BT, smem, st);
+    return launch_of(chain_kernel<float, 256, 1>, p, grid, BT, smem, st);
 }
 
 cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate, double n_rate, double* out, int BT,

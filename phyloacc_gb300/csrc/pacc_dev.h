@@ -119,7 +119,8 @@ struct DevResult {
 // Work counters accumulated by the kernel (atomicAdd per CTA per element).
 struct DevCounters {
     unsigned long long edge_internal, edge_leaf, col_ll, tg_draws, z_draws, pmat, iters;
-    unsigned long long phase_cycles[8];  // batched kernel: cycles per phase (summed over warps)
+    unsigned long long phase_cycles[8];  // cycles per phase (summed over chains)
+    unsigned long long idle_exits;       // serving: blocks that left on the idle bound
 };
 
 // One internal node of the pruned tree, in postorder, as the batched kernel
@@ -150,6 +151,7 @@ struct ChainParams {
     size_t ws_stride;
     int n_int_max, GGp_max;
     int stack_cap;             // rows of the prune's shared-memory stack (>= every element's stack_depth)
+    int trial_burn, trial_mcmc;  // > 0: a tuning trial with these chain lengths instead of the model's
     DevCounters* counters;
     // stream mode (serving): CTAs take slots from a queue the host appends to
     // while the kernel runs; element data and results are indexed by slot.

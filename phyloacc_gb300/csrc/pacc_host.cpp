@@ -32,10 +32,12 @@ namespace pacc {
 
 cudaError_t set_model(const DevModel& m, cudaStream_t st);
 size_t smem_bytes(int N, int BT, int prec, int D);
-int chain_occupancy(int prec, int BT, size_t smem);
+int chain_occupancy(int prec, int variant, int BT, size_t smem);
+int chain_variants(int prec);
+int chain_variant_max_threads(int prec, int v);
 size_t ws_bytes(int n_int, int GGp, int T, int mcmc, int N, int prec);
 size_t topo_bytes(int N);
-cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, cudaStream_t st);
+cudaError_t launch_chain(const ChainParams& p, int grid, int BT, size_t smem, int prec, int variant, cudaStream_t st);
 cudaError_t launch_loglik(const ChainParams& p, const int32_t* z, double c_rate, double n_rate, double* out, int BT,
                           size_t smem, int prec, cudaStream_t st);
 cudaError_t launch_pmatrix(int n, const double* d, const double* r, double* out, cudaStream_t st);
@@ -432,7 +434,7 @@ struct Server {
 // for a while returns; the host launches again when work arrives.
 struct StreamServer {
     bool ready = false;
-    int n_slots = 0, grid = 0, BT = 128, prec = 0, GG_cap = 0, GGp_cap = 0, n_int_cap = 0, TI = 0;
+    int n_slots = 0, grid = 0, BT = 128, variant = 0, prec = 0, GG_cap = 0, GGp_cap = 0, n_int_cap = 0, TI = 0;
     size_t smem = 0, ws1 = 0, blob_b = 0, o_tg = 0, o_prefix = 0, o_topo = 0;
     char* dev = nullptr;
     ElemHeader* d_hdr = nullptr;
@@ -478,6 +480,10 @@ struct pacc_ctx {
     int device = 0;
     int n_sm = 0;
     int stack_cap = 1;       // pending partials of the CTA kernel's prune (the full tree's stack order)
+    // launch shape of the CTA-per-chain kernel (chosen at the first launch)
+    bool shape_ready = false;
+    int shape_variant = 0, shape_bt = 128, shape_per_sm = 0;
+    double shape_trial_ms = 0;
     bool gpu_ok = false;
     cudaStream_t stream = nullptr;
     // pending and finished work
@@ -586,6 +592,12 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
         return fail(PACC_EUNSUPPORTED, "SAMPLE_HYPER chains need PACC_FP64 or PACC_FP32 without serving");
     if (opts->mcmc < 1 || opts->burnin < 0 || opts->adapt_freq < 1)
         return fail(PACC_EINVAL, "MCMC must be >= 1, BURNIN >= 0, ADAPT_FREQ >= 1");
+    if (opts->register_budget != 0 && opts->register_budget != 128 && opts->register_budget != 168 &&
+        opts->register_budget != 255)
+        return fail(PACC_EINVAL, "register_budget must be 0, 128, 168 or 255");
+    if (opts->block_threads < 0 || opts->block_threads > 256 || opts->block_threads % 32 != 0)
+        return fail(PACC_EINVAL, "block_threads must be 0 or a multiple of 32 up to 256");
+    if (opts->serve_idle_ns < 0) return fail(PACC_EINVAL, "serve_idle_ns must be >= 0");
     pacc_ctx* c = new pacc_ctx();
     c->o = *opts;
     HostModel& M = c->M;
@@ -1217,15 +1229,213 @@ static int server_step(pacc_ctx* c) {
     return PACC_OK;
 }
 
-// Threads per chain of the CTA-per-chain kernel: the caller's, else 128.
-// With FP32 partials that fits four chains per SM (128 registers a thread,
-// about 54 KB of shared memory a chain at 43 taxa); with FP64 partials two
-// (214 registers a thread).  More chains per SM hide the chain's serial
-// steps better than more threads per chain.
-static int plain_block_threads(const pacc_ctx* c, int prec) {
-    (void)prec;
-    if (c->o.block_threads > 0) return c->o.block_threads;
-    return 128;
+// ---------------------------------------------------------------------------
+// packing of elements into one device blob
+// ---------------------------------------------------------------------------
+// Element data (codes, codes by column, initial Tg, draw prefix, topology and
+// branch lengths, site patterns) at 256-byte aligned offsets of one blob, and
+// the matching headers.  Returns the blob size.
+static size_t pack_elems(const pacc_ctx* c, const std::vector<const HostElem*>& els, std::vector<ElemHeader>& hdr,
+                         std::vector<uint8_t>& blob, int& n_int_max, int& GGp_max, int& GGuP_max) {
+    const int N = c->M.N, S = c->M.S;
+    const int n = (int)els.size();
+    hdr.assign(n, ElemHeader());
+    size_t off = 0;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    n_int_max = 1; GGp_max = 32; GGuP_max = 32;
+    const size_t tb = topo_bytes(N);
+    for (int e = 0; e < n; e++) {
+        const HostElem& E = *els[e];
+        ElemHeader& H = hdr[e];
+        std::memset(&H, 0, sizeof(H));
+        H.element_no = E.no;
+        H.filtered = E.filtered;
+        if (E.filtered) continue;
+        H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
+        H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws;
+        H.stack_depth = E.stack_depth;
+        H.codes_off = off; off = al(off + E.codes.size());
+        H.codes_t_off = off; off = al(off + E.codes_t.size());
+        H.SP = (S + 15) & ~15;
+        H.tg_off = off; off = al(off + E.tg0.size());
+        H.prefix_off = off; off = al(off + E.prefix.size() * 4);
+        H.topo_off = off; off = al(off + tb);
+        H.GGu = E.GGu;
+        H.pcodes_off = off; off = al(off + E.pcodes_t.size());
+        H.pw_off = off; off = al(off + E.pw.size() * 4);
+        H.pof_off = off; off = al(off + E.pattern_of.size() * 4);
+        n_int_max = std::max(n_int_max, E.n_int);
+        GGuP_max = std::max(GGuP_max, (E.GGu + 31) & ~31);
+        GGp_max = std::max(GGp_max, E.GGp);
+    }
+    blob.assign(std::max<size_t>(off, 256), 0);
+    for (int e = 0; e < n; e++) {
+        const HostElem& E = *els[e];
+        if (E.filtered) continue;
+        ElemHeader& H = hdr[e];
+        std::memcpy(&blob[H.codes_off], E.codes.data(), E.codes.size());
+        std::memcpy(&blob[H.codes_t_off], E.codes_t.data(), E.codes_t.size());
+        std::memcpy(&blob[H.tg_off], E.tg0.data(), E.tg0.size());
+        std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
+        std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
+        std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
+        std::memcpy(&blob[H.pcodes_off], E.pcodes_t.data(), E.pcodes_t.size());
+        std::memcpy(&blob[H.pw_off], E.pw.data(), E.pw.size() * 4);
+        std::memcpy(&blob[H.pof_off], E.pattern_of.data(), E.pattern_of.size() * 4);
+    }
+    return off;
+}
+
+// ---------------------------------------------------------------------------
+// launch shape of the CTA-per-chain kernel and its trial-launch tuner
+// ---------------------------------------------------------------------------
+// A shape is a kernel instance (registers a thread) and a block size; with
+// the shared memory of that block size they fix the resident chains per SM.
+// Results do not depend on the shape (every column is computed by one thread
+// in the same arithmetic, and the column sums are exact), so the tuner may
+// pick any of them.
+struct ChainShape {
+    int variant = 0, BT = 128, per_sm = 0;
+};
+static const int kChainRegs[3] = {128, 168, 255};
+static std::mutex g_shape_mu;
+static std::map<std::array<int, 3>, std::array<int, 2>> g_shape_cache;   // (device, S, prec) -> (variant, BT)
+
+static int chain_regs(int prec, int variant) { return prec == 0 ? 255 : kChainRegs[variant]; }
+
+static std::vector<ChainShape> shape_candidates(const pacc_ctx* c, int prec) {
+    std::vector<ChainShape> v;
+    const int N = c->M.N;
+    for (int var = 0; var < chain_variants(prec); var++) {
+        if (prec == 1 && c->o.register_budget > 0 && kChainRegs[var] != c->o.register_budget) continue;
+        std::vector<int> bts;
+        if (c->o.block_threads > 0) bts.push_back(c->o.block_threads);
+        else if (prec == 0) bts = {64, 128, 256};
+        else if (var == 0) bts = {64, 128};
+        else if (var == 1) bts = {128};
+        else bts = {128, 256};
+        for (int bt : bts) {
+            if (bt > chain_variant_max_threads(prec, var)) continue;
+            ChainShape s;
+            s.variant = var;
+            s.BT = bt;
+            s.per_sm = chain_occupancy(prec, var, bt, smem_bytes(N, bt, prec, c->stack_cap));
+            if (s.per_sm > 0) v.push_back(s);
+        }
+    }
+    return v;
+}
+
+// Chooses the launch shape once per context: the options' shape if they fix
+// it, else the one an earlier context chose for this device, taxon count and
+// precision, else the fastest candidate on a short trial (BURNIN 8 + MCMC 24
+// per model) over the elements at hand (at least one per SM; with fewer the
+// default of 128 threads and the smallest register budget is kept).
+static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*>& els) {
+    if (c->shape_ready) return PACC_OK;
+    std::vector<ChainShape> cand = shape_candidates(c, prec);
+    if (cand.empty()) {
+        c->err = "no kernel instance fits the block_threads / register_budget options";
+        return PACC_EINVAL;
+    }
+    auto take = [&](const ChainShape& s) {
+        c->shape_variant = s.variant;
+        c->shape_bt = s.BT;
+        c->shape_per_sm = s.per_sm;
+        c->shape_ready = true;
+        return PACC_OK;
+    };
+    if (cand.size() == 1) return take(cand[0]);
+    const std::array<int, 3> key = {c->device, c->M.S, prec};
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        auto it = g_shape_cache.find(key);
+        if (it != g_shape_cache.end())
+            for (const ChainShape& s : cand)
+                if (s.variant == it->second[0] && s.BT == it->second[1]) return take(s);
+    }
+    std::vector<const HostElem*> trial;
+    int max_per_sm = 1;
+    for (const ChainShape& s : cand) max_per_sm = std::max(max_per_sm, s.per_sm);
+    const size_t want = (size_t)c->n_sm * max_per_sm * 2;
+    for (const HostElem* E : els)
+        if (!E->filtered && trial.size() < want) trial.push_back(E);
+    if ((int)trial.size() < c->n_sm) {
+        for (const ChainShape& s : cand)
+            if (s.variant == 0 && s.BT == 128) return take(s);
+        return take(cand[0]);
+    }
+    const int N = c->M.N;
+    const int n = (int)trial.size();
+    std::vector<ElemHeader> hdr;
+    std::vector<uint8_t> blob;
+    int n_int_max, GGp_max, GGuP_max;
+    pack_elems(c, trial, hdr, blob, n_int_max, GGp_max, GGuP_max);
+    const int tb = 8, tm = 24;
+    size_t ws1 = (ws_bytes(n_int_max, GGp_max, tb + tm, tm, N, prec) + 4095) & ~(size_t)4095;
+    int grid_max = 1;
+    for (const ChainShape& s : cand) grid_max = std::max(grid_max, std::min(n, c->n_sm * s.per_sm));
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_hdr = 0, o_res = al(sizeof(ElemHeader) * n), o_mz = al(o_res + sizeof(DevResult) * n),
+                 o_pz = al(o_mz + sizeof(int32_t) * 3 * N * (size_t)n),
+                 o_cnt = al(o_pz + sizeof(double) * 12 * N * (size_t)n), o_next = al(o_cnt + sizeof(DevCounters)),
+                 o_ws = al(o_next + 256), total = o_ws + ws1 * grid_max;
+    char* dev = nullptr;
+    char* dblob = nullptr;
+    if (!cuda_ok(c, cudaMalloc((void**)&dev, total), "cudaMalloc (tuner)")) return PACC_OOM;
+    if (!cuda_ok(c, cudaMalloc((void**)&dblob, blob.size()), "cudaMalloc (tuner)")) { cudaFree(dev); return PACC_OOM; }
+    cudaStream_t st = c->stream;
+    bool ok = cuda_ok(c, cudaMemcpyAsync(dblob, blob.data(), blob.size(), cudaMemcpyHostToDevice, st), "H2D (tuner)") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st),
+                      "H2D (tuner)");
+    ChainParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.hdr = (const ElemHeader*)(dev + o_hdr);
+    p.blob = (const uint8_t*)dblob;
+    p.n_elem = n;
+    p.next_elem = (int*)(dev + o_next);
+    p.results = (DevResult*)(dev + o_res);
+    p.max_z = (int32_t*)(dev + o_mz);
+    p.post_z = (double*)(dev + o_pz);
+    p.ws = dev + o_ws;
+    p.ws_stride = ws1;
+    p.n_int_max = n_int_max;
+    p.GGp_max = GGp_max;
+    p.stack_cap = c->stack_cap;
+    p.counters = (DevCounters*)(dev + o_cnt);
+    p.trial_burn = tb;
+    p.trial_mcmc = tm;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ok = ok && cuda_ok(c, cudaEventCreate(&e0), "event") && cuda_ok(c, cudaEventCreate(&e1), "event");
+    int best = -1;
+    float best_ms = 0, total_ms = 0;
+    for (int pass = 0; ok && pass < 2; pass++) {        // pass 0 warms every instance up
+        for (int i = 0; ok && i < (int)cand.size(); i++) {
+            const ChainShape& s = cand[i];
+            const int grid = std::max(1, std::min(n, c->n_sm * s.per_sm));
+            p.n_elem = pass == 0 ? std::min(n, grid) : n;
+            const size_t smem = smem_bytes(N, s.BT, prec, c->stack_cap);
+            ok = cuda_ok(c, cudaMemsetAsync(dev + o_next, 0, 256, st), "memset (tuner)") &&
+                 cuda_ok(c, cudaEventRecord(e0, st), "event") &&
+                 cuda_ok(c, launch_chain(p, grid, s.BT, smem, prec, s.variant, st), "launch (tuner)") &&
+                 cuda_ok(c, cudaEventRecord(e1, st), "event") && cuda_ok(c, cudaEventSynchronize(e1), "tuner");
+            float ms = 0;
+            if (ok) cudaEventElapsedTime(&ms, e0, e1);
+            total_ms += ms;
+            if (ok && pass == 1 && (best < 0 || ms < best_ms)) { best = i; best_ms = ms; }
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(dblob);
+    cudaFree(dev);
+    if (!ok || best < 0) return PACC_ECUDA;
+    c->shape_trial_ms = total_ms;
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        g_shape_cache[key] = {cand[best].variant, cand[best].BT};
+    }
+    return take(cand[best]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1246,7 +1456,7 @@ struct OutLayout {
 };
 static size_t stream_out_bytes(const StreamServer& v, int N) { return OutLayout(v, N).bytes; }
 
-static int stream_setup(pacc_ctx* c, int GG_needed) {
+static int stream_setup(pacc_ctx* c, int GG_needed, const std::vector<const HostElem*>& els) {
     StreamServer& v = c->ss;
     if (v.ready) return PACC_OK;
     cudaSetDevice(c->device);
@@ -1259,9 +1469,12 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.GGp_cap = v.GG_cap;
     v.n_int_cap = S - 1;
     v.TI = std::min(c->o.trace_iters, T);
-    v.BT = plain_block_threads(c, v.prec);
+    const int sst = choose_shape(c, v.prec, els);
+    if (sst != PACC_OK) return sst;
+    v.BT = c->shape_bt;
+    v.variant = c->shape_variant;
     v.smem = smem_bytes(N, v.BT, v.prec, c->stack_cap);
-    const int per_sm = std::max(1, chain_occupancy(v.prec, v.BT, v.smem));
+    const int per_sm = std::max(1, chain_occupancy(v.prec, v.variant, v.BT, v.smem));
     v.grid = c->n_sm * per_sm;
     v.ws1 = (ws_bytes(v.n_int_cap, v.GGp_cap, T, c->o.mcmc, N, v.prec) + 4095) & ~(size_t)4095;
     const size_t tb = al(topo_bytes(N));
@@ -1347,7 +1560,8 @@ static int stream_setup(pacc_ctx* c, int GG_needed) {
     v.p.q_cap = ns;
     v.p.done_flag = d_map + 64 + ns;
     v.p.q_stop = d_map + 1;
-    v.p.idle_ns = 30000000000LL;   // 30 s: only a safety bound, q_stop ends idle launches
+    // a safety bound: q_stop ends idle launches (default 30 s)
+    v.p.idle_ns = c->o.serve_idle_ns > 0 ? (long long)c->o.serve_idle_ns : 30000000000LL;
     v.p.z_start_zero = c->o.chain > 0 ? 1 : 0;
     v.free_slots.clear();
     for (int i = ns - 1; i >= 0; i--) v.free_slots.push_back(i);
@@ -1544,7 +1758,7 @@ static int stream_step(pacc_ctx* c) {
         std::atomic_thread_fence(std::memory_order_seq_cst);
         cudaStream_t ks = c->stream;
         if (!cuda_ok(c, cudaEventRecord(v.ev0, ks), "event") ||
-            !cuda_ok(c, launch_chain(v.p, v.grid, v.BT, v.smem, v.prec, ks), "launch (serving)") ||
+            !cuda_ok(c, launch_chain(v.p, v.grid, v.BT, v.smem, v.prec, v.variant, ks), "launch (serving)") ||
             !cuda_ok(c, cudaEventRecord(v.ev1, ks), "event"))
             return PACC_ECUDA;
         v.running = true;
@@ -1573,6 +1787,9 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
             // the chain kernels index an element's partials with 32-bit offsets
             else if ((size_t)8 * c->M.S * (size_t)E.GGp >= (size_t)INT32_MAX)
                 bad = 1;
+            // emission histogram bins are 16 bits; the prune's stack holds the full tree's depth
+            else if (!E.filtered && (E.GG > 65535 || E.stack_depth > c->stack_cap))
+                bad = 1;
             if (c->o.sample_hyper) {
                 const int N = c->M.N;
                 if (b->start_z) E.start_z.assign(b->start_z + (size_t)e * N, b->start_z + (size_t)(e + 1) * N);
@@ -1591,7 +1808,9 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
         int gmax = 0;
         for (size_t i = base; i < c->pending.size(); i++) gmax = std::max(gmax, c->pending[i].GG);
         const bool warp = batched_layout(c);
-        int st = warp ? server_setup(c, gmax) : stream_setup(c, gmax);
+        std::vector<const HostElem*> els;
+        for (size_t i = base; i < c->pending.size(); i++) els.push_back(&c->pending[i]);
+        int st = warp ? server_setup(c, gmax) : stream_setup(c, gmax, els);
         if (st != PACC_OK) { c->pending.resize(base); return st; }
         const int cap = warp ? c->srv.GG_cap : c->ss.GG_cap;
         auto& queue = warp ? c->srv.queue : c->ss.queue;
@@ -1692,56 +1911,21 @@ static int run_pending(pacc_ctx* c) {
     const int T = c->o.burnin + c->o.mcmc;
     const int TI = std::min(c->o.trace_iters, T);
     // pack the blob
-    std::vector<ElemHeader> hdr(n);
-    size_t off = 0;
+    std::vector<const HostElem*> els(n);
+    for (int e = 0; e < n; e++) els[e] = &c->pending[e];
+    std::vector<ElemHeader> hdr;
+    std::vector<uint8_t> blob;
+    int n_int_max, GGp_max, GGuP_max;
+    const size_t off = pack_elems(c, els, hdr, blob, n_int_max, GGp_max, GGuP_max);
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    int n_int_max = 1, GGp_max = 32, GGuP_max = 32;
-    const size_t tb = topo_bytes(N);
-    for (int e = 0; e < n; e++) {
-        HostElem& E = c->pending[e];
-        ElemHeader& H = hdr[e];
-        std::memset(&H, 0, sizeof(H));
-        H.element_no = E.no;
-        H.filtered = E.filtered;
-        if (E.filtered) continue;
-        H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = E.n_nodes; H.n_int = E.n_int;
-        H.n_hlev = E.n_hlev; H.n_dlev = E.n_dlev; H.tg_draws = E.tg_draws;
-        H.stack_depth = E.stack_depth;
-        H.codes_off = off; off = al(off + E.codes.size());
-        H.codes_t_off = off; off = al(off + E.codes_t.size());
-        H.SP = (S + 15) & ~15;
-        H.tg_off = off; off = al(off + E.tg0.size());
-        H.prefix_off = off; off = al(off + E.prefix.size() * 4);
-        H.topo_off = off; off = al(off + tb);
-        H.GGu = E.GGu;
-        H.pcodes_off = off; off = al(off + E.pcodes_t.size());
-        H.pw_off = off; off = al(off + E.pw.size() * 4);
-        H.pof_off = off; off = al(off + E.pattern_of.size() * 4);
-        n_int_max = std::max(n_int_max, E.n_int);
-        GGuP_max = std::max(GGuP_max, (E.GGu + 31) & ~31);
-        GGp_max = std::max(GGp_max, E.GGp);
-    }
-    std::vector<uint8_t> blob(off);
-    for (int e = 0; e < n; e++) {
-        HostElem& E = c->pending[e];
-        if (E.filtered) continue;
-        ElemHeader& H = hdr[e];
-        std::memcpy(&blob[H.codes_off], E.codes.data(), E.codes.size());
-        std::memcpy(&blob[H.codes_t_off], E.codes_t.data(), E.codes_t.size());
-        std::memcpy(&blob[H.tg_off], E.tg0.data(), E.tg0.size());
-        std::memcpy(&blob[H.prefix_off], E.prefix.data(), E.prefix.size() * 4);
-        std::memcpy(&blob[H.topo_off], E.topo.data(), E.topo.size() * 2);
-        std::memcpy(&blob[H.topo_off + ((E.topo.size() * 2 + 15) & ~(size_t)15)], E.dist2.data(), N * 8);
-        std::memcpy(&blob[H.pcodes_off], E.pcodes_t.data(), E.pcodes_t.size());
-        std::memcpy(&blob[H.pw_off], E.pw.data(), E.pw.size() * 4);
-        std::memcpy(&blob[H.pof_off], E.pattern_of.data(), E.pattern_of.size() * 4);
-    }
     if (batched_layout(c)) return run_batched(c, hdr, blob, off, n_int_max, GGuP_max);
-    // launch geometry
-    const int BT = plain_block_threads(c, prec);
+    // launch geometry: the context's shape (tuned at the first launch)
+    const int sst = choose_shape(c, prec, els);
+    if (sst != PACC_OK) return sst;
+    const int BT = c->shape_bt, variant = c->shape_variant;
     size_t smem = smem_bytes(N, BT, prec, c->stack_cap);
     // resident CTAs per SM from the kernel's registers and shared memory
-    int per_sm = std::max(1, chain_occupancy(prec, BT, smem));
+    int per_sm = std::max(1, chain_occupancy(prec, variant, BT, smem));
     int grid = std::max(1, std::min(n, c->n_sm * per_sm));
     size_t ws1 = ws_bytes(n_int_max, GGp_max, T, c->o.mcmc, N, prec);
     ws1 = (ws1 + 4095) & ~(size_t)4095;
@@ -1836,7 +2020,7 @@ static int run_pending(pacc_ctx* c) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    if (!cuda_ok(c, launch_chain(p, grid, BT, smem, prec, st), "launch chain")) return PACC_ECUDA;
+    if (!cuda_ok(c, launch_chain(p, grid, BT, smem, prec, variant, st), "launch chain")) return PACC_ECUDA;
     cudaEventRecord(e1, st);
     std::vector<DevResult> res(n);
     std::vector<int32_t> mz((size_t)3 * N * n);
@@ -2179,6 +2363,7 @@ int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
         pc.kernel_ms = c->ss.kernel_ms + running_ms;
         pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
         pc.iterations = (double)c->ss.launches;
+        pc.serve_idle_exits = (double)dc.idle_exits;
     } else if (serving(c) && c->srv.ready) {
         if (c->srv.inflight) cudaStreamSynchronize(c->stream);
         DevCounters dc;
@@ -2194,6 +2379,18 @@ int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
         for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
     }
     *out = c->counters;
+    return PACC_OK;
+}
+
+int pacc_get_launch_shape(pacc_ctx* c, int32_t* block_threads, int32_t* registers, int32_t* chains_per_sm,
+                          double* trial_ms) {
+    if (!c) return PACC_EINVAL;
+    const bool cta = !batched_layout(c) && c->shape_ready;
+    const int prec = c->o.precision == PACC_FP32 ? 1 : 0;
+    if (block_threads) *block_threads = cta ? c->shape_bt : 0;
+    if (registers) *registers = cta ? chain_regs(prec, c->shape_variant) : 0;
+    if (chains_per_sm) *chains_per_sm = cta ? c->shape_per_sm : 0;
+    if (trial_ms) *trial_ms = cta ? c->shape_trial_ms : 0;
     return PACC_OK;
 }
 

@@ -92,6 +92,20 @@ def test_abi_exports_every_declared_symbol(built):
         assert hasattr(L, n), n
 
 
+def test_default_opts_match_the_library(built):
+    """pacc_default_opts writes the same values into the ctypes mirror of
+    pacc_opts as abi.default_opts (the two layouts agree field by field)."""
+    L = pg.lib()
+    a = abi.PaccOpts()
+    C.memset(C.byref(a), 0x5A, C.sizeof(a))
+    L.pacc_default_opts(C.byref(a))
+    b = abi.default_opts()
+    for name, _ in abi.PaccOpts._fields_:
+        if name == "reserved0":
+            continue
+        assert getattr(a, name) == getattr(b, name), name
+
+
 def test_run_without_gpu_fails_loudly(built):
     import os
     if os.path.exists("/dev/nvidia0"):
