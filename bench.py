@@ -10,22 +10,35 @@ log-normal (median 250 bp, sigma 0.6, clipped 50-2000); 10% accelerated
 (r2 ~ U[1.5, 4]) and r1 ~ U[0.2, 0.6]; 5% of (taxon, element) pairs missing and
 3% gap cells; BURNIN 500 + MCMC 1500.
 
-A step is one batch of E elements (default 1,216: two per resident chain, four
-chains per SM) of the FP32-partial path, served and batched: the W warm-up
-batches and then the K timed batches are each submitted at once to a serving
-context, whose persistent kernel (one CTA per chain) takes elements from a
-host-fed queue as chains finish, so a batch's tail overlaps the next batch.
---serve-sweeps 0 runs the same kernel as one batched launch per step instead.
+A step is one batch of E elements (default 1,216, eight per SM) of the
+FP32-partial path, served and batched: the W warm-up batches and then the K
+timed batches are each submitted at once to a serving context, whose
+persistent kernel (one CTA per chain) takes elements from a host-fed queue
+as chains finish, so a batch's tail overlaps the next batch.  The kernel's
+launch shape (threads per chain, registers a thread, chains per SM) is the
+trial-launch tuner's choice, made during the first warm-up batch and
+recorded in config.launch_shape.  --serve-sweeps 0 runs the same kernel as
+one batched launch per step instead.
 
 value     = K * E / device time of the persistent launch (inputs resident)
 e2e       = K * E / wall time through pacc_submit/pacc_poll from host buffers
             (preprocessing, H2D admission, sweeps, D2H of results inside)
-fp64      = the plain FP64 path (one CTA per chain, one launch) on a batch of
-            the same workload, the baseline of the FP32/FP64 ratio
+fp64      = the plain FP64 path on the first E64 (default 304) elements of the
+            same batch, the same K timed and W warm-up steps, one launch per
+            step through pacc_run from host buffers (value: device time, e2e:
+            wall time); the baseline of the FP32/FP64 ratio
+error     = FP32 against that FP64 leg on the same elements: posterior
+            P(accelerated) per branch and both log Bayes factors (Monte-Carlo
+            differences of two chains), and the FP32 likelihood kernel's
+            relative error at a fixed state per element
+config1   = the 12-taxon configuration (100 elements, BURNIN 500 + MCMC 1000,
+            seed 0), FP32 and FP64, K timed steps each, with e2e
 serving   = an open-loop Poisson stream at 80% of `value`: p50/p99 latency
---impl reference runs the CPU oracle (the restatement of PhyloAcc-ST's
-path; the unmodified reference needs GSL/Armadillo, absent here) on all host
-cores over a bounded sample of the same workload.
+cpu_baseline and --impl reference run the CPU oracle (the restatement of
+PhyloAcc-ST's path in its own log-space arithmetic) on the host cores over
+elements taken from the start of the same batch: one element per core per
+step, step s of the reference arm taking elements s*cores..; cpu_baseline is
+step 0's sample.
 Multi-GPU: replicas (elements are independent; no collective), weak scaling.
 """
 from __future__ import annotations
@@ -164,24 +177,41 @@ def cpu_baseline(ds, n_sample, threads):
     return n_sample / dt, dt
 
 
+# The workload every arm measures: the GPU arm's batch (43 taxa, seed 100 for
+# rank 0).  The CPU figures take their elements from the start of that batch.
+WORKLOAD_SEED = 100
+
+
 def run_reference(args, ws, rank):
+    """The reference's algorithm on the host cores (the oracle, OpenMP over
+    elements like main.cpp:452).  Step s runs one element per core: elements
+    [s*cores, (s+1)*cores) of the GPU arm's batch (wrapping), so the K timed
+    steps together cover the first K*cores elements of that batch and step 0
+    is the same sample as the GPU line's cpu_baseline.  value = elements of
+    the timed steps / their summed wall time."""
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    ds = make_workload(max(cores, 1) * 2, seed=0)
-    vals = []
+    E = args.elements
+    ds = make_workload(E, seed=WORKLOAD_SEED)
+    n_done, t_sum = 0, 0.0
     for step in range(args.warmup + args.steps):
-        sub = ds.subset(list(range((step % 2) * cores, (step % 2) * cores + cores)))
-        v, dt = cpu_baseline(sub, cores, cores)
+        s = step - args.warmup if step >= args.warmup else step
+        idx = [(s * cores + i) % E for i in range(cores)]
+        v, dt = cpu_baseline(ds.subset(idx), cores, cores)
         if step >= args.warmup:
-            vals.append((v, dt))
-    v = float(np.mean([x[0] for x in vals]))
-    ms = float(np.mean([x[1] for x in vals])) * 1e3
-    sample = "%d elements per step (one per host core) of the 43-taxon workload, full 2,000 iterations x 3 models" % cores
+            n_done += cores
+            t_sum += dt
+    v = n_done / t_sum
+    ms = t_sum / args.steps * 1e3
+    sample = ("%d elements per step (one per host core) of the GPU arm's %d-element batch (seed %d), step s "
+              "taking elements s*%d.., %d elements over the timed steps; full 2,000 iterations x 3 models"
+              % (cores, E, WORKLOAD_SEED, cores, n_done))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "elements_per_step": cores, "parallelism": "OpenMP over elements"},
+            "config": {"workload": WORKLOAD, "elements_per_step": cores, "batch_seed": WORKLOAD_SEED,
+                       "parallelism": "OpenMP over elements"},
             "cpu_baseline": {"value": v, "unit": "elements/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -282,6 +312,73 @@ def serve_stream(ctx, ds, n_batches, ws):
     return reduce_max(ws, dev), reduce_max(ws, wall), got
 
 
+def by_element(got, n_per_step):
+    """element index within the batch -> (Results, row), from the first
+    served step (element_no = step * E + e)."""
+    out = {}
+    for r in got:
+        for i in range(r.n):
+            no = int(r.arr[i].element_no)
+            if no < n_per_step:
+                out[no] = (r, i)
+    return out
+
+
+def summary_error(ctx32_res, res64, ds, E64):
+    """FP32 against FP64 on the FP64 leg's elements: differences of the
+    posterior P(accelerated) per branch and of both log Bayes factors
+    (Monte-Carlo differences of two chains), and the relative error of the
+    FP32 likelihood kernel at a fixed state per element (each element's M2
+    Max_Z of the FP64 run at its median rates), which is deterministic."""
+    import phyloacc_gb300 as pg
+    from phyloacc_gb300 import abi
+    p32, p64, bf1, bf2 = [], [], [], []
+    for e in range(E64):
+        r, i = ctx32_res[e]
+        if r.arr[i].status != abi.PACC_OK or res64.arr[e].status != abi.PACC_OK:
+            continue
+        a = [r.arr[i].model[m].loglik for m in range(3)]
+        b = [res64.arr[e].model[m].loglik for m in range(3)]
+        if all(np.isfinite(a)) and all(np.isfinite(b)):
+            bf1.append(abs((a[1] - a[0]) - (b[1] - b[0])))
+            bf2.append(abs((a[1] - a[2]) - (b[1] - b[2])))
+        if r.post_z is not None:
+            p32.append(r.post_z[i, 1:, :, 3])
+            p64.append(res64.post_z[e, 1:, :, 3])
+    out = {"elements": E64, "compared": len(bf1)}
+    if p32:
+        d = np.abs(np.array(p32) - np.array(p64))
+        out["pacc_abs_max"] = float(d.max())
+        out["pacc_abs_mean"] = float(d.mean())
+    if bf1:
+        out["logbf1_abs_max"], out["logbf1_abs_median"] = float(np.max(bf1)), float(np.median(bf1))
+        out["logbf2_abs_max"], out["logbf2_abs_median"] = float(np.max(bf2)), float(np.median(bf2))
+    # likelihood kernel at a fixed state
+    o32, o64 = opts_for(abi.PACC_FP32), opts_for(abi.PACC_FP64)
+    n_ll = min(E64, 64)
+    sub = ds.subset(list(range(n_ll)))
+    c32, c64 = pg.Context(sub, o32), pg.Context(sub, o64)
+    rel = []
+    for e in range(n_ll):
+        if res64.arr[e].status != abi.PACC_OK:
+            continue
+        z = res64.max_z[e, 2].astype(np.int32)
+        m = res64.arr[e].model[2]
+        a = c32.loglik(e, z, m.c_rate, m.n_rate).sum()
+        b = c64.loglik(e, z, m.c_rate, m.n_rate).sum()
+        rel.append(abs(a - b) / abs(b))
+    c32.close()
+    c64.close()
+    if rel:
+        out["loglik_rel_max"] = float(np.max(rel))
+        out["loglik_rel_p99"] = float(np.percentile(rel, 99))
+        out["loglik_elements"] = len(rel)
+    out["note"] = ("pacc/logbf: FP32 vs FP64 chains on the same elements and seed (Monte-Carlo differences; the "
+                   "GPU tests bound them by the Monte-Carlo error); loglik: the FP32 likelihood kernel against FP64 "
+                   "at each element's M2 Max_Z and median rates")
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import phyloacc_gb300 as pg
     from phyloacc_gb300 import abi
@@ -289,17 +386,19 @@ def run_gpu(args, ws, rank, local):
         from phyloacc_gb300.build import build
         build()
     E, K, W = args.elements, args.steps, args.warmup
-    ds = make_workload(E, seed=100 + rank)
+    ds = make_workload(E, seed=WORKLOAD_SEED + rank)
     # FP32 served/batched path: a step is one batch of E elements streamed
     # through the persistent chain kernel (continuous batching)
     o32 = opts_for(abi.PACC_FP32)
     o32.device = 0
     o32.sweeps_per_launch = args.serve_sweeps
+    o32.trace_iters = 0
     ctx32 = pg.Context(ds, o32)
     clocks = ClockSampler(local)
     keys = ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "flop")
+    first = None
     if args.serve_sweeps > 0:
-        serve_stream(ctx32, ds, W, ws)                   # W warm-up steps
+        serve_stream(ctx32, ds, W, ws)                   # W warm-up steps (the first one tunes the shape)
         clocks.start()
         c0 = ctx32.counters()
         dev, wall, got = serve_stream(ctx32, ds, K, ws)  # K timed steps
@@ -307,6 +406,7 @@ def run_gpu(args, ws, rank, local):
         c1 = ctx32.counters()
         cnt = {k: c1[k] - c0[k] for k in keys}
         launches = int(c1["iterations"] - c0["iterations"])
+        first = by_element(got, E)
     else:
         # the same kernel without serving: one launch per batch of E elements
         kern, walls, c_last, res = time_gpu(ctx32, ds, K, W, ws, clocks)
@@ -314,38 +414,56 @@ def run_gpu(args, ws, rank, local):
         dev, wall, got = float(np.sum(kern)), float(np.sum(walls)), [res]
         cnt = {k: c_last[k] * K for k in keys}          # every step runs the same batch
         launches = K
+        first = {e: (res, e) for e in range(E)}
+    shape = ctx32.launch_shape()
     value = ws * E * K / dev
     e2e = ws * E * K / wall
     h2d = int(ds.bases.nbytes + ds.lengths.nbytes + ds.offsets.nbytes)
     d2h = int(E * (3 * 9 * 8 + 64))
     dev_ms = np.concatenate([[r.arr[i].device_ms for i in range(r.n)] for r in got])
-    # FP64 plain path (one CTA per chain, all elements in one launch)
-    E64 = args.fp64_elements
-    if args.no_fp64:
-        k64, c64, v64 = [float("nan")], {"flop": float("nan")}, float("nan")
-    else:
-        ds64 = ds.subset(list(range(E64)))
+    # FP32 results with Max_Z / P(Z) buffers for the error comparison: the
+    # first E64 elements once more (the chains are deterministic)
+    E64 = min(args.fp64_elements, E)
+    ds64 = ds.subset(list(range(E64)))
+    # FP64 plain path: the same K timed and W warm-up steps, a step one launch
+    # over E64 elements from host buffers (e2e) and its device time (value)
+    fp64 = None
+    err = None
+    if not args.no_fp64:
         ctx64 = pg.Context(ds64, opts_for(abi.PACC_FP64))
-        ctx64.run(ds.subset(list(range(152))))           # warm-up on one element per SM
-        k64, w64, c64, _ = time_gpu(ctx64, ds64, 1, 0, ws)
-        v64 = ws * E64 / float(np.mean(k64))
+        k64, w64, c64, res64 = time_gpu(ctx64, ds64, K, W, ws)
+        v64 = ws * E64 * K / float(np.sum(k64))
+        fp64 = {"value": v64, "unit": "elements/s", "elements_per_step": E64, "steps": K, "warmup": W,
+                "path": "plain FP64, one CTA per chain, one launch per step",
+                "e2e": {"value": ws * E64 * K / float(np.sum(w64)), "unit": "elements/s",
+                        "h2d_bytes_per_step": int(ds64.bases.nbytes + ds64.lengths.nbytes + ds64.offsets.nbytes),
+                        "d2h_bytes_per_step": int(E64 * (3 * 9 * 8 + 64))},
+                "shape": ctx64.launch_shape()}
+        fp64_flop = c64["flop"]
+        fp64_s = float(np.mean(k64))
+        ctx64.close()
+        c32b = pg.Context(ds64, opts_for(abi.PACC_FP32))
+        res32 = c32b.run(ds64)
+        c32b.close()
+        err = summary_error({e: (res32, e) for e in range(E64)}, res64, ds, E64)
     fp64_peak, fp32_peak = pg.measure_fma_peak(0)
     achieved = cnt["flop"] / dev
     updates = (cnt["edge_updates_internal"] + cnt["edge_updates_leaf"]) / 2
     # DRAM traffic of the launch: bytes per column-node update from one ncu
     # capture of this kernel on a smaller case of the same workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum, 608 elements x 60
-    # iterations), scaled by the updates this launch made
+    # (dram__bytes_read.sum + dram__bytes_write.sum), scaled by the updates
+    # this launch made
     traffic = DRAM_BYTES_PER_UPDATE * updates
     hbm_peak, hbm_src = hbm_peak_gbs()
     line = {
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": dev / K * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32-partials+fp64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "elements_per_step": E,
+        "config": {"workload": WORKLOAD, "elements_per_step": E, "batch_seed": WORKLOAD_SEED,
                    "path": ("FP32 partials, served and batched: one CTA per chain, a persistent kernel taking "
                             "elements from a host-fed queue (continuous batching)") if args.serve_sweeps > 0 else
                            "FP32 partials, batched: one CTA per chain, one launch per batch",
+                   "launch_shape": shape,
                    "l2": "inputs larger than L2 (resident chain state and partial buffers)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "elements/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -359,16 +477,19 @@ def run_gpu(args, ws, rank, local):
                      "hbm": {"achieved": traffic / dev / 1e9, "peak": hbm_peak, "unit": "GB/s",
                              "frac": traffic / dev / 1e9 / hbm_peak, "peak_source": hbm_src}},
         "column_node_updates_per_s": updates / dev,
-        "fp64": {"value": v64, "unit": "elements/s", "elements_per_step": E64,
-                 "path": "plain FP64, one CTA per chain, one launch",
-                 "achieved_tflops": c64["flop"] / float(np.mean(k64)) / 1e12,
-                 "peak_tflops": fp64_peak / 1e12,
-                 "frac": c64["flop"] / float(np.mean(k64)) / fp64_peak},
-        "fp32_over_fp64": value / v64,
         "element_device_ms": {"p50": float(np.percentile(dev_ms, 50)), "p99": float(np.percentile(dev_ms, 99))},
         "counters": cnt,
         "clocks": clk,
     }
+    if fp64 is not None:
+        fp64["achieved_tflops"] = fp64_flop / fp64_s / 1e12
+        fp64["peak_tflops"] = fp64_peak / 1e12
+        fp64["frac"] = fp64_flop / fp64_s / fp64_peak
+        line["fp64"] = fp64
+        line["fp32_over_fp64"] = value / fp64["value"]
+        line["error"] = err
+    if not args.no_config1:
+        line["config1"] = run_config1(K, W, ws)
     if args.serve_seconds > 0:
         line["serving"] = serve_latency(ds, value / ws, args.serve_seconds, args.serve_sweeps)
         line["latency_ms"] = {"p50": line["serving"]["p50_ms"], "p99": line["serving"]["p99_ms"]}
@@ -376,9 +497,32 @@ def run_gpu(args, ws, rank, local):
         cores = os.cpu_count() or 1
         v, dt = cpu_baseline(ds, cores, cores)
         line["cpu_baseline"] = {"value": v, "unit": "elements/s", "cores": cores, "kind": "port",
-                                "sample": "%d elements of the same workload, one per host core, %.1f s" % (cores, dt)}
+                                "sample": "elements 0..%d of this batch (one per host core), %.1f s; the same "
+                                          "elements as step 0 of --impl reference" % (cores - 1, dt)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_config1(K, W, ws):
+    """The 12-taxon configuration: 100 elements, BURNIN 500 + MCMC 1000,
+    seed 0, FP32 and FP64 paths; a step is one launch over the 100 elements
+    from host buffers."""
+    import phyloacc_gb300 as pg
+    from phyloacc_gb300 import abi, synth
+    ds = synth.make_dataset("st12", n_elements=100, seed=0)
+    out = {"workload": "12-taxon Yule tree (total length 1.2, one outgroup); 100 elements U{100..300} bp, 80 "
+                       "conserved (r1 0.35), 20 accelerated (r2 2.5) on a 3-taxon clade; BURNIN 500 + MCMC 1000; "
+                       "seed 0", "elements_per_step": 100}
+    for name, prec in (("fp32", abi.PACC_FP32), ("fp64", abi.PACC_FP64)):
+        o = abi.default_opts()
+        o.burnin, o.mcmc, o.seed, o.precision = 500, 1000, 0, prec
+        ctx = pg.Context(ds, o)
+        kern, wall, _, _ = time_gpu(ctx, ds, K, W, ws)
+        out[name] = {"value": ws * 100 * K / float(np.sum(kern)), "unit": "elements/s",
+                     "e2e": {"value": ws * 100 * K / float(np.sum(wall)), "unit": "elements/s"},
+                     "launch_shape": ctx.launch_shape()}
+        ctx.close()
+    return out
 
 
 def main():
@@ -389,9 +533,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--elements", type=int, default=1216,
                     help="elements per step (default: two per resident chain, four chains per SM)")
-    ap.add_argument("--fp64-elements", type=int, default=912)
+    ap.add_argument("--fp64-elements", type=int, default=304,
+                    help="elements per step of the FP64 leg (the first ones of the batch)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the 80%%-load serving run (0: skip)")
     ap.add_argument("--serve-sweeps", type=int, default=64,

@@ -1309,8 +1309,11 @@ static std::vector<ChainShape> shape_candidates(const pacc_ctx* c, int prec) {
     for (int var = 0; var < chain_variants(prec); var++) {
         if (prec == 1 && c->o.register_budget > 0 && kChainRegs[var] != c->o.register_budget) continue;
         std::vector<int> bts;
+        // FP64 partials: 128 threads (two chains per SM); on whole chains of
+        // the 43-taxon workload 256 threads (one chain per SM) ran at 0.77x
+        // and 64 threads fit no more chains per SM (shared memory)
         if (c->o.block_threads > 0) bts.push_back(c->o.block_threads);
-        else if (prec == 0) bts = {64, 128, 256};
+        else if (prec == 0) bts = {128};
         else if (var == 0) bts = {64, 128};
         else if (var == 1) bts = {128};
         else bts = {128, 256};
@@ -1328,9 +1331,12 @@ static std::vector<ChainShape> shape_candidates(const pacc_ctx* c, int prec) {
 
 // Chooses the launch shape once per context: the options' shape if they fix
 // it, else the one an earlier context chose for this device, taxon count and
-// precision, else the fastest candidate on a short trial (BURNIN 8 + MCMC 24
-// per model) over the elements at hand (at least one per SM; with fewer the
-// default of 128 threads and the smallest register budget is kept).
+// precision, else the fastest candidate on a short trial (BURNIN 40 + MCMC 80
+// per model, elements claimed longest first as in a real launch) over the
+// elements at hand (at least one per SM; with fewer the default of 128
+// threads and the smallest register budget is kept).  Shorter trials
+// over-weight the first iterations, whose Z state makes every prune a full
+// one, and pick shapes that are slower over whole chains.
 static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*>& els) {
     if (c->shape_ready) return PACC_OK;
     std::vector<ChainShape> cand = shape_candidates(c, prec);
@@ -1357,7 +1363,7 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     std::vector<const HostElem*> trial;
     int max_per_sm = 1;
     for (const ChainShape& s : cand) max_per_sm = std::max(max_per_sm, s.per_sm);
-    const size_t want = (size_t)c->n_sm * max_per_sm * 2;
+    const size_t want = (size_t)c->n_sm * max_per_sm;
     for (const HostElem* E : els)
         if (!E->filtered && trial.size() < want) trial.push_back(E);
     if ((int)trial.size() < c->n_sm) {
@@ -1371,7 +1377,7 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     std::vector<uint8_t> blob;
     int n_int_max, GGp_max, GGuP_max;
     pack_elems(c, trial, hdr, blob, n_int_max, GGp_max, GGuP_max);
-    const int tb = 8, tm = 24;
+    const int tb = 40, tm = 80;
     size_t ws1 = (ws_bytes(n_int_max, GGp_max, tb + tm, tm, N, prec) + 4095) & ~(size_t)4095;
     int grid_max = 1;
     for (const ChainShape& s : cand) grid_max = std::max(grid_max, std::min(n, c->n_sm * s.per_sm));
@@ -1379,7 +1385,10 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     const size_t o_hdr = 0, o_res = al(sizeof(ElemHeader) * n), o_mz = al(o_res + sizeof(DevResult) * n),
                  o_pz = al(o_mz + sizeof(int32_t) * 3 * N * (size_t)n),
                  o_cnt = al(o_pz + sizeof(double) * 12 * N * (size_t)n), o_next = al(o_cnt + sizeof(DevCounters)),
-                 o_ws = al(o_next + 256), total = o_ws + ws1 * grid_max;
+                 o_order = al(o_next + 256), o_ws = al(o_order + sizeof(int32_t) * n), total = o_ws + ws1 * grid_max;
+    std::vector<int32_t> order(n);
+    for (int e = 0; e < n; e++) order[e] = e;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return trial[a]->GG > trial[b]->GG; });
     char* dev = nullptr;
     char* dblob = nullptr;
     if (!cuda_ok(c, cudaMalloc((void**)&dev, total), "cudaMalloc (tuner)")) return PACC_OOM;
@@ -1387,6 +1396,8 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     cudaStream_t st = c->stream;
     bool ok = cuda_ok(c, cudaMemcpyAsync(dblob, blob.data(), blob.size(), cudaMemcpyHostToDevice, st), "H2D (tuner)") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hdr.data(), sizeof(ElemHeader) * n, cudaMemcpyHostToDevice, st),
+                      "H2D (tuner)") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_order, order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
                       "H2D (tuner)");
     ChainParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1394,6 +1405,7 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     p.blob = (const uint8_t*)dblob;
     p.n_elem = n;
     p.next_elem = (int*)(dev + o_next);
+    p.order = (const int32_t*)(dev + o_order);
     p.results = (DevResult*)(dev + o_res);
     p.max_z = (int32_t*)(dev + o_mz);
     p.post_z = (double*)(dev + o_pz);
@@ -1409,11 +1421,11 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     ok = ok && cuda_ok(c, cudaEventCreate(&e0), "event") && cuda_ok(c, cudaEventCreate(&e1), "event");
     int best = -1;
     float best_ms = 0, total_ms = 0;
-    for (int pass = 0; ok && pass < 2; pass++) {        // pass 0 warms every instance up
+    for (int pass = 0; ok && pass < 2; pass++) {        // pass 0 warms every instance up on one element
         for (int i = 0; ok && i < (int)cand.size(); i++) {
             const ChainShape& s = cand[i];
             const int grid = std::max(1, std::min(n, c->n_sm * s.per_sm));
-            p.n_elem = pass == 0 ? std::min(n, grid) : n;
+            p.n_elem = pass == 0 ? 1 : n;
             const size_t smem = smem_bytes(N, s.BT, prec, c->stack_cap);
             ok = cuda_ok(c, cudaMemsetAsync(dev + o_next, 0, 256, st), "memset (tuner)") &&
                  cuda_ok(c, cudaEventRecord(e0, st), "event") &&
