@@ -393,6 +393,7 @@ def run_gpu(args, ws, rank, local):
     o32.device = 0
     o32.sweeps_per_launch = args.serve_sweeps
     o32.trace_iters = 0
+    o32.block_threads, o32.register_budget = args.block_threads, args.register_budget
     ctx32 = pg.Context(ds, o32)
     clocks = ClockSampler(local)
     keys = ("edge_updates_internal", "edge_updates_leaf", "tg_draws", "flop")
@@ -538,6 +539,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--block-threads", type=int, default=0,
+                    help="FP32 chain kernel: threads per chain (0: the tuner's choice)")
+    ap.add_argument("--register-budget", type=int, default=0,
+                    help="FP32 chain kernel: registers a thread, 128/168/255 (0: the tuner's choice)")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the 80%%-load serving run (0: skip)")
     ap.add_argument("--serve-sweeps", type=int, default=64,

@@ -266,10 +266,13 @@ int pacc_debug_pmatrix(pacc_ctx* ctx, int n, const double* d, const double* r, d
  * (distance, rate) pairs and their matrices (about 590 KB per device); larger
  * requests return PACC_EINVAL.  Nothing in the scratch has to start at zero:
  * the kernel writes every matrix that is copied back.
- * Set-up: the first call on a device looks the scratch up with
- * cudaGetSymbolAddress (which loads the module on that device); later calls
- * reuse the address.  Make the first call from ordinary code, before any
- * stream capture.
+ * Set-up: every call looks the scratch's device address up with
+ * cudaGetSymbolAddress; the first call on a device also loads the module
+ * there.  Make the first call from ordinary code, before any stream capture.
+ * The call runs on the context's own second stream, so a serving launch of
+ * the same context does not hold it back (the serving launch leaves one
+ * chain slot of the GPU free for it); a context whose model is not the
+ * device's current one first waits for the other context's launch.
  * The scratch is shared by every context on a device: calls that overlap on
  * one device (two threads, or two contexts' streams) race on it.
  * n: 1..PACC_NOALLOC_MAX_PAIRS; d, r, out: host arrays as for pacc_debug_pmatrix.

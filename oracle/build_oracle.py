@@ -4,6 +4,10 @@ against the stand-in GSL/Armadillo headers of oracle/shim (oracle/_ref/).
 
     python oracle/build_oracle.py            # oracle only
     python oracle/build_oracle.py --ref DIR  # also build DIR/src/PhyloAcc-ST and PhyloAcc-ST-GBGC
+
+__graft_entry__.build() builds the reference too when it finds a checkout:
+the directory named by the PHYLOACC_REFERENCE environment variable, else a
+"reference" directory beside the repository.
 """
 import os
 import subprocess

@@ -486,6 +486,7 @@ struct pacc_ctx {
     double shape_trial_ms = 0;
     bool gpu_ok = false;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;   // the allocation-free entry point's own stream (beside a serving launch)
     // pending and finished work
     std::vector<HostElem> pending;
     size_t tune_grp_b = 0;   // per-warp scratch of the batched kernel (largest candidate)
@@ -690,6 +691,7 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     c->gpu_ok = cuda_ok(c, cudaSetDevice(c->device), "cudaSetDevice") &&
                 cuda_ok(c, cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device), "attr") &&
                 cuda_ok(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream") &&
+                cuda_ok(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking), "stream") &&
                 ensure_model(c);
     std::memset(&c->counters, 0, sizeof(c->counters));
     if (status) *status = PACC_OK;
@@ -728,6 +730,7 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->ss.ev0) cudaEventDestroy(c->ss.ev0);
     if (c->ss.ev1) cudaEventDestroy(c->ss.ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->aux) cudaStreamDestroy(c->aux);
     delete c;
 }
 
@@ -1487,7 +1490,11 @@ static int stream_setup(pacc_ctx* c, int GG_needed, const std::vector<const Host
     v.variant = c->shape_variant;
     v.smem = smem_bytes(N, v.BT, v.prec, c->stack_cap);
     const int per_sm = std::max(1, chain_occupancy(v.prec, v.variant, v.BT, v.smem));
-    v.grid = c->n_sm * per_sm;
+    // one chain slot fewer than the GPU holds: the persistent launch fills
+    // every SM's registers otherwise, and a small kernel of the same context
+    // on another stream (pacc_pmatrix_noalloc) could not start until the
+    // launch drained
+    v.grid = std::max(1, c->n_sm * per_sm - 1);
     v.ws1 = (ws_bytes(v.n_int_cap, v.GGp_cap, T, c->o.mcmc, N, v.prec) + 4095) & ~(size_t)4095;
     const size_t tb = al(topo_bytes(N));
     v.o_tg = al((size_t)S * v.GGp_cap);
@@ -2413,8 +2420,10 @@ int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, dou
     if (!ensure_model(c)) return PACC_ECUDA;
     double *dd = nullptr, *dr = nullptr, *dout = nullptr;
     if (!cuda_ok(c, cudaMalloc(&dd, n * 8), "malloc") || !cuda_ok(c, cudaMalloc(&dr, n * 8), "malloc") ||
-        !cuda_ok(c, cudaMalloc(&dout, (size_t)n * 128), "malloc"))
+        !cuda_ok(c, cudaMalloc(&dout, (size_t)n * 128), "malloc")) {
+        cudaFree(dd); cudaFree(dr); cudaFree(dout);     // cudaFree(nullptr) is a no-op
         return PACC_OOM;
+    }
     // inputs on the kernel's stream: a plain cudaMemcpy from pageable memory
     // may still be in flight when a kernel on a non-blocking stream starts
     cudaMemcpyAsync(dd, d, n * 8, cudaMemcpyHostToDevice, c->stream);
@@ -2426,36 +2435,35 @@ int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, dou
     return cuda_ok(c, e, "pmatrix") ? PACC_OK : PACC_ECUDA;
 }
 
-// Scratch address per device, looked up once (pacc_noalloc.cu).
-static std::mutex g_noalloc_mu;
-static double* g_noalloc_base[64];
-
 int pacc_pmatrix_noalloc(pacc_ctx* c, int n, const double* d, const double* r, double* out) {
-    if (!c || n <= 0 || n > PACC_NOALLOC_MAX_PAIRS || !d || !r || !out) return PACC_EINVAL;
-    if (!c->gpu_ok || c->device < 0 || c->device >= 64) return PACC_ECUDA;
-    if (cudaSetDevice(c->device) != cudaSuccess) return PACC_ECUDA;
-    if (!ensure_model(c)) return PACC_ECUDA;
-    double* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_base[c->device]) {
-            double* p = nullptr;
-            if (noalloc_scratch_address(&p) != cudaSuccess || !p) return PACC_ECUDA;
-            g_noalloc_base[c->device] = p;
-        }
-        base = g_noalloc_base[c->device];
+    if (!c) return PACC_EINVAL;
+    if (n <= 0 || n > PACC_NOALLOC_MAX_PAIRS || !d || !r || !out) {
+        c->err = "pmatrix_noalloc: n must be in 1.." + std::to_string(PACC_NOALLOC_MAX_PAIRS) +
+                 " and d, r, out non-null";
+        return PACC_EINVAL;
     }
+    if (!c->gpu_ok) { c->err = "pmatrix_noalloc: no usable GPU"; return PACC_ECUDA; }
+    if (!cuda_ok(c, cudaSetDevice(c->device), "pmatrix_noalloc: cudaSetDevice")) return PACC_ECUDA;
+    // returns at once when this context's model is the device's (it may be
+    // serving); otherwise the other context's launch is waited for
+    if (!ensure_model(c)) return PACC_ECUDA;
+    // the scratch's device address, looked up on every call (a lookup after
+    // the module is loaded is cheap, and it stays right across a device reset)
+    double* base = nullptr;
+    if (!cuda_ok(c, noalloc_scratch_address(&base), "pmatrix_noalloc: cudaGetSymbolAddress")) return PACC_ECUDA;
     const size_t M = PACC_NOALLOC_MAX_PAIRS;
     double* sd = base;
     double* sr = base + M;
     double* so = base + 2 * M;
-    cudaStream_t st = c->stream;
+    // the context's own second stream: a serving launch on the main stream
+    // does not hold this call back
+    cudaStream_t st = c->aux;
     cudaError_t e = cudaMemcpyAsync(sd, d, sizeof(double) * n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sr, r, sizeof(double) * n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = launch_pmatrix(n, sd, sr, so, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, so, sizeof(double) * 16 * n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return e == cudaSuccess ? PACC_OK : PACC_ECUDA;
+    return cuda_ok(c, e, "pmatrix_noalloc") ? PACC_OK : PACC_ECUDA;
 }
 
 int pacc_debug_encode(pacc_ctx* c, const uint8_t* bases, int32_t length, int8_t* tg_out, int32_t* n_cols,

@@ -2,6 +2,8 @@
 device scratch instead of per-call allocations (an entry point with no
 counterpart in the reference).  Collected last, so it also runs after every
 other test has used the device."""
+import time
+
 import numpy as np
 import pytest
 
@@ -34,3 +36,35 @@ def test_noalloc_pmatrix_refuses_oversize(built):
     # the refusal leaves the entry point usable
     d, r = np.array([0.1, 0.2]), np.array([1.0, 2.0])
     assert np.array_equal(ctx.pmatrix_noalloc(d, r), ctx.pmatrix(d, r))
+
+
+def test_noalloc_pmatrix_beside_a_serving_launch(built):
+    """Called while a serving launch of the same context still has chains in
+    flight, the entry point returns long before that launch drains (it runs on
+    the context's second stream), and its matrices equal the allocating entry
+    point's."""
+    ds = synth.make_dataset("st43", n_elements=48, seed=14)
+    o = abi.default_opts()
+    o.seed, o.burnin, o.mcmc = 1, 500, 1500
+    o.precision = abi.PACC_FP32
+    o.sweeps_per_launch = 8
+    o.block_threads, o.register_budget = 128, 128
+    ctx = pg.Context(ds, o)
+    d = np.concatenate([ds.tree.distances[:-1], [0.3, 1e-11, 0.0]])
+    r = np.linspace(0.05, 6.0, len(d))
+    first = ctx.pmatrix_noalloc(d, r)          # the set-up call, before the launch
+    t0 = time.perf_counter()
+    ctx.submit(ds, element_no=np.arange(ds.n_elements))
+    ctx.poll(ds.n_elements)                    # the persistent launch is running
+    t1 = time.perf_counter()
+    got = ctx.pmatrix_noalloc(d, r)
+    t_call = time.perf_counter() - t1
+    in_flight = ctx.pending()
+    while ctx.pending() > 0:
+        ctx.poll(ds.n_elements)
+    t_drain = time.perf_counter() - t0
+    assert in_flight > 0, "the chains finished before the call returned"
+    assert t_call < 0.25 * t_drain, (t_call, t_drain)
+    want = ctx.pmatrix(d, r)
+    assert np.array_equal(got, want)
+    assert np.array_equal(first, want)
