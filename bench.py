@@ -147,7 +147,7 @@ ITERS = {"burnin": 500, "mcmc": 1500}
 
 # DRAM bytes per column-node update of chain_kernel<float> (ncu capture of
 # 608 elements x 60 iterations: 59.7 GB over 1.666e9 updates)
-DRAM_BYTES_PER_UPDATE = 35.8
+DRAM_BYTES_PER_UPDATE = 28.5
 
 
 def hbm_peak_gbs():
