@@ -146,7 +146,8 @@ ITERS = {"burnin": 500, "mcmc": 1500}
 
 
 # DRAM bytes per column-node update of chain_kernel<float> (ncu capture of
-# 608 elements x 60 iterations: 59.7 GB over 1.666e9 updates)
+# 608 elements x 60 iterations, 128 threads x 255 registers: 47.4 GB over
+# 1.666e9 updates)
 DRAM_BYTES_PER_UPDATE = 28.5
 
 
