@@ -727,14 +727,13 @@ __device__ void build_sample_list(Ctx<Real>& c) {
     __syncthreads();
 }
 
-// One histogram count for the branch above `row`: lanes of the warp with
-// the same key are merged before the shared atomic.  Bins are 16 bits, two
-// to a word (a branch counts at most one pair per column, and elements have
-// fewer than 65,536 columns).  Called by all 32 lanes.
+// One histogram count for the branch above `row`: one shared atomic per
+// lane (the hardware merges a warp's atomics on one address; merging them
+// first with match_any or ballots measured slower).  Bins are 16 bits, two to
+// a word (a branch counts at most one pair per column, and elements have
+// fewer than 65,536 columns).
 __device__ __forceinline__ void emit_key(unsigned* cnt, int row, int key) {
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-        atomicAdd(&cnt[row * (NSYM * 2) + (key >> 1)], (unsigned)__popc(peers) << (16 * (key & 1)));
+    if (key >= 0) atomicAdd(&cnt[row * (NSYM * 2) + (key >> 1)], 1u << (16 * (key & 1)));
 }
 __device__ __forceinline__ int bin_count(const unsigned* cnt, int row, int key) {
     return (int)((cnt[row * (NSYM * 2) + (key >> 1)] >> (16 * (key & 1))) & 0xffffu);
@@ -937,8 +936,6 @@ template <typename Real>
 __device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
     const int T = c.T, m = c.cs->m;
     const double gr = c.trd[TR_G * T + m], lr = c.trd[TR_L * T + m], lr2 = c.trd[TR_L2 * T + m];
-    const double Tf[3][3] = {{1 - gr, 0, 0}, {gr, 1, 0}, {0, 0, 0}};
-    const double Tn[3][3] = {{1 - gr, 0, 0}, {gr, 1 - lr, lr2}, {0, lr, 1 - lr2}};
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         const int s = c.nodes[i];
         const double e0 = c.emis[s * 3 + 0], e1 = c.emis[s * 3 + 1], e2 = c.emis[s * 3 + 2];
@@ -951,56 +948,70 @@ __device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
         c.changed[s] = 0;
     }
     __syncthreads();
-    for (int h = 0; h < c.n_hlev; h++) {
-        const int a = c.hlev_start[h], b = c.hlev_start[h + 1];
-        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-            const int p = c.hlev_nodes[i];
-            double v[3] = {c.beta[p * 3 + 0], c.beta[p * 3 + 1], c.beta[p * 3 + 2]};
-            const int ch[2] = {c.c2a[p], c.c2b[p]};
-            for (int q = 0; q < 2; q++) {
-                const int ci = ch[q];
-                const double(*Tm)[3] = (c.fixZ[ci] == 1) ? Tf : Tn;
-                for (int zp = 0; zp < 3; zp++) {
-                    double mm = 0;
-                    for (int zc = 0; zc < 3; zc++) mm += Tm[zc][zp] * c.beta[ci * 3 + zc];
-                    v[zp] *= mm;
-                }
-            }
-            const double mx = fmax(v[0], fmax(v[1], v[2]));
-            const double inv = mx > 0 ? 1.0 / mx : 1.0;
-            for (int zp = 0; zp < 3; zp++) c.beta[p * 3 + zp] = v[zp] * inv;
-        }
-        __syncthreads();
-    }
+    // the tree's levels on one warp (warp barriers between levels); the
+    // message of child ci to parent state zp is sum_zc T[zc][zp] beta_ci[zc]
+    // with T the fixed nodes' (no state 2) or the free nodes' matrix
     int err = 0;
-    if (threadIdx.x == 0) {
-        double pr[3] = {0.5 * c.beta[c.root * 3 + 0], 0.5 * c.beta[c.root * 3 + 1], 0.0};
-        uint32_t wd[4];
-        philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
-        int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
-        if (nn > 2) { err = 1; nn = c.Z[c.root]; }
-        if (nn != c.Z[c.root]) c.changed[c.root] = 1;
-        c.Z[c.root] = (int8_t)nn;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int h = 0; h < c.n_hlev; h++) {
+            const int a = c.hlev_start[h], b = c.hlev_start[h + 1];
+            for (int i = a + lane; i < b; i += 32) {
+                const int p = c.hlev_nodes[i];
+                double v0 = c.beta[p * 3 + 0], v1 = c.beta[p * 3 + 1], v2 = c.beta[p * 3 + 2];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const int ci = q ? c.c2b[p] : c.c2a[p];
+                    const double b0 = c.beta[ci * 3 + 0], b1 = c.beta[ci * 3 + 1], b2 = c.beta[ci * 3 + 2];
+                    const bool fx = c.fixZ[ci] == 1;
+                    v0 *= fma(gr, b1, (1 - gr) * b0);
+                    v1 *= fx ? b1 : fma(lr, b2, (1 - lr) * b1);
+                    v2 *= fx ? 0.0 : fma(1 - lr2, b2, lr2 * b1);
+                }
+                // exact power-of-two normalisation (the values are relative)
+                const double mx = fmax(v0, fmax(v1, v2));
+                if (mx > 0) {
+                    int ex;
+                    frexp(mx, &ex);
+                    v0 = ldexp(v0, -ex); v1 = ldexp(v1, -ex); v2 = ldexp(v2, -ex);
+                }
+                c.beta[p * 3 + 0] = v0; c.beta[p * 3 + 1] = v1; c.beta[p * 3 + 2] = v2;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            double pr[3] = {0.5 * c.beta[c.root * 3 + 0], 0.5 * c.beta[c.root * 3 + 1], 0.0};
+            uint32_t wd[4];
+            philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
+            int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
+            if (nn > 2) { err = 1; nn = c.Z[c.root]; }
+            if (nn != c.Z[c.root]) c.changed[c.root] = 1;
+            c.Z[c.root] = (int8_t)nn;
+        }
+        __syncwarp();
+        for (int d = 0; d < c.n_dlev; d++) {
+            const int a = c.dlev_start[d], b = c.dlev_start[d + 1];
+            for (int i = a + lane; i < b; i += 32) {
+                const int s = c.dlev_nodes[i];
+                const int zp = c.Z[c.par[s]];
+                const bool fx = c.fixZ[s] == 1;
+                const double b0 = c.beta[s * 3 + 0], b1 = c.beta[s * 3 + 1], b2 = c.beta[s * 3 + 2];
+                double pr[3];
+                if (zp == 0) { pr[0] = (1 - gr) * b0; pr[1] = gr * b1; pr[2] = 0.0; }
+                else if (zp == 1) { pr[0] = 0.0; pr[1] = fx ? b1 : (1 - lr) * b1; pr[2] = fx ? 0.0 : lr * b2; }
+                else { pr[0] = 0.0; pr[1] = fx ? 0.0 : lr2 * b1; pr[2] = fx ? 0.0 : (1 - lr2) * b2; }
+                const uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
+                uint32_t wd[4];
+                philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
+                int nn = categorical(3, pr, word_to_uniform(wd[w & 3]));
+                if (nn > 2) { err = 1; nn = c.Z[s]; }
+                if (nn != c.Z[s]) c.changed[s] = 1;
+                c.Z[s] = (int8_t)nn;
+            }
+            __syncwarp();
+        }
     }
     __syncthreads();
-    for (int d = 0; d < c.n_dlev; d++) {
-        const int a = c.dlev_start[d], b = c.dlev_start[d + 1];
-        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-            const int s = c.dlev_nodes[i];
-            const int zp = c.Z[c.par[s]];
-            const double(*Tm)[3] = (c.fixZ[s] == 1) ? Tf : Tn;
-            double pr[3];
-            for (int k = 0; k < 3; k++) pr[k] = Tm[k][zp] * c.beta[s * 3 + k];
-            const uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
-            uint32_t wd[4];
-            philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
-            int nn = categorical(3, pr, word_to_uniform(wd[w & 3]));
-            if (nn > 2) { err = 1; nn = c.Z[s]; }
-            if (nn != c.Z[s]) c.changed[s] = 1;
-            c.Z[s] = (int8_t)nn;
-        }
-        __syncthreads();
-    }
     if (threadIdx.x == 0) c.local.z_draws += c.n_nodes;
     return err;
 }
@@ -1016,9 +1027,12 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
         c.changed[s] = 0;
     }
     __syncthreads();
+    // the tree's levels on one warp (warp barriers between levels)
+    int err = 0;
+    if (threadIdx.x >= 32) goto done;
     for (int h = 0; h < c.n_hlev; h++) {
         int a = c.hlev_start[h], b = c.hlev_start[h + 1];
-        for (int i = a * 3 + threadIdx.x; i < b * 3; i += blockDim.x) {
+        for (int i = a * 3 + (int)threadIdx.x; i < b * 3; i += 32) {
             int p = c.hlev_nodes[i / 3];
             int zp = i % 3;
             double v = c.beta[p * 3 + zp];
@@ -1026,9 +1040,8 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
             v += msg(c.ltm, c.beta, c.c2b[p], zp);
             c.beta[p * 3 + zp] = v;
         }
-        __syncthreads();
+        __syncwarp();
     }
-    int err = 0;
     if (threadIdx.x == 0) {
         const double prior_z[3] = {d_log(0.5), d_log(0.5), NI};
         double lp[3], pr[3];
@@ -1044,10 +1057,10 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
         if (nn != c.Z[c.root]) c.changed[c.root] = 1;
         c.Z[c.root] = (int8_t)nn;
     }
-    __syncthreads();
+    __syncwarp();
     for (int d = 0; d < c.n_dlev; d++) {
         int a = c.dlev_start[d], b = c.dlev_start[d + 1];
-        for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+        for (int i = a + (int)threadIdx.x; i < b; i += 32) {
             int s = c.dlev_nodes[i];
             int zp = c.Z[c.par[s]];
             double lt[3], pr[3];
@@ -1064,8 +1077,10 @@ __device__ int update_z(Ctx<Real>& c, uint64_t pos) {
             if (nn != c.Z[s]) c.changed[s] = 1;
             c.Z[s] = (int8_t)nn;
         }
-        __syncthreads();
+        __syncwarp();
     }
+done:
+    __syncthreads();
     if (threadIdx.x == 0) c.local.z_draws += c.n_nodes;
     return err;
 }
