@@ -1335,11 +1335,12 @@ static std::vector<ChainShape> shape_candidates(const pacc_ctx* c, int prec) {
 // Chooses the launch shape once per context: the options' shape if they fix
 // it, else the one an earlier context chose for this device, taxon count and
 // precision, else the fastest candidate on a short trial (BURNIN 40 + MCMC 80
-// per model, elements claimed longest first as in a real launch) over the
-// elements at hand (at least one per SM; with fewer the default of 128
-// threads and the smallest register budget is kept).  Shorter trials
-// over-weight the first iterations, whose Z state makes every prune a full
-// one, and pick shapes that are slower over whole chains.
+// per model) over the elements at hand (at least one per SM; with fewer the
+// default of 128 threads and the smallest register budget is kept).  A
+// shape's speed is its resident chains per SM over the mean device time of
+// an element's chain (the kernel's per-element clock): the rate at which a
+// long stream of elements goes through, without the tail of the trial batch
+// (whose last chains run alone), which favours shapes with fewer chains.
 static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*>& els) {
     if (c->shape_ready) return PACC_OK;
     std::vector<ChainShape> cand = shape_candidates(c, prec);
@@ -1423,7 +1424,9 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ok = ok && cuda_ok(c, cudaEventCreate(&e0), "event") && cuda_ok(c, cudaEventCreate(&e1), "event");
     int best = -1;
-    float best_ms = 0, total_ms = 0;
+    double best_rate = 0;
+    float total_ms = 0;
+    std::vector<DevResult> tres(n);
     for (int pass = 0; ok && pass < 2; pass++) {        // pass 0 warms every instance up on one element
         for (int i = 0; ok && i < (int)cand.size(); i++) {
             const ChainShape& s = cand[i];
@@ -1431,13 +1434,21 @@ static int choose_shape(pacc_ctx* c, int prec, const std::vector<const HostElem*
             p.n_elem = pass == 0 ? 1 : n;
             const size_t smem = smem_bytes(N, s.BT, prec, c->stack_cap);
             ok = cuda_ok(c, cudaMemsetAsync(dev + o_next, 0, 256, st), "memset (tuner)") &&
+                 cuda_ok(c, cudaMemsetAsync(dev + o_res, 0, sizeof(DevResult) * n, st), "memset (tuner)") &&
                  cuda_ok(c, cudaEventRecord(e0, st), "event") &&
                  cuda_ok(c, launch_chain(p, grid, s.BT, smem, prec, s.variant, st), "launch (tuner)") &&
                  cuda_ok(c, cudaEventRecord(e1, st), "event") && cuda_ok(c, cudaEventSynchronize(e1), "tuner");
             float ms = 0;
             if (ok) cudaEventElapsedTime(&ms, e0, e1);
             total_ms += ms;
-            if (ok && pass == 1 && (best < 0 || ms < best_ms)) { best = i; best_ms = ms; }
+            if (ok && pass == 1) {
+                ok = cuda_ok(c, cudaMemcpy(tres.data(), dev + o_res, sizeof(DevResult) * n, cudaMemcpyDeviceToHost),
+                             "D2H (tuner)");
+                double cyc = 0;
+                for (int e = 0; e < n; e++) cyc += tres[e].device_ms;   // clock cycles of the element's chain
+                const double rate = cyc > 0 ? (double)s.per_sm * n / cyc : 0;
+                if (ok && (best < 0 || rate > best_rate)) { best = i; best_rate = rate; }
+            }
         }
     }
     if (e0) cudaEventDestroy(e0);
