@@ -31,11 +31,12 @@ def build_oracle(force=False):
     out_dir = os.path.join(HERE, "_build")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "liboracle.so")
-    srcs = [os.path.join(HERE, "oracle_st.cpp"), os.path.join(HERE, "oracle_rng.h"),
+    srcs = [os.path.join(HERE, "oracle_st.cpp"), os.path.join(HERE, "oracle_gbgc.cpp"),
+            os.path.join(HERE, "oracle_rng.h"),
             os.path.join(ROOT, "include", "pacc.h"), os.path.join(ROOT, "phyloacc_gb300", "csrc", "eigen4.h")]
     if not force and _newer(out, srcs):
         return out
-    cmd = [CXX] + FLAGS + ["-shared", "-I" + os.path.join(ROOT, "include"), srcs[0], "-o", out + ".tmp"]
+    cmd = [CXX] + FLAGS + ["-shared", "-I" + os.path.join(ROOT, "include"), srcs[0], srcs[1], "-o", out + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(out + ".tmp", out)
     return out

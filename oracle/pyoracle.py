@@ -169,3 +169,40 @@ def eigen(Q):
     Vi = np.zeros(16)
     st = lib().oracle_eigen(*(abi.ptr(a, C.c_double) for a in (Q, lam, V, Vi)))
     return st, lam, V.reshape(4, 4), Vi.reshape(4, 4)
+
+
+def gbgc_engine(ds, e, z, b, sc, sn, gb, gapchar="*", missing_thres=0.8, conserve_prop=0.8):
+    """The gBGC model's likelihood engine on element e at one state (Z and B
+    per node, conserved/accelerated selection sc/sn, GC bias gb): the six
+    per-branch log transition matrices [6][N][4][4], per-column
+    log-likelihoods, expected (child, parent) base counts [N][4][4], the
+    element's root and missing flags (oracle_gbgc.cpp)."""
+    L = lib()
+    if not hasattr(L, "_gbgc_set"):
+        L.oracle_gbgc_engine.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(C.c_uint8), C.c_int32, C.c_int32,
+                                         C.c_double, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_uint8), C.POINTER(C.c_int32)]
+        L.oracle_gbgc_engine.restype = C.c_int
+        L._gbgc_set = True
+    m = abi.ModelArgs(ds)
+    N = ds.tree.n_nodes
+    GG = int(ds.lengths[e])
+    blk = np.ascontiguousarray(ds.element(e).reshape(-1))
+    z = np.ascontiguousarray(z, dtype=np.int32)
+    b = np.ascontiguousarray(b, dtype=np.int32)
+    logp = np.zeros(6 * N * 16)
+    col = np.zeros(GG)
+    counts = np.zeros(N * 16)
+    root = C.c_int32()
+    miss = np.zeros(N, np.uint8)
+    filt = C.c_int32()
+    st = L.oracle_gbgc_engine(C.byref(m.model), abi.ptr(blk, C.c_uint8), GG, ord(gapchar), missing_thres,
+                              conserve_prop, abi.ptr(z, C.c_int32), abi.ptr(b, C.c_int32), sc, sn, gb,
+                              abi.ptr(logp, C.c_double), abi.ptr(col, C.c_double), abi.ptr(counts, C.c_double),
+                              C.byref(root), abi.ptr(miss, C.c_uint8), C.byref(filt))
+    if st not in (abi.PACC_OK, abi.PACC_FILTERED):
+        raise RuntimeError("oracle_gbgc_engine failed: %d" % st)
+    return {"logp": logp.reshape(6, N, 4, 4), "col": col, "counts": counts.reshape(N, 4, 4), "root": root.value,
+            "missing": miss, "filtered": filt.value}
