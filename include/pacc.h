@@ -280,6 +280,35 @@ int pacc_debug_pmatrix(pacc_ctx* ctx, int n, const double* d, const double* r, d
 #define PACC_NOALLOC_MAX_PAIRS 4096
 int pacc_pmatrix_noalloc(pacc_ctx* ctx, int n, const double* d, const double* r, double* out);
 
+/* The likelihood engine of the PhyloAcc-ST-GBGC model (selection plus
+ * GC-biased gene conversion) on one element at one state, on the device.
+ * It replaces, for that model (src/PhyloAcc-ST-GBGC/SRC):
+ *   - the BPP_C constructor's column encoding, missing taxa, conserved-species
+ *     filter and outgroup-path collapse (bpp_c.hpp:153-379, bpp_c.cpp:53-111);
+ *   - getRate (bpp_c.cpp:13-30) and init_cache_TM (bpp_c.cpp:1563-1621): the six
+ *     classes of branch matrices, null, conserved, accelerated, each without
+ *     and with the GC bias, built here by Pade scaling and squaring in FP64;
+ *   - Update_Tg's pruning pass and per-column log-likelihood (bpp_c.cpp:477-540)
+ *     and its expected (child base, parent base) counts (bpp_c.cpp:541-596).
+ * bases: S rows of length lower-case characters in tree leaf order; gapchar
+ * and missing_thres as the model's GAPCHAR ('*') and MISSING_THRES (0.8);
+ * the conserved-species filter uses the context's conserve_prop.
+ * z: [N] 0 null / 1 conserved / 2 accelerated (not 2 on the outgroup path);
+ * b: [N] 0 or 1 (the gBGC flag); both read on the element's branches only;
+ * sel_c, sel_n: conserved and accelerated selection; gc_bias: the GC bias.
+ * Partials are FP32 when the context's precision is PACC_FP32 or
+ * PACC_FP32_WARP, else FP64.
+ * Out: logp [6][N][16] log P(child | parent) in the class order above (0 on
+ * branches not built: missing ones, and the accelerated classes on the
+ * outgroup path); col [length] per-column log-likelihoods; counts [N][16]
+ * expected counts summed over columns (the root's posterior in entries j*4);
+ * root (the element's root after the collapse); missing [N]; filtered.
+ * Returns PACC_FILTERED (outputs other than missing and filtered untouched)
+ * for a filtered element. */
+int pacc_gbgc_engine(pacc_ctx* ctx, const uint8_t* bases, int32_t length, int32_t gapchar, double missing_thres,
+                     const int32_t* z, const int32_t* b, double sel_c, double sel_n, double gc_bias, double* logp,
+                     double* col, double* counts, int32_t* root, uint8_t* missing, int32_t* filtered);
+
 /* (b) Per-column log-likelihood of one element for a given Z (int32 [N]) and
  * conserved/accelerated rates, using the chosen precision's pruning kernel.
  * out: [columns after trimming]; returns the column count via *n_cols. */

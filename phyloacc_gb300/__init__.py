@@ -59,6 +59,11 @@ def lib():
         L.pacc_measure_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.pacc_get_launch_shape.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.pacc_gbgc_engine.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_double,
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_double, C.c_double,
+                                       C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8),
+                                       C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
@@ -179,6 +184,36 @@ class Context:
         if st != 0:
             self._err("pacc_debug_loglik", st)
         return out[:ncol.value]
+
+    def gbgc_engine(self, e: int, z, b, sel_c: float, sel_n: float, gc_bias: float, gapchar: str = "*",
+                    missing_thres: float = 0.8) -> dict:
+        """The gBGC model's likelihood engine on element e at one state (Z and
+        the gBGC flag B per node, selection sel_c / sel_n, GC bias): the six
+        classes' log transition matrices [6][N][4][4], per-column
+        log-likelihoods, expected (child, parent) base counts [N][4][4], the
+        element's root and missing flags.  A filtered element returns
+        {"filtered": 1, "missing": ...}."""
+        N = self.ds.tree.n_nodes
+        blk = np.ascontiguousarray(self.ds.element(e).reshape(-1))
+        L = int(self.ds.lengths[e])
+        z = np.ascontiguousarray(z, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.int32)
+        logp = np.zeros(6 * N * 16)
+        col = np.zeros(L)
+        counts = np.zeros(N * 16)
+        root = C.c_int32()
+        miss = np.zeros(N, np.uint8)
+        filt = C.c_int32()
+        st = lib().pacc_gbgc_engine(self.h, abi.ptr(blk, C.c_uint8), L, ord(gapchar), missing_thres,
+                                    abi.ptr(z, C.c_int32), abi.ptr(b, C.c_int32), sel_c, sel_n, gc_bias,
+                                    abi.ptr(logp, C.c_double), abi.ptr(col, C.c_double), abi.ptr(counts, C.c_double),
+                                    C.byref(root), abi.ptr(miss, C.c_uint8), C.byref(filt))
+        if st == abi.PACC_FILTERED:
+            return {"filtered": 1, "missing": miss}
+        if st != 0:
+            self._err("pacc_gbgc_engine", st)
+        return {"logp": logp.reshape(6, N, 4, 4), "col": col, "counts": counts.reshape(N, 4, 4), "root": root.value,
+                "missing": miss, "filtered": 0}
 
     def patterns(self, e: int):
         """(pattern_of [n_cols], weights [n_patterns]) of element e (host only)."""

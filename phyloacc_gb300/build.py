@@ -46,6 +46,7 @@ def build(force=False, verbose=False):
         "pacc_batch.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_batch.cu")],
         "pacc_host.o": [NVCC] + ARCH + COMMON + ["-x", "cu", "-c", os.path.join(CSRC, "pacc_host.cpp")],
         "pacc_noalloc.o": [NVCC] + ARCH + COMMON + ["-c", os.path.join(CSRC, "pacc_noalloc.cu")],
+        "pacc_gbgc.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_gbgc.cu")],
     }
     cmds = []
     for name, cmd in objs.items():

@@ -214,4 +214,30 @@ struct BatchParams {
     int GGuP_max;             // pattern capacity of the per-warp partial buffers (multiple of 32)
 };
 
+
+// Parameters of one launch of the gBGC likelihood engine (one element at one
+// state of the PhyloAcc-ST-GBGC model).
+struct GbgcParams {
+    int S, N, GG, GGp, root, n_nodes;   // GGp: columns rounded up to 32 (padding columns allow every base)
+    int warps;                          // warps of the engine's CTA
+    const int16_t* nodes;               // [n_nodes] postorder of the element's tree (collapsed outgroup path)
+    const int16_t* c0;                  // [N] children in that tree (-1: leaf)
+    const int16_t* c1;
+    const int16_t* parent;              // [N]
+    const uint8_t* missing;             // [N]
+    const uint8_t* fixed;               // [N] no accelerated class on this branch (the outgroup path)
+    const double* dist;                 // [N] branch lengths after the collapse
+    const int32_t* cls;                 // [N] matrix class of the branch above the node: Z + 3 B
+    const uint8_t* masks;               // [S][GGp] allowed bases of a leaf at a column (bit i: base i)
+    double Q0[16], pi[4];
+    double sc, sn, gb;                  // conserved / accelerated selection, GC bias
+    double* logp;                       // [6][N][16] log P, (child, parent) row-major
+    void* pmat;                         // [6][N][16] P in the partials' type
+    double* col;                        // [GG] per-column log-likelihood
+    double* counts;                     // [N][16] expected (child, parent) base counts
+    double* wcounts;                    // [warps][N][16] per-warp sums
+    void* part;                         // [N][GGp][4] partials, then marginals
+    int32_t* scl;                       // [N][GGp] power-of-two exponents of the partials
+};
+
 }  // namespace pacc

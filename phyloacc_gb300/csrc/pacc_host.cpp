@@ -52,6 +52,7 @@ bool batch_supports(int prec, int C);
 int batch_occupancy(int prec, int C, int warps, size_t smem);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
 cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st);
+cudaError_t launch_gbgc(const GbgcParams& p, int prec, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // model (BPP, bpp.hpp:173-404)
@@ -62,6 +63,7 @@ struct HostModel {
     std::vector<double> dist;
     std::vector<int> conserve, outgroup;
     std::vector<char> upper, upper_conserve;  // [N]
+    double rate[16], pi[4];                   // RATE_MAT (row-major, i -> j) and BACKGROUND
     DevModel dm;
 };
 
@@ -146,6 +148,133 @@ static void compress_patterns(HostElem& E, int SP) {
         std::memcpy(&E.pcodes_t[(size_t)p * SP], &E.codes_t[(size_t)first[p] * SP], SP);
 }
 
+// Collapse the missing branches of the nodes marked in up, moving the root
+// down where the root itself loses a child (getSubtree_missing,
+// bpp_c.cpp:64-113; the same walk in PhyloAcc-ST-GBGC, bpp_c.cpp:53-111).
+static void collapse_missing_path(int S, const std::vector<char>& up, std::vector<int>& c2a, std::vector<int>& c2b,
+                                  std::vector<int>& par, std::vector<double>& d2, const std::vector<char>& missing,
+                                  int& root) {
+    struct Walker {
+        int S;
+        const std::vector<char>& up;
+        std::vector<int>&c2a, &c2b, &par;
+        std::vector<double>& d2;
+        const std::vector<char>& missing;
+        int& root;
+        void walk(int ss, int child) {
+            if (!up[ss] || ss < S) return;
+            int s = ss;
+            while (up[s] && s >= S) {
+                int p0 = c2a[s], p1 = c2b[s];
+                int keep;
+                if (missing[p0] && !missing[p1]) { keep = p1; par[p0] = -1; }
+                else if (!missing[p0] && missing[p1]) { keep = p0; par[p1] = -1; }
+                else {
+                    walk(p0, 0);
+                    walk(p1, 1);
+                    return;
+                }
+                d2[keep] += d2[s];
+                if (s == root) root = keep;
+                else {
+                    (child == 0 ? c2a : c2b)[par[ss]] = keep;
+                    par[keep] = par[ss];
+                }
+                s = keep;
+            }
+        }
+    } wk{S, up, c2a, c2b, par, d2, missing, root};
+    wk.walk(root, -1);
+}
+
+// Postorder of the tree below root, first children first (bpp_c.cpp:44-60).
+static std::vector<int> postorder_nodes(int root, const std::vector<int>& c2a, const std::vector<int>& c2b) {
+    std::vector<int> nodes;
+    nodes.reserve(c2a.size());
+    std::vector<std::pair<int, int>> st;
+    st.push_back({root, 0});
+    while (!st.empty()) {
+        auto& t = st.back();
+        int j = t.first;
+        if (t.second == 0) {
+            t.second = 1;
+            if (c2a[j] != -1) { st.push_back({c2a[j], 0}); continue; }
+        }
+        if (t.second == 1) {
+            t.second = 2;
+            if (c2b[j] != -1) { st.push_back({c2b[j], 0}); continue; }
+        }
+        nodes.push_back(j);
+        st.pop_back();
+    }
+    return nodes;
+}
+
+// One element of the PhyloAcc-ST-GBGC model, preprocessed for its
+// likelihood engine (BPP_C ctor of that model, src/PhyloAcc-ST-GBGC/SRC/
+// bpp_c.hpp:153-379): allowed-base masks per leaf and column, missing taxa,
+// the conserved-species filter, and the tree with the missing outgroup path
+// collapsed (getSubtree_missing, bpp_c.cpp:53-111).
+struct GbgcElem {
+    int GG = 0, GGp = 0, root = 0, filtered = 0;
+    std::vector<uint8_t> masks;          // [S][GGp]
+    std::vector<char> missing, fixed;    // [N]
+    std::vector<int> c2a, c2b, par;      // [N] after the collapse
+    std::vector<double> d2;              // [N]
+    std::vector<int> nodes;              // postorder from root
+};
+
+// bit i: base i (A, C, G, T) allowed (bpp_c.hpp:203-251 of the gBGC model);
+// '-', 'n', the gap character and anything else allow all four
+static inline uint8_t gbgc_mask(uint8_t ch) {
+    switch ((char)ch) {
+        case 'a': return 1;
+        case 'c': return 2;
+        case 'g': return 4;
+        case 't': return 8;
+        case 'r': return 1 | 4;
+        case 'y': return 2 | 8;
+        case 'k': return 4 | 8;
+        case 'm': return 1 | 2;
+        case 's': return 2 | 4;
+        case 'w': return 1 | 8;
+        default: return 15;
+    }
+}
+
+static void gbgc_prepare(const HostModel& M, const uint8_t* bases, int GG, char gapchar, double missing_thres,
+                         double conserve_prop, GbgcElem& E) {
+    const int S = M.S, N = M.N;
+    E.GG = GG;
+    E.GGp = (GG + 31) & ~31;
+    E.masks.assign((size_t)S * E.GGp, 15);
+    std::vector<int> num_missing(S, 0);
+    for (int s = 0; s < S; s++)
+        for (int g = 0; g < GG; g++) {
+            const uint8_t ch = bases[(size_t)s * GG + g];
+            if ((char)ch == gapchar) num_missing[s]++;
+            E.masks[(size_t)s * E.GGp + g] = gbgc_mask(ch);
+        }
+    E.missing.assign(N, 0);
+    for (int s = S; s < N; s++) {
+        const int p[2] = {M.ch0[s], M.ch1[s]};
+        for (int q = 0; q < 2; q++)
+            if (p[q] < S && num_missing[p[q]] > missing_thres * GG) E.missing[p[q]] = 1;
+        if (E.missing[p[0]] && E.missing[p[1]]) E.missing[s] = 1;
+    }
+    int ct = 0;
+    for (int cidx : M.conserve) if (cidx >= 0 && cidx < N && E.missing[cidx]) ct++;
+    if (ct > conserve_prop * (double)M.conserve.size()) { E.filtered = 1; return; }
+    E.c2a = M.ch0; E.c2b = M.ch1; E.par = M.parent; E.d2 = M.dist;
+    E.root = N - 1;
+    collapse_missing_path(S, M.upper, E.c2a, E.c2b, E.par, E.d2, E.missing, E.root);
+    E.par[E.root] = N;
+    E.nodes = postorder_nodes(E.root, E.c2a, E.c2b);
+    // the outgroup path has no accelerated class (fixZ, bpp_c.cpp:144-150)
+    E.fixed.assign(N, 0);
+    for (int s : E.nodes) if (M.upper[s] && s != E.root) E.fixed[s] = 1;
+}
+
 // Per-element preprocessing (BPP_C ctor, bpp_c.hpp:143-476).  Returns false
 // only on invalid input; filtered elements return true with E.filtered = 1.
 static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* bases, int len, HostElem& E,
@@ -206,58 +335,9 @@ static bool preprocess(const HostModel& M, const pacc_opts& o, const uint8_t* ba
     int root = N - 1;
     std::vector<char> up(N, 0);
     for (int s = 0; s < N; s++) up[s] = o.prune_tree ? 1 : M.upper[s];
-    struct Walker {
-        int S;
-        std::vector<int>&c2a, &c2b, &par;
-        std::vector<double>& d2;
-        std::vector<char>&missing, &up;
-        int& root;
-        void walk(int ss, int child) {
-            if (!up[ss] || ss < S) return;
-            int s = ss;
-            while (up[s] && s >= S) {
-                int p0 = c2a[s], p1 = c2b[s];
-                int keep;
-                if (missing[p0] && !missing[p1]) { keep = p1; par[p0] = -1; }
-                else if (!missing[p0] && missing[p1]) { keep = p0; par[p1] = -1; }
-                else {
-                    walk(p0, 0);
-                    walk(p1, 1);
-                    return;
-                }
-                d2[keep] += d2[s];
-                if (s == root) root = keep;
-                else {
-                    (child == 0 ? c2a : c2b)[par[ss]] = keep;
-                    par[keep] = par[ss];
-                }
-                s = keep;
-            }
-        }
-    } wk{S, c2a, c2b, par, d2, missing, up, root};
-    wk.walk(N - 1, -1);
+    collapse_missing_path(S, up, c2a, c2b, par, d2, missing, root);
     par[root] = N;
-    // postorder of the pruned tree (bpp_c.cpp:44-60)
-    std::vector<int> nodes;
-    nodes.reserve(N);
-    {
-        std::vector<std::pair<int, int>> st;
-        st.push_back({root, 0});
-        while (!st.empty()) {
-            auto& t = st.back();
-            int j = t.first;
-            if (t.second == 0) {
-                t.second = 1;
-                if (c2a[j] != -1) { st.push_back({c2a[j], 0}); continue; }
-            }
-            if (t.second == 1) {
-                t.second = 2;
-                if (c2b[j] != -1) { st.push_back({c2b[j], 0}); continue; }
-            }
-            nodes.push_back(j);
-            st.pop_back();
-        }
-    }
+    const std::vector<int> nodes = postorder_nodes(root, c2a, c2b);
     std::vector<int> internal;
     for (int s : nodes) if (s >= S) internal.push_back(s);
     if (internal.empty()) { E.filtered = 2; return true; }  // the whole tree collapsed to one leaf
@@ -659,9 +739,11 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
     DevModel& dm = M.dm;
     std::memset(&dm, 0, sizeof(dm));
     dm.S = S; dm.N = N;
+    std::memcpy(M.rate, model->rate_matrix, sizeof(M.rate));
     for (int i = 0; i < 4; i++) {
         dm.lam[i] = lam[i];
         dm.pi[i] = model->pi[i];
+        M.pi[i] = model->pi[i];
         dm.log_pi[i] = std::log(model->pi[i]);
         for (int j = 0; j < 4; j++) {
             dm.evec[i * 4 + j] = V[j * 4 + i];
@@ -2422,6 +2504,101 @@ int pacc_get_launch_shape(pacc_ctx* c, int32_t* block_threads, int32_t* register
     if (chains_per_sm) *chains_per_sm = cta ? c->shape_per_sm : 0;
     if (trial_ms) *trial_ms = cta ? c->shape_trial_ms : 0;
     return PACC_OK;
+}
+
+int pacc_gbgc_engine(pacc_ctx* c, const uint8_t* bases, int32_t length, int32_t gapchar, double missing_thres,
+                     const int32_t* z, const int32_t* bflag, double sel_c, double sel_n, double gc_bias, double* logp,
+                     double* col, double* counts, int32_t* root, uint8_t* missing, int32_t* filtered) {
+    if (!c) return PACC_EINVAL;
+    const int S = c->M.S, N = c->M.N;
+    if (!bases || length <= 0 || !z || !bflag || !logp || !col || !counts || !root || !missing || !filtered) {
+        c->err = "gbgc_engine: length must be positive and every array non-null";
+        return PACC_EINVAL;
+    }
+    if (!c->gpu_ok) { c->err = "gbgc_engine: no usable GPU"; return PACC_ECUDA; }
+    GbgcElem E;
+    gbgc_prepare(c->M, bases, length, (char)gapchar, missing_thres, c->o.conserve_prop, E);
+    *filtered = E.filtered;
+    for (int s = 0; s < N; s++) missing[s] = (uint8_t)E.missing[s];
+    if (E.filtered) return PACC_FILTERED;
+    // the state of every branch of the element's tree (other nodes are not read)
+    for (size_t k = 0; k + 1 < E.nodes.size(); k++) {
+        const int s = E.nodes[k];
+        if (z[s] < 0 || z[s] > 2 || (bflag[s] != 0 && bflag[s] != 1) || (z[s] == 2 && E.fixed[s])) {
+            c->err = "gbgc_engine: z must be 0..2 (0..1 on the outgroup path) and b 0 or 1 on node " +
+                     std::to_string(s);
+            return PACC_EINVAL;
+        }
+    }
+    *root = E.root;
+    if (!cuda_ok(c, cudaSetDevice(c->device), "gbgc_engine: cudaSetDevice")) return PACC_ECUDA;
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
+    const size_t rb = prec ? 4 : 8;
+    const int warps = std::max(1, std::min(8, E.GGp / 32));
+    const int GGp = E.GGp, nn = (int)E.nodes.size();
+    // one device allocation: host-built inputs first, then outputs and scratch
+    std::vector<int16_t> i16((size_t)nn + 3 * N);
+    for (int k = 0; k < nn; k++) i16[k] = (int16_t)E.nodes[k];
+    for (int s = 0; s < N; s++) {
+        i16[nn + s] = (int16_t)E.c2a[s];
+        i16[nn + N + s] = (int16_t)E.c2b[s];
+        i16[nn + 2 * N + s] = (int16_t)E.par[s];
+    }
+    std::vector<int32_t> cls(N);
+    std::vector<uint8_t> u8(2 * (size_t)N);
+    for (int s = 0; s < N; s++) {
+        cls[s] = 0;
+        u8[s] = (uint8_t)E.missing[s];
+        u8[N + s] = (uint8_t)E.fixed[s];
+    }
+    for (size_t k = 0; k + 1 < E.nodes.size(); k++) cls[E.nodes[k]] = z[E.nodes[k]] + 3 * bflag[E.nodes[k]];
+    auto up16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    size_t o = 0;
+    const size_t o_d2 = o;     o += up16(8 * (size_t)N);
+    const size_t o_logp = o;   o += up16(8 * 96 * (size_t)N);
+    const size_t o_pm = o;     o += up16(rb * 96 * (size_t)N);
+    const size_t o_col = o;    o += up16(8 * (size_t)GGp);
+    const size_t o_cnt = o;    o += up16(8 * 16 * (size_t)N);
+    const size_t o_wc = o;     o += up16(8 * 16 * (size_t)N * warps);
+    const size_t o_part = o;   o += up16(rb * 4 * (size_t)N * GGp);
+    const size_t o_scl = o;    o += up16(4 * (size_t)N * GGp);
+    const size_t o_cls = o;    o += up16(4 * (size_t)N);
+    const size_t o_i16 = o;    o += up16(2 * i16.size());
+    const size_t o_u8 = o;     o += up16(u8.size());
+    const size_t o_mask = o;   o += up16(E.masks.size());
+    char* dev = nullptr;
+    if (!cuda_ok(c, cudaMalloc((void**)&dev, o), "gbgc_engine: cudaMalloc")) return PACC_OOM;
+    cudaStream_t st = c->aux;
+    GbgcParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.S = S; p.N = N; p.GG = E.GG; p.GGp = GGp; p.root = E.root; p.n_nodes = nn; p.warps = warps;
+    p.nodes = (const int16_t*)(dev + o_i16);
+    p.c0 = p.nodes + nn; p.c1 = p.c0 + N; p.parent = p.c1 + N;
+    p.missing = (const uint8_t*)(dev + o_u8); p.fixed = p.missing + N;
+    p.dist = (const double*)(dev + o_d2);
+    p.cls = (const int32_t*)(dev + o_cls);
+    p.masks = (const uint8_t*)(dev + o_mask);
+    std::memcpy(p.Q0, c->M.rate, sizeof(p.Q0));
+    std::memcpy(p.pi, c->M.pi, sizeof(p.pi));
+    p.sc = sel_c; p.sn = sel_n; p.gb = gc_bias;
+    p.logp = (double*)(dev + o_logp); p.pmat = dev + o_pm;
+    p.col = (double*)(dev + o_col); p.counts = (double*)(dev + o_cnt); p.wcounts = (double*)(dev + o_wc);
+    p.part = dev + o_part; p.scl = (int32_t*)(dev + o_scl);
+    // logp and the matrices start at zero: classes that are not built stay 0,
+    // as the reference's zero-initialised caches do
+    bool ok = cuda_ok(c, cudaMemsetAsync(dev + o_logp, 0, o_col - o_logp, st), "gbgc_engine: memset") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_d2, E.d2.data(), 8 * (size_t)N, cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_cls, cls.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_i16, i16.data(), 2 * i16.size(), cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_u8, u8.data(), u8.size(), cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_mask, E.masks.data(), E.masks.size(), cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, launch_gbgc(p, prec, st), "gbgc_engine: launch") &&
+              cuda_ok(c, cudaMemcpyAsync(logp, dev + o_logp, 8 * 96 * (size_t)N, cudaMemcpyDeviceToHost, st), "D2H") &&
+              cuda_ok(c, cudaMemcpyAsync(col, dev + o_col, 8 * (size_t)E.GG, cudaMemcpyDeviceToHost, st), "D2H") &&
+              cuda_ok(c, cudaMemcpyAsync(counts, dev + o_cnt, 8 * 16 * (size_t)N, cudaMemcpyDeviceToHost, st), "D2H") &&
+              cuda_ok(c, cudaStreamSynchronize(st), "gbgc_engine");
+    cudaFree(dev);
+    return ok ? PACC_OK : PACC_ECUDA;
 }
 
 int pacc_debug_pmatrix(pacc_ctx* c, int n, const double* d, const double* r, double* out) {
