@@ -249,6 +249,61 @@ int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);
 int pacc_get_launch_shape(pacc_ctx* ctx, int32_t* block_threads, int32_t* registers, int32_t* chains_per_sm,
                           double* trial_ms);
 
+/* --- The gBGC model (PhyloAcc-ST-GBGC, src/PhyloAcc-ST-GBGC/SRC) --- */
+
+/* Options of the gBGC model's chains.  pacc_gbgc_default_opts() gives that
+ * program's defaults (main.cpp:36-81; bpp.cpp:217-219; bpp_c.hpp:365-370). */
+typedef struct pacc_gbgc_opts {
+    int32_t burnin;               /* BURNIN (200) */
+    int32_t mcmc;                 /* MCMC (800) */
+    uint32_t seed;                /* SEED (7728): every element's stream starts from it */
+    int32_t gapchar;              /* GAPCHAR ('*'): the character counted as missing */
+    double conserve_rate;         /* CONSERVE_RATE (-2): initial conserved selection */
+    double acce_rate;             /* ACCE_RATE (0): initial accelerated selection */
+    double init_gc;               /* initial GC bias (3; cur_nGB, bpp.cpp:219) */
+    double conserve_prior_a;      /* CONSERVE_PRIOR_A (5): -selection_c ~ Gamma(a, b) */
+    double conserve_prior_b;      /* CONSERVE_PRIOR_B (0.4) */
+    double acce_prior_a;          /* ACCE_PRIOR_A (5): selection_n + shift ~ Gamma(a, b) */
+    double acce_prior_b;          /* ACCE_PRIOR_B (0.4) */
+    double acce_prior_shift;      /* nprior_c (2, bpp.hpp:199) */
+    double gc_prior_a;            /* nGBprior_a (4): GC bias ~ Gamma(a, b) */
+    double gc_prior_b;            /* nGBprior_b (0.8) */
+    double gc_prior_c;            /* nGBprior_c (0.2): prior probability of B = 1 on a branch */
+    double prep_lrate;            /* PREP_LRATE (0.1): P(Z 1 -> 2) */
+    double prep_grate;            /* PREP_GRATE (0.8): P(Z 0 -> 1) */
+    double cons_to_mis;           /* CONSTOMIS (0.01) */
+    double ncons_to_mis;          /* nconsToMis (0.1) */
+    double missing_thres;         /* GAP_PROP (0.8): a taxon with more gap characters is missing */
+    double conserve_prop;         /* CONSERVE_PROP (0.8) */
+    double prop_c, prop_n, prop_gc;   /* proposal widths (1.2, 1.2, 0.2; bpp_c.hpp:365-370) */
+    const int32_t* target;        /* TARGETSPECIES node ids (M2 lets only these leaves accelerate) */
+    int32_t n_target;
+    int32_t reserved;
+} pacc_gbgc_opts;
+
+void pacc_gbgc_default_opts(pacc_gbgc_opts* opts);
+
+/* One element's gBGC results: the three models run M0 (null), M2 (res),
+ * M1 (full) from one stream, as main.cpp:383-412 does; arrays are indexed by
+ * model 0 = M0, 1 = M1, 2 = M2. */
+typedef struct pacc_gbgc_result {
+    int64_t element_no;
+    int32_t status;               /* PACC_OK or PACC_FILTERED */
+    int32_t root;                 /* the element's root after the outgroup-path collapse */
+    double loglik_null;           /* Eval2 of M0 (bpp_c2.cpp:29-286): loglik_NUll */
+    double loglik_res;            /* Eval2 of M2: loglik_RES */
+    double loglik_all;            /* Eval2 of M1: loglik_all */
+    double max_loglik[3];         /* loglik_Max1..3: the best full log-likelihood after burn-in */
+    double rates[3][3];           /* posterior medians: [model][n_rate, c_rate, gBC] (bpp_c2.cpp:603-615) */
+    double device_ms;
+    /* caller-provided outputs (NULL to skip) */
+    int32_t* max_z;               /* [3][N] Max_Z */
+    int8_t* max_b;                /* [3][N] Max_B */
+    double* post_b;               /* [3][N] fraction of samples with B = 1 */
+    double* post_z;               /* [3][N][4] fractions of Z = -1, 0, 1, 2 (missing branches: 1 in column 0) */
+    double* trace;                /* [3][burnin+mcmc][4 + 2N]: full loglik, n, c, gBC, B[N], Z[N] */
+} pacc_gbgc_result;
+
 /* --- Kernel-level entry points used by parity tests (same kernels as the chain) --- */
 
 /* (a) P^T = eigeninv * diag(exp(lambda*d*r)) * eigenvec for n branch lengths

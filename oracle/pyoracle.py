@@ -206,3 +206,37 @@ def gbgc_engine(ds, e, z, b, sc, sn, gb, gapchar="*", missing_thres=0.8, conserv
         raise RuntimeError("oracle_gbgc_engine failed: %d" % st)
     return {"logp": logp.reshape(6, N, 4, 4), "col": col, "counts": counts.reshape(N, 4, 4), "root": root.value,
             "missing": miss, "filtered": filt.value}
+
+
+def gbgc_run(ds, o: abi.PaccGbgcOpts, e: int, trace: bool = True) -> dict:
+    """One element through the gBGC model's three chains on the CPU
+    (oracle_gbgc.cpp, oracle_gbgc_run_element).  Arrays by model index
+    0 = M0, 1 = M1, 2 = M2; trace rows: full loglik, n, c, gBC, B[N], Z[N]."""
+    L = lib()
+    if not hasattr(L, "_gbgc_run_set"):
+        L.oracle_gbgc_run_element.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccGbgcOpts),
+                                              C.POINTER(C.c_uint8), C.c_int32, C.POINTER(abi.PaccGbgcResult)]
+        L.oracle_gbgc_run_element.restype = C.c_int
+        L._gbgc_run_set = True
+    m = abi.ModelArgs(ds)
+    N = ds.tree.n_nodes
+    GG = int(ds.lengths[e])
+    T = o.burnin + o.mcmc
+    blk = np.ascontiguousarray(ds.element(e).reshape(-1))
+    r = abi.PaccGbgcResult()
+    out = {"max_z": np.zeros((3, N), np.int32), "max_b": np.zeros((3, N), np.int8),
+           "post_b": np.zeros((3, N)), "post_z": np.zeros((3, N, 4))}
+    r.max_z = abi.ptr(out["max_z"], C.c_int32)
+    r.max_b = abi.ptr(out["max_b"], C.c_int8)
+    r.post_b = abi.ptr(out["post_b"], C.c_double)
+    r.post_z = abi.ptr(out["post_z"], C.c_double)
+    if trace:
+        out["trace"] = np.zeros((3, T, 4 + 2 * N))
+        r.trace = abi.ptr(out["trace"], C.c_double)
+    st = L.oracle_gbgc_run_element(C.byref(m.model), C.byref(o), abi.ptr(blk, C.c_uint8), GG, C.byref(r))
+    if st not in (abi.PACC_OK, abi.PACC_FILTERED):
+        raise RuntimeError("oracle_gbgc_run_element failed: %d" % st)
+    out.update({"status": r.status, "root": r.root, "loglik_null": r.loglik_null, "loglik_res": r.loglik_res,
+                "loglik_all": r.loglik_all, "max_loglik": np.array(r.max_loglik[:]),
+                "rates": np.array([[r.rates[i][j] for j in range(3)] for i in range(3)])})
+    return out

@@ -145,6 +145,54 @@ def ptr(a: np.ndarray, ctype):
     return a.ctypes.data_as(C.POINTER(ctype))
 
 
+class PaccGbgcOpts(C.Structure):
+    _fields_ = [
+        ("burnin", C.c_int32), ("mcmc", C.c_int32), ("seed", C.c_uint32), ("gapchar", C.c_int32),
+        ("conserve_rate", C.c_double), ("acce_rate", C.c_double), ("init_gc", C.c_double),
+        ("conserve_prior_a", C.c_double), ("conserve_prior_b", C.c_double),
+        ("acce_prior_a", C.c_double), ("acce_prior_b", C.c_double), ("acce_prior_shift", C.c_double),
+        ("gc_prior_a", C.c_double), ("gc_prior_b", C.c_double), ("gc_prior_c", C.c_double),
+        ("prep_lrate", C.c_double), ("prep_grate", C.c_double),
+        ("cons_to_mis", C.c_double), ("ncons_to_mis", C.c_double),
+        ("missing_thres", C.c_double), ("conserve_prop", C.c_double),
+        ("prop_c", C.c_double), ("prop_n", C.c_double), ("prop_gc", C.c_double),
+        ("target", C.POINTER(C.c_int32)), ("n_target", C.c_int32), ("reserved", C.c_int32)]
+
+
+def gbgc_default_opts(target=None) -> PaccGbgcOpts:
+    """PhyloAcc-ST-GBGC's defaults (src/PhyloAcc-ST-GBGC/SRC/main.cpp:36-81,
+    bpp.cpp:217-219, bpp_c.hpp:365-370); the values pacc_gbgc_default_opts()
+    writes.  target: TARGETSPECIES node ids (kept alive on the object)."""
+    o = PaccGbgcOpts()
+    o.burnin, o.mcmc, o.seed, o.gapchar = 200, 800, 7728, ord("*")
+    o.conserve_rate, o.acce_rate, o.init_gc = -2.0, 0.0, 3.0
+    o.conserve_prior_a, o.conserve_prior_b = 5.0, 0.4
+    o.acce_prior_a, o.acce_prior_b, o.acce_prior_shift = 5.0, 0.4, 2.0
+    o.gc_prior_a, o.gc_prior_b, o.gc_prior_c = 4.0, 0.8, 0.2
+    o.prep_lrate, o.prep_grate = 0.1, 0.8
+    o.cons_to_mis, o.ncons_to_mis = 0.01, 0.1
+    o.missing_thres, o.conserve_prop = 0.8, 0.8
+    o.prop_c, o.prop_n, o.prop_gc = 1.2, 1.2, 0.2
+    set_gbgc_target(o, target or [])
+    return o
+
+
+def set_gbgc_target(o: PaccGbgcOpts, target):
+    arr = np.ascontiguousarray(target, dtype=np.int32)
+    o._target_keep = arr
+    o.target = ptr(arr, C.c_int32)
+    o.n_target = len(arr)
+
+
+class PaccGbgcResult(C.Structure):
+    _fields_ = [
+        ("element_no", C.c_int64), ("status", C.c_int32), ("root", C.c_int32),
+        ("loglik_null", C.c_double), ("loglik_res", C.c_double), ("loglik_all", C.c_double),
+        ("max_loglik", C.c_double * 3), ("rates", (C.c_double * 3) * 3), ("device_ms", C.c_double),
+        ("max_z", C.POINTER(C.c_int32)), ("max_b", C.POINTER(C.c_int8)), ("post_b", C.POINTER(C.c_double)),
+        ("post_z", C.POINTER(C.c_double)), ("trace", C.POINTER(C.c_double))]
+
+
 class ModelArgs:
     """Keeps the numpy buffers behind a PaccModel alive."""
 

@@ -1,0 +1,65 @@
+"""The oracle's gBGC chain (oracle/oracle_gbgc.cpp, oracle_gbgc_run_element)
+against what the unmodified gBGC reference wrote for the gbgc12_default case
+(tests/golden/gbgc12_default): the per-iteration traces of the three models
+(full log-likelihood, selection, GC bias, B and Z on every node), the
+element table (Eval2's marginal likelihoods and the best full
+log-likelihoods) and the per-model tables of rate medians and B / Z
+frequencies.  The reference prints 8 significant digits in the traces and
+element table and 6 in the per-model tables; the comparisons allow those."""
+import os
+
+import numpy as np
+
+from golden_io import GOLDEN, as_float, load_case, read_table
+from oracle import pyoracle as po
+from phyloacc_gb300 import abi
+
+
+def gbgc_opts(ds, kv):
+    o = abi.gbgc_default_opts(ds.target)
+    o.burnin, o.mcmc, o.seed = int(kv["BURNIN"]), int(kv["MCMC"]), int(kv["SEED"])
+    if "GAPCHAR" in kv:
+        o.gapchar = ord(kv["GAPCHAR"][0])
+    return o
+
+
+def _runs(case):
+    ds, _, kv = load_case(case)
+    o = gbgc_opts(ds, kv)
+    return ds, o, [po.gbgc_run(ds, o, e) for e in range(ds.n_elements)]
+
+
+def test_gbgc_chain_traces_match_reference(built):
+    ds, o, runs = _runs("gbgc12_default")
+    tr = np.load(os.path.join(GOLDEN, "gbgc12_default", "traces.npz"))
+    for e, r in enumerate(runs):
+        assert r["status"] == abi.PACC_OK
+        for m in range(3):
+            want = tr["%d_%d" % (m, e)]
+            got = r["trace"][m]
+            assert got.shape == want.shape
+            np.testing.assert_allclose(got, want, rtol=1e-7, atol=1e-9)
+
+
+def test_gbgc_chain_tables_match_reference(built):
+    ds, o, runs = _runs("gbgc12_default")
+    N = ds.tree.n_nodes
+    out = os.path.join(GOLDEN, "gbgc12_default", "out")
+    hdr, rows = read_table(os.path.join(out, "case_elem_lik.txt"))
+    assert hdr[2:] == ["loglik_NUll", "loglik_RES", "loglik_all", "log_ratio", "loglik_Max1", "loglik_Max2",
+                       "loglik_Max3"]
+    for e, (r, row) in enumerate(zip(runs, rows)):
+        got = [r["loglik_null"], r["loglik_res"], r["loglik_all"], r["loglik_res"] - r["loglik_null"]] + \
+            list(r["max_loglik"])
+        np.testing.assert_allclose(got, [as_float(x) for x in row[2:9]], rtol=1e-7, atol=1e-6)
+    for m in range(3):
+        _, rows = read_table(os.path.join(out, "case_rate_postZ_%d.txt" % m))
+        for e, (r, row) in enumerate(zip(runs, rows)):
+            vals = [as_float(x) for x in row[1:] if x != ""]
+            got = list(r["rates"][m]) + list(r["post_b"][m]) + list(r["post_z"][m].reshape(-1))
+            assert len(vals) == 3 + N + 4 * N
+            np.testing.assert_allclose(got, vals, rtol=1e-5, atol=1e-6)
+    # Max_Z of the full model (the _1_elem_Z table)
+    lines = [ln.rstrip("\n\t").split("\t") for ln in open(os.path.join(out, "case_1_elem_Z.txt"))][1:]
+    for r, ln in zip(runs, lines):
+        assert [int(x) for x in ln] == list(r["max_z"][1])
