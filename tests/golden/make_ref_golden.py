@@ -43,8 +43,10 @@ CASES = {
     "st12_hyper": ("st12", [0, 1, 85, 90], 60, 150, 4, {"CHAIN": 3, "SAMPLE_HYPER": 1}),
     # the gBGC model (src/PhyloAcc-ST-GBGC): same inputs, its own outputs and traces
     "gbgc12_default": ("st12", [0, 1, 85, 90], 20, 60, 0, {}),
+    # 43 taxa with missing taxa ('*' rows): the outgroup (root moves), conserved and target leaves
+    "gbgc43_missing": ("st43", [0, 7, 12, 20], 30, 90, 5, {}),
 }
-GBGC_CASES = {"gbgc12_default"}
+GBGC_CASES = {"gbgc12_default", "gbgc43_missing"}
 
 
 def mask_taxa(ds, case):
@@ -59,6 +61,15 @@ def mask_taxa(ds, case):
             blk[s, :] = ord("n")
         blk = ds.element(3)
         blk[ds.target[0], : blk.shape[1] // 2] = ord("-")
+    if case == "gbgc43_missing":
+        star = ord("*")
+        ds.element(1)[ds.outgroup[0], :] = star
+        blk = ds.element(2)
+        for s in ds.conserve[:3]:
+            blk[s, :] = star
+        blk = ds.element(3)
+        blk[ds.target[0], :] = star
+        blk[ds.target[1], : blk.shape[1] // 3] = star      # under the threshold: not missing
     if case == "st43_default":
         blk = ds.element(1)
         blk[0, :] = ord("-")

@@ -1,6 +1,7 @@
 """The oracle's gBGC chain (oracle/oracle_gbgc.cpp, oracle_gbgc_run_element)
 against what the unmodified gBGC reference wrote for the gbgc12_default case
-(tests/golden/gbgc12_default): the per-iteration traces of the three models
+(tests/golden/gbgc12_default) and the gbgc43_missing case (43 taxa with the
+outgroup, three conserved leaves and a target leaf missing in some elements): the per-iteration traces of the three models
 (full log-likelihood, selection, GC bias, B and Z on every node), the
 element table (Eval2's marginal likelihoods and the best full
 log-likelihoods) and the per-model tables of rate medians and B / Z
@@ -9,6 +10,7 @@ element table and 6 in the per-model tables; the comparisons allow those."""
 import os
 
 import numpy as np
+import pytest
 
 from golden_io import GOLDEN, as_float, load_case, read_table
 from oracle import pyoracle as po
@@ -29,9 +31,13 @@ def _runs(case):
     return ds, o, [po.gbgc_run(ds, o, e) for e in range(ds.n_elements)]
 
 
-def test_gbgc_chain_traces_match_reference(built):
-    ds, o, runs = _runs("gbgc12_default")
-    tr = np.load(os.path.join(GOLDEN, "gbgc12_default", "traces.npz"))
+CASES = ["gbgc12_default", "gbgc43_missing"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gbgc_chain_traces_match_reference(built, case):
+    ds, o, runs = _runs(case)
+    tr = np.load(os.path.join(GOLDEN, case, "traces.npz"))
     for e, r in enumerate(runs):
         assert r["status"] == abi.PACC_OK
         for m in range(3):
@@ -41,10 +47,11 @@ def test_gbgc_chain_traces_match_reference(built):
             np.testing.assert_allclose(got, want, rtol=1e-7, atol=1e-9)
 
 
-def test_gbgc_chain_tables_match_reference(built):
-    ds, o, runs = _runs("gbgc12_default")
+@pytest.mark.parametrize("case", CASES)
+def test_gbgc_chain_tables_match_reference(built, case):
+    ds, o, runs = _runs(case)
     N = ds.tree.n_nodes
-    out = os.path.join(GOLDEN, "gbgc12_default", "out")
+    out = os.path.join(GOLDEN, case, "out")
     hdr, rows = read_table(os.path.join(out, "case_elem_lik.txt"))
     assert hdr[2:] == ["loglik_NUll", "loglik_RES", "loglik_all", "log_ratio", "loglik_Max1", "loglik_Max2",
                        "loglik_Max3"]
