@@ -304,6 +304,16 @@ typedef struct pacc_gbgc_result {
     double* trace;                /* [3][burnin+mcmc][4 + 2N]: full loglik, n, c, gBC, B[N], Z[N] */
 } pacc_gbgc_result;
 
+/* Run every element of the batch through the gBGC model's three chains on
+ * the device (one CTA an element; the element loop of main.cpp:383-412 with
+ * BPP_C, initMCMC, Gibbs, Eval2 and Output_init per model).  The context gives
+ * the tree, rate matrix, outgroup and conserved sets and the precision of the
+ * partials (PACC_FP32 / PACC_FP32_WARP: FP32, else FP64); its other options
+ * are not used.  Eval2 and Output_init run on the host from the device's
+ * traces.  Returns when every element's result is written. */
+int pacc_gbgc_run(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_batch* batch,
+                  pacc_gbgc_result* out);
+
 /* --- Kernel-level entry points used by parity tests (same kernels as the chain) --- */
 
 /* (a) P^T = eigeninv * diag(exp(lambda*d*r)) * eigenvec for n branch lengths

@@ -59,6 +59,9 @@ def lib():
         L.pacc_measure_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.pacc_get_launch_shape.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.pacc_gbgc_default_opts.argtypes = [C.POINTER(abi.PaccGbgcOpts)]
+        L.pacc_gbgc_run.argtypes = [C.c_void_p, C.POINTER(abi.PaccGbgcOpts), C.POINTER(abi.PaccElementBatch),
+                                    C.POINTER(abi.PaccGbgcResult)]
         L.pacc_gbgc_engine.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_double,
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_double, C.c_double,
                                        C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -214,6 +217,43 @@ class Context:
             self._err("pacc_gbgc_engine", st)
         return {"logp": logp.reshape(6, N, 4, 4), "col": col, "counts": counts.reshape(N, 4, 4), "root": root.value,
                 "missing": miss, "filtered": 0}
+
+    def gbgc_run(self, gopts, elements=None, trace: bool = False, ds=None) -> list:
+        """The gBGC model's three chains for the given elements (default: all)
+        on the device; one dict per element with the fields of
+        pacc_gbgc_result and arrays by model index 0 = M0, 1 = M1, 2 = M2."""
+        ds = ds or self.ds
+        idx = list(range(ds.n_elements)) if elements is None else list(elements)
+        N = ds.tree.n_nodes
+        T = gopts.burnin + gopts.mcmc
+        sub = ds.subset(idx) if idx != list(range(ds.n_elements)) else ds
+        batch = abi.BatchArgs(sub, np.array(idx, np.int64))
+        res = (abi.PaccGbgcResult * len(idx))()
+        bufs = []
+        for k in range(len(idx)):
+            b = {"max_z": np.zeros((3, N), np.int32), "max_b": np.zeros((3, N), np.int8),
+                 "post_b": np.zeros((3, N)), "post_z": np.zeros((3, N, 4))}
+            res[k].max_z = abi.ptr(b["max_z"], C.c_int32)
+            res[k].max_b = abi.ptr(b["max_b"], C.c_int8)
+            res[k].post_b = abi.ptr(b["post_b"], C.c_double)
+            res[k].post_z = abi.ptr(b["post_z"], C.c_double)
+            if trace:
+                b["trace"] = np.zeros((3, T, 4 + 2 * N))
+                res[k].trace = abi.ptr(b["trace"], C.c_double)
+            bufs.append(b)
+        st = lib().pacc_gbgc_run(self.h, C.byref(gopts), C.byref(batch.batch), res)
+        if st != 0:
+            self._err("pacc_gbgc_run", st)
+        out = []
+        for k in range(len(idx)):
+            r = res[k]
+            d = dict(bufs[k])
+            d.update({"element_no": r.element_no, "status": r.status, "root": r.root,
+                      "loglik_null": r.loglik_null, "loglik_res": r.loglik_res, "loglik_all": r.loglik_all,
+                      "max_loglik": np.array(r.max_loglik[:]), "device_ms": r.device_ms,
+                      "rates": np.array([[r.rates[i][j] for j in range(3)] for i in range(3)])})
+            out.append(d)
+        return out
 
     def patterns(self, e: int):
         """(pattern_of [n_cols], weights [n_patterns]) of element e (host only)."""

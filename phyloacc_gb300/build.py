@@ -47,6 +47,7 @@ def build(force=False, verbose=False):
         "pacc_host.o": [NVCC] + ARCH + COMMON + ["-x", "cu", "-c", os.path.join(CSRC, "pacc_host.cpp")],
         "pacc_noalloc.o": [NVCC] + ARCH + COMMON + ["-c", os.path.join(CSRC, "pacc_noalloc.cu")],
         "pacc_gbgc.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_gbgc.cu")],
+        "pacc_gbgc_chain.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_gbgc_chain.cu")],
     }
     cmds = []
     for name, cmd in objs.items():

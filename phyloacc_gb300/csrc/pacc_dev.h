@@ -240,4 +240,68 @@ struct GbgcParams {
     int32_t* scl;                       // [N][GGp] power-of-two exponents of the partials
 };
 
+// ---- the gBGC model's chain kernel ----
+
+// One element of the gBGC chain: its tree after the outgroup-path collapse
+// and its leaf columns, as byte offsets into the element's blob.
+struct GbgcElemHdr {
+    int32_t S, N, GG, GGp, root, n_nodes, n_int, n_hlev, n_dlev;
+    int32_t o_nodes, o_c0, o_c1, o_par, o_irank, o_pidx, o_flags;   // int16 / uint8 [N]
+    int32_t o_dist;                  // double [N]
+    int32_t o_hlev, o_hnodes;        // internal nodes by height: starts [n_hlev + 1], nodes
+    int32_t o_dlev, o_dnodes;        // non-root nodes by depth: starts [n_dlev + 1], nodes
+    int32_t o_masks;                 // uint8 [S][GGp] allowed bases
+    int32_t pad;
+    int64_t blob_off;
+};
+
+enum { GBGC_MISSING = 1, GBGC_UPPER = 2, GBGC_TARGET = 4 };
+
+// Per-CTA workspace of the gBGC chain kernel (byte offsets).  Matrix slots:
+// 0 the null class; 1 + 5 q + (k - 1) class k = 1..5 of cache set q = 0..2.
+struct GbgcWs {
+    size_t lP, pm, post, wc, emis, emis_tmp, lpb, eraw, colsum, part, scl, total;
+    static __host__ __device__ size_t up(size_t b) { return (b + 255) & ~(size_t)255; }
+    static __host__ __device__ GbgcWs make(int N, int n_int, int GGp, int warps, int rb) {
+        GbgcWs w;
+        size_t o = 0;
+        w.lP = o;       o += up((size_t)16 * N * 16 * 8);
+        w.pm = o;       o += up((size_t)16 * N * 16 * rb);
+        w.post = o;     o += up((size_t)2 * N * 16 * 8);
+        w.wc = o;       o += up((size_t)warps * N * 16 * 8);
+        w.emis = o;     o += up((size_t)N * 6 * 8);
+        w.emis_tmp = o; o += up((size_t)N * 6 * 8);
+        w.lpb = o;      o += up((size_t)N * 6 * 8);
+        w.eraw = o;     o += up((size_t)N * 8);
+        w.colsum = o;   o += up((size_t)warps * 8);
+        w.part = o;     o += up((size_t)2 * n_int * GGp * 4 * rb);
+        w.scl = o;      o += up((size_t)2 * n_int * GGp * 4);
+        w.total = o;
+        return w;
+    }
+};
+
+struct GbgcChainParams {
+    const GbgcElemHdr* hdr;
+    const uint8_t* blob;
+    int n_elem;
+    int* next_elem;
+    int T, burn, mcmc;
+    uint32_t seed;
+    double conserve_rate, acce_rate, init_gc;
+    double ca, cb, na, nb, nshift, gca, gcb, gcc;   // priors: conserved, accelerated (+ shift), GC bias
+    double lrate, grate, c2m, nc2m, prop_c, prop_n, prop_gc;
+    double Q0[16], pi[4];
+    const uint8_t* target;    // [N_max] TARGETSPECIES flags
+    char* ws;
+    size_t ws_stride;
+    int N_max, n_int_max, GGp_max;
+    // outputs
+    double* tr_d;             // [n_elem][3][4][T]: full loglik, n, c, gBC
+    int8_t* tr_zb;            // [n_elem][3][T][2][N_max]: Z then B
+    int8_t* max_zb;           // [n_elem][3][2][N_max]
+    double* max_ll;           // [n_elem][3]
+    int32_t* status;          // [n_elem]
+};
+
 }  // namespace pacc

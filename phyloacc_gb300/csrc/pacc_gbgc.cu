@@ -28,29 +28,9 @@
 #include <stdint.h>
 
 #include "pacc_dev.h"
+#include "pacc_gbgc.cuh"
 
 namespace pacc {
-
-// getRate (bpp_c.cpp:13-30): Q0 scaled entrywise by f(s + b B_ij) with
-// f(x) = x / (1 - e^-x) (f(0) = 1), B_ij = +1 from A/T to C/G, -1 from C/G
-// to A/T, 0 otherwise (the diagonal included); then each diagonal entry
-// reset so that its row sums to zero.
-__device__ void gbgc_rate(const double* Q0, double s, double b, double* Q) {
-    for (int q = 0; q < 16; q++) Q[q] = Q0[q];
-    if (s == 0 && b == 0) return;
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) {
-            const bool weak_i = (i == 0 || i == 3), weak_j = (j == 0 || j == 3);
-            const double bij = (weak_i && !weak_j) ? b : ((!weak_i && weak_j) ? -b : 0.0);
-            const double v = bij + s;
-            Q[i * 4 + j] *= (v == 0) ? 1.0 : v / (1 - exp(-v));
-        }
-    for (int i = 0; i < 4; i++) {
-        double c = 0;
-        for (int j = 0; j < 4; j++) c += Q[i * 4 + j];
-        Q[i * 4 + i] -= c;
-    }
-}
 
 __device__ __forceinline__ void mm4(const double* A, const double* B, double* C) {
 #pragma unroll
@@ -155,18 +135,6 @@ __global__ void gbgc_pmat_kernel(GbgcParams p) {
     }
 }
 
-template <typename Real> struct GbgcScale;
-template <> struct GbgcScale<float> {
-    static __device__ __forceinline__ float tiny() { return 0x1p-60f; }
-    static __device__ __forceinline__ float pow2(int k) { return ldexpf(1.0f, k); }
-    static __device__ __forceinline__ int expo(float x) { int e; frexpf(x, &e); return e; }
-};
-template <> struct GbgcScale<double> {
-    static __device__ __forceinline__ double tiny() { return 0x1p-500; }
-    static __device__ __forceinline__ double pow2(int k) { return ldexp(1.0, k); }
-    static __device__ __forceinline__ int expo(double x) { int e; frexp(x, &e); return e; }
-};
-
 // A node's partial at column g: a leaf's allowed bases, or an internal node's
 // stored partial and exponent.
 template <typename Real>
@@ -181,20 +149,6 @@ __device__ __forceinline__ void gbgc_load(const GbgcParams& p, int s, int g, Rea
 #pragma unroll
         for (int i = 0; i < 4; i++) L[i] = q[i];
         *e = p.scl[(size_t)s * p.GGp + g];
-    }
-}
-
-// m(j) = sum_i P[i][j] L(i): what a child sends its parent (log_multi,
-// bpp.hpp:414-431, in linear space)
-template <typename Real>
-__device__ __forceinline__ void gbgc_message(const Real* P, const Real* L, Real* m) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        Real v = P[j] * L[0];
-        v = fma(P[4 + j], L[1], v);
-        v = fma(P[8 + j], L[2], v);
-        v = fma(P[12 + j], L[3], v);
-        m[j] = v;
     }
 }
 

@@ -1,0 +1,898 @@
+// pacc_gbgc_chain.cu — the PhyloAcc-ST-GBGC chain on the GPU (sm_103a): one
+// CTA runs one element through the three models M0, M2, M1 (main.cpp:383-412),
+// taking elements from a queue until none are left.
+//
+// Per iteration the reference (src/PhyloAcc-ST-GBGC/SRC) does
+//   MonitorChain (bpp_c.cpp:598-699), the expected-count pass of Update_Tg
+//   (bpp_c.cpp:541-596), initial_prob_back (bpp_c2.cpp:354-457), three MH
+//   moves of sample_rates with integrate_ZB (bpp_c.cpp:881-976,1765-1799) and
+//   update_rates with Update_ZB, a pruning pass and ELBO (bpp_c.cpp:1079-1137,
+//   1667-1763, 477-540, 840-878).
+// The GPU keeps that sequence and its draw stream, and spreads each step over
+// the CTA:
+//   * branch matrices: for each class's rate matrix Q = getRate(Q0, s, b) the
+//     powers Q^1..Q^13 are formed once (16 threads a class), and each branch's
+//     exp(Q d) is the Padé [m/m] approximant of Higham (2005) with m and the
+//     scaling chosen from d ||Q||_1, evaluated from the shared powers, in FP64;
+//     one thread per (class, branch);
+//   * emissions: one thread per (node, class), sum(log P % posterior);
+//   * the Z-message pass over log_prob_back: tree levels in parallel, the
+//     children of a node added in postorder as the reference adds them;
+//   * Z/B sampling: tree depths in parallel, every node's uniform taken at its
+//     own position of the stream (one categorical draw per node, in reverse
+//     postorder);
+//   * pruning and expected counts: one column per lane with linear partials
+//     (FP32 or FP64) and exact power-of-two rescaling; counts reduced per warp
+//     in a fixed order.
+// Partials live in two buffers: the accepted one and the one update_rates
+// proposes into; the proposal becomes the accepted one when the move is
+// accepted.  Branch matrices of classes 1..5 live in three cache sets: the
+// accepted set, the set of the last accepted rate proposal and the set being
+// proposed into, so a rejected update_rates restores the caches
+// (bpp_c.cpp:318-337) by keeping the old index.
+// Eval2 and Output_init run on the host from the traces this kernel writes.
+#include "pacc_common.cuh"
+#include "pacc_gbgc.cuh"
+
+namespace pacc {
+
+// Padé [m/m] coefficients b_0..b_m of exp for m = 3, 5, 7, 9, 13, and the
+// bounds theta_m on ||A||_1 up to which each meets double precision (Higham 2005).
+__constant__ double kPadeB[5][14] = {
+    {120.0, 60.0, 12.0, 1.0},
+    {30240.0, 15120.0, 3360.0, 420.0, 30.0, 1.0},
+    {17297280.0, 8648640.0, 1995840.0, 277200.0, 25200.0, 1512.0, 56.0, 1.0},
+    {17643225600.0, 8821612800.0, 2075673600.0, 302702400.0, 30270240.0, 2162160.0, 110880.0, 3960.0, 90.0, 1.0},
+    {64764752532480000.0, 32382376266240000.0, 7771770303897600.0, 1187353796428800.0, 129060195264000.0,
+     10559470521600.0, 670442572800.0, 33522128640.0, 1323241920.0, 40840800.0, 960960.0, 16380.0, 182.0, 1.0}};
+__constant__ int kPadeM[5] = {3, 5, 7, 9, 13};
+__constant__ double kPadeTheta[5] = {1.495585217958292e-2, 2.539398330063230e-1, 9.504178996162932e-1,
+                                     2.097847961257068e0, 5.371920351148152e0};
+
+constexpr int GB_BT = 128;
+constexpr int GB_WARPS = GB_BT / 32;
+constexpr double LN2 = 0.6931471805599453;
+
+// exp(d Q) from Q's powers pw[k-1] = Q^k (k = 1..13) and ||Q||_1.
+__device__ __noinline__ void pade_branch(const double* __restrict__ pw, double qn, double d, double* E) {
+    const double a = qn * d;
+    int mi = 0;
+    while (mi < 4 && a > kPadeTheta[mi]) mi++;
+    int sq = 0;
+    if (a > kPadeTheta[4]) sq = (int)ceil(log2(a / kPadeTheta[4]));
+    const double sc = ldexp(d, -sq);
+    const int m = kPadeM[mi];
+    double U[16], V[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) { U[q] = 0; V[q] = 0; }
+    double c = 1;
+    for (int k = 1; k <= m; k++) {
+        c *= sc;
+        const double bk = kPadeB[mi][k] * c;
+        const double* Qk = pw + (k - 1) * 16;
+        if (k & 1) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) U[q] = fma(bk, Qk[q], U[q]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 16; q++) V[q] = fma(bk, Qk[q], V[q]);
+        }
+    }
+    const double b0 = kPadeB[mi][0];
+#pragma unroll
+    for (int q = 0; q < 16; q += 5) V[q] += b0;
+    // (V - U) E = (V + U): Gaussian elimination with partial pivoting, in place
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const double u = U[q], v = V[q];
+        U[q] = v - u;
+        V[q] = v + u;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        int pr = k;
+#pragma unroll
+        for (int i = k + 1; i < 4; i++)
+            if (fabs(U[i * 4 + k]) > fabs(U[pr * 4 + k])) pr = i;
+#pragma unroll
+        for (int i = k + 1; i < 4; i++)
+            if (i == pr)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    double t = U[k * 4 + j]; U[k * 4 + j] = U[i * 4 + j]; U[i * 4 + j] = t;
+                    t = V[k * 4 + j]; V[k * 4 + j] = V[i * 4 + j]; V[i * 4 + j] = t;
+                }
+#pragma unroll
+        for (int i = k + 1; i < 4; i++) {
+            const double l = U[i * 4 + k] / U[k * 4 + k];
+#pragma unroll
+            for (int j = k; j < 4; j++) U[i * 4 + j] -= l * U[k * 4 + j];
+#pragma unroll
+            for (int j = 0; j < 4; j++) V[i * 4 + j] -= l * V[k * 4 + j];
+        }
+    }
+#pragma unroll
+    for (int k = 3; k >= 0; k--)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            double s = V[k * 4 + j];
+#pragma unroll
+            for (int c2 = k + 1; c2 < 4; c2++) s -= U[k * 4 + c2] * E[c2 * 4 + j];
+            E[k * 4 + j] = s / U[k * 4 + k];
+        }
+    for (int r = 0; r < sq; r++) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            double row[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                double s = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) s = fma(E[i * 4 + k], E[k * 4 + j], s);
+                row[j] = s;
+            }
+            // rows below i are still read as E's old rows: keep them in V
+#pragma unroll
+            for (int j = 0; j < 4; j++) V[i * 4 + j] = row[j];
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q++) E[q] = V[q];
+    }
+}
+
+__device__ __forceinline__ double block_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Scalars of one CTA's chain.
+struct GbgcScalars {
+    double tm[2][3][3], lt[2][3][3];   // Z transition [outgroup path][child Z][parent Z] and its log
+    double ec_gc[2], ec_mis[2];        // emission constants: log(1 - c) / log(c); log(1 - cons2mis) / log(1 - ncons2mis)
+    double logpZC, logp_Z, MaxLoglik;
+    double tl, tl_next, full;          // trace_loglik[m], trace_loglik[m + 1], trace_full_loglik[m]
+    double r_n, r_c, r_gb;             // rates of iteration m
+    double x_n, x_c, x_gb;             // the rate proposal
+    double loglik_old, elbo_old, colsum;
+    double sel[5], bias[5];
+    uint64_t pos;
+    int cur, acc, prop, pbuf, post_cur, post_nxt;
+    int move_r, changed;
+};
+
+template <typename Real>
+struct GbgcCtx {
+    int S, N, GG, GGp, root, nn, n_int, n_hlev, n_dlev;
+    const int16_t *nodes, *c0, *c1, *par, *irank, *pidx, *hlev, *hnodes, *dlev, *dnodes;
+    const uint8_t* flags;
+    const double* dist;
+    const uint8_t* masks;
+    double *lP, *post, *wc, *emis, *emis_tmp, *lpb, *eraw, *colsum;
+    Real *pm, *part;
+    int32_t* scl;
+    Real* Pcur;
+    double *pw, *qn;
+    int8_t *Z, *B, *fixZ, *Zp, *Bp, *MZ, *MB;
+    __device__ bool missing(int s) const { return flags[s] & GBGC_MISSING; }
+    __device__ int upper(int s) const { return (flags[s] & GBGC_UPPER) ? 1 : 0; }
+    __device__ int slot(int cls, int set) const { return cls == 0 ? 0 : 1 + 5 * set + (cls - 1); }
+    __device__ double* lp(int sl, int s) const { return lP + ((size_t)sl * N + s) * 16; }
+    __device__ Real* pmat(int sl, int s) const { return pm + ((size_t)sl * N + s) * 16; }
+    __device__ Real* partial(int buf, int s, int g) const {
+        return part + (((size_t)buf * n_int + irank[s]) * GGp + g) * 4;
+    }
+    __device__ int32_t* expo(int buf, int s, int g) const { return scl + ((size_t)buf * n_int + irank[s]) * GGp + g; }
+};
+
+// Branch matrices of nc classes (cls[i], selection sel[i], bias bias[i]) into
+// cache set `set`; neutral classes are skipped on fixed branches.
+template <typename Real>
+__device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, int nc, const int* cls,
+                             const double* sel, const double* bias, int set) {
+    const int tid = threadIdx.x;
+    if (tid < nc) {
+        double* Q = G.pw + tid * 13 * 16;
+        gbgc_rate(p.Q0, sel[tid], bias[tid], Q);
+        double n1 = 0;
+        for (int j = 0; j < 4; j++) {
+            double c = 0;
+            for (int i = 0; i < 4; i++) c += fabs(Q[i * 4 + j]);
+            n1 = fmax(n1, c);
+        }
+        G.qn[tid] = n1;
+    }
+    __syncthreads();
+    for (int k = 2; k <= 13; k++) {
+        if (tid < nc * 16) {
+            const int ci = tid >> 4, e = tid & 15, r = e >> 2, c = e & 3;
+            double* Qm = G.pw + ci * 13 * 16;
+            const double* Qp = Qm + (k - 2) * 16;
+            double s = 0;
+            for (int l = 0; l < 4; l++) s = fma(Qp[r * 4 + l], Qm[l * 4 + c], s);
+            Qm[(k - 1) * 16 + e] = s;   // writes row k-1 only; rows read are k-2 and 0
+        }
+        __syncthreads();
+    }
+    const int nb = G.nn - 1;
+    for (int it = tid; it < nc * nb; it += blockDim.x) {
+        const int ci = it / nb, s = G.nodes[it - ci * nb];
+        if (G.missing(s) || (cls[ci] % 3 == 2 && G.fixZ[s] == 1)) continue;
+        double E[16];
+        pade_branch(G.pw + ci * 13 * 16, G.qn[ci], G.dist[s], E);
+        const int sl = G.slot(cls[ci], set);
+        double* lo = G.lp(sl, s);
+        Real* po = G.pmat(sl, s);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const double v = E[(q & 3) * 4 + (q >> 2)];   // (child q/4, parent q%4) = E[parent][child]
+            lo[q] = d_log(v);
+            po[q] = (Real)v;
+        }
+    }
+    __syncthreads();
+}
+
+// Emissions sum(log P % posterior) (+ the B and missing-data constants) of the
+// classes lo..5 from cache set `set` into out; with raw, the value of each
+// node's current class before the constants goes to eraw.
+template <typename Real>
+__device__ void emissions(const GbgcCtx<Real>& G, const GbgcScalars& sc, double* out, int lo, int set,
+                          const double* post, bool raw) {
+    const int nb = G.nn - 1, ncl = 6 - lo;
+    for (int it = threadIdx.x; it < nb * ncl; it += blockDim.x) {
+        const int s = G.nodes[it / ncl], j = lo + it % ncl;
+        if (G.missing(s) || (G.fixZ[s] == 1 && j % 3 == 2)) continue;
+        const double* a = G.lp(G.slot(j, set), s);
+        const double* b = post + (size_t)s * 16;
+        double t = 0;
+        for (int c = 0; c < 4; c++)
+            for (int r = 0; r < 4; r++) t += a[r * 4 + c] * b[r * 4 + c];
+        if (raw && j == G.Z[s] + 3 * G.B[s]) G.eraw[s] = t;
+        t += sc.ec_gc[j < 3 ? 0 : 1];
+        t += sc.ec_mis[j % 3 == 1 ? 0 : 1];
+        out[s * 6 + j] = t;
+    }
+    __syncthreads();
+}
+
+// The Z-message pass: lpb[p] += log_multi(log_TM_Int[c], lpb[c]) (- log 2)
+// for every non-root c, bottom-up.
+template <typename Real>
+__device__ void up_pass(const GbgcCtx<Real>& G, const GbgcScalars& sc, bool half) {
+    for (int h = 0; h < G.n_hlev; h++) {
+        const int a = G.hlev[h], b = G.hlev[h + 1];
+        for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
+            const int p = G.hnodes[it];
+            double acc[6];
+#pragma unroll
+            for (int r = 0; r < 6; r++) acc[r] = G.lpb[p * 6 + r];
+            const int ch[2] = {G.c0[p], G.c1[p]};
+            for (int q = 0; q < 2; q++) {
+                const int c = ch[q];
+                const double* y = G.lpb + c * 6;
+                double mx = y[0];
+#pragma unroll
+                for (int r = 1; r < 6; r++) mx = fmax(mx, y[r]);
+                double t[3];
+                if (mx == -CUDART_INF) {
+                    t[0] = t[1] = t[2] = -CUDART_INF;
+                } else {
+                    double ez[3];
+#pragma unroll
+                    for (int z = 0; z < 3; z++) ez[z] = d_exp(y[z] - mx) + d_exp(y[z + 3] - mx);
+                    const int u = G.upper(c);
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        double v = 0;
+#pragma unroll
+                        for (int z = 0; z < 3; z++) v += sc.tm[u][z][j] * ez[z];
+                        t[j] = d_log(v) + mx;
+                        if (half) t[j] -= LN2;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    acc[j] += t[j];
+                    acc[3 + j] += t[j];
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 6; r++) G.lpb[p * 6 + r] = acc[r];
+        }
+        __syncthreads();
+    }
+}
+
+// lpb = src on the branches, 0 at the root, then the message pass.
+template <typename Real>
+__device__ void prob_back(const GbgcCtx<Real>& G, const GbgcScalars& sc, const double* src) {
+    for (int i = threadIdx.x; i < G.nn * 6; i += blockDim.x) {
+        const int s = G.nodes[i / 6];
+        G.lpb[s * 6 + i % 6] = (s == G.root) ? 0.0 : src[s * 6 + i % 6];
+    }
+    __syncthreads();
+    up_pass(G, sc, false);
+}
+
+// The current class's matrices of every branch into shared memory.
+template <typename Real>
+__device__ void stage_pcur(const GbgcCtx<Real>& G, int set) {
+    for (int i = threadIdx.x; i < (G.nn - 1) * 16; i += blockDim.x) {
+        const int s = G.nodes[i >> 4];
+        const int k = G.Z[s] + 3 * G.B[s];
+        G.Pcur[s * 16 + (i & 15)] = (G.missing(s) || k < 0) ? Real(0) : G.pmat(G.slot(k, set), s)[i & 15];
+    }
+    __syncthreads();
+}
+
+template <typename Real>
+__device__ __forceinline__ void leaf_or_partial(const GbgcCtx<Real>& G, int buf, int s, int g, Real* L, int* e) {
+    if (s < G.S) {
+        const int msk = G.masks[(size_t)s * G.GGp + g];
+#pragma unroll
+        for (int i = 0; i < 4; i++) L[i] = ((msk >> i) & 1) ? Real(1) : Real(0);
+        *e = 0;
+    } else {
+        const Real* q = G.partial(buf, s, g);
+#pragma unroll
+        for (int i = 0; i < 4; i++) L[i] = q[i];
+        *e = *G.expo(buf, s, g);
+    }
+}
+
+// Update_Tg without sampling over every column into partial buffer buf;
+// returns (in sc.colsum) sum over columns of log(sum_j pi_j L_root(j)).
+template <typename Real>
+__device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScalars& sc, int buf) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double tot = 0;
+    for (int g0 = w * 32; g0 < G.GGp; g0 += GB_WARPS * 32) {
+        const int g = g0 + lane;
+        for (int k = 0; k < G.nn; k++) {
+            const int s = G.nodes[k];
+            if (s < G.S || G.missing(s)) continue;
+            Real a[4] = {1, 1, 1, 1};
+            int e = 0;
+            const int ch[2] = {G.c0[s], G.c1[s]};
+            for (int q = 0; q < 2; q++) {
+                const int c = ch[q];
+                if (G.missing(c)) continue;
+                Real L[4], m[4];
+                int ec;
+                leaf_or_partial(G, buf, c, g, L, &ec);
+                gbgc_message(G.Pcur + c * 16, L, m);
+#pragma unroll
+                for (int j = 0; j < 4; j++) a[j] *= m[j];
+                e += ec;
+            }
+            const Real mx = fmax(fmax(a[0], a[1]), fmax(a[2], a[3]));
+            if (mx > 0 && mx < GbgcScale<Real>::tiny()) {
+                const int sh = -GbgcScale<Real>::expo(mx);
+                const Real f1 = GbgcScale<Real>::pow2(sh / 2), f2 = GbgcScale<Real>::pow2(sh - sh / 2);
+#pragma unroll
+                for (int j = 0; j < 4; j++) a[j] = (a[j] * f1) * f2;
+                e -= sh;
+            }
+            Real* o = G.partial(buf, s, g);
+#pragma unroll
+            for (int j = 0; j < 4; j++) o[j] = a[j];
+            *G.expo(buf, s, g) = e;
+        }
+        if (g < G.GG) {
+            Real Lr[4];
+            int er;
+            leaf_or_partial(G, buf, G.root, g, Lr, &er);
+            double t = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) t += (double)Lr[j] * p.pi[j];
+            tot += t > 0 ? d_log(t) + (double)er * LN2 : -CUDART_INF;
+        }
+    }
+    tot = block_warp_sum(tot);
+    if (lane == 0) G.colsum[w] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int v = 0; v < GB_WARPS; v++) t += G.colsum[v];
+        sc.colsum = t;
+    }
+    __syncthreads();
+}
+
+// Update_Tg with sampling over every column from partial buffer buf (its
+// internal partials are replaced by marginals): expected counts into dst.
+template <typename Real>
+__device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf, double* dst) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double* wc = G.wc + (size_t)w * G.N * 16;
+    for (int i = lane; i < G.N * 16; i += 32) wc[i] = 0;
+    __syncwarp();
+    for (int g0 = w * 32; g0 < G.GGp; g0 += GB_WARPS * 32) {
+        const int g = g0 + lane;
+        const bool real_col = g < G.GG;
+        Real Lr[4];
+        int er;
+        leaf_or_partial(G, buf, G.root, g, Lr, &er);
+        double wr[4], tot = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) { wr[j] = (double)Lr[j] * p.pi[j]; tot += wr[j]; }
+        Real* qr = G.partial(buf, G.root, g);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const double q = (real_col && tot > 0) ? wr[j] / tot : 0.0;
+            const double sum = block_warp_sum(q);
+            if (lane == j * 4) wc[G.root * 16 + j * 4] += sum;
+            qr[j] = (Real)q;
+        }
+        for (int k = G.nn - 2; k >= 0; k--) {
+            const int s = G.nodes[k];
+            if (G.missing(s)) continue;
+            Real L[4], m[4];
+            int es;
+            leaf_or_partial(G, buf, s, g, L, &es);
+            const Real* P = G.Pcur + s * 16;
+            gbgc_message(P, L, m);
+            const Real* qp = G.partial(buf, G.par[s], g);
+            Real r[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) r[j] = m[j] > 0 ? qp[j] / m[j] : Real(0);
+            Real qs[4];
+            double mine = 0;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                Real acc = 0;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const Real jt = r[j] * P[i * 4 + j] * L[i];
+                    acc += jt;
+                    const double sum = block_warp_sum(real_col ? (double)jt : 0.0);
+                    if (lane == i * 4 + j) mine = sum;
+                }
+                qs[i] = acc;
+            }
+            if (lane < 16) wc[s * 16 + lane] += mine;
+            if (s >= G.S) {
+                Real* o = G.partial(buf, s, g);
+#pragma unroll
+                for (int i = 0; i < 4; i++) o[i] = qs[i];
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < G.N * 16; i += blockDim.x) {
+        double t = 0;
+        for (int v = 0; v < GB_WARPS; v++) t += G.wc[(size_t)v * G.N * 16 + i];
+        dst[i] = t;
+    }
+    __syncthreads();
+}
+
+// Update_ZB's sampling (bpp_c.cpp:1710-1761): depths top-down, the node at
+// reverse-postorder index k drawing the uniform at position pos0 + k.
+template <typename Real>
+__device__ void sample_zb(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScalars& sc) {
+    for (int d = 0; d < G.n_dlev; d++) {
+        const int a = G.dlev[d], b = G.dlev[d + 1];
+        for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
+            const int s = G.dnodes[it], pz = G.Z[G.par[s]];
+            StreamReader rd;
+            rd.init(p.seed, sc.pos + (uint64_t)(G.nn - 2 - G.pidx[s]));
+            const double u = rd.uniform();
+            const int old = G.Z[s];
+            const double* y = G.lpb + s * 6;
+            if (pz != 2) {
+                double x[6], wv[6];
+                const int up = G.upper(s);
+#pragma unroll
+                for (int r = 0; r < 6; r++) x[r] = sc.lt[up][r % 3][pz] + y[r];
+                double mx = x[0];
+#pragma unroll
+                for (int r = 1; r < 6; r++)
+                    if (x[r] > mx) mx = x[r];
+#pragma unroll
+                for (int r = 0; r < 6; r++) wv[r] = d_exp(x[r] - mx);
+                const int nn = categorical(6, wv, u);
+                G.Z[s] = (int8_t)(nn % 3);
+                if (!G.missing(s)) G.B[s] = nn > 2 ? 1 : 0;
+            } else {
+                G.Z[s] = 2;
+                const double mx = fmax(y[2], y[5]);
+                const double wv[2] = {d_exp(y[2] - mx), d_exp(y[5] - mx)};
+                const int nn = categorical(2, wv, u);
+                if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
+            }
+            if (old != G.Z[s]) sc.changed = 1;
+        }
+        __syncthreads();
+    }
+}
+
+// prior_Z (bpp_c2.cpp:484-498), reverse postorder
+template <typename Real>
+__device__ double prior_z(const GbgcCtx<Real>& G, const GbgcScalars& sc) {
+    double r = 0;
+    for (int k = G.nn - 2; k >= 0; k--) {
+        const int s = G.nodes[k];
+        r += sc.lt[G.upper(s)][G.Z[s]][G.Z[G.par[s]]];
+    }
+    return r;
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(GB_BT) gbgc_chain_kernel(GbgcChainParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ GbgcScalars sc;
+    __shared__ int s_elem;
+    const int tid = threadIdx.x;
+    StreamReader rng;   // thread 0's sequential reader
+    for (;;) {
+        if (tid == 0) s_elem = atomicAdd(p.next_elem, 1);
+        __syncthreads();
+        const int e = s_elem;
+        if (e >= p.n_elem) break;
+        const GbgcElemHdr H = p.hdr[e];
+        const uint8_t* eb = p.blob + H.blob_off;
+        GbgcCtx<Real> G;
+        G.S = H.S; G.N = H.N; G.GG = H.GG; G.GGp = H.GGp; G.root = H.root; G.nn = H.n_nodes; G.n_int = H.n_int;
+        G.n_hlev = H.n_hlev; G.n_dlev = H.n_dlev;
+        const int N = G.N;
+        // shared layout
+        size_t o = 0;
+        G.Pcur = (Real*)(smem + o);   o += (size_t)N * 16 * sizeof(Real);
+        G.pw = (double*)(smem + o);   o += 5 * 13 * 16 * 8;
+        G.qn = (double*)(smem + o);   o += 8 * 8;
+        int16_t* i16 = (int16_t*)(smem + o);
+        const int nh = H.n_hlev + 1, nd = H.n_dlev + 1, nhn = H.n_int, ndn = G.nn - 1;
+        o += ((size_t)6 * N + nh + nhn + nd + ndn) * 2;
+        o = (o + 15) & ~(size_t)15;
+        uint8_t* u8 = smem + o;
+        for (int i = tid; i < N; i += blockDim.x) {
+            i16[i] = i < G.nn ? ((const int16_t*)(eb + H.o_nodes))[i] : 0;
+            i16[N + i] = ((const int16_t*)(eb + H.o_c0))[i];
+            i16[2 * N + i] = ((const int16_t*)(eb + H.o_c1))[i];
+            i16[3 * N + i] = ((const int16_t*)(eb + H.o_par))[i];
+            i16[4 * N + i] = ((const int16_t*)(eb + H.o_irank))[i];
+            i16[5 * N + i] = ((const int16_t*)(eb + H.o_pidx))[i];
+            u8[i] = (eb + H.o_flags)[i] | (p.target[i] ? GBGC_TARGET : 0);
+        }
+        int16_t* lv = i16 + 6 * N;
+        for (int i = tid; i < nh; i += blockDim.x) lv[i] = ((const int16_t*)(eb + H.o_hlev))[i];
+        for (int i = tid; i < nhn; i += blockDim.x) lv[nh + i] = ((const int16_t*)(eb + H.o_hnodes))[i];
+        for (int i = tid; i < nd; i += blockDim.x) lv[nh + nhn + i] = ((const int16_t*)(eb + H.o_dlev))[i];
+        for (int i = tid; i < ndn; i += blockDim.x) lv[nh + nhn + nd + i] = ((const int16_t*)(eb + H.o_dnodes))[i];
+        G.nodes = i16; G.c0 = i16 + N; G.c1 = i16 + 2 * N; G.par = i16 + 3 * N; G.irank = i16 + 4 * N;
+        G.pidx = i16 + 5 * N;
+        G.hlev = lv; G.hnodes = lv + nh; G.dlev = lv + nh + nhn; G.dnodes = lv + nh + nhn + nd;
+        G.flags = u8;
+        G.Z = (int8_t*)u8 + N; G.B = G.Z + N; G.fixZ = G.B + N; G.Zp = G.fixZ + N; G.Bp = G.Zp + N;
+        G.MZ = G.Bp + N; G.MB = G.MZ + N;
+        G.dist = (const double*)(eb + H.o_dist);
+        G.masks = eb + H.o_masks;
+        const GbgcWs W = GbgcWs::make(p.N_max, p.n_int_max, p.GGp_max, GB_WARPS, sizeof(Real));
+        char* ws = p.ws + (size_t)blockIdx.x * p.ws_stride;
+        G.lP = (double*)(ws + W.lP); G.pm = (Real*)(ws + W.pm); G.post = (double*)(ws + W.post);
+        G.wc = (double*)(ws + W.wc); G.emis = (double*)(ws + W.emis); G.emis_tmp = (double*)(ws + W.emis_tmp);
+        G.lpb = (double*)(ws + W.lpb); G.eraw = (double*)(ws + W.eraw); G.colsum = (double*)(ws + W.colsum);
+        G.part = (Real*)(ws + W.part); G.scl = (int32_t*)(ws + W.scl);
+        if (tid == 0) {
+            for (int u = 0; u < 2; u++) {
+                double t[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                t[0][0] = 1 - p.grate;
+                t[1][0] = p.grate;
+                t[1][1] = 1 - p.lrate;
+                t[2][1] = p.lrate;
+                t[2][2] = 1;
+                if (u) { t[1][1] = 1; t[2][1] = 0; }
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) {
+                        sc.tm[u][a][b] = t[a][b];
+                        sc.lt[u][a][b] = d_log(t[a][b]);
+                    }
+            }
+            sc.ec_gc[0] = d_log(1 - p.gcc);
+            sc.ec_gc[1] = d_log(p.gcc);
+            sc.ec_mis[0] = d_log(1 - p.c2m);
+            sc.ec_mis[1] = d_log(1 - p.nc2m);
+            rng.init(p.seed, 0);
+        }
+        __syncthreads();
+        const int order[3] = {0, 2, 1};
+        for (int q = 0; q < 3; q++) {
+            const int resZ = order[q];
+            double* trd = p.tr_d + ((size_t)e * 3 + resZ) * 4 * p.T;
+            int8_t* trzb = p.tr_zb + ((size_t)e * 3 + resZ) * p.T * 2 * p.N_max;
+            // ---- initMCMC (bpp_c.cpp:120-257) ----
+            for (int s = tid; s < N; s += blockDim.x) {
+                G.B[s] = 0;
+                G.Z[s] = -1;
+                int f = -1;
+                if (G.upper(s)) f = 1;
+                if (resZ == 2 && s < G.S) f = (G.flags[s] & GBGC_TARGET) ? -1 : 1;
+                G.fixZ[s] = (int8_t)f;
+                G.MZ[s] = 0;
+                G.MB[s] = 0;
+            }
+            __syncthreads();
+            for (int k = tid; k < G.nn; k += blockDim.x) {
+                const int s = G.nodes[k];
+                G.Z[s] = 0;
+                int f = G.upper(s) ? 1 : -1;
+                if (resZ == 2 && s < G.S) f = (G.flags[s] & GBGC_TARGET) ? -1 : 1;
+                if (resZ == 0) f = 1;
+                if (s == G.root) f = 0;
+                G.fixZ[s] = (int8_t)f;
+            }
+            if (tid == 0) {
+                sc.MaxLoglik = -CUDART_INF;
+                sc.r_n = p.acce_rate;
+                sc.r_c = p.conserve_rate;
+                sc.r_gb = p.init_gc;
+                sc.cur = 0;
+                sc.pbuf = 0;
+                sc.post_cur = 0;
+                sc.post_nxt = 0;
+            }
+            __syncthreads();
+            {
+                const int cls[5] = {1, 2, 3, 4, 5};
+                const double sel[5] = {sc.r_c, sc.r_n, 0.0, sc.r_c, sc.r_n};
+                const double bias[5] = {0.0, 0.0, sc.r_gb, sc.r_gb, sc.r_gb};
+                const int c0[1] = {0};
+                const double z0[1] = {0.0};
+                build_caches(p, G, 1, c0, z0, z0, 0);
+                build_caches(p, G, 5, cls, sel, bias, 0);
+            }
+            const double lnc = d_log(p.nc2m), lc = d_log(p.c2m);
+            for (int i = tid; i < N * 6; i += blockDim.x) {
+                const int s = i / 6, j = i % 6;
+                double v = 0;
+                G.lpb[i] = 0;
+                if (G.fixZ[s] == 1 && j % 3 == 2) { v = -CUDART_INF; G.lpb[i] = -CUDART_INF; }
+                G.emis[i] = v;
+            }
+            __syncthreads();
+            for (int k = tid; k < G.nn - 1; k += blockDim.x) {
+                const int s = G.nodes[k];
+                if (G.missing(G.par[s]) || !G.missing(s)) continue;
+                for (int j = 0; j < 6; j++) {
+                    if (G.fixZ[s] == 1 && j % 3 == 2) continue;
+                    G.emis[s * 6 + j] = (j % 3 == 1) ? lc : lnc;
+                }
+            }
+            __syncthreads();
+            up_pass(G, sc, true);
+            if (tid == 0) sc.logpZC = G.lpb[G.root * 6];
+            __syncthreads();
+            // ---- Gibbs (bpp_c.cpp:259-349) ----
+            stage_pcur(G, sc.cur);
+            prune(p, G, sc, sc.pbuf);
+            if (tid == 0) {
+                sc.tl = sc.colsum;
+                sc.logp_Z = prior_z(G, sc) - sc.logpZC;
+                sc.move_r = 1;
+            }
+            __syncthreads();
+            for (int m = 0; m < p.T; m++) {
+                // MonitorChain
+                if (tid == 0) {
+                    if (m > 0) {
+                        if (sc.move_r) sc.tl = sc.tl_next;
+                    }
+                    if (sc.move_r) {
+                        double f = sc.tl + sc.logp_Z;
+                        f += log_gamma_pdf(-sc.r_c, p.ca, p.cb);
+                        if (resZ != 0) f += log_gamma_pdf(sc.r_n + p.nshift, p.na, p.nb);
+                        int gb = 0, ungb = 0, mz[4] = {0, 0, 0, 0};
+                        for (int k = 0; k < G.nn - 1; k++) {
+                            const int s = G.nodes[k];
+                            if (G.missing(G.par[s])) continue;
+                            mz[2 * (G.missing(s) ? 1 : 0) + (G.Z[s] == 1 ? 1 : 0)] += 1;
+                            if (G.missing(s)) continue;
+                            if (G.B[s]) gb++; else ungb++;
+                        }
+                        f += d_log(1 - p.nc2m) * mz[0] + d_log(1 - p.c2m) * mz[1] + d_log(p.nc2m) * mz[2] +
+                             d_log(p.c2m) * mz[3];
+                        f += d_log(1 - p.gcc) * ungb + log_gamma_pdf(sc.r_gb, p.gca, p.gcb) + d_log(p.gcc) * gb;
+                        sc.full = f;
+                    }
+                    trd[0 * p.T + m] = sc.full;
+                    trd[1 * p.T + m] = sc.r_n;
+                    trd[2 * p.T + m] = sc.r_c;
+                    trd[3 * p.T + m] = sc.r_gb;
+                    sc.changed = (m >= p.burn && sc.full > sc.MaxLoglik) ? 1 : 0;
+                    if (sc.changed) sc.MaxLoglik = sc.full;
+                }
+                __syncthreads();
+                for (int s = tid; s < N; s += blockDim.x) {
+                    trzb[((size_t)m * 2) * p.N_max + s] = G.Z[s];
+                    trzb[((size_t)m * 2 + 1) * p.N_max + s] = G.B[s];
+                    if (sc.changed) { G.MZ[s] = G.Z[s]; G.MB[s] = G.B[s]; }
+                }
+                if (m == p.T - 1) break;
+                __syncthreads();
+                // expected counts of the accepted partials
+                if (sc.move_r) {
+                    const int nx = 1 - sc.post_cur;
+                    counts(p, G, sc.pbuf, G.post + (size_t)nx * N * 16);
+                    if (tid == 0) sc.post_nxt = nx;
+                    __syncthreads();
+                }
+                if (m == 0) {
+                    if (tid == 0) sc.post_cur = sc.post_nxt;
+                    __syncthreads();
+                }
+                const double* post = G.post + (size_t)sc.post_cur * N * 16;
+                // initial_prob_back
+                emissions(G, sc, G.emis, 0, sc.cur, post, true);
+                if (tid == 0) {
+                    double el = 0;
+                    for (int k = 0; k < G.nn - 1; k++) {
+                        const int s = G.nodes[k];
+                        if (!G.missing(s)) el += G.eraw[s];
+                    }
+                    sc.elbo_old = el;
+                }
+                prob_back(G, sc, G.emis);
+                if (tid == 0) {
+                    sc.loglik_old = G.lpb[G.root * 6];
+                    sc.acc = sc.cur;
+                }
+                for (int i = tid; i < N * 6; i += blockDim.x) G.emis_tmp[i] = G.emis[i];
+                __syncthreads();
+                // sample_rates: three MH moves of (gB, n, c) with Z and B integrated out
+                if (tid == 0) { sc.x_gb = sc.r_gb; sc.x_n = sc.r_n; sc.x_c = sc.r_c; }
+                for (int mm = 0; mm < 3; mm++) {
+                    __shared__ double cur3[3];
+                    if (tid == 0) {
+                        // cur3: the chain's values (the last accepted proposal); x_*: the new proposal
+                        cur3[0] = sc.x_gb; cur3[1] = sc.x_n; cur3[2] = sc.x_c;
+                        double u = __dmul_rn(__dmul_rn(__dsub_rn(rng.uniform(), 0.5), p.prop_gc), 2.0);
+                        double ngb = __dadd_rn(cur3[0], u);
+                        if (ngb < 0.01) ngb = cur3[0];
+                        double nn_ = cur3[1];
+                        if (resZ != 0) {
+                            const double inv = __ddiv_rn(1.0, p.prop_n);
+                            u = __dadd_rn(__dmul_rn(rng.uniform(), __dsub_rn(p.prop_n, inv)), inv);
+                            nn_ = __dsub_rn(__dmul_rn(__dadd_rn(cur3[1], p.nshift), u), p.nshift);
+                        }
+                        const double invc = __ddiv_rn(1.0, p.prop_c);
+                        u = __dadd_rn(__dmul_rn(rng.uniform(), __dsub_rn(p.prop_c, invc)), invc);
+                        const double nc_ = __dmul_rn(cur3[2], u);
+                        sc.sel[0] = nc_; sc.sel[1] = nn_; sc.sel[2] = 0.0; sc.sel[3] = nc_; sc.sel[4] = nn_;
+                        sc.bias[0] = 0.0; sc.bias[1] = 0.0; sc.bias[2] = ngb; sc.bias[3] = ngb; sc.bias[4] = ngb;
+                        int pr = 0;
+                        while (pr == sc.cur || pr == sc.acc) pr++;
+                        sc.prop = pr;
+                    }
+                    __syncthreads();
+                    {
+                        const int cls[5] = {1, 2, 3, 4, 5};
+                        build_caches(p, G, 5, cls, sc.sel, sc.bias, sc.prop);
+                    }
+                    emissions(G, sc, G.emis_tmp, 1, sc.prop, post, false);
+                    prob_back(G, sc, G.emis_tmp);
+                    if (tid == 0) {
+                        const double lr = G.lpb[G.root * 6];
+                        const double ngb = sc.bias[2], nn_ = sc.sel[1], nc_ = sc.sel[0];
+                        double MH = __dsub_rn(__dadd_rn(__dsub_rn(lr, sc.loglik_old), log_gamma_pdf(ngb, p.gca, p.gcb)),
+                                              log_gamma_pdf(cur3[0], p.gca, p.gcb));
+                        if (resZ != 0)
+                            MH = __dadd_rn(MH, __dsub_rn(log_gamma_pdf(__dadd_rn(nn_, p.nshift), p.na, p.nb),
+                                                         log_gamma_pdf(__dadd_rn(cur3[1], p.nshift), p.na, p.nb)));
+                        MH = __dadd_rn(MH, __dadd_rn(__dsub_rn(__dsub_rn(log_gamma_pdf(-nc_, p.ca, p.cb),
+                                                                         log_gamma_pdf(-cur3[2], p.ca, p.cb)),
+                                                               d_log(-nc_)),
+                                                     d_log(-cur3[2])));
+                        const bool acc = d_log(rng.uniform()) < MH;
+                        sc.changed = acc ? 1 : 0;
+                        if (acc) {
+                            sc.x_gb = ngb; sc.x_n = nn_; sc.x_c = nc_;
+                            sc.loglik_old = lr;
+                            sc.acc = sc.prop;
+                        }
+                    }
+                    __syncthreads();
+                    const bool accepted = sc.changed;
+                    for (int i = tid; i < (G.nn - 1) * 5; i += blockDim.x) {
+                        const int s = G.nodes[i / 5], j = 1 + i % 5;
+                        if (G.missing(s) || (G.fixZ[s] == 1 && j % 3 == 2)) continue;
+                        if (accepted) G.emis[s * 6 + j] = G.emis_tmp[s * 6 + j];
+                        else G.emis_tmp[s * 6 + j] = G.emis[s * 6 + j];
+                    }
+                    __syncthreads();
+                }
+                // update_rates: Update_ZB, a pruning pass, ELBO, one MH step
+                for (int s = tid; s < N; s += blockDim.x) { G.Zp[s] = G.Z[s]; G.Bp[s] = G.B[s]; }
+                if (tid == 0) sc.changed = 0;
+                prob_back(G, sc, G.emis);
+                if (tid == 0) sc.pos = rng.pos;
+                __syncthreads();
+                sample_zb(p, G, sc);
+                stage_pcur(G, sc.acc);
+                prune(p, G, sc, 1 - sc.pbuf);
+                for (int k = tid; k < G.nn - 1; k += blockDim.x) {
+                    const int s = G.nodes[k];
+                    if (G.missing(s)) continue;
+                    const double* a2 = G.lp(G.slot(G.Z[s] + 3 * G.B[s], sc.acc), s);
+                    const double* b2 = post + (size_t)s * 16;
+                    double t = 0;
+                    for (int c = 0; c < 4; c++)
+                        for (int r = 0; r < 4; r++) t += a2[r * 4 + c] * b2[r * 4 + c];
+                    G.eraw[s] = t;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    rng.pos += (uint64_t)(G.nn - 1);
+                    double elbo_new = 0;
+                    for (int k = 0; k < G.nn - 1; k++) {
+                        const int s = G.nodes[k];
+                        if (!G.missing(s)) elbo_new += G.eraw[s];
+                    }
+                    const double MH = __dsub_rn(__dadd_rn(__dsub_rn(sc.colsum, sc.tl), sc.elbo_old), elbo_new);
+                    if (d_log(rng.uniform()) < MH) {
+                        sc.tl_next = sc.colsum;
+                        if (sc.changed) sc.logp_Z = prior_z(G, sc) - sc.logpZC;
+                        sc.cur = sc.acc;
+                        sc.pbuf = 1 - sc.pbuf;
+                        sc.r_gb = sc.x_gb; sc.r_n = sc.x_n; sc.r_c = sc.x_c;
+                        sc.move_r = 1;
+                    } else {
+                        sc.move_r = 0;
+                    }
+                    sc.post_cur = sc.post_nxt;
+                }
+                __syncthreads();
+                if (!sc.move_r)
+                    for (int s = tid; s < N; s += blockDim.x) { G.Z[s] = G.Zp[s]; G.B[s] = G.Bp[s]; }
+                __syncthreads();
+            }
+            __syncthreads();
+            if (tid == 0) p.max_ll[(size_t)e * 3 + resZ] = sc.MaxLoglik;
+            for (int s = tid; s < N; s += blockDim.x) {
+                p.max_zb[(((size_t)e * 3 + resZ) * 2) * p.N_max + s] = G.MZ[s];
+                p.max_zb[(((size_t)e * 3 + resZ) * 2 + 1) * p.N_max + s] = G.MB[s];
+            }
+            __syncthreads();
+        }
+        if (tid == 0) p.status[e] = 0;
+        __syncthreads();
+    }
+}
+
+// Dynamic shared memory of the chain kernel for N nodes.
+size_t gbgc_chain_smem(int N, int prec) {
+    const size_t rb = prec ? 4 : 8;
+    size_t o = (size_t)N * 16 * rb + 5 * 13 * 16 * 8 + 8 * 8;
+    o += ((size_t)6 * N + 4 * (size_t)N + 4) * 2;
+    o = (o + 15) & ~(size_t)15;
+    o += (size_t)8 * N;
+    return o;
+}
+
+int gbgc_chain_threads() { return GB_BT; }
+int gbgc_chain_warps() { return GB_WARPS; }
+
+int gbgc_chain_occupancy(int prec, size_t smem) {
+    int n = 0;
+    cudaError_t e = prec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<float>, GB_BT, smem)
+                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<double>, GB_BT, smem);
+    return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, cudaStream_t st) {
+    cudaError_t e;
+    if (prec) {
+        e = cudaFuncSetAttribute(gbgc_chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        gbgc_chain_kernel<float><<<grid, GB_BT, smem, st>>>(p);
+    } else {
+        e = cudaFuncSetAttribute(gbgc_chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        gbgc_chain_kernel<double><<<grid, GB_BT, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace pacc

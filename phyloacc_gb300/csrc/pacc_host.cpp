@@ -53,6 +53,11 @@ int batch_occupancy(int prec, int C, int warps, size_t smem);
 cudaError_t launch_init_slots(void* slots, const int32_t* elem, int n, cudaStream_t st);
 cudaError_t launch_batch(const void* params, int grid, int warps, size_t smem, int prec, int C, cudaStream_t st);
 cudaError_t launch_gbgc(const GbgcParams& p, int prec, cudaStream_t st);
+size_t gbgc_chain_smem(int N, int prec);
+int gbgc_chain_threads();
+int gbgc_chain_warps();
+int gbgc_chain_occupancy(int prec, size_t smem);
+cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // model (BPP, bpp.hpp:173-404)
@@ -273,6 +278,225 @@ static void gbgc_prepare(const HostModel& M, const uint8_t* bases, int GG, char 
     // the outgroup path has no accelerated class (fixZ, bpp_c.cpp:144-150)
     E.fixed.assign(N, 0);
     for (int s : E.nodes) if (M.upper[s] && s != E.root) E.fixed[s] = 1;
+}
+
+
+// ---------------------------------------------------------------------------
+// The gBGC chain (PhyloAcc-ST-GBGC): element blobs for the chain kernel, and
+// Eval2 / Output_init on the host from the traces the kernel writes.
+// ---------------------------------------------------------------------------
+
+// Element blob of the chain kernel: the collapsed tree, its levels and the
+// leaf columns (GbgcElemHdr gives the offsets).
+static void gbgc_blob(const HostModel& M, const GbgcElem& E, GbgcElemHdr& H, std::vector<uint8_t>& out) {
+    const int S = M.S, N = M.N;
+    const int nn = (int)E.nodes.size();
+    std::vector<int> height(N, 0), depth(N, 0), pidx(N, -1);
+    for (int k = 0; k < nn; k++) pidx[E.nodes[k]] = k;
+    int H_max = 0;
+    for (int s : E.nodes)
+        if (s >= S) {
+            height[s] = 1 + std::max(height[E.c2a[s]], height[E.c2b[s]]);
+            H_max = std::max(H_max, height[s]);
+        }
+    int D_max = 0;
+    for (int k = nn - 1; k >= 0; k--) {
+        const int s = E.nodes[k];
+        depth[s] = (s == E.root) ? 0 : depth[E.par[s]] + 1;
+        D_max = std::max(D_max, depth[s]);
+    }
+    std::vector<int16_t> hstart, hnodes, dstart, dnodes;
+    for (int h = 1; h <= H_max; h++) {
+        hstart.push_back((int16_t)hnodes.size());
+        for (int s : E.nodes)
+            if (s >= S && height[s] == h) hnodes.push_back((int16_t)s);
+    }
+    hstart.push_back((int16_t)hnodes.size());
+    for (int d = 1; d <= D_max; d++) {
+        dstart.push_back((int16_t)dnodes.size());
+        for (int k = nn - 1; k >= 0; k--)
+            if (E.nodes[k] != E.root && depth[E.nodes[k]] == d) dnodes.push_back((int16_t)E.nodes[k]);
+    }
+    dstart.push_back((int16_t)dnodes.size());
+    out.clear();
+    auto put = [&](const void* src, size_t bytes, size_t align) -> int32_t {
+        while (out.size() % align) out.push_back(0);
+        const int32_t o = (int32_t)out.size();
+        out.insert(out.end(), (const uint8_t*)src, (const uint8_t*)src + bytes);
+        return o;
+    };
+    std::vector<int16_t> nodes(N, 0), c0(N), c1(N), par(N), irank(N), pi16(N);
+    std::vector<uint8_t> flags(N);
+    for (int k = 0; k < nn; k++) nodes[k] = (int16_t)E.nodes[k];
+    for (int s = 0; s < N; s++) {
+        c0[s] = (int16_t)E.c2a[s];
+        c1[s] = (int16_t)E.c2b[s];
+        par[s] = (int16_t)std::min(E.par[s], N);
+        irank[s] = (int16_t)(s >= S ? s - S : -1);
+        pi16[s] = (int16_t)pidx[s];
+        flags[s] = (uint8_t)((E.missing[s] ? GBGC_MISSING : 0) | (M.upper[s] ? GBGC_UPPER : 0));
+    }
+    H.S = S; H.N = N; H.GG = E.GG; H.GGp = E.GGp; H.root = E.root; H.n_nodes = nn; H.n_int = S - 1;
+    H.n_hlev = H_max; H.n_dlev = D_max;
+    H.o_nodes = put(nodes.data(), 2 * N, 16);
+    H.o_c0 = put(c0.data(), 2 * N, 2);
+    H.o_c1 = put(c1.data(), 2 * N, 2);
+    H.o_par = put(par.data(), 2 * N, 2);
+    H.o_irank = put(irank.data(), 2 * N, 2);
+    H.o_pidx = put(pi16.data(), 2 * N, 2);
+    H.o_flags = put(flags.data(), N, 1);
+    H.o_dist = put(E.d2.data(), 8 * (size_t)N, 8);
+    H.o_hlev = put(hstart.data(), 2 * hstart.size(), 2);
+    hnodes.resize((size_t)std::max(S - 1, (int)hnodes.size()), 0);   // the kernel copies S - 1 entries
+    H.o_hnodes = put(hnodes.data(), 2 * hnodes.size(), 2);
+    H.o_dlev = put(dstart.data(), 2 * dstart.size(), 2);
+    H.o_dnodes = put(dnodes.data(), 2 * dnodes.size(), 2);
+    H.o_masks = put(E.masks.data(), E.masks.size(), 16);
+    while (out.size() % 16) out.push_back(0);
+    H.pad = 0;
+    H.blob_off = 0;
+}
+
+// Eval2 (bpp_c2.cpp:29-286) of one model from its trace: the marginal
+// log-likelihood.  trd: [4][T] full loglik, n, c, gBC; tz / tb: Z and B of
+// sample i at tz[i * stride + s] / tb[i * stride + s].
+static double gbgc_eval2(int resZ, int T, int burn, int mcmc, int N, const std::vector<int>& nodes,
+                         const std::vector<char>& missing, const double* trd, const int8_t* tz, const int8_t* tb,
+                         size_t stride, const int8_t* maxz, double max_loglik) {
+    const double* tr_full = trd;
+    const double* tr_n = trd + T;
+    const double* tr_c = trd + 2 * T;
+    const double* tr_gb = trd + 3 * T;
+    std::vector<int> uncertain;
+    for (int s = 0; s < N; s++) {
+        int c = 0;
+        for (int i = burn; i < T; i++)
+            if (tz[(size_t)i * stride + s] == maxz[s]) c++;
+        if (c < mcmc) uncertain.push_back(s);
+    }
+    const int d = 2 + (resZ != 0 ? 1 : 0);
+    auto zkey = [&](const int8_t* z) {
+        std::string k(uncertain.size(), '\0');
+        for (size_t u = 0; u < uncertain.size(); u++) k[u] = (char)z[uncertain[u]];
+        return k;
+    };
+    std::unordered_map<std::string, int> cfg;
+    cfg.emplace(zkey(maxz), 0);
+    std::vector<int> nZ(1, 0);
+    std::vector<std::unordered_map<std::string, int>> zbIndex(1);
+    std::vector<std::vector<int>> nZB(1);
+    std::vector<std::vector<double>> means(1, std::vector<double>(d, 0.0)), var(1, std::vector<double>(d * d, 0.0));
+    std::vector<double> sumf(1, 0.0);
+    std::string bkey;
+    for (int i = T - 1; i >= burn; i--) {
+        const int8_t* z = tz + (size_t)i * stride;
+        const int8_t* b = tb + (size_t)i * stride;
+        auto ins = cfg.emplace(zkey(z), (int)nZ.size());
+        const int j = ins.first->second;
+        if (ins.second) {
+            nZ.push_back(0);
+            zbIndex.emplace_back();
+            nZB.emplace_back();
+            means.emplace_back(d, 0.0);
+            var.emplace_back(d * d, 0.0);
+            sumf.push_back(0.0);
+        }
+        nZ[j]++;
+        // getShifts (bpp_c2.cpp:14-27): the element's branches with B = 1
+        bkey.assign((size_t)N, '\0');
+        for (int s : nodes)
+            if (!missing[s] && b[s]) bkey[s] = 1;
+        auto kb = zbIndex[j].emplace(bkey, (int)nZB[j].size());
+        if (kb.second) nZB[j].push_back(0);
+        nZB[j][kb.first->second]++;
+        auto V = [&](int r, int c) -> double& { return var[j][c * d + r]; };
+        V(1, 1) += tr_c[i] * tr_c[i];
+        means[j][1] += tr_c[i];
+        V(0, 0) += tr_gb[i] * tr_gb[i];
+        means[j][0] += tr_gb[i];
+        V(0, 1) += tr_c[i] * tr_gb[i];
+        if (resZ != 0) {
+            V(2, 2) += tr_n[i] * tr_n[i];
+            means[j][2] += tr_n[i];
+            V(1, 2) += tr_c[i] * tr_n[i];
+            V(0, 2) += tr_gb[i] * tr_n[i];
+        }
+        sumf[j] += tr_full[i];
+    }
+    auto cov = [&](const std::vector<double>& v, const std::vector<double>& mu, double n) {
+        std::vector<double> t(d * d);
+        for (int c = 0; c < d; c++)
+            for (int r = 0; r < d; r++) t[c * d + r] = (r > c) ? v[r * d + c] : v[c * d + r];   // symmatu
+        for (int c = 0; c < d; c++)
+            for (int r = 0; r < d; r++) t[c * d + r] -= mu[r] * mu[c] / n;
+        for (int q = 0; q < d * d; q++) t[q] /= (n - 1);
+        return t;
+    };
+    auto log_det = [&](std::vector<double> u, double& val, double& sign) {   // LU, partial pivoting
+        sign = 1.0;
+        val = 0.0;
+        for (int k = 0; k < d; k++) {
+            int pv = k;
+            for (int i = k + 1; i < d; i++)
+                if (std::fabs(u[k * d + i]) > std::fabs(u[k * d + pv])) pv = i;
+            if (pv != k) {
+                for (int j = 0; j < d; j++) std::swap(u[j * d + k], u[j * d + pv]);
+                sign = -sign;
+            }
+            const double piv = u[k * d + k];
+            if (piv == 0) { val = -INFINITY; sign = 0; return; }
+            if (piv < 0) sign = -sign;
+            val += std::log(std::fabs(piv));
+            for (int i = k + 1; i < d; i++) {
+                const double f = u[k * d + i] / piv;
+                for (int j = k; j < d; j++) u[j * d + i] -= f * u[j * d + k];
+            }
+        }
+    };
+    auto logdiag = [&](const std::vector<double>& t) {
+        double r = 0;
+        for (int q = 0; q < d; q++) r += std::log(t[q * d + q]);
+        return r;
+    };
+    double VB = 0, logdet = 0, sign = 1;
+    int eff = 0;
+    for (size_t i = 0; i < nZ.size(); i++) {
+        const double w = (double)nZ[i] / mcmc;
+        if (w < 0.05) continue;
+        const std::vector<double> tv = cov(var[i], means[i], (double)nZ[i]);
+        if (nZ[i] > 10) log_det(tv, logdet, sign);
+        if (nZ[i] <= 10 || sign < 0) logdet = logdiag(tv);
+        if (logdet == -INFINITY) continue;
+        eff += nZ[i];
+        double tB = 0;
+        for (int c : nZB[i]) tB += (double)c * std::log((double)c);
+        VB -= tB;
+        VB += (double)(nZ[i] - 1) / 2 * d;
+        VB += sumf[i];
+        VB += 0.5 * logdet * nZ[i];
+    }
+    if (eff == 0) {
+        std::vector<double> mean0(d, 0.0), var0(d * d, 0.0);
+        VB = 0;
+        double tB = 0;
+        for (size_t i = 0; i < nZ.size(); i++) {
+            for (int q = 0; q < d; q++) mean0[q] += means[i][q];
+            for (int q = 0; q < d * d; q++) var0[q] += var[i][q];
+            VB += sumf[i];
+            for (int c : nZB[i]) tB += (double)c * std::log((double)c);
+        }
+        VB -= tB;
+        const std::vector<double> tv = cov(var0, mean0, (double)mcmc);
+        log_det(tv, logdet, sign);
+        if (sign < 0) logdet = logdiag(tv);
+        if (logdet != -INFINITY) {
+            VB += 0.5 * logdet * mcmc;
+            VB += (double)(mcmc - 1) / 2 * d;
+            eff = mcmc;
+        }
+    }
+    if (resZ == 1 && eff == 0) return max_loglik;
+    return VB / eff + std::log((double)eff) + (double)d / 2 * std::log(2 * M_PI);
 }
 
 // Per-element preprocessing (BPP_C ctor, bpp_c.hpp:143-476).  Returns false
@@ -2504,6 +2728,215 @@ int pacc_get_launch_shape(pacc_ctx* c, int32_t* block_threads, int32_t* register
     if (chains_per_sm) *chains_per_sm = cta ? c->shape_per_sm : 0;
     if (trial_ms) *trial_ms = cta ? c->shape_trial_ms : 0;
     return PACC_OK;
+}
+
+
+void pacc_gbgc_default_opts(pacc_gbgc_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->burnin = 200; o->mcmc = 800; o->seed = 7728; o->gapchar = '*';
+    o->conserve_rate = -2.0; o->acce_rate = 0.0; o->init_gc = 3.0;
+    o->conserve_prior_a = 5.0; o->conserve_prior_b = 0.4;
+    o->acce_prior_a = 5.0; o->acce_prior_b = 0.4; o->acce_prior_shift = 2.0;
+    o->gc_prior_a = 4.0; o->gc_prior_b = 0.8; o->gc_prior_c = 0.2;
+    o->prep_lrate = 0.1; o->prep_grate = 0.8;
+    o->cons_to_mis = 0.01; o->ncons_to_mis = 0.1;
+    o->missing_thres = 0.8; o->conserve_prop = 0.8;
+    o->prop_c = 1.2; o->prop_n = 1.2; o->prop_gc = 0.2;
+}
+
+int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batch* b, pacc_gbgc_result* out) {
+    if (!c) return PACC_EINVAL;
+    if (!go || !b || !out || b->n_elements < 0 || (b->n_elements > 0 && (!b->lengths || !b->offsets || !b->bases))) {
+        c->err = "gbgc_run: options, batch and results must be non-null";
+        return PACC_EINVAL;
+    }
+    if (go->burnin < 0 || go->mcmc < 2 || go->burnin + go->mcmc < 2 || go->prop_c <= 1 || go->prop_n <= 1 ||
+        go->prop_gc <= 0) {
+        c->err = "gbgc_run: burnin >= 0, mcmc >= 2, prop_c and prop_n > 1, prop_gc > 0";
+        return PACC_EINVAL;
+    }
+    if (!c->gpu_ok) { c->err = "gbgc_run: no usable GPU"; return PACC_ECUDA; }
+    const HostModel& M = c->M;
+    const int S = M.S, N = M.N, n = b->n_elements;
+    const int T = go->burnin + go->mcmc;
+    std::vector<uint8_t> target(N, 0);
+    for (int i = 0; i < go->n_target; i++)
+        if (go->target && go->target[i] >= 0 && go->target[i] < N) target[go->target[i]] = 1;
+    // host preprocessing, in parallel over elements
+    std::vector<GbgcElem> E(n);
+    std::vector<GbgcElemHdr> hdr(n);
+    std::vector<std::vector<uint8_t>> blobs(n);
+    {
+        const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+        std::atomic<int> next(0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; t++)
+            th.emplace_back([&]() {
+                for (int i = next++; i < n; i = next++) {
+                    gbgc_prepare(M, b->bases + b->offsets[i], b->lengths[i], (char)go->gapchar, go->missing_thres,
+                                 go->conserve_prop, E[i]);
+                    if (!E[i].filtered) {
+                        int nint = 0;
+                        for (int s : E[i].nodes) nint += s >= S;
+                        if (nint == 0) E[i].filtered = 2;
+                    }
+                    if (!E[i].filtered) gbgc_blob(M, E[i], hdr[i], blobs[i]);
+                }
+            });
+        for (auto& t : th) t.join();
+    }
+    std::vector<int> run;   // elements that reach the device
+    for (int i = 0; i < n; i++) {
+        pacc_gbgc_result& r = out[i];
+        r.element_no = b->element_no ? b->element_no[i] : i;
+        r.status = E[i].filtered ? PACC_FILTERED : PACC_OK;
+        r.root = E[i].filtered ? -1 : E[i].root;
+        if (!E[i].filtered) run.push_back(i);
+    }
+    if (run.empty()) return PACC_OK;
+    if (!cuda_ok(c, cudaSetDevice(c->device), "gbgc_run: cudaSetDevice")) return PACC_ECUDA;
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
+    int GGp_max = 32;
+    for (int i : run) GGp_max = std::max(GGp_max, E[i].GGp);
+    const size_t smem = gbgc_chain_smem(N, prec);
+    const int per_sm = gbgc_chain_occupancy(prec, smem);
+    if (per_sm <= 0) { c->err = "gbgc_run: the chain kernel does not fit on an SM"; return PACC_ECUDA; }
+    const GbgcWs W = GbgcWs::make(N, S - 1, GGp_max, gbgc_chain_warps(), prec ? 4 : 8);
+    const size_t tzb_el = (size_t)3 * T * 2 * N;
+    // elements per launch: bounded by the trace and workspace budget
+    const size_t budget = (size_t)16 << 30;
+    const int grid_full = c->n_sm * per_sm;
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>(run.size(), budget / (tzb_el + 256)));
+    const int grid = std::max(1, std::min(grid_full, chunk));
+    // device buffers
+    size_t blob_total = 0;
+    for (int i : run) blob_total += blobs[i].size();
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_hdr = 0, o_blob = up(sizeof(GbgcElemHdr) * run.size());
+    const size_t o_tgt = up(o_blob + blob_total), o_ctr = up(o_tgt + N);
+    const size_t o_ws = up(o_ctr + 256);
+    const size_t o_trd = up(o_ws + W.total * (size_t)grid);
+    const size_t o_tzb = up(o_trd + (size_t)chunk * 3 * 4 * T * 8);
+    const size_t o_mzb = up(o_tzb + (size_t)chunk * tzb_el);
+    const size_t o_mll = up(o_mzb + (size_t)chunk * 3 * 2 * N);
+    const size_t o_st = up(o_mll + (size_t)chunk * 3 * 8);
+    const size_t total = up(o_st + (size_t)chunk * 4);
+    char* dev = nullptr;
+    if (!cuda_ok(c, cudaMalloc((void**)&dev, total), "gbgc_run: cudaMalloc")) return PACC_OOM;
+    cudaStream_t st = c->stream;
+    std::vector<uint8_t> hblob(blob_total);
+    std::vector<GbgcElemHdr> hh(run.size());
+    {
+        size_t off = 0;
+        for (size_t k = 0; k < run.size(); k++) {
+            hh[k] = hdr[run[k]];
+            hh[k].blob_off = (int64_t)off;
+            std::memcpy(hblob.data() + off, blobs[run[k]].data(), blobs[run[k]].size());
+            off += blobs[run[k]].size();
+        }
+    }
+    GbgcChainParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.T = T; p.burn = go->burnin; p.mcmc = go->mcmc; p.seed = go->seed;
+    p.conserve_rate = go->conserve_rate; p.acce_rate = go->acce_rate; p.init_gc = go->init_gc;
+    p.ca = go->conserve_prior_a; p.cb = go->conserve_prior_b;
+    p.na = go->acce_prior_a; p.nb = go->acce_prior_b; p.nshift = go->acce_prior_shift;
+    p.gca = go->gc_prior_a; p.gcb = go->gc_prior_b; p.gcc = go->gc_prior_c;
+    p.lrate = go->prep_lrate; p.grate = go->prep_grate; p.c2m = go->cons_to_mis; p.nc2m = go->ncons_to_mis;
+    p.prop_c = go->prop_c; p.prop_n = go->prop_n; p.prop_gc = go->prop_gc;
+    std::memcpy(p.Q0, M.rate, sizeof(p.Q0));
+    std::memcpy(p.pi, M.pi, sizeof(p.pi));
+    p.target = (const uint8_t*)(dev + o_tgt);
+    p.ws = dev + o_ws; p.ws_stride = W.total;
+    p.N_max = N; p.n_int_max = S - 1; p.GGp_max = GGp_max;
+    p.next_elem = (int*)(dev + o_ctr);
+    p.tr_d = (double*)(dev + o_trd); p.tr_zb = (int8_t*)(dev + o_tzb); p.max_zb = (int8_t*)(dev + o_mzb);
+    p.max_ll = (double*)(dev + o_mll); p.status = (int32_t*)(dev + o_st);
+    bool ok = cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hh.data(), sizeof(GbgcElemHdr) * hh.size(), cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_blob, hblob.data(), blob_total, cudaMemcpyHostToDevice, st), "H2D") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_tgt, target.data(), N, cudaMemcpyHostToDevice, st), "H2D");
+    std::vector<double> trd((size_t)chunk * 3 * 4 * T), mll((size_t)chunk * 3);
+    std::vector<int8_t> tzb((size_t)chunk * tzb_el), mzb((size_t)chunk * 3 * 2 * N);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ok = ok && cuda_ok(c, cudaEventCreate(&e0), "event") && cuda_ok(c, cudaEventCreate(&e1), "event");
+    for (size_t c0 = 0; ok && c0 < run.size(); c0 += chunk) {
+        const int nc = (int)std::min<size_t>(chunk, run.size() - c0);
+        p.hdr = (const GbgcElemHdr*)(dev + o_hdr) + c0;
+        p.blob = (const uint8_t*)(dev + o_blob);
+        p.n_elem = nc;
+        float ms = 0;
+        ok = cuda_ok(c, cudaMemsetAsync(dev + o_ctr, 0, 256, st), "memset") &&
+             cuda_ok(c, cudaEventRecord(e0, st), "event") &&
+             cuda_ok(c, launch_gbgc_chain(p, std::min(grid, nc), smem, prec, st), "gbgc_run: launch") &&
+             cuda_ok(c, cudaEventRecord(e1, st), "event") &&
+             cuda_ok(c, cudaMemcpyAsync(trd.data(), dev + o_trd, (size_t)nc * 3 * 4 * T * 8, cudaMemcpyDeviceToHost, st), "D2H") &&
+             cuda_ok(c, cudaMemcpyAsync(tzb.data(), dev + o_tzb, (size_t)nc * tzb_el, cudaMemcpyDeviceToHost, st), "D2H") &&
+             cuda_ok(c, cudaMemcpyAsync(mzb.data(), dev + o_mzb, (size_t)nc * 3 * 2 * N, cudaMemcpyDeviceToHost, st), "D2H") &&
+             cuda_ok(c, cudaMemcpyAsync(mll.data(), dev + o_mll, (size_t)nc * 3 * 8, cudaMemcpyDeviceToHost, st), "D2H") &&
+             cuda_ok(c, cudaStreamSynchronize(st), "gbgc_run") && cuda_ok(c, cudaEventElapsedTime(&ms, e0, e1), "event");
+        if (!ok) break;
+        c->counters.kernel_ms += ms;
+        // Eval2 and Output_init per element and model, in parallel over elements
+        const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+        std::atomic<int> next(0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; t++)
+            th.emplace_back([&]() {
+                for (int k = next++; k < nc; k = next++) {
+                    const int i = run[c0 + k];
+                    pacc_gbgc_result& r = out[i];
+                    r.device_ms = ms / nc;
+                    for (int m = 0; m < 3; m++) {
+                        const double* d = trd.data() + ((size_t)k * 3 + m) * 4 * T;
+                        const int8_t* zb = tzb.data() + ((size_t)k * 3 + m) * T * 2 * N;
+                        const int8_t* mz = mzb.data() + (((size_t)k * 3 + m) * 2) * N;
+                        const int8_t* mb = mz + N;
+                        r.max_loglik[m] = mll[(size_t)k * 3 + m];
+                        const double ll = gbgc_eval2(m, T, go->burnin, go->mcmc, N, E[i].nodes, E[i].missing, d, zb,
+                                                     zb + N, 2 * (size_t)N, mz, r.max_loglik[m]);
+                        if (m == 0) r.loglik_null = ll;
+                        else if (m == 2) r.loglik_res = ll;
+                        else r.loglik_all = ll;
+                        // Output_init (bpp_c2.cpp:603-660)
+                        for (int q = 0; q < 3; q++) {
+                            std::vector<double> v(d + (q + 1) * T, d + (q + 2) * T);
+                            std::sort(v.begin() + go->burnin, v.end());
+                            r.rates[m][q] = v[v.size() / 2];
+                        }
+                        for (int s = 0; s < N; s++) {
+                            int cz[4] = {0, 0, 0, 0}, cb = 0;
+                            for (int it = go->burnin; it < T; it++) {
+                                cz[zb[(size_t)it * 2 * N + s] + 1]++;
+                                cb += zb[(size_t)it * 2 * N + N + s];
+                            }
+                            if (E[i].missing[s]) cz[0] = go->mcmc;
+                            if (r.post_b) r.post_b[(size_t)m * N + s] = (double)cb / go->mcmc;
+                            if (r.post_z)
+                                for (int q = 0; q < 4; q++) r.post_z[((size_t)m * N + s) * 4 + q] = (double)cz[q] / go->mcmc;
+                            if (r.max_z) r.max_z[(size_t)m * N + s] = mz[s];
+                            if (r.max_b) r.max_b[(size_t)m * N + s] = mb[s];
+                        }
+                        if (r.trace) {
+                            const int Wd = 4 + 2 * N;
+                            for (int it = 0; it < T; it++) {
+                                double* row = r.trace + ((size_t)m * T + it) * Wd;
+                                for (int q = 0; q < 4; q++) row[q] = d[(size_t)q * T + it];
+                                for (int s = 0; s < N; s++) {
+                                    row[4 + s] = zb[(size_t)it * 2 * N + N + s];
+                                    row[4 + N + s] = zb[(size_t)it * 2 * N + s];
+                                }
+                            }
+                        }
+                    }
+                }
+            });
+        for (auto& t : th) t.join();
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(dev);
+    return ok ? PACC_OK : PACC_ECUDA;
 }
 
 int pacc_gbgc_engine(pacc_ctx* c, const uint8_t* bases, int32_t length, int32_t gapchar, double missing_thres,

@@ -1,0 +1,79 @@
+"""The gBGC chain on the GPU (pacc_gbgc_run) against the unmodified gBGC
+reference's traces and tables (tests/golden/gbgc12_default, gbgc43_missing)
+and against the oracle's chain on larger inputs.
+
+With FP64 partials the device follows the reference draw for draw: the
+branch matrices come from Padé approximants instead of eigendecompositions
+and the passes run in linear instead of log space, which moves the
+log-likelihoods by about 1e-12 relative, far below what could flip an MH
+decision in these chains; the traces are compared at the reference's 8 printed
+digits (rtol 1e-7) and the tables as the oracle's test compares them.  With
+FP32 partials the per-column log-likelihoods move by ~1e-6 relative, so the
+chain leaves the reference's path at the first MH decision that close; that
+leg checks the first iterations draw for draw and the element table within
+Monte Carlo error."""
+import os
+
+import numpy as np
+import pytest
+
+from golden_io import GOLDEN, as_float, load_case, read_table
+from test_oracle_gbgc_chain import gbgc_opts
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["gbgc12_default", "gbgc43_missing"]
+
+
+def _ctx(ds, precision):
+    from phyloacc_gb300 import Context, abi
+    o = abi.default_opts()
+    o.precision = precision
+    return Context(ds, o)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gbgc_chain_fp64_matches_reference(built, case):
+    ds, _, kv = load_case(case)
+    o = gbgc_opts(ds, kv)
+    ctx = _ctx(ds, 0)
+    runs = ctx.gbgc_run(o, trace=True)
+    tr = np.load(os.path.join(GOLDEN, case, "traces.npz"))
+    N = ds.tree.n_nodes
+    for e, r in enumerate(runs):
+        assert r["status"] == 0
+        for m in range(3):
+            want = tr["%d_%d" % (m, e)]
+            np.testing.assert_allclose(r["trace"][m], want, rtol=1e-7, atol=1e-9,
+                                       err_msg="element %d model %d" % (e, m))
+    out = os.path.join(GOLDEN, case, "out")
+    _, rows = read_table(os.path.join(out, "case_elem_lik.txt"))
+    for r, row in zip(runs, rows):
+        got = [r["loglik_null"], r["loglik_res"], r["loglik_all"], r["loglik_res"] - r["loglik_null"]] + \
+            list(r["max_loglik"])
+        np.testing.assert_allclose(got, [as_float(x) for x in row[2:9]], rtol=1e-7, atol=1e-6)
+    for m in range(3):
+        _, rows = read_table(os.path.join(out, "case_rate_postZ_%d.txt" % m))
+        for r, row in zip(runs, rows):
+            vals = [as_float(x) for x in row[1:] if x != ""]
+            got = list(r["rates"][m]) + list(r["post_b"][m]) + list(r["post_z"][m].reshape(-1))
+            assert len(vals) == 3 + N + 4 * N
+            np.testing.assert_allclose(got, vals, rtol=1e-5, atol=1e-6)
+    lines = [ln.rstrip("\n\t").split("\t") for ln in open(os.path.join(out, "case_1_elem_Z.txt"))][1:]
+    for r, ln in zip(runs, lines):
+        assert [int(x) for x in ln] == list(r["max_z"][1])
+
+
+def test_gbgc_chain_fp32_follows_reference(built):
+    ds, _, kv = load_case("gbgc12_default")
+    o = gbgc_opts(ds, kv)
+    runs = _ctx(ds, 1).gbgc_run(o, trace=True)
+    tr = np.load(os.path.join(GOLDEN, "gbgc12_default", "traces.npz"))
+    _, rows = read_table(os.path.join(GOLDEN, "gbgc12_default", "out", "case_elem_lik.txt"))
+    for e, (r, row) in enumerate(zip(runs, rows)):
+        want = tr["0_%d" % e]
+        # the first iterations of M0, before FP32 rounding can move an MH decision
+        np.testing.assert_allclose(r["trace"][0][:3], want[:3], rtol=1e-5, atol=1e-6)
+        ref = [as_float(x) for x in row[2:5]]
+        got = [r["loglik_null"], r["loglik_res"], r["loglik_all"]]
+        assert np.all(np.abs(np.array(got) - ref) < 0.02 * np.abs(ref)), (got, ref)
