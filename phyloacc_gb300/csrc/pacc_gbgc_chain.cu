@@ -81,7 +81,9 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
     const double b0 = kPadeB[mi][0];
 #pragma unroll
     for (int q = 0; q < 16; q += 5) V[q] += b0;
-    // (V - U) E = (V + U): Gaussian elimination with partial pivoting, in place
+    // (V - U) E = (V + U): Gaussian elimination with partial pivoting, in
+    // place, one reciprocal per pivot
+    double rp[4];
 #pragma unroll
     for (int q = 0; q < 16; q++) {
         const double u = U[q], v = V[q];
@@ -102,9 +104,10 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
                     double t = U[k * 4 + j]; U[k * 4 + j] = U[i * 4 + j]; U[i * 4 + j] = t;
                     t = V[k * 4 + j]; V[k * 4 + j] = V[i * 4 + j]; V[i * 4 + j] = t;
                 }
+        rp[k] = 1.0 / U[k * 4 + k];
 #pragma unroll
         for (int i = k + 1; i < 4; i++) {
-            const double l = U[i * 4 + k] / U[k * 4 + k];
+            const double l = U[i * 4 + k] * rp[k];
 #pragma unroll
             for (int j = k; j < 4; j++) U[i * 4 + j] -= l * U[k * 4 + j];
 #pragma unroll
@@ -118,7 +121,7 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
             double s = V[k * 4 + j];
 #pragma unroll
             for (int c2 = k + 1; c2 < 4; c2++) s -= U[k * 4 + c2] * E[c2 * 4 + j];
-            E[k * 4 + j] = s / U[k * 4 + k];
+            E[k * 4 + j] = s * rp[k];
         }
     for (int r = 0; r < sq; r++) {
 #pragma unroll
@@ -141,6 +144,13 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
 }
 
 __device__ __forceinline__ double block_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename Real>
+__device__ __forceinline__ Real warp_sum_real(Real v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -185,6 +195,19 @@ struct GbgcCtx {
     __device__ int32_t* expo(int buf, int s, int g) const { return scl + ((size_t)buf * n_int + irank[s]) * GGp + g; }
 };
 
+// log of a branch-matrix entry for the emissions.  With FP64 partials in FP64;
+// with FP32 partials in FP32, the diagonal (close to 1 on short branches) as
+// log1p of its distance from 1, taken in FP64 -- an error below the one the
+// FP32 partials already put on the expected counts it multiplies.
+template <typename Real>
+__device__ __forceinline__ double branch_log(double v, bool diag);
+template <>
+__device__ __forceinline__ double branch_log<double>(double v, bool) { return d_log(v); }
+template <>
+__device__ __forceinline__ double branch_log<float>(double v, bool diag) {
+    return diag ? (double)log1pf((float)(v - 1.0)) : (double)logf((float)v);
+}
+
 // Branch matrices of nc classes (cls[i], selection sel[i], bias bias[i]) into
 // cache set `set`; neutral classes are skipped on fixed branches.
 template <typename Real>
@@ -226,7 +249,7 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const double v = E[(q & 3) * 4 + (q >> 2)];   // (child q/4, parent q%4) = E[parent][child]
-            lo[q] = d_log(v);
+            lo[q] = branch_log<Real>(v, (q & 3) == (q >> 2));
             po[q] = (Real)v;
         }
     }
@@ -446,8 +469,8 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
                 for (int j = 0; j < 4; j++) {
                     const Real jt = r[j] * P[i * 4 + j] * L[i];
                     acc += jt;
-                    const double sum = block_warp_sum(real_col ? (double)jt : 0.0);
-                    if (lane == i * 4 + j) mine = sum;
+                    const Real sum = warp_sum_real(real_col ? jt : Real(0));
+                    if (lane == i * 4 + j) mine = (double)sum;
                 }
                 qs[i] = acc;
             }
@@ -520,8 +543,8 @@ __device__ double prior_z(const GbgcCtx<Real>& G, const GbgcScalars& sc) {
     return r;
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(GB_BT) gbgc_chain_kernel(GbgcChainParams p) {
+template <typename Real, int MINB>
+__global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ GbgcScalars sc;
     __shared__ int s_elem;
@@ -874,25 +897,31 @@ size_t gbgc_chain_smem(int N, int prec) {
 int gbgc_chain_threads() { return GB_BT; }
 int gbgc_chain_warps() { return GB_WARPS; }
 
-int gbgc_chain_occupancy(int prec, size_t smem) {
+// Register budgets: 168 (3 CTAs an SM) or 96 (5 CTAs an SM, some spills).
+template <typename Real, int MINB>
+static cudaError_t launch_one(const GbgcChainParams& p, int grid, size_t smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(gbgc_chain_kernel<Real, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    gbgc_chain_kernel<Real, MINB><<<grid, GB_BT, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+int gbgc_chain_occupancy(int prec, int regs, size_t smem) {
     int n = 0;
-    cudaError_t e = prec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<float>, GB_BT, smem)
-                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<double>, GB_BT, smem);
+    cudaError_t e;
+    if (regs == 168)
+        e = prec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<float, 3>, GB_BT, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<double, 3>, GB_BT, smem);
+    else
+        e = prec ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<float, 5>, GB_BT, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gbgc_chain_kernel<double, 5>, GB_BT, smem);
     return e == cudaSuccess ? n : 0;
 }
 
-cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, cudaStream_t st) {
-    cudaError_t e;
-    if (prec) {
-        e = cudaFuncSetAttribute(gbgc_chain_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        gbgc_chain_kernel<float><<<grid, GB_BT, smem, st>>>(p);
-    } else {
-        e = cudaFuncSetAttribute(gbgc_chain_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        gbgc_chain_kernel<double><<<grid, GB_BT, smem, st>>>(p);
-    }
-    return cudaGetLastError();
+cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, int regs, cudaStream_t st) {
+    if (regs == 168) return prec ? launch_one<float, 3>(p, grid, smem, st) : launch_one<double, 3>(p, grid, smem, st);
+    return prec ? launch_one<float, 5>(p, grid, smem, st) : launch_one<double, 5>(p, grid, smem, st);
 }
 
 }  // namespace pacc

@@ -56,8 +56,8 @@ cudaError_t launch_gbgc(const GbgcParams& p, int prec, cudaStream_t st);
 size_t gbgc_chain_smem(int N, int prec);
 int gbgc_chain_threads();
 int gbgc_chain_warps();
-int gbgc_chain_occupancy(int prec, size_t smem);
-cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, cudaStream_t st);
+int gbgc_chain_occupancy(int prec, int regs, size_t smem);
+cudaError_t launch_gbgc_chain(const GbgcChainParams& p, int grid, size_t smem, int prec, int regs, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // model (BPP, bpp.hpp:173-404)
@@ -2800,7 +2800,9 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     int GGp_max = 32;
     for (int i : run) GGp_max = std::max(GGp_max, E[i].GGp);
     const size_t smem = gbgc_chain_smem(N, prec);
-    const int per_sm = gbgc_chain_occupancy(prec, smem);
+    // register budget of the chain kernel: opts.register_budget 168, else 96
+    const int regs = c->o.register_budget == 168 ? 168 : 96;
+    const int per_sm = gbgc_chain_occupancy(prec, regs, smem);
     if (per_sm <= 0) { c->err = "gbgc_run: the chain kernel does not fit on an SM"; return PACC_ECUDA; }
     const GbgcWs W = GbgcWs::make(N, S - 1, GGp_max, gbgc_chain_warps(), prec ? 4 : 8);
     const size_t tzb_el = (size_t)3 * T * 2 * N;
@@ -2868,7 +2870,7 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
         float ms = 0;
         ok = cuda_ok(c, cudaMemsetAsync(dev + o_ctr, 0, 256, st), "memset") &&
              cuda_ok(c, cudaEventRecord(e0, st), "event") &&
-             cuda_ok(c, launch_gbgc_chain(p, std::min(grid, nc), smem, prec, st), "gbgc_run: launch") &&
+             cuda_ok(c, launch_gbgc_chain(p, std::min(grid, nc), smem, prec, regs, st), "gbgc_run: launch") &&
              cuda_ok(c, cudaEventRecord(e1, st), "event") &&
              cuda_ok(c, cudaMemcpyAsync(trd.data(), dev + o_trd, (size_t)nc * 3 * 4 * T * 8, cudaMemcpyDeviceToHost, st), "D2H") &&
              cuda_ok(c, cudaMemcpyAsync(tzb.data(), dev + o_tzb, (size_t)nc * tzb_el, cudaMemcpyDeviceToHost, st), "D2H") &&

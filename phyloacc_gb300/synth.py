@@ -291,7 +291,18 @@ def make_dataset(kind: str, n_elements: Optional[int] = None, seed: int = 0) -> 
                        and 3% gap cells;
              'st43_stress' — underflow stress set: the st43 tree with all branch
                        lengths x5, 1,000 elements of 2,000 bp, r2 = 6;
-             'st43_serve' — st43 with lengths clipped 50..5000."""
+             'st43_serve' — st43 with lengths clipped 50..5000;
+             'gbgc120' — the gBGC model's workload: 120 taxa, total length 4.0,
+                       20 targets in 6 clades, 20,000 elements of log-normal
+                       length (median 300, sigma 0.6, clipped 50..3000), each
+                       with a GC-bias strength B ~ Gamma(2, 1) on a random 20%
+                       of its branches, selection -2 (conserved) everywhere but
+                       the target clades of the 10% accelerated elements
+                       (selection 0); sequences simulated under the
+                       non-reversible rate matrix getRate(Q0, s, b) of
+                       PhyloAcc-ST-GBGC (bpp_c.cpp:13-30); 3% gap cells and 5%
+                       of (taxon, element) pairs missing, written with '*', the
+                       model's gap character."""
     rng = np.random.default_rng(seed + 1000)
     if kind == "st12":
         S, total, E = 12, 1.2, 100 if n_elements is None else n_elements
@@ -328,6 +339,8 @@ def make_dataset(kind: str, n_elements: Optional[int] = None, seed: int = 0) -> 
         r2 = np.where(accel, 6.0 if kind == "st43_stress" else rng.uniform(1.5, 4.0, E), 0.0)
         miss_pairs = 0.05
         gap_p, n_p = 0.03, 0.0
+    elif kind == "gbgc120":
+        return _make_gbgc(20000 if n_elements is None else n_elements, seed, rng)
     else:
         raise ValueError(kind)
     Q = make_rev_q(pi, exch)
@@ -365,6 +378,84 @@ def make_dataset(kind: str, n_elements: Optional[int] = None, seed: int = 0) -> 
     conserve = [s for s in range(S) if s not in target_leaves and s not in outgroup]
     names = ["elem%05d" % e for e in range(E)]
     return Dataset(tree, pi, Q, outgroup, conserve, target_leaves, lengths, offsets, blocks, names, accel, r1, r2)
+
+
+def gbgc_rate(Q0: np.ndarray, s: float, b: float) -> np.ndarray:
+    """getRate of PhyloAcc-ST-GBGC (bpp_c.cpp:13-30): Q0 scaled entrywise by
+    f(s + b B_ij), f(x) = x / (1 - e^-x), B = +1 from A/T to C/G, -1 back."""
+    if s == 0 and b == 0:
+        return Q0.copy()
+    weak = np.array([1, 0, 0, 1], bool)
+    B = np.where(weak[:, None] & ~weak[None, :], b, np.where(~weak[:, None] & weak[None, :], -b, 0.0)) + s
+    with np.errstate(divide="ignore", invalid="ignore"):
+        F = np.where(B == 0, 1.0, B / (1 - np.exp(-B)))
+    Q = Q0 * F
+    Q[np.diag_indices(4)] -= Q.sum(1)
+    return Q
+
+
+def _make_gbgc(E: int, seed: int, rng) -> Dataset:
+    S, total = 120, 4.0
+    tree = make_tree(S, total, seed)
+    N = tree.n_nodes
+    exch = rng.uniform(0.5, 2.0, 6)
+    pi = np.array([0.30, 0.20, 0.20, 0.30])
+    Q0 = make_rev_q(pi, exch)
+    ingroup_root = int(tree.children[-1][1]) if tree.children[-1][1] >= S else int(tree.children[-1][0])
+    clades = pick_clades(tree, [4, 4, 3, 3, 3, 3], seed, exclude_root_child=ingroup_root)
+    target_nodes = set()
+    for c in clades:
+        target_nodes |= set(tree.nodes_under(c))
+    target_leaves = sorted(v for v in target_nodes if v < S)
+    tmask = np.zeros(N, bool)
+    tmask[list(target_nodes)] = True
+    lengths = np.clip(np.rint(np.exp(np.log(300) + 0.6 * rng.standard_normal(E))), 50, 3000).astype(np.int32)
+    accel = rng.random(E) < 0.10
+    bstr = rng.gamma(2.0, 1.0, E)
+    bflag = rng.random((E, N)) < 0.2
+    # per element, the four rate matrices (selection -2 / 0) x (no bias / bias)
+    Qs = np.empty((E, 4, 4, 4))
+    for e in range(E):
+        for k, (sv, bv) in enumerate(((-2.0, 0.0), (0.0, 0.0), (-2.0, bstr[e]), (0.0, bstr[e]))):
+            Qs[e, k] = gbgc_rate(Q0, sv, bv)
+    lam, V = np.linalg.eig(Qs)
+    Vi = np.linalg.inv(V)
+    tot = int(lengths.sum())
+    eidx = np.repeat(np.arange(E), lengths)
+    srng = np.random.default_rng(seed + 7)
+    states = np.zeros((N, tot), dtype=np.int8)
+    cum_pi = np.cumsum(pi)
+    states[N - 1] = np.searchsorted(cum_pi, srng.random(tot) * cum_pi[-1], side="right").clip(0, 3)
+    par = tree.parent()
+    for v in range(N - 2, -1, -1):
+        k = np.where(accel & tmask[v], 1, 0) + np.where(bflag[:, v], 2, 0)
+        ar = np.arange(E)
+        ex = np.exp(lam[ar, k] * tree.distances[v])
+        P = np.einsum("eij,ej,ejk->eik", V[ar, k], ex, Vi[ar, k]).real.clip(0.0, None)
+        cum = np.cumsum(P, axis=2)
+        cum /= cum[:, :, 3:4]
+        cp = cum[eidx, states[par[v]]]
+        states[v] = (srng.random(tot)[:, None] > cp).sum(1).clip(0, 3)
+    chars = BASES[states[:S]]
+    u = rng.random((S, tot))
+    star = np.uint8(ord("*"))
+    chars = np.where(u < 0.03, star, chars)
+    starts = np.zeros(E + 1, dtype=np.int64)
+    starts[1:] = np.cumsum(lengths)
+    mp = rng.random((E, S)) < 0.05
+    for e, sp in zip(*np.nonzero(mp)):
+        chars[sp, starts[e]:starts[e + 1]] = star
+    offsets = np.zeros(E, dtype=np.int64)
+    offsets[1:] = np.cumsum(lengths[:-1].astype(np.int64) * S)
+    blocks = np.empty(int(lengths.sum()) * S, dtype=np.uint8)
+    for e in range(E):
+        blocks[offsets[e]:offsets[e] + S * int(lengths[e])] = chars[:, starts[e]:starts[e + 1]].reshape(-1)
+    outgroup = [0] if tree.children[-1][0] == 0 else [int(tree.children[-1][0])]
+    outgroup = [v for v in outgroup if v < S]
+    conserve = [s for s in range(S) if s not in target_leaves and s not in outgroup]
+    names = ["elem%05d" % e for e in range(E)]
+    return Dataset(tree, pi, Q0, outgroup, conserve, target_leaves, lengths, offsets, blocks, names, accel,
+                   np.full(E, -2.0), np.where(accel, 0.0, -2.0))
 
 
 # ---------------------------------------------------------------------------
