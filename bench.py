@@ -34,6 +34,16 @@ error     = FP32 against that FP64 leg on the same elements: posterior
 config1   = the 12-taxon configuration (100 elements, BURNIN 500 + MCMC 1000,
             seed 0), FP32 and FP64, K timed steps each, with e2e
 serving   = an open-loop Poisson stream at 80% of `value`: p50/p99 latency
+gbgc      = the gBGC model's configuration (PhyloAcc-ST-GBGC): 120-taxon Yule
+            tree (total length 4.0, 20 targets in 6 clades), elements log-normal
+            (median 300 bp, clipped 50-3000) with a GC-bias strength ~ Gamma(2, 1)
+            each; BURNIN 200 + MCMC 800 (that program's defaults); M0, M2, M1 with
+            Eval2 and the rate / B / Z tables.  A step is one pacc_gbgc_run of
+            --gbgc-elements elements from host buffers (value: device time; e2e:
+            wall time incl. preprocessing, H2D, D2H of the traces and the host's
+            Eval2); FP32 partials, with an FP64-partial leg on the same batch
+            over 40 + 160 iterations, scaled to 1,000; cpu_baseline: the oracle on one element per host core,
+            OpenMP over elements, over a bounded chain scaled to 1,000 iterations
 cpu_baseline and --impl reference run the CPU oracle (the restatement of
 PhyloAcc-ST's path in its own log-space arithmetic) on the host cores over
 elements taken from the start of the same batch: one element per core per
@@ -503,6 +513,8 @@ def run_gpu(args, ws, rank, local):
         line["error"] = err
     if not args.no_config1:
         line["config1"] = run_config1(K, W, ws)
+    if args.gbgc_elements > 0:
+        line["gbgc"] = run_gbgc(args, K, ws, rank)
     if args.serve_seconds > 0:
         line["serving"] = serve_latency(ds, value / ws, args.serve_seconds, args.serve_sweeps)
         line["latency_ms"] = {"p50": line["serving"]["p50_ms"], "p99": line["serving"]["p99_ms"]}
@@ -514,6 +526,76 @@ def run_gpu(args, ws, rank, local):
                                           "elements as step 0 of --impl reference" % (cores - 1, dt)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+GBGC_WORKLOAD = ("120-taxon Yule tree (total length 4.0, 20 targets in 6 clades); elements log-normal (median 300 "
+                 "bp, sigma 0.6, clipped 50-3000), GC-bias strength ~ Gamma(2, 1) on 20% of branches, 10% "
+                 "accelerated; '*' gaps 3%, 5% of (taxon, element) pairs missing; BURNIN 200 + MCMC 800; "
+                 "M0 + M2 + M1 with Eval2 and tables per element")
+
+
+def run_gbgc(args, K, ws, rank):
+    """The gBGC model's leg: K timed steps (after one small warm-up) of
+    --gbgc-elements elements each through pacc_gbgc_run."""
+    import phyloacc_gb300 as pg
+    from phyloacc_gb300 import abi, synth
+    E = args.gbgc_elements
+    ds = synth.make_dataset("gbgc120", n_elements=E, seed=WORKLOAD_SEED + rank)
+    g = abi.gbgc_default_opts(ds.target)
+    g.seed = 1
+    out = {"workload": GBGC_WORKLOAD, "metric": "posterior elements/sec (gBGC model, 120 taxa)",
+           "unit": "elements/s", "elements_per_step": E, "steps": K, "warmup": "one 8-element run",
+           "path": "one CTA per element (persistent, longest element first); FP64 Pade branch matrices; "
+                   "FP32 partials"}
+    # FP64 partials: the same batch on chains of a fifth of the length (the
+    # cost of an iteration does not change along the chain), scaled to 1,000
+    g64 = abi.gbgc_default_opts(ds.target)
+    g64.seed, g64.burnin, g64.mcmc = 1, 40, 160
+    legs = (("fp32", abi.PACC_FP32, g, K), ("fp64", abi.PACC_FP64, g64, 1))
+    for name, prec, gg, steps in legs:
+        o = abi.default_opts()
+        o.precision = prec
+        ctx = pg.Context(ds, o)
+        ctx.gbgc_run(gg, elements=range(8))
+        kern, wall = [], []
+        for _ in range(steps):
+            barrier(ws)
+            c0 = ctx.counters()["kernel_ms"]
+            t = time.perf_counter()
+            r = ctx.gbgc_run(gg)
+            dt = time.perf_counter() - t
+            kern.append(reduce_max(ws, (ctx.counters()["kernel_ms"] - c0) * 1e-3))
+            wall.append(reduce_max(ws, dt))
+        ctx.close()
+        T = gg.burnin + gg.mcmc
+        scale = T / float(g.burnin + g.mcmc)
+        leg = {"value": ws * E * steps / float(np.sum(kern)) * scale, "unit": "elements/s", "elements_per_step": E,
+               "steps": steps, "iterations": T, "ms_per_step": float(np.mean(kern)) * 1e3,
+               "e2e": {"value": ws * E * steps / float(np.sum(wall)) * scale, "unit": "elements/s",
+                       "h2d_bytes_per_step": int(ds.bases.nbytes + ds.lengths.nbytes + ds.offsets.nbytes),
+                       "d2h_bytes_per_step": int(E * 3 * T * (4 * 8 + 2 * ds.tree.n_nodes))},
+               "filtered": int(sum(1 for x in r if x["status"] != 0))}
+        if scale != 1.0:
+            leg["note"] = "measured on %d-iteration chains, scaled to %d" % (T, g.burnin + g.mcmc)
+        out[name] = leg
+    out["value"] = out["fp32"]["value"]
+    out["e2e"] = out["fp32"]["e2e"]
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    if rank == 0 and not args.no_cpu:
+        from oracle import pyoracle
+        cores = os.cpu_count() or 1
+        gc = abi.gbgc_default_opts(ds.target)
+        gc.seed, gc.burnin, gc.mcmc = 1, 20, 80
+        sub = ds.subset(list(range(cores)))
+        t = time.time()
+        pyoracle.gbgc_run_batch(sub, gc, threads=cores)
+        dt = time.time() - t
+        scale = (g.burnin + g.mcmc) / float(gc.burnin + gc.mcmc)
+        out["cpu_baseline"] = {"value": cores / (dt * scale), "unit": "elements/s", "cores": cores, "kind": "port",
+                               "sample": "elements 0..%d of this batch (one per host core), 20 + 80 iterations x 3 "
+                                         "models in %.1f s, scaled to 200 + 800 (the chain's cost per iteration "
+                                         "does not change along the chain)" % (cores - 1, dt)}
+    return out
 
 
 def run_config1(K, W, ws):
@@ -551,6 +633,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
+    ap.add_argument("--gbgc-elements", type=int, default=760,
+                    help="elements per step of the gBGC leg (0: skip; default five chains per SM)")
     ap.add_argument("--block-threads", type=int, default=0,
                     help="FP32 chain kernel: threads per chain (0: the tuner's choice)")
     ap.add_argument("--register-budget", type=int, default=0,

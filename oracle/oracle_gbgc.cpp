@@ -964,6 +964,20 @@ int oracle_gbgc_run_element(const pacc_model* m, const pacc_gbgc_opts* o, const 
     return PACC_OK;
 }
 
+// Every element of a batch, elements spread over n_threads OpenMP threads
+// like the reference's element loop (main.cpp:376-378, schedule guided).
+int oracle_gbgc_run(const pacc_model* m, const pacc_gbgc_opts* o, const pacc_element_batch* b, pacc_gbgc_result* out,
+                    int n_threads) {
+    int bad = 0;
+#pragma omp parallel for schedule(guided) num_threads(n_threads > 0 ? n_threads : 1) reduction(+ : bad)
+    for (int i = 0; i < b->n_elements; i++) {
+        out[i].element_no = b->element_no ? b->element_no[i] : i;
+        const int st = oracle_gbgc_run_element(m, o, b->bases + b->offsets[i], b->lengths[i], &out[i]);
+        if (st != PACC_OK && st != PACC_FILTERED) bad++;
+    }
+    return bad ? PACC_EINVAL : PACC_OK;
+}
+
 int oracle_gbgc_engine(const pacc_model* m, const uint8_t* bases, int32_t GG, int32_t gapchar, double missing_thres,
                        double conserve_prop, const int32_t* z, const int32_t* bflag, double sc, double sn, double gb,
                        double* logp, double* col, double* counts, int32_t* root_out, uint8_t* missing_out,

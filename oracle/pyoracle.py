@@ -240,3 +240,23 @@ def gbgc_run(ds, o: abi.PaccGbgcOpts, e: int, trace: bool = True) -> dict:
                 "loglik_all": r.loglik_all, "max_loglik": np.array(r.max_loglik[:]),
                 "rates": np.array([[r.rates[i][j] for j in range(3)] for i in range(3)])})
     return out
+
+
+def gbgc_run_batch(ds, o: abi.PaccGbgcOpts, threads: int = 0) -> list:
+    """Every element of ds through the gBGC chains on the CPU, OpenMP over
+    elements (oracle_gbgc_run); summary fields only."""
+    import os as _os
+    L = lib()
+    if not hasattr(L, "_gbgc_batch_set"):
+        L.oracle_gbgc_run.argtypes = [C.POINTER(abi.PaccModel), C.POINTER(abi.PaccGbgcOpts),
+                                      C.POINTER(abi.PaccElementBatch), C.POINTER(abi.PaccGbgcResult), C.c_int]
+        L.oracle_gbgc_run.restype = C.c_int
+        L._gbgc_batch_set = True
+    m = abi.ModelArgs(ds)
+    b = abi.BatchArgs(ds)
+    res = (abi.PaccGbgcResult * ds.n_elements)()
+    st = L.oracle_gbgc_run(C.byref(m.model), C.byref(o), C.byref(b.batch), res, threads or (_os.cpu_count() or 1))
+    if st != abi.PACC_OK:
+        raise RuntimeError("oracle_gbgc_run failed: %d" % st)
+    return [{"status": r.status, "loglik_null": r.loglik_null, "loglik_res": r.loglik_res,
+             "loglik_all": r.loglik_all} for r in res]

@@ -2795,6 +2795,8 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
         if (!E[i].filtered) run.push_back(i);
     }
     if (run.empty()) return PACC_OK;
+    // the device queue takes the longest elements first (a shorter tail)
+    std::stable_sort(run.begin(), run.end(), [&](int a, int b2) { return E[a].GG > E[b2].GG; });
     if (!cuda_ok(c, cudaSetDevice(c->device), "gbgc_run: cudaSetDevice")) return PACC_ECUDA;
     const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
     int GGp_max = 32;

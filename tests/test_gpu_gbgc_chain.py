@@ -77,3 +77,27 @@ def test_gbgc_chain_fp32_follows_reference(built):
         ref = [as_float(x) for x in row[2:5]]
         got = [r["loglik_null"], r["loglik_res"], r["loglik_all"]]
         assert np.all(np.abs(np.array(got) - ref) < 0.02 * np.abs(ref)), (got, ref)
+
+
+def test_gbgc_chain_fp64_matches_oracle_st43(built):
+    """43 taxa, elements of 150-700 columns with '-' as the gap character (so
+    that taxa go missing and the outgroup path collapses), 30 + 90
+    iterations: the device's traces and tables against the oracle's."""
+    from oracle import pyoracle as po
+    from phyloacc_gb300 import abi, synth
+    ds = synth.make_dataset("st43", n_elements=6, seed=3)
+    o = abi.gbgc_default_opts(ds.target)
+    o.burnin, o.mcmc, o.seed, o.gapchar = 30, 90, 11, ord("-")
+    runs = _ctx(ds, 0).gbgc_run(o, trace=True)
+    for e, r in enumerate(runs):
+        ref = po.gbgc_run(ds, o, e)
+        assert r["status"] == ref["status"] == 0
+        assert r["root"] == ref["root"]
+        np.testing.assert_allclose(r["trace"], ref["trace"], rtol=1e-9, atol=1e-9, err_msg="element %d" % e)
+        np.testing.assert_allclose([r["loglik_null"], r["loglik_res"], r["loglik_all"]],
+                                   [ref["loglik_null"], ref["loglik_res"], ref["loglik_all"]], rtol=1e-9)
+        np.testing.assert_allclose(r["max_loglik"], ref["max_loglik"], rtol=1e-9)
+        np.testing.assert_allclose(r["rates"], ref["rates"], rtol=1e-9)
+        np.testing.assert_allclose(r["post_b"], ref["post_b"], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(r["post_z"], ref["post_z"], rtol=0, atol=1e-12)
+        assert (r["max_z"] == ref["max_z"]).all() and (r["max_b"] == ref["max_b"]).all()
