@@ -178,8 +178,8 @@ struct GbgcCtx {
     const uint8_t* flags;
     const double* dist;
     const uint8_t* masks;
-    double *lP, *post, *wc, *emis, *emis_tmp, *lpb, *eraw, *colsum;
-    Real *pm, *part;
+    double *wc, *emis, *emis_tmp, *lpb, *eraw, *colsum;
+    Real *lP, *post, *pm, *part;   // log P, expected counts, P, partials in the partials' type
     int32_t* scl;
     Real* Pcur;
     double *pw, *qn;
@@ -187,7 +187,7 @@ struct GbgcCtx {
     __device__ bool missing(int s) const { return flags[s] & GBGC_MISSING; }
     __device__ int upper(int s) const { return (flags[s] & GBGC_UPPER) ? 1 : 0; }
     __device__ int slot(int cls, int set) const { return cls == 0 ? 0 : 1 + 5 * set + (cls - 1); }
-    __device__ double* lp(int sl, int s) const { return lP + ((size_t)sl * N + s) * 16; }
+    __device__ Real* lp(int sl, int s) const { return lP + ((size_t)sl * N + s) * 16; }
     __device__ Real* pmat(int sl, int s) const { return pm + ((size_t)sl * N + s) * 16; }
     __device__ Real* partial(int buf, int s, int g) const {
         return part + (((size_t)buf * n_int + irank[s]) * GGp + g) * 4;
@@ -196,16 +196,17 @@ struct GbgcCtx {
 };
 
 // log of a branch-matrix entry for the emissions.  With FP64 partials in FP64;
-// with FP32 partials in FP32, the diagonal (close to 1 on short branches) as
-// log1p of its distance from 1, taken in FP64 -- an error below the one the
-// FP32 partials already put on the expected counts it multiplies.
+// with FP32 partials in FP32 (and so the emissions' dot products), the
+// diagonal (close to 1 on short branches) as log1p of its distance from 1,
+// taken in FP64 -- an error below the one the FP32 partials already put on
+// the expected counts it multiplies.
 template <typename Real>
-__device__ __forceinline__ double branch_log(double v, bool diag);
+__device__ __forceinline__ Real branch_log(double v, bool diag);
 template <>
 __device__ __forceinline__ double branch_log<double>(double v, bool) { return d_log(v); }
 template <>
-__device__ __forceinline__ double branch_log<float>(double v, bool diag) {
-    return diag ? (double)log1pf((float)(v - 1.0)) : (double)logf((float)v);
+__device__ __forceinline__ float branch_log<float>(double v, bool diag) {
+    return diag ? log1pf((float)(v - 1.0)) : logf((float)v);
 }
 
 // Branch matrices of nc classes (cls[i], selection sel[i], bias bias[i]) into
@@ -244,7 +245,7 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
         double E[16];
         pade_branch(G.pw + ci * 13 * 16, G.qn[ci], G.dist[s], E);
         const int sl = G.slot(cls[ci], set);
-        double* lo = G.lp(sl, s);
+        Real* lo = G.lp(sl, s);
         Real* po = G.pmat(sl, s);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
@@ -261,22 +262,56 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
 // node's current class before the constants goes to eraw.
 template <typename Real>
 __device__ void emissions(const GbgcCtx<Real>& G, const GbgcScalars& sc, double* out, int lo, int set,
-                          const double* post, bool raw) {
+                          const Real* post, bool raw) {
     const int nb = G.nn - 1, ncl = 6 - lo;
     for (int it = threadIdx.x; it < nb * ncl; it += blockDim.x) {
         const int s = G.nodes[it / ncl], j = lo + it % ncl;
         if (G.missing(s) || (G.fixZ[s] == 1 && j % 3 == 2)) continue;
-        const double* a = G.lp(G.slot(j, set), s);
-        const double* b = post + (size_t)s * 16;
-        double t = 0;
+        const Real* a = G.lp(G.slot(j, set), s);
+        const Real* b = post + (size_t)s * 16;
+        Real tr = 0;
         for (int c = 0; c < 4; c++)
-            for (int r = 0; r < 4; r++) t += a[r * 4 + c] * b[r * 4 + c];
+            for (int r = 0; r < 4; r++) tr += a[r * 4 + c] * b[r * 4 + c];
+        double t = (double)tr;
         if (raw && j == G.Z[s] + 3 * G.B[s]) G.eraw[s] = t;
         t += sc.ec_gc[j < 3 ? 0 : 1];
         t += sc.ec_mis[j % 3 == 1 ? 0 : 1];
         out[s * 6 + j] = t;
     }
     __syncthreads();
+}
+
+// log_multi of the 6 x 3 log_TM_Int by log_prob_back y (max mx), in linear
+// space: t_j = mx + log(sum_z TM[z][j] (e^(y_z - mx) + e^(y_(z+3) - mx))).
+// With FP32 partials the exponentials and logarithm are FP32 (differences and
+// sums of the FP64 log values stay FP64).
+template <typename Real>
+__device__ __forceinline__ void lm63(const double (*tm)[3], const double* y, double mx, double* t);
+template <>
+__device__ __forceinline__ void lm63<double>(const double (*tm)[3], const double* y, double mx, double* t) {
+    double ez[3];
+#pragma unroll
+    for (int z = 0; z < 3; z++) ez[z] = d_exp(y[z] - mx) + d_exp(y[z + 3] - mx);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        double v = 0;
+#pragma unroll
+        for (int z = 0; z < 3; z++) v += tm[z][j] * ez[z];
+        t[j] = d_log(v) + mx;
+    }
+}
+template <>
+__device__ __forceinline__ void lm63<float>(const double (*tm)[3], const double* y, double mx, double* t) {
+    float ez[3];
+#pragma unroll
+    for (int z = 0; z < 3; z++) ez[z] = expf((float)(y[z] - mx)) + expf((float)(y[z + 3] - mx));
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        float v = 0;
+#pragma unroll
+        for (int z = 0; z < 3; z++) v += (float)tm[z][j] * ez[z];
+        t[j] = (double)logf(v) + mx;
+    }
 }
 
 // The Z-message pass: lpb[p] += log_multi(log_TM_Int[c], lpb[c]) (- log 2)
@@ -301,18 +336,10 @@ __device__ void up_pass(const GbgcCtx<Real>& G, const GbgcScalars& sc, bool half
                 if (mx == -CUDART_INF) {
                     t[0] = t[1] = t[2] = -CUDART_INF;
                 } else {
-                    double ez[3];
+                    lm63<Real>(sc.tm[G.upper(c)], y, mx, t);
 #pragma unroll
-                    for (int z = 0; z < 3; z++) ez[z] = d_exp(y[z] - mx) + d_exp(y[z + 3] - mx);
-                    const int u = G.upper(c);
-#pragma unroll
-                    for (int j = 0; j < 3; j++) {
-                        double v = 0;
-#pragma unroll
-                        for (int z = 0; z < 3; z++) v += sc.tm[u][z][j] * ez[z];
-                        t[j] = d_log(v) + mx;
+                    for (int j = 0; j < 3; j++)
                         if (half) t[j] -= LN2;
-                    }
                 }
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
@@ -426,7 +453,7 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
 // Update_Tg with sampling over every column from partial buffer buf (its
 // internal partials are replaced by marginals): expected counts into dst.
 template <typename Real>
-__device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf, double* dst) {
+__device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf, Real* dst) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double* wc = G.wc + (size_t)w * G.N * 16;
     for (int i = lane; i < G.N * 16; i += 32) wc[i] = 0;
@@ -487,9 +514,15 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
     for (int i = threadIdx.x; i < G.N * 16; i += blockDim.x) {
         double t = 0;
         for (int v = 0; v < GB_WARPS; v++) t += G.wc[(size_t)v * G.N * 16 + i];
-        dst[i] = t;
+        dst[i] = (Real)t;
     }
     __syncthreads();
+}
+
+// The categorical weights of Z/B sampling: FP64, or FP32 with FP32 partials.
+template <typename Real>
+__device__ __forceinline__ double zb_exp(double x) {
+    return sizeof(Real) == 8 ? d_exp(x) : (double)expf((float)x);
 }
 
 // Update_ZB's sampling (bpp_c.cpp:1710-1761): depths top-down, the node at
@@ -515,14 +548,14 @@ __device__ void sample_zb(const GbgcChainParams& p, const GbgcCtx<Real>& G, Gbgc
                 for (int r = 1; r < 6; r++)
                     if (x[r] > mx) mx = x[r];
 #pragma unroll
-                for (int r = 0; r < 6; r++) wv[r] = d_exp(x[r] - mx);
+                for (int r = 0; r < 6; r++) wv[r] = zb_exp<Real>(x[r] - mx);
                 const int nn = categorical(6, wv, u);
                 G.Z[s] = (int8_t)(nn % 3);
                 if (!G.missing(s)) G.B[s] = nn > 2 ? 1 : 0;
             } else {
                 G.Z[s] = 2;
                 const double mx = fmax(y[2], y[5]);
-                const double wv[2] = {d_exp(y[2] - mx), d_exp(y[5] - mx)};
+                const double wv[2] = {zb_exp<Real>(y[2] - mx), zb_exp<Real>(y[5] - mx)};
                 const int nn = categorical(2, wv, u);
                 if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
             }
@@ -595,7 +628,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
         G.masks = eb + H.o_masks;
         const GbgcWs W = GbgcWs::make(p.N_max, p.n_int_max, p.GGp_max, GB_WARPS, sizeof(Real));
         char* ws = p.ws + (size_t)blockIdx.x * p.ws_stride;
-        G.lP = (double*)(ws + W.lP); G.pm = (Real*)(ws + W.pm); G.post = (double*)(ws + W.post);
+        G.lP = (Real*)(ws + W.lP); G.pm = (Real*)(ws + W.pm); G.post = (Real*)(ws + W.post);
         G.wc = (double*)(ws + W.wc); G.emis = (double*)(ws + W.emis); G.emis_tmp = (double*)(ws + W.emis_tmp);
         G.lpb = (double*)(ws + W.lpb); G.eraw = (double*)(ws + W.eraw); G.colsum = (double*)(ws + W.colsum);
         G.part = (Real*)(ws + W.part); G.scl = (int32_t*)(ws + W.scl);
@@ -746,7 +779,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                     if (tid == 0) sc.post_cur = sc.post_nxt;
                     __syncthreads();
                 }
-                const double* post = G.post + (size_t)sc.post_cur * N * 16;
+                const Real* post = G.post + (size_t)sc.post_cur * N * 16;
                 // initial_prob_back
                 emissions(G, sc, G.emis, 0, sc.cur, post, true);
                 if (tid == 0) {
@@ -838,12 +871,12 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 for (int k = tid; k < G.nn - 1; k += blockDim.x) {
                     const int s = G.nodes[k];
                     if (G.missing(s)) continue;
-                    const double* a2 = G.lp(G.slot(G.Z[s] + 3 * G.B[s], sc.acc), s);
-                    const double* b2 = post + (size_t)s * 16;
-                    double t = 0;
+                    const Real* a2 = G.lp(G.slot(G.Z[s] + 3 * G.B[s], sc.acc), s);
+                    const Real* b2 = post + (size_t)s * 16;
+                    Real t = 0;
                     for (int c = 0; c < 4; c++)
                         for (int r = 0; r < 4; r++) t += a2[r * 4 + c] * b2[r * 4 + c];
-                    G.eraw[s] = t;
+                    G.eraw[s] = (double)t;
                 }
                 __syncthreads();
                 if (tid == 0) {
