@@ -543,6 +543,8 @@ def run_gbgc(args, K, ws, rank):
     ds = synth.make_dataset("gbgc120", n_elements=E, seed=WORKLOAD_SEED + rank)
     g = abi.gbgc_default_opts(ds.target)
     g.seed = 1
+    if args.gbgc_burnin is not None:
+        g.burnin, g.mcmc = args.gbgc_burnin, args.gbgc_mcmc
     out = {"workload": GBGC_WORKLOAD, "metric": "posterior elements/sec (gBGC model, 120 taxa)",
            "unit": "elements/s", "elements_per_step": E, "steps": K, "warmup": "one 8-element run",
            "path": "one CTA per element (persistent, longest element first); FP64 Pade branch matrices; "
@@ -552,6 +554,8 @@ def run_gbgc(args, K, ws, rank):
     g64 = abi.gbgc_default_opts(ds.target)
     g64.seed, g64.burnin, g64.mcmc = 1, 40, 160
     legs = (("fp32", abi.PACC_FP32, g, K), ("fp64", abi.PACC_FP64, g64, 1))
+    if args.gbgc_fp32_only:
+        legs = legs[:1]
     for name, prec, gg, steps in legs:
         o = abi.default_opts()
         o.precision = prec
@@ -580,7 +584,8 @@ def run_gbgc(args, K, ws, rank):
         out[name] = leg
     out["value"] = out["fp32"]["value"]
     out["e2e"] = out["fp32"]["e2e"]
-    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    if "fp64" in out:
+        out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
     if rank == 0 and not args.no_cpu:
         from oracle import pyoracle
         cores = os.cpu_count() or 1
@@ -635,6 +640,10 @@ def main():
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--gbgc-elements", type=int, default=760,
                     help="elements per step of the gBGC leg (0: skip; default five chains per SM)")
+    ap.add_argument("--gbgc-only", action="store_true", help="profiling: run only the gBGC leg, print it")
+    ap.add_argument("--gbgc-fp32-only", action="store_true", help="profiling: skip the gBGC FP64 leg")
+    ap.add_argument("--gbgc-burnin", type=int, default=None, help="profiling only: shorter gBGC chains")
+    ap.add_argument("--gbgc-mcmc", type=int, default=None, help="profiling only: shorter gBGC chains")
     ap.add_argument("--block-threads", type=int, default=0,
                     help="FP32 chain kernel: threads per chain (0: the tuner's choice)")
     ap.add_argument("--register-budget", type=int, default=0,
@@ -651,6 +660,14 @@ def main():
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.gbgc_only:
+        import phyloacc_gb300 as pg
+        if not os.path.exists(pg.LIB_PATH):
+            from phyloacc_gb300.build import build
+            build()
+        out = run_gbgc(args, args.steps, ws, rank)
+        if rank == 0:
+            print(json.dumps({"gbgc": out}), flush=True)
     else:
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if ws > 1 else None
         run_gpu(args, ws, rank, local)
