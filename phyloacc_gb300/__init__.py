@@ -22,6 +22,7 @@ from .abi import default_opts  # noqa: F401
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libpaccgpu.so")
 CLI_PATH = os.path.join(HERE, "_build", "phyloacc-st-gpu")
+CLI_GBGC_PATH = os.path.join(os.path.dirname(CLI_PATH), "phyloacc-gbgc-gpu")
 _lib = None
 
 

@@ -17,6 +17,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.pat
 
 LIB = os.path.join(OUT, "libpaccgpu.so")
 CLI = os.path.join(OUT, "phyloacc-st-gpu")
+CLI_GBGC = os.path.join(OUT, "phyloacc-gbgc-gpu")
 
 
 def _deps():
@@ -39,7 +40,7 @@ def _run(cmd):
 
 def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
-    if not force and not _stale(LIB) and not _stale(CLI):
+    if not force and not _stale(LIB) and not _stale(CLI) and not _stale(CLI_GBGC):
         return LIB
     objs = {
         "pacc_chain.o": [NVCC] + ARCH + COMMON + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "pacc_chain.cu")],
@@ -60,13 +61,12 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp] + [os.path.join(OUT, n) for n in objs])
     os.replace(tmp, LIB)
-    cli_src = os.path.join(CSRC, "phyloacc_st_gpu.cpp")
-    if os.path.exists(cli_src):
-        tmp = CLI + ".tmp"
+    for src, exe in (("phyloacc_st_gpu.cpp", CLI), ("phyloacc_gbgc_gpu.cpp", CLI_GBGC)):
+        tmp = exe + ".tmp"
         # -ffp-contract=off: the host's hyper-parameter MH rounds like the oracle's
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", tmp,
-              "-L" + OUT, "-lpaccgpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
-        os.replace(tmp, CLI)
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
+              os.path.join(CSRC, src), "-o", tmp, "-L" + OUT, "-lpaccgpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
+        os.replace(tmp, exe)
     return LIB
 
 

@@ -128,3 +128,42 @@ def test_gbgc_chain_fp32_against_fp64_at_size(built):
     print("gbgc fp32 vs fp64: max %.3g median %.3g over %d" % (rel.max(), np.median(rel), len(rel)))
     assert len(rel) >= 100
     assert rel.max() < 1e-3 and np.median(rel) < 1e-6
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gbgc_cli_matches_reference(built, tmp_path, case):
+    """phyloacc-gbgc-gpu on the golden case's own cfg and inputs: every table
+    the reference wrote (elem_lik, rate_postZ_{0,1,2}, 1_elem_Z,
+    species_names) and every VERBOSE trace file."""
+    import shutil
+    import subprocess
+    import phyloacc_gb300 as pg
+    from golden_io import read_cfg
+    src = os.path.join(GOLDEN, case)
+    work = tmp_path / case
+    shutil.copytree(src, work)
+    shutil.rmtree(work / "out")
+    os.makedirs(work / "out")
+    r = subprocess.run([pg.CLI_GBGC_PATH, "case.cfg"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    ref_dir = os.path.join(src, "out")
+    for f in sorted(os.listdir(ref_dir)):
+        lines1 = [ln.rstrip("\n").split("\t") for ln in open(os.path.join(ref_dir, f))]
+        lines2 = [ln.rstrip("\n").split("\t") for ln in open(str(work / "out" / f))]
+        assert len(lines1) == len(lines2), f
+        assert lines1[0] == lines2[0], f
+        for a, b in zip(lines1[1:], lines2[1:]):
+            assert len(a) == len(b), f
+            for x, y in zip(a, b):
+                if x == y:
+                    continue
+                fx, fy = as_float(x), as_float(y)
+                assert np.isclose(fx, fy, rtol=2e-6, atol=1e-12) or (np.isnan(fx) and np.isnan(fy)), (f, x, y)
+    kv = read_cfg(str(work / "case.cfg"))
+    T = int(kv["BURNIN"]) + int(kv["MCMC"])
+    tr = np.load(os.path.join(src, "traces.npz"))
+    for key in tr.files:
+        p = work / "out" / ("case_mcmc_trace_%s.txt" % key)
+        got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
+        assert got.shape[0] == T
+        np.testing.assert_allclose(got, tr[key], rtol=2e-7, atol=1e-300, err_msg=key)

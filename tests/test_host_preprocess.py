@@ -201,3 +201,30 @@ def test_cli_chain_zero_writes_headers_only(tmp_path):
                                                    "case_rate_postZ_M2.txt", "case_species_names.txt"]
     for m in range(3):
         assert len(open(tmp_path / "out" / ("case_rate_postZ_M%d.txt" % m)).read().splitlines()) == 1
+
+
+def test_gbgc_cli_chain_zero_and_unbuilt_modes(tmp_path):
+    """phyloacc-gbgc-gpu: with CHAIN 0 (no default in the reference) only the
+    headers, the hyper header and the species names are written and no device
+    is touched; INDEL > 0 and SAMPLE_HYPER fail loudly."""
+    import shutil
+    import subprocess
+    from phyloacc_gb300.build import build, CLI_GBGC
+    build()
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gbgc12_default")
+    for f in ("case.mod", "case.bed", "case.fa"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    (tmp_path / "out").mkdir()
+    base = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines() if not ln.startswith("CHAIN ")]
+    (tmp_path / "case.cfg").write_text("\n".join(base + ["CHAIN 0"]) + "\n")
+    r = subprocess.run([CLI_GBGC, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert sorted(os.listdir(tmp_path / "out")) == ["case_hyper.txt", "case_rate_postZ_0.txt", "case_rate_postZ_1.txt",
+                                                    "case_rate_postZ_2.txt", "case_species_names.txt"]
+    hdr = open(tmp_path / "out" / "case_rate_postZ_1.txt").read().split("\n")[0]
+    want = open(os.path.join(src, "out", "case_rate_postZ_1.txt")).read().split("\n")[0]
+    assert hdr == want
+    for extra, message in ((["INDEL 1"], "INDEL"), (["SAMPLE_HYPER 1"], "SAMPLE_HYPER")):
+        (tmp_path / "case.cfg").write_text("\n".join(base + ["CHAIN 1"] + extra) + "\n")
+        r = subprocess.run([CLI_GBGC, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+        assert r.returncode != 0 and message in r.stderr
