@@ -314,6 +314,23 @@ typedef struct pacc_gbgc_result {
 int pacc_gbgc_run(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_batch* batch,
                   pacc_gbgc_result* out);
 
+/* Serving form of pacc_gbgc_run: elements are admitted while others run.  A
+ * persistent chain kernel (one CTA an element) takes elements from a queue
+ * the host appends to; submit preprocesses the batch and queues it (a change
+ * of options, precision or a longer element than the serving slots hold
+ * first lets the running elements finish and re-creates the slots); poll
+ * collects finished elements (Eval2 and the tables on the host) and writes
+ * up to max results, in completion order, into out, copying the per-node
+ * arrays into the buffers out[i].max_z / max_b / post_b / post_z point to
+ * (when non-null; traces are not kept); out[i].device_ms is the element's
+ * time from submit to collection.  sync returns when every submitted element
+ * has finished (their results stay for poll).  The blocks leave after
+ * opts.serve_idle_ns of the context without work; opts.max_resident (> 0)
+ * caps the device slots (default: two per resident CTA). */
+int pacc_gbgc_submit(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_batch* batch);
+int pacc_gbgc_poll(pacc_ctx* ctx, pacc_gbgc_result* out, int max);
+int pacc_gbgc_sync(pacc_ctx* ctx);
+
 /* --- Kernel-level entry points used by parity tests (same kernels as the chain) --- */
 
 /* (a) P^T = eigeninv * diag(exp(lambda*d*r)) * eigenvec for n branch lengths

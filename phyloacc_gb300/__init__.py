@@ -63,6 +63,9 @@ def lib():
         L.pacc_gbgc_default_opts.argtypes = [C.POINTER(abi.PaccGbgcOpts)]
         L.pacc_gbgc_run.argtypes = [C.c_void_p, C.POINTER(abi.PaccGbgcOpts), C.POINTER(abi.PaccElementBatch),
                                     C.POINTER(abi.PaccGbgcResult)]
+        L.pacc_gbgc_submit.argtypes = [C.c_void_p, C.POINTER(abi.PaccGbgcOpts), C.POINTER(abi.PaccElementBatch)]
+        L.pacc_gbgc_poll.argtypes = [C.c_void_p, C.POINTER(abi.PaccGbgcResult), C.c_int]
+        L.pacc_gbgc_sync.argtypes = [C.c_void_p]
         L.pacc_gbgc_engine.argtypes = [C.c_void_p, C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_double,
                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_double, C.c_double,
                                        C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -255,6 +258,48 @@ class Context:
                       "rates": np.array([[r.rates[i][j] for j in range(3)] for i in range(3)])})
             out.append(d)
         return out
+
+    def gbgc_submit(self, gopts, elements=None, ds=None):
+        """Queue elements for the gBGC serving kernel (pacc_gbgc_submit)."""
+        ds = ds or self.ds
+        idx = list(range(ds.n_elements)) if elements is None else list(elements)
+        sub = ds.subset(idx)
+        batch = abi.BatchArgs(sub, np.array(idx, np.int64))
+        st = lib().pacc_gbgc_submit(self.h, C.byref(gopts), C.byref(batch.batch))
+        if st != 0:
+            self._err("pacc_gbgc_submit", st)
+
+    def gbgc_poll(self, max_results: int = 1 << 16) -> list:
+        """Finished gBGC elements so far (completion order), as gbgc_run's dicts."""
+        N = self.ds.tree.n_nodes
+        res = (abi.PaccGbgcResult * max_results)()
+        bufs = []
+        for k in range(max_results):
+            b = {"max_z": np.zeros((3, N), np.int32), "max_b": np.zeros((3, N), np.int8),
+                 "post_b": np.zeros((3, N)), "post_z": np.zeros((3, N, 4))}
+            res[k].max_z = abi.ptr(b["max_z"], C.c_int32)
+            res[k].max_b = abi.ptr(b["max_b"], C.c_int8)
+            res[k].post_b = abi.ptr(b["post_b"], C.c_double)
+            res[k].post_z = abi.ptr(b["post_z"], C.c_double)
+            bufs.append(b)
+        n = lib().pacc_gbgc_poll(self.h, res, max_results)
+        if n < 0:
+            self._err("pacc_gbgc_poll", n)
+        out = []
+        for k in range(n):
+            r = res[k]
+            d = dict(bufs[k])
+            d.update({"element_no": r.element_no, "status": r.status, "root": r.root,
+                      "loglik_null": r.loglik_null, "loglik_res": r.loglik_res, "loglik_all": r.loglik_all,
+                      "max_loglik": np.array(r.max_loglik[:]), "device_ms": r.device_ms,
+                      "rates": np.array([[r.rates[i][j] for j in range(3)] for i in range(3)])})
+            out.append(d)
+        return out
+
+    def gbgc_sync(self):
+        st = lib().pacc_gbgc_sync(self.h)
+        if st != 0:
+            self._err("pacc_gbgc_sync", st)
 
     def patterns(self, e: int):
         """(pattern_of [n_cols], weights [n_patterns]) of element e (host only)."""

@@ -302,6 +302,17 @@ struct GbgcChainParams {
     int8_t* max_zb;           // [n_elem][3][2][N_max]
     double* max_ll;           // [n_elem][3]
     int32_t* status;          // [n_elem]
+    // stream mode (serving): elements come from a queue the host appends to
+    // while the kernel runs; element data and outputs are indexed by slot
+    int stream;
+    int* q_head;                     // device: next queue position to take
+    const volatile int* q_tail;      // host-mapped: positions published so far
+    const volatile int* q_slot;      // host-mapped: slot of position i (ring of q_cap)
+    int q_cap;
+    volatile int* done_flag;         // host-mapped, per slot: 1 once the slot's outputs are written
+    const volatile int* q_stop;      // host-mapped: nonzero asks idle blocks to return
+    long long idle_ns;               // a block idle this long returns even without q_stop
+    unsigned long long* idle_exits;  // blocks that left on the idle bound
 };
 
 }  // namespace pacc

@@ -143,6 +143,12 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
     }
 }
 
+__device__ __forceinline__ unsigned long long gb_timer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ double block_warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -584,11 +590,46 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
     const int tid = threadIdx.x;
     StreamReader rng;   // thread 0's sequential reader
     for (;;) {
-        if (tid == 0) s_elem = atomicAdd(p.next_elem, 1);
+        if (tid == 0) {
+            if (!p.stream) {
+                s_elem = atomicAdd(p.next_elem, 1);
+            } else {
+                // the next published queue position; return when the host asks
+                // idle blocks to stop, or after idle_ns without work
+                s_elem = p.n_elem;
+                const unsigned long long t0 = gb_timer_ns();
+                for (;;) {
+                    const int h = *(volatile int*)p.q_head;
+                    const int t = *p.q_tail;
+                    if (h >= t && *p.q_stop) break;
+                    if (h < t) {
+                        if (atomicCAS(p.q_head, h, h + 1) == h) {
+                            __threadfence_system();   // the slot id and its data after the tail
+                            s_elem = p.q_slot[h % p.q_cap];
+                            break;
+                        }
+                        continue;
+                    }
+                    if ((long long)(gb_timer_ns() - t0) > p.idle_ns) {
+                        if (p.idle_exits) atomicAdd(p.idle_exits, 1ull);
+                        break;
+                    }
+                    __nanosleep(4000);
+                }
+            }
+        }
         __syncthreads();
         const int e = s_elem;
-        if (e >= p.n_elem) break;
-        const GbgcElemHdr H = p.hdr[e];
+        if (e < 0 || e >= p.n_elem) break;
+        GbgcElemHdr H;
+        if (p.stream) {
+            // the host rewrote this slot while the kernel ran: read it past L1
+            const int* src = (const int*)(p.hdr + e);
+            int* dst = (int*)&H;
+            for (int i = 0; i < (int)(sizeof(GbgcElemHdr) / 4); i++) dst[i] = __ldcg(src + i);
+        } else {
+            H = p.hdr[e];
+        }
         const uint8_t* eb = p.blob + H.blob_off;
         GbgcCtx<Real> G;
         G.S = H.S; G.N = H.N; G.GG = H.GG; G.GGp = H.GGp; G.root = H.root; G.nn = H.n_nodes; G.n_int = H.n_int;
@@ -913,6 +954,12 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             __syncthreads();
         }
         if (tid == 0) p.status[e] = 0;
+        if (p.stream) {
+            // publish the slot once every thread's output writes are visible
+            __threadfence_system();
+            __syncthreads();
+            if (tid == 0) p.done_flag[e] = 1;
+        }
         __syncthreads();
     }
 }

@@ -777,6 +777,58 @@ struct StreamServer {
     double kernel_ms = 0;
 };
 
+
+// The gBGC model's serving state: a persistent chain kernel fed from a host
+// queue (slots of element blob + outputs on the device, a mapped ring of
+// queue positions and per-slot done flags); everything is allocated once at
+// set-up, because allocations synchronise the device and would wait for the
+// persistent launch.
+struct GbgcServer {
+    bool ready = false, running = false;
+    int ns = 0, grid = 0, prec = 0, regs = 96, N = 0, T = 0, GGp_cap = 0;
+    size_t smem = 0, blob_cap = 0, out_b = 0;
+    pacc_gbgc_opts g;
+    std::vector<int32_t> target;
+    char* dev = nullptr;
+    GbgcElemHdr* d_hdr = nullptr;
+    char* d_blob = nullptr;
+    char* d_out = nullptr;          // per slot: tr_d, tr_zb, max_zb, max_ll, status
+    int* h_map = nullptr;           // host-mapped: [0] tail, [1] stop, [64, 64+ns) slot ring, [64+ns, 64+2ns) done
+    volatile int *h_tail = nullptr, *h_stop = nullptr, *h_qslot = nullptr, *h_done = nullptr;
+    char* h_stage = nullptr;        // pinned admission staging
+    size_t h_stage_cap = 0;
+    char* h_out = nullptr;          // pinned result staging, out_chunk slots
+    int out_chunk = 0;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_done = nullptr, ev0 = nullptr;
+    GbgcChainParams p;
+    std::vector<int> free_slots;
+    std::vector<char> busy;
+    std::vector<int64_t> slot_no;
+    std::vector<double> slot_t0;
+    std::vector<GbgcElem> slot_elem;
+    struct Pending {
+        GbgcElem E;
+        GbgcElemHdr H;
+        std::vector<uint8_t> blob;
+        int64_t no;
+        double t0;
+        int filtered;
+    };
+    std::deque<Pending> queue;
+    struct Done {
+        pacc_gbgc_result r;
+        std::vector<int32_t> max_z;
+        std::vector<int8_t> max_b;
+        std::vector<double> post_b, post_z;
+    };
+    std::deque<Done> done;
+    int tail = 0, resident = 0;
+    long long launches = 0;
+    double kernel_ms = 0;
+    unsigned long long* d_idle = nullptr;
+};
+
 struct pacc_ctx {
     HostModel M;
     pacc_opts o;
@@ -812,6 +864,7 @@ struct pacc_ctx {
     void* d_misc = nullptr; size_t misc_cap = 0;
     Server srv;
     StreamServer ss;
+    GbgcServer gs;
 };
 
 static std::string g_create_error;
@@ -830,6 +883,329 @@ static bool grow(pacc_ctx* c, void** p, size_t* cap, size_t need) {
     size_t n = std::max(need, (size_t)(*cap * 3 / 2));
     if (!cuda_ok(c, cudaMalloc(p, n), "cudaMalloc")) return false;
     *cap = n;
+    return true;
+}
+
+// Eval2 and Output_init (bpp_c2.cpp:29-286, 603-660) of one element from its
+// device traces: trd [3][4][T], tzb [3][T][2][N] (Z then B), mzb [3][2][N]
+// (Max_Z then Max_B), mll [3].  Fills r and the buffers r points to.
+static void gbgc_finish(const pacc_gbgc_opts& g, int N, const GbgcElem& E, const double* trd, const int8_t* tzb,
+                        const int8_t* mzb, const double* mll, pacc_gbgc_result& r) {
+    const int T = g.burnin + g.mcmc;
+    for (int m = 0; m < 3; m++) {
+        const double* d = trd + (size_t)m * 4 * T;
+        const int8_t* zb = tzb + (size_t)m * T * 2 * N;
+        const int8_t* mz = mzb + (size_t)m * 2 * N;
+        const int8_t* mb = mz + N;
+        r.max_loglik[m] = mll[m];
+        const double ll = gbgc_eval2(m, T, g.burnin, g.mcmc, N, E.nodes, E.missing, d, zb,
+                                     zb + N, 2 * (size_t)N, mz, r.max_loglik[m]);
+        if (m == 0) r.loglik_null = ll;
+        else if (m == 2) r.loglik_res = ll;
+        else r.loglik_all = ll;
+        // Output_init (bpp_c2.cpp:603-660)
+        for (int q = 0; q < 3; q++) {
+            std::vector<double> v(d + (q + 1) * T, d + (q + 2) * T);
+            std::sort(v.begin() + g.burnin, v.end());
+            r.rates[m][q] = v[v.size() / 2];
+        }
+        for (int s = 0; s < N; s++) {
+            int cz[4] = {0, 0, 0, 0}, cb = 0;
+            for (int it = g.burnin; it < T; it++) {
+                cz[zb[(size_t)it * 2 * N + s] + 1]++;
+                cb += zb[(size_t)it * 2 * N + N + s];
+            }
+            if (E.missing[s]) cz[0] = g.mcmc;
+            if (r.post_b) r.post_b[(size_t)m * N + s] = (double)cb / g.mcmc;
+            if (r.post_z)
+                for (int q = 0; q < 4; q++) r.post_z[((size_t)m * N + s) * 4 + q] = (double)cz[q] / g.mcmc;
+            if (r.max_z) r.max_z[(size_t)m * N + s] = mz[s];
+            if (r.max_b) r.max_b[(size_t)m * N + s] = mb[s];
+        }
+        if (r.trace) {
+            const int Wd = 4 + 2 * N;
+            for (int it = 0; it < T; it++) {
+                double* row = r.trace + ((size_t)m * T + it) * Wd;
+                for (int q = 0; q < 4; q++) row[q] = d[(size_t)q * T + it];
+                for (int s = 0; s < N; s++) {
+                    row[4 + s] = zb[(size_t)it * 2 * N + N + s];
+                    row[4 + N + s] = zb[(size_t)it * 2 * N + s];
+                }
+            }
+        }
+    }
+}
+
+
+// ---- gBGC serving (pacc_gbgc_submit / pacc_gbgc_poll / pacc_gbgc_sync) ----
+
+static double gbgc_now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static size_t gbgc_blob_cap(int S, int N, int GGp) {
+    return (size_t)64 * N + (size_t)16 * S + (size_t)S * GGp + 1024;
+}
+
+static size_t gbgc_out_bytes(int N, int T) {
+    return (size_t)3 * 4 * T * 8 + (size_t)3 * T * 2 * N + (size_t)3 * 2 * N + 3 * 8 + 8;
+}
+
+static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) {
+    GbgcServer& v = c->gs;
+    const HostModel& M = c->M;
+    const int S = M.S, N = M.N;
+    v.N = N;
+    v.T = g.burnin + g.mcmc;
+    v.GGp_cap = std::max(512, (GGp_need + 255) & ~255);
+    v.prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
+    v.regs = c->o.register_budget == 168 ? 168 : 96;
+    v.smem = gbgc_chain_smem(N, v.prec);
+    const int per_sm = gbgc_chain_occupancy(v.prec, v.regs, v.smem);
+    if (per_sm <= 0) { c->err = "gbgc serving: the chain kernel does not fit on an SM"; return PACC_ECUDA; }
+    v.grid = c->n_sm * per_sm;
+    v.g = g;
+    v.target.assign(g.target, g.target + g.n_target);
+    v.g.target = v.target.data();
+    v.blob_cap = (gbgc_blob_cap(S, N, v.GGp_cap) + 255) & ~(size_t)255;
+    v.out_b = (gbgc_out_bytes(N, v.T) + 255) & ~(size_t)255;
+    const GbgcWs W = GbgcWs::make(N, S - 1, v.GGp_cap, gbgc_chain_warps(), v.prec ? 4 : 8);
+    // slots: two queued elements per resident CTA, within the memory budget
+    const size_t budget = c->o.memory_budget_bytes > 0 ? (size_t)c->o.memory_budget_bytes : ((size_t)32 << 30);
+    const size_t fixed = W.total * v.grid + 4096;
+    const size_t per_slot = sizeof(GbgcElemHdr) + v.blob_cap + v.out_b;
+    if (budget <= fixed + per_slot) { c->err = "gbgc serving: memory budget too small"; return PACC_OOM; }
+    const size_t want = c->o.max_resident > 0 ? (size_t)c->o.max_resident : (size_t)2 * v.grid;
+    v.ns = (int)std::min<size_t>(want, (budget - fixed) / per_slot);
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_hdr = 0, o_blob = up(sizeof(GbgcElemHdr) * v.ns), o_out = up(o_blob + v.blob_cap * v.ns);
+    // outputs by kind, as the kernel writes them: tr_d [ns][3][4][T], tr_zb [ns][3][T][2][N],
+    // max_zb [ns][3][2][N], max_ll [ns][3], status [ns]
+    const size_t o_trd = o_out, o_tzb = up(o_trd + (size_t)v.ns * 3 * 4 * v.T * 8);
+    const size_t o_mzb = up(o_tzb + (size_t)v.ns * 3 * v.T * 2 * N), o_mll = up(o_mzb + (size_t)v.ns * 3 * 2 * N);
+    const size_t o_st = up(o_mll + (size_t)v.ns * 3 * 8), o_out_end = up(o_st + (size_t)v.ns * 4);
+    const size_t o_tgt = up(o_out_end), o_head = up(o_tgt + N), o_idle = o_head + 128;
+    const size_t o_ws = up(o_head + 256), total = up(o_ws + W.total * v.grid);
+    if (!cuda_ok(c, cudaMalloc((void**)&v.dev, total), "cudaMalloc (gbgc serving)")) return PACC_OOM;
+    if (!cuda_ok(c, cudaMemset(v.dev, 0, o_ws), "memset")) return PACC_ECUDA;
+    std::vector<uint8_t> tgt(N, 0);
+    for (int t : v.target)
+        if (t >= 0 && t < N) tgt[t] = 1;
+    if (!cuda_ok(c, cudaMemcpy(v.dev + o_tgt, tgt.data(), N, cudaMemcpyHostToDevice), "H2D")) return PACC_ECUDA;
+    const size_t map_b = sizeof(int) * (64 + 2 * (size_t)v.ns);
+    if (!cuda_ok(c, cudaHostAlloc((void**)&v.h_map, map_b, cudaHostAllocMapped), "cudaHostAlloc")) return PACC_OOM;
+    std::memset(v.h_map, 0, map_b);
+    int* d_map = nullptr;
+    if (!cuda_ok(c, cudaHostGetDevicePointer((void**)&d_map, v.h_map, 0), "cudaHostGetDevicePointer")) return PACC_ECUDA;
+    v.h_tail = v.h_map;
+    v.h_stop = v.h_map + 1;
+    v.h_qslot = v.h_map + 64;
+    v.h_done = v.h_map + 64 + v.ns;
+    v.h_stage_cap = 8 * (v.blob_cap + sizeof(GbgcElemHdr));
+    v.out_chunk = (int)std::max<size_t>(1, std::min<size_t>(v.ns, ((size_t)256 << 20) / v.out_b));
+    if (!cuda_ok(c, cudaMallocHost((void**)&v.h_stage, v.h_stage_cap), "cudaMallocHost") ||
+        !cuda_ok(c, cudaMallocHost((void**)&v.h_out, v.out_b * v.out_chunk), "cudaMallocHost"))
+        return PACC_OOM;
+    if (!cuda_ok(c, cudaStreamCreateWithFlags(&v.copy, cudaStreamNonBlocking), "stream") ||
+        !cuda_ok(c, cudaEventCreateWithFlags(&v.ev_done, cudaEventDisableTiming), "event") ||
+        !cuda_ok(c, cudaEventCreate(&v.ev0), "event"))
+        return PACC_ECUDA;
+    v.d_hdr = (GbgcElemHdr*)(v.dev + o_hdr);
+    v.d_blob = v.dev + o_blob;
+    v.d_out = v.dev + o_out;
+    v.d_idle = (unsigned long long*)(v.dev + o_idle);
+    GbgcChainParams& p = v.p;
+    std::memset(&p, 0, sizeof(p));
+    p.hdr = v.d_hdr;
+    p.blob = (const uint8_t*)v.d_blob;
+    p.n_elem = v.ns;
+    p.T = v.T; p.burn = g.burnin; p.mcmc = g.mcmc; p.seed = g.seed;
+    p.conserve_rate = g.conserve_rate; p.acce_rate = g.acce_rate; p.init_gc = g.init_gc;
+    p.ca = g.conserve_prior_a; p.cb = g.conserve_prior_b;
+    p.na = g.acce_prior_a; p.nb = g.acce_prior_b; p.nshift = g.acce_prior_shift;
+    p.gca = g.gc_prior_a; p.gcb = g.gc_prior_b; p.gcc = g.gc_prior_c;
+    p.lrate = g.prep_lrate; p.grate = g.prep_grate; p.c2m = g.cons_to_mis; p.nc2m = g.ncons_to_mis;
+    p.prop_c = g.prop_c; p.prop_n = g.prop_n; p.prop_gc = g.prop_gc;
+    std::memcpy(p.Q0, M.rate, sizeof(p.Q0));
+    std::memcpy(p.pi, M.pi, sizeof(p.pi));
+    p.target = (const uint8_t*)(v.dev + o_tgt);
+    p.ws = v.dev + o_ws;
+    p.ws_stride = W.total;
+    p.N_max = N; p.n_int_max = S - 1; p.GGp_max = v.GGp_cap;
+    p.tr_d = (double*)(v.dev + o_trd);
+    p.tr_zb = (int8_t*)(v.dev + o_tzb);
+    p.max_zb = (int8_t*)(v.dev + o_mzb);
+    p.max_ll = (double*)(v.dev + o_mll);
+    p.status = (int32_t*)(v.dev + o_st);
+    p.stream = 1;
+    p.q_head = (int*)(v.dev + o_head);
+    p.q_tail = d_map;
+    p.q_stop = d_map + 1;
+    p.q_slot = d_map + 64;
+    p.q_cap = v.ns;
+    p.done_flag = d_map + 64 + v.ns;
+    p.idle_ns = c->o.serve_idle_ns > 0 ? c->o.serve_idle_ns : 30000000000ll;
+    p.idle_exits = v.d_idle;
+    v.free_slots.clear();
+    for (int i = v.ns - 1; i >= 0; i--) v.free_slots.push_back(i);
+    v.busy.assign(v.ns, 0);
+    v.slot_no.assign(v.ns, 0);
+    v.slot_t0.assign(v.ns, 0);
+    v.slot_elem.assign(v.ns, GbgcElem());
+    v.tail = 0;
+    v.resident = 0;
+    v.ready = true;
+    return PACC_OK;
+}
+
+// Admit queued elements into free slots, publish them, and (re)launch the
+// persistent kernel when it is not running.
+static int gbgc_pump(pacc_ctx* c) {
+    GbgcServer& v = c->gs;
+    while (!v.free_slots.empty() && !v.queue.empty()) {
+        // one staging round: up to 8 elements
+        std::vector<int> adm;
+        size_t off = 0;
+        while (!v.free_slots.empty() && !v.queue.empty() && adm.size() < 8) {
+            GbgcServer::Pending& q = v.queue.front();
+            const int slot = v.free_slots.back();
+            v.free_slots.pop_back();
+            q.H.blob_off = (int64_t)slot * (int64_t)v.blob_cap;
+            std::memcpy(v.h_stage + off, &q.H, sizeof(GbgcElemHdr));
+            std::memcpy(v.h_stage + off + sizeof(GbgcElemHdr), q.blob.data(), q.blob.size());
+            bool ok = cuda_ok(c, cudaMemcpyAsync(v.d_blob + (size_t)slot * v.blob_cap, v.h_stage + off + sizeof(GbgcElemHdr),
+                                                 q.blob.size(), cudaMemcpyHostToDevice, v.copy), "H2D (gbgc admission)") &&
+                      cuda_ok(c, cudaMemcpyAsync(v.d_hdr + slot, v.h_stage + off, sizeof(GbgcElemHdr),
+                                                 cudaMemcpyHostToDevice, v.copy), "H2D (gbgc admission)");
+            if (!ok) return PACC_ECUDA;
+            off += (sizeof(GbgcElemHdr) + q.blob.size() + 255) & ~(size_t)255;
+            v.slot_no[slot] = q.no;
+            v.slot_t0[slot] = q.t0;
+            q.E.masks.clear();
+            q.E.masks.shrink_to_fit();
+            v.slot_elem[slot] = std::move(q.E);
+            v.busy[slot] = 1;
+            adm.push_back(slot);
+            v.queue.pop_front();
+        }
+        if (!cuda_ok(c, cudaStreamSynchronize(v.copy), "gbgc admission")) return PACC_ECUDA;
+        for (int slot : adm) {
+            v.h_done[slot] = 0;
+            v.h_qslot[v.tail % v.ns] = slot;
+            v.tail++;
+        }
+        __sync_synchronize();
+        *v.h_tail = v.tail;
+        v.resident += (int)adm.size();
+    }
+    if (v.resident > 0) {
+        const bool exited = v.running && cudaEventQuery(v.ev_done) == cudaSuccess;
+        if (!v.running || exited) {
+            *v.h_stop = 0;
+            if (!cuda_ok(c, cudaEventRecord(v.ev0, c->stream), "event") ||
+                !cuda_ok(c, launch_gbgc_chain(v.p, v.grid, v.smem, v.prec, v.regs, c->stream), "gbgc serving launch") ||
+                !cuda_ok(c, cudaEventRecord(v.ev_done, c->stream), "event"))
+                return PACC_ECUDA;
+            v.running = true;
+            v.launches++;
+        }
+    }
+    return PACC_OK;
+}
+
+// Collect finished slots: their outputs to the host, Eval2 and the tables.
+static int gbgc_collect(pacc_ctx* c) {
+    GbgcServer& v = c->gs;
+    std::vector<int> fin;
+    for (int s = 0; s < v.ns; s++)
+        if (v.busy[s] && v.h_done[s]) fin.push_back(s);
+    const int N = v.N, T = v.T;
+    for (size_t a = 0; a < fin.size(); a += v.out_chunk) {
+        const size_t nb = std::min(fin.size() - a, (size_t)v.out_chunk);
+        const size_t b_trd = (size_t)3 * 4 * T * 8, b_tzb = (size_t)3 * T * 2 * N, b_mzb = (size_t)3 * 2 * N;
+        for (size_t k = 0; k < nb; k++) {
+            const size_t sl = (size_t)fin[a + k];
+            char* h = v.h_out + k * v.out_b;
+            const bool ok =
+                cuda_ok(c, cudaMemcpyAsync(h, (const char*)v.p.tr_d + sl * b_trd, b_trd, cudaMemcpyDeviceToHost, v.copy), "D2H") &&
+                cuda_ok(c, cudaMemcpyAsync(h + b_trd, (const char*)v.p.tr_zb + sl * b_tzb, b_tzb, cudaMemcpyDeviceToHost, v.copy), "D2H") &&
+                cuda_ok(c, cudaMemcpyAsync(h + b_trd + b_tzb, (const char*)v.p.max_zb + sl * b_mzb, b_mzb, cudaMemcpyDeviceToHost, v.copy), "D2H") &&
+                cuda_ok(c, cudaMemcpyAsync(h + b_trd + b_tzb + b_mzb, (const char*)v.p.max_ll + sl * 24, 24, cudaMemcpyDeviceToHost, v.copy), "D2H");
+            if (!ok) return PACC_ECUDA;
+        }
+        if (!cuda_ok(c, cudaStreamSynchronize(v.copy), "gbgc results")) return PACC_ECUDA;
+        std::vector<GbgcServer::Done> got(nb);
+        const double t_done = gbgc_now();
+        auto work = [&](size_t k) {
+            const int slot = fin[a + k];
+            GbgcServer::Done& d = got[k];
+            std::memset(&d.r, 0, sizeof(d.r));
+            d.max_z.resize(3 * N);
+            d.max_b.resize(3 * N);
+            d.post_b.resize(3 * N);
+            d.post_z.resize(12 * N);
+            d.r.max_z = d.max_z.data();
+            d.r.max_b = d.max_b.data();
+            d.r.post_b = d.post_b.data();
+            d.r.post_z = d.post_z.data();
+            const char* o = v.h_out + k * v.out_b;
+            const double* trd = (const double*)o;
+            const int8_t* tzb = (const int8_t*)(o + (size_t)3 * 4 * T * 8);
+            const int8_t* mzb = tzb + (size_t)3 * T * 2 * N;
+            double mll[3];
+            std::memcpy(mll, mzb + (size_t)3 * 2 * N, sizeof(mll));
+            d.r.element_no = v.slot_no[slot];
+            d.r.status = PACC_OK;
+            d.r.root = v.slot_elem[slot].root;
+            gbgc_finish(v.g, N, v.slot_elem[slot], trd, tzb, mzb, mll, d.r);
+            d.r.device_ms = (t_done - v.slot_t0[slot]) * 1e3;   // submit to collection
+            d.r.max_z = nullptr; d.r.max_b = nullptr; d.r.post_b = nullptr; d.r.post_z = nullptr;
+        };
+        const int nth = std::max(1, std::min((int)nb, std::min(16, (int)std::thread::hardware_concurrency())));
+        std::atomic<size_t> next(0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; t++)
+            th.emplace_back([&]() { for (size_t k = next++; k < nb; k = next++) work(k); });
+        for (auto& t : th) t.join();
+        for (size_t k = 0; k < nb; k++) {
+            const int slot = fin[a + k];
+            v.done.push_back(std::move(got[k]));
+            v.busy[slot] = 0;
+            v.h_done[slot] = 0;
+            v.free_slots.push_back(slot);
+            v.resident--;
+        }
+    }
+    return PACC_OK;
+}
+
+
+static void gbgc_serve_teardown(pacc_ctx* c) {
+    GbgcServer& v = c->gs;
+    if (!v.ready) return;
+    if (v.h_stop) *v.h_stop = 1;
+    cudaStreamSynchronize(c->stream);
+    if (v.dev) cudaFree(v.dev);
+    if (v.h_map) cudaFreeHost(v.h_map);
+    if (v.h_stage) cudaFreeHost(v.h_stage);
+    if (v.h_out) cudaFreeHost(v.h_out);
+    if (v.copy) cudaStreamDestroy(v.copy);
+    if (v.ev_done) cudaEventDestroy(v.ev_done);
+    if (v.ev0) cudaEventDestroy(v.ev0);
+    std::deque<GbgcServer::Done> keep = std::move(v.done);
+    const long long launches = v.launches;
+    v = GbgcServer();
+    v.done = std::move(keep);
+    v.launches = launches;
+}
+
+static bool gbgc_same_opts(const pacc_gbgc_opts& a, const GbgcServer& v) {
+    pacc_gbgc_opts x = a, y = v.g;
+    x.target = nullptr; y.target = nullptr;
+    if (std::memcmp(&x, &y, sizeof(x)) != 0) return false;
+    if (a.n_target != (int)v.target.size()) return false;
+    for (int i = 0; i < a.n_target; i++)
+        if (a.target[i] != v.target[i]) return false;
     return true;
 }
 
@@ -1011,6 +1387,7 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->gpu_ok && c->stream) {
         cudaSetDevice(c->device);
         if (c->ss.h_stop) *c->ss.h_stop = 1;   // idle serving blocks return
+        if (c->gs.h_stop) *c->gs.h_stop = 1;
         cudaStreamSynchronize(c->stream);      // a serving launch may still be in flight
     }
     {
@@ -1028,6 +1405,13 @@ void pacc_destroy(pacc_ctx* c) {
     if (c->srv.h_stage) cudaFreeHost(c->srv.h_stage);
     if (c->srv.ev0) cudaEventDestroy(c->srv.ev0);
     if (c->srv.ev1) cudaEventDestroy(c->srv.ev1);
+    if (c->gs.dev) cudaFree(c->gs.dev);
+    if (c->gs.h_map) cudaFreeHost(c->gs.h_map);
+    if (c->gs.h_stage) cudaFreeHost(c->gs.h_stage);
+    if (c->gs.h_out) cudaFreeHost(c->gs.h_out);
+    if (c->gs.copy) cudaStreamDestroy(c->gs.copy);
+    if (c->gs.ev_done) cudaEventDestroy(c->gs.ev_done);
+    if (c->gs.ev0) cudaEventDestroy(c->gs.ev0);
     if (c->ss.dev) cudaFree(c->ss.dev);
     if (c->ss.h_map) cudaFreeHost(c->ss.h_map);
     if (c->ss.h_stage) cudaFreeHost(c->ss.h_stage);
@@ -2745,6 +3129,128 @@ void pacc_gbgc_default_opts(pacc_gbgc_opts* o) {
     o->prop_c = 1.2; o->prop_n = 1.2; o->prop_gc = 0.2;
 }
 
+
+int pacc_gbgc_sync(pacc_ctx* c) {
+    if (!c) return PACC_EINVAL;
+    GbgcServer& v = c->gs;
+    if (!v.ready) return PACC_OK;
+    cudaSetDevice(c->device);
+    while (v.resident > 0 || !v.queue.empty()) {
+        int st = gbgc_collect(c);
+        if (st == PACC_OK) st = gbgc_pump(c);
+        if (st != PACC_OK) return st;
+        if (v.running) {
+            const cudaError_t e = cudaEventQuery(v.ev_done);
+            if (e != cudaSuccess && e != cudaErrorNotReady) return cuda_ok(c, e, "gbgc serving launch") ? PACC_OK : PACC_ECUDA;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    return PACC_OK;
+}
+
+int pacc_gbgc_submit(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batch* b) {
+    if (!c) return PACC_EINVAL;
+    if (!go || !b || b->n_elements < 0 || (b->n_elements > 0 && (!b->lengths || !b->offsets || !b->bases))) {
+        c->err = "gbgc_submit: options and batch must be non-null";
+        return PACC_EINVAL;
+    }
+    if (go->burnin < 0 || go->mcmc < 2 || go->prop_c <= 1 || go->prop_n <= 1 || go->prop_gc <= 0) {
+        c->err = "gbgc_submit: burnin >= 0, mcmc >= 2, prop_c and prop_n > 1, prop_gc > 0";
+        return PACC_EINVAL;
+    }
+    if (!c->gpu_ok) { c->err = "gbgc_submit: no usable GPU"; return PACC_ECUDA; }
+    cudaSetDevice(c->device);
+    GbgcServer& v = c->gs;
+    const HostModel& M = c->M;
+    const int n = b->n_elements;
+    const double t0 = gbgc_now();
+    std::vector<GbgcServer::Pending> pend(n);
+    {
+        const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+        std::atomic<int> next(0);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; t++)
+            th.emplace_back([&]() {
+                for (int i = next++; i < n; i = next++) {
+                    GbgcServer::Pending& q = pend[i];
+                    gbgc_prepare(M, b->bases + b->offsets[i], b->lengths[i], (char)go->gapchar, go->missing_thres,
+                                 go->conserve_prop, q.E);
+                    if (!q.E.filtered) {
+                        int nint = 0;
+                        for (int s2 : q.E.nodes) nint += s2 >= M.S;
+                        if (nint == 0) q.E.filtered = 2;
+                    }
+                    if (!q.E.filtered) gbgc_blob(M, q.E, q.H, q.blob);
+                    q.no = b->element_no ? b->element_no[i] : i;
+                    q.t0 = t0;
+                    q.filtered = q.E.filtered;
+                }
+            });
+        for (auto& t : th) t.join();
+    }
+    int GGp_need = 32;
+    for (auto& q : pend)
+        if (!q.filtered) GGp_need = std::max(GGp_need, q.E.GGp);
+    const int prec = (c->o.precision == PACC_FP32 || c->o.precision == PACC_FP32_WARP) ? 1 : 0;
+    if (v.ready && (!gbgc_same_opts(*go, v) || GGp_need > v.GGp_cap || prec != v.prec)) {
+        const int st = pacc_gbgc_sync(c);   // the running elements finish under the old set-up
+        if (st != PACC_OK) return st;
+        gbgc_serve_teardown(c);
+    }
+    if (!v.ready) {
+        const int st = gbgc_serve_setup(c, *go, GGp_need);
+        if (st != PACC_OK) return st;
+    }
+    for (auto& q : pend) {
+        if (q.filtered) {
+            GbgcServer::Done d;
+            std::memset(&d.r, 0, sizeof(d.r));
+            d.r.element_no = q.no;
+            d.r.status = PACC_FILTERED;
+            d.r.root = -1;
+            v.done.push_back(std::move(d));
+        } else {
+            v.queue.push_back(std::move(q));
+        }
+    }
+    return gbgc_pump(c);
+}
+
+int pacc_gbgc_poll(pacc_ctx* c, pacc_gbgc_result* out, int max) {
+    if (!c || (max > 0 && !out)) return PACC_EINVAL;
+    GbgcServer& v = c->gs;
+    if (v.ready) {
+        cudaSetDevice(c->device);
+        int st = gbgc_collect(c);
+        if (st == PACC_OK) st = gbgc_pump(c);
+        if (st != PACC_OK) return st;
+        if (v.running) {
+            const cudaError_t e = cudaEventQuery(v.ev_done);
+            if (e != cudaSuccess && e != cudaErrorNotReady) return cuda_ok(c, e, "gbgc serving launch") ? 0 : PACC_ECUDA;
+        }
+    }
+    int k = 0;
+    const int N = c->M.N;
+    while (k < max && !v.done.empty()) {
+        GbgcServer::Done& d = v.done.front();
+        pacc_gbgc_result& r = out[k];
+        int32_t* mz = r.max_z;
+        int8_t* mb = r.max_b;
+        double *pb = r.post_b, *pz = r.post_z;
+        r = d.r;
+        r.max_z = mz; r.max_b = mb; r.post_b = pb; r.post_z = pz; r.trace = nullptr;
+        if (d.r.status == PACC_OK) {
+            if (mz) std::memcpy(mz, d.max_z.data(), sizeof(int32_t) * 3 * N);
+            if (mb) std::memcpy(mb, d.max_b.data(), 3 * N);
+            if (pb) std::memcpy(pb, d.post_b.data(), sizeof(double) * 3 * N);
+            if (pz) std::memcpy(pz, d.post_z.data(), sizeof(double) * 12 * N);
+        }
+        v.done.pop_front();
+        k++;
+    }
+    return k;
+}
+
 int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batch* b, pacc_gbgc_result* out) {
     if (!c) return PACC_EINVAL;
     if (!go || !b || !out || b->n_elements < 0 || (b->n_elements > 0 && (!b->lengths || !b->offsets || !b->bases))) {
@@ -2891,48 +3397,8 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
                     const int i = run[c0 + k];
                     pacc_gbgc_result& r = out[i];
                     r.device_ms = ms / nc;
-                    for (int m = 0; m < 3; m++) {
-                        const double* d = trd.data() + ((size_t)k * 3 + m) * 4 * T;
-                        const int8_t* zb = tzb.data() + ((size_t)k * 3 + m) * T * 2 * N;
-                        const int8_t* mz = mzb.data() + (((size_t)k * 3 + m) * 2) * N;
-                        const int8_t* mb = mz + N;
-                        r.max_loglik[m] = mll[(size_t)k * 3 + m];
-                        const double ll = gbgc_eval2(m, T, go->burnin, go->mcmc, N, E[i].nodes, E[i].missing, d, zb,
-                                                     zb + N, 2 * (size_t)N, mz, r.max_loglik[m]);
-                        if (m == 0) r.loglik_null = ll;
-                        else if (m == 2) r.loglik_res = ll;
-                        else r.loglik_all = ll;
-                        // Output_init (bpp_c2.cpp:603-660)
-                        for (int q = 0; q < 3; q++) {
-                            std::vector<double> v(d + (q + 1) * T, d + (q + 2) * T);
-                            std::sort(v.begin() + go->burnin, v.end());
-                            r.rates[m][q] = v[v.size() / 2];
-                        }
-                        for (int s = 0; s < N; s++) {
-                            int cz[4] = {0, 0, 0, 0}, cb = 0;
-                            for (int it = go->burnin; it < T; it++) {
-                                cz[zb[(size_t)it * 2 * N + s] + 1]++;
-                                cb += zb[(size_t)it * 2 * N + N + s];
-                            }
-                            if (E[i].missing[s]) cz[0] = go->mcmc;
-                            if (r.post_b) r.post_b[(size_t)m * N + s] = (double)cb / go->mcmc;
-                            if (r.post_z)
-                                for (int q = 0; q < 4; q++) r.post_z[((size_t)m * N + s) * 4 + q] = (double)cz[q] / go->mcmc;
-                            if (r.max_z) r.max_z[(size_t)m * N + s] = mz[s];
-                            if (r.max_b) r.max_b[(size_t)m * N + s] = mb[s];
-                        }
-                        if (r.trace) {
-                            const int Wd = 4 + 2 * N;
-                            for (int it = 0; it < T; it++) {
-                                double* row = r.trace + ((size_t)m * T + it) * Wd;
-                                for (int q = 0; q < 4; q++) row[q] = d[(size_t)q * T + it];
-                                for (int s = 0; s < N; s++) {
-                                    row[4 + s] = zb[(size_t)it * 2 * N + N + s];
-                                    row[4 + N + s] = zb[(size_t)it * 2 * N + s];
-                                }
-                            }
-                        }
-                    }
+                    gbgc_finish(*go, N, E[i], trd.data() + (size_t)k * 3 * 4 * T, tzb.data() + (size_t)k * tzb_el,
+                                mzb.data() + (size_t)k * 3 * 2 * N, mll.data() + (size_t)k * 3, r);
                 }
             });
         for (auto& t : th) t.join();

@@ -167,3 +167,43 @@ def test_gbgc_cli_matches_reference(built, tmp_path, case):
         got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
         assert got.shape[0] == T
         np.testing.assert_allclose(got, tr[key], rtol=2e-7, atol=1e-300, err_msg=key)
+
+
+def test_gbgc_served_equals_batch(built):
+    """The serving form (pacc_gbgc_submit / poll / sync): every element
+    served equals the same element run by pacc_gbgc_run, bit for bit, with
+    the elements split over two submits, fewer slots than elements (eight),
+    and a 0.1 ms idle bound between the submits (the blocks
+    leave, the next submit launches again)."""
+    import time
+    from phyloacc_gb300 import abi, synth
+    ds = synth.make_dataset("st43", n_elements=40, seed=9)
+    o = abi.gbgc_default_opts(ds.target)
+    o.burnin, o.mcmc, o.seed, o.gapchar = 20, 60, 5, ord("-")
+    ref = {r["element_no"]: r for r in _ctx(ds, 1).gbgc_run(o)}
+    from phyloacc_gb300 import Context
+    so = abi.default_opts()
+    so.precision = 1
+    so.serve_idle_ns = 100000
+    so.max_resident = 8
+    ctx = Context(ds, so)
+    ctx.gbgc_submit(o, elements=range(0, 25))
+    got = []
+    while len(got) < 25:
+        got += ctx.gbgc_poll()
+        time.sleep(0.01)
+    time.sleep(0.05)                       # idle: the serving blocks leave
+    ctx.gbgc_submit(o, elements=range(25, 40))
+    ctx.gbgc_sync()
+    got += ctx.gbgc_poll()
+    assert sorted(r["element_no"] for r in got) == list(range(40))
+    for r in got:
+        w = ref[r["element_no"]]
+        assert r["status"] == w["status"]
+        if r["status"] != 0:
+            continue
+        for k in ("loglik_null", "loglik_res", "loglik_all"):
+            assert r[k] == w[k] or (np.isnan(r[k]) and np.isnan(w[k])), (r["element_no"], k)
+        assert (r["max_loglik"] == w["max_loglik"]).all() and (r["rates"] == w["rates"]).all()
+        for k in ("max_z", "max_b", "post_b", "post_z"):
+            assert (r[k] == w[k]).all(), (r["element_no"], k)
