@@ -41,7 +41,9 @@ gbgc      = the gBGC model's configuration (PhyloAcc-ST-GBGC): 120-taxon Yule
             Eval2 and the rate / B / Z tables.  A step is one pacc_gbgc_run of
             --gbgc-elements elements from host buffers (value: device time; e2e:
             wall time incl. preprocessing, H2D, D2H of the traces and the host's
-            Eval2); FP32 partials, with an FP64-partial leg on the same batch
+            Eval2); FP32 partials served (the K steps' batches submitted at
+            once to the persistent kernel, elements admitted as slots free up;
+            --gbgc-batched: one launch per step), with an FP64-partial leg on the same batch
             over 40 + 160 iterations, scaled to 1,000; cpu_baseline: the oracle on one element per host core,
             OpenMP over elements, over a bounded chain scaled to 1,000 iterations
 cpu_baseline and --impl reference run the CPU oracle (the restatement of
@@ -546,16 +548,55 @@ def run_gbgc(args, K, ws, rank):
     if args.gbgc_burnin is not None:
         g.burnin, g.mcmc = args.gbgc_burnin, args.gbgc_mcmc
     out = {"workload": GBGC_WORKLOAD, "metric": "posterior elements/sec (gBGC model, 120 taxa)",
-           "unit": "elements/s", "elements_per_step": E, "steps": K, "warmup": "one 8-element, 10-iteration run",
-           "path": "one CTA per element (persistent, longest element first); FP64 Pade branch matrices; "
-                   "FP32 partials"}
+           "unit": "elements/s", "elements_per_step": E, "steps": K,
+           "warmup": "served: the 8 longest elements once; batched: one 8-element, 10-iteration run",
+           "path": "one CTA per element, persistent kernel fed from a host queue (served) or over one "
+                   "batch's queue (batched, longest first); FP64 Pade branch matrices; FP32 partials"}
+    # FP32 partials, served: the K steps' batches submitted at once to the
+    # serving kernel (elements admitted as slots free up, so no batch waits
+    # for another's tail); value = elements / device time of the launches,
+    # e2e = elements / wall time from submit to the last poll
+    if not args.gbgc_batched:
+        o = abi.default_opts()
+        o.precision = abi.PACC_FP32
+        ctx = pg.Context(ds, o)
+        longest = list(np.argsort(-ds.lengths)[:8])
+        ctx.gbgc_submit(g, elements=longest)         # warm-up: slots sized for the longest element
+        ctx.gbgc_sync()
+        ctx.gbgc_poll()
+        barrier(ws)
+        k0 = ctx.counters()["kernel_ms"]
+        t = time.perf_counter()
+        for _ in range(K):
+            ctx.gbgc_submit(g)
+        got = []
+        while len(got) < K * E:
+            got += ctx.gbgc_poll()
+            if len(got) < K * E:
+                time.sleep(0.005)
+        ctx.gbgc_sync()
+        wall = reduce_max(ws, time.perf_counter() - t)
+        dev = reduce_max(ws, (ctx.counters()["kernel_ms"] - k0) * 1e-3)
+        ctx.close()
+        T = g.burnin + g.mcmc
+        lat = np.array([r["device_ms"] for r in got])
+        out["fp32"] = {"value": ws * K * E / dev, "unit": "elements/s", "elements_per_step": E, "steps": K,
+                       "iterations": T, "ms_per_step": dev / K * 1e3, "path": "served (pacc_gbgc_submit / poll)",
+                       "e2e": {"value": ws * K * E / wall, "unit": "elements/s",
+                               "h2d_bytes_per_step": int(ds.bases.nbytes + ds.lengths.nbytes + ds.offsets.nbytes),
+                               "d2h_bytes_per_step": int(E * 3 * T * (4 * 8 + 2 * ds.tree.n_nodes))},
+                       "filtered": int(sum(1 for x in got if x["status"] != 0)) // K,
+                       "latency_submit_to_result_ms": {"p50": float(np.percentile(lat, 50)),
+                                                       "p99": float(np.percentile(lat, 99))}}
     # FP64 partials: the same batch on chains of a fifth of the length (the
     # cost of an iteration does not change along the chain), scaled to 1,000
     g64 = abi.gbgc_default_opts(ds.target)
     g64.seed, g64.burnin, g64.mcmc = 1, 40, 160
     legs = (("fp32", abi.PACC_FP32, g, K), ("fp64", abi.PACC_FP64, g64, 1))
+    if not args.gbgc_batched:
+        legs = legs[1:]
     if args.gbgc_fp32_only:
-        legs = legs[:1]
+        legs = [l for l in legs if l[0] == "fp32"]
     for name, prec, gg, steps in legs:
         o = abi.default_opts()
         o.precision = prec
@@ -644,6 +685,8 @@ def main():
                     help="elements per step of the gBGC leg (0: skip; default five chains per SM)")
     ap.add_argument("--gbgc-only", action="store_true", help="profiling: run only the gBGC leg, print it")
     ap.add_argument("--gbgc-fp32-only", action="store_true", help="profiling: skip the gBGC FP64 leg")
+    ap.add_argument("--gbgc-batched", action="store_true",
+                    help="gBGC FP32 leg as one pacc_gbgc_run per step instead of served (the form ncu replays)")
     ap.add_argument("--gbgc-burnin", type=int, default=None, help="profiling only: shorter gBGC chains")
     ap.add_argument("--gbgc-mcmc", type=int, default=None, help="profiling only: shorter gBGC chains")
     ap.add_argument("--block-threads", type=int, default=0,

@@ -1007,7 +1007,7 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
         !cuda_ok(c, cudaMallocHost((void**)&v.h_out, v.out_b * v.out_chunk), "cudaMallocHost"))
         return PACC_OOM;
     if (!cuda_ok(c, cudaStreamCreateWithFlags(&v.copy, cudaStreamNonBlocking), "stream") ||
-        !cuda_ok(c, cudaEventCreateWithFlags(&v.ev_done, cudaEventDisableTiming), "event") ||
+        !cuda_ok(c, cudaEventCreate(&v.ev_done), "event") ||
         !cuda_ok(c, cudaEventCreate(&v.ev0), "event"))
         return PACC_ECUDA;
     v.d_hdr = (GbgcElemHdr*)(v.dev + o_hdr);
@@ -1100,7 +1100,12 @@ static int gbgc_pump(pacc_ctx* c) {
     }
     if (v.resident > 0) {
         const bool exited = v.running && cudaEventQuery(v.ev_done) == cudaSuccess;
-        if (!v.running || exited) {
+        if (exited) {   // the blocks left on the idle bound: count the launch's time
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, v.ev0, v.ev_done) == cudaSuccess) c->counters.kernel_ms += ms;
+            v.running = false;
+        }
+        if (!v.running) {
             *v.h_stop = 0;
             if (!cuda_ok(c, cudaEventRecord(v.ev0, c->stream), "event") ||
                 !cuda_ok(c, launch_gbgc_chain(v.p, v.grid, v.smem, v.prec, v.regs, c->stream), "gbgc serving launch") ||
@@ -3144,6 +3149,14 @@ int pacc_gbgc_sync(pacc_ctx* c) {
             if (e != cudaSuccess && e != cudaErrorNotReady) return cuda_ok(c, e, "gbgc serving launch") ? PACC_OK : PACC_ECUDA;
         }
         std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    // nothing left: the blocks return now, and the launch's time is counted
+    if (v.running) {
+        *v.h_stop = 1;
+        float ms = 0;
+        if (!cuda_ok(c, cudaEventSynchronize(v.ev_done), "gbgc serving launch")) return PACC_ECUDA;
+        if (cudaEventElapsedTime(&ms, v.ev0, v.ev_done) == cudaSuccess) c->counters.kernel_ms += ms;
+        v.running = false;
     }
     return PACC_OK;
 }
