@@ -236,7 +236,11 @@ typedef struct pacc_counters {
                                       Z-change likelihood, accelerated-rate MH, conserved-rate MH,
                                       transitions.  Warp kernel: internal-base pass, emission sums, Z
                                       filter, Z-change likelihood, accelerated-rate MH, conserved-rate
-                                      MH, monitor/transitions, model init + Eval2 + output */
+                                      MH, monitor/transitions, model init + Eval2 + output.
+                                      gBGC chain (pacc_gbgc_run): monitor + model set-up, expected
+                                      counts, initial_prob_back, branch matrices of the rate
+                                      proposals, the rest of sample_rates, Update_ZB, pruning,
+                                      ELBO + update_rates' MH */
     double serve_idle_exits;       /* serving (CTA layout): blocks that left a launch on the idle bound */
 } pacc_counters;
 int pacc_get_counters(pacc_ctx* ctx, pacc_counters* out);

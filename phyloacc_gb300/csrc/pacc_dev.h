@@ -251,7 +251,7 @@ struct GbgcElemHdr {
     int32_t o_hlev, o_hnodes;        // internal nodes by height: starts [n_hlev + 1], nodes
     int32_t o_dlev, o_dnodes;        // non-root nodes by depth: starts [n_dlev + 1], nodes
     int32_t o_masks;                 // uint8 [S][GGp] allowed bases
-    int32_t pad;
+    int32_t o_blen, n_blen;          // int16: the branches that are not missing, by length
     int64_t blob_off;
 };
 
@@ -313,6 +313,7 @@ struct GbgcChainParams {
     const volatile int* q_stop;      // host-mapped: nonzero asks idle blocks to return
     long long idle_ns;               // a block idle this long returns even without q_stop
     unsigned long long* idle_exits;  // blocks that left on the idle bound
+    unsigned long long* phase;       // [8] cycles per phase (summed over elements), or null
 };
 
 }  // namespace pacc

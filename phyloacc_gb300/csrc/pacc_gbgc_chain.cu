@@ -155,6 +155,17 @@ __device__ __forceinline__ double block_warp_sum(double v) {
     return v;
 }
 
+// log of the Gamma(a, scale b) density (the gsl_ran_gamma_pdf terms of
+// sample_rates and MonitorChain, bpp_c.cpp:913-925, 620-642) with lgamma(a)
+// and a log(b) computed once: the same terms, in the same order, as
+// log_gamma_pdf.
+__device__ __noinline__ double lgpdf(double x, double a, double b, double lga, double alb) {
+    if (x < 0) return -CUDART_INF;
+    if (x == 0) return (a == 1) ? d_log(1.0 / b) : -CUDART_INF;
+    const double t = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a - 1, d_log(x)), __ddiv_rn(x, b)), lga), alb);
+    return d_log(d_exp(t));
+}
+
 template <typename Real>
 __device__ __forceinline__ Real warp_sum_real(Real v) {
 #pragma unroll
@@ -166,6 +177,9 @@ __device__ __forceinline__ Real warp_sum_real(Real v) {
 struct GbgcScalars {
     double tm[2][3][3], lt[2][3][3];   // Z transition [outgroup path][child Z][parent Z] and its log
     double ec_gc[2], ec_mis[2];        // emission constants: log(1 - c) / log(c); log(1 - cons2mis) / log(1 - ncons2mis)
+    double lmis[4];                    // log(1 - ncons2mis), log(1 - cons2mis), log(ncons2mis), log(cons2mis)
+    double pr_lg[3], pr_alb[3];        // lgamma(a) and a log(b) of the conserved, accelerated and GC-bias priors
+    int n_all, n_free;                 // branch lists of the model (by length): all, not fixed
     double logpZC, logp_Z, MaxLoglik;
     double tl, tl_next, full;          // trace_loglik[m], trace_loglik[m + 1], trace_full_loglik[m]
     double r_n, r_c, r_gb;             // rates of iteration m
@@ -190,6 +204,8 @@ struct GbgcCtx {
     Real* Pcur;
     double *pw, *qn;
     int8_t *Z, *B, *fixZ, *Zp, *Bp, *MZ, *MB;
+    int16_t *lst_all, *lst_free;   // the model's branches (not missing) by length: all / not fixed
+    int nall, nfree;
     __device__ bool missing(int s) const { return flags[s] & GBGC_MISSING; }
     __device__ int upper(int s) const { return (flags[s] & GBGC_UPPER) ? 1 : 0; }
     __device__ int slot(int cls, int set) const { return cls == 0 ? 0 : 1 + 5 * set + (cls - 1); }
@@ -244,10 +260,18 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
         }
         __syncthreads();
     }
-    const int nb = G.nn - 1;
-    for (int it = tid; it < nc * nb; it += blockDim.x) {
-        const int ci = it / nb, s = G.nodes[it - ci * nb];
-        if (G.missing(s) || (cls[ci] % 3 == 2 && G.fixZ[s] == 1)) continue;
+    // work items: each class over its branch list (the neutral classes skip
+    // fixed branches), branches by length so a warp's lanes choose the same
+    // Padé degree
+    int cnt[5], tot = 0;
+    for (int i = 0; i < nc; i++) {
+        cnt[i] = (cls[i] % 3 == 2) ? G.nfree : G.nall;
+        tot += cnt[i];
+    }
+    for (int it = tid; it < tot; it += blockDim.x) {
+        int ci = 0, k = it;
+        while (k >= cnt[ci]) { k -= cnt[ci]; ci++; }
+        const int s = (cls[ci] % 3 == 2) ? G.lst_free[k] : G.lst_all[k];
         double E[16];
         pade_branch(G.pw + ci * 13 * 16, G.qn[ci], G.dist[s], E);
         const int sl = G.slot(cls[ci], set);
@@ -456,65 +480,98 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
     __syncthreads();
 }
 
+// Reduce-scatter of 16 values across a warp by recursive halving (16
+// shuffles): afterwards lane l holds the warp's sum of value (l >> 1) & 15
+// (lanes 2i and 2i + 1 both hold sum i).  The order of the additions depends
+// only on the lane numbers.
+template <typename Real>
+__device__ __forceinline__ Real warp_reduce_scatter16(Real* v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16, h = 8; o >= 2; o >>= 1, h >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; i++) {
+            const Real send = up ? v[i] : v[i + h];
+            const Real keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
 // Update_Tg with sampling over every column from partial buffer buf (its
 // internal partials are replaced by marginals): expected counts into dst.
+// Nodes top-down in the outer loop and a thread's columns in the inner one:
+// a node's joint counts are summed over the thread's columns in registers,
+// then once over the warp (reduce-scatter) into the warp's slice, and the
+// slices are summed in warp order.  Column g stays on thread g mod blockDim,
+// so the parent's marginal a thread reads is one it wrote itself.
 template <typename Real>
 __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf, Real* dst) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double* wc = G.wc + (size_t)w * G.N * 16;
     for (int i = lane; i < G.N * 16; i += 32) wc[i] = 0;
     __syncwarp();
-    for (int g0 = w * 32; g0 < G.GGp; g0 += GB_WARPS * 32) {
-        const int g = g0 + lane;
-        const bool real_col = g < G.GG;
-        Real Lr[4];
-        int er;
-        leaf_or_partial(G, buf, G.root, g, Lr, &er);
-        double wr[4], tot = 0;
+    {
+        // the root: posterior of each column (root marginal stored in place)
+        Real acc[16];
 #pragma unroll
-        for (int j = 0; j < 4; j++) { wr[j] = (double)Lr[j] * p.pi[j]; tot += wr[j]; }
-        Real* qr = G.partial(buf, G.root, g);
+        for (int q = 0; q < 16; q++) acc[q] = 0;
+        for (int g = threadIdx.x; g < G.GG; g += blockDim.x) {
+            Real Lr[4];
+            int er;
+            leaf_or_partial(G, buf, G.root, g, Lr, &er);
+            double wr[4], tot = 0;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const double q = (real_col && tot > 0) ? wr[j] / tot : 0.0;
-            const double sum = block_warp_sum(q);
-            if (lane == j * 4) wc[G.root * 16 + j * 4] += sum;
-            qr[j] = (Real)q;
+            for (int j = 0; j < 4; j++) { wr[j] = (double)Lr[j] * p.pi[j]; tot += wr[j]; }
+            Real* qr = G.partial(buf, G.root, g);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const Real q = tot > 0 ? (Real)(wr[j] / tot) : Real(0);
+                acc[j * 4] += q;
+                qr[j] = q;
+            }
         }
-        for (int k = G.nn - 2; k >= 0; k--) {
-            const int s = G.nodes[k];
-            if (G.missing(s)) continue;
+        const Real sum = warp_reduce_scatter16(acc);
+        if ((lane & 1) == 0) wc[G.root * 16 + (lane >> 1)] = (double)sum;
+    }
+    for (int k = G.nn - 2; k >= 0; k--) {
+        const int s = G.nodes[k];
+        if (G.missing(s)) continue;
+        const Real* P = G.Pcur + s * 16;
+        Real acc[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) acc[q] = 0;
+        for (int g = threadIdx.x; g < G.GG; g += blockDim.x) {
             Real L[4], m[4];
             int es;
             leaf_or_partial(G, buf, s, g, L, &es);
-            const Real* P = G.Pcur + s * 16;
             gbgc_message(P, L, m);
             const Real* qp = G.partial(buf, G.par[s], g);
             Real r[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) r[j] = m[j] > 0 ? qp[j] / m[j] : Real(0);
             Real qs[4];
-            double mine = 0;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                Real acc = 0;
+                Real a = 0;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const Real jt = r[j] * P[i * 4 + j] * L[i];
-                    acc += jt;
-                    const Real sum = warp_sum_real(real_col ? jt : Real(0));
-                    if (lane == i * 4 + j) mine = (double)sum;
+                    a += jt;
+                    acc[i * 4 + j] += jt;
                 }
-                qs[i] = acc;
+                qs[i] = a;
             }
-            if (lane < 16) wc[s * 16 + lane] += mine;
             if (s >= G.S) {
                 Real* o = G.partial(buf, s, g);
 #pragma unroll
                 for (int i = 0; i < 4; i++) o[i] = qs[i];
             }
-            __syncwarp();
         }
+        const Real sum = warp_reduce_scatter16(acc);
+        if ((lane & 1) == 0) wc[s * 16 + (lane >> 1)] = (double)sum;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < G.N * 16; i += blockDim.x) {
@@ -587,6 +644,18 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ GbgcScalars sc;
     __shared__ int s_elem;
+    // phase clock (thread 0, at phase ends that follow a block barrier):
+    // 0 monitor and init, 1 expected counts, 2 initial_prob_back, 3 branch
+    // matrices of the rate proposals, 4 the rest of sample_rates, 5 Update_ZB,
+    // 6 pruning, 7 ELBO and update_rates' MH
+    __shared__ unsigned long long s_ph[8];
+    __shared__ long long s_t;
+#define GB_MARK(i)                                          \
+    if (p.phase && tid == 0) {                              \
+        const long long t_ = clock64();                     \
+        s_ph[i] += (unsigned long long)(t_ - s_t);          \
+        s_t = t_;                                           \
+    }
     const int tid = threadIdx.x;
     StreamReader rng;   // thread 0's sequential reader
     for (;;) {
@@ -643,6 +712,9 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
         int16_t* i16 = (int16_t*)(smem + o);
         const int nh = H.n_hlev + 1, nd = H.n_dlev + 1, nhn = H.n_int, ndn = G.nn - 1;
         o += ((size_t)6 * N + nh + nhn + nd + ndn) * 2;
+        G.lst_all = (int16_t*)(smem + o);
+        G.lst_free = G.lst_all + N;
+        o += (size_t)4 * N;
         o = (o + 15) & ~(size_t)15;
         uint8_t* u8 = smem + o;
         for (int i = tid; i < N; i += blockDim.x) {
@@ -659,6 +731,8 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
         for (int i = tid; i < nhn; i += blockDim.x) lv[nh + i] = ((const int16_t*)(eb + H.o_hnodes))[i];
         for (int i = tid; i < nd; i += blockDim.x) lv[nh + nhn + i] = ((const int16_t*)(eb + H.o_dlev))[i];
         for (int i = tid; i < ndn; i += blockDim.x) lv[nh + nhn + nd + i] = ((const int16_t*)(eb + H.o_dnodes))[i];
+        for (int i = tid; i < H.n_blen; i += blockDim.x) G.lst_all[i] = ((const int16_t*)(eb + H.o_blen))[i];
+        G.nall = H.n_blen;
         G.nodes = i16; G.c0 = i16 + N; G.c1 = i16 + 2 * N; G.par = i16 + 3 * N; G.irank = i16 + 4 * N;
         G.pidx = i16 + 5 * N;
         G.hlev = lv; G.hnodes = lv + nh; G.dlev = lv + nh + nhn; G.dnodes = lv + nh + nhn + nd;
@@ -674,6 +748,8 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
         G.lpb = (double*)(ws + W.lpb); G.eraw = (double*)(ws + W.eraw); G.colsum = (double*)(ws + W.colsum);
         G.part = (Real*)(ws + W.part); G.scl = (int32_t*)(ws + W.scl);
         if (tid == 0) {
+            for (int q = 0; q < 8; q++) s_ph[q] = 0;
+            s_t = clock64();
             for (int u = 0; u < 2; u++) {
                 double t[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 t[0][0] = 1 - p.grate;
@@ -692,6 +768,15 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             sc.ec_gc[1] = d_log(p.gcc);
             sc.ec_mis[0] = d_log(1 - p.c2m);
             sc.ec_mis[1] = d_log(1 - p.nc2m);
+            sc.lmis[0] = d_log(1 - p.nc2m);
+            sc.lmis[1] = d_log(1 - p.c2m);
+            sc.lmis[2] = d_log(p.nc2m);
+            sc.lmis[3] = d_log(p.c2m);
+            const double pa[3] = {p.ca, p.na, p.gca}, pb[3] = {p.cb, p.nb, p.gcb};
+            for (int q = 0; q < 3; q++) {
+                sc.pr_lg[q] = d_lgamma(pa[q]);
+                sc.pr_alb[q] = __dmul_rn(pa[q], d_log(pb[q]));
+            }
             rng.init(p.seed, 0);
         }
         __syncthreads();
@@ -721,6 +806,15 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 if (s == G.root) f = 0;
                 G.fixZ[s] = (int8_t)f;
             }
+            __syncthreads();
+            if (tid == 0) {
+                int k = 0;
+                for (int i = 0; i < G.nall; i++)
+                    if (G.fixZ[G.lst_all[i]] != 1) G.lst_free[k++] = G.lst_all[i];
+                sc.n_free = k;
+            }
+            __syncthreads();
+            G.nfree = sc.n_free;
             if (tid == 0) {
                 sc.MaxLoglik = -CUDART_INF;
                 sc.r_n = p.acce_rate;
@@ -779,8 +873,8 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                     }
                     if (sc.move_r) {
                         double f = sc.tl + sc.logp_Z;
-                        f += log_gamma_pdf(-sc.r_c, p.ca, p.cb);
-                        if (resZ != 0) f += log_gamma_pdf(sc.r_n + p.nshift, p.na, p.nb);
+                        f += lgpdf(-sc.r_c, p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0]);
+                        if (resZ != 0) f += lgpdf(sc.r_n + p.nshift, p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1]);
                         int gb = 0, ungb = 0, mz[4] = {0, 0, 0, 0};
                         for (int k = 0; k < G.nn - 1; k++) {
                             const int s = G.nodes[k];
@@ -789,9 +883,9 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                             if (G.missing(s)) continue;
                             if (G.B[s]) gb++; else ungb++;
                         }
-                        f += d_log(1 - p.nc2m) * mz[0] + d_log(1 - p.c2m) * mz[1] + d_log(p.nc2m) * mz[2] +
-                             d_log(p.c2m) * mz[3];
-                        f += d_log(1 - p.gcc) * ungb + log_gamma_pdf(sc.r_gb, p.gca, p.gcb) + d_log(p.gcc) * gb;
+                        f += sc.lmis[0] * mz[0] + sc.lmis[1] * mz[1] + sc.lmis[2] * mz[2] + sc.lmis[3] * mz[3];
+                        f += sc.ec_gc[0] * ungb + lgpdf(sc.r_gb, p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2]) +
+                             sc.ec_gc[1] * gb;
                         sc.full = f;
                     }
                     trd[0 * p.T + m] = sc.full;
@@ -809,10 +903,12 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 }
                 if (m == p.T - 1) break;
                 __syncthreads();
+                GB_MARK(0)
                 // expected counts of the accepted partials
                 if (sc.move_r) {
                     const int nx = 1 - sc.post_cur;
                     counts(p, G, sc.pbuf, G.post + (size_t)nx * N * 16);
+                    GB_MARK(1)
                     if (tid == 0) sc.post_nxt = nx;
                     __syncthreads();
                 }
@@ -838,6 +934,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 }
                 for (int i = tid; i < N * 6; i += blockDim.x) G.emis_tmp[i] = G.emis[i];
                 __syncthreads();
+                GB_MARK(2)
                 // sample_rates: three MH moves of (gB, n, c) with Z and B integrated out
                 if (tid == 0) { sc.x_gb = sc.r_gb; sc.x_n = sc.r_n; sc.x_c = sc.r_c; }
                 for (int mm = 0; mm < 3; mm++) {
@@ -868,18 +965,19 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                         const int cls[5] = {1, 2, 3, 4, 5};
                         build_caches(p, G, 5, cls, sc.sel, sc.bias, sc.prop);
                     }
+                    GB_MARK(3)
                     emissions(G, sc, G.emis_tmp, 1, sc.prop, post, false);
                     prob_back(G, sc, G.emis_tmp);
                     if (tid == 0) {
                         const double lr = G.lpb[G.root * 6];
                         const double ngb = sc.bias[2], nn_ = sc.sel[1], nc_ = sc.sel[0];
-                        double MH = __dsub_rn(__dadd_rn(__dsub_rn(lr, sc.loglik_old), log_gamma_pdf(ngb, p.gca, p.gcb)),
-                                              log_gamma_pdf(cur3[0], p.gca, p.gcb));
+                        double MH = __dsub_rn(__dadd_rn(__dsub_rn(lr, sc.loglik_old), lgpdf(ngb, p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2])),
+                                              lgpdf(cur3[0], p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2]));
                         if (resZ != 0)
-                            MH = __dadd_rn(MH, __dsub_rn(log_gamma_pdf(__dadd_rn(nn_, p.nshift), p.na, p.nb),
-                                                         log_gamma_pdf(__dadd_rn(cur3[1], p.nshift), p.na, p.nb)));
-                        MH = __dadd_rn(MH, __dadd_rn(__dsub_rn(__dsub_rn(log_gamma_pdf(-nc_, p.ca, p.cb),
-                                                                         log_gamma_pdf(-cur3[2], p.ca, p.cb)),
+                            MH = __dadd_rn(MH, __dsub_rn(lgpdf(__dadd_rn(nn_, p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1]),
+                                                         lgpdf(__dadd_rn(cur3[1], p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1])));
+                        MH = __dadd_rn(MH, __dadd_rn(__dsub_rn(__dsub_rn(lgpdf(-nc_, p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0]),
+                                                                         lgpdf(-cur3[2], p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0])),
                                                                d_log(-nc_)),
                                                      d_log(-cur3[2])));
                         const bool acc = d_log(rng.uniform()) < MH;
@@ -899,6 +997,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                         else G.emis_tmp[s * 6 + j] = G.emis[s * 6 + j];
                     }
                     __syncthreads();
+                    GB_MARK(4)
                 }
                 // update_rates: Update_ZB, a pruning pass, ELBO, one MH step
                 for (int s = tid; s < N; s += blockDim.x) { G.Zp[s] = G.Z[s]; G.Bp[s] = G.B[s]; }
@@ -907,8 +1006,10 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 if (tid == 0) sc.pos = rng.pos;
                 __syncthreads();
                 sample_zb(p, G, sc);
+                GB_MARK(5)
                 stage_pcur(G, sc.acc);
                 prune(p, G, sc, 1 - sc.pbuf);
+                GB_MARK(6)
                 for (int k = tid; k < G.nn - 1; k += blockDim.x) {
                     const int s = G.nodes[k];
                     if (G.missing(s)) continue;
@@ -944,6 +1045,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 if (!sc.move_r)
                     for (int s = tid; s < N; s += blockDim.x) { G.Z[s] = G.Zp[s]; G.B[s] = G.Bp[s]; }
                 __syncthreads();
+                GB_MARK(7)
             }
             __syncthreads();
             if (tid == 0) p.max_ll[(size_t)e * 3 + resZ] = sc.MaxLoglik;
@@ -953,7 +1055,11 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             }
             __syncthreads();
         }
-        if (tid == 0) p.status[e] = 0;
+        if (tid == 0) {
+            p.status[e] = 0;
+            if (p.phase)
+                for (int q = 0; q < 8; q++) atomicAdd(&p.phase[q], s_ph[q]);
+        }
         if (p.stream) {
             // publish the slot once every thread's output writes are visible
             __threadfence_system();
@@ -968,7 +1074,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
 size_t gbgc_chain_smem(int N, int prec) {
     const size_t rb = prec ? 4 : 8;
     size_t o = (size_t)N * 16 * rb + 5 * 13 * 16 * 8 + 8 * 8;
-    o += ((size_t)6 * N + 4 * (size_t)N + 4) * 2;
+    o += ((size_t)6 * N + 4 * (size_t)N + 4) * 2 + (size_t)4 * N;
     o = (o + 15) & ~(size_t)15;
     o += (size_t)8 * N;
     return o;

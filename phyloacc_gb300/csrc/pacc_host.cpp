@@ -351,9 +351,17 @@ static void gbgc_blob(const HostModel& M, const GbgcElem& E, GbgcElemHdr& H, std
     H.o_hnodes = put(hnodes.data(), 2 * hnodes.size(), 2);
     H.o_dlev = put(dstart.data(), 2 * dstart.size(), 2);
     H.o_dnodes = put(dnodes.data(), 2 * dnodes.size(), 2);
+    // the branches that are not missing, by length (ties by id)
+    std::vector<int16_t> blen;
+    for (int k = 0; k + 1 < nn; k++)
+        if (!E.missing[E.nodes[k]]) blen.push_back((int16_t)E.nodes[k]);
+    std::stable_sort(blen.begin(), blen.end(), [&](int16_t a, int16_t b2) {
+        return E.d2[a] < E.d2[b2] || (E.d2[a] == E.d2[b2] && a < b2);
+    });
+    H.n_blen = (int32_t)blen.size();
+    H.o_blen = put(blen.data(), 2 * blen.size() + 2, 2);
     H.o_masks = put(E.masks.data(), E.masks.size(), 16);
     while (out.size() % 16) out.push_back(0);
-    H.pad = 0;
     H.blob_off = 0;
 }
 
@@ -944,7 +952,7 @@ static double gbgc_now() {
 }
 
 static size_t gbgc_blob_cap(int S, int N, int GGp) {
-    return (size_t)64 * N + (size_t)16 * S + (size_t)S * GGp + 1024;
+    return (size_t)72 * N + (size_t)16 * S + (size_t)S * GGp + 1024;
 }
 
 static size_t gbgc_out_bytes(int N, int T) {
@@ -3344,7 +3352,8 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     const size_t o_mzb = up(o_tzb + (size_t)chunk * tzb_el);
     const size_t o_mll = up(o_mzb + (size_t)chunk * 3 * 2 * N);
     const size_t o_st = up(o_mll + (size_t)chunk * 3 * 8);
-    const size_t total = up(o_st + (size_t)chunk * 4);
+    const size_t o_ph = up(o_st + (size_t)chunk * 4);
+    const size_t total = up(o_ph + 8 * 8);
     char* dev = nullptr;
     if (!cuda_ok(c, cudaMalloc((void**)&dev, total), "gbgc_run: cudaMalloc")) return PACC_OOM;
     cudaStream_t st = c->stream;
@@ -3376,7 +3385,9 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     p.next_elem = (int*)(dev + o_ctr);
     p.tr_d = (double*)(dev + o_trd); p.tr_zb = (int8_t*)(dev + o_tzb); p.max_zb = (int8_t*)(dev + o_mzb);
     p.max_ll = (double*)(dev + o_mll); p.status = (int32_t*)(dev + o_st);
-    bool ok = cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hh.data(), sizeof(GbgcElemHdr) * hh.size(), cudaMemcpyHostToDevice, st), "H2D") &&
+    p.phase = (unsigned long long*)(dev + o_ph);
+    bool ok = cuda_ok(c, cudaMemsetAsync(dev + o_ph, 0, 64, st), "memset") &&
+              cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hh.data(), sizeof(GbgcElemHdr) * hh.size(), cudaMemcpyHostToDevice, st), "H2D") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_blob, hblob.data(), blob_total, cudaMemcpyHostToDevice, st), "H2D") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_tgt, target.data(), N, cudaMemcpyHostToDevice, st), "H2D");
     std::vector<double> trd((size_t)chunk * 3 * 4 * T), mll((size_t)chunk * 3);
@@ -3415,6 +3426,11 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
                 }
             });
         for (auto& t : th) t.join();
+    }
+    if (ok) {   // cycles per phase of the chain kernel, summed over elements (pacc_counters.phase_cycles)
+        unsigned long long ph[8];
+        if (cuda_ok(c, cudaMemcpy(ph, dev + o_ph, sizeof(ph), cudaMemcpyDeviceToHost), "D2H"))
+            for (int q = 0; q < 8; q++) c->counters.phase_cycles[q] += (double)ph[q];
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
