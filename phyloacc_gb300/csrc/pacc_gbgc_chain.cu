@@ -480,6 +480,11 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
     __syncthreads();
 }
 
+// q / m in the expected-count pass: exact in FP64; with FP32 partials the
+// fast FP32 quotient (within 2 ulp), far inside the partials' own error.
+__device__ __forceinline__ double gb_div(double q, double m) { return q / m; }
+__device__ __forceinline__ float gb_div(float q, float m) { return __fdividef(q, m); }
+
 // Reduce-scatter of 16 values across a warp by recursive halving (16
 // shuffles): afterwards lane l holds the warp's sum of value (l >> 1) & 15
 // (lanes 2i and 2i + 1 both hold sum i).  The order of the additions depends
@@ -551,7 +556,7 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             const Real* qp = G.partial(buf, G.par[s], g);
             Real r[4];
 #pragma unroll
-            for (int j = 0; j < 4; j++) r[j] = m[j] > 0 ? qp[j] / m[j] : Real(0);
+            for (int j = 0; j < 4; j++) r[j] = m[j] > 0 ? gb_div(qp[j], m[j]) : Real(0);
             Real qs[4];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
