@@ -249,7 +249,20 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
         G.qn[tid] = n1;
     }
     __syncthreads();
-    for (int k = 2; k <= 13; k++) {
+    // powers up to the largest degree any branch of the list needs (the
+    // longest branch of the element is the last of the list; scaling and
+    // squaring only with degree 13)
+    int kmax = 3;
+    {
+        const double dmax = G.nall > 0 ? G.dist[G.lst_all[G.nall - 1]] : 0.0;
+        for (int i = 0; i < nc; i++) {
+            const double a = G.qn[i] * dmax;
+            int mi = 0;
+            while (mi < 4 && a > kPadeTheta[mi]) mi++;
+            kmax = max(kmax, kPadeM[mi]);
+        }
+    }
+    for (int k = 2; k <= kmax; k++) {
         if (tid < nc * 16) {
             const int ci = tid >> 4, e = tid & 15, r = e >> 2, c = e & 3;
             double* Qm = G.pw + ci * 13 * 16;
