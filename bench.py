@@ -566,6 +566,7 @@ def run_gbgc(args, K, ws, rank):
         ctx.gbgc_poll()
         barrier(ws)
         k0 = ctx.counters()["kernel_ms"]
+        ph0 = np.array(ctx.counters()["phase_cycles"])
         t = time.perf_counter()
         for _ in range(K):
             ctx.gbgc_submit(g)
@@ -577,6 +578,7 @@ def run_gbgc(args, K, ws, rank):
         ctx.gbgc_sync()
         wall = reduce_max(ws, time.perf_counter() - t)
         dev = reduce_max(ws, (ctx.counters()["kernel_ms"] - k0) * 1e-3)
+        ph = np.array(ctx.counters()["phase_cycles"]) - ph0
         ctx.close()
         T = g.burnin + g.mcmc
         lat = np.array([r["device_ms"] for r in got])
@@ -587,7 +589,10 @@ def run_gbgc(args, K, ws, rank):
                                "d2h_bytes_per_step": int(E * 3 * T * (4 * 8 + 2 * ds.tree.n_nodes))},
                        "filtered": int(sum(1 for x in got if x["status"] != 0)) // K,
                        "latency_submit_to_result_ms": {"p50": float(np.percentile(lat, 50)),
-                                                       "p99": float(np.percentile(lat, 99))}}
+                                                       "p99": float(np.percentile(lat, 99))},
+                       "phase_share": {n: float(v / max(ph.sum(), 1.0)) for n, v in zip(
+                           ("monitor_and_setup", "expected_counts", "initial_prob_back", "pade_branch_matrices",
+                            "rest_of_sample_rates", "update_zb", "pruning", "elbo_and_mh"), ph)}}
     # FP64 partials: the same batch on chains of a fifth of the length (the
     # cost of an iteration does not change along the chain), scaled to 1,000
     g64 = abi.gbgc_default_opts(ds.target)

@@ -992,7 +992,7 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
     const size_t o_trd = o_out, o_tzb = up(o_trd + (size_t)v.ns * 3 * 4 * v.T * 8);
     const size_t o_mzb = up(o_tzb + (size_t)v.ns * 3 * v.T * 2 * N), o_mll = up(o_mzb + (size_t)v.ns * 3 * 2 * N);
     const size_t o_st = up(o_mll + (size_t)v.ns * 3 * 8), o_out_end = up(o_st + (size_t)v.ns * 4);
-    const size_t o_tgt = up(o_out_end), o_head = up(o_tgt + N), o_idle = o_head + 128;
+    const size_t o_tgt = up(o_out_end), o_head = up(o_tgt + N), o_idle = o_head + 128, o_phase = o_head + 192;
     const size_t o_ws = up(o_head + 256), total = up(o_ws + W.total * v.grid);
     if (!cuda_ok(c, cudaMalloc((void**)&v.dev, total), "cudaMalloc (gbgc serving)")) return PACC_OOM;
     if (!cuda_ok(c, cudaMemset(v.dev, 0, o_ws), "memset")) return PACC_ECUDA;
@@ -1054,6 +1054,7 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
     p.done_flag = d_map + 64 + v.ns;
     p.idle_ns = c->o.serve_idle_ns > 0 ? c->o.serve_idle_ns : 30000000000ll;
     p.idle_exits = v.d_idle;
+    p.phase = (unsigned long long*)(v.dev + o_phase);   // 8 counters in the zeroed head block
     v.free_slots.clear();
     for (int i = v.ns - 1; i >= 0; i--) v.free_slots.push_back(i);
     v.busy.assign(v.ns, 0);
@@ -3158,13 +3159,18 @@ int pacc_gbgc_sync(pacc_ctx* c) {
         }
         std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
-    // nothing left: the blocks return now, and the launch's time is counted
+    // nothing left: the blocks return now, and the launch's time and phase
+    // cycles are counted
     if (v.running) {
         *v.h_stop = 1;
         float ms = 0;
         if (!cuda_ok(c, cudaEventSynchronize(v.ev_done), "gbgc serving launch")) return PACC_ECUDA;
         if (cudaEventElapsedTime(&ms, v.ev0, v.ev_done) == cudaSuccess) c->counters.kernel_ms += ms;
         v.running = false;
+        unsigned long long ph[8];
+        if (cuda_ok(c, cudaMemcpy(ph, v.p.phase, sizeof(ph), cudaMemcpyDeviceToHost), "D2H (phases)") &&
+            cuda_ok(c, cudaMemset(v.p.phase, 0, sizeof(ph)), "memset (phases)"))
+            for (int q = 0; q < 8; q++) c->counters.phase_cycles[q] += (double)ph[q];
     }
     return PACC_OK;
 }
