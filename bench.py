@@ -566,6 +566,7 @@ def run_gbgc(args, K, ws, rank):
         ctx.gbgc_poll()
         barrier(ws)
         k0 = ctx.counters()["kernel_ms"]
+        f0 = ctx.counters()["flop"]
         ph0 = np.array(ctx.counters()["phase_cycles"])
         t = time.perf_counter()
         for _ in range(K):
@@ -579,7 +580,9 @@ def run_gbgc(args, K, ws, rank):
         wall = reduce_max(ws, time.perf_counter() - t)
         dev = reduce_max(ws, (ctx.counters()["kernel_ms"] - k0) * 1e-3)
         ph = np.array(ctx.counters()["phase_cycles"]) - ph0
+        flop = ctx.counters()["flop"] - f0
         ctx.close()
+        fp64_peak, _ = pg.measure_fma_peak(0)
         T = g.burnin + g.mcmc
         lat = np.array([r["device_ms"] for r in got])
         out["fp32"] = {"value": ws * K * E / dev, "unit": "elements/s", "elements_per_step": E, "steps": K,
@@ -590,6 +593,12 @@ def run_gbgc(args, K, ws, rank):
                        "filtered": int(sum(1 for x in got if x["status"] != 0)) // K,
                        "latency_submit_to_result_ms": {"p50": float(np.percentile(lat, 50)),
                                                        "p99": float(np.percentile(lat, 99))},
+                       "roofline": {"bound": "fp64", "achieved": flop / dev / 1e12, "peak": fp64_peak / 1e12,
+                                    "unit": "TFLOP/s", "frac": flop / dev / fp64_peak,
+                                    "work": "FP64 flops of the Pade solves (34 m + 198 + 128 squarings per branch "
+                                            "matrix, device counters); the kernel's other FP64 work is not counted",
+                                    "peak_source": "measured FP64 FMA rate of this GPU (pacc_measure_fma_peak)",
+                                    "traffic": None},
                        "phase_share": {n: float(v / max(ph.sum(), 1.0)) for n, v in zip(
                            ("monitor_and_setup", "expected_counts", "initial_prob_back", "pade_branch_matrices",
                             "rest_of_sample_rates", "update_zb", "pruning", "elbo_and_mh"), ph)}}

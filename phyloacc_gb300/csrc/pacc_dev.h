@@ -314,6 +314,7 @@ struct GbgcChainParams {
     long long idle_ns;               // a block idle this long returns even without q_stop
     unsigned long long* idle_exits;  // blocks that left on the idle bound
     unsigned long long* phase;       // [8] cycles per phase (summed over elements), or null
+    unsigned long long* flop;        // FP64 flops of the Padé solves (algorithmic count), or null
 };
 
 }  // namespace pacc

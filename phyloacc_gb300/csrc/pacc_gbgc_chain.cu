@@ -54,7 +54,9 @@ constexpr int GB_WARPS = GB_BT / 32;
 constexpr double LN2 = 0.6931471805599453;
 
 // exp(d Q) from Q's powers pw[k-1] = Q^k (k = 1..13) and ||Q||_1.
-__device__ __noinline__ void pade_branch(const double* __restrict__ pw, double qn, double d, double* E) {
+// Returns the solve's FP64 flops: 34 m for the sums, 198 for V + U, V - U and
+// the 4x4 solve with four right-hand sides, 128 a squaring.
+__device__ __noinline__ int pade_branch(const double* __restrict__ pw, double qn, double d, double* E) {
     const double a = qn * d;
     int mi = 0;
     while (mi < 4 && a > kPadeTheta[mi]) mi++;
@@ -141,6 +143,7 @@ __device__ __noinline__ void pade_branch(const double* __restrict__ pw, double q
 #pragma unroll
         for (int q = 0; q < 16; q++) E[q] = V[q];
     }
+    return 34 * m + 198 + 128 * sq;
 }
 
 __device__ __forceinline__ unsigned long long gb_timer_ns() {
@@ -281,12 +284,13 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
         cnt[i] = (cls[i] % 3 == 2) ? G.nfree : G.nall;
         tot += cnt[i];
     }
+    unsigned fl = 0;
     for (int it = tid; it < tot; it += blockDim.x) {
         int ci = 0, k = it;
         while (k >= cnt[ci]) { k -= cnt[ci]; ci++; }
         const int s = (cls[ci] % 3 == 2) ? G.lst_free[k] : G.lst_all[k];
         double E[16];
-        pade_branch(G.pw + ci * 13 * 16, G.qn[ci], G.dist[s], E);
+        fl += (unsigned)pade_branch(G.pw + ci * 13 * 16, G.qn[ci], G.dist[s], E);
         const int sl = G.slot(cls[ci], set);
         Real* lo = G.lp(sl, s);
         Real* po = G.pmat(sl, s);
@@ -296,6 +300,11 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
             lo[q] = branch_log<Real>(v, (q & 3) == (q >> 2));
             po[q] = (Real)v;
         }
+    }
+    if (p.flop) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) fl += __shfl_xor_sync(0xffffffffu, fl, o);
+        if ((tid & 31) == 0) atomicAdd(p.flop, (unsigned long long)fl);
     }
     __syncthreads();
 }

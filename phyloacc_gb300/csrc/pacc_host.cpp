@@ -1055,6 +1055,7 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
     p.idle_ns = c->o.serve_idle_ns > 0 ? c->o.serve_idle_ns : 30000000000ll;
     p.idle_exits = v.d_idle;
     p.phase = (unsigned long long*)(v.dev + o_phase);   // 8 counters in the zeroed head block
+    p.flop = (unsigned long long*)(v.dev + o_head + 160);
     v.free_slots.clear();
     for (int i = v.ns - 1; i >= 0; i--) v.free_slots.push_back(i);
     v.busy.assign(v.ns, 0);
@@ -3167,10 +3168,14 @@ int pacc_gbgc_sync(pacc_ctx* c) {
         if (!cuda_ok(c, cudaEventSynchronize(v.ev_done), "gbgc serving launch")) return PACC_ECUDA;
         if (cudaEventElapsedTime(&ms, v.ev0, v.ev_done) == cudaSuccess) c->counters.kernel_ms += ms;
         v.running = false;
-        unsigned long long ph[8];
+        unsigned long long ph[8], fl = 0;
         if (cuda_ok(c, cudaMemcpy(ph, v.p.phase, sizeof(ph), cudaMemcpyDeviceToHost), "D2H (phases)") &&
-            cuda_ok(c, cudaMemset(v.p.phase, 0, sizeof(ph)), "memset (phases)"))
+            cuda_ok(c, cudaMemcpy(&fl, v.p.flop, sizeof(fl), cudaMemcpyDeviceToHost), "D2H (flop)") &&
+            cuda_ok(c, cudaMemset(v.p.phase, 0, sizeof(ph)), "memset (phases)") &&
+            cuda_ok(c, cudaMemset(v.p.flop, 0, sizeof(fl)), "memset (flop)")) {
             for (int q = 0; q < 8; q++) c->counters.phase_cycles[q] += (double)ph[q];
+            c->counters.flop += (double)fl;
+        }
     }
     return PACC_OK;
 }
@@ -3359,7 +3364,7 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     const size_t o_mll = up(o_mzb + (size_t)chunk * 3 * 2 * N);
     const size_t o_st = up(o_mll + (size_t)chunk * 3 * 8);
     const size_t o_ph = up(o_st + (size_t)chunk * 4);
-    const size_t total = up(o_ph + 8 * 8);
+    const size_t total = up(o_ph + 9 * 8);
     char* dev = nullptr;
     if (!cuda_ok(c, cudaMalloc((void**)&dev, total), "gbgc_run: cudaMalloc")) return PACC_OOM;
     cudaStream_t st = c->stream;
@@ -3392,7 +3397,8 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     p.tr_d = (double*)(dev + o_trd); p.tr_zb = (int8_t*)(dev + o_tzb); p.max_zb = (int8_t*)(dev + o_mzb);
     p.max_ll = (double*)(dev + o_mll); p.status = (int32_t*)(dev + o_st);
     p.phase = (unsigned long long*)(dev + o_ph);
-    bool ok = cuda_ok(c, cudaMemsetAsync(dev + o_ph, 0, 64, st), "memset") &&
+    p.flop = p.phase + 8;
+    bool ok = cuda_ok(c, cudaMemsetAsync(dev + o_ph, 0, 72, st), "memset") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_hdr, hh.data(), sizeof(GbgcElemHdr) * hh.size(), cudaMemcpyHostToDevice, st), "H2D") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_blob, hblob.data(), blob_total, cudaMemcpyHostToDevice, st), "H2D") &&
               cuda_ok(c, cudaMemcpyAsync(dev + o_tgt, target.data(), N, cudaMemcpyHostToDevice, st), "H2D");
@@ -3434,9 +3440,11 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
         for (auto& t : th) t.join();
     }
     if (ok) {   // cycles per phase of the chain kernel, summed over elements (pacc_counters.phase_cycles)
-        unsigned long long ph[8];
-        if (cuda_ok(c, cudaMemcpy(ph, dev + o_ph, sizeof(ph), cudaMemcpyDeviceToHost), "D2H"))
+        unsigned long long ph[9];
+        if (cuda_ok(c, cudaMemcpy(ph, dev + o_ph, sizeof(ph), cudaMemcpyDeviceToHost), "D2H")) {
             for (int q = 0; q < 8; q++) c->counters.phase_cycles[q] += (double)ph[q];
+            c->counters.flop += (double)ph[8];
+        }
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
