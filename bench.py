@@ -639,6 +639,26 @@ def run_gbgc(args, K, ws, rank):
         if scale != 1.0:
             leg["note"] = "measured on %d-iteration chains, scaled to %d" % (T, g.burnin + g.mcmc)
         out[name] = leg
+        if name == "fp64":
+            # FP32 against these FP64 chains: the same elements, seed and chain
+            # length (the marginal likelihoods are Monte Carlo estimates of two
+            # chains that part at the first MH decision FP32 rounding moves)
+            o32 = abi.default_opts()
+            o32.precision = abi.PACC_FP32
+            c32 = pg.Context(ds, o32)
+            r32 = c32.gbgc_run(gg)
+            c32.close()
+            rel = []
+            for a, b in zip(r32, r):
+                if a["status"] == 0 and b["status"] == 0:
+                    for k in ("loglik_null", "loglik_res", "loglik_all"):
+                        if np.isfinite(b[k]) and np.isfinite(a[k]):
+                            rel.append(abs(a[k] - b[k]) / abs(b[k]))
+            rel = np.array(rel) if rel else np.zeros(1)
+            out["error"] = {"marginal_loglik_rel_max": float(rel.max()),
+                            "marginal_loglik_rel_median": float(np.median(rel)), "values": int(rel.size),
+                            "note": "FP32 against FP64 partials, %d elements x 3 models, %d-iteration chains" %
+                                    (E, T)}
     out["value"] = out["fp32"]["value"]
     out["e2e"] = out["fp32"]["e2e"]
     if "fp64" in out:

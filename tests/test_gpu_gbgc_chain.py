@@ -207,3 +207,37 @@ def test_gbgc_served_equals_batch(built):
         assert (r["max_loglik"] == w["max_loglik"]).all() and (r["rates"] == w["rates"]).all()
         for k in ("max_z", "max_b", "post_b", "post_z"):
             assert (r[k] == w[k]).all(), (r["element_no"], k)
+
+
+def test_gbgc_filtered_elements(built):
+    """Elements the reference filters (more than CONSERVE_PROP of the
+    conserved species missing, bpp_c.hpp:301-311) and elements whose tree
+    collapses to a single taxon come back as PACC_FILTERED from both the
+    batch and the serving paths, and the others are unaffected."""
+    from phyloacc_gb300 import abi, synth
+    ds = synth.make_dataset("st43", n_elements=6, seed=13)
+    ds.bases = ds.bases.copy()
+    S = ds.tree.n_species
+    star = ord("*")
+    blk = ds.element(1)
+    for sp in ds.conserve:
+        blk[sp, :] = star                     # every conserved species missing
+    blk = ds.element(3)
+    blk[:, :] = star
+    blk[0, :] = ord("a")                      # one taxon left
+    o = abi.gbgc_default_opts(ds.target)
+    o.burnin, o.mcmc, o.seed = 10, 30, 2
+    ref = _ctx(ds, 1).gbgc_run(o)
+    assert [r["status"] for r in ref] == [0, 1, 0, 1, 0, 0]
+    from phyloacc_gb300 import Context
+    so = abi.default_opts()
+    so.precision = 1
+    ctx = Context(ds, so)
+    ctx.gbgc_submit(o)
+    ctx.gbgc_sync()
+    got = {r["element_no"]: r for r in ctx.gbgc_poll()}
+    assert sorted(got) == list(range(6))
+    for e, r in enumerate(ref):
+        assert got[e]["status"] == r["status"]
+        if r["status"] == 0:
+            assert got[e]["loglik_all"] == r["loglik_all"]
