@@ -179,6 +179,7 @@ __device__ __forceinline__ Real warp_sum_real(Real v) {
 // Scalars of one CTA's chain.
 struct GbgcScalars {
     double tm[2][3][3], lt[2][3][3];   // Z transition [outgroup path][child Z][parent Z] and its log
+    float tmf[2][3][3];                // the transition in FP32 (the FP32 message pass)
     double ec_gc[2], ec_mis[2];        // emission constants: log(1 - c) / log(c); log(1 - cons2mis) / log(1 - ncons2mis)
     double lmis[4];                    // log(1 - ncons2mis), log(1 - cons2mis), log(ncons2mis), log(cons2mis)
     double pr_lg[3], pr_alb[3];        // lgamma(a) and a log(b) of the conserved, accelerated and GC-bias priors
@@ -338,9 +339,10 @@ __device__ void emissions(const GbgcCtx<Real>& G, const GbgcScalars& sc, double*
 // With FP32 partials the exponentials and logarithm are FP32 (differences and
 // sums of the FP64 log values stay FP64).
 template <typename Real>
-__device__ __forceinline__ void lm63(const double (*tm)[3], const double* y, double mx, double* t);
+__device__ __forceinline__ void lm63(const GbgcScalars& sc, int u, const double* y, double mx, double* t);
 template <>
-__device__ __forceinline__ void lm63<double>(const double (*tm)[3], const double* y, double mx, double* t) {
+__device__ __forceinline__ void lm63<double>(const GbgcScalars& sc, int u, const double* y, double mx, double* t) {
+    const double (*tm)[3] = sc.tm[u];
     double ez[3];
 #pragma unroll
     for (int z = 0; z < 3; z++) ez[z] = d_exp(y[z] - mx) + d_exp(y[z + 3] - mx);
@@ -353,7 +355,8 @@ __device__ __forceinline__ void lm63<double>(const double (*tm)[3], const double
     }
 }
 template <>
-__device__ __forceinline__ void lm63<float>(const double (*tm)[3], const double* y, double mx, double* t) {
+__device__ __forceinline__ void lm63<float>(const GbgcScalars& sc, int u, const double* y, double mx, double* t) {
+    const float (*tm)[3] = sc.tmf[u];
     float ez[3];
 #pragma unroll
     for (int z = 0; z < 3; z++) ez[z] = expf((float)(y[z] - mx)) + expf((float)(y[z + 3] - mx));
@@ -361,7 +364,7 @@ __device__ __forceinline__ void lm63<float>(const double (*tm)[3], const double*
     for (int j = 0; j < 3; j++) {
         float v = 0;
 #pragma unroll
-        for (int z = 0; z < 3; z++) v += (float)tm[z][j] * ez[z];
+        for (int z = 0; z < 3; z++) v += tm[z][j] * ez[z];
         t[j] = (double)logf(v) + mx;
     }
 }
@@ -388,7 +391,7 @@ __device__ void up_pass(const GbgcCtx<Real>& G, const GbgcScalars& sc, bool half
                 if (mx == -CUDART_INF) {
                     t[0] = t[1] = t[2] = -CUDART_INF;
                 } else {
-                    lm63<Real>(sc.tm[G.upper(c)], y, mx, t);
+                    lm63<Real>(sc, G.upper(c), y, mx, t);
 #pragma unroll
                     for (int j = 0; j < 3; j++)
                         if (half) t[j] -= LN2;
@@ -426,6 +429,22 @@ __device__ void stage_pcur(const GbgcCtx<Real>& G, int set) {
         G.Pcur[s * 16 + (i & 15)] = (G.missing(s) || k < 0) ? Real(0) : G.pmat(G.slot(k, set), s)[i & 15];
     }
     __syncthreads();
+}
+
+// log(sum_j pi_j L_root(j)) + e log 2 of one column: FP64 with FP64
+// partials; with FP32 partials the sum and its logarithm in FP32 (the
+// partials' own error is larger), the exponent term in FP64.
+__device__ __forceinline__ double column_loglik(const double* L, const double* pi, int e) {
+    double t = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) t += L[j] * pi[j];
+    return t > 0 ? d_log(t) + (double)e * LN2 : -CUDART_INF;
+}
+__device__ __forceinline__ double column_loglik(const float* L, const double* pi, int e) {
+    float t = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) t += L[j] * (float)pi[j];
+    return t > 0 ? (double)logf(t) + (double)e * LN2 : -CUDART_INF;
 }
 
 template <typename Real>
@@ -485,10 +504,7 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
             Real Lr[4];
             int er;
             leaf_or_partial(G, buf, G.root, g, Lr, &er);
-            double t = 0;
-#pragma unroll
-            for (int j = 0; j < 4; j++) t += (double)Lr[j] * p.pi[j];
-            tot += t > 0 ? d_log(t) + (double)er * LN2 : -CUDART_INF;
+            tot += column_loglik(Lr, p.pi, er);
         }
     }
     tot = block_warp_sum(tot);
@@ -549,13 +565,13 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             Real Lr[4];
             int er;
             leaf_or_partial(G, buf, G.root, g, Lr, &er);
-            double wr[4], tot = 0;
+            Real wr[4], tot = 0;
 #pragma unroll
-            for (int j = 0; j < 4; j++) { wr[j] = (double)Lr[j] * p.pi[j]; tot += wr[j]; }
+            for (int j = 0; j < 4; j++) { wr[j] = Lr[j] * (Real)p.pi[j]; tot += wr[j]; }
             Real* qr = G.partial(buf, G.root, g);
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const Real q = tot > 0 ? (Real)(wr[j] / tot) : Real(0);
+                const Real q = tot > 0 ? gb_div(wr[j], tot) : Real(0);
                 acc[j * 4] += q;
                 qr[j] = q;
             }
@@ -788,6 +804,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 for (int a = 0; a < 3; a++)
                     for (int b = 0; b < 3; b++) {
                         sc.tm[u][a][b] = t[a][b];
+                        sc.tmf[u][a][b] = (float)t[a][b];
                         sc.lt[u][a][b] = d_log(t[a][b]);
                     }
             }
