@@ -282,7 +282,9 @@ typedef struct pacc_gbgc_opts {
     double prop_c, prop_n, prop_gc;   /* proposal widths (1.2, 1.2, 0.2; bpp_c.hpp:365-370) */
     const int32_t* target;        /* TARGETSPECIES node ids (M2 lets only these leaves accelerate) */
     int32_t n_target;
-    int32_t reserved;
+    int32_t chain;                /* chain k of the CHAIN loop (main.cpp:372): a later chain starts
+                                     every node, inside the element's tree or not, from Z = 0
+                                     (bpp.cur_Z, never written without SAMPLE_HYPER; bpp_c.cpp:128-131) */
 } pacc_gbgc_opts;
 
 void pacc_gbgc_default_opts(pacc_gbgc_opts* opts);

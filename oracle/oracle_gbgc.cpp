@@ -395,7 +395,9 @@ struct GChain {
     // initMCMC (bpp_c.cpp:120-257), first chain
     bool init(int resZ) {
         B.assign(N, 0);
-        Z.assign(N, -1);
+        // the first chain: -1 off the element's tree, 0 on it; a later chain
+        // takes bpp.cur_Z, all zeros without SAMPLE_HYPER (bpp_c.cpp:124-135)
+        Z.assign(N, o->chain > 0 ? 0 : -1);
         for (int s : E.nodes) Z[s] = 0;
         Z[root] = 0;
         fixZ.assign(N, -1);

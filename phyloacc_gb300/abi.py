@@ -156,7 +156,7 @@ class PaccGbgcOpts(C.Structure):
         ("cons_to_mis", C.c_double), ("ncons_to_mis", C.c_double),
         ("missing_thres", C.c_double), ("conserve_prop", C.c_double),
         ("prop_c", C.c_double), ("prop_n", C.c_double), ("prop_gc", C.c_double),
-        ("target", C.POINTER(C.c_int32)), ("n_target", C.c_int32), ("reserved", C.c_int32)]
+        ("target", C.POINTER(C.c_int32)), ("n_target", C.c_int32), ("chain", C.c_int32)]
 
 
 def gbgc_default_opts(target=None) -> PaccGbgcOpts:

@@ -288,6 +288,7 @@ struct GbgcChainParams {
     int* next_elem;
     int T, burn, mcmc;
     uint32_t seed;
+    int chain;                // > 0: a later chain of a CHAIN > 1 run (Z starts at 0 everywhere)
     double conserve_rate, acce_rate, init_gc;
     double ca, cb, na, nb, nshift, gca, gcb, gcc;   // priors: conserved, accelerated (+ shift), GC bias
     double lrate, grate, c2m, nc2m, prop_c, prop_n, prop_gc;

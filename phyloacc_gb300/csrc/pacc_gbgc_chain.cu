@@ -832,7 +832,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             // ---- initMCMC (bpp_c.cpp:120-257) ----
             for (int s = tid; s < N; s += blockDim.x) {
                 G.B[s] = 0;
-                G.Z[s] = -1;
+                G.Z[s] = p.chain > 0 ? 0 : -1;   // a later chain: bpp.cur_Z, all zeros
                 int f = -1;
                 if (G.upper(s)) f = 1;
                 if (resZ == 2 && s < G.S) f = (G.flags[s] & GBGC_TARGET) ? -1 : 1;

@@ -1027,7 +1027,7 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
     p.hdr = v.d_hdr;
     p.blob = (const uint8_t*)v.d_blob;
     p.n_elem = v.ns;
-    p.T = v.T; p.burn = g.burnin; p.mcmc = g.mcmc; p.seed = g.seed;
+    p.T = v.T; p.burn = g.burnin; p.mcmc = g.mcmc; p.seed = g.seed; p.chain = g.chain;
     p.conserve_rate = g.conserve_rate; p.acce_rate = g.acce_rate; p.init_gc = g.init_gc;
     p.ca = g.conserve_prior_a; p.cb = g.conserve_prior_b;
     p.na = g.acce_prior_a; p.nb = g.acce_prior_b; p.nshift = g.acce_prior_shift;
@@ -3381,7 +3381,7 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     }
     GbgcChainParams p;
     std::memset(&p, 0, sizeof(p));
-    p.T = T; p.burn = go->burnin; p.mcmc = go->mcmc; p.seed = go->seed;
+    p.T = T; p.burn = go->burnin; p.mcmc = go->mcmc; p.seed = go->seed; p.chain = go->chain;
     p.conserve_rate = go->conserve_rate; p.acce_rate = go->acce_rate; p.init_gc = go->init_gc;
     p.ca = go->conserve_prior_a; p.cb = go->conserve_prior_b;
     p.na = go->acce_prior_a; p.nb = go->acce_prior_b; p.nshift = go->acce_prior_shift;

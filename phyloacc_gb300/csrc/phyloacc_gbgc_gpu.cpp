@@ -222,6 +222,7 @@ int main(int argc, char** argv) {
         oh << chain << "\t" << C.g.acce_prior_a << "\t" << C.g.acce_prior_b << "\t" << C.g.conserve_prior_a << "\t"
            << C.g.conserve_prior_b << "\t" << 0 << "\t" << 0 << "\t" << C.g.prep_grate << "\t" << C.g.prep_lrate
            << std::endl;
+        C.g.chain = chain;
         if (!ctx) {
             ctx = pacc_create(&model, &C.o, &st);
             if (!ctx) die(string("pacc_create failed: ") + pacc_last_error(nullptr));

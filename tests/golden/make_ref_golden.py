@@ -45,8 +45,11 @@ CASES = {
     "gbgc12_default": ("st12", [0, 1, 85, 90], 20, 60, 0, {}),
     # 43 taxa with missing taxa ('*' rows): the outgroup (root moves), conserved and target leaves
     "gbgc43_missing": ("st43", [0, 7, 12, 20], 30, 90, 5, {}),
+    # two chains: a later chain starts every node from Z = 0 (bpp_c.cpp:124-135), which shows on
+    # the nodes off the element's tree (a missing outgroup moves the root in element 1)
+    "gbgc43_chain2": ("st43", [0, 7], 20, 40, 6, {"CHAIN": 2}),
 }
-GBGC_CASES = {"gbgc12_default", "gbgc43_missing"}
+GBGC_CASES = {"gbgc12_default", "gbgc43_missing", "gbgc43_chain2"}
 
 
 def mask_taxa(ds, case):
@@ -61,6 +64,8 @@ def mask_taxa(ds, case):
             blk[s, :] = ord("n")
         blk = ds.element(3)
         blk[ds.target[0], : blk.shape[1] // 2] = ord("-")
+    if case == "gbgc43_chain2":
+        ds.element(1)[ds.outgroup[0], :] = ord("*")
     if case == "gbgc43_missing":
         star = ord("*")
         ds.element(1)[ds.outgroup[0], :] = star

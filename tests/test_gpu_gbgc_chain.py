@@ -130,7 +130,7 @@ def test_gbgc_chain_fp32_against_fp64_at_size(built):
     assert rel.max() < 1e-3 and np.median(rel) < 1e-6
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + ["gbgc43_chain2"])
 def test_gbgc_cli_matches_reference(built, tmp_path, case):
     """phyloacc-gbgc-gpu on the golden case's own cfg and inputs: every table
     the reference wrote (elem_lik, rate_postZ_{0,1,2}, 1_elem_Z,
@@ -162,11 +162,14 @@ def test_gbgc_cli_matches_reference(built, tmp_path, case):
     kv = read_cfg(str(work / "case.cfg"))
     T = int(kv["BURNIN"]) + int(kv["MCMC"])
     tr = np.load(os.path.join(src, "traces.npz"))
+    chains = int(kv.get("CHAIN", 1))
     for key in tr.files:
-        p = work / "out" / ("case_mcmc_trace_%s.txt" % key)
+        w = key.split("_")
+        k = 1 if len(w) == 3 else 0                   # "m_e" or "m_e_c1"
+        p = work / "out" / ("case_mcmc_trace_%s_%s.txt" % (w[0], w[1]))
         got = np.array([[float(v) for v in ln.rstrip("\n\t").split("\t")] for ln in list(open(p))[1:]])
-        assert got.shape[0] == T
-        np.testing.assert_allclose(got, tr[key], rtol=2e-7, atol=1e-300, err_msg=key)
+        assert got.shape[0] == chains * T
+        np.testing.assert_allclose(got[k * T:(k + 1) * T], tr[key], rtol=2e-7, atol=1e-300, err_msg=key)
 
 
 def test_gbgc_served_equals_batch(built):

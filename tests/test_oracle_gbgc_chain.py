@@ -70,3 +70,39 @@ def test_gbgc_chain_tables_match_reference(built, case):
     lines = [ln.rstrip("\n\t").split("\t") for ln in open(os.path.join(out, "case_1_elem_Z.txt"))][1:]
     for r, ln in zip(runs, lines):
         assert [int(x) for x in ln] == list(r["max_z"][1])
+
+
+def test_gbgc_chain_two_chains_match_reference(built):
+    """CHAIN 2 (gbgc43_chain2): the second chain starts every node from Z = 0
+    (bpp.cur_Z, never written without SAMPLE_HYPER), which changes the traces
+    and Z frequencies of the nodes off the element's tree (element 1 lost its
+    outgroup, so its root moved); both chains' traces and every table the
+    reference wrote (rate_postZ rows of both chains, the last chain's
+    elem_lik and 1_elem_Z)."""
+    case = "gbgc43_chain2"
+    ds, _, kv = load_case(case)
+    N = ds.tree.n_nodes
+    tr = np.load(os.path.join(GOLDEN, case, "traces.npz"))
+    runs = []
+    for k in range(2):
+        o = gbgc_opts(ds, kv)
+        o.chain = k
+        runs.append([po.gbgc_run(ds, o, e) for e in range(ds.n_elements)])
+        for e, r in enumerate(runs[k]):
+            for m in range(3):
+                want = tr["%d_%d" % (m, e) + ("_c1" if k else "")]
+                np.testing.assert_allclose(r["trace"][m], want, rtol=1e-7, atol=1e-9, err_msg="%d %d %d" % (k, e, m))
+    assert not np.array_equal(runs[0][1]["post_z"], runs[1][1]["post_z"])   # the off-tree nodes differ
+    out = os.path.join(GOLDEN, case, "out")
+    for m in range(3):
+        _, rows = read_table(os.path.join(out, "case_rate_postZ_%d.txt" % m))
+        assert len(rows) == 2 * ds.n_elements
+        for i, row in enumerate(rows):
+            r = runs[i // ds.n_elements][i % ds.n_elements]
+            vals = [as_float(x) for x in row[1:] if x != ""]
+            got = list(r["rates"][m]) + list(r["post_b"][m]) + list(r["post_z"][m].reshape(-1))
+            np.testing.assert_allclose(got, vals, rtol=1e-5, atol=1e-6)
+    _, rows = read_table(os.path.join(out, "case_elem_lik.txt"))
+    for r, row in zip(runs[1], rows):
+        got = [r["loglik_null"], r["loglik_res"], r["loglik_all"]]
+        np.testing.assert_allclose(got, [as_float(x) for x in row[2:5]], rtol=1e-7, atol=1e-6)
