@@ -932,19 +932,36 @@ __device__ __forceinline__ double msg(const double* ltm, const double* beta, int
 // exp per node and state).  Transition matrix T[zc][zp] from g, l, l2
 // (bpp_c.cpp:573-599); fixed nodes cannot be in state 2.  Draws use the same
 // stream words as the log-space filter.
+// Inverse-CDF draw over three FP32 weights from one 32-bit word (24-bit
+// uniform), as the FP32 path's internal-base draws take theirs.
+__device__ __forceinline__ int categorical3f(const float* p, uint32_t wd) {
+    const float u = ((float)(wd >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    const float c0 = p[0], c1 = c0 + p[1], c2 = c1 + p[2];
+    const float t = u * c2;
+    if (t < c2) return (t >= c0) + (t >= c1);
+    for (int k = 2; k >= 0; k--)
+        if (p[k] > 0) return k;
+    return 3;
+}
+
+// The Z filter of the FP32 path in linear FP32: the emissions, relative to
+// each node's largest, as FP32 weights; messages up the tree with exact
+// power-of-two normalisation; draws from the same stream positions as the
+// FP64 filter, with FP32 categoricals.
 template <typename Real>
 __device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
     const int T = c.T, m = c.cs->m;
-    const double gr = c.trd[TR_G * T + m], lr = c.trd[TR_L * T + m], lr2 = c.trd[TR_L2 * T + m];
+    const float gr = (float)c.trd[TR_G * T + m], lr = (float)c.trd[TR_L * T + m], lr2 = (float)c.trd[TR_L2 * T + m];
+    float* beta = (float*)c.beta;   // [N][3] in the FP64 buffer's space
     for (int i = threadIdx.x; i < c.n_nodes; i += blockDim.x) {
         const int s = c.nodes[i];
         const double e0 = c.emis[s * 3 + 0], e1 = c.emis[s * 3 + 1], e2 = c.emis[s * 3 + 2];
         const bool ban = c.fixZ[s] == 1;
         double mx = e0 > e1 ? e0 : e1;
         if (!ban && e2 > mx) mx = e2;
-        c.beta[s * 3 + 0] = d_exp(e0 - mx);
-        c.beta[s * 3 + 1] = d_exp(e1 - mx);
-        c.beta[s * 3 + 2] = ban ? 0.0 : d_exp(e2 - mx);
+        beta[s * 3 + 0] = expf((float)(e0 - mx));
+        beta[s * 3 + 1] = expf((float)(e1 - mx));
+        beta[s * 3 + 2] = ban ? 0.0f : expf((float)(e2 - mx));
         c.changed[s] = 0;
     }
     __syncthreads();
@@ -958,32 +975,32 @@ __device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
             const int a = c.hlev_start[h], b = c.hlev_start[h + 1];
             for (int i = a + lane; i < b; i += 32) {
                 const int p = c.hlev_nodes[i];
-                double v0 = c.beta[p * 3 + 0], v1 = c.beta[p * 3 + 1], v2 = c.beta[p * 3 + 2];
+                float v0 = beta[p * 3 + 0], v1 = beta[p * 3 + 1], v2 = beta[p * 3 + 2];
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     const int ci = q ? c.c2b[p] : c.c2a[p];
-                    const double b0 = c.beta[ci * 3 + 0], b1 = c.beta[ci * 3 + 1], b2 = c.beta[ci * 3 + 2];
+                    const float b0 = beta[ci * 3 + 0], b1 = beta[ci * 3 + 1], b2 = beta[ci * 3 + 2];
                     const bool fx = c.fixZ[ci] == 1;
-                    v0 *= fma(gr, b1, (1 - gr) * b0);
-                    v1 *= fx ? b1 : fma(lr, b2, (1 - lr) * b1);
-                    v2 *= fx ? 0.0 : fma(1 - lr2, b2, lr2 * b1);
+                    v0 *= fmaf(gr, b1, (1 - gr) * b0);
+                    v1 *= fx ? b1 : fmaf(lr, b2, (1 - lr) * b1);
+                    v2 *= fx ? 0.0f : fmaf(1 - lr2, b2, lr2 * b1);
                 }
                 // exact power-of-two normalisation (the values are relative)
-                const double mx = fmax(v0, fmax(v1, v2));
+                const float mx = fmaxf(v0, fmaxf(v1, v2));
                 if (mx > 0) {
                     int ex;
-                    frexp(mx, &ex);
-                    v0 = ldexp(v0, -ex); v1 = ldexp(v1, -ex); v2 = ldexp(v2, -ex);
+                    frexpf(mx, &ex);
+                    v0 = ldexpf(v0, -ex); v1 = ldexpf(v1, -ex); v2 = ldexpf(v2, -ex);
                 }
-                c.beta[p * 3 + 0] = v0; c.beta[p * 3 + 1] = v1; c.beta[p * 3 + 2] = v2;
+                beta[p * 3 + 0] = v0; beta[p * 3 + 1] = v1; beta[p * 3 + 2] = v2;
             }
             __syncwarp();
         }
         if (lane == 0) {
-            double pr[3] = {0.5 * c.beta[c.root * 3 + 0], 0.5 * c.beta[c.root * 3 + 1], 0.0};
+            const float pr[3] = {0.5f * beta[c.root * 3 + 0], 0.5f * beta[c.root * 3 + 1], 0.0f};
             uint32_t wd[4];
             philox4x32_10((uint32_t)(pos >> 2), (uint32_t)(pos >> 34), 0u, 0u, dM.seed, 0u, wd);
-            int nn = categorical(3, pr, word_to_uniform(wd[pos & 3]));
+            int nn = categorical3f(pr, wd[pos & 3]);
             if (nn > 2) { err = 1; nn = c.Z[c.root]; }
             if (nn != c.Z[c.root]) c.changed[c.root] = 1;
             c.Z[c.root] = (int8_t)nn;
@@ -995,15 +1012,15 @@ __device__ int update_z_linear(Ctx<Real>& c, uint64_t pos) {
                 const int s = c.dlev_nodes[i];
                 const int zp = c.Z[c.par[s]];
                 const bool fx = c.fixZ[s] == 1;
-                const double b0 = c.beta[s * 3 + 0], b1 = c.beta[s * 3 + 1], b2 = c.beta[s * 3 + 2];
-                double pr[3];
-                if (zp == 0) { pr[0] = (1 - gr) * b0; pr[1] = gr * b1; pr[2] = 0.0; }
-                else if (zp == 1) { pr[0] = 0.0; pr[1] = fx ? b1 : (1 - lr) * b1; pr[2] = fx ? 0.0 : lr * b2; }
-                else { pr[0] = 0.0; pr[1] = fx ? 0.0 : lr2 * b1; pr[2] = fx ? 0.0 : (1 - lr2) * b2; }
+                const float b0 = beta[s * 3 + 0], b1 = beta[s * 3 + 1], b2 = beta[s * 3 + 2];
+                float pr[3];
+                if (zp == 0) { pr[0] = (1 - gr) * b0; pr[1] = gr * b1; pr[2] = 0.0f; }
+                else if (zp == 1) { pr[0] = 0.0f; pr[1] = fx ? b1 : (1 - lr) * b1; pr[2] = fx ? 0.0f : lr * b2; }
+                else { pr[0] = 0.0f; pr[1] = fx ? 0.0f : lr2 * b1; pr[2] = fx ? 0.0f : (1 - lr2) * b2; }
                 const uint64_t w = pos + 1 + (uint64_t)(c.n_nodes - 2 - c.pos[s]);
                 uint32_t wd[4];
                 philox4x32_10((uint32_t)(w >> 2), (uint32_t)(w >> 34), 0u, 0u, dM.seed, 0u, wd);
-                int nn = categorical(3, pr, word_to_uniform(wd[w & 3]));
+                int nn = categorical3f(pr, wd[w & 3]);
                 if (nn > 2) { err = 1; nn = c.Z[s]; }
                 if (nn != c.Z[s]) c.changed[s] = 1;
                 c.Z[s] = (int8_t)nn;
