@@ -244,3 +244,27 @@ def test_gbgc_filtered_elements(built):
         assert got[e]["status"] == r["status"]
         if r["status"] == 0:
             assert got[e]["loglik_all"] == r["loglik_all"]
+
+
+def test_gbgc_served_longer_element_recreates_slots(built):
+    """A submit whose element is longer than the serving slots hold lets the
+    running elements finish, re-creates the slots and goes on; every result
+    equals the batch path's."""
+    from phyloacc_gb300 import Context, abi, synth
+    ds = synth.make_dataset("st43", n_elements=60, seed=21)
+    short = [int(e) for e in np.flatnonzero(ds.lengths < 300)[:10]]
+    long_ = [int(e) for e in np.flatnonzero(ds.lengths > 700)[:2]]
+    assert len(short) == 10 and len(long_) == 2
+    o = abi.gbgc_default_opts(ds.target)
+    o.burnin, o.mcmc, o.seed, o.gapchar = 10, 30, 4, ord("-")
+    ref = {r["element_no"]: r for r in _ctx(ds, 1).gbgc_run(o, elements=short + long_)}
+    so = abi.default_opts()
+    so.precision = 1
+    ctx = Context(ds, so)
+    ctx.gbgc_submit(o, elements=short)
+    ctx.gbgc_submit(o, elements=long_)
+    ctx.gbgc_sync()
+    got = {r["element_no"]: r for r in ctx.gbgc_poll()}
+    assert sorted(got) == sorted(short + long_)
+    for e, r in got.items():
+        assert r["loglik_all"] == ref[e]["loglik_all"] and (r["max_z"] == ref[e]["max_z"]).all()
