@@ -1,5 +1,6 @@
 """Build the CUDA/C++ library in-tree: phyloacc_gb300/_build/libpaccgpu.so and
-the PhyloAcc-ST-compatible driver phyloacc_gb300/_build/phyloacc-st-gpu.
+the command-line drop-ins phyloacc_gb300/_build/phyloacc-st-gpu (PhyloAcc-ST)
+and phyloacc_gb300/_build/phyloacc-gbgc-gpu (PhyloAcc-ST-GBGC).
 
 sm_103a only (GB300); nvcc cross-compiles without a GPU."""
 import os

@@ -50,7 +50,7 @@ int main(int argc, char** argv) {
     const int n_states = argc > 8 ? atoi(argv[8]) : 3;
     PhyloProf profile = LoadPhyloProfiles(argv[2], argv[3]);
     PhyloTree tree = LoadPhyloTree(argv[1]);
-    // main.cpp:36-80 defaults (gBGC driver)
+    // main.cpp:36-80 defaults of the gBGC program
     BPP bpp(0, profile, tree, ".", argv[4], argv[5], 0.8, argv[6], "", -2, 0, 0, 1, 0.6, 5, 0.4, 5, 0.4, 4, 0.8, 0.2,
             1, 1, 7728, 0.1, 0.8, 0.01, 0.1, 0.8, false);
     bpp.InitMCMC(20, 60, 100);
