@@ -157,10 +157,11 @@ def make_workload(n, seed):
 ITERS = {"burnin": 500, "mcmc": 1500}
 
 
-# DRAM bytes per column-node update of chain_kernel<float> (ncu capture of
-# 608 elements x 60 iterations, 128 threads x 255 registers: 47.4 GB over
-# 1.666e9 updates)
-DRAM_BYTES_PER_UPDATE = 28.5
+# DRAM bytes per column-node update of chain_kernel<float> in the shape the
+# tuner serves with (ncu capture of 608 elements x 60 iterations, 128 threads
+# x 128 registers, four chains an SM: 55.1 GB over 1.666e9 updates; the
+# 255-register shape moved 28.5 bytes an update)
+DRAM_BYTES_PER_UPDATE = 33.1
 
 
 def hbm_peak_gbs():
@@ -497,7 +498,7 @@ def run_gpu(args, ws, rank, local):
                      "frac": achieved / fp32_peak, "traffic": traffic,
                      "work": "36 flop per internal-child edge-column + 4 per leaf-child edge-column (device counters)",
                      "peak_source": "measured FP32 FMA rate of this GPU (pacc_measure_fma_peak)",
-                     "traffic_source": "%.1f DRAM bytes per column-node update (ncu, 608 elements x 60 iterations) "
+                     "traffic_source": "%.1f DRAM bytes per column-node update (ncu, 608 elements x 60 iterations, 128 x 128 shape) "
                                        "x the launch's updates" % DRAM_BYTES_PER_UPDATE,
                      "hbm": {"achieved": traffic / dev / 1e9, "peak": hbm_peak, "unit": "GB/s",
                              "frac": traffic / dev / 1e9 / hbm_peak, "peak_source": hbm_src}},
