@@ -33,7 +33,11 @@ error     = FP32 against that FP64 leg on the same elements: posterior
             relative error at a fixed state per element
 config1   = the 12-taxon configuration (100 elements, BURNIN 500 + MCMC 1000,
             seed 0), FP32 and FP64, K timed steps each, with e2e
-serving   = an open-loop Poisson stream at 80% of `value`: p50/p99 latency
+serving   = the serving form of the 43-taxon workload: an open-loop Poisson
+            stream at 80% of `value` of elements whose lengths are log-normal
+            (median 250 bp, sigma 0.6) clipped at 50-5000 (--serve-elements
+            distinct elements of the same tree, cycled), admitted against a
+            150 GB device-memory budget: p50/p99 latency from arrival to result
 gbgc      = the gBGC model's configuration (PhyloAcc-ST-GBGC): 120-taxon Yule
             tree (total length 4.0, 20 targets in 6 clades), elements log-normal
             (median 300 bp, clipped 50-3000) with a GC-bias strength ~ Gamma(2, 1)
@@ -252,18 +256,23 @@ def time_gpu(ctx, ds, steps, warmup, ws, clocks=None):
     return kern, wall, cnt, res
 
 
+# device memory the serving form of the workload admits chains against
+SERVE_BUDGET_BYTES = 150 * 10**9
+
+
 def serve_latency(ds, throughput, seconds, sweeps, seed=1):
     """Open-loop serving at 80% of the batch throughput.
 
     Elements arrive as a Poisson process (rate 0.8 x throughput, cycling
-    through the workload); each poll runs one sweep step of the resident
-    chains and retires the finished ones.  Latency = time the result came back
+    through ds); the host feeds the persistent kernel's queue as they arrive
+    and retires results as chains finish.  Latency = time the result came back
     minus the element's scheduled arrival time, for elements arriving in the
     last two thirds of the window (after the slots have filled)."""
     import phyloacc_gb300 as pg
     from phyloacc_gb300 import abi
     o = opts_for(abi.PACC_FP32)
     o.sweeps_per_launch = sweeps
+    o.memory_budget_bytes = SERVE_BUDGET_BYTES
     ctx = pg.Context(ds, o)
     rate = 0.8 * throughput
     rng = np.random.default_rng(seed)
@@ -298,7 +307,11 @@ def serve_latency(ds, throughput, seconds, sweeps, seed=1):
     wall = time.perf_counter() - t0
     ctx.close()
     v = np.array(list(lat.values()))
+    lens = np.array([ds.element(e).shape[1] for e in range(E)])
     return {"load": 0.8, "arrival_rate": rate, "window_s": seconds, "sweeps_per_launch": sweeps,
+            "elements": {"distinct": E, "length_median": float(np.median(lens)), "length_max": int(lens.max()),
+                         "clip": [50, 5000]},
+            "memory_budget_bytes": SERVE_BUDGET_BYTES,
             "elements_measured": int(len(v)), "elements_submitted": int(k_next),
             "p50_ms": float(np.percentile(v, 50)) if len(v) else None,
             "p99_ms": float(np.percentile(v, 99)) if len(v) else None,
@@ -519,7 +532,9 @@ def run_gpu(args, ws, rank, local):
     if args.gbgc_elements > 0:
         line["gbgc"] = run_gbgc(args, K, ws, rank)
     if args.serve_seconds > 0:
-        line["serving"] = serve_latency(ds, value / ws, args.serve_seconds, args.serve_sweeps)
+        from phyloacc_gb300 import synth
+        ds_serve = synth.make_dataset("st43_serve", n_elements=args.serve_elements, seed=WORKLOAD_SEED + rank)
+        line["serving"] = serve_latency(ds_serve, value / ws, args.serve_seconds, args.serve_sweeps)
         line["latency_ms"] = {"p50": line["serving"]["p50_ms"], "p99": line["serving"]["p99_ms"]}
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count() or 1
@@ -730,6 +745,8 @@ def main():
                     help="FP32 chain kernel: registers a thread, 128/168/255 (0: the tuner's choice)")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the 80%%-load serving run (0: skip)")
+    ap.add_argument("--serve-elements", type=int, default=4096,
+                    help="distinct elements of the serving stream (lengths clipped 50-5000), cycled")
     ap.add_argument("--serve-sweeps", type=int, default=64,
                     help="serving on (>0) or off (0: one batched launch per step, the form an ncu "
                          "capture can replay)")

@@ -104,7 +104,8 @@ typedef struct pacc_opts {
     /* --- GPU keys (no counterpart in PhyloAcc-ST) --- */
     int32_t precision;            /* pacc_precision (PACC_FP64) */
     int32_t device;               /* CUDA device ordinal (0) */
-    int64_t memory_budget_bytes;  /* device bytes the context may hold for chain state (0 = 25% of free) */
+    int64_t memory_budget_bytes;  /* device bytes the context may hold for chain state (0 = 25% of free);
+                                     pacc_gbgc_run: for one launch's traces (0 = 16 GB) */
     int32_t max_resident;         /* max chains resident at once (0 = derived from the budget) */
     int32_t sweeps_per_launch;    /* MCMC iterations per kernel launch (0 = run chains to completion) */
     int32_t trace_iters;          /* record the first trace_iters iterations of every model (0 = off) */

@@ -979,7 +979,12 @@ static int gbgc_serve_setup(pacc_ctx* c, const pacc_gbgc_opts& g, int GGp_need) 
     v.out_b = (gbgc_out_bytes(N, v.T) + 255) & ~(size_t)255;
     const GbgcWs W = GbgcWs::make(N, S - 1, v.GGp_cap, gbgc_chain_warps(), v.prec ? 4 : 8);
     // slots: two queued elements per resident CTA, within the memory budget
-    const size_t budget = c->o.memory_budget_bytes > 0 ? (size_t)c->o.memory_budget_bytes : ((size_t)32 << 30);
+    size_t budget = (size_t)c->o.memory_budget_bytes;
+    if (budget == 0) {   // as the plain path: a quarter of the free device memory
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = fr / 4;
+    }
     const size_t fixed = W.total * v.grid + 4096;
     const size_t per_slot = sizeof(GbgcElemHdr) + v.blob_cap + v.out_b;
     if (budget <= fixed + per_slot) { c->err = "gbgc serving: memory budget too small"; return PACC_OOM; }
@@ -3346,8 +3351,8 @@ int pacc_gbgc_run(pacc_ctx* c, const pacc_gbgc_opts* go, const pacc_element_batc
     if (per_sm <= 0) { c->err = "gbgc_run: the chain kernel does not fit on an SM"; return PACC_ECUDA; }
     const GbgcWs W = GbgcWs::make(N, S - 1, GGp_max, gbgc_chain_warps(), prec ? 4 : 8);
     const size_t tzb_el = (size_t)3 * T * 2 * N;
-    // elements per launch: bounded by the trace and workspace budget
-    const size_t budget = (size_t)16 << 30;
+    // elements per launch: bounded by the traces' budget (opts.memory_budget_bytes, else 16 GB)
+    const size_t budget = c->o.memory_budget_bytes > 0 ? (size_t)c->o.memory_budget_bytes : ((size_t)16 << 30);
     const int grid_full = c->n_sm * per_sm;
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(run.size(), budget / (tzb_el + 256)));
     const int grid = std::max(1, std::min(grid_full, chunk));

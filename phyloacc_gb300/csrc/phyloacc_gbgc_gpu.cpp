@@ -11,7 +11,8 @@
 //   <PREFIX>_hyper.txt, <PREFIX>_species_names.txt and, with VERBOSE,
 //   <PREFIX>_mcmc_trace_{0,1,2}_{No}.txt.
 // The chains run on the GPU through pacc_gbgc_run (include/pacc.h).
-// Extra keys (ignored by the reference): GPU_PRECISION fp64|fp32, GPU_DEVICE.
+// Extra keys (ignored by the reference): GPU_PRECISION fp64|fp32, GPU_DEVICE,
+// GPU_MEMORY_BUDGET_GB (device memory for the traces of one launch).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -78,6 +79,7 @@ static GConfig load_config(const string& path) {
                  k == "SAMPLE_INDEL" || k == "NUM_THREAD" || k == "RESULT_INDIV") {}
         else if (k == "GPU_PRECISION") C.o.precision = (v == "fp32" || v == "FP32") ? PACC_FP32 : PACC_FP64;
         else if (k == "GPU_DEVICE") C.o.device = std::stoi(v);
+        else if (k == "GPU_MEMORY_BUDGET_GB") C.o.memory_budget_bytes = (int64_t)(std::stod(v) * 1e9);
         else std::cout << "Unknown parameter: " << k << ", skipping..." << std::endl;
     }
     C.phytree = trim(C.phytree, " \"\t\n");
