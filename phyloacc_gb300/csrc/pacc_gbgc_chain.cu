@@ -179,7 +179,7 @@ __device__ __forceinline__ Real warp_sum_real(Real v) {
 // Scalars of one CTA's chain.
 struct GbgcScalars {
     double tm[2][3][3], lt[2][3][3];   // Z transition [outgroup path][child Z][parent Z] and its log
-    float tmf[2][3][3];                // the transition in FP32 (the FP32 message pass)
+    float tmf[2][3][3], ltf[2][3][3];  // the transition and its log in FP32 (the FP32 message pass)
     double ec_gc[2], ec_mis[2];        // emission constants: log(1 - c) / log(c); log(1 - cons2mis) / log(1 - ncons2mis)
     double lmis[4];                    // log(1 - ncons2mis), log(1 - cons2mis), log(ncons2mis), log(cons2mis)
     double pr_lg[3], pr_alb[3];        // lgamma(a) and a log(b) of the conserved, accelerated and GC-bias priors
@@ -188,6 +188,7 @@ struct GbgcScalars {
     double tl, tl_next, full;          // trace_loglik[m], trace_loglik[m + 1], trace_full_loglik[m]
     double r_n, r_c, r_gb;             // rates of iteration m
     double x_n, x_c, x_gb;             // the rate proposal
+    double lg_x[4];                    // at the chain's (x_gb, x_n, x_c): the three prior terms, log(-x_c)
     double loglik_old, elbo_old, colsum;
     double sel[5], bias[5];
     uint64_t pos;
@@ -203,6 +204,10 @@ struct GbgcCtx {
     const double* dist;
     const uint8_t* masks;
     double *wc, *emis, *emis_tmp, *lpb, *eraw, *colsum;
+    // FP32 partials: log_prob_back as lpo[s] + lpr[s][k] (an FP64 offset a
+    // node and six FP32 values), in the memory of lpb
+    float* lpr;
+    double* lpo;
     Real *lP, *post, *pm, *part;   // log P, expected counts, P, partials in the partials' type
     int32_t* scl;
     Real* Pcur;
@@ -220,20 +225,6 @@ struct GbgcCtx {
     }
     __device__ int32_t* expo(int buf, int s, int g) const { return scl + ((size_t)buf * n_int + irank[s]) * GGp + g; }
 };
-
-// log of a branch-matrix entry for the emissions.  With FP64 partials in FP64;
-// with FP32 partials in FP32 (and so the emissions' dot products), the
-// diagonal (close to 1 on short branches) as log1p of its distance from 1,
-// taken in FP64 -- an error below the one the FP32 partials already put on
-// the expected counts it multiplies.
-template <typename Real>
-__device__ __forceinline__ Real branch_log(double v, bool diag);
-template <>
-__device__ __forceinline__ double branch_log<double>(double v, bool) { return d_log(v); }
-template <>
-__device__ __forceinline__ float branch_log<float>(double v, bool diag) {
-    return diag ? log1pf((float)(v - 1.0)) : logf((float)v);
-}
 
 // Branch matrices of nc classes (cls[i], selection sel[i], bias bias[i]) into
 // cache set `set`; neutral classes are skipped on fixed branches.
@@ -295,11 +286,39 @@ __device__ void build_caches(const GbgcChainParams& p, const GbgcCtx<Real>& G, i
         const int sl = G.slot(cls[ci], set);
         Real* lo = G.lp(sl, s);
         Real* po = G.pmat(sl, s);
+        if constexpr (sizeof(Real) == 4) {
+            // FP32 partials: log P in FP32 (an error below the one the
+            // partials put on the expected counts it multiplies), one
+            // conversion an entry; the diagonal (close to 1 on short
+            // branches) as log1p of minus its row's off-diagonal sum (rows of
+            // exp(dQ) sum to one)
+            float ef[16];
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-            const double v = E[(q & 3) * 4 + (q >> 2)];   // (child q/4, parent q%4) = E[parent][child]
-            lo[q] = branch_log<Real>(v, (q & 3) == (q >> 2));
-            po[q] = (Real)v;
+            for (int q = 0; q < 16; q++) ef[q] = (float)E[q];
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int r = q & 3, c = q >> 2;   // (child c, parent r) = E[r][c]
+                const float v = ef[r * 4 + c];
+                float l;
+                if (r == c) {
+                    float off = 0;
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (j != r) off += ef[r * 4 + j];
+                    l = log1pf(-off);
+                } else {
+                    l = logf(v);
+                }
+                lo[q] = l;
+                po[q] = v;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const double v = E[(q & 3) * 4 + (q >> 2)];   // (child q/4, parent q%4) = E[parent][child]
+                lo[q] = d_log(v);
+                po[q] = (Real)v;
+            }
         }
     }
     if (p.flop) {
@@ -373,51 +392,134 @@ __device__ __forceinline__ void lm63<float>(const GbgcScalars& sc, int u, const 
 // for every non-root c, bottom-up.
 template <typename Real>
 __device__ void up_pass(const GbgcCtx<Real>& G, const GbgcScalars& sc, bool half) {
-    for (int h = 0; h < G.n_hlev; h++) {
-        const int a = G.hlev[h], b = G.hlev[h + 1];
-        for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
-            const int p = G.hnodes[it];
-            double acc[6];
+    if constexpr (sizeof(Real) == 4) {
+        // FP32 partials: the values relative to each node's FP64 offset in
+        // FP32; a child's maximum goes to the parent's offset, so FP64 work
+        // is two additions a child (the FP64 pipe is narrow and these
+        // levels run on few threads)
+        for (int h = 0; h < G.n_hlev; h++) {
+            const int a = G.hlev[h], b = G.hlev[h + 1];
+            for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
+                const int p = G.hnodes[it];
+                float acc[6];
 #pragma unroll
-            for (int r = 0; r < 6; r++) acc[r] = G.lpb[p * 6 + r];
-            const int ch[2] = {G.c0[p], G.c1[p]};
-            for (int q = 0; q < 2; q++) {
-                const int c = ch[q];
-                const double* y = G.lpb + c * 6;
-                double mx = y[0];
+                for (int r = 0; r < 6; r++) acc[r] = G.lpr[p * 6 + r];
+                double off = G.lpo[p];
+                const int ch[2] = {G.c0[p], G.c1[p]};
+                for (int q = 0; q < 2; q++) {
+                    const int c = ch[q];
+                    const float* y = G.lpr + c * 6;
+                    float mx = y[0];
 #pragma unroll
-                for (int r = 1; r < 6; r++) mx = fmax(mx, y[r]);
-                double t[3];
-                if (mx == -CUDART_INF) {
-                    t[0] = t[1] = t[2] = -CUDART_INF;
-                } else {
-                    lm63<Real>(sc, G.upper(c), y, mx, t);
+                    for (int r = 1; r < 6; r++) mx = fmaxf(mx, y[r]);
+                    float t[3];
+                    if (mx == -CUDART_INF_F) {
+                        t[0] = t[1] = t[2] = -CUDART_INF_F;
+                    } else {
+                        const float (*tm)[3] = sc.tmf[G.upper(c)];
+                        float ez[3];
 #pragma unroll
-                    for (int j = 0; j < 3; j++)
-                        if (half) t[j] -= LN2;
+                        for (int z = 0; z < 3; z++) ez[z] = expf(y[z] - mx) + expf(y[z + 3] - mx);
+#pragma unroll
+                        for (int j = 0; j < 3; j++) {
+                            float v = 0;
+#pragma unroll
+                            for (int z = 0; z < 3; z++) v += tm[z][j] * ez[z];
+                            t[j] = logf(v) - (half ? (float)LN2 : 0.0f);
+                        }
+                        off += G.lpo[c] + (double)mx;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        acc[j] += t[j];
+                        acc[3 + j] += t[j];
+                    }
                 }
 #pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    acc[j] += t[j];
-                    acc[3 + j] += t[j];
-                }
+                for (int r = 0; r < 6; r++) G.lpr[p * 6 + r] = acc[r];
+                G.lpo[p] = off;
             }
-#pragma unroll
-            for (int r = 0; r < 6; r++) G.lpb[p * 6 + r] = acc[r];
+            __syncthreads();
         }
-        __syncthreads();
+    } else {
+        for (int h = 0; h < G.n_hlev; h++) {
+            const int a = G.hlev[h], b = G.hlev[h + 1];
+            for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
+                const int p = G.hnodes[it];
+                double acc[6];
+    #pragma unroll
+                for (int r = 0; r < 6; r++) acc[r] = G.lpb[p * 6 + r];
+                const int ch[2] = {G.c0[p], G.c1[p]};
+                for (int q = 0; q < 2; q++) {
+                    const int c = ch[q];
+                    const double* y = G.lpb + c * 6;
+                    double mx = y[0];
+    #pragma unroll
+                    for (int r = 1; r < 6; r++) mx = fmax(mx, y[r]);
+                    double t[3];
+                    if (mx == -CUDART_INF) {
+                        t[0] = t[1] = t[2] = -CUDART_INF;
+                    } else {
+                        lm63<Real>(sc, G.upper(c), y, mx, t);
+    #pragma unroll
+                        for (int j = 0; j < 3; j++)
+                            if (half) t[j] -= LN2;
+                    }
+    #pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        acc[j] += t[j];
+                        acc[3 + j] += t[j];
+                    }
+                }
+    #pragma unroll
+                for (int r = 0; r < 6; r++) G.lpb[p * 6 + r] = acc[r];
+            }
+            __syncthreads();
+        }
     }
+}
+
+// log_prob_back of the root's first class (the integrated log-likelihood).
+template <typename Real>
+__device__ __forceinline__ double lpb_root(const GbgcCtx<Real>& G) {
+    if constexpr (sizeof(Real) == 4) return G.lpo[G.root] + (double)G.lpr[G.root * 6];
+    else return G.lpb[G.root * 6];
 }
 
 // lpb = src on the branches, 0 at the root, then the message pass.
 template <typename Real>
 __device__ void prob_back(const GbgcCtx<Real>& G, const GbgcScalars& sc, const double* src) {
-    for (int i = threadIdx.x; i < G.nn * 6; i += blockDim.x) {
-        const int s = G.nodes[i / 6];
-        G.lpb[s * 6 + i % 6] = (s == G.root) ? 0.0 : src[s * 6 + i % 6];
+    if constexpr (sizeof(Real) == 4) {
+        // offset: the node's largest finite value
+        for (int k = threadIdx.x; k < G.nn; k += blockDim.x) {
+            const int s = G.nodes[k];
+            if (s == G.root) {
+                G.lpo[s] = 0;
+#pragma unroll
+                for (int r = 0; r < 6; r++) G.lpr[s * 6 + r] = 0.0f;
+                continue;
+            }
+            double v[6], m = -CUDART_INF;
+#pragma unroll
+            for (int r = 0; r < 6; r++) {
+                v[r] = src[s * 6 + r];
+                if (v[r] > m && v[r] < CUDART_INF) m = v[r];
+            }
+            if (m == -CUDART_INF) m = 0;
+            G.lpo[s] = m;
+#pragma unroll
+            for (int r = 0; r < 6; r++) G.lpr[s * 6 + r] = (float)(v[r] - m);
+        }
+        __syncthreads();
+        up_pass(G, sc, false);
+    } else {
+        for (int i = threadIdx.x; i < G.nn * 6; i += blockDim.x) {
+            const int s = G.nodes[i / 6];
+            G.lpb[s * 6 + i % 6] = (s == G.root) ? 0.0 : src[s * 6 + i % 6];
+        }
+        __syncthreads();
+        up_pass(G, sc, false);
     }
-    __syncthreads();
-    up_pass(G, sc, false);
 }
 
 // The current class's matrices of every branch into shared memory.
@@ -553,7 +655,8 @@ __device__ __forceinline__ Real warp_reduce_scatter16(Real* v) {
 template <typename Real>
 __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf, Real* dst) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double* wc = G.wc + (size_t)w * G.N * 16;
+    // per-warp sums in the partials' type (FP32 sums stay off the FP64 pipe)
+    Real* wc = (Real*)G.wc + (size_t)w * G.N * 16;
     for (int i = lane; i < G.N * 16; i += 32) wc[i] = 0;
     __syncwarp();
     {
@@ -577,7 +680,7 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             }
         }
         const Real sum = warp_reduce_scatter16(acc);
-        if ((lane & 1) == 0) wc[G.root * 16 + (lane >> 1)] = (double)sum;
+        if ((lane & 1) == 0) wc[G.root * 16 + (lane >> 1)] = sum;
     }
     for (int k = G.nn - 2; k >= 0; k--) {
         const int s = G.nodes[k];
@@ -614,15 +717,34 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             }
         }
         const Real sum = warp_reduce_scatter16(acc);
-        if ((lane & 1) == 0) wc[s * 16 + (lane >> 1)] = (double)sum;
+        if ((lane & 1) == 0) wc[s * 16 + (lane >> 1)] = sum;
     }
     __syncthreads();
+    const Real* wa = (const Real*)G.wc;
     for (int i = threadIdx.x; i < G.N * 16; i += blockDim.x) {
-        double t = 0;
-        for (int v = 0; v < GB_WARPS; v++) t += G.wc[(size_t)v * G.N * 16 + i];
-        dst[i] = (Real)t;
+        Real t = 0;
+        for (int v = 0; v < GB_WARPS; v++) t += wa[(size_t)v * G.N * 16 + i];
+        dst[i] = t;
     }
     __syncthreads();
+}
+
+// Inverse-CDF draw over K unnormalised FP32 weights with the 24-bit uniform
+// ((w >> 8) + 0.5) 2^-24 of word w: the first k with u * total below the
+// k-th cumulative sum.
+__device__ __forceinline__ int categorical_f(int K, const float* p, uint32_t w) {
+    const float u = ((float)(w >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    float tot = 0;
+    for (int k = 0; k < K; k++) tot += p[k];
+    const float t = u * tot;
+    float cum = 0;
+    for (int k = 0; k < K; k++) {
+        cum += p[k];
+        if (t < cum) return k;
+    }
+    for (int k = K - 1; k >= 0; k--)
+        if (p[k] > 0) return k;
+    return K;
 }
 
 // The categorical weights of Z/B sampling: FP64, or FP32 with FP32 partials.
@@ -641,8 +763,36 @@ __device__ void sample_zb(const GbgcChainParams& p, const GbgcCtx<Real>& G, Gbgc
             const int s = G.dnodes[it], pz = G.Z[G.par[s]];
             StreamReader rd;
             rd.init(p.seed, sc.pos + (uint64_t)(G.nn - 2 - G.pidx[s]));
-            const double u = rd.uniform();
             const int old = G.Z[s];
+            if constexpr (sizeof(Real) == 4) {
+                // FP32 weights from the FP32 values (the node's offset cancels)
+                // and the word's 24-bit uniform
+                const uint32_t wd = rd.word_at(rd.pos);
+                const float* y = G.lpr + s * 6;
+                if (pz != 2) {
+                    float x[6], wv[6];
+                    const int up = G.upper(s);
+#pragma unroll
+                    for (int r = 0; r < 6; r++) x[r] = sc.ltf[up][r % 3][pz] + y[r];
+                    float mx = x[0];
+#pragma unroll
+                    for (int r = 1; r < 6; r++) mx = fmaxf(mx, x[r]);
+#pragma unroll
+                    for (int r = 0; r < 6; r++) wv[r] = expf(x[r] - mx);
+                    const int nn = categorical_f(6, wv, wd);
+                    G.Z[s] = (int8_t)(nn % 3);
+                    if (!G.missing(s)) G.B[s] = nn > 2 ? 1 : 0;
+                } else {
+                    G.Z[s] = 2;
+                    const float mx = fmaxf(y[2], y[5]);
+                    const float wv[2] = {expf(y[2] - mx), expf(y[5] - mx)};
+                    const int nn = categorical_f(2, wv, wd);
+                    if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
+                }
+                if (old != G.Z[s]) sc.changed = 1;
+                continue;
+            }
+            const double u = rd.uniform();
             const double* y = G.lpb + s * 6;
             if (pz != 2) {
                 double x[6], wv[6];
@@ -789,6 +939,8 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
         G.lP = (Real*)(ws + W.lP); G.pm = (Real*)(ws + W.pm); G.post = (Real*)(ws + W.post);
         G.wc = (double*)(ws + W.wc); G.emis = (double*)(ws + W.emis); G.emis_tmp = (double*)(ws + W.emis_tmp);
         G.lpb = (double*)(ws + W.lpb); G.eraw = (double*)(ws + W.eraw); G.colsum = (double*)(ws + W.colsum);
+        G.lpr = (float*)G.lpb;
+        G.lpo = (double*)(G.lpr + (size_t)N * 6);   // 24 N + 8 N bytes within lpb's 48 N
         G.part = (Real*)(ws + W.part); G.scl = (int32_t*)(ws + W.scl);
         if (tid == 0) {
             for (int q = 0; q < 8; q++) s_ph[q] = 0;
@@ -806,6 +958,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                         sc.tm[u][a][b] = t[a][b];
                         sc.tmf[u][a][b] = (float)t[a][b];
                         sc.lt[u][a][b] = d_log(t[a][b]);
+                        sc.ltf[u][a][b] = (float)sc.lt[u][a][b];
                     }
             }
             sc.ec_gc[0] = d_log(1 - p.gcc);
@@ -882,10 +1035,14 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             const double lnc = d_log(p.nc2m), lc = d_log(p.c2m);
             for (int i = tid; i < N * 6; i += blockDim.x) {
                 const int s = i / 6, j = i % 6;
-                double v = 0;
-                G.lpb[i] = 0;
-                if (G.fixZ[s] == 1 && j % 3 == 2) { v = -CUDART_INF; G.lpb[i] = -CUDART_INF; }
-                G.emis[i] = v;
+                const bool ban = G.fixZ[s] == 1 && j % 3 == 2;
+                if constexpr (sizeof(Real) == 4) {
+                    G.lpr[i] = ban ? -CUDART_INF_F : 0.0f;
+                    if (j == 0) G.lpo[s] = 0;
+                } else {
+                    G.lpb[i] = ban ? -CUDART_INF : 0.0;
+                }
+                G.emis[i] = ban ? -CUDART_INF : 0.0;
             }
             __syncthreads();
             for (int k = tid; k < G.nn - 1; k += blockDim.x) {
@@ -898,7 +1055,7 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
             }
             __syncthreads();
             up_pass(G, sc, true);
-            if (tid == 0) sc.logpZC = G.lpb[G.root * 6];
+            if (tid == 0) sc.logpZC = lpb_root(G);
             __syncthreads();
             // ---- Gibbs (bpp_c.cpp:259-349) ----
             stage_pcur(G, sc.cur);
@@ -973,14 +1130,22 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                 }
                 prob_back(G, sc, G.emis);
                 if (tid == 0) {
-                    sc.loglik_old = G.lpb[G.root * 6];
+                    sc.loglik_old = lpb_root(G);
                     sc.acc = sc.cur;
                 }
                 for (int i = tid; i < N * 6; i += blockDim.x) G.emis_tmp[i] = G.emis[i];
                 __syncthreads();
                 GB_MARK(2)
                 // sample_rates: three MH moves of (gB, n, c) with Z and B integrated out
-                if (tid == 0) { sc.x_gb = sc.r_gb; sc.x_n = sc.r_n; sc.x_c = sc.r_c; }
+                if (tid == 0) {
+                    sc.x_gb = sc.r_gb; sc.x_n = sc.r_n; sc.x_c = sc.r_c;
+                    // the current values' terms of the MH ratio, computed once
+                    // and carried over to an accepted proposal's
+                    sc.lg_x[0] = lgpdf(sc.x_gb, p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2]);
+                    sc.lg_x[1] = resZ != 0 ? lgpdf(__dadd_rn(sc.x_n, p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1]) : 0.0;
+                    sc.lg_x[2] = lgpdf(-sc.x_c, p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0]);
+                    sc.lg_x[3] = d_log(-sc.x_c);
+                }
                 for (int mm = 0; mm < 3; mm++) {
                     __shared__ double cur3[3];
                     if (tid == 0) {
@@ -1013,21 +1178,21 @@ __global__ void __launch_bounds__(GB_BT, MINB) gbgc_chain_kernel(GbgcChainParams
                     emissions(G, sc, G.emis_tmp, 1, sc.prop, post, false);
                     prob_back(G, sc, G.emis_tmp);
                     if (tid == 0) {
-                        const double lr = G.lpb[G.root * 6];
+                        const double lr = lpb_root(G);
                         const double ngb = sc.bias[2], nn_ = sc.sel[1], nc_ = sc.sel[0];
-                        double MH = __dsub_rn(__dadd_rn(__dsub_rn(lr, sc.loglik_old), lgpdf(ngb, p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2])),
-                                              lgpdf(cur3[0], p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2]));
-                        if (resZ != 0)
-                            MH = __dadd_rn(MH, __dsub_rn(lgpdf(__dadd_rn(nn_, p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1]),
-                                                         lgpdf(__dadd_rn(cur3[1], p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1])));
-                        MH = __dadd_rn(MH, __dadd_rn(__dsub_rn(__dsub_rn(lgpdf(-nc_, p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0]),
-                                                                         lgpdf(-cur3[2], p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0])),
-                                                               d_log(-nc_)),
-                                                     d_log(-cur3[2])));
+                        // the proposal's terms; the current values' are in lg_x
+                        const double ly[4] = {
+                            lgpdf(ngb, p.gca, p.gcb, sc.pr_lg[2], sc.pr_alb[2]),
+                            resZ != 0 ? lgpdf(__dadd_rn(nn_, p.nshift), p.na, p.nb, sc.pr_lg[1], sc.pr_alb[1]) : 0.0,
+                            lgpdf(-nc_, p.ca, p.cb, sc.pr_lg[0], sc.pr_alb[0]), d_log(-nc_)};
+                        double MH = __dsub_rn(__dadd_rn(__dsub_rn(lr, sc.loglik_old), ly[0]), sc.lg_x[0]);
+                        if (resZ != 0) MH = __dadd_rn(MH, __dsub_rn(ly[1], sc.lg_x[1]));
+                        MH = __dadd_rn(MH, __dadd_rn(__dsub_rn(__dsub_rn(ly[2], sc.lg_x[2]), ly[3]), sc.lg_x[3]));
                         const bool acc = d_log(rng.uniform()) < MH;
                         sc.changed = acc ? 1 : 0;
                         if (acc) {
                             sc.x_gb = ngb; sc.x_n = nn_; sc.x_c = nc_;
+                            for (int q = 0; q < 4; q++) sc.lg_x[q] = ly[q];
                             sc.loglik_old = lr;
                             sc.acc = sc.prop;
                         }
