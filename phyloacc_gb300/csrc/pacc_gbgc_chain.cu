@@ -226,6 +226,22 @@ struct GbgcCtx {
     __device__ int32_t* expo(int buf, int s, int g) const { return scl + ((size_t)buf * n_int + irank[s]) * GGp + g; }
 };
 
+// 16-byte accesses of a 4-vector (a column's partial, a row of P): float4,
+// or two double2 (partials and shared rows are 16-byte aligned).
+__device__ __forceinline__ void ldv4(const float* p, float* x) {
+    const float4 v = *(const float4*)p;
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void ldv4(const double* p, double* x) {
+    const double2 a = ((const double2*)p)[0], b = ((const double2*)p)[1];
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+}
+__device__ __forceinline__ void stv4(float* p, const float* x) { *(float4*)p = make_float4(x[0], x[1], x[2], x[3]); }
+__device__ __forceinline__ void stv4(double* p, const double* x) {
+    ((double2*)p)[0] = make_double2(x[0], x[1]);
+    ((double2*)p)[1] = make_double2(x[2], x[3]);
+}
+
 // Branch matrices of nc classes (cls[i], selection sel[i], bias bias[i]) into
 // cache set `set`; neutral classes are skipped on fixed branches.
 template <typename Real>
@@ -339,10 +355,16 @@ __device__ void emissions(const GbgcCtx<Real>& G, const GbgcScalars& sc, double*
     for (int it = threadIdx.x; it < nb * ncl; it += blockDim.x) {
         const int s = G.nodes[it / ncl], j = lo + it % ncl;
         if (G.missing(s) || (G.fixZ[s] == 1 && j % 3 == 2)) continue;
-        const Real* a = G.lp(G.slot(j, set), s);
-        const Real* b = post + (size_t)s * 16;
+        Real a[16], b[16];
+#pragma unroll
+        for (int q = 0; q < 16; q += 4) {
+            ldv4(G.lp(G.slot(j, set), s) + q, a + q);
+            ldv4(post + (size_t)s * 16 + q, b + q);
+        }
         Real tr = 0;
+#pragma unroll
         for (int c = 0; c < 4; c++)
+#pragma unroll
             for (int r = 0; r < 4; r++) tr += a[r * 4 + c] * b[r * 4 + c];
         double t = (double)tr;
         if (raw && j == G.Z[s] + 3 * G.B[s]) G.eraw[s] = t;
@@ -549,6 +571,21 @@ __device__ __forceinline__ double column_loglik(const float* L, const double* pi
     return t > 0 ? (double)logf(t) + (double)e * LN2 : -CUDART_INF;
 }
 
+// gbgc_message with P's rows read as 4-vectors (the same arithmetic).
+template <typename Real>
+__device__ __forceinline__ void message_v(const Real* P, const Real* L, Real* m) {
+    Real r0[4], r1[4], r2[4], r3[4];
+    ldv4(P, r0); ldv4(P + 4, r1); ldv4(P + 8, r2); ldv4(P + 12, r3);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        Real v = r0[j] * L[0];
+        v = fma(r1[j], L[1], v);
+        v = fma(r2[j], L[2], v);
+        v = fma(r3[j], L[3], v);
+        m[j] = v;
+    }
+}
+
 template <typename Real>
 __device__ __forceinline__ void leaf_or_partial(const GbgcCtx<Real>& G, int buf, int s, int g, Real* L, int* e) {
     if (s < G.S) {
@@ -557,9 +594,7 @@ __device__ __forceinline__ void leaf_or_partial(const GbgcCtx<Real>& G, int buf,
         for (int i = 0; i < 4; i++) L[i] = ((msk >> i) & 1) ? Real(1) : Real(0);
         *e = 0;
     } else {
-        const Real* q = G.partial(buf, s, g);
-#pragma unroll
-        for (int i = 0; i < 4; i++) L[i] = q[i];
+        ldv4(G.partial(buf, s, g), L);
         *e = *G.expo(buf, s, g);
     }
 }
@@ -584,7 +619,7 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
                 Real L[4], m[4];
                 int ec;
                 leaf_or_partial(G, buf, c, g, L, &ec);
-                gbgc_message(G.Pcur + c * 16, L, m);
+                message_v(G.Pcur + c * 16, L, m);
 #pragma unroll
                 for (int j = 0; j < 4; j++) a[j] *= m[j];
                 e += ec;
@@ -597,9 +632,7 @@ __device__ void prune(const GbgcChainParams& p, const GbgcCtx<Real>& G, GbgcScal
                 for (int j = 0; j < 4; j++) a[j] = (a[j] * f1) * f2;
                 e -= sh;
             }
-            Real* o = G.partial(buf, s, g);
-#pragma unroll
-            for (int j = 0; j < 4; j++) o[j] = a[j];
+            stv4(G.partial(buf, s, g), a);
             *G.expo(buf, s, g) = e;
         }
         if (g < G.GG) {
@@ -671,13 +704,13 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             Real wr[4], tot = 0;
 #pragma unroll
             for (int j = 0; j < 4; j++) { wr[j] = Lr[j] * (Real)p.pi[j]; tot += wr[j]; }
-            Real* qr = G.partial(buf, G.root, g);
+            Real qv[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const Real q = tot > 0 ? gb_div(wr[j], tot) : Real(0);
-                acc[j * 4] += q;
-                qr[j] = q;
+                qv[j] = tot > 0 ? gb_div(wr[j], tot) : Real(0);
+                acc[j * 4] += qv[j];
             }
+            stv4(G.partial(buf, G.root, g), qv);
         }
         const Real sum = warp_reduce_scatter16(acc);
         if ((lane & 1) == 0) wc[G.root * 16 + (lane >> 1)] = sum;
@@ -693,8 +726,19 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
             Real L[4], m[4];
             int es;
             leaf_or_partial(G, buf, s, g, L, &es);
-            gbgc_message(P, L, m);
-            const Real* qp = G.partial(buf, G.par[s], g);
+            // P's rows once for the message and the joint terms
+            Real pr[4][4];
+            ldv4(P, pr[0]); ldv4(P + 4, pr[1]); ldv4(P + 8, pr[2]); ldv4(P + 12, pr[3]);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                Real v = pr[0][j] * L[0];
+                v = fma(pr[1][j], L[1], v);
+                v = fma(pr[2][j], L[2], v);
+                v = fma(pr[3][j], L[3], v);
+                m[j] = v;
+            }
+            Real qp[4];
+            ldv4(G.partial(buf, G.par[s], g), qp);
             Real r[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) r[j] = m[j] > 0 ? gb_div(qp[j], m[j]) : Real(0);
@@ -704,17 +748,13 @@ __device__ void counts(const GbgcChainParams& p, const GbgcCtx<Real>& G, int buf
                 Real a = 0;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const Real jt = r[j] * P[i * 4 + j] * L[i];
+                    const Real jt = r[j] * pr[i][j] * L[i];
                     a += jt;
                     acc[i * 4 + j] += jt;
                 }
                 qs[i] = a;
             }
-            if (s >= G.S) {
-                Real* o = G.partial(buf, s, g);
-#pragma unroll
-                for (int i = 0; i < 4; i++) o[i] = qs[i];
-            }
+            if (s >= G.S) stv4(G.partial(buf, s, g), qs);
         }
         const Real sum = warp_reduce_scatter16(acc);
         if ((lane & 1) == 0) wc[s * 16 + (lane >> 1)] = sum;
