@@ -216,7 +216,9 @@ def test_gbgc_cli_chain_zero_and_unbuilt_modes(tmp_path):
         shutil.copy(os.path.join(src, f), tmp_path / f)
     (tmp_path / "out").mkdir()
     base = [ln for ln in open(os.path.join(src, "case.cfg")).read().splitlines() if not ln.startswith("CHAIN ")]
-    (tmp_path / "case.cfg").write_text("\n".join(base + ["CHAIN 0"]) + "\n")
+    # the GPU keys the reference skips as unknown are taken without a device
+    gpu_keys = ["GPU_PRECISION fp32", "GPU_DEVICE 0", "GPU_MEMORY_BUDGET_GB 2.5"]
+    (tmp_path / "case.cfg").write_text("\n".join(base + ["CHAIN 0"] + gpu_keys) + "\n")
     r = subprocess.run([CLI_GBGC, "case.cfg"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert sorted(os.listdir(tmp_path / "out")) == ["case_hyper.txt", "case_rate_postZ_0.txt", "case_rate_postZ_1.txt",
