@@ -315,9 +315,12 @@ typedef struct pacc_gbgc_result {
  * the device (one CTA an element; the element loop of main.cpp:383-412 with
  * BPP_C, initMCMC, Gibbs, Eval2 and Output_init per model).  The context gives
  * the tree, rate matrix, outgroup and conserved sets and the precision of the
- * partials (PACC_FP32 / PACC_FP32_WARP: FP32, else FP64); its other options
- * are not used.  Eval2 and Output_init run on the host from the device's
- * traces.  Returns when every element's result is written. */
+ * partials (PACC_FP32 / PACC_FP32_WARP: FP32, else FP64), the device memory
+ * for one launch's traces (memory_budget_bytes, 0 = 16 GB; more elements run
+ * as several launches) and the chain kernel's register budget
+ * (register_budget 168: three CTAs an SM, else 96 registers and five); its
+ * other options are not used.  Eval2 and Output_init run on the host from
+ * the device's traces.  Returns when every element's result is written. */
 int pacc_gbgc_run(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_batch* batch,
                   pacc_gbgc_result* out);
 
@@ -333,7 +336,8 @@ int pacc_gbgc_run(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_
  * time from submit to collection.  sync returns when every submitted element
  * has finished (their results stay for poll).  The blocks leave after
  * opts.serve_idle_ns of the context without work; opts.max_resident (> 0)
- * caps the device slots (default: two per resident CTA). */
+ * caps the device slots (default: two per resident CTA), within
+ * opts.memory_budget_bytes (0 = a quarter of the free device memory). */
 int pacc_gbgc_submit(pacc_ctx* ctx, const pacc_gbgc_opts* opts, const pacc_element_batch* batch);
 int pacc_gbgc_poll(pacc_ctx* ctx, pacc_gbgc_result* out, int max);
 int pacc_gbgc_sync(pacc_ctx* ctx);
