@@ -376,13 +376,9 @@ __device__ void emissions(const GbgcCtx<Real>& G, const GbgcScalars& sc, double*
 }
 
 // log_multi of the 6 x 3 log_TM_Int by log_prob_back y (max mx), in linear
-// space: t_j = mx + log(sum_z TM[z][j] (e^(y_z - mx) + e^(y_(z+3) - mx))).
-// With FP32 partials the exponentials and logarithm are FP32 (differences and
-// sums of the FP64 log values stay FP64).
-template <typename Real>
-__device__ __forceinline__ void lm63(const GbgcScalars& sc, int u, const double* y, double mx, double* t);
-template <>
-__device__ __forceinline__ void lm63<double>(const GbgcScalars& sc, int u, const double* y, double mx, double* t) {
+// space: t_j = mx + log(sum_z TM[z][j] (e^(y_z - mx) + e^(y_(z+3) - mx))), in
+// FP64 (the FP64-partial path; the FP32 path's message pass has its own form).
+__device__ __forceinline__ void lm63(const GbgcScalars& sc, int u, const double* y, double mx, double* t) {
     const double (*tm)[3] = sc.tm[u];
     double ez[3];
 #pragma unroll
@@ -393,20 +389,6 @@ __device__ __forceinline__ void lm63<double>(const GbgcScalars& sc, int u, const
 #pragma unroll
         for (int z = 0; z < 3; z++) v += tm[z][j] * ez[z];
         t[j] = d_log(v) + mx;
-    }
-}
-template <>
-__device__ __forceinline__ void lm63<float>(const GbgcScalars& sc, int u, const double* y, double mx, double* t) {
-    const float (*tm)[3] = sc.tmf[u];
-    float ez[3];
-#pragma unroll
-    for (int z = 0; z < 3; z++) ez[z] = expf((float)(y[z] - mx)) + expf((float)(y[z + 3] - mx));
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        float v = 0;
-#pragma unroll
-        for (int z = 0; z < 3; z++) v += tm[z][j] * ez[z];
-        t[j] = (double)logf(v) + mx;
     }
 }
 
@@ -469,31 +451,31 @@ __device__ void up_pass(const GbgcCtx<Real>& G, const GbgcScalars& sc, bool half
             for (int it = a + threadIdx.x; it < b; it += blockDim.x) {
                 const int p = G.hnodes[it];
                 double acc[6];
-    #pragma unroll
+#pragma unroll
                 for (int r = 0; r < 6; r++) acc[r] = G.lpb[p * 6 + r];
                 const int ch[2] = {G.c0[p], G.c1[p]};
                 for (int q = 0; q < 2; q++) {
                     const int c = ch[q];
                     const double* y = G.lpb + c * 6;
                     double mx = y[0];
-    #pragma unroll
+#pragma unroll
                     for (int r = 1; r < 6; r++) mx = fmax(mx, y[r]);
                     double t[3];
                     if (mx == -CUDART_INF) {
                         t[0] = t[1] = t[2] = -CUDART_INF;
                     } else {
-                        lm63<Real>(sc, G.upper(c), y, mx, t);
-    #pragma unroll
+                        lm63(sc, G.upper(c), y, mx, t);
+#pragma unroll
                         for (int j = 0; j < 3; j++)
                             if (half) t[j] -= LN2;
                     }
-    #pragma unroll
+#pragma unroll
                     for (int j = 0; j < 3; j++) {
                         acc[j] += t[j];
                         acc[3 + j] += t[j];
                     }
                 }
-    #pragma unroll
+#pragma unroll
                 for (int r = 0; r < 6; r++) G.lpb[p * 6 + r] = acc[r];
             }
             __syncthreads();
@@ -787,12 +769,6 @@ __device__ __forceinline__ int categorical_f(int K, const float* p, uint32_t w) 
     return K;
 }
 
-// The categorical weights of Z/B sampling: FP64, or FP32 with FP32 partials.
-template <typename Real>
-__device__ __forceinline__ double zb_exp(double x) {
-    return sizeof(Real) == 8 ? d_exp(x) : (double)expf((float)x);
-}
-
 // Update_ZB's sampling (bpp_c.cpp:1710-1761): depths top-down, the node at
 // reverse-postorder index k drawing the uniform at position pos0 + k.
 template <typename Real>
@@ -830,32 +806,32 @@ __device__ void sample_zb(const GbgcChainParams& p, const GbgcCtx<Real>& G, Gbgc
                     if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
                 }
                 if (old != G.Z[s]) sc.changed = 1;
-                continue;
-            }
-            const double u = rd.uniform();
-            const double* y = G.lpb + s * 6;
-            if (pz != 2) {
-                double x[6], wv[6];
-                const int up = G.upper(s);
-#pragma unroll
-                for (int r = 0; r < 6; r++) x[r] = sc.lt[up][r % 3][pz] + y[r];
-                double mx = x[0];
-#pragma unroll
-                for (int r = 1; r < 6; r++)
-                    if (x[r] > mx) mx = x[r];
-#pragma unroll
-                for (int r = 0; r < 6; r++) wv[r] = zb_exp<Real>(x[r] - mx);
-                const int nn = categorical(6, wv, u);
-                G.Z[s] = (int8_t)(nn % 3);
-                if (!G.missing(s)) G.B[s] = nn > 2 ? 1 : 0;
             } else {
-                G.Z[s] = 2;
-                const double mx = fmax(y[2], y[5]);
-                const double wv[2] = {zb_exp<Real>(y[2] - mx), zb_exp<Real>(y[5] - mx)};
-                const int nn = categorical(2, wv, u);
-                if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
+                const double u = rd.uniform();
+                const double* y = G.lpb + s * 6;
+                if (pz != 2) {
+                    double x[6], wv[6];
+                    const int up = G.upper(s);
+#pragma unroll
+                    for (int r = 0; r < 6; r++) x[r] = sc.lt[up][r % 3][pz] + y[r];
+                    double mx = x[0];
+#pragma unroll
+                    for (int r = 1; r < 6; r++)
+                        if (x[r] > mx) mx = x[r];
+#pragma unroll
+                    for (int r = 0; r < 6; r++) wv[r] = d_exp(x[r] - mx);
+                    const int nn = categorical(6, wv, u);
+                    G.Z[s] = (int8_t)(nn % 3);
+                    if (!G.missing(s)) G.B[s] = nn > 2 ? 1 : 0;
+                } else {
+                    G.Z[s] = 2;
+                    const double mx = fmax(y[2], y[5]);
+                    const double wv[2] = {d_exp(y[2] - mx), d_exp(y[5] - mx)};
+                    const int nn = categorical(2, wv, u);
+                    if (!G.missing(s)) G.B[s] = nn > 0 ? 1 : 0;
+                }
+                if (old != G.Z[s]) sc.changed = 1;
             }
-            if (old != G.Z[s]) sc.changed = 1;
         }
         __syncthreads();
     }
