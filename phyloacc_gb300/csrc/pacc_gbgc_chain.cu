@@ -17,7 +17,8 @@
 //     one thread per (class, branch);
 //   * emissions: one thread per (node, class), sum(log P % posterior);
 //   * the Z-message pass over log_prob_back: tree levels in parallel, the
-//     children of a node added in postorder as the reference adds them;
+//     children of a node added in postorder as the reference adds them (with
+//     FP32 partials in FP32 values relative to a per-node FP64 offset);
 //   * Z/B sampling: tree depths in parallel, every node's uniform taken at its
 //     own position of the stream (one categorical draw per node, in reverse
 //     postorder);
