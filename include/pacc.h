@@ -199,8 +199,11 @@ pacc_ctx* pacc_create(const pacc_model* model, const pacc_opts* opts, int* statu
 /* Queue a batch (replaces the element loop of main.cpp:452-500).  Columns
  * are encoded, trimmed and the tree pruned per element on the host
  * (bpp_c.hpp:204-428); elements are admitted to the device as chain slots
- * and memory free up.  Returns PACC_OK or an error; per-element outcomes
- * are reported by pacc_poll. */
+ * and memory free up.  Serving on the CTA layout sizes its slots for at
+ * least 5,120 columns at the first submit; a later element longer than that
+ * first lets the running chains finish, then the slots are made again for
+ * it.  Returns PACC_OK or an error; per-element outcomes are reported by
+ * pacc_poll. */
 int pacc_submit(pacc_ctx* ctx, const pacc_element_batch* batch);
 
 /* Advance the device and collect up to max finished elements into out.

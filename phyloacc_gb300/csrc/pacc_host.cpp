@@ -783,6 +783,7 @@ struct StreamServer {
     int resident = 0, tail = 0;
     long long launches = 0;
     double kernel_ms = 0;
+    DevCounters carry{};            // device counters of earlier set-ups of this context
 };
 
 
@@ -2507,6 +2508,52 @@ static int stream_step(pacc_ctx* c) {
     return PACC_OK;
 }
 
+// Lets the queued and resident chains finish (their results go to done),
+// then frees the serving slots, so that they can be made again for longer
+// elements; launches, kernel time and device counters carry over.
+static int stream_teardown(pacc_ctx* c) {
+    StreamServer& v = c->ss;
+    if (!v.ready) return PACC_OK;
+    while (!v.queue.empty() || v.resident > 0) {
+        const size_t nd = c->done.size();
+        const int st = stream_step(c);
+        if (st != PACC_OK) return st;
+        if (c->done.size() == nd) std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    int st = stream_step(c);   // asks the idle blocks to return
+    if (st != PACC_OK) return st;
+    if (!cuda_ok(c, cudaStreamSynchronize(c->stream), "serving teardown")) return PACC_ECUDA;
+    st = stream_step(c);       // accounts the ended launch's time
+    if (st != PACC_OK) return st;
+    DevCounters dc;
+    if (!cuda_ok(c, cudaMemcpy(&dc, v.d_cnt, sizeof(dc), cudaMemcpyDeviceToHost), "serving teardown: counters"))
+        return PACC_ECUDA;
+    DevCounters carry = v.carry;
+    carry.edge_internal += dc.edge_internal;
+    carry.edge_leaf += dc.edge_leaf;
+    carry.col_ll += dc.col_ll;
+    carry.tg_draws += dc.tg_draws;
+    carry.z_draws += dc.z_draws;
+    carry.pmat += dc.pmat;
+    carry.iters += dc.iters;
+    for (int q = 0; q < 8; q++) carry.phase_cycles[q] += dc.phase_cycles[q];
+    carry.idle_exits += dc.idle_exits;
+    cudaFree(v.dev);
+    cudaFreeHost(v.h_map);
+    cudaFreeHost(v.h_stage);
+    cudaFreeHost(v.h_out);
+    cudaStreamDestroy(v.copy);
+    cudaEventDestroy(v.ev0);
+    cudaEventDestroy(v.ev1);
+    const long long launches = v.launches;
+    const double kernel_ms = v.kernel_ms;
+    v = StreamServer();
+    v.launches = launches;
+    v.kernel_ms = kernel_ms;
+    v.carry = carry;
+    return PACC_OK;
+}
+
 int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
     if (!c || !b || b->n_elements < 0) return PACC_EINVAL;
     const int n = b->n_elements;
@@ -2550,6 +2597,12 @@ int pacc_submit(pacc_ctx* c, const pacc_element_batch* b) {
         const bool warp = batched_layout(c);
         std::vector<const HostElem*> els;
         for (size_t i = base; i < c->pending.size(); i++) els.push_back(&c->pending[i]);
+        if (!warp && c->ss.ready && gmax > c->ss.GG_cap) {
+            // longer than the slots hold: the running chains finish under the
+            // old set-up, then the slots are made for the new length
+            const int st = stream_teardown(c);
+            if (st != PACC_OK) { c->pending.resize(base); return st; }
+        }
         int st = warp ? server_setup(c, gmax) : stream_setup(c, gmax, els);
         if (st != PACC_OK) { c->pending.resize(base); return st; }
         const int cap = warp ? c->srv.GG_cap : c->ss.GG_cap;
@@ -3081,12 +3134,13 @@ int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
             return PACC_ECUDA;
         pacc_counters& pc = c->counters;
         std::memset(&pc, 0, sizeof(pc));
-        pc.edge_updates_internal = (double)dc.edge_internal;
-        pc.edge_updates_leaf = (double)dc.edge_leaf;
-        pc.column_loglik = (double)dc.col_ll;
-        pc.tg_draws = (double)dc.tg_draws;
-        pc.z_draws = (double)dc.z_draws;
-        pc.pmatrix_builds = (double)dc.pmat;
+        const DevCounters& cy = c->ss.carry;
+        pc.edge_updates_internal = (double)(dc.edge_internal + cy.edge_internal);
+        pc.edge_updates_leaf = (double)(dc.edge_leaf + cy.edge_leaf);
+        pc.column_loglik = (double)(dc.col_ll + cy.col_ll);
+        pc.tg_draws = (double)(dc.tg_draws + cy.tg_draws);
+        pc.z_draws = (double)(dc.z_draws + cy.z_draws);
+        pc.pmatrix_builds = (double)(dc.pmat + cy.pmat);
         double running_ms = 0;
         if (c->ss.running && cudaEventQuery(c->ss.ev0) == cudaSuccess) {
             // the launch in progress: time from its start event to now
@@ -3099,11 +3153,11 @@ int pacc_get_counters(pacc_ctx* c, pacc_counters* out) {
             cudaEventDestroy(now);
             running_ms = ms;
         }
-        for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)dc.phase_cycles[q];
+        for (int q = 0; q < 8; q++) pc.phase_cycles[q] = (double)(dc.phase_cycles[q] + cy.phase_cycles[q]);
         pc.kernel_ms = c->ss.kernel_ms + running_ms;
         pc.flop = 36.0 * pc.edge_updates_internal + 4.0 * pc.edge_updates_leaf;
         pc.iterations = (double)c->ss.launches;
-        pc.serve_idle_exits = (double)dc.idle_exits;
+        pc.serve_idle_exits = (double)(dc.idle_exits + cy.idle_exits);
     } else if (serving(c) && c->srv.ready) {
         if (c->srv.inflight) cudaStreamSynchronize(c->stream);
         DevCounters dc;

@@ -110,3 +110,35 @@ def test_served_filtered_elements_return_at_once(built, prec):
     assert r.n == 12
     assert (r.status()[:12] == abi.PACC_FILTERED).all()
     assert ctx.pending() == 0
+
+
+def test_longer_element_recreates_serving_slots(built):
+    """CTA serving sizes its slots for 5,120 columns at the first submit; a
+    later element of 6,000 columns lets the running chains finish, the slots
+    are made again, and every element still equals its batched run."""
+    import dataclasses
+    ds = synth.make_dataset("st43", n_elements=60, seed=5)
+    S = ds.tree.n_species
+    long_cols = np.concatenate([ds.element(e) for e in range(20, 60)], axis=1)[:, :6000]
+    assert long_cols.shape[1] == 6000
+    blocks = [ds.element(e) for e in range(8)] + [long_cols, np.ascontiguousarray(long_cols[:, ::-1])]
+    lens = np.array([b.shape[1] for b in blocks], np.int32)
+    offs = np.zeros(len(blocks), np.int64)
+    offs[1:] = np.cumsum(lens[:-1].astype(np.int64) * S)
+    mix = dataclasses.replace(ds, lengths=lens, offsets=offs, bases=np.concatenate([b.reshape(-1) for b in blocks]),
+                              element_names=["e%d" % i for i in range(10)], accelerated=np.zeros(10, bool),
+                              r1=np.zeros(10), r2=np.zeros(10))
+    ctx = pg.Context(mix, _opts(abi.PACC_FP32, sweeps=3))
+    ctx.submit(mix.subset(list(range(8))), element_no=np.arange(8))
+    got = [ctx.poll(10)]
+    ctx.submit(mix.subset([8, 9]), element_no=np.array([8, 9]))
+    while ctx.pending() > 0:
+        got.append(ctx.poll(10))
+    got = _index(got)
+    assert sorted(got) == list(range(10))
+    ref = pg.Context(mix, _opts(abi.PACC_FP32)).run()
+    for e in range(10):
+        r, i = got[e]
+        assert r.arr[i].status == abi.PACC_OK
+        _same(r, i, ref, e)
+    assert ctx.counters()["kernel_ms"] > 0
