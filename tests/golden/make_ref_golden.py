@@ -48,8 +48,13 @@ CASES = {
     # two chains: a later chain starts every node from Z = 0 (bpp_c.cpp:124-135), which shows on
     # the nodes off the element's tree (a missing outgroup moves the root in element 1)
     "gbgc43_chain2": ("st43", [0, 7], 20, 40, 6, {"CHAIN": 2}),
+    # non-default selection coefficients, priors, transition and missing-data options
+    "gbgc12_options": ("st12", [2, 3, 86, 91], 20, 60, 8,
+                       {"CONSERVE_RATE": -1.5, "ACCE_RATE": 0.5, "CONSERVE_PRIOR_A": 4, "CONSERVE_PRIOR_B": 0.5,
+                        "ACCE_PRIOR_A": 6, "ACCE_PRIOR_B": 0.3, "PREP_LRATE": 0.3, "PREP_GRATE": 0.2,
+                        "CONSTOMIS": 0.05, "GAP_PROP": 0.5, "CONSERVE_PROP": 0.6}),
 }
-GBGC_CASES = {"gbgc12_default", "gbgc43_missing", "gbgc43_chain2"}
+GBGC_CASES = {"gbgc12_default", "gbgc43_missing", "gbgc43_chain2", "gbgc12_options"}
 
 
 def mask_taxa(ds, case):
@@ -66,6 +71,10 @@ def mask_taxa(ds, case):
         blk[ds.target[0], : blk.shape[1] // 2] = ord("-")
     if case == "gbgc43_chain2":
         ds.element(1)[ds.outgroup[0], :] = ord("*")
+    if case == "gbgc12_options":
+        blk = ds.element(1)
+        blk[ds.conserve[0], : (3 * blk.shape[1]) // 5] = ord("*")   # over GAP_PROP 0.5: missing
+        ds.element(2)[ds.outgroup[0], :] = ord("*")
     if case == "gbgc43_missing":
         star = ord("*")
         ds.element(1)[ds.outgroup[0], :] = star

@@ -17,11 +17,22 @@ from oracle import pyoracle as po
 from phyloacc_gb300 import abi
 
 
+# cfg keys of the gBGC program (src/PhyloAcc-ST-GBGC/SRC/main.cpp:83-259) -> option fields
+GBGC_KEYS = {"CONSERVE_RATE": "conserve_rate", "ACCE_RATE": "acce_rate",
+             "CONSERVE_PRIOR_A": "conserve_prior_a", "CONSERVE_PRIOR_B": "conserve_prior_b",
+             "ACCE_PRIOR_A": "acce_prior_a", "ACCE_PRIOR_B": "acce_prior_b",
+             "PREP_LRATE": "prep_lrate", "PREP_GRATE": "prep_grate", "CONSTOMIS": "cons_to_mis",
+             "GAP_PROP": "missing_thres", "CONSERVE_PROP": "conserve_prop"}
+
+
 def gbgc_opts(ds, kv):
     o = abi.gbgc_default_opts(ds.target)
     o.burnin, o.mcmc, o.seed = int(kv["BURNIN"]), int(kv["MCMC"]), int(kv["SEED"])
     if "GAPCHAR" in kv:
         o.gapchar = ord(kv["GAPCHAR"][0])
+    for k, f in GBGC_KEYS.items():
+        if k in kv:
+            setattr(o, f, float(kv[k]))
     return o
 
 
@@ -31,7 +42,7 @@ def _runs(case):
     return ds, o, [po.gbgc_run(ds, o, e) for e in range(ds.n_elements)]
 
 
-CASES = ["gbgc12_default", "gbgc43_missing"]
+CASES = ["gbgc12_default", "gbgc43_missing", "gbgc12_options"]
 
 
 @pytest.mark.parametrize("case", CASES)
