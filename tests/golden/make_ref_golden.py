@@ -37,6 +37,13 @@ CASES = {
                      {"PRUNE_TREE": 1, "TRIM_GAP_PERCENT": 0.4, "GAP_PROP": 0.3, "ROPT": 2,
                       "HYPER_LRATE2_A": 0, "ADAPT_FREQ": 25, "INIT_CONSERVE_RATE": 0.3}),
     "st43_default": ("st43", [0, 7, 12], 50, 150, 1, {}),
+    # non-default priors, hyper-priors, initial values and rate bounds, and a MIN_LEN filter
+    "st12_priors": ("st12", [6, 7, 8, 87, 93], 60, 200, 9,
+                    {"CONSERVE_PRIOR_A": 4, "CONSERVE_PRIOR_B": 0.08, "ACCE_PRIOR_A": 8, "ACCE_PRIOR_B": 0.3,
+                     "HYPER_LRATE_A": 2, "HYPER_LRATE_B": 8, "HYPER_GRATE_A": 2, "HYPER_GRATE_B": 2,
+                     "HYPER_LRATE2_A": 2, "HYPER_LRATE2_B": 6, "INIT_LRATE": 0.2, "INIT_GRATE": 0.6,
+                     "INIT_LRATE2": 0.2, "INIT_ACCE_RATE": 2.5, "CONSTOMIS": 0.05, "ROPT": 1, "NLB": 0.8,
+                     "CUB": 0.9, "MIN_LEN": 150}),
     # two chains: the second starts every element from Z = 0 (main.cpp:445, bpp_c.cpp:150)
     "st12_chain2": ("st12", [0, 85, 90], 60, 150, 2, {"CHAIN": 2}),
     # SAMPLE_HYPER: three chains of M2, hyper-parameters drawn between chains
