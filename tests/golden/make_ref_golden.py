@@ -60,8 +60,10 @@ CASES = {
                        {"CONSERVE_RATE": -1.5, "ACCE_RATE": 0.5, "CONSERVE_PRIOR_A": 4, "CONSERVE_PRIOR_B": 0.5,
                         "ACCE_PRIOR_A": 6, "ACCE_PRIOR_B": 0.3, "PREP_LRATE": 0.3, "PREP_GRATE": 0.2,
                         "CONSTOMIS": 0.05, "GAP_PROP": 0.5, "CONSERVE_PROP": 0.6}),
+    # '-' as the gap character: the 43-taxon data's gap cells and missing taxa count as gaps
+    "gbgc43_dash": ("st43", [3, 9, 15], 20, 40, 10, {"GAPCHAR": "-"}),
 }
-GBGC_CASES = {"gbgc12_default", "gbgc43_missing", "gbgc43_chain2", "gbgc12_options"}
+GBGC_CASES = {"gbgc12_default", "gbgc43_missing", "gbgc43_chain2", "gbgc12_options", "gbgc43_dash"}
 
 
 def mask_taxa(ds, case):

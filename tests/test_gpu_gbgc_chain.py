@@ -22,7 +22,7 @@ from test_oracle_gbgc_chain import gbgc_opts
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["gbgc12_default", "gbgc43_missing", "gbgc12_options"]
+CASES = ["gbgc12_default", "gbgc43_missing", "gbgc12_options", "gbgc43_dash"]
 
 
 def _ctx(ds, precision):

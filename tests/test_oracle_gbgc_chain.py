@@ -42,7 +42,7 @@ def _runs(case):
     return ds, o, [po.gbgc_run(ds, o, e) for e in range(ds.n_elements)]
 
 
-CASES = ["gbgc12_default", "gbgc43_missing", "gbgc12_options"]
+CASES = ["gbgc12_default", "gbgc43_missing", "gbgc12_options", "gbgc43_dash"]
 
 
 @pytest.mark.parametrize("case", CASES)
