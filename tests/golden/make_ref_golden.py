@@ -44,6 +44,9 @@ CASES = {
                      "HYPER_LRATE2_A": 2, "HYPER_LRATE2_B": 6, "INIT_LRATE": 0.2, "INIT_GRATE": 0.6,
                      "INIT_LRATE2": 0.2, "INIT_ACCE_RATE": 2.5, "CONSTOMIS": 0.05, "ROPT": 1, "NLB": 0.8,
                      "CUB": 0.9, "MIN_LEN": 150}),
+    # missing-species filters: an element whose missing conserved taxa exceed CONSERVE_PROP is
+    # filtered; a target taxon 90% gaps is missing
+    "st12_filters": ("st12", [9, 10, 11, 88], 60, 150, 11, {"CONSERVE_PROP": 0.2}),
     # two chains: the second starts every element from Z = 0 (main.cpp:445, bpp_c.cpp:150)
     "st12_chain2": ("st12", [0, 85, 90], 60, 150, 2, {"CHAIN": 2}),
     # SAMPLE_HYPER: three chains of M2, hyper-parameters drawn between chains
@@ -78,6 +81,12 @@ def mask_taxa(ds, case):
             blk[s, :] = ord("n")
         blk = ds.element(3)
         blk[ds.target[0], : blk.shape[1] // 2] = ord("-")
+    if case == "st12_filters":
+        blk = ds.element(1)
+        for s in ds.conserve[:3]:
+            blk[s, :] = ord("-")
+        blk = ds.element(2)
+        blk[ds.target[0], : (9 * blk.shape[1]) // 10] = ord("-")
     if case == "gbgc43_chain2":
         ds.element(1)[ds.outgroup[0], :] = ord("*")
     if case == "gbgc12_options":

@@ -9,7 +9,7 @@ import numpy as np
 from phyloacc_gb300 import abi, synth
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["st12_default", "st12_options", "st43_default", "st12_priors"]
+CASES = ["st12_default", "st12_options", "st43_default", "st12_priors", "st12_filters"]
 
 
 def _parse_newick(s, i, nodes):
