@@ -106,6 +106,20 @@ def test_default_opts_match_the_library(built):
         assert getattr(a, name) == getattr(b, name), name
 
 
+def test_gbgc_default_opts_match_the_library(built):
+    """pacc_gbgc_default_opts writes the values abi.gbgc_default_opts gives
+    (the gBGC program's defaults) into the ctypes mirror of pacc_gbgc_opts."""
+    L = pg.lib()
+    a = abi.PaccGbgcOpts()
+    C.memset(C.byref(a), 0x5A, C.sizeof(a))
+    L.pacc_gbgc_default_opts(C.byref(a))
+    b = abi.gbgc_default_opts()
+    for name, _ in abi.PaccGbgcOpts._fields_:
+        if name in ("target", "n_target"):
+            continue
+        assert getattr(a, name) == getattr(b, name), name
+
+
 def test_run_without_gpu_fails_loudly(built):
     import os
     if os.path.exists("/dev/nvidia0"):
